@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Walker-steps/s of the plain FP64 DMC step on one GB300.
+
+Workload: H2O local-mode PES (O,H,H), 20000 walkers, dt = 10 a.u., discrete
+birth/death with descendant weighting in 50-step windows, Philox4x32-10
+noise.  A "step" is one pass of the walker step (move + PES + weights +
+branching + vref) over the current population.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``value``: device-resident walker-steps/s,
+each step timed with CUDA events on the launching stream, with a 256 MiB
+buffer written between steps so every step starts with the walkers in HBM
+(L2 flushed).  ``e2e``: the same metric through the C ABI with the walkers in
+pinned host memory: every step copies them host->device, runs
+``gbdmc_sim_step`` and copies the branched walkers and the control block
+back.  ``--impl reference`` times the CPU restatement of the reference's
+step loop (oracle/) on the host cores.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s on 1 GB300, plain FP64 vs IS+NN-PES+batched at ZPE err ≤1 cm⁻¹"
+UNIT = "walker-steps/s"
+N_WALKERS = 20000
+DT = 10.0
+DESC_WINDOW = 50
+WORKLOAD = "h2o_local_mode_plain_discrete_20k"
+BYTES_MOVE_KERNEL = 2 * 9 * 8 + 8 + 4  # x read+write, V write, count write per walker (A=3, fp64)
+
+
+def start_structures(n, seed):
+    p = dict(re=1.81, theta_e=np.deg2rad(104.5))
+    eq = np.array([[0.0, 0.0, 0.0], [p["re"], 0.0, 0.0],
+                   [p["re"] * np.cos(p["theta_e"]), p["re"] * np.sin(p["theta_e"]), 0.0]])
+    return eq[None] + 0.05 * np.random.default_rng(seed).standard_normal((n, 3, 3))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# -------------------------------------------------------------- CPU sides
+class _NumpyNoise:
+    """NumPy Generator deviates for the CPU baseline (the reference draws from
+    NumPy's legacy global RandomState; the cost per deviate is similar)."""
+
+    def __init__(self, seed):
+        self.g = np.random.default_rng(seed)
+
+    def normal(self, loc=0.0, scale=1.0, size=None):
+        return loc + scale * self.g.standard_normal(size)
+
+    def random(self, size=None):
+        return self.g.random(size)
+
+
+def _pool_pes(chunk):
+    import oracle
+    p, _ = oracle.h2o_config()
+    return oracle.pes_h2o_lm(chunk, p)
+
+
+def cpu_reference_rate(n_walkers, steps, cores):
+    """Oracle port of DMC_Sim.propagate on the host: walker-steps/s.  With
+    cores > 1 the PES is sharded over a spawn pool the way
+    potential_manager.Potential.getpot does (np.array_split, pool.map,
+    np.concatenate)."""
+    import oracle
+    p, m = oracle.h2o_config()
+    x0 = start_structures(n_walkers, 5)
+    if cores > 1:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        pool = ctx.Pool(cores)
+        pes = lambda c: np.concatenate(pool.map(_pool_pes, np.array_split(c, cores)))  # noqa: E731
+    else:
+        pool = None
+        pes = lambda c: oracle.pes_h2o_lm(c, p)  # noqa: E731
+    try:
+        sim = oracle.OracleDMC(x0, m, DT, pes, _NumpyNoise(1))
+        sim.run(3)  # warm-up (step 0 potential + vref)
+        pops = []
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            pops.append(len(sim.x))
+            _single_step(sim)
+        dt = time.perf_counter() - t0
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
+    return float(np.sum(pops)) / dt, dt
+
+
+def _single_step(sim):
+    """One oracle step continuing an OracleDMC that has run (restates the
+    loop body of pyvibdmc.py:772-848 for the plain discrete case)."""
+    import oracle
+    oracle.move_randomly(sim.x, sim.sigmas, sim.noise)
+    sim.v = sim.pes(sim.x)
+    u = sim.noise.random(size=len(sim.x))
+    idx, counts, b, d = oracle.birth_or_death_discrete(sim.v, sim.vref, sim.dt, u, sim.pop_thresh[1])
+    sim.x = sim.x[idx]
+    sim.v = sim.v[idx]
+    sim.vref = oracle.calc_vref(sim.v, sim.n0, sim.alpha)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    rate1, t1 = cpu_reference_rate(N_WALKERS, max(args.steps // 10, 20), 1)
+    best, kind_cores = rate1, 1
+    if cores > 1:
+        try:
+            ratep, tp = cpu_reference_rate(N_WALKERS, max(args.steps // 20, 10), cores)
+            if ratep > best:
+                best, kind_cores = ratep, cores
+        except Exception:
+            pass
+    line = {"impl": "reference", "metric": METRIC, "value": best, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "walkers": N_WALKERS, "dt": DT},
+            "cpu_baseline": {"value": best, "unit": UNIT, "cores": kind_cores, "kind": "port",
+                             "sample": f"oracle restatement of DMC_Sim.propagate (plain, discrete), "
+                                       f"{N_WALKERS} walkers, numpy; best of 1-process and "
+                                       f"{cores}-process PES pool"},
+            "e2e": {"value": best, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args):
+    import torch
+    import pyvibdmc_gb300 as pg
+    from pyvibdmc_gb300 import _capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = _capi.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    masses = [pg.Constants.mass("O"), pg.Constants.mass("H"), pg.Constants.mass("H")]
+    K, W = args.steps, args.warmup
+    sim = pg.DMC_Sim(sim_name="bench", num_walkers=N_WALKERS, num_timesteps=W + 3 * K + 8, equil_steps=10 ** 9,
+                     atoms=["O", "H", "H"], masses=masses, delta_t=DT, potential=pg.h2o_local_mode(),
+                     start_structures=start_structures(N_WALKERS, 1 + rank), seed=1234 + rank, write_files=False)
+    sim._init_device()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ctrl_ptr = C.c_void_p(sim._ctrl.data_ptr())
+
+    def who_ptr():
+        return C.c_void_p(sim._bufs[sim._cur]["who"].data_ptr())
+
+    desc = torch.zeros(int(sim.capacity), dtype=torch.float64, device=dev)
+    launches = [0]
+
+    def one_step(i):
+        if i % DESC_WINDOW == 0:
+            _capi.check(L.gbdmc_desc_begin(who_ptr(), ctrl_ptr, sp), "desc_begin")
+            launches[0] += 1
+        sim._cur = sim._launch_step(sim._cur)
+        launches[0] += 2
+        if (i + 1) % DESC_WINDOW == 0:
+            _capi.check(L.gbdmc_desc_weights(who_ptr(), None, ctrl_ptr, int(sim.capacity), C.c_void_p(desc.data_ptr()),
+                                             sp), "desc_weights")
+            launches[0] += 2
+
+    for i in range(W):
+        one_step(i)
+    torch.cuda.synchronize()
+    step0 = int(sim._read_ctrl().step)
+    # ---- timed: per-step events, L2 flushed between steps
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    launches[0] = 0
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(K):
+            flush.fill_(i & 0xFF)
+            ev0[i].record(stream)
+            one_step(W + i)
+            ev1[i].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    gpu_launches = launches[0]
+    ms = float(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)))
+    c = sim._read_ctrl()
+    if c.status:
+        raise RuntimeError(f"device status {c.status} during the bench")
+    pop = sim._hist["pop"][step0 - 1:step0 - 1 + K].cpu().numpy()
+    walker_steps = float(pop.sum())  # population entering each timed step
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        ws = torch.tensor([walker_steps], device=dev, dtype=torch.float64)
+        dist.all_reduce(ws)
+        walker_steps = float(ws.item())
+    value = walker_steps / (ms / 1e3)
+    ms_per_step = ms / K
+
+    # ---- warm-L2 graph replay (information: back-to-back steps as DMC_Sim.run issues them)
+    gsteps = 32
+    sim.graph_steps = gsteps
+    g = sim._graph_for(sim._cur)
+    g.replay()
+    torch.cuda.synchronize()
+    s_before = int(sim._read_ctrl().step)
+    reps = max(1, K // gsteps)
+    e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_a.record(stream)
+    for _ in range(reps):
+        g.replay()
+    e_b.record(stream)
+    torch.cuda.synchronize()
+    s_after = int(sim._read_ctrl().step)
+    popg = sim._hist["pop"][s_before - 1:s_after - 1].cpu().numpy()
+    graph_rate = float(popg.sum()) / (e_a.elapsed_time(e_b) / 1e3)
+
+    # ---- dominant kernel: event pairs around each move kernel launch (same protocol, L2 flushed)
+    _capi.check(L.gbdmc_prof_enable(1), "prof_enable")
+    kp = min(K, 4096)
+    s_before = int(sim._read_ctrl().step)
+    for i in range(kp):
+        flush.fill_(i & 0xFF)
+        sim._cur = sim._launch_step(sim._cur)
+    mv_ms, mv_n, sc_ms, sc_n = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
+    _capi.check(L.gbdmc_prof_read(C.byref(mv_ms), C.byref(mv_n), C.byref(sc_ms), C.byref(sc_n)), "prof_read")
+    _capi.check(L.gbdmc_prof_enable(0), "prof_enable")
+    s_after = int(sim._read_ctrl().step)
+    popp = sim._hist["pop"][s_before - 1:s_after - 1].cpu().numpy()
+    move_avg_s = mv_ms.value / 1e3 / max(mv_n.value, 1)
+    achieved = BYTES_MOVE_KERNEL * float(popp.mean()) / move_avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "k_move_h2o_20k_traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get("dram_bytes_per_launch")
+
+    # ---- fp64 pipe probe (measured fp64 FMA rate)
+    sink = torch.zeros(152 * 8, dtype=torch.float64, device=dev)
+    flops = C.c_double()
+    _capi.check(L.gbdmc_fp64_fma_probe(C.c_void_p(sink.data_ptr()), 64, 152 * 8, C.byref(flops), sp), "fp64")
+    e_a.record(stream)
+    _capi.check(L.gbdmc_fp64_fma_probe(C.c_void_p(sink.data_ptr()), 512, 152 * 8, C.byref(flops), sp), "fp64")
+    e_b.record(stream)
+    torch.cuda.synchronize()
+    fp64_tflops = flops.value / (e_a.elapsed_time(e_b) / 1e3) / 1e12
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = run_e2e(sim, L, dev, max(50, min(K, 500)))
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded start geometries, Philox4x32-10 deviates)",
+            "config": {"workload": WORKLOAD, "walkers_per_gpu": N_WALKERS, "dt": DT, "atoms": "O,H,H",
+                       "weighting": "discrete", "desc_window": DESC_WINDOW, "noise": "philox32",
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                       "graph_replay_l2_warm_walker_steps_per_s": graph_rate, "wall_s_timed": wall},
+            "gpu_launches": gpu_launches,
+            "roofline": {"bound": "hbm", "kernel": "k_move (move+PES+weights+counts)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "bytes_per_walker": BYTES_MOVE_KERNEL,
+                         "kernel_avg_us": move_avg_s * 1e6, "scatter_avg_us": sc_ms.value / max(sc_n.value, 1) * 1e3,
+                         "fp64_fma_probe_tflops": fp64_tflops},
+            "e2e": e2e}
+    if rank == 0 and world == 1:
+        rate, secs = cpu_reference_rate(N_WALKERS, 150, 1)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"oracle restatement of DMC_Sim.propagate (plain, discrete), "
+                                          f"{N_WALKERS} walkers x 150 steps, numpy, {secs:.1f} s"}
+    line["clocks"] = clk.summary()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_e2e(sim, L, dev, steps):
+    """Walkers in pinned host memory; per step: H2D walkers, gbdmc_sim_step,
+    D2H branched walkers + control block (the reference-facing call with host
+    buffers)."""
+    import torch
+    from pyvibdmc_gb300 import _capi
+    A3 = 3 * sim.natoms
+    cap = sim.capacity
+    n = int(sim._read_ctrl().n)
+    host_x = torch.empty((A3, cap), dtype=torch.float64).pin_memory()
+    host_v = torch.empty(cap, dtype=torch.float64).pin_memory()
+    host_ctrl = torch.empty(C.sizeof(_capi.Ctrl), dtype=torch.uint8).pin_memory()
+    host_x[:, :n].copy_(sim._bufs[sim._cur]["x"][:, :n])
+    h2d = d2h = 0
+    total = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b = sim._bufs[sim._cur]
+        b["x"][:, :n].copy_(host_x[:, :n], non_blocking=True)
+        h2d += A3 * n * 8
+        total += n
+        sim._cur = sim._launch_step(sim._cur)
+        host_ctrl.copy_(sim._ctrl, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        c = _capi.Ctrl.from_buffer_copy(host_ctrl.numpy().tobytes())
+        n = int(c.n)
+        nb = sim._bufs[sim._cur]
+        host_x[:, :n].copy_(nb["x"][:, :n], non_blocking=True)
+        host_v[:n].copy_(nb["v"][:n], non_blocking=True)
+        d2h += (A3 + 1) * n * 8 + C.sizeof(_capi.Ctrl)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
+            "d2h_bytes_per_step": d2h // steps, "steps": steps,
+            "path": "pinned host walkers -> H2D -> gbdmc_sim_step (C ABI) -> D2H walkers, V, ctrl"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,224 @@
+/*
+ * gbdmc.h -- C ABI of the GB300 diffusion Monte Carlo walker-step library
+ * (libgbdmc.so, sm_103a).
+ *
+ * Conventions
+ *  - Every pointer named *_dev is device memory owned by the caller; the
+ *    library allocates nothing on any call.  Host structs are read during the
+ *    call only.
+ *  - Walker arrays are structure-of-arrays: coordinate component k = 3*atom+dim
+ *    of walker i lives at x[k*ld + i]; ld (leading dimension) >= capacity.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Every call returns GBDMC_OK (0) or an error code; gbdmc_last_error()
+ *    gives a message for the calling thread's last failure.
+ *  - Calls are stream-ordered and asynchronous.  Population-control guards
+ *    raised on the device are reported in gbdmc_ctrl_t.status, which the host
+ *    reads once per batch of steps.
+ *
+ * The entry points replace the reference's plug-in and engine interfaces
+ * (paths relative to the reference project root):
+ *   gbdmc_pes_eval      <- Potential*.getpot(cds)          simulation_utilities/potential_manager.py:71,144,196,237
+ *   gbdmc_trial_eval    <- ImpSamp.drift(cds) = call_trial + call_derivs
+ *                          simulation_utilities/imp_samp.py:21-26, imp_samp_manager.py:92-139,197-224
+ *   gbdmc_sim_init      <- DMC_Sim.propagate step-0 potential + calc_vref   pyvibdmc.py:760-769
+ *   gbdmc_sim_step      <- one iteration of DMC_Sim.propagate               pyvibdmc.py:710-848
+ *                          (move_randomly :540, imp_move_randomly :549, getpot :785-793,
+ *                           local_kin :807-809, birth_or_death :380-454, calc_vref :651-661,
+ *                           update_sim_arrays :674-682)
+ *   gbdmc_desc_weights  <- DMC_Sim.calc_desc_wts                            pyvibdmc.py:663-672
+ */
+#ifndef GBDMC_H
+#define GBDMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBDMC_MAX_ATOMS 8
+#define GBDMC_ABI_VERSION 1
+
+/* return codes */
+enum {
+  GBDMC_OK = 0,
+  GBDMC_ERR_ARG = 1,      /* invalid argument (sizes, kinds, null pointers) */
+  GBDMC_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  GBDMC_ERR_CAPACITY = 3  /* request exceeds a documented maximum */
+};
+
+/* device status bits (gbdmc_ctrl_t.status); any bit stops further steps */
+enum {
+  GBDMC_ST_NONFINITE_WEIGHT = 1, /* pyvibdmc.py:397 non-finite weight          */
+  GBDMC_ST_HUGE_WEIGHT = 2,      /* pyvibdmc.py:397 weight > 1.5 N0 + 1        */
+  GBDMC_ST_POP_LOW = 4,          /* pyvibdmc.py:409,716 population < 0.5 N0    */
+  GBDMC_ST_POP_HIGH = 8,         /* pyvibdmc.py:409,716 population > 1.5 N0    */
+  GBDMC_ST_OVERFLOW = 16         /* population would exceed the capacity ld    */
+};
+
+/* potential energy surfaces */
+enum {
+  GBDMC_PES_HO = 1,     /* p[0]=k : V = 1/2 k |x|^2                              */
+  GBDMC_PES_H2O_LM = 2, /* O,H,H; p = De, a, re, ktheta, theta_e, krr            */
+  GBDMC_PES_DIMER = 3   /* O,H,H,O,H,H; p = De,a,re,ktheta,theta_e,krr,eps,sigma,qH,qO */
+};
+
+typedef struct {
+  int32_t kind;
+  int32_t natoms;
+  double p[16];
+} gbdmc_pes_t;
+
+/* trial wave functions for importance sampling */
+enum {
+  GBDMC_TRIAL_NONE = 0,
+  GBDMC_TRIAL_HO_GAUSS = 1,  /* p[a] = alpha of atom a; separable Cartesian Gaussian        */
+  GBDMC_TRIAL_H2O_GAUSS = 2  /* O,H,H; p = alpha_r1, alpha_r2, alpha_th, r1e, r2e, theta_e  */
+};
+
+typedef struct {
+  int32_t kind;
+  int32_t natoms;
+  double p[16];
+} gbdmc_trial_t;
+
+/* noise sources */
+enum {
+  GBDMC_NOISE_PHILOX32 = 0, /* Philox4x32-10, Box-Muller in fp32, widened to fp64 */
+  GBDMC_NOISE_PHILOX64 = 1, /* Philox4x32-10, Box-Muller in fp64                  */
+  GBDMC_NOISE_INJECTED = 2  /* caller-provided standard normals and uniforms      */
+};
+
+enum { GBDMC_DISCRETE = 0, GBDMC_CONTINUOUS = 1 };
+
+/* walker state, SoA, caller-owned device memory */
+typedef struct {
+  double* x;    /* [3A][ld] coordinates (bohr)                               */
+  double* v;    /* [ld] potential, or local energy when importance sampling */
+  int32_t* who; /* [ld] ancestor index for descendant weighting, or NULL    */
+  double* f;    /* [3A][ld] drift dpsi/dx / psi (importance sampling)       */
+  double* psi;  /* [ld] trial psi (importance sampling)                     */
+  double* ke;   /* [ld] local kinetic energy (importance sampling)          */
+  double* w;    /* [ld] continuous weights, or NULL                         */
+} gbdmc_walkers_t;
+
+/* device-resident control block (caller allocates sizeof(gbdmc_ctrl_t)) */
+typedef struct {
+  int64_t n;        /* population of the current walker buffer          */
+  int64_t n_prev;   /* population before the last branching             */
+  int64_t step;     /* index of the next step                           */
+  double vref;      /* current reference energy                         */
+  double dt_eff;    /* importance sampling: dt * accepted fraction      */
+  double eff_ts;    /* importance sampling: cumulative effective time   */
+  int32_t status;   /* GBDMC_ST_* bits; nonzero stops all further steps */
+  int32_t err_step; /* step at which status was first raised            */
+  uint32_t ticket;  /* last-block election counter (kept at 0 between calls) */
+  int32_t flags;    /* guard bits raised by blocks of the running kernel; folded
+                       into status by the kernel's last block */
+  int64_t n_acc;    /* importance sampling: accepted moves, last step   */
+  int64_t reserved[6];
+} gbdmc_ctrl_t;
+
+/* per-step history written by the device (each pointer may be NULL) */
+typedef struct {
+  double* vref;      /* [len] vref after step t        (pyvibdmc.py:678)  */
+  double* pop;       /* [len] population or sum of weights (:680-682)     */
+  int32_t* births;   /* [len] discrete births / continuous branched count */
+  int32_t* deaths;   /* [len] discrete deaths                              */
+  int32_t* rejected; /* [len] Metropolis rejections                        */
+  double* vmin;      /* [len] min / max / mean potential before branching */
+  double* vmax;
+  double* vmean;
+  double* eff_ts;    /* [len] cumulative effective time (importance sampling) */
+  int64_t len;
+} gbdmc_history_t;
+
+typedef struct {
+  int32_t natoms;
+  int32_t weighting;   /* GBDMC_DISCRETE / GBDMC_CONTINUOUS */
+  int32_t noise_mode;  /* GBDMC_NOISE_* */
+  int32_t track_who;   /* gather ancestor ids with the walkers */
+  int64_t ld;          /* capacity and leading dimension */
+  int64_t n0;          /* target population num_walkers */
+  double dt;
+  double alpha;        /* 1/(2 dt) unless overridden (pyvibdmc.py:200-203) */
+  double sigma[GBDMC_MAX_ATOMS];    /* sqrt(dt/m_a) (pyvibdmc.py:199) */
+  double inv_mass[GBDMC_MAX_ATOMS];
+  double thresh_lower; /* continuous weighting thresholds (pyvibdmc.py:214-231) */
+  double thresh_upper; /* <= 0 : none */
+  uint64_t seed;
+  gbdmc_pes_t pes;
+  gbdmc_trial_t trial; /* kind GBDMC_TRIAL_NONE: plain DMC */
+  gbdmc_history_t hist;
+} gbdmc_sim_t;
+
+/* injected noise for one step (GBDMC_NOISE_INJECTED only; device pointers) */
+typedef struct {
+  const double* normal;   /* [3A][ld_noise] standard normals for the move     */
+  const double* u_branch; /* [ld_noise] uniforms for birth/death              */
+  const double* u_accept; /* [ld_noise] uniforms for the Metropolis test      */
+  int64_t ld_noise;
+} gbdmc_noise_t;
+
+/* library information */
+int gbdmc_abi_version(void);
+const char* gbdmc_last_error(void);
+
+/* Bytes of device scratch the step calls need for capacity ld (block partials). */
+size_t gbdmc_scratch_bytes(int64_t ld);
+
+/* V(x) for n walkers; grad_dev (SoA like x, may be NULL) receives dV/dx. */
+int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x_dev, int64_t n, int64_t ld,
+                   double* v_dev, double* grad_dev, void* stream);
+
+/* psi, (dpsi/dx)/psi and (d2psi/dx2)/psi per Cartesian component. */
+int gbdmc_trial_eval(const gbdmc_trial_t* trial, const double* x_dev, int64_t n, int64_t ld,
+                     double* psi_dev, double* d1_dev, double* d2_dev, void* stream);
+
+/* Step 0: potential (+ local KE) of the start walkers and the first vref.
+ * ctrl->n must hold the start population; resets step, status, eff_ts. */
+int gbdmc_sim_init(const gbdmc_sim_t* sim, const gbdmc_walkers_t* w, gbdmc_ctrl_t* ctrl_dev,
+                   void* scratch_dev, void* stream);
+
+/* One full walker step.  Discrete weighting reads `src` and writes the
+ * branched population to `dst` (ping-pong); continuous weighting updates
+ * `src` in place and ignores `dst`.  noise may be NULL unless
+ * sim->noise_mode == GBDMC_NOISE_INJECTED. */
+int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                   gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, const gbdmc_noise_t* noise,
+                   void* stream);
+
+/* Descendant weights: desc_dev[q] = #walkers (or sum of weights, w_dev != NULL)
+ * whose ancestor id is q; desc_dev has n_parent entries and is overwritten. */
+int gbdmc_desc_weights(const int32_t* who_dev, const double* w_dev, const int64_t* n_dev,
+                       int64_t n_parent, double* desc_dev, void* stream);
+
+/* Start of a descendant-weighting window: who_dev[i] = i for i < *n_dev
+ * (pyvibdmc.py:739-745, `_who_from = np.arange(len(coords))`). */
+int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);
+
+/* sizeof() of the ABI structs, for binding self-checks:
+ * 0 gbdmc_sim_t, 1 gbdmc_walkers_t, 2 gbdmc_ctrl_t, 3 gbdmc_noise_t,
+ * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t; 0 for unknown ids. */
+size_t gbdmc_struct_size(int32_t which);
+
+/* ---- measurement aids (no counterpart in the reference; used by bench.py) ----
+ * gbdmc_prof_enable(1) makes every later gbdmc_sim_step record CUDA events
+ * around its walker-move kernel (move + PES + weights) and its branching
+ * scatter kernel, on the stream of the call; gbdmc_prof_read synchronises
+ * those events, returns the summed milliseconds and launch counts, and
+ * clears them.  Up to 8192 steps are recorded between reads.  Not for use
+ * under stream capture. */
+int gbdmc_prof_enable(int32_t on);
+int gbdmc_prof_read(double* move_ms, int64_t* move_launches, double* scatter_ms, int64_t* scatter_launches);
+
+/* Measured fp64 FMA throughput: `blocks` x 256 threads each run `iters`
+ * dependent-free DFMA groups; *flops_out = flops executed.  Time it with
+ * events around the call. */
+int gbdmc_fp64_fma_probe(double* sink_dev, int64_t iters, int32_t blocks, double* flops_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDMC_H */

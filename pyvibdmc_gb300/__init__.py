@@ -1,0 +1,25 @@
+"""pyvibdmc_gb300 -- GB300-native diffusion Monte Carlo walker engine.
+
+Drop-in for PyVibDMC's walker step loop: ``DMC_Sim`` / ``dmc_restart`` with the
+reference's keywords, GPU potential plug-ins with the ``getpot`` contract and
+GPU importance-sampling managers with ``call_trial`` / ``call_derivs``.  The
+per-step work runs in hand-written sm_103a CUDA kernels (libgbdmc.so) behind
+the C ABI of ``include/gbdmc.h``.
+"""
+from .constants import Constants, get_atomic_num, get_atomic_string
+from .potentials import (Potential_GPU, PESFunction, harmonic_oscillator, h2o_local_mode, water_dimer,
+                         to_soa, from_soa)
+from .imp_samp import ImpSampManager_GPU, TrialFunction, h2o_gaussian_trial, ho_gaussian_trial
+from .engine import DMC_Sim, dmc_restart
+from . import _capi
+
+__all__ = ["Constants", "get_atomic_num", "get_atomic_string", "Potential_GPU", "PESFunction",
+           "harmonic_oscillator", "h2o_local_mode", "water_dimer", "ImpSampManager_GPU", "TrialFunction",
+           "h2o_gaussian_trial", "ho_gaussian_trial", "DMC_Sim", "dmc_restart", "to_soa", "from_soa"]
+
+__version__ = "0.1.0"
+
+
+def library():
+    """Load (building when absent) and return the ctypes handle of libgbdmc.so."""
+    return _capi.load()

@@ -1,0 +1,119 @@
+"""ctypes binding of libgbdmc.so (the C ABI declared in include/gbdmc.h).
+
+The structs here mirror the header field by field; ``check_abi()`` compares
+their sizes against ``gbdmc_struct_size`` of the loaded library.  Loading
+fails loudly when the library is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+from . import _build
+
+MAX_ATOMS = 8
+
+OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY = 0, 1, 2, 3
+ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW = 1, 2, 4, 8, 16
+PES_HO, PES_H2O_LM, PES_DIMER = 1, 2, 3
+TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS = 0, 1, 2
+NOISE_PHILOX32, NOISE_PHILOX64, NOISE_INJECTED = 0, 1, 2
+DISCRETE, CONTINUOUS = 0, 1
+
+
+class PES(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("natoms", C.c_int32), ("p", C.c_double * 16)]
+
+
+class Trial(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("natoms", C.c_int32), ("p", C.c_double * 16)]
+
+
+class Walkers(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("f", C.c_void_p),
+                ("psi", C.c_void_p), ("ke", C.c_void_p), ("w", C.c_void_p)]
+
+
+class Ctrl(C.Structure):
+    _fields_ = [("n", C.c_int64), ("n_prev", C.c_int64), ("step", C.c_int64), ("vref", C.c_double),
+                ("dt_eff", C.c_double), ("eff_ts", C.c_double), ("status", C.c_int32),
+                ("err_step", C.c_int32), ("ticket", C.c_uint32), ("flags", C.c_int32),
+                ("n_acc", C.c_int64), ("reserved", C.c_int64 * 6)]
+
+
+class History(C.Structure):
+    _fields_ = [("vref", C.c_void_p), ("pop", C.c_void_p), ("births", C.c_void_p), ("deaths", C.c_void_p),
+                ("rejected", C.c_void_p), ("vmin", C.c_void_p), ("vmax", C.c_void_p), ("vmean", C.c_void_p),
+                ("eff_ts", C.c_void_p), ("len", C.c_int64)]
+
+
+class Sim(C.Structure):
+    _fields_ = [("natoms", C.c_int32), ("weighting", C.c_int32), ("noise_mode", C.c_int32),
+                ("track_who", C.c_int32), ("ld", C.c_int64), ("n0", C.c_int64), ("dt", C.c_double),
+                ("alpha", C.c_double), ("sigma", C.c_double * MAX_ATOMS), ("inv_mass", C.c_double * MAX_ATOMS),
+                ("thresh_lower", C.c_double), ("thresh_upper", C.c_double), ("seed", C.c_uint64),
+                ("pes", PES), ("trial", Trial), ("hist", History)]
+
+
+class Noise(C.Structure):
+    _fields_ = [("normal", C.c_void_p), ("u_branch", C.c_void_p), ("u_accept", C.c_void_p),
+                ("ld_noise", C.c_int64)]
+
+
+_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History]
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load():
+    """Load libgbdmc.so (building it first when absent); raises if that fails."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        _build.build()
+    L = C.CDLL(path)
+    P = C.c_void_p
+    sig = {
+        "gbdmc_abi_version": ([], C.c_int),
+        "gbdmc_last_error": ([], C.c_char_p),
+        "gbdmc_scratch_bytes": ([C.c_int64], C.c_size_t),
+        "gbdmc_struct_size": ([C.c_int32], C.c_size_t),
+        "gbdmc_pes_eval": ([C.POINTER(PES), P, C.c_int64, C.c_int64, P, P, P], C.c_int),
+        "gbdmc_trial_eval": ([C.POINTER(Trial), P, C.c_int64, C.c_int64, P, P, P, P], C.c_int),
+        "gbdmc_sim_init": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, P], C.c_int),
+        "gbdmc_sim_step": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P,
+                            C.POINTER(Noise), P], C.c_int),
+        "gbdmc_desc_weights": ([P, P, P, C.c_int64, P, P], C.c_int),
+        "gbdmc_desc_begin": ([P, P, P], C.c_int),
+        "gbdmc_prof_enable": ([C.c_int32], C.c_int),
+        "gbdmc_prof_read": ([C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                             C.POINTER(C.c_int64)], C.c_int),
+        "gbdmc_fp64_fma_probe": ([P, C.c_int64, C.c_int32, C.POINTER(C.c_double), P], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    check_abi()
+    return L
+
+
+def check_abi():
+    L = _lib
+    if L.gbdmc_abi_version() != 1:
+        raise RuntimeError("libgbdmc ABI version mismatch")
+    for i, s in enumerate(_STRUCTS):
+        n = L.gbdmc_struct_size(i)
+        if n != C.sizeof(s):
+            raise RuntimeError(f"ABI struct {s.__name__}: C sizeof {n} != ctypes {C.sizeof(s)}")
+
+
+def check(rc, what="gbdmc"):
+    if rc != OK:
+        msg = _lib.gbdmc_last_error().decode(errors="replace")
+        raise RuntimeError(f"{what} failed (code {rc}): {msg}")

@@ -1,0 +1,117 @@
+"""Output files with the reference's names and keys.
+
+* ``save_h5`` writes ``keyz -> valz`` (SimArchivist.save_h5,
+  simulation_utilities/sim_archive.py:12-23).  With h5py installed it writes
+  HDF5; otherwise the same keys go to ``<fname>.npz`` next to the requested
+  name (h5py is optional here).
+* ``create_filesystem`` / ``delete_older_checkpoints`` mirror FileManager
+  (simulation_utilities/file_manager.py:7-54).
+* The text log follows SimLogger's lines (simulation_utilities/sim_logger.py).
+"""
+import glob
+import os
+
+import numpy as np
+
+from .constants import Constants
+
+__all__ = ["save_h5", "load_h5", "create_filesystem", "delete_older_checkpoints", "SimLogger"]
+
+try:  # optional dependency
+    import h5py as _h5py
+except Exception:  # pragma: no cover - depends on the environment
+    _h5py = None
+
+
+def save_h5(fname, keyz, valz):
+    if _h5py is not None:
+        with _h5py.File(fname, "w") as hf:
+            for k, v in zip(keyz, valz):
+                hf.create_dataset(k, data=v)
+        return fname
+    path = fname + ".npz"
+    np.savez(path, **{k: np.asarray(v) for k, v in zip(keyz, valz)})
+    return path
+
+
+def load_h5(fname):
+    if os.path.exists(fname + ".npz"):
+        with np.load(fname + ".npz") as z:
+            return {k: z[k] for k in z.files}
+    if _h5py is None:
+        raise FileNotFoundError(fname)
+    with _h5py.File(fname, "r") as hf:
+        return {k: hf[k][()] for k in hf.keys()}
+
+
+def create_filesystem(output_folder):
+    for sub in ("", "/chkpts", "/wfns"):
+        os.makedirs(output_folder + sub, exist_ok=True)
+
+
+def delete_older_checkpoints(sim_folder, sim_name, time_step):
+    for p in glob.glob(f"{sim_folder}/chkpts/{sim_name}_*.pickle"):
+        try:
+            t = int(p.split("_")[-1].split(".")[0])
+        except ValueError:
+            continue
+        if t < time_step:
+            os.remove(p)
+
+
+class SimLogger:
+    """Text log with the reference's wording (sim_logger.py:6-93)."""
+
+    def __init__(self, fname, overwrite=False):
+        self.fl = open(fname, "w" if overwrite else "a")
+
+    def close(self):
+        self.fl.close()
+
+    def write(self, s):
+        self.fl.write(s)
+
+    def beginning(self, sim):
+        w = self.fl.write
+        w(f"Simulation {sim.sim_name} starting at step {sim.cur_timestep}\n")
+        w("Potential attributes: \n")
+        for k, v in sim.potential_info.items():
+            if not k.startswith("_"):
+                w(f"\t{k}: {v}\n")
+        w(f"Num Walkers: {sim.num_walkers}\n")
+        w(f"Num Time Steps: {sim.num_timesteps}\n")
+        w(f"Weighting Type: {sim.weighting}\n")
+        w(f"Branch every {sim.branch_every} Time Step(s)\n")
+        w(f"Delta Tau: {sim.delta_t} a.u.\n")
+        w(f"Masses of Each Atom: {sim.masses}\n")
+        w(f"Equilibration Steps Before Collecting Wave Functions: {sim.equil_steps}\n")
+        w(f"Checkpoint Every {sim.chkpt_every} time steps\n")
+        w(f"Collect Wave Functions Every {sim.wfn_every} Time Steps After Equilibration\n\n")
+
+    def step_block(self, t, weighting, h, gpu_time=None):
+        """Per-step lines for step t from the device history h (dict of arrays)."""
+        cv = lambda e: Constants.convert(e, "wavenumbers", to_AU=False)  # noqa: E731
+        w = self.fl.write
+        w(f"Time step {t}\n")
+        if "rejected" in h:
+            tot = h["pop_before"][t]
+            w(f"Metropolis rejected {h['rejected'][t]} of {tot} walkers "
+              f"({(h['rejected'][t] / max(tot, 1)) * 100:0.2f} %)\n")
+        w(f"Potential call time at time step {t}:\n")
+        w(f"\t{gpu_time if gpu_time is not None else 'fused'} seconds\n")
+        w(f"\tAverage energy of ensemble: {cv(h['vmean'][t])} cm-1 (without vref correction)\n")
+        w(f"\tHighest energy walker: {cv(h['vmax'][t])} cm-1\n")
+        w(f"\tLowest energy walker: {cv(h['vmin'][t])} cm-1\n")
+        if weighting == "discrete":
+            w(f"Birth/Death at time step {t}:\n")
+            w(f"\tWalker Births: {h['births'][t]}\n")
+            w(f"\tWalker Deaths: {h['deaths'][t]}\n")
+            w(f"\tNumber of Walkers: {int(h['pop'][t])}\n")
+        else:
+            w(f"Branching at time step {t}:\n")
+            w(f"\tWalkers Branched: {h['births'][t]}:\n")
+
+    def finish(self, seconds):
+        self.fl.write("Simulation has finished.\n\n")
+        self.fl.write(f"Simulation took {seconds} seconds.\n\n")
+        self.fl.close()

@@ -1,0 +1,364 @@
+// Device building blocks of the walker step: counter-based RNG, Gaussian
+// deviates, the analytic potentials with their hand-written adjoints, the
+// internal-coordinate trial wave function with its first/second Cartesian
+// derivatives, and block reductions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math_constants.h>
+#include "gbdmc.h"
+
+namespace gbdmc {
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with the
+// published multipliers and Weyl key increments.
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = M0 * c.x, hi0 = __umulhi(M0, c.x);
+    const uint32_t lo1 = M1 * c.z, hi1 = __umulhi(M1, c.z);
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// Counter layout: (walker index, step low word, stream slot | replica << 8, step high word).
+struct Rng {
+  uint32_t k0, k1, i, s_lo, s_hi, rep;
+  uint32_t slot;
+  U4 buf;
+  int used;
+  __device__ Rng(uint64_t seed, uint64_t step, uint64_t walker, uint32_t replica = 0)
+      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), i((uint32_t)walker),
+        s_lo((uint32_t)step), s_hi((uint32_t)(step >> 32)), rep(replica), slot(0), used(4) {}
+  __device__ __forceinline__ U4 block() {
+    U4 c{i, s_lo, slot | (rep << 8), s_hi ^ (uint32_t)(i >> 31)};
+    ++slot;
+    return philox4x32_10(c, k0, k1);
+  }
+  __device__ __forceinline__ uint32_t next32() {
+    if (used == 4) {
+      buf = block();
+      used = 0;
+    }
+    const uint32_t v = used == 0 ? buf.x : used == 1 ? buf.y : used == 2 ? buf.z : buf.w;
+    ++used;
+    return v;
+  }
+  // uniform in [0,1) with 53 random bits
+  __device__ __forceinline__ double uniform53() {
+    const uint64_t hi = next32(), lo = next32();
+    return (double)((hi << 21) | (lo >> 11)) * 0x1.0p-53;
+  }
+  // two standard normals, Box-Muller in fp32 (u1 in (0,1] from 32 bits)
+  __device__ __forceinline__ void normal2_f32(float& z0, float& z1) {
+    const uint32_t a = next32(), b = next32();
+    const float u1 = fmaf((float)a, 0x1.0p-32f, 0x1.0p-33f);
+    const float u2 = (float)(b >> 8) * 0x1.0p-24f;
+    const float rad = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    z0 = rad * c;
+    z1 = rad * s;
+  }
+  // two standard normals, Box-Muller in fp64 (53-bit uniforms)
+  __device__ __forceinline__ void normal2_f64(double& z0, double& z1) {
+    const double u1 = 1.0 - uniform53();  // (0,1]
+    const double u2 = uniform53();
+    const double rad = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    z0 = rad * c;
+    z1 = rad * s;
+  }
+};
+
+// Fill z[0..n) with standard normals for the chosen noise mode.
+template <int NM, int N>
+__device__ __forceinline__ void gen_normals(Rng& g, double (&z)[N]) {
+  if constexpr (NM == GBDMC_NOISE_PHILOX32) {
+#pragma unroll
+    for (int k = 0; k < N; k += 2) {
+      float a, b;
+      g.normal2_f32(a, b);
+      z[k] = (double)a;
+      if (k + 1 < N) z[k + 1] = (double)b;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; k += 2) {
+      double a, b;
+      g.normal2_f64(a, b);
+      z[k] = a;
+      if (k + 1 < N) z[k + 1] = b;
+    }
+  }
+}
+
+// ------------------------------------------------------------- potentials
+__device__ __forceinline__ double rsqrt_guard(double y) { return y > 0.0 ? 1.0 / sqrt(y) : 0.0; }
+
+// Local-mode water: two Morse OH stretches, harmonic bend 1/2 k (th-th_e)^2,
+// stretch-stretch coupling krr dr1 dr2.  Atoms (o, h1, h2) inside x[3*A].
+// With G: accumulates dV/dx into g.
+template <bool G, int A>
+__device__ __forceinline__ double h2o_lm(const double (&x)[3 * A], const double* p, int o, int h1, int h2,
+                                         double (&g)[3 * A]) {
+  const double De = p[0], a = p[1], re = p[2], kth = p[3], the = p[4], krr = p[5];
+  double d1[3], d2[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    d1[d] = x[3 * h1 + d] - x[3 * o + d];
+    d2[d] = x[3 * h2 + d] - x[3 * o + d];
+  }
+  const double r1 = sqrt(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
+  const double r2 = sqrt(d2[0] * d2[0] + d2[1] * d2[1] + d2[2] * d2[2]);
+  const double dot = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2];
+  const double inv12 = 1.0 / (r1 * r2);
+  double c = dot * inv12;
+  c = fmin(1.0, fmax(-1.0, c));
+  const double th = acos(c);
+  const double dr1 = r1 - re, dr2 = r2 - re;
+  const double x1 = exp(-a * dr1), x2 = exp(-a * dr2);
+  const double e1 = 1.0 - x1, e2 = 1.0 - x2;
+  const double dth = th - the;
+  const double v = De * e1 * e1 + De * e2 * e2 + 0.5 * kth * dth * dth + krr * dr1 * dr2;
+  if constexpr (G) {
+    // adjoint: dV/dr1, dV/dr2, dV/dth, then chain rule through r1, r2, theta
+    const double vr1 = 2.0 * De * e1 * a * x1 + krr * dr2;
+    const double vr2 = 2.0 * De * e2 * a * x2 + krr * dr1;
+    const double vth = kth * dth;
+    const double s = -rsqrt_guard(1.0 - c * c);
+    const double ir1 = 1.0 / r1, ir2 = 1.0 / r2;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double e1d = d1[d] * ir1, e2d = d2[d] * ir2;
+      const double dch1 = d2[d] * inv12 - c * ir1 * e1d;
+      const double dch2 = d1[d] * inv12 - c * ir2 * e2d;
+      const double gh1 = vr1 * e1d + vth * s * dch1;
+      const double gh2 = vr2 * e2d + vth * s * dch2;
+      g[3 * h1 + d] += gh1;
+      g[3 * h2 + d] += gh2;
+      g[3 * o + d] -= gh1 + gh2;
+    }
+  }
+  return v;
+}
+
+template <bool G, int A>
+__device__ __forceinline__ double pes_ho(const double (&x)[3 * A], const double* p, double (&g)[3 * A]) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3 * A; ++k) s = s + x[k] * x[k];
+  if constexpr (G) {
+#pragma unroll
+    for (int k = 0; k < 3 * A; ++k) g[k] += p[0] * x[k];
+  }
+  return 0.5 * p[0] * s;
+}
+
+// Water dimer: monomers (0,1,2) and (3,4,5) + O-O Lennard-Jones + 9
+// intermolecular charge pairs.
+template <bool G>
+__device__ __forceinline__ double pes_dimer(const double (&x)[18], const double* p, double (&g)[18]) {
+  double v = h2o_lm<G, 6>(x, p, 0, 1, 2, g) + h2o_lm<G, 6>(x, p, 3, 4, 5, g);
+  const double eps = p[6], sig = p[7], qH = p[8], qO = p[9];
+  {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
+    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double ir2 = 1.0 / r2;
+    const double s2 = sig * sig * ir2;
+    const double s6 = s2 * s2 * s2;
+    v += 4.0 * eps * (s6 * s6 - s6);
+    if constexpr (G) {
+      const double f = 4.0 * eps * (-12.0 * s6 * s6 + 6.0 * s6) * ir2;  // (dV/dr)/r
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        g[9 + k] += f * d[k];
+        g[k] -= f * d[k];
+      }
+    }
+  }
+  const double q[3] = {qO, qH, qH};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double d[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[k] = x[3 * (3 + j) + k] - x[3 * i + k];
+      const double ir = rsqrt_guard(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      const double qq = q[i] * q[j];
+      v += qq * ir;
+      if constexpr (G) {
+        const double f = -qq * ir * ir * ir;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          g[3 * (3 + j) + k] += f * d[k];
+          g[3 * i + k] -= f * d[k];
+        }
+      }
+    }
+  }
+  return v;
+}
+
+template <int PK, int A, bool G>
+__device__ __forceinline__ double pes(const double (&x)[3 * A], const gbdmc_pes_t& P, double (&g)[3 * A]) {
+  if constexpr (PK == GBDMC_PES_HO) {
+    return pes_ho<G, A>(x, P.p, g);
+  } else if constexpr (PK == GBDMC_PES_H2O_LM) {
+    static_assert(A == 3, "H2O local-mode PES has 3 atoms");
+    return h2o_lm<G, 3>(x, P.p, 0, 1, 2, g);
+  } else {
+    static_assert(A == 6, "dimer PES has 6 atoms");
+    return pes_dimer<G>(x, P.p, g);
+  }
+}
+
+// ----------------------------------------------------------- trial psi
+// psi, d1 = (dpsi/dx)/psi, d2 = (d2psi/dx2)/psi per Cartesian component.
+// Separable Cartesian Gaussian, p[a] = alpha of atom a.
+template <int A>
+__device__ __forceinline__ double trial_ho(const double (&x)[3 * A], const double* p, double (&d1)[3 * A],
+                                           double (&d2)[3 * A]) {
+  double arg = 0.0, norm = 1.0;
+#pragma unroll
+  for (int k = 0; k < 3 * A; ++k) {
+    const double al = p[k / 3];
+    arg += al * x[k] * x[k];
+    norm *= sqrt(sqrt(al * (1.0 / CUDART_PI)));
+    d1[k] = -al * x[k];
+    d2[k] = d1[k] * d1[k] - al;
+  }
+  return norm * exp(-0.5 * arg);
+}
+
+// Product of Gaussians in (r1, r2, theta) of one water (O vertex).  The
+// Cartesian chain rule: with L_q = -alpha_q (q - q_e),
+//   d1_k = sum_q L_q dq/dx_k
+//   d2_k = d1_k^2 + sum_q [ -alpha_q (dq/dx_k)^2 + L_q d2q/dx_k^2 ]
+// which equals the ChainRuleHelper d2psidx2 sum for a direct-product psi.
+template <int A>
+__device__ __forceinline__ double trial_h2o(const double (&x)[3 * A], const double* p, double (&d1o)[3 * A],
+                                            double (&d2o)[3 * A]) {
+  const double a1 = p[0], a2 = p[1], ath = p[2], r1e = p[3], r2e = p[4], the = p[5];
+  double v1[3], v2[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v1[d] = x[3 + d] - x[d];
+    v2[d] = x[6 + d] - x[d];
+  }
+  const double r1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const double r2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const double ir1 = 1.0 / r1, ir2 = 1.0 / r2;
+  const double g = ir1 * ir2;
+  double c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) * g;
+  c = fmin(1.0, fmax(-1.0, c));
+  const double th = acos(c);
+  const double one_m_c2 = 1.0 - c * c;
+  const double s = -rsqrt_guard(one_m_c2);      // dtheta/dcos
+  const double s2 = c * s * s * s;              // d2theta/dcos2 = -c/(1-c^2)^1.5
+  const double L1 = -a1 * (r1 - r1e), L2 = -a2 * (r2 - r2e), Lt = -ath * (th - the);
+  const double n = sqrt(sqrt(a1 * a2 * ath * (1.0 / (CUDART_PI * CUDART_PI * CUDART_PI))));
+  const double psi = n * exp(-0.5 * (a1 * (r1 - r1e) * (r1 - r1e) + a2 * (r2 - r2e) * (r2 - r2e) +
+                                     ath * (th - the) * (th - the)));
+  const double ir1s = ir1 * ir1, ir2s = ir2 * ir2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double e1 = v1[d] * ir1, e2 = v2[d] * ir2;
+    // cos(theta) first derivatives
+    const double dch1 = v2[d] * g - c * ir1 * e1;
+    const double dch2 = v1[d] * g - c * ir2 * e2;
+    const double dco = -(dch1 + dch2);
+    // cos(theta) diagonal second derivatives
+    const double d2ch1 = c * (3.0 * e1 * e1 - 1.0) * ir1s - 2.0 * v2[d] * e1 * ir1s * ir2;
+    const double d2ch2 = c * (3.0 * e2 * e2 - 1.0) * ir2s - 2.0 * v1[d] * e2 * ir2s * ir1;
+    const double h = e1 * ir1 + e2 * ir2;
+    const double d2co = 2.0 * g - 2.0 * (v1[d] + v2[d]) * g * h +
+                        c * (h * h + (2.0 * e1 * e1 - 1.0) * ir1s + (2.0 * e2 * e2 - 1.0) * ir2s);
+    // theta derivatives
+    const double dth_o = s * dco, dth_1 = s * dch1, dth_2 = s * dch2;
+    const double d2th_o = s2 * dco * dco + s * d2co;
+    const double d2th_1 = s2 * dch1 * dch1 + s * d2ch1;
+    const double d2th_2 = s2 * dch2 * dch2 + s * d2ch2;
+    // r derivatives
+    const double d2r1 = (1.0 - e1 * e1) * ir1, d2r2 = (1.0 - e2 * e2) * ir2;
+    // O: depends on r1 (-e1), r2 (-e2), theta
+    {
+      const double f = -L1 * e1 - L2 * e2 + Lt * dth_o;
+      const double t = -a1 * e1 * e1 - a2 * e2 * e2 - ath * dth_o * dth_o + L1 * d2r1 + L2 * d2r2 + Lt * d2th_o;
+      d1o[d] = f;
+      d2o[d] = f * f + t;
+    }
+    // H1: r1 (+e1), theta
+    {
+      const double f = L1 * e1 + Lt * dth_1;
+      const double t = -a1 * e1 * e1 - ath * dth_1 * dth_1 + L1 * d2r1 + Lt * d2th_1;
+      d1o[3 + d] = f;
+      d2o[3 + d] = f * f + t;
+    }
+    // H2: r2 (+e2), theta
+    {
+      const double f = L2 * e2 + Lt * dth_2;
+      const double t = -a2 * e2 * e2 - ath * dth_2 * dth_2 + L2 * d2r2 + Lt * d2th_2;
+      d1o[6 + d] = f;
+      d2o[6 + d] = f * f + t;
+    }
+  }
+  return psi;
+}
+
+template <int TK, int A>
+__device__ __forceinline__ double trial(const double (&x)[3 * A], const gbdmc_trial_t& T, double (&d1)[3 * A],
+                                        double (&d2)[3 * A]) {
+  if constexpr (TK == GBDMC_TRIAL_HO_GAUSS) {
+    return trial_ho<A>(x, T.p, d1, d2);
+  } else {
+    static_assert(A == 3, "H2O trial has 3 atoms");
+    return trial_h2o<A>(x, T.p, d1, d2);
+  }
+}
+
+// ----------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Inclusive warp scan of ints.
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+}  // namespace gbdmc

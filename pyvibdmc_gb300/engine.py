@@ -1,0 +1,558 @@
+"""``DMC_Sim`` -- the GPU diffusion Monte Carlo engine with PyVibDMC's API.
+
+Constructor keywords, properties, output files and error behaviour follow
+``DMC_Sim`` of pyvibdmc/pyvibdmc.py:67-130 (keywords), :132-297 (set-up),
+:358-370 (properties), :701-876 (``propagate``) and :878-932 (``run``).
+The per-step work runs in libgbdmc (sm_103a) on walkers that stay resident in
+HBM; the host only orders steps, handles the event schedule (checkpoints,
+descendant-weighting windows, logs) and reads a 128-byte control block once
+per batch of steps.  Batches of steps are captured into CUDA graphs.
+
+Extra keywords (after ``*``): ``seed`` (Philox key), ``rng`` ('philox32',
+'philox64', or an object with ``standard_normal(shape)`` / ``uniform(n)``
+that supplies the deviates on the host in the reference's call order),
+``capacity`` (walker buffer size, default ``floor(1.5 N0) + 1`` rounded up to
+256), ``graph_steps`` (steps per captured CUDA graph), ``device``,
+``write_files``.
+"""
+import copy
+import ctypes as C
+import os
+import pickle
+import time
+
+import numpy as np
+import torch
+
+from . import _capi
+from . import archive
+from .constants import Constants, get_atomic_num
+from .potentials import Potential_GPU, default_device, to_soa, from_soa
+
+__all__ = ["DMC_Sim", "dmc_restart"]
+
+_MASSIVE = "Massive walker birth or death event!!!!!!! Dying..."
+
+
+class DMC_Sim:
+    def __init__(self, sim_name="DMC_Sim", output_folder="exSimResults", weighting="discrete", num_walkers=10000,
+                 num_timesteps=20000, equil_steps=2000, chkpt_every=1000, wfn_every=1000, desc_wt_steps=100,
+                 atoms=[], delta_t=1, potential=None, masses=None, start_structures=None, start_cont_wts=None,
+                 branch_every=1, log_every=1, cur_timestep=0, cont_wt_thresh=None, imp_samp=None,
+                 imp_samp_oned=False, second_impsamp_displacement=False, excited_state_imp_samp=False,
+                 adiabatic_dmc=None, fixed_node=None, DEBUG_alpha=None, DEBUG_save_desc_wt_tracker=None,
+                 DEBUG_save_training_every=None, DEBUG_save_before_bod=False, DEBUG_mass_change=None,
+                 *, seed=0, rng="philox32", capacity=None, graph_steps=32, device=None, write_files=True,
+                 training_sink=None):
+        unsupported = {"imp_samp_oned": imp_samp_oned, "second_impsamp_displacement": second_impsamp_displacement,
+                       "excited_state_imp_samp": excited_state_imp_samp, "adiabatic_dmc": adiabatic_dmc,
+                       "fixed_node": fixed_node, "DEBUG_mass_change": DEBUG_mass_change,
+                       "DEBUG_save_desc_wt_tracker": DEBUG_save_desc_wt_tracker,
+                       "DEBUG_save_before_bod": DEBUG_save_before_bod}
+        bad = [k for k, v in unsupported.items() if v not in (None, False)]
+        if bad:
+            raise NotImplementedError(f"DMC_Sim options not provided by the GPU engine: {bad}")
+        if branch_every != 1:
+            raise NotImplementedError("the GPU engine branches every step (branch_every=1)")
+        if not isinstance(potential, Potential_GPU):
+            raise TypeError("potential must be a pyvibdmc_gb300.Potential_GPU (the PES is fused into the step "
+                            "kernel); wrap analytic surfaces with the factories in pyvibdmc_gb300.potentials")
+        self.atoms = atoms if isinstance(atoms, list) else [atoms]
+        self.sim_name = sim_name
+        self.output_folder = output_folder
+        self.num_walkers = int(num_walkers)
+        self.num_timesteps = int(num_timesteps)
+        self.potential_info = {k: v for k, v in vars(potential).items()}
+        self.potential = potential
+        self.weighting = weighting.lower()
+        self.desc_wt_time_steps = desc_wt_steps
+        self.branch_every = branch_every
+        self.delta_t = delta_t
+        self.start_structures = start_structures
+        self.start_cont_wts = start_cont_wts
+        self.equil_steps = equil_steps
+        self.chkpt_every = chkpt_every
+        self.wfn_every = wfn_every
+        self.log_every = log_every
+        self.cur_timestep = int(cur_timestep)
+        self.cont_wt_thresh = cont_wt_thresh
+        self.impsamp_manager = imp_samp
+        self._deb_training_every = DEBUG_save_training_every
+        self._deb_alpha = DEBUG_alpha
+        self.seed = int(seed)
+        self.rng = rng
+        self.graph_steps = max(2, int(graph_steps) // 2 * 2)
+        self.write_files = write_files
+        self.training_sink = training_sink
+        self.device = torch.device(device) if device is not None else default_device()
+        self.masses = masses
+        self._initialize(capacity)
+
+    # ------------------------------------------------------------ set-up
+    def _initialize(self, capacity):
+        """pyvibdmc.py:132-297 (schedules, walkers, masses, weighting, guards)."""
+        T = self.num_timesteps
+        self._chkpt_step = set(range(self.chkpt_every, T + self.chkpt_every, self.chkpt_every))
+        wfn = np.arange(self.equil_steps, T + self.wfn_every, self.wfn_every)
+        self._wfn_save_step = set(int(v) for v in wfn)
+        self._desc_wt_save_step = set(int(v) for v in wfn + self.desc_wt_time_steps)
+        if self._deb_training_every is not None:
+            self._train_step = set(range(0, T + self._deb_training_every, self._deb_training_every))
+        else:
+            self._train_step = set()
+        self._log_steps = set(range(0, T, self.log_every))
+        if self.start_structures is None:
+            raise Exception("Please supply a starting structure for your chemical system.")
+        ss = np.asarray(self.start_structures, dtype=np.float64)
+        if ss.ndim != 3:
+            raise Exception("Start structure must have format (n,m,d), where n = 1 or num_walkers, m = num atoms, "
+                            "d = dimensions (usually 3)")
+        if ss.shape[0] == 1:
+            coords = np.repeat(ss, self.num_walkers, axis=0)
+        else:
+            if ss.shape[0] != self.num_walkers:
+                print("WARNING: NUMBER OF STARTING GEOMETRIES DOES NOT EQUAL NUM_WALKERS VARIABLE. MAKE SURE THIS IS"
+                      "INTENTIONAL.")
+            coords = ss
+        if self.masses is None:
+            if "-" in self.atoms[0]:
+                self.masses = np.array([Constants.reduced_mass(self.atoms[0])])
+                self._atm_nums = get_atomic_num(self.atoms[0].split("-"))
+            else:
+                self.masses = np.array([Constants.mass(a) for a in self.atoms])
+                self._atm_nums = get_atomic_num(self.atoms)
+        elif isinstance(self.masses, (int, float)):
+            self.masses = np.array([self.masses])
+            self._atm_nums = [-1]
+        else:
+            self.masses = np.array(self.masses, dtype=np.float64)
+            self._atm_nums = get_atomic_num(self.atoms)
+        if len(self.masses) != len(self.atoms):
+            raise Exception("Your number of atoms list does not match your number of masses you provided.")
+        if coords.shape[1] != len(self.atoms):
+            raise Exception("Your number of atoms list does not match the shape of your walkers.")
+        if coords.shape[2] != 3:
+            raise NotImplementedError("the GPU engine propagates 3D Cartesian walkers")
+        self.natoms = coords.shape[1]
+        if self.natoms != self.potential.natoms:
+            raise ValueError(f"potential has {self.potential.natoms} atoms, walkers have {self.natoms}")
+        if self.natoms > _capi.MAX_ATOMS:
+            raise ValueError(f"at most {_capi.MAX_ATOMS} atoms")
+        self._sigmas = np.sqrt(self.delta_t / self.masses)
+        self._alpha = 1.0 / (2.0 * self.delta_t) if self._deb_alpha is None else self._deb_alpha
+        self._pop_thresh = [self.num_walkers - self.num_walkers * 0.5, self.num_walkers + self.num_walkers * 0.5]
+        n = coords.shape[0]
+        if n < self._pop_thresh[0] or n > self._pop_thresh[1]:
+            if self.weighting == "discrete":
+                raise ValueError(_MASSIVE)
+        self._thresh_lower, self._thresh_upper = None, None
+        if self.weighting == "continuous":
+            t = self.cont_wt_thresh
+            if t is None:
+                self._thresh_lower = 1 / self.num_walkers
+            elif isinstance(t, (int, float)):
+                self._thresh_lower = t
+            elif isinstance(t, list) and len(t) in (1, 2):
+                self._thresh_lower = t[0]
+                self._thresh_upper = t[1] if len(t) == 2 else None
+            else:
+                raise ValueError("Invalid input for continuous weight threshold")
+        elif self.weighting != "discrete":
+            raise ValueError(f"weighting must be 'discrete' or 'continuous', got {self.weighting!r}")
+        if self.impsamp_manager is not None:
+            if getattr(self.impsamp_manager, "natoms", None) != self.natoms or \
+                    not hasattr(self.impsamp_manager, "trial_struct"):
+                raise TypeError("imp_samp must be a pyvibdmc_gb300.ImpSampManager_GPU for these atoms")
+            if self.delta_t != 1:
+                print("WARNING! Using DT>1 for Imp Samp. Make sure this is not a mistake!!!!")
+        if isinstance(self.rng, str):
+            if self.rng not in ("philox32", "philox64"):
+                raise ValueError("rng must be 'philox32', 'philox64' or a deviate source object")
+            self._noise_mode = _capi.NOISE_PHILOX32 if self.rng == "philox32" else _capi.NOISE_PHILOX64
+        else:
+            self._noise_mode = _capi.NOISE_INJECTED
+        min_cap = int(np.floor(self._pop_thresh[1])) + 1
+        cap = max(min_cap, n) if capacity is None else int(capacity)
+        if cap < max(min_cap, n):
+            raise ValueError(f"capacity must be >= {max(min_cap, n)}")
+        self.capacity = (cap + 255) // 256 * 256
+        self._alloc(coords)
+        self._vref_vs_tau = np.zeros(self.num_timesteps)
+        self._pop_vs_tau = np.zeros(self.num_timesteps)
+        self._eff_ts = np.zeros(self.num_timesteps)
+        self._desc_open = None
+        self._graphs = {}
+        if self.write_files:
+            archive.create_filesystem(self.output_folder)
+
+    def _alloc(self, coords):
+        dev, ld, A = self.device, self.capacity, self.natoms
+        f64 = dict(dtype=torch.float64, device=dev)
+        IS = self.impsamp_manager is not None
+        self._bufs = []
+        for _ in range(2 if self.weighting == "discrete" else 1):
+            b = dict(x=torch.zeros(3 * A, ld, **f64), v=torch.zeros(ld, **f64),
+                     who=torch.zeros(ld, dtype=torch.int32, device=dev))
+            if IS:
+                b.update(f=torch.zeros(3 * A, ld, **f64), psi=torch.zeros(ld, **f64), ke=torch.zeros(ld, **f64))
+            self._bufs.append(b)
+        self._w = None
+        if self.weighting == "continuous":
+            self._w = torch.zeros(ld, **f64)
+            w0 = np.ones(len(coords)) if self.start_cont_wts is None else np.asarray(self.start_cont_wts, float)
+            self._w[:len(coords)] = torch.as_tensor(w0, **f64)
+        self._bufs[0]["x"][:, :len(coords)] = to_soa(coords, dev)
+        self._cur = 0
+        self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
+        L = _capi.load()
+        self._scratch = torch.zeros(L.gbdmc_scratch_bytes(ld), dtype=torch.uint8, device=dev)
+        T = max(self.num_timesteps, 1)
+        self._hist = dict(vref=torch.zeros(T, **f64), pop=torch.zeros(T, **f64),
+                          births=torch.zeros(T, dtype=torch.int32, device=dev),
+                          deaths=torch.zeros(T, dtype=torch.int32, device=dev),
+                          rejected=torch.zeros(T, dtype=torch.int32, device=dev),
+                          vmin=torch.zeros(T, **f64), vmax=torch.zeros(T, **f64), vmean=torch.zeros(T, **f64),
+                          eff_ts=torch.zeros(T, **f64))
+        self._n_start = len(coords)
+        self._sim = self._make_sim()
+        self._walkers = [self._walker_struct(b) for b in self._bufs]
+
+    def _make_sim(self):
+        s = _capi.Sim()
+        s.natoms = self.natoms
+        s.weighting = _capi.DISCRETE if self.weighting == "discrete" else _capi.CONTINUOUS
+        s.noise_mode = self._noise_mode
+        s.track_who = 1
+        s.ld = self.capacity
+        s.n0 = self.num_walkers
+        s.dt = float(self.delta_t)
+        s.alpha = float(self._alpha)
+        for a in range(self.natoms):
+            s.sigma[a] = float(self._sigmas[a])
+            s.inv_mass[a] = float(1.0 / self.masses[a])
+        s.thresh_lower = float(self._thresh_lower) if self._thresh_lower is not None else 0.0
+        s.thresh_upper = float(self._thresh_upper) if self._thresh_upper is not None else -1.0
+        s.seed = self.seed & 0xFFFFFFFFFFFFFFFF
+        s.pes = self.potential.pes_struct()
+        if self.impsamp_manager is not None:
+            s.trial = self.impsamp_manager.trial_struct()
+        else:
+            s.trial.kind = _capi.TRIAL_NONE
+            s.trial.natoms = self.natoms
+        h = self._hist
+        s.hist.vref, s.hist.pop = h["vref"].data_ptr(), h["pop"].data_ptr()
+        s.hist.births, s.hist.deaths = h["births"].data_ptr(), h["deaths"].data_ptr()
+        s.hist.rejected = h["rejected"].data_ptr()
+        s.hist.vmin, s.hist.vmax, s.hist.vmean = h["vmin"].data_ptr(), h["vmax"].data_ptr(), h["vmean"].data_ptr()
+        s.hist.eff_ts = h["eff_ts"].data_ptr()
+        s.hist.len = self.num_timesteps
+        return s
+
+    def _walker_struct(self, b):
+        w = _capi.Walkers()
+        w.x, w.v, w.who = b["x"].data_ptr(), b["v"].data_ptr(), b["who"].data_ptr()
+        if "f" in b:
+            w.f, w.psi, w.ke = b["f"].data_ptr(), b["psi"].data_ptr(), b["ke"].data_ptr()
+        if self._w is not None:
+            w.w = self._w.data_ptr()
+        return w
+
+    # ------------------------------------------------------- device calls
+    @staticmethod
+    def _stream():
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _read_ctrl(self):
+        return _capi.Ctrl.from_buffer_copy(self._ctrl.cpu().numpy().tobytes())
+
+    def _write_ctrl(self, ctrl):
+        self._ctrl.copy_(torch.frombuffer(bytearray(bytes(ctrl)), dtype=torch.uint8))
+
+    def _init_device(self):
+        """Step-0 potential / local energy and vref (pyvibdmc.py:760-769)."""
+        c = _capi.Ctrl()
+        c.n = self._n_start if self.cur_timestep == 0 or not hasattr(self, "_n_now") else self._n_now
+        c.step = self.cur_timestep
+        c.eff_ts = self._eff_ts[self.cur_timestep - 1] if self.cur_timestep > 0 else 0.0
+        self._write_ctrl(c)
+        L = _capi.load()
+        _capi.check(L.gbdmc_sim_init(C.byref(self._sim), C.byref(self._walkers[self._cur]),
+                                     C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
+                                     self._stream()), "gbdmc_sim_init")
+
+    def _launch_step(self, cur, noise=None):
+        L = _capi.load()
+        dst = self._walkers[1 - cur] if self.weighting == "discrete" else self._walkers[cur]
+        rc = L.gbdmc_sim_step(C.byref(self._sim), C.byref(self._walkers[cur]), C.byref(dst),
+                              C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
+                              C.byref(noise) if noise is not None else None, self._stream())
+        _capi.check(rc, "gbdmc_sim_step")
+        return 1 - cur if self.weighting == "discrete" else cur
+
+    def _graph_for(self, cur):
+        key = cur
+        g = self._graphs.get(key)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                c = cur
+                for _ in range(self.graph_steps):
+                    c = self._launch_step(c)
+            torch.cuda.current_stream().wait_stream(side)
+            self._graphs[key] = g
+        return g
+
+    def _injected_step(self, cur, n):
+        """Host-supplied deviates in the reference's draw order (pyvibdmc.py:544, :556, :601, :392)."""
+        A = self.natoms
+        z = np.asarray(self.rng.standard_normal((n, 3, A)), dtype=np.float64)
+        zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(3 * A, n)), device=self.device)
+        ua = None
+        if self.impsamp_manager is not None:
+            ua = torch.as_tensor(np.asarray(self.rng.uniform(n), dtype=np.float64), device=self.device)
+        ub = torch.as_tensor(np.asarray(self.rng.uniform(n), dtype=np.float64), device=self.device) \
+            if self.weighting == "discrete" else torch.zeros(max(n, 1), dtype=torch.float64, device=self.device)
+        nz = _capi.Noise()
+        nz.normal, nz.u_branch = zs.data_ptr(), ub.data_ptr()
+        nz.u_accept = ua.data_ptr() if ua is not None else None
+        nz.ld_noise = n
+        self._keep = (zs, ub, ua)
+        return self._launch_step(cur, nz)
+
+    def _run_steps(self, nsteps):
+        """Run nsteps steps on the device; returns after queueing (no sync) in Philox modes."""
+        if self._noise_mode == _capi.NOISE_INJECTED:
+            for _ in range(nsteps):
+                c = self._read_ctrl()
+                if c.status:
+                    return
+                self._cur = self._injected_step(self._cur, c.n)
+            return
+        done = 0
+        while nsteps - done >= self.graph_steps:
+            self._graph_for(self._cur).replay()
+            done += self.graph_steps
+        while done < nsteps:
+            self._cur = self._launch_step(self._cur)
+            done += 1
+
+    # ------------------------------------------------------------ events
+    def _boundaries(self):
+        pts = set(self._chkpt_step) | set(self._wfn_save_step) | set(self._desc_wt_save_step)
+        pts |= {s + 1 for s in self._train_step}
+        return sorted(p for p in pts if p > 0)
+
+    def _n_device(self):
+        return int(self._read_ctrl().n)
+
+    def _coords_host(self, n=None):
+        n = self._n_device() if n is None else n
+        return from_soa(self._bufs[self._cur]["x"], n, self.natoms)
+
+    def _begin_desc(self, t):
+        """pyvibdmc.py:739-747."""
+        L = _capi.load()
+        n = self._n_device()
+        self._parent = self._coords_host(n)
+        self._parent_wts = None if self._w is None else self._w[:n].cpu().numpy().copy()
+        _capi.check(L.gbdmc_desc_begin(C.c_void_p(self._bufs[self._cur]["who"].data_ptr()),
+                                       C.c_void_p(self._ctrl.data_ptr()), self._stream()), "gbdmc_desc_begin")
+        self._desc_open = t
+
+    def _end_desc(self, t):
+        """pyvibdmc.py:856-872."""
+        L = _capi.load()
+        npar = len(self._parent)
+        desc = torch.zeros(max(npar, 1), dtype=torch.float64, device=self.device)
+        wptr = C.c_void_p(self._w.data_ptr()) if self._w is not None else None
+        _capi.check(L.gbdmc_desc_weights(C.c_void_p(self._bufs[self._cur]["who"].data_ptr()), wptr,
+                                         C.c_void_p(self._ctrl.data_ptr()), npar, C.c_void_p(desc.data_ptr()),
+                                         self._stream()), "gbdmc_desc_weights")
+        self._desc_wts = desc[:npar].cpu().numpy()
+        start = t + 1 - self.desc_wt_time_steps
+        self.wfns = getattr(self, "wfns", [])
+        rec = dict(start=start, coords=self._parent, desc_wts=self._desc_wts, parent_wts=self._parent_wts)
+        self.wfns.append(rec)
+        if self.write_files:
+            fname = f"{self.output_folder}/wfns/{self.sim_name}_wfn_{start}ts.hdf5"
+            if self.weighting == "continuous":
+                archive.save_h5(fname, ["coords", "desc_wts", "parent_wts"],
+                                [self._parent, self._desc_wts, self._parent_wts])
+            else:
+                archive.save_h5(fname, ["coords", "desc_wts"], [self._parent, self._desc_wts])
+        self._desc_open = None
+
+    def _harvest(self, t):
+        n = self._n_device()
+        b = self._bufs[self._cur]
+        if self.training_sink is not None:
+            self.training_sink(t, b["x"], b["v"], n)
+        if self.write_files and self._deb_training_every is not None:
+            archive.save_h5(f"{self.output_folder}/{self.sim_name}_training_{t}ts.hdf5", ["coords", "pots"],
+                            [self._coords_host(n), b["v"][:n].cpu().numpy()])
+
+    def _sync_history(self, t0, t1):
+        h = {k: v[t0:t1].cpu().numpy() for k, v in self._hist.items()}
+        self._vref_vs_tau[t0:t1] = h["vref"]
+        self._pop_vs_tau[t0:t1] = h["pop"]
+        self._eff_ts[t0:t1] = h["eff_ts"]
+        return h
+
+    def _log(self, t0, t1, h, secs):
+        if not self.write_files or self._logger is None:
+            return
+        full = {k: np.zeros(self.num_timesteps, dtype=v.dtype) for k, v in h.items()}
+        for k, v in h.items():
+            full[k][t0:t1] = v
+        if self.impsamp_manager is not None:
+            prev = np.concatenate([[self._pop_before], self._pop_vs_tau[t0:t1 - 1]]) if t1 > t0 else []
+            full["pop_before"] = np.zeros(self.num_timesteps, dtype=np.int64)
+            full["pop_before"][t0:t1] = np.asarray(prev, dtype=np.int64)
+        for t in range(t0, t1):
+            if t in self._log_steps:
+                self._logger.step_block(t, self.weighting, full, gpu_time=secs / max(t1 - t0, 1))
+        self._logger.fl.flush()
+
+    # ------------------------------------------------------------ run
+    def propagate(self):
+        """The main loop (pyvibdmc.py:701-876), batched between events."""
+        T = self.num_timesteps
+        t = self.cur_timestep
+        if self.write_files:
+            self._logger.beginning(self)
+        self._init_device()
+        bounds = [b for b in self._boundaries() if b > t] + [T]
+        while t < T:
+            if t in self._chkpt_step and self.write_files:
+                archive.delete_older_checkpoints(self.output_folder, self.sim_name, t)
+                self._chkpt(t)
+            if t in self._wfn_save_step:
+                self._begin_desc(t)
+            t_end = min(b for b in bounds if b > t)
+            t_end = min(t_end, T)
+            self._pop_before = self._n_device() if self.impsamp_manager is not None else 0
+            cur0 = self._cur
+            t_start = time.perf_counter()
+            self._run_steps(t_end - t)
+            c = self._read_ctrl()
+            secs = time.perf_counter() - t_start
+            if c.status:
+                done = int(c.err_step) - t
+                if self.weighting == "discrete":
+                    self._cur = cur0 ^ (done & 1)
+                h = self._sync_history(t, int(c.err_step))
+                self.cur_timestep = int(c.err_step)
+                self._n_now = int(c.n)
+                raise ValueError(_MASSIVE)
+            self._n_now = int(c.n)
+            h = self._sync_history(t, t_end)
+            self._log(t, t_end, h, secs)
+            self.cur_timestep = t_end - 1
+            last = t_end - 1
+            if t_end in self._desc_wt_save_step and self._desc_open is not None:
+                self._end_desc(last)
+            if last in self._train_step:
+                self._harvest(last)
+            t = t_end
+        self.cur_timestep = T - 1
+
+    def run(self):
+        """pyvibdmc.py:878-932: propagate, final checkpoint, ZPE, sim_info."""
+        print("Starting Simulation...")
+        start = time.time()
+        self._logger = archive.SimLogger(f"{self.output_folder}/{self.sim_name}_log.txt",
+                                         overwrite=self.cur_timestep == 0) if self.write_files else None
+        err = None
+        try:
+            self.propagate()
+            if self.write_files:
+                archive.delete_older_checkpoints(self.output_folder, self.sim_name, self.cur_timestep)
+        except Exception as e:  # the reference dumps a checkpoint and re-raises
+            import traceback
+            print("ERROR! An error occurred while running the DMC simulation. Dumping a final checkpoint...")
+            print("Ignore Approximate ZPE!!!")
+            traceback.print_exc()
+            err = e
+        finally:
+            if self.write_files:
+                self._logger.write("\nFinal checkpoint is written to chkpts folder.\n\n")
+                self._chkpt(self.cur_timestep)
+            vref_wvn = Constants.convert(self._vref_vs_tau, "wavenumbers", to_AU=False)
+            print("Simulation Complete")
+            print("Approximate ZPE", np.average(vref_wvn[len(vref_wvn) // 4:]))
+            ts = self._eff_ts if self.impsamp_manager is not None else np.arange(len(vref_wvn)) * self.delta_t
+            if self.write_files:
+                archive.save_h5(f"{self.output_folder}/{self.sim_name}_sim_info.hdf5",
+                                ["vref_vs_tau", "pop_vs_tau", "atomic_nums", "atomic_masses"],
+                                [np.column_stack((ts, self._vref_vs_tau)), np.column_stack((ts, self._pop_vs_tau)),
+                                 self._atm_nums, self.masses])
+            self.elapsed = time.time() - start
+        if self.write_files:
+            self._logger.finish(self.elapsed)
+        self._logger = None
+        if err is not None:
+            raise err
+
+    # ---------------------------------------------------- checkpointing
+    def _state(self):
+        n = self._n_device()
+        st = {k: v for k, v in self.__dict__.items() if not k.startswith("_") and k not in (
+            "potential", "impsamp_manager", "potential_info", "training_sink", "device", "rng")}
+        st.update(_coords=self._coords_host(n), _vref_vs_tau=self._vref_vs_tau.copy(),
+                  _pop_vs_tau=self._pop_vs_tau.copy(), _eff_ts=self._eff_ts.copy(),
+                  _cont_wts=None if self._w is None else self._w[:n].cpu().numpy(),
+                  _masses=np.asarray(self.masses), _atm_nums=self._atm_nums,
+                  _rng=self.rng if isinstance(self.rng, str) else "philox32",
+                  _vref=float(self._read_ctrl().vref))
+        return st
+
+    def _chkpt(self, t):
+        with open(f"{self.output_folder}/chkpts/{self.sim_name}_{t}.pickle", "wb") as fh:
+            pickle.dump(self._state(), fh, protocol=4)
+
+    # ------------------------------------------------------ properties
+    @property
+    def vref_vs_tau(self):
+        v = self._vref_vs_tau[:self.cur_timestep]
+        return np.column_stack((np.arange(len(v)), v))
+
+    @property
+    def walkers(self):
+        x = self._coords_host()
+        if self.weighting == "continuous":
+            return x, self._w[:len(x)].cpu().numpy()
+        return x
+
+    def zpe(self, onwards=None, ret_cm=True):
+        """Mean vref from step ``onwards`` (default: last 3/4 of the run), cm^-1."""
+        v = self._vref_vs_tau
+        o = len(v) // 4 if onwards is None else onwards
+        z = np.average(v[o:])
+        return Constants.convert(z, "wavenumbers", to_AU=False) if ret_cm else z
+
+
+def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsamp=None, **kw):
+    """Reload the first checkpoint of ``sim_name`` and extend the run
+    (pyvibdmc.py:949-965).  The Philox streams are keyed by step index, so a
+    restarted run continues the same trajectory."""
+    import glob
+    files = sorted(glob.glob(f"{chkpt_folder}/chkpts/{sim_name}_*.pickle"))
+    if not files:
+        raise FileNotFoundError(f"no checkpoint for {sim_name} in {chkpt_folder}/chkpts")
+    with open(files[0], "rb") as fh:
+        st = pickle.load(fh)
+    T = st["num_timesteps"] + additional_timesteps
+    sim = DMC_Sim(sim_name=st["sim_name"], output_folder=st["output_folder"], weighting=st["weighting"],
+                  num_walkers=st["num_walkers"], num_timesteps=T, equil_steps=st["equil_steps"],
+                  chkpt_every=st["chkpt_every"], wfn_every=st["wfn_every"], desc_wt_steps=st["desc_wt_time_steps"],
+                  atoms=st["atoms"], delta_t=st["delta_t"], potential=potential, masses=list(st["_masses"]),
+                  start_structures=st["_coords"], start_cont_wts=st["_cont_wts"], log_every=st["log_every"],
+                  cur_timestep=st["cur_timestep"], cont_wt_thresh=st["cont_wt_thresh"], imp_samp=impsamp,
+                  seed=st["seed"], rng=st["_rng"], **kw)
+    n = len(st["_vref_vs_tau"])
+    sim._vref_vs_tau[:n] = st["_vref_vs_tau"]
+    sim._pop_vs_tau[:n] = st["_pop_vs_tau"]
+    sim._eff_ts[:n] = st["_eff_ts"]
+    return sim

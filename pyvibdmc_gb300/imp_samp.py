@@ -1,0 +1,120 @@
+"""GPU importance-sampling plug-ins with the reference's manager contract.
+
+``ImpSampManager_GPU`` exposes ``call_trial(cds) -> (N,)`` and
+``call_derivs(cds) -> (dpsi/dx / psi, d2psi/dx2 / psi)`` (each (N, A, 3),
+already divided by psi), the interface of ImpSampManager /
+ImpSampManager_NoMP (pyvibdmc/simulation_utilities/imp_samp_manager.py:92-139,
+197-224) that ``ImpSamp.drift`` (imp_samp.py:21-26) consumes.  The
+derivatives are the analytic chain rule of the internal-coordinate trial
+(the ChainRuleHelper formulas of imp_samp_helper.py), evaluated by
+``gbdmc_trial_eval`` -- no finite differences.  Inside
+:class:`pyvibdmc_gb300.DMC_Sim` the same device function runs fused in the
+importance-sampled step kernel.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _capi
+from .constants import Constants
+from .potentials import to_soa, from_soa, default_device, _ptr, _stream
+
+__all__ = ["ImpSampManager_GPU", "TrialFunction", "h2o_gaussian_trial", "ho_gaussian_trial"]
+
+
+class ImpSampManager_GPU:
+    """Trial wave function evaluated on the GPU.
+
+    :param kind: 'h2o_gauss' (product of Gaussians in r1, r2, theta of an
+        O,H,H water) or 'ho_gauss' (separable Cartesian Gaussian)
+    :param alpha: Gaussian exponents (3 for h2o_gauss, one per atom for ho_gauss)
+    :param qe: centres (r1e, r2e, theta_e) for h2o_gauss
+    """
+
+    def __init__(self, kind, alpha, qe=None, natoms=None, device=None):
+        if kind not in ("h2o_gauss", "ho_gauss"):
+            raise ValueError(f"unknown trial kind {kind!r}")
+        self.kind = kind
+        self.alpha = [float(a) for a in alpha]
+        self.qe = None if qe is None else [float(q) for q in qe]
+        self.natoms = 3 if kind == "h2o_gauss" else (natoms or len(self.alpha))
+        if kind == "h2o_gauss" and (len(self.alpha) != 3 or self.qe is None or len(self.qe) != 3):
+            raise ValueError("h2o_gauss needs 3 alphas and 3 centres")
+        if kind == "ho_gauss" and len(self.alpha) != self.natoms:
+            raise ValueError("ho_gauss needs one alpha per atom")
+        self.device = device
+
+    def trial_struct(self):
+        t = _capi.Trial()
+        t.natoms = self.natoms
+        if self.kind == "h2o_gauss":
+            t.kind = _capi.TRIAL_H2O_GAUSS
+            for i, v in enumerate(self.alpha + self.qe):
+                t.p[i] = v
+        else:
+            t.kind = _capi.TRIAL_HO_GAUSS
+            for i, v in enumerate(self.alpha):
+                t.p[i] = v
+        return t
+
+    def _dev(self):
+        return torch.device(self.device) if self.device is not None else default_device()
+
+    def eval_soa(self, x, n, ld=None):
+        L = _capi.load()
+        ld = x.shape[1] if ld is None else ld
+        psi = torch.empty(max(n, 1), dtype=torch.float64, device=x.device)
+        d1 = torch.empty_like(x)
+        d2 = torch.empty_like(x)
+        _capi.check(L.gbdmc_trial_eval(C.byref(self.trial_struct()), _ptr(x), n, ld, _ptr(psi), _ptr(d1),
+                                       _ptr(d2), _stream()), "gbdmc_trial_eval")
+        return psi[:n], d1, d2
+
+    def call_trial(self, cds):
+        cds = np.asarray(cds, dtype=np.float64)
+        psi, _, _ = self.eval_soa(to_soa(cds, self._dev()), len(cds))
+        return psi.cpu().numpy()
+
+    def call_derivs(self, cds):
+        cds = np.asarray(cds, dtype=np.float64)
+        n = len(cds)
+        _, d1, d2 = self.eval_soa(to_soa(cds, self._dev()), n)
+        return from_soa(d1, n, self.natoms), from_soa(d2, n, self.natoms)
+
+
+class TrialFunction(torch.autograd.Function):
+    """psi_T(x) for x (N, A, 3) float64 on the GPU; backward uses the
+    hand-written adjoint: dpsi/dx = psi * (dpsi/dx / psi)."""
+
+    @staticmethod
+    def forward(ctx, x, manager):
+        n, A, _ = x.shape
+        xs = x.detach().reshape(n, 3 * A).t().contiguous()
+        psi, d1, _ = manager.eval_soa(xs, n)
+        ctx.save_for_backward(psi, d1.t().reshape(n, A, 3))
+        return psi.clone()
+
+    @staticmethod
+    def backward(ctx, gp):
+        psi, d1 = ctx.saved_tensors
+        return (gp * psi)[:, None, None] * d1, None
+
+
+def h2o_gaussian_trial(omega_r=3800.0, omega_theta=1600.0, re=1.81, theta_e_deg=104.5, device=None):
+    """Gaussians in (r1, r2, theta): alpha_r = mu_OH omega_r and
+    alpha_theta = omega_theta / G_thetatheta at the equilibrium geometry
+    (the bend G-matrix element of call_trl_h2o.py:38-46)."""
+    mo, mh = Constants.mass("O"), Constants.mass("H")
+    mu = mo * mh / (mo + mh)
+    th = np.deg2rad(theta_e_deg)
+    g = 1 / (mh * re ** 2) + 1 / (mh * re ** 2) + (1 / mo) * (2 / re ** 2 - 2 * np.cos(th) / (re * re))
+    w = Constants.atomic_units["wavenumbers"]
+    alpha = [mu * omega_r * w, mu * omega_r * w, omega_theta * w / g]
+    return ImpSampManager_GPU("h2o_gauss", alpha, [re, re, th], device=device)
+
+
+def ho_gaussian_trial(masses, omega_wavenumbers, device=None):
+    """Separable Gaussian with alpha_a = m_a omega per atom."""
+    w = Constants.convert(omega_wavenumbers, "wavenumbers")
+    return ImpSampManager_GPU("ho_gauss", [m * w for m in masses], natoms=len(masses), device=device)

@@ -1,0 +1,245 @@
+"""Generate the golden fixtures by running the UNMODIFIED reference engine.
+
+Run from the repository root with the reference checkout available::
+
+    python tests/golden/make_golden.py /root/reference
+
+What it does:
+
+* stubs ``h5py`` (in-memory ``File`` that records every dataset written by
+  ``SimArchivist.save_h5``) and ``matplotlib`` -- neither is installed and the
+  reference uses them only for output files and plots;
+* imports ``pyvibdmc`` from the given checkout;
+* replaces ``np.random.normal`` / ``np.random.random`` with
+  :class:`oracle.InjectedNoise` (deterministic, platform independent), so the
+  reference and the GPU engine consume identical deviates in the reference's
+  call order;
+* runs small DMC simulations through the reference's own plug-in path
+  (``Potential_Direct`` for the PES, ``ImpSampManager_NoMP`` for the trial
+  wave function, whose derivative function uses the reference's
+  ``ChainRuleHelper``), and ``ImpSamp.finite_diff`` / ``ChainRuleHelper`` on
+  the reference test geometry;
+* writes ``tests/golden/*.npz``.
+
+The fixtures hold the seeds, the inputs and the reference outputs.
+"""
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+H5_STORE = {}
+
+
+def _install_stubs():
+    h5 = types.ModuleType("h5py")
+
+    class File:
+        def __init__(self, fname, mode="r"):
+            self.fname = fname
+            self.mode = mode
+            if "w" in mode:
+                H5_STORE[fname] = {}
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+        def create_dataset(self, key, data):
+            H5_STORE[self.fname][key] = np.array(data, copy=True)
+
+        def __getitem__(self, key):
+            return H5_STORE[self.fname][key]
+
+    h5.File = File
+    sys.modules["h5py"] = h5
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    plt.rcParams = {}
+    mpl.pyplot = plt
+    mpl.use = lambda *a, **k: None
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = plt
+
+
+def _import_reference(path):
+    _install_stubs()
+    sys.path.insert(0, path)
+    import pyvibdmc as pv
+    return pv
+
+
+class _Patch:
+    def __init__(self, noise):
+        self.noise = noise
+
+    def __enter__(self):
+        self.saved = (np.random.normal, np.random.random)
+        np.random.normal = self.noise.normal
+        np.random.random = self.noise.random
+        return self
+
+    def __exit__(self, *a):
+        np.random.normal, np.random.random = self.saved
+
+
+TRIAL_MODULE = '''
+import numpy as np
+import pyvibdmc as pv
+
+ALPHA = {alpha!r}
+QE = {qe!r}
+
+
+def _internals(cds):
+    an = pv.AnalyzeWfn(cds)
+    r1 = an.bond_length(1, 0)
+    r2 = an.bond_length(2, 0)
+    th = an.bond_angle(1, 0, 2)
+    return r1, r2, th
+
+
+def trial(cds):
+    qs = _internals(cds)
+    out = np.ones(len(cds))
+    for q, a, qe in zip(qs, ALPHA, QE):
+        out = out * ((a / np.pi) ** 0.25 * np.exp(-a * (q - qe) ** 2 / 2))
+    return out
+
+
+def derivs(cds):
+    """dpsi/dx/psi, d2psi/dx2/psi through the reference ChainRuleHelper,
+    mirroring call_trl_h2o.py:101-149 for one water (O,H,H)."""
+    qs = _internals(cds)
+    dpsi_dr = np.stack([-a * (q - qe) for q, a, qe in zip(qs, ALPHA, QE)])
+    d2psi_dr2 = np.stack([(a * (q - qe)) ** 2 - a for q, a, qe in zip(qs, ALPHA, QE)])
+    crh = pv.ChainRuleHelper(cds, np)
+    ohs = [[0, 1], [0, 2]]
+    hoh = [1, 0, 2]
+    cos_theta = np.cos(qs[2])
+    dr_dxs = np.stack([crh.dr_dx(oh) for oh in ohs])
+    d2r_dx2s = np.stack([crh.d2r_dx2(oh, dr_dx=dr_dxs[n]) for n, oh in enumerate(ohs)])
+    dcth_dx = crh.dcth_dx(hoh, cos_theta=cos_theta, dr_da=dr_dxs[0], dr_dc=dr_dxs[1])
+    dth_dx = crh.dth_dx(hoh, cos_theta=cos_theta, dcth_dx=dcth_dx, dr_da=dr_dxs[0], dr_dc=dr_dxs[1])
+    d2th_dx2 = crh.d2th_dx2(hoh, cos_theta=cos_theta, dcth_dx=dcth_dx, dr_da=dr_dxs[0],
+                            dr_dc=dr_dxs[1], d2r_da2=d2r_dx2s[0], d2r_dc2=d2r_dx2s[1])
+    dint = np.stack([dr_dxs[0], dr_dxs[1], dth_dx])
+    d2int = np.stack([d2r_dx2s[0], d2r_dx2s[1], d2th_dx2])
+    return crh.dpsidx(dpsi_dr, dint), crh.d2psidx2(d2psi_dr2, d2int, dpsi_dr, dint)
+'''
+
+
+def run_reference(pv, out_dir, name, x0, atoms, masses, dt, nsteps, pes, seed, weighting="discrete",
+                  imp=None, equil=None, wfn_every=None, desc=None, thresh=None):
+    noise = oracle.InjectedNoise(seed)
+    kw = dict(sim_name=name, output_folder=os.path.join(out_dir, name), weighting=weighting,
+              num_walkers=len(x0), num_timesteps=nsteps, equil_steps=equil if equil is not None else nsteps + 10,
+              chkpt_every=10 ** 6, wfn_every=wfn_every or 10 ** 6, desc_wt_steps=desc or 1,
+              atoms=atoms, masses=masses, delta_t=dt, potential=pv.Potential_Direct(pes),
+              start_structures=np.array(x0, copy=True), log_every=10 ** 6, cont_wt_thresh=thresh,
+              imp_samp=imp)
+    sim = pv.DMC_Sim(**kw)
+    with _Patch(noise):
+        sim.run()
+    out = dict(vref=np.array(sim._vref_vs_tau), pop=np.array(sim._pop_vs_tau),
+               x_final=np.array(sim._walker_coords), v_final=np.array(sim._walker_pots),
+               n_noise_calls=noise.calls)
+    if weighting == "continuous":
+        out["w_final"] = np.array(sim._cont_wts)
+    if imp is not None:
+        out["eff_ts"] = np.array(sim.eff_ts)
+        out["psi_final"] = np.array(sim.psi_1)
+        out["f_final"] = np.array(sim.f_x)
+    wfns = sorted(k for k in H5_STORE if "/wfns/" in k and k.startswith(kw["output_folder"]))
+    for i, k in enumerate(wfns):
+        for key, val in H5_STORE[k].items():
+            out[f"wfn{i}_{key}"] = val
+    return out
+
+
+def main(ref_path):
+    pv = _import_reference(ref_path)
+    tmp = tempfile.mkdtemp(prefix="gbdmc_golden_")
+    fixtures = {}
+
+    # --- config-1 family: 3D HO, discrete, 40 steps
+    ho = oracle.ho_config()
+    n = 256
+    x0 = 0.1 * oracle.InjectedNoise(101).standard_normal((n, 1, 3))
+    pes = lambda c, k=ho["k"]: oracle.pes_ho(c, k)
+    r = run_reference(pv, tmp, "ho", x0, ["H"], ho["masses"], 10.0, 40, pes, seed=1)
+    fixtures["ho_discrete"] = dict(x0=x0, seed=1, dt=10.0, nsteps=40, **r)
+
+    # --- config-2 family: H2O local mode, discrete + descendant weights
+    p, masses = oracle.h2o_config()
+    eq = oracle.h2o_equilibrium(p)
+    n = 384
+    x0 = eq[None] + 0.05 * oracle.InjectedNoise(202).standard_normal((n, 3, 3))
+    pes = lambda c, p=p: oracle.pes_h2o_lm(c, p)
+    r = run_reference(pv, tmp, "h2o", x0, ["O", "H", "H"], masses, 10.0, 60, pes, seed=2,
+                      equil=20, wfn_every=30, desc=10)
+    fixtures["h2o_discrete"] = dict(x0=x0, seed=2, dt=10.0, nsteps=60, equil=20, wfn_every=30, desc=10, **r)
+
+    # --- continuous weights (lower threshold only), H2O
+    n = 192
+    x0 = eq[None] + 0.05 * oracle.InjectedNoise(303).standard_normal((n, 3, 3))
+    r = run_reference(pv, tmp, "h2o_cont", x0, ["O", "H", "H"], masses, 10.0, 40, pes, seed=3,
+                      weighting="continuous", thresh=0.2)
+    fixtures["h2o_continuous"] = dict(x0=x0, seed=3, dt=10.0, nsteps=40, thresh=0.2, **r)
+
+    # --- config-3 family: importance sampling with the Gaussian internal trial
+    alpha, qe = oracle.h2o_trial_config(p)
+    mod_dir = os.path.join(tmp, "trialmod")
+    os.makedirs(mod_dir)
+    with open(os.path.join(mod_dir, "gauss_trial_h2o.py"), "w") as fh:
+        fh.write(TRIAL_MODULE.format(alpha=list(alpha), qe=list(qe)))
+    imp = pv.ImpSampManager_NoMP(trial_function="trial", trial_directory=mod_dir,
+                                 python_file="gauss_trial_h2o.py", deriv_function="derivs")
+    n = 256
+    x0 = eq[None] + 0.03 * oracle.InjectedNoise(404).standard_normal((n, 3, 3))
+    r = run_reference(pv, tmp, "h2o_is", x0, ["O", "H", "H"], masses, 10.0, 30, pes, seed=4, imp=imp)
+    fixtures["h2o_is"] = dict(x0=x0, seed=4, dt=10.0, nsteps=30, alpha=np.array(alpha), qe=np.array(qe), **r)
+
+    # --- derivative pins on the reference test geometry (test_imp_samp_helper.py:8-11),
+    # reordered O,H,H, plus random displacements
+    wc = np.array([[1.81005599, 0., 0.], [-0.45344658, 1.75233806, 0.], [0., 0., 0.]]) * 1.01
+    wc = wc[[2, 0, 1]]
+    geo = wc[None] + 0.05 * oracle.InjectedNoise(505).standard_normal((64, 3, 3))
+    sys.path.insert(0, mod_dir)
+    import gauss_trial_h2o as gt  # noqa: E402
+    d1, d2 = gt.derivs(geo)
+    fd1, fd2, fpsi = pv.ImpSamp.finite_diff(np.array(geo, copy=True), gt.trial)
+    fixtures["h2o_trial_derivs"] = dict(geo=geo, psi=gt.trial(geo), d1=d1, d2=d2, fd1=fd1, fd2=fd2,
+                                        fpsi=fpsi, alpha=np.array(alpha), qe=np.array(qe))
+
+    # --- Metropolis / local KE pins through the reference's static methods
+    ns = oracle.InjectedNoise(606)
+    xa = geo
+    xb = geo + 0.02 * ns.standard_normal(geo.shape)
+    sig = np.sqrt(10.0 / np.asarray(masses))
+    sig3 = np.repeat(sig, 3).reshape(3, 3)[None]
+    inv3 = (1 / np.repeat(masses, 3)).reshape(3, 3)[None]
+    fa, _ = gt.derivs(xa)
+    fb, sdb = gt.derivs(xb)
+    met = pv.ImpSamp.metropolis(sig3, gt.trial(xa), gt.trial(xb), xa, xb, inv3 * fa, inv3 * fb, 10.0)
+    ke = pv.ImpSamp.local_kin(inv3, sdb)
+    fixtures["h2o_metropolis"] = dict(xa=xa, xb=xb, met=met, ke=ke, masses=np.asarray(masses))
+
+    for name, d in fixtures.items():
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
+        print(f"wrote {path} ({os.path.getsize(path)} bytes)")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,206 @@
+"""GPU parity: libgbdmc kernels (through the C ABI) against the oracle and the
+golden fixtures of the reference engine.
+
+Tolerances: coordinates, populations, branch counts and descendant weights
+bit-exact; potentials 1e-12 Eh; vref 1e-12 Eh; importance-sampled runs 1e-10
+(the adjoint derivatives differ from the reference's NumPy chain rule in
+the last bits, which moves proposals by ~1e-16 bohr)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pyvibdmc_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    with np.load(os.path.join(G, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def geoms(n, seed=3, scale=0.08):
+    p, _ = oracle.h2o_config()
+    return oracle.h2o_equilibrium(p)[None] + scale * oracle.InjectedNoise(seed).standard_normal((n, 3, 3))
+
+
+def dimer_geoms(n, seed=4):
+    x = geoms(2 * n, seed)
+    return np.concatenate([x[:n], x[n:] + np.array([5.6, 0.2, -0.3])], axis=1)
+
+
+# ---------------------------------------------------------------- kernels
+@pytest.mark.parametrize("n", [1, 31, 33, 1025, 20000])
+def test_h2o_pes_matches_oracle(n):
+    p, _ = oracle.h2o_config()
+    x = geoms(n)
+    v = pg.h2o_local_mode().getpot(x)
+    np.testing.assert_allclose(v, oracle.pes_h2o_lm(x, p), rtol=0, atol=1e-12)
+
+
+def test_ho_and_dimer_pes_match_oracle():
+    ho = oracle.ho_config()
+    x1 = 0.3 * oracle.InjectedNoise(5).standard_normal((777, 1, 3))
+    np.testing.assert_allclose(pg.harmonic_oscillator().getpot(x1), oracle.pes_ho(x1, ho["k"]), rtol=1e-14, atol=0)
+    x3 = 0.3 * oracle.InjectedNoise(6).standard_normal((300, 3, 3))
+    pot3 = pg.Potential_GPU("harmonic_oscillator", {"k": ho["k"]}, natoms=3)
+    np.testing.assert_allclose(pot3.getpot(x3), oracle.pes_ho(x3, ho["k"]), rtol=1e-14, atol=0)
+    pd, _ = oracle.dimer_config()
+    xd = dimer_geoms(513)
+    np.testing.assert_allclose(pg.water_dimer().getpot(xd), oracle.pes_dimer(xd, pd), rtol=0, atol=1e-12)
+
+
+def test_pes_adjoint_matches_oracle_fd_and_autograd():
+    p, _ = oracle.h2o_config()
+    x = geoms(257)
+    pot = pg.h2o_local_mode()
+    v, g = pot.getgrad(x)
+    np.testing.assert_allclose(g, oracle.grad_h2o_lm(x, p), rtol=0, atol=1e-12)
+    # central finite differences, h = 1e-3 bohr as the reference's ImpSamp.finite_diff
+    h = 1e-3
+    for a in range(3):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[:, a, d] += h
+            xm[:, a, d] -= h
+            fd = (pot.getpot(xp) - pot.getpot(xm)) / (2 * h)
+            np.testing.assert_allclose(g[:, a, d], fd, rtol=0, atol=2e-6)
+    # torch autograd of a float64 torch restatement of the PES
+    xt = torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+    d1 = xt[:, 1] - xt[:, 0]
+    d2 = xt[:, 2] - xt[:, 0]
+    r1, r2 = d1.norm(dim=1), d2.norm(dim=1)
+    th = torch.acos((d1 * d2).sum(1) / (r1 * r2))
+    vt = (p["De"] * (1 - torch.exp(-p["a"] * (r1 - p["re"]))) ** 2 + p["De"] * (1 - torch.exp(-p["a"] * (r2 - p["re"]))) ** 2
+          + 0.5 * p["ktheta"] * (th - p["theta_e"]) ** 2 + p["krr"] * (r1 - p["re"]) * (r2 - p["re"]))
+    gt, = torch.autograd.grad(vt.sum(), xt)
+    np.testing.assert_allclose(g, gt.cpu().numpy(), rtol=0, atol=1e-12)
+    # the autograd.Function wrapper routes backward through the adjoint kernel
+    xg = torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+    vv = pg.PESFunction.apply(xg, pot)
+    (vv * 2.0).sum().backward()
+    np.testing.assert_allclose(xg.grad.cpu().numpy(), 2.0 * g, rtol=0, atol=1e-12)
+    pd, _ = oracle.dimer_config()
+    xd = dimer_geoms(129)
+    _, gd = pg.water_dimer().getgrad(xd)
+    np.testing.assert_allclose(gd, oracle.grad_dimer(xd, pd), rtol=0, atol=1e-12)
+
+
+def test_trial_adjoint_matches_chain_rule_helper_golden():
+    g = load("h2o_trial_derivs")
+    t = pg.ImpSampManager_GPU("h2o_gauss", g["alpha"], g["qe"])
+    np.testing.assert_allclose(t.call_trial(g["geo"]), g["psi"], rtol=1e-13)
+    d1, d2 = t.call_derivs(g["geo"])
+    np.testing.assert_allclose(d1, g["d1"], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(d2, g["d2"], rtol=0, atol=1e-10)
+    # against the reference's central finite differences (h = 1e-3)
+    np.testing.assert_allclose(d1, g["fd1"] / g["fpsi"][:, None, None], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(d2, g["fd2"] / g["fpsi"][:, None, None], rtol=0, atol=2e-3)
+    # and torch autograd through the TrialFunction adjoint
+    xg = torch.tensor(g["geo"], dtype=torch.float64, device="cuda", requires_grad=True)
+    psi = pg.TrialFunction.apply(xg, t)
+    psi.sum().backward()
+    np.testing.assert_allclose(xg.grad.cpu().numpy(), d1 * g["psi"][:, None, None], rtol=1e-10, atol=1e-14)
+
+
+# ----------------------------------------------------------------- engine
+def _sim(x0, masses, atoms, pot, seed, nsteps, **kw):
+    return pg.DMC_Sim(sim_name="t", output_folder="/tmp/gbdmc_test", num_walkers=len(x0), num_timesteps=nsteps,
+                      equil_steps=kw.pop("equil", nsteps + 10), wfn_every=kw.pop("wfn_every", 10 ** 6),
+                      desc_wt_steps=kw.pop("desc", 1), chkpt_every=10 ** 6, atoms=atoms, masses=masses,
+                      delta_t=10.0, potential=pot, start_structures=x0, rng=oracle.InjectedNoise(seed),
+                      write_files=False, **kw)
+
+
+def test_engine_ho_discrete_bit_exact_vs_reference():
+    g = load("ho_discrete")
+    ho = oracle.ho_config()
+    sim = _sim(g["x0"], ho["masses"], ["H"], pg.harmonic_oscillator(), int(g["seed"]), int(g["nsteps"]))
+    sim.run()
+    np.testing.assert_array_equal(sim._pop_vs_tau, g["pop"])
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    x = sim.walkers
+    assert np.array_equal(x, g["x_final"])  # coordinates bit-exact
+
+
+def test_engine_h2o_discrete_descendants_bit_exact_vs_reference():
+    g = load("h2o_discrete")
+    _, m = oracle.h2o_config()
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pg.h2o_local_mode(), int(g["seed"]), int(g["nsteps"]),
+               equil=int(g["equil"]), wfn_every=int(g["wfn_every"]), desc=int(g["desc"]))
+    sim.run()
+    np.testing.assert_array_equal(sim._pop_vs_tau, g["pop"])
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    assert np.array_equal(sim.walkers, g["x_final"])
+    assert len(sim.wfns) == 2
+    for i, w in enumerate(sim.wfns):
+        assert np.array_equal(w["coords"], g[f"wfn{i}_coords"])
+        assert np.array_equal(w["desc_wts"], g[f"wfn{i}_desc_wts"])
+
+
+def test_engine_continuous_vs_reference():
+    g = load("h2o_continuous")
+    _, m = oracle.h2o_config()
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pg.h2o_local_mode(), int(g["seed"]), int(g["nsteps"]),
+               weighting="continuous", cont_wt_thresh=float(g["thresh"]))
+    sim.run()
+    x, w = sim.walkers
+    assert np.array_equal(x, g["x_final"])
+    np.testing.assert_allclose(w, g["w_final"], rtol=1e-12)
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sim._pop_vs_tau, g["pop"], rtol=1e-13)
+
+
+def test_engine_importance_sampling_vs_reference():
+    g = load("h2o_is")
+    _, m = oracle.h2o_config()
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pg.h2o_local_mode(), int(g["seed"]), int(g["nsteps"]),
+               imp_samp=pg.ImpSampManager_GPU("h2o_gauss", g["alpha"], g["qe"]))
+    sim.run()
+    np.testing.assert_array_equal(sim._pop_vs_tau, g["pop"])
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(sim._eff_ts, g["eff_ts"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(sim.walkers, g["x_final"], rtol=0, atol=1e-10)
+
+
+def test_population_guard_raises_value_error():
+    ho = oracle.ho_config()
+    x0 = np.zeros((100, 1, 3))
+    x0[50:, 0, 0] = np.sqrt(2 * 2.0 / ho["k"])  # V = 2 Eh for half the walkers -> w ~ e^10
+    sim = _sim(x0, ho["masses"], ["H"], pg.harmonic_oscillator(), 3, 20)
+    with pytest.raises(ValueError, match="Massive walker"):
+        sim.run()
+    assert sim.cur_timestep == 0
+
+
+def test_philox_graph_batching_is_deterministic():
+    _, m = oracle.h2o_config()
+    x0 = geoms(4000, seed=11, scale=0.05)
+    runs = []
+    for gs in (2, 32):
+        sim = pg.DMC_Sim(num_walkers=4000, num_timesteps=100, equil_steps=1000, atoms=["O", "H", "H"], masses=m,
+                         delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=123,
+                         graph_steps=gs, write_files=False)
+        sim.run()
+        runs.append((sim._vref_vs_tau.copy(), sim.walkers))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
+@pytest.mark.parametrize("rng", ["philox32", "philox64"])
+def test_ho_zpe_analytic(rng):
+    """3D HO, omega = 3000 cm^-1: ZPE = 4500 cm^-1."""
+    ho = oracle.ho_config()
+    x0 = 0.1 * oracle.InjectedNoise(12).standard_normal((10000, 1, 3))
+    sim = pg.DMC_Sim(num_walkers=10000, num_timesteps=6000, equil_steps=10 ** 6, atoms=["H"], masses=ho["masses"],
+                     delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=7, rng=rng,
+                     write_files=False)
+    sim.run()
+    v = pg.Constants.convert(sim._vref_vs_tau[1000:], "wavenumbers", to_AU=False)
+    blocks = v.reshape(10, -1).mean(1)
+    err = blocks.std(ddof=1) / np.sqrt(len(blocks))
+    assert abs(v.mean() - 4500.0) < max(5 * err, 15.0), (v.mean(), err)

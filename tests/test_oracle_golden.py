@@ -1,0 +1,130 @@
+"""The oracle (oracle/dmc_oracle.py) against fixtures produced by running the
+unmodified reference engine (tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    with np.load(os.path.join(G, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def test_injected_noise_is_deterministic():
+    a = oracle.InjectedNoise(7)
+    b = oracle.InjectedNoise(7)
+    z1, u1 = a.standard_normal((5, 3, 2)), a.uniform(9)
+    z2, u2 = b.standard_normal((5, 3, 2)), b.uniform(9)
+    assert np.array_equal(z1, z2) and np.array_equal(u1, u2)
+    big = oracle.InjectedNoise(1).standard_normal((200000,))
+    assert abs(big.mean()) < 0.01 and abs(big.std() - 1) < 0.01
+
+
+def test_ho_discrete_matches_reference():
+    g = load("ho_discrete")
+    ho = oracle.ho_config()
+    sim = oracle.OracleDMC(g["x0"], ho["masses"], float(g["dt"]), lambda c: oracle.pes_ho(c, ho["k"]),
+                           oracle.InjectedNoise(int(g["seed"]))).run(int(g["nsteps"]))
+    assert np.array_equal(np.array(sim.vref_hist), g["vref"])
+    assert np.array_equal(np.array(sim.pop_hist), g["pop"])
+    assert np.array_equal(sim.x, g["x_final"])
+    assert np.array_equal(sim.v, g["v_final"])
+
+
+def test_h2o_discrete_and_descendants_match_reference():
+    g = load("h2o_discrete")
+    p, m = oracle.h2o_config()
+    sim = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), equil_steps=int(g["equil"]),
+                           wfn_every=int(g["wfn_every"]), desc_wt_steps=int(g["desc"])).run(int(g["nsteps"]))
+    assert np.array_equal(np.array(sim.vref_hist), g["vref"])
+    assert np.array_equal(sim.x, g["x_final"])
+    assert len(sim.wfns) == 2
+    for i, w in enumerate(sim.wfns):
+        assert np.array_equal(w["coords"], g[f"wfn{i}_coords"])
+        assert np.array_equal(w["desc_wts"], g[f"wfn{i}_desc_wts"])
+
+
+def test_h2o_continuous_matches_reference():
+    g = load("h2o_continuous")
+    p, m = oracle.h2o_config()
+    sim = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), weighting="continuous",
+                           cont_wt_thresh=float(g["thresh"])).run(int(g["nsteps"]))
+    assert np.array_equal(np.array(sim.vref_hist), g["vref"])
+    assert np.array_equal(sim.x, g["x_final"])
+    assert np.array_equal(sim.w, g["w_final"])
+    assert sum(c[0] for c in sim.counters) > 0  # branching happened
+
+
+def test_h2o_importance_sampling_matches_reference():
+    g = load("h2o_is")
+    p, m = oracle.h2o_config()
+    tr = oracle.TrialH2OGauss(g["alpha"], g["qe"])
+    sim = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), trial=tr).run(int(g["nsteps"]))
+    # the oracle's chain rule differs from ChainRuleHelper's evaluation order at 1e-15
+    np.testing.assert_allclose(np.array(sim.vref_hist), g["vref"], rtol=0, atol=1e-12)
+    assert sim.x.shape == g["x_final"].shape
+    np.testing.assert_allclose(sim.x, g["x_final"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(np.array(sim.eff_ts), g["eff_ts"], rtol=0, atol=1e-12)
+
+
+def test_trial_derivatives_match_chain_rule_helper():
+    g = load("h2o_trial_derivs")
+    tr = oracle.TrialH2OGauss(g["alpha"], g["qe"])
+    d1, d2 = tr.derivs(g["geo"])
+    np.testing.assert_allclose(tr.psi(g["geo"]), g["psi"], rtol=1e-13)
+    np.testing.assert_allclose(d1, g["d1"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(d2, g["d2"], rtol=0, atol=1e-11)
+    # reference finite differences (h = 1e-3 bohr) agree to their truncation error
+    fd1, fd2, fpsi = oracle.finite_diff(g["geo"], tr.psi)
+    np.testing.assert_allclose(fd1, g["fd1"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(fd1 / fpsi[:, None, None], d1, rtol=0, atol=1e-4)
+    np.testing.assert_allclose(fd2 / fpsi[:, None, None], d2, rtol=0, atol=2e-3)
+
+
+def test_metropolis_and_local_kin_match_reference():
+    g = load("h2o_metropolis")
+    a, qe = oracle.h2o_trial_config()
+    tr = oracle.TrialH2OGauss(a, qe)
+    m = g["masses"]
+    sig3 = np.repeat(np.sqrt(10.0 / m), 3).reshape(3, 3)[None]
+    inv3 = (1 / np.repeat(m, 3)).reshape(3, 3)[None]
+    fa, _ = tr.derivs(g["xa"])
+    fb, sdb = tr.derivs(g["xb"])
+    met = oracle.metropolis(sig3, tr.psi(g["xa"]), tr.psi(g["xb"]), g["xa"], g["xb"], inv3 * fa, inv3 * fb, 10.0)
+    np.testing.assert_allclose(met, g["met"], rtol=1e-10)
+    np.testing.assert_allclose(oracle.local_kin(inv3, sdb), g["ke"], rtol=1e-12)
+
+
+def test_pes_gradients_match_finite_differences():
+    p, _ = oracle.h2o_config()
+    rng = oracle.InjectedNoise(9)
+    x = oracle.h2o_equilibrium(p)[None] + 0.05 * rng.standard_normal((16, 3, 3))
+    g = oracle.grad_h2o_lm(x, p)
+    h = 1e-5
+    fd = np.zeros_like(x)
+    for a in range(3):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[:, a, d] += h
+            xm[:, a, d] -= h
+            fd[:, a, d] = (oracle.pes_h2o_lm(xp, p) - oracle.pes_h2o_lm(xm, p)) / (2 * h)
+    np.testing.assert_allclose(g, fd, atol=1e-8)
+    pd, _ = oracle.dimer_config()
+    xd = np.concatenate([x[:4], x[:4] + np.array([5.5, 0.3, 0.2])], axis=1)
+    gd = oracle.grad_dimer(xd, pd)
+    fdd = np.zeros_like(xd)
+    for a in range(6):
+        for d in range(3):
+            xp, xm = xd.copy(), xd.copy()
+            xp[:, a, d] += h
+            xm[:, a, d] -= h
+            fdd[:, a, d] = (oracle.pes_dimer(xp, pd) - oracle.pes_dimer(xm, pd)) / (2 * h)
+    np.testing.assert_allclose(gd, fdd, atol=1e-8)
