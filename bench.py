@@ -233,14 +233,17 @@ def run_ours(args):
 
     def one_step(i):
         if i % DESC_WINDOW == 0:
+            launches[0] += 1 if sim._lazy else 0
+            sim._compact()
             _capi.check(L.gbdmc_desc_begin(who_ptr(), ctrl_ptr, sp), "desc_begin")
             launches[0] += 1
-        sim._cur = sim._launch_step(sim._cur)
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
         launches[0] += 2
         if (i + 1) % DESC_WINDOW == 0:
+            sim._compact()
             _capi.check(L.gbdmc_desc_weights(who_ptr(), None, ctrl_ptr, int(sim.capacity), C.c_void_p(desc.data_ptr()),
                                              sp), "desc_weights")
-            launches[0] += 2
+            launches[0] += 3
 
     for i in range(W):
         one_step(i)
@@ -282,7 +285,9 @@ def run_ours(args):
     # ---- warm-L2 graph replay (information: back-to-back steps as DMC_Sim.run issues them)
     gsteps = 32
     sim.graph_steps = gsteps
-    g = sim._graph_for(sim._cur)
+    if not sim._lazy:
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
+    g = sim._graph_for(sim._cur, sim._lazy)
     g.replay()
     torch.cuda.synchronize()
     s_before = int(sim._read_ctrl().step)
@@ -303,7 +308,7 @@ def run_ours(args):
     s_before = int(sim._read_ctrl().step)
     for i in range(kp):
         flush.fill_(i & 0xFF)
-        sim._cur = sim._launch_step(sim._cur)
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
     mv_ms, mv_n, sc_ms, sc_n = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
     _capi.check(L.gbdmc_prof_read(C.byref(mv_ms), C.byref(mv_n), C.byref(sc_ms), C.byref(sc_n)), "prof_read")
     _capi.check(L.gbdmc_prof_enable(0), "prof_enable")
@@ -358,12 +363,13 @@ def run_ours(args):
 
 def run_e2e(sim, L, dev, steps):
     """Walkers in pinned host memory; per step: H2D walkers, gbdmc_sim_step,
-    D2H branched walkers + control block (the reference-facing call with host
-    buffers)."""
+    gbdmc_walkers_compact, D2H branched walkers, potentials and the control
+    block (the reference-facing call with host buffers)."""
     import torch
     from pyvibdmc_gb300 import _capi
     A3 = 3 * sim.natoms
     cap = sim.capacity
+    sim._compact()
     n = int(sim._read_ctrl().n)
     host_x = torch.empty((A3, cap), dtype=torch.float64).pin_memory()
     host_v = torch.empty(cap, dtype=torch.float64).pin_memory()
@@ -375,23 +381,25 @@ def run_e2e(sim, L, dev, steps):
     t0 = time.perf_counter()
     for _ in range(steps):
         b = sim._bufs[sim._cur]
-        b["x"][:, :n].copy_(host_x[:, :n], non_blocking=True)
-        h2d += A3 * n * 8
+        b["x"].copy_(host_x, non_blocking=True)
+        h2d += A3 * cap * 8
         total += n
-        sim._cur = sim._launch_step(sim._cur)
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
+        sim._compact()
+        nb = sim._bufs[sim._cur]
         host_ctrl.copy_(sim._ctrl, non_blocking=True)
+        host_x.copy_(nb["x"], non_blocking=True)
+        host_v.copy_(nb["v"], non_blocking=True)
         torch.cuda.current_stream().synchronize()
         c = _capi.Ctrl.from_buffer_copy(host_ctrl.numpy().tobytes())
         n = int(c.n)
-        nb = sim._bufs[sim._cur]
-        host_x[:, :n].copy_(nb["x"][:, :n], non_blocking=True)
-        host_v[:n].copy_(nb["v"][:n], non_blocking=True)
-        d2h += (A3 + 1) * n * 8 + C.sizeof(_capi.Ctrl)
+        d2h += (A3 + 1) * cap * 8 + C.sizeof(_capi.Ctrl)
     torch.cuda.synchronize()
     secs = time.perf_counter() - t0
     return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
             "d2h_bytes_per_step": d2h // steps, "steps": steps,
-            "path": "pinned host walkers -> H2D -> gbdmc_sim_step (C ABI) -> D2H walkers, V, ctrl"}
+            "path": "pinned host walker buffer -> H2D -> gbdmc_sim_step + gbdmc_walkers_compact (C ABI) -> "
+                    "D2H walkers, V, control block; host sync per step"}
 
 
 def main():

@@ -92,7 +92,10 @@ enum {
 
 enum { GBDMC_DISCRETE = 0, GBDMC_CONTINUOUS = 1 };
 
-/* walker state, SoA, caller-owned device memory */
+/* walker state, SoA, caller-owned device memory.
+ * Logical walker j of a replica with slot offset `off` is stored at slot
+ * off + idx[off + j] when idx != NULL (lazy compaction after branching) and
+ * at slot off + j when idx == NULL. */
 typedef struct {
   double* x;    /* [3A][ld] coordinates (bohr)                               */
   double* v;    /* [ld] potential, or local energy when importance sampling */
@@ -101,6 +104,7 @@ typedef struct {
   double* psi;  /* [ld] trial psi (importance sampling)                     */
   double* ke;   /* [ld] local kinetic energy (importance sampling)          */
   double* w;    /* [ld] continuous weights, or NULL                         */
+  int32_t* idx; /* [ld] gather index of the logical walkers, or NULL        */
 } gbdmc_walkers_t;
 
 /* device-resident control block (caller allocates sizeof(gbdmc_ctrl_t)) */
@@ -148,10 +152,24 @@ typedef struct {
   double thresh_lower; /* continuous weighting thresholds (pyvibdmc.py:214-231) */
   double thresh_upper; /* <= 0 : none */
   uint64_t seed;
+  int32_t block_threads; /* walkers per tile / threads per block (32..256, multiple of 32);
+                            0 = chosen from n0 so that the tiles spread over all SMs */
+  uint32_t replica_id;   /* Philox stream of a single simulation (gbdmc_sim_*)      */
   gbdmc_pes_t pes;
   gbdmc_trial_t trial; /* kind GBDMC_TRIAL_NONE: plain DMC */
   gbdmc_history_t hist;
 } gbdmc_sim_t;
+
+/* One replica of a batched ensemble: its walkers occupy slots
+ * [off, off + cap) of every SoA array of the batch. */
+#define GBDMC_MAX_REPLICAS 64
+typedef struct {
+  int64_t off;     /* first slot                                    */
+  int64_t cap;     /* slots reserved (>= 1.5 n0 + 1)                */
+  int64_t n0;      /* target population num_walkers                 */
+  uint32_t stream; /* Philox stream id of the replica               */
+  int32_t reserved;
+} gbdmc_replica_t;
 
 /* injected noise for one step (GBDMC_NOISE_INJECTED only; device pointers) */
 typedef struct {
@@ -181,13 +199,36 @@ int gbdmc_trial_eval(const gbdmc_trial_t* trial, const double* x_dev, int64_t n,
 int gbdmc_sim_init(const gbdmc_sim_t* sim, const gbdmc_walkers_t* w, gbdmc_ctrl_t* ctrl_dev,
                    void* scratch_dev, void* stream);
 
-/* One full walker step.  Discrete weighting reads `src` and writes the
- * branched population to `dst` (ping-pong); continuous weighting updates
- * `src` in place and ignores `dst`.  noise may be NULL unless
- * sim->noise_mode == GBDMC_NOISE_INJECTED. */
+/* One full walker step.  Reads the logical walkers of `src` (state + its
+ * gather index) and writes the moved walkers in pre-branch order to the
+ * state arrays of `dst`; with discrete weighting the branched population
+ * is dst's state gathered through dst->idx (written by the call), with
+ * continuous weighting dst->idx must be NULL and dst holds the walkers in
+ * order.  src and dst must not share arrays.  noise may be NULL unless
+ * sim->noise_mode == GBDMC_NOISE_INJECTED (normals/uniforms indexed by the
+ * logical walker). */
 int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
                    gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, const gbdmc_noise_t* noise,
                    void* stream);
+
+/* Batched ensemble of nrep <= GBDMC_MAX_REPLICAS independent replicas in
+ * one launch per phase (persistent grid over all replicas' tiles).  sim->ld
+ * is the total slot count, sim->n0 is ignored (per replica in reps), ctrl_dev
+ * holds nrep control blocks and the history arrays are replica-major with
+ * stride sim->hist.len.  Scratch: gbdmc_batch_scratch_bytes(reps, nrep). */
+int gbdmc_batch_init(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                     const gbdmc_walkers_t* w, gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
+int gbdmc_batch_step(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                     const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl_dev,
+                     void* scratch_dev, const gbdmc_noise_t* noise, void* stream);
+size_t gbdmc_batch_scratch_bytes(const gbdmc_replica_t* reps, int32_t nrep);
+
+/* Compaction: out[off + j] = the logical walker j of `in` (through in->idx)
+ * for j < ctrl[r].n of every replica; out->idx is ignored.  For the single
+ * simulation pass nrep = 0 and reps = NULL (one replica over [0, sim->ld)). */
+int gbdmc_walkers_compact(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                          const gbdmc_walkers_t* in, const gbdmc_walkers_t* out,
+                          const gbdmc_ctrl_t* ctrl_dev, void* stream);
 
 /* Descendant weights: desc_dev[q] = #walkers (or sum of weights, w_dev != NULL)
  * whose ancestor id is q; desc_dev has n_parent entries and is overwritten. */
@@ -200,7 +241,7 @@ int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);
 
 /* sizeof() of the ABI structs, for binding self-checks:
  * 0 gbdmc_sim_t, 1 gbdmc_walkers_t, 2 gbdmc_ctrl_t, 3 gbdmc_noise_t,
- * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t; 0 for unknown ids. */
+ * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t, 7 gbdmc_replica_t; 0 for unknown ids. */
 size_t gbdmc_struct_size(int32_t which);
 
 /* ---- measurement aids (no counterpart in the reference; used by bench.py) ----

@@ -29,7 +29,7 @@ class Trial(C.Structure):
 
 class Walkers(C.Structure):
     _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("f", C.c_void_p),
-                ("psi", C.c_void_p), ("ke", C.c_void_p), ("w", C.c_void_p)]
+                ("psi", C.c_void_p), ("ke", C.c_void_p), ("w", C.c_void_p), ("idx", C.c_void_p)]
 
 
 class Ctrl(C.Structure):
@@ -50,7 +50,16 @@ class Sim(C.Structure):
                 ("track_who", C.c_int32), ("ld", C.c_int64), ("n0", C.c_int64), ("dt", C.c_double),
                 ("alpha", C.c_double), ("sigma", C.c_double * MAX_ATOMS), ("inv_mass", C.c_double * MAX_ATOMS),
                 ("thresh_lower", C.c_double), ("thresh_upper", C.c_double), ("seed", C.c_uint64),
+                ("block_threads", C.c_int32), ("replica_id", C.c_uint32),
                 ("pes", PES), ("trial", Trial), ("hist", History)]
+
+
+MAX_REPLICAS = 64
+
+
+class Replica(C.Structure):
+    _fields_ = [("off", C.c_int64), ("cap", C.c_int64), ("n0", C.c_int64), ("stream", C.c_uint32),
+                ("reserved", C.c_int32)]
 
 
 class Noise(C.Structure):
@@ -58,7 +67,7 @@ class Noise(C.Structure):
                 ("ld_noise", C.c_int64)]
 
 
-_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History]
+_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica]
 
 _lib = None
 
@@ -89,6 +98,13 @@ def load():
                             C.POINTER(Noise), P], C.c_int),
         "gbdmc_desc_weights": ([P, P, P, C.c_int64, P, P], C.c_int),
         "gbdmc_desc_begin": ([P, P, P], C.c_int),
+        "gbdmc_batch_init": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers), P, P, P],
+                             C.c_int),
+        "gbdmc_batch_step": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers),
+                              C.POINTER(Walkers), P, P, C.POINTER(Noise), P], C.c_int),
+        "gbdmc_batch_scratch_bytes": ([C.POINTER(Replica), C.c_int32], C.c_size_t),
+        "gbdmc_walkers_compact": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers),
+                                   C.POINTER(Walkers), P, P], C.c_int),
         "gbdmc_prof_enable": ([C.c_int32], C.c_int),
         "gbdmc_prof_read": ([C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                              C.POINTER(C.c_int64)], C.c_int),

@@ -7,6 +7,9 @@
 
 namespace gbdmc {
 
+constexpr int kEvalTPB = 128;  // threads per block of the plug-in evaluation kernels
+static inline int eval_grid(int64_t n) { return (int)((n + kEvalTPB - 1) / kEvalTPB); }
+
 static thread_local char g_err[512] = "";
 
 void set_error(const char* fmt, ...) {
@@ -27,7 +30,7 @@ int check_launch(const char* what) {
 
 // V (and optionally dV/dx) for walkers i < n, SoA with leading dimension ld.
 template <int PK, int A, bool G>
-__global__ void __launch_bounds__(kTPB) k_pes_eval(const gbdmc_pes_t P, const double* __restrict__ x, int64_t n,
+__global__ void __launch_bounds__(kEvalTPB) k_pes_eval(const gbdmc_pes_t P, const double* __restrict__ x, int64_t n,
                                                     int64_t ld, double* __restrict__ v, double* __restrict__ g) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -45,7 +48,7 @@ __global__ void __launch_bounds__(kTPB) k_pes_eval(const gbdmc_pes_t P, const do
 }
 
 template <int TK, int A>
-__global__ void __launch_bounds__(kTPB) k_trial_eval(const gbdmc_trial_t T, const double* __restrict__ x, int64_t n,
+__global__ void __launch_bounds__(kEvalTPB) k_trial_eval(const gbdmc_trial_t T, const double* __restrict__ x, int64_t n,
                                                       int64_t ld, double* __restrict__ psi, double* __restrict__ d1,
                                                       double* __restrict__ d2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,11 +67,11 @@ __global__ void __launch_bounds__(kTPB) k_trial_eval(const gbdmc_trial_t T, cons
 template <int PK, int A>
 static void launch_pes(const gbdmc_pes_t& P, const double* x, int64_t n, int64_t ld, double* v, double* g,
                        cudaStream_t s) {
-  const int G = grid_for(n);
+  const int G = eval_grid(n);
   if (g)
-    k_pes_eval<PK, A, true><<<G, kTPB, 0, s>>>(P, x, n, ld, v, g);
+    k_pes_eval<PK, A, true><<<G, kEvalTPB, 0, s>>>(P, x, n, ld, v, g);
   else
-    k_pes_eval<PK, A, false><<<G, kTPB, 0, s>>>(P, x, n, ld, v, g);
+    k_pes_eval<PK, A, false><<<G, kEvalTPB, 0, s>>>(P, x, n, ld, v, g);
 }
 
 }  // namespace gbdmc
@@ -79,10 +82,6 @@ extern "C" int gbdmc_abi_version(void) { return GBDMC_ABI_VERSION; }
 
 extern "C" const char* gbdmc_last_error(void) { return g_err; }
 
-extern "C" size_t gbdmc_scratch_bytes(int64_t ld) {
-  if (ld <= 0) return 0;
-  return scratch_layout(nullptr, ld).bytes;
-}
 
 extern "C" int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x, int64_t n, int64_t ld, double* v,
                               double* grad, void* stream) {
@@ -133,11 +132,11 @@ extern "C" int gbdmc_trial_eval(const gbdmc_trial_t* t, const double* x, int64_t
   }
   if (n == 0) return GBDMC_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  const int G = grid_for(n);
+  const int G = eval_grid(n);
   const int A = t->natoms;
   if (t->kind == GBDMC_TRIAL_HO_GAUSS) {
-    if (A == 1) k_trial_eval<GBDMC_TRIAL_HO_GAUSS, 1><<<G, kTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
-    else if (A == 3) k_trial_eval<GBDMC_TRIAL_HO_GAUSS, 3><<<G, kTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
+    if (A == 1) k_trial_eval<GBDMC_TRIAL_HO_GAUSS, 1><<<G, kEvalTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
+    else if (A == 3) k_trial_eval<GBDMC_TRIAL_HO_GAUSS, 3><<<G, kEvalTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
     else {
       set_error("gbdmc_trial_eval: HO trial supports 1 or 3 atoms (got %d)", A);
       return GBDMC_ERR_ARG;
@@ -147,7 +146,7 @@ extern "C" int gbdmc_trial_eval(const gbdmc_trial_t* t, const double* x, int64_t
       set_error("gbdmc_trial_eval: H2O trial needs 3 atoms (got %d)", A);
       return GBDMC_ERR_ARG;
     }
-    k_trial_eval<GBDMC_TRIAL_H2O_GAUSS, 3><<<G, kTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
+    k_trial_eval<GBDMC_TRIAL_H2O_GAUSS, 3><<<G, kEvalTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
   } else {
     set_error("gbdmc_trial_eval: unknown trial kind %d", t->kind);
     return GBDMC_ERR_ARG;
@@ -164,6 +163,7 @@ extern "C" size_t gbdmc_struct_size(int32_t which) {
     case 4: return sizeof(gbdmc_pes_t);
     case 5: return sizeof(gbdmc_trial_t);
     case 6: return sizeof(gbdmc_history_t);
+    case 7: return sizeof(gbdmc_replica_t);
   }
   return 0;
 }

@@ -1,4 +1,4 @@
-// Host-side helpers shared by the C-ABI translation units.
+// Host/device helpers shared by the C-ABI translation units.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -7,9 +7,10 @@
 
 namespace gbdmc {
 
-constexpr int kTPB = 256;  // threads per block of the per-walker kernels
+constexpr int kMaxTPB = 256;  // largest tile (walkers per tile = threads per block)
+constexpr int kMinTPB = 32;
 
-// Per-block partial results of a walker kernel (64 bytes).
+// Per-tile partial results of a walker kernel (64 bytes).
 struct Partial {
   long long c;       // sum of branch counts (or accepted moves)
   long long births;  // sum of max(c-1, 0)
@@ -22,11 +23,20 @@ struct Partial {
 };
 static_assert(sizeof(Partial) == 64, "Partial is 64 bytes");
 
-inline int grid_for(int64_t ld) { return (int)((ld + kTPB - 1) / kTPB); }
+// Replica table passed by value (__grid_constant__) to every step kernel.
+struct RepTable {
+  int32_t nrep;
+  int32_t tpb;
+  int32_t tile_off[GBDMC_MAX_REPLICAS + 1];  // first tile of each replica; [nrep] = total tiles
+  int64_t off[GBDMC_MAX_REPLICAS];
+  int64_t cap[GBDMC_MAX_REPLICAS];
+  int64_t n0[GBDMC_MAX_REPLICAS];
+  uint32_t stream[GBDMC_MAX_REPLICAS];
+};
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// scratch layout: [Partial x G][int64 prefix x G][int32 counts x ld][int32 list x ld][uint8 flags x ld]
+// scratch layout: [Partial x tiles][int64 prefix x tiles][int32 counts x ld][int32 list x ld][uint8 flags x ld]
 struct ScratchLayout {
   Partial* part;
   long long* prefix;
@@ -36,15 +46,14 @@ struct ScratchLayout {
   size_t bytes;
 };
 
-inline ScratchLayout scratch_layout(void* base, int64_t ld) {
+inline ScratchLayout scratch_layout(void* base, int64_t ld, int64_t max_tiles) {
   ScratchLayout L;
-  const int G = grid_for(ld);
   size_t off = 0;
   char* b = (char*)base;
   L.part = (Partial*)(b + off);
-  off += align256(sizeof(Partial) * (size_t)G);
+  off += align256(sizeof(Partial) * (size_t)max_tiles);
   L.prefix = (long long*)(b + off);
-  off += align256(sizeof(long long) * (size_t)G);
+  off += align256(sizeof(long long) * (size_t)max_tiles);
   L.counts = (int*)(b + off);
   off += align256(sizeof(int) * (size_t)ld);
   L.list = (int*)(b + off);
@@ -55,7 +64,15 @@ inline ScratchLayout scratch_layout(void* base, int64_t ld) {
   return L;
 }
 
+// Upper bound of the tile count for any tile width >= kMinTPB.
+inline int64_t max_tiles_for(const gbdmc_replica_t* reps, int nrep) {
+  int64_t t = 0;
+  for (int r = 0; r < nrep; ++r) t += (reps[r].cap + kMinTPB - 1) / kMinTPB;
+  return t;
+}
+
 void set_error(const char* fmt, ...);
+int check_launch(const char* what);
 
 // Event-pair timing of the step kernels (gbdmc_prof_enable / gbdmc_prof_read).
 struct ProfState {
@@ -66,6 +83,7 @@ struct ProfState {
   cudaEvent_t ev[kSlots][3];
 };
 extern ProfState g_prof;
-int check_launch(const char* what);
+
+int num_sms();
 
 }  // namespace gbdmc

@@ -1,18 +1,27 @@
-// The DMC walker step on the GPU.
+// The DMC walker step on the GPU, for one simulation or a batch of
+// independent replicas (up to GBDMC_MAX_REPLICAS per launch).
 //
-// Discrete weighting, plain DMC (2 launches per step):
-//   k_move_count  : x += sigma*z (bit-exact x + fl(sigma*z)), V = PES(x),
-//                   w = exp(-(V-vref) dt), c = floor(w) + [u < w - floor(w)],
-//                   per-block partials; the last block to finish scans the
-//                   block counts into prefix[], computes N', vref' and the
-//                   population guards (pyvibdmc.py:380-431, :651-661).
-//   k_scatter     : each walker writes its c copies at prefix + local scan
-//                   into the other buffer (np.repeat(arange(N), c) order).
-// Importance sampling inserts k_is_move (drift-diffusion proposal, trial psi
-// adjoint at the proposal, Metropolis, accept, V + local KE; pyvibdmc.py:549-612,
-// :807-809) before a k_count pass that uses dt_eff = dt * accepted/N.
-// Continuous weighting replaces count/scatter by the single-CTA
-// k_cont_branch (sequential argmax cloning, pyvibdmc.py:340-356, :432-454).
+// Walkers are SoA; replica r owns slots [off_r, off_r + cap_r).  Each
+// replica's capacity is cut into tiles of `tpb` walkers; a launch runs a
+// grid-stride (persistent) loop over all tiles of all replicas.  Per step,
+// discrete weighting, plain DMC (2 launches):
+//   k_move   : gather walker j of the replica through src->idx, x += sigma*z
+//              (bit-exact x + fl(sigma*z)), V = PES(x), w = exp(-(V-vref) dt),
+//              c = floor(w) + [u < w - floor(w)]; writes the moved walker to
+//              slot j of dst (pre-branch order), c to counts[], a partial per
+//              tile.  The last tile of each replica to finish scans the tile
+//              counts into prefix[], computes N', vref' and the population
+//              guards (pyvibdmc.py:380-431, :651-661).
+//   k_branch : walker j writes its index j into dst->idx[prefix + scan, +c),
+//              i.e. np.repeat(arange(N), counts); the next step gathers
+//              through it, so branching moves 4 bytes per walker copy instead
+//              of the whole walker state.
+// Importance sampling: k_is_move (drift-diffusion proposal, trial psi and its
+// adjoint at the proposal, Metropolis, accept, V + local KE;
+// pyvibdmc.py:549-612, :807-809), then k_count (weights with
+// dt_eff = dt * accepted/N) and k_branch.  Continuous weighting replaces
+// count/branch by k_cont_branch, one CTA per replica (sequential argmax
+// cloning, pyvibdmc.py:340-356, :432-454).
 #include "gbdmc_device.cuh"
 #include "gbdmc_internal.cuh"
 
@@ -28,32 +37,38 @@ __device__ __forceinline__ Partial partial_zero() {
 }
 
 // Deterministic block reduction of a Partial (fixed shuffle/shared tree).
+// STATS: also the fp64 sum/min/max of V.  Result valid in thread 0.
+template <bool STATS>
 __device__ Partial block_reduce_partial(Partial p) {
-  __shared__ Partial sh[kTPB / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ Partial sh[kMaxTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   p.c = warp_sum(p.c);
   p.births = warp_sum(p.births);
   p.deaths = warp_sum(p.deaths);
   p.aux = warp_sum(p.aux);
   p.s0 = warp_sum(p.s0);
-  p.s1 = warp_sum(p.s1);
-  p.vmin = warp_min(p.vmin);
-  p.vmax = warp_max(p.vmax);
+  if (STATS) {
+    p.s1 = warp_sum(p.s1);
+    p.vmin = warp_min(p.vmin);
+    p.vmax = warp_max(p.vmax);
+  }
   if (lane == 0) sh[wid] = p;
   __syncthreads();
   if (wid == 0) {
-    p = lane < kTPB / 32 ? sh[lane] : partial_zero();
+    p = lane < nw ? sh[lane] : partial_zero();
     p.c = warp_sum(p.c);
     p.births = warp_sum(p.births);
     p.deaths = warp_sum(p.deaths);
     p.aux = warp_sum(p.aux);
     p.s0 = warp_sum(p.s0);
-    p.s1 = warp_sum(p.s1);
-    p.vmin = warp_min(p.vmin);
-    p.vmax = warp_max(p.vmax);
+    if (STATS) {
+      p.s1 = warp_sum(p.s1);
+      p.vmin = warp_min(p.vmin);
+      p.vmax = warp_max(p.vmax);
+    }
   }
   __syncthreads();
-  return p;  // valid in thread 0
+  return p;
 }
 
 __device__ __forceinline__ Partial load_partial(const Partial* p) {
@@ -76,32 +91,43 @@ __device__ __forceinline__ void accumulate(Partial& a, const Partial& b) {
   a.vmax = fmax(a.vmax, b.vmax);
 }
 
-// Elects the last block of the grid to finish (threadFenceReduction pattern).
-// All blocks call it after writing their partial; returns true in every thread
-// of the last block.
-__device__ __forceinline__ bool last_block(gbdmc_ctrl_t* ctrl) {
+__device__ __forceinline__ int replica_of(const RepTable& T, int tile) {
+  int lo = 0, hi = T.nrep - 1;
+  while (lo < hi) {  // last r with tile_off[r] <= tile
+    const int mid = (lo + hi + 1) >> 1;
+    if (T.tile_off[mid] <= tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Elects the last tile of replica `ctrl` to finish (threadFenceReduction
+// pattern, no waiting).  Every thread of the block calls it after the tile's
+// partial is written; returns true in all threads of the electing block.
+__device__ __forceinline__ bool last_tile(gbdmc_ctrl_t* ctrl, int ntiles) {
   __shared__ bool am_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned t = atomicAdd(&ctrl->ticket, 1u);
-    am_last = (t == gridDim.x - 1);
+    am_last = (t == (unsigned)ntiles - 1u);
   }
   __syncthreads();
-  if (am_last) __threadfence();
-  return am_last;
+  const bool r = am_last;
+  if (r) __threadfence();
+  __syncthreads();
+  return r;
 }
 
-// Last block: fixed-order reduction of all partials (and, when prefix != NULL,
-// an exclusive scan of the block counts into prefix[]).  Result in thread 0.
-__device__ Partial reduce_partials(const Partial* part, int G, long long* prefix) {
-  const int per = (G + kTPB - 1) / kTPB;
-  const int beg = min(G, threadIdx.x * per), end = min(G, beg + per);
+// Fixed-order reduction of the partials of tiles [t0, t0+nt) (and, when
+// prefix != NULL, an exclusive scan of their counts into prefix[]).
+template <bool STATS>
+__device__ Partial reduce_partials(const Partial* part, int t0, int nt, long long* prefix) {
+  const int per = (nt + blockDim.x - 1) / blockDim.x;
+  const int beg = min(nt, (int)threadIdx.x * per), end = min(nt, beg + per);
   Partial acc = partial_zero();
-  for (int j = beg; j < end; ++j) accumulate(acc, load_partial(part + j));
+  for (int j = beg; j < end; ++j) accumulate(acc, load_partial(part + t0 + j));
   if (prefix) {
-    // exclusive scan of per-thread count sums across the block
-    __shared__ long long wsum[kTPB / 32];
+    __shared__ long long wsum[kMaxTPB / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     long long v = acc.c;
 #pragma unroll
@@ -113,14 +139,14 @@ __device__ Partial reduce_partials(const Partial* part, int G, long long* prefix
     __syncthreads();
     long long base = 0;
     for (int w = 0; w < wid; ++w) base += wsum[w];
-    long long run = base + v - acc.c;  // exclusive prefix of this thread
+    long long run = base + v - acc.c;
     for (int j = beg; j < end; ++j) {
-      prefix[j] = run;
-      run += __ldcg(&part[j].c);
+      prefix[t0 + j] = run;
+      run += __ldcg(&part[t0 + j].c);
     }
     __syncthreads();
   }
-  return block_reduce_partial(acc);
+  return block_reduce_partial<STATS>(acc);
 }
 
 // Discrete weight and branch count of one walker (pyvibdmc.py:392-403).
@@ -142,31 +168,38 @@ __device__ __forceinline__ int branch_count(double v, double vref, double dt, do
   return c;
 }
 
-// Finalisation of a discrete branching pass (thread 0 of the last block).
-__device__ void finalize_discrete(const gbdmc_sim_t& S, gbdmc_ctrl_t* ctrl, const Partial& tot) {
+__device__ __forceinline__ int64_t hidx(const gbdmc_sim_t& S, int r, long long step) {
+  return (int64_t)r * S.hist.len + step;
+}
+
+// Finalisation of a discrete branching pass of replica r (thread 0).
+__device__ void finalize_discrete(const gbdmc_sim_t& S, const RepTable& T, int r, gbdmc_ctrl_t* ctrl,
+                                  const Partial& tot) {
   const long long n = ctrl->n;
   const long long step = ctrl->step;
   const long long nn = tot.c;
+  const long long n0 = T.n0[r];
   int st = ctrl->status | *(volatile int*)&ctrl->flags;
   ctrl->flags = 0;
   if (!st) {
-    const double n0 = (double)S.n0;
-    if ((double)nn < n0 - n0 * 0.5) st |= GBDMC_ST_POP_LOW;
-    if ((double)nn > n0 + n0 * 0.5) st |= GBDMC_ST_POP_HIGH;
-    if (nn > S.ld) st |= GBDMC_ST_OVERFLOW;
+    const double d0 = (double)n0;
+    if ((double)nn < d0 - d0 * 0.5) st |= GBDMC_ST_POP_LOW;
+    if ((double)nn > d0 + d0 * 0.5) st |= GBDMC_ST_POP_HIGH;
+    if (nn > T.cap[r]) st |= GBDMC_ST_OVERFLOW;
   }
   if (st) {
     ctrl->status = st;
     ctrl->err_step = (int)step;
   } else {
     const double vbar = tot.s0 / (double)nn;
-    const double corr = (double)(nn - S.n0) / (double)S.n0;
+    const double corr = (double)(nn - n0) / (double)n0;
     const double vref = vbar - S.alpha * corr;
     if (step < S.hist.len) {
-      if (S.hist.vref) S.hist.vref[step] = vref;
-      if (S.hist.pop) S.hist.pop[step] = (double)nn;
-      if (S.hist.births) S.hist.births[step] = (int)tot.births;
-      if (S.hist.deaths) S.hist.deaths[step] = (int)tot.deaths;
+      const int64_t h = hidx(S, r, step);
+      if (S.hist.vref) S.hist.vref[h] = vref;
+      if (S.hist.pop) S.hist.pop[h] = (double)nn;
+      if (S.hist.births) S.hist.births[h] = (int)tot.births;
+      if (S.hist.deaths) S.hist.deaths[h] = (int)tot.deaths;
     }
     ctrl->n_prev = n;
     ctrl->n = nn;
@@ -176,136 +209,171 @@ __device__ void finalize_discrete(const gbdmc_sim_t& S, gbdmc_ctrl_t* ctrl, cons
   ctrl->ticket = 0;
 }
 
-__device__ __forceinline__ void record_vstats(const gbdmc_sim_t& S, long long step, long long n, const Partial& t) {
-  if (step < S.hist.len) {
-    if (S.hist.vmin) S.hist.vmin[step] = t.vmin;
-    if (S.hist.vmax) S.hist.vmax[step] = t.vmax;
-    if (S.hist.vmean) S.hist.vmean[step] = t.s1 / (double)n;
+template <bool STATS>
+__device__ __forceinline__ void record_vstats(const gbdmc_sim_t& S, int r, long long step, long long n,
+                                              const Partial& t) {
+  if (STATS && step < S.hist.len) {
+    const int64_t h = hidx(S, r, step);
+    if (S.hist.vmin) S.hist.vmin[h] = t.vmin;
+    if (S.hist.vmax) S.hist.vmax[h] = t.vmax;
+    if (S.hist.vmean) S.hist.vmean[h] = t.s1 / (double)n;
   }
 }
 
-// ------------------------------------------------------------------ init
-// Step 0: V (+ local KE with a trial psi) and the first vref (pyvibdmc.py:760-769).
-template <int PK, int A, int TK>
-__global__ void __launch_bounds__(kTPB) k_init(const gbdmc_sim_t S, gbdmc_walkers_t W, gbdmc_ctrl_t* ctrl,
-                                                Partial* part) {
-  const long long n = ctrl->n;
-  const int64_t ld = S.ld;
-  const int64_t i = (int64_t)blockIdx.x * kTPB + threadIdx.x;
-  Partial p = partial_zero();
-  if (i < n) {
-    double x[3 * A], g[3 * A];
+template <int A>
+__device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&d2)[3 * A]) {
+  // -1/2 sum_d sum_a (1/m_a) d2psi/psi (imp_samp.py:49-53: atoms first, then dims)
+  double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + i];
-    double v = pes<PK, A, false>(x, S.pes, g);
-    if constexpr (TK != GBDMC_TRIAL_NONE) {
-      double d1[3 * A], d2[3 * A];
-      const double psi = trial<TK, A>(x, S.trial, d1, d2);
-      double ke = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    double t = 0.0;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        double s = 0.0;
-#pragma unroll
-        for (int a = 0; a < A; ++a) s = s + S.inv_mass[a] * d2[3 * a + d];
-        ke = ke + s;
-      }
-      ke = -0.5 * ke;
-#pragma unroll
-      for (int k = 0; k < 3 * A; ++k) W.f[k * ld + i] = d1[k];
-      W.psi[i] = psi;
-      W.ke[i] = ke;
-      v = v + ke;
-    }
-    W.v[i] = v;
-    if (S.weighting == GBDMC_CONTINUOUS) {
-      const double w = W.w[i];
-      p.s0 = v * w;
-      p.s1 = w;
-    } else {
-      p.s0 = v;
-      p.s1 = 1.0;
-    }
-    p.c = 1;
+    for (int a = 0; a < A; ++a) t = t + S.inv_mass[a] * d2[3 * a + d];
+    s = s + t;
   }
-  p = block_reduce_partial(p);
-  if (threadIdx.x == 0) part[blockIdx.x] = p;
-  if (last_block(ctrl)) {
-    const Partial t = reduce_partials(part, gridDim.x, nullptr);
-    if (threadIdx.x == 0) {
-      double vref;
-      if (S.weighting == GBDMC_CONTINUOUS)
-        vref = t.s0 / t.s1 - S.alpha * ((t.s1 - (double)S.n0) / (double)S.n0);
-      else
-        vref = t.s0 / (double)n - S.alpha * ((double)(n - S.n0) / (double)S.n0);
-      ctrl->vref = vref;
-      ctrl->ticket = 0;
+  return -0.5 * s;
+}
+
+// ------------------------------------------------------------------ init
+// Step 0 on compact walkers: V (+ local KE with a trial psi) and the first
+// vref (pyvibdmc.py:760-769).
+template <int PK, int A, int TK>
+__global__ void __launch_bounds__(kMaxTPB) k_init(const __grid_constant__ gbdmc_sim_t S,
+                                                   const __grid_constant__ RepTable T, gbdmc_walkers_t W,
+                                                   gbdmc_ctrl_t* ctrls, Partial* part) {
+  const int64_t ld = S.ld;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    const long long n = ctrl->n;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t slot = T.off[r] + i;
+    Partial p = partial_zero();
+    if (i < n) {
+      double x[3 * A], g[3 * A];
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + slot];
+      double v = pes<PK, A, false>(x, S.pes, g);
+      if constexpr (TK != GBDMC_TRIAL_NONE) {
+        double d1[3 * A], d2[3 * A];
+        const double psi = trial<TK, A>(x, S.trial, d1, d2);
+        const double ke = local_ke<A>(S, d2);
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) W.f[k * ld + slot] = d1[k];
+        W.psi[slot] = psi;
+        W.ke[slot] = ke;
+        v = v + ke;
+      }
+      W.v[slot] = v;
+      if (S.weighting == GBDMC_CONTINUOUS) {
+        const double w = W.w[slot];
+        p.s0 = v * w;
+        p.s1 = w;
+      } else {
+        p.s0 = v;
+        p.s1 = 1.0;
+      }
+      p.c = 1;
+    }
+    p = block_reduce_partial<true>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial t = reduce_partials<true>(part, T.tile_off[r], nt, nullptr);
+      if (threadIdx.x == 0) {
+        const double n0 = (double)T.n0[r];
+        double vref;
+        if (S.weighting == GBDMC_CONTINUOUS)
+          vref = t.s0 / t.s1 - S.alpha * ((t.s1 - n0) / n0);
+        else
+          vref = t.s0 / (double)n - S.alpha * ((double)(n - T.n0[r]) / n0);
+        ctrl->vref = vref;
+        ctrl->ticket = 0;
+      }
     }
   }
 }
 
 // --------------------------------------------------------- plain move
-// COUNT: fused discrete weights/counts (+ last-block scan); otherwise the
+// COUNT: fused discrete weights/counts (+ last-tile scan); otherwise the
 // move and potential only (continuous weighting).
-template <int PK, int A, int NM, bool COUNT>
-__global__ void __launch_bounds__(kTPB) k_move(const gbdmc_sim_t S, gbdmc_walkers_t W, gbdmc_ctrl_t* ctrl,
-                                                Partial* part, long long* prefix, int* counts,
-                                                const gbdmc_noise_t nz) {
-  if (*(volatile int*)&ctrl->status) return;
-  const long long n = ctrl->n;
-  const long long step = ctrl->step;
-  const double vref = ctrl->vref;
+template <int PK, int A, int NM, bool COUNT, bool STATS>
+__global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_sim_t S,
+                                                   const __grid_constant__ RepTable T, const gbdmc_walkers_t in,
+                                                   gbdmc_walkers_t out, gbdmc_ctrl_t* ctrls, Partial* part,
+                                                   long long* prefix, int* counts, const gbdmc_noise_t nz) {
   const int64_t ld = S.ld;
-  const int64_t i = (int64_t)blockIdx.x * kTPB + threadIdx.x;
-  Partial p = partial_zero();
-  int flag = 0;
-  if (i < n) {
-    double x[3 * A], z[3 * A], g[3 * A];
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;  // replica stopped by a previous kernel
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const double vref = ctrl->vref;
+    const int64_t base = T.off[r];
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    Partial p = partial_zero();
+    int flag = 0;
+    if (i < n) {
+      const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+      const int64_t dst = base + i;
+      double x[3 * A], z[3 * A], g[3 * A];
 #pragma unroll
-    for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + i];
-    Rng rng(S.seed, (uint64_t)step, (uint64_t)i);
-    if constexpr (NM == GBDMC_NOISE_INJECTED) {
+      for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
+      Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
 #pragma unroll
-      for (int k = 0; k < 3 * A; ++k) z[k] = nz.normal[k * nz.ld_noise + i];
-    } else {
-      gen_normals<NM, 3 * A>(rng, z);
-    }
-    // x + (0 + sigma*z): the reference adds the drawn displacement (pyvibdmc.py:544-547)
+        for (int k = 0; k < 3 * A; ++k) z[k] = nz.normal[k * nz.ld_noise + dst];
+      } else {
+        gen_normals<NM, 3 * A>(rng, z);
+      }
+      // x + (0 + sigma*z): the reference adds the drawn displacement (pyvibdmc.py:544-547)
 #pragma unroll
-    for (int k = 0; k < 3 * A; ++k) {
-      x[k] = __dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k]));
-      W.x[k * ld + i] = x[k];
+      for (int k = 0; k < 3 * A; ++k) {
+        x[k] = __dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k]));
+        out.x[k * ld + dst] = x[k];
+      }
+      if (out.who) out.who[dst] = in.who[src];
+      const double v = pes<PK, A, false>(x, S.pes, g);
+      out.v[dst] = v;
+      if (STATS) {
+        p.s1 = v;
+        p.vmin = v;
+        p.vmax = v;
+      }
+      if constexpr (COUNT) {
+        double u;
+        if constexpr (NM == GBDMC_NOISE_INJECTED)
+          u = nz.u_branch[dst];
+        else
+          u = rng.uniform53();
+        const double n0 = (double)T.n0[r];
+        const double w_hi = (n0 + n0 * 0.5) + 1.0;
+        const int c = branch_count(v, vref, S.dt, u, w_hi, flag, p.births, p.deaths);
+        counts[dst] = c;
+        p.c = c;
+        p.s0 = c == 1 ? v : (double)c * v;
+      } else if (S.weighting == GBDMC_CONTINUOUS) {
+        out.w[dst] = in.w[src];
+      }
     }
-    const double v = pes<PK, A, false>(x, S.pes, g);
-    W.v[i] = v;
-    p.s1 = v;
-    p.vmin = v;
-    p.vmax = v;
-    if constexpr (COUNT) {
-      double u;
-      if constexpr (NM == GBDMC_NOISE_INJECTED)
-        u = nz.u_branch[i];
-      else
-        u = rng.uniform53();
-      const double w_hi = ((double)S.n0 + (double)S.n0 * 0.5) + 1.0;
-      const int c = branch_count(v, vref, S.dt, u, w_hi, flag, p.births, p.deaths);
-      counts[i] = c;
-      p.c = c;
-      p.s0 = (double)c * v;
+    if (COUNT && __syncthreads_or(flag)) {
+      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
     }
-  }
-  if (COUNT && __syncthreads_or(flag)) {
-    if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-  }
-  p = block_reduce_partial(p);
-  if (threadIdx.x == 0) part[blockIdx.x] = p;
-  if (last_block(ctrl)) {
-    const Partial t = reduce_partials(part, gridDim.x, COUNT ? prefix : nullptr);
-    if (threadIdx.x == 0) {
-      record_vstats(S, step, n, t);
-      if constexpr (COUNT)
-        finalize_discrete(S, ctrl, t);
-      else
-        ctrl->ticket = 0;
+    p = block_reduce_partial<STATS>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial t = reduce_partials<STATS>(part, T.tile_off[r], nt, COUNT ? prefix : nullptr);
+      if (threadIdx.x == 0) {
+        record_vstats<STATS>(S, r, step, n, t);
+        if constexpr (COUNT)
+          finalize_discrete(S, T, r, ctrl, t);
+        else
+          ctrl->ticket = 0;
+      }
     }
   }
 }
@@ -315,202 +383,235 @@ __global__ void __launch_bounds__(kTPB) k_move(const gbdmc_sim_t S, gbdmc_walker
 // local_kin (imp_samp.py:49-53).  The Green's-function ratio prod_k
 // exp(-a_k^2/2s^2)/exp(-b_k^2/2s^2) is evaluated as one exp of the summed
 // exponents.
-template <int PK, int A, int TK, int NM>
-__global__ void __launch_bounds__(kTPB) k_is_move(const gbdmc_sim_t S, gbdmc_walkers_t W, gbdmc_ctrl_t* ctrl,
-                                                   Partial* part, const gbdmc_noise_t nz) {
-  if (*(volatile int*)&ctrl->status) return;
-  const long long n = ctrl->n;
-  const long long step = ctrl->step;
+template <int PK, int A, int TK, int NM, bool STATS>
+__global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbdmc_sim_t S,
+                                                      const __grid_constant__ RepTable T, const gbdmc_walkers_t in,
+                                                      gbdmc_walkers_t out, gbdmc_ctrl_t* ctrls, Partial* part,
+                                                      const gbdmc_noise_t nz) {
   const int64_t ld = S.ld;
   const double dt = S.dt;
-  const int64_t i = (int64_t)blockIdx.x * kTPB + threadIdx.x;
-  Partial p = partial_zero();
-  if (i < n) {
-    double x[3 * A], y[3 * A], fx[3 * A], fy[3 * A], sdy[3 * A], g[3 * A];
-#pragma unroll
-    for (int k = 0; k < 3 * A; ++k) {
-      x[k] = W.x[k * ld + i];
-      fx[k] = W.f[k * ld + i];
-    }
-    const double psi_x = W.psi[i];
-    Rng rng(S.seed, (uint64_t)step, (uint64_t)i);
-    double z[3 * A];
-    if constexpr (NM == GBDMC_NOISE_INJECTED) {
-#pragma unroll
-      for (int k = 0; k < 3 * A; ++k) z[k] = nz.normal[k * nz.ld_noise + i];
-    } else {
-      gen_normals<NM, 3 * A>(rng, z);
-    }
-    // y = (x + disp) + (f_x/m) dt   (pyvibdmc.py:556-576)
-#pragma unroll
-    for (int k = 0; k < 3 * A; ++k) {
-      const double dx = __dmul_rn(S.inv_mass[k / 3], fx[k]);
-      y[k] = __dadd_rn(__dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k])), __dmul_rn(dx, dt));
-    }
-    const double psi_y = trial<TK, A>(y, S.trial, fy, sdy);
-    // Metropolis ratio
-    double expo = 0.0;
-#pragma unroll
-    for (int k = 0; k < 3 * A; ++k) {
-      const double im = S.inv_mass[k / 3];
-      const double s2 = S.sigma[k / 3] * S.sigma[k / 3];
-      const double a = x[k] - y[k] - im * fy[k] * dt;
-      const double b = y[k] - x[k] - im * fx[k] * dt;
-      expo += (b * b - a * a) / (2.0 * s2);
-    }
-    const double r = psi_y / psi_x;
-    double met = exp(expo) * (r * r);
-    if (psi_x * psi_y <= 0.0) met = 0.0;
-    double u;
-    if constexpr (NM == GBDMC_NOISE_INJECTED)
-      u = nz.u_accept[i];
-    else
-      u = rng.uniform53();
-    const bool acc = met > u;
-    double ke;
-    if (acc) {
-      double s = 0.0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        double t = 0.0;
-#pragma unroll
-        for (int a = 0; a < A; ++a) t = t + S.inv_mass[a] * sdy[3 * a + d];
-        s = s + t;
-      }
-      ke = -0.5 * s;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const int64_t base = T.off[r];
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    Partial p = partial_zero();
+    if (i < n) {
+      const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+      const int64_t dst = base + i;
+      double x[3 * A], y[3 * A], fx[3 * A], fy[3 * A], sdy[3 * A], g[3 * A];
 #pragma unroll
       for (int k = 0; k < 3 * A; ++k) {
-        x[k] = y[k];
-        W.x[k * ld + i] = y[k];
-        W.f[k * ld + i] = fy[k];
+        x[k] = in.x[k * ld + src];
+        fx[k] = in.f[k * ld + src];
       }
-      W.psi[i] = psi_y;
-      W.ke[i] = ke;
-    } else {
-      ke = W.ke[i];
+      const double psi_x = in.psi[src];
+      Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+      double z[3 * A];
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) z[k] = nz.normal[k * nz.ld_noise + dst];
+      } else {
+        gen_normals<NM, 3 * A>(rng, z);
+      }
+      // y = (x + disp) + (f_x/m) dt   (pyvibdmc.py:556-576)
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) {
+        const double dx = __dmul_rn(S.inv_mass[k / 3], fx[k]);
+        y[k] = __dadd_rn(__dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k])), __dmul_rn(dx, dt));
+      }
+      const double psi_y = trial<TK, A>(y, S.trial, fy, sdy);
+      double expo = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) {
+        const double im = S.inv_mass[k / 3];
+        const double s2 = S.sigma[k / 3] * S.sigma[k / 3];
+        const double a = x[k] - y[k] - im * fy[k] * dt;
+        const double b = y[k] - x[k] - im * fx[k] * dt;
+        expo += (b * b - a * a) / (2.0 * s2);
+      }
+      const double rr = psi_y / psi_x;
+      double met = exp(expo) * (rr * rr);
+      if (psi_x * psi_y <= 0.0) met = 0.0;
+      double u;
+      if constexpr (NM == GBDMC_NOISE_INJECTED)
+        u = nz.u_accept[dst];
+      else
+        u = rng.uniform53();
+      const bool acc = met > u;
+      double ke, psi;
+      if (acc) {
+        ke = local_ke<A>(S, sdy);
+        psi = psi_y;
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) {
+          x[k] = y[k];
+          fx[k] = fy[k];
+        }
+      } else {
+        ke = in.ke[src];
+        psi = psi_x;
+      }
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) {
+        out.x[k * ld + dst] = x[k];
+        out.f[k * ld + dst] = fx[k];
+      }
+      out.psi[dst] = psi;
+      out.ke[dst] = ke;
+      if (out.who) out.who[dst] = in.who[src];
+      if (S.weighting == GBDMC_CONTINUOUS) out.w[dst] = in.w[src];
+      const double v = pes<PK, A, false>(x, S.pes, g);
+      out.v[dst] = v + ke;
+      p.aux = acc ? 1 : 0;
+      if (STATS) {
+        p.s1 = v;
+        p.vmin = v;
+        p.vmax = v;
+      }
     }
-    const double v = pes<PK, A, false>(x, S.pes, g);
-    W.v[i] = v + ke;
-    p.aux = acc ? 1 : 0;
-    p.s1 = v;
-    p.vmin = v;
-    p.vmax = v;
-  }
-  p = block_reduce_partial(p);
-  if (threadIdx.x == 0) part[blockIdx.x] = p;
-  if (last_block(ctrl)) {
-    const Partial t = reduce_partials(part, gridDim.x, nullptr);
-    if (threadIdx.x == 0) {
-      record_vstats(S, step, n, t);
-      // dt_factor = accepted / N (pyvibdmc.py:603); effective time (:372-378)
-      const double dte = S.dt * ((double)t.aux / (double)n);
-      ctrl->dt_eff = dte;
-      ctrl->n_acc = t.aux;
-      ctrl->eff_ts = (step == 0) ? dte : ctrl->eff_ts + dte;
-      if (step < S.hist.len) {
-        if (S.hist.rejected) S.hist.rejected[step] = (int)(n - t.aux);
-        if (S.hist.eff_ts) S.hist.eff_ts[step] = ctrl->eff_ts;
+    p = block_reduce_partial<STATS>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial t = reduce_partials<STATS>(part, T.tile_off[r], nt, nullptr);
+      if (threadIdx.x == 0) {
+        record_vstats<STATS>(S, r, step, n, t);
+        // dt_factor = accepted / N (pyvibdmc.py:603); effective time (:372-378)
+        const double dte = S.dt * ((double)t.aux / (double)n);
+        ctrl->dt_eff = dte;
+        ctrl->n_acc = t.aux;
+        ctrl->eff_ts = (step == 0) ? dte : ctrl->eff_ts + dte;
+        if (step < S.hist.len) {
+          const int64_t h = hidx(S, r, step);
+          if (S.hist.rejected) S.hist.rejected[h] = (int)(n - t.aux);
+          if (S.hist.eff_ts) S.hist.eff_ts[h] = ctrl->eff_ts;
+        }
+        ctrl->ticket = 0;
       }
-      ctrl->ticket = 0;
     }
   }
 }
 
 // Discrete weights and counts from stored energies with dt_eff (importance sampling).
 template <int NM>
-__global__ void __launch_bounds__(kTPB) k_count(const gbdmc_sim_t S, gbdmc_walkers_t W, gbdmc_ctrl_t* ctrl,
-                                                 Partial* part, long long* prefix, int* counts,
-                                                 const gbdmc_noise_t nz) {
-  if (*(volatile int*)&ctrl->status) return;
-  const long long n = ctrl->n;
-  const long long step = ctrl->step;
-  const double vref = ctrl->vref;
-  const double dt = ctrl->dt_eff;
-  const int64_t i = (int64_t)blockIdx.x * kTPB + threadIdx.x;
-  Partial p = partial_zero();
-  int flag = 0;
-  if (i < n) {
-    const double v = W.v[i];
-    double u;
-    if constexpr (NM == GBDMC_NOISE_INJECTED) {
-      u = nz.u_branch[i];
-    } else {
-      Rng rng(S.seed, (uint64_t)step, (uint64_t)i);
-      rng.slot = 64;  // stream disjoint from the move's draws
-      u = rng.uniform53();
+__global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
+                                                    const __grid_constant__ RepTable T, gbdmc_walkers_t out,
+                                                    gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
+                                                    int* counts, const gbdmc_noise_t nz) {
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const double vref = ctrl->vref;
+    const double dt = ctrl->dt_eff;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t dst = T.off[r] + i;
+    Partial p = partial_zero();
+    int flag = 0;
+    if (i < n) {
+      const double v = out.v[dst];
+      double u;
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
+        u = nz.u_branch[dst];
+      } else {
+        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+        rng.slot = 64;  // stream disjoint from the move's draws
+        u = rng.uniform53();
+      }
+      const double n0 = (double)T.n0[r];
+      const double w_hi = (n0 + n0 * 0.5) + 1.0;
+      const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
+      counts[dst] = c;
+      p.c = c;
+      p.s0 = c == 1 ? v : (double)c * v;
     }
-    const double w_hi = ((double)S.n0 + (double)S.n0 * 0.5) + 1.0;
-    const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
-    counts[i] = c;
-    p.c = c;
-    p.s0 = (double)c * v;
-  }
-  if (__syncthreads_or(flag)) {
-    if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-  }
-  p = block_reduce_partial(p);
-  if (threadIdx.x == 0) part[blockIdx.x] = p;
-  if (last_block(ctrl)) {
-    const Partial t = reduce_partials(part, gridDim.x, prefix);
-    if (threadIdx.x == 0) finalize_discrete(S, ctrl, t);
+    if (__syncthreads_or(flag)) {
+      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
+    }
+    p = block_reduce_partial<false>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
+      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, t);
+    }
   }
 }
 
-// ---------------------------------------------------------------- scatter
-// Walker i writes its counts[i] copies to dst at prefix[block] + (exclusive
-// scan of counts inside the block): the order of np.repeat(arange(N), counts).
-template <int A, bool IS, bool WHO>
-__global__ void __launch_bounds__(kTPB) k_scatter(const gbdmc_sim_t S, const gbdmc_walkers_t src,
-                                                   gbdmc_walkers_t dst, const gbdmc_ctrl_t* ctrl,
-                                                   const long long* prefix, const int* counts) {
-  if (*(volatile const int*)&ctrl->status) return;
-  const long long n = ctrl->n_prev;
+// ----------------------------------------------------------- branching
+// Walker j (pre-branch order) writes j into idx[prefix[tile] + scan .. + c):
+// the np.repeat(arange(N), counts) order of pyvibdmc.py:417-430.
+__global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepTable T, int32_t* __restrict__ idx,
+                                                     const gbdmc_ctrl_t* ctrls, const long long* prefix,
+                                                     const int* counts) {
+  const int ntile = T.tile_off[T.nrep];
+  __shared__ int wsum[kMaxTPB / 32];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    const gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile const int*)&ctrl->status) continue;
+    const long long n = ctrl->n_prev;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t base = T.off[r];
+    const int c = i < n ? counts[base + i] : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int inc = warp_incl_scan(c);
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    int off = 0;
+    for (int w = 0; w < wid; ++w) off += wsum[w];
+    __syncthreads();
+    const long long dest = prefix[tile] + off + inc - c;
+    const long long cap = T.cap[r];
+    for (int q = 0; q < c; ++q)
+      if (dest + q < cap) idx[base + dest + q] = (int32_t)i;
+  }
+}
+
+// ---------------------------------------------------------- compaction
+template <int A, bool IS>
+__global__ void __launch_bounds__(kMaxTPB) k_compact(const __grid_constant__ gbdmc_sim_t S,
+                                                      const __grid_constant__ RepTable T, const gbdmc_walkers_t in,
+                                                      gbdmc_walkers_t out, const gbdmc_ctrl_t* ctrls) {
   const int64_t ld = S.ld;
-  const int64_t i = (int64_t)blockIdx.x * kTPB + threadIdx.x;
-  const int c = i < n ? counts[i] : 0;
-  // block exclusive scan of c
-  __shared__ int wsum[kTPB / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int inc = warp_incl_scan(c);
-  if (lane == 31) wsum[wid] = inc;
-  __syncthreads();
-  int base = 0;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    const long long n = ctrls[r].n;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    if (i >= n) continue;
+    const int64_t base = T.off[r];
+    const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+    const int64_t dst = base + i;
 #pragma unroll
-  for (int w = 0; w < kTPB / 32; ++w) base += (w < wid) ? wsum[w] : 0;
-  const long long dest = prefix[blockIdx.x] + base + inc - c;
-  if (c == 0) return;
-  const long long lim = dest + c <= ld ? c : (ld - dest > 0 ? ld - dest : 0);
+    for (int k = 0; k < 3 * A; ++k) out.x[k * ld + dst] = in.x[k * ld + src];
+    out.v[dst] = in.v[src];
+    if (in.who && out.who) out.who[dst] = in.who[src];
+    if (in.w && out.w) out.w[dst] = in.w[src];
+    if constexpr (IS) {
 #pragma unroll
-  for (int k = 0; k < 3 * A; ++k) {
-    const double xv = src.x[k * ld + i];
-    for (long long r = 0; r < lim; ++r) dst.x[k * ld + dest + r] = xv;
-  }
-  const double v = src.v[i];
-  for (long long r = 0; r < lim; ++r) dst.v[dest + r] = v;
-  if constexpr (WHO) {
-    const int wh = src.who[i];
-    for (long long r = 0; r < lim; ++r) dst.who[dest + r] = wh;
-  }
-  if constexpr (IS) {
-#pragma unroll
-    for (int k = 0; k < 3 * A; ++k) {
-      const double fv = src.f[k * ld + i];
-      for (long long r = 0; r < lim; ++r) dst.f[k * ld + dest + r] = fv;
-    }
-    const double ps = src.psi[i], ke = src.ke[i];
-    for (long long r = 0; r < lim; ++r) {
-      dst.psi[dest + r] = ps;
-      dst.ke[dest + r] = ke;
+      for (int k = 0; k < 3 * A; ++k) out.f[k * ld + dst] = in.f[k * ld + src];
+      out.psi[dst] = in.psi[src];
+      out.ke[dst] = in.ke[src];
     }
   }
 }
 
 // ---------------------------------------------------- continuous weights
-// One CTA of 1024 threads: w *= exp(-(V-vref) dt); clone the current argmax
-// into every walker below the lower threshold, in index order, halving the
-// argmax each time (pyvibdmc.py:340-356, :432-438); the optional upper
-// threshold branches the k smallest weights (k = #w > upper) in ascending
-// index order; then vref from the weighted mean (:659-661).
+// One CTA of 1024 threads per replica: w *= exp(-(V-vref) dt); clone the
+// current argmax into every walker below the lower threshold, in index order,
+// halving the argmax each time (pyvibdmc.py:340-356, :432-438); the optional
+// upper threshold branches the k smallest weights (k = #w > upper) in
+// ascending index order; then vref from the weighted mean (:659-661).
+// Works in place on compact walkers.
 constexpr int kCTA = 1024;
 
 struct ArgBest {
@@ -518,7 +619,6 @@ struct ArgBest {
   long long i;
 };
 
-// first index of the maximum (MAX) or minimum (!MAX) over w[0..n), skipping flagged entries
 template <bool MAX>
 __device__ long long block_arg(const double* w, long long n, const unsigned char* skip) {
   __shared__ ArgBest sh[kCTA / 32];
@@ -559,39 +659,39 @@ __device__ long long block_arg(const double* w, long long n, const unsigned char
     if (lane == 0) sh[0] = b;
   }
   __syncthreads();
-  const long long r = sh[0].i;
+  const long long res = sh[0].i;
   __syncthreads();
-  return r;
+  return res;
 }
 
-template <int A, bool IS, bool WHO>
-__device__ void clone_walker(const gbdmc_sim_t& S, gbdmc_walkers_t& W, long long from, long long to) {
+template <int A, bool IS>
+__device__ void clone_walker(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t base, long long from, long long to) {
   const int64_t ld = S.ld;
   const int t = threadIdx.x;
+  const int64_t f = base + from, d = base + to;
   if (t < 3 * A) {
-    W.x[t * ld + to] = W.x[t * ld + from];
-    if constexpr (IS) W.f[t * ld + to] = W.f[t * ld + from];
+    W.x[t * ld + d] = W.x[t * ld + f];
+    if constexpr (IS) W.f[t * ld + d] = W.f[t * ld + f];
   } else if (t == 3 * A) {
-    W.v[to] = W.v[from];
+    W.v[d] = W.v[f];
   } else if (t == 3 * A + 1) {
-    if constexpr (WHO) W.who[to] = W.who[from];
+    if (W.who) W.who[d] = W.who[f];
   } else if (t == 3 * A + 2) {
     if constexpr (IS) {
-      W.psi[to] = W.psi[from];
-      W.ke[to] = W.ke[from];
+      W.psi[d] = W.psi[f];
+      W.ke[d] = W.ke[f];
     }
   }
 }
 
-// ordered list of indices with flag set: list[0..k), returns k
-__device__ long long block_compact(const unsigned char* flag, long long n, int* list) {
+__device__ long long block_compact_flags(const unsigned char* flag, long long n, int* list) {
   __shared__ int wsum[kCTA / 32];
   __shared__ long long total;
   if (threadIdx.x == 0) total = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (long long base = 0; base < n; base += kCTA) {
-    const long long i = base + threadIdx.x;
+  for (long long b = 0; b < n; b += kCTA) {
+    const long long i = b + threadIdx.x;
     const int f = (i < n && flag[i]) ? 1 : 0;
     const int inc = warp_incl_scan(f);
     if (lane == 31) wsum[wid] = inc;
@@ -606,21 +706,29 @@ __device__ long long block_compact(const unsigned char* flag, long long n, int* 
   return total;
 }
 
-template <int A, bool IS, bool WHO>
-__global__ void __launch_bounds__(kCTA) k_cont_branch(const gbdmc_sim_t S, gbdmc_walkers_t W, gbdmc_ctrl_t* ctrl,
-                                                       int* list, unsigned char* flags) {
+template <int A, bool IS>
+__global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gbdmc_sim_t S,
+                                                       const __grid_constant__ RepTable T, gbdmc_walkers_t W,
+                                                       gbdmc_ctrl_t* ctrls, int* list_all, unsigned char* flags_all) {
+  const int r = blockIdx.x;
+  gbdmc_ctrl_t* ctrl = ctrls + r;
   if (*(volatile int*)&ctrl->status) return;
+  const int64_t base = T.off[r];
   const long long n = ctrl->n;
   const long long step = ctrl->step;
   const double vref = ctrl->vref;
   const double dt = IS ? ctrl->dt_eff : S.dt;
+  double* w = W.w + base;
+  const double* v = W.v + base;
+  int* list = list_all + base;
+  unsigned char* flags = flags_all + base;
   __shared__ long long s_nb;
   int bad = 0;
   for (long long i = threadIdx.x; i < n; i += kCTA) {
-    const double w = W.w[i] * exp(__dmul_rn(-__dsub_rn(W.v[i], vref), dt));
-    W.w[i] = w;
-    if (!isfinite(w)) bad = 1;
-    flags[i] = (w < S.thresh_lower) ? 1 : 0;
+    const double wi = w[i] * exp(__dmul_rn(-__dsub_rn(v[i], vref), dt));
+    w[i] = wi;
+    if (!isfinite(wi)) bad = 1;
+    flags[i] = (wi < S.thresh_lower) ? 1 : 0;
   }
   if (__syncthreads_or(bad)) {
     if (threadIdx.x == 0) {
@@ -629,17 +737,17 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const gbdmc_sim_t S, gbdmc
     }
     return;
   }
-  long long nk = block_compact(flags, n, list);
+  const long long nk = block_compact_flags(flags, n, list);
   long long nb = nk;
   for (long long j = 0; j < nk; ++j) {
     const long long to = list[j];
-    const long long m = block_arg<true>(W.w, n, nullptr);
-    clone_walker<A, IS, WHO>(S, W, m, to);
+    const long long m = block_arg<true>(w, n, nullptr);
+    clone_walker<A, IS>(S, W, base, m, to);
     __syncthreads();
     if (threadIdx.x == 0) {
-      const double h = W.w[m] / 2.0;
-      W.w[m] = h;
-      W.w[to] = h;
+      const double h = w[m] / 2.0;
+      w[m] = h;
+      w[to] = h;
     }
     __syncthreads();
   }
@@ -648,42 +756,40 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const gbdmc_sim_t S, gbdmc
     __syncthreads();
     long long cnt = 0;
     for (long long i = threadIdx.x; i < n; i += kCTA) {
-      cnt += W.w[i] > S.thresh_upper ? 1 : 0;
+      cnt += w[i] > S.thresh_upper ? 1 : 0;
       flags[i] = 0;
     }
     cnt = warp_sum(cnt);
     if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long*)&s_nb, (unsigned long long)cnt);
     __syncthreads();
     const long long nup = s_nb;
-    // mark the nup smallest weights (ties: lowest index first)
     for (long long j = 0; j < nup; ++j) {
-      const long long m = block_arg<false>(W.w, n, flags);
-      if (threadIdx.x == 0) flags[m] = 1;
+      const long long m = block_arg<false>(w, n, flags);
+      if (threadIdx.x == 0 && m >= 0) flags[m] = 1;
       __syncthreads();
     }
-    const long long nk2 = block_compact(flags, n, list);
+    const long long nk2 = block_compact_flags(flags, n, list);
     for (long long j = 0; j < nk2; ++j) {
       const long long to = list[j];
-      const long long m = block_arg<true>(W.w, n, nullptr);
-      clone_walker<A, IS, WHO>(S, W, m, to);
+      const long long m = block_arg<true>(w, n, nullptr);
+      clone_walker<A, IS>(S, W, base, m, to);
       __syncthreads();
       if (threadIdx.x == 0) {
-        const double h = W.w[m] / 2.0;
-        W.w[m] = h;
-        W.w[to] = h;
+        const double h = w[m] / 2.0;
+        w[m] = h;
+        w[to] = h;
       }
       __syncthreads();
     }
     nb += nk2;
   }
-  // weighted vref and statistics (fixed-order reduction)
   double swv = 0.0, sw = 0.0, wmx = -CUDART_INF, wmn = CUDART_INF;
   for (long long i = threadIdx.x; i < n; i += kCTA) {
-    const double w = W.w[i];
-    swv += W.v[i] * w;
-    sw += w;
-    wmx = fmax(wmx, w);
-    wmn = fmin(wmn, w);
+    const double wi = w[i];
+    swv += v[i] * wi;
+    sw += wi;
+    wmx = fmax(wmx, wi);
+    wmn = fmin(wmn, wi);
   }
   __shared__ double r4[4][kCTA / 32];
   swv = warp_sum(swv);
@@ -704,16 +810,17 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const gbdmc_sim_t S, gbdmc
     wmx = warp_max(r4[2][lane]);
     wmn = warp_min(r4[3][lane]);
     if (lane == 0) {
-      const double vr = swv / sw - S.alpha * ((sw - (double)S.n0) / (double)S.n0);
+      const double n0 = (double)T.n0[r];
+      const double vr = swv / sw - S.alpha * ((sw - n0) / n0);
       if (step < S.hist.len) {
-        if (S.hist.vref) S.hist.vref[step] = vr;
-        if (S.hist.pop) S.hist.pop[step] = sw;
-        if (S.hist.births) S.hist.births[step] = (int)nb;
+        const int64_t h = hidx(S, r, step);
+        if (S.hist.vref) S.hist.vref[h] = vr;
+        if (S.hist.pop) S.hist.pop[h] = sw;
+        if (S.hist.births) S.hist.births[h] = (int)nb;
       }
       ctrl->vref = vr;
       ctrl->n_prev = n;
       ctrl->step = step + 1;
-      // logging extras: max / min weight after branching
       ctrl->reserved[0] = __double_as_longlong(wmx);
       ctrl->reserved[1] = __double_as_longlong(wmn);
     }
@@ -735,77 +842,169 @@ __global__ void k_iota(int32_t* who, const int64_t* n_dev) {
     who[i] = (int32_t)i;
 }
 
-// ------------------------------------------------------------ dispatch
+// ============================================================ host side
+int num_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+  if (dev < 64 && cached[dev]) return cached[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  if (dev < 64) cached[dev] = n;
+  return n;
+}
+
+// Tile width: spread sum(n0) over all SMs in one wave (multiple of 32, 64..256).
+static int pick_tpb(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep) {
+  if (S.block_threads) return S.block_threads;
+  int64_t tot = 0;
+  for (int r = 0; r < nrep; ++r) tot += reps[r].n0;
+  const int64_t per_sm = (tot * 103 / 100 + num_sms() - 1) / num_sms();
+  int t = (int)((per_sm + 31) / 32 * 32);
+  return t < 64 ? 64 : (t > kMaxTPB ? kMaxTPB : t);
+}
+
+static int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, RepTable& T, const char* what) {
+  memset(&T, 0, sizeof(T));
+  if (nrep < 1 || nrep > GBDMC_MAX_REPLICAS) {
+    set_error("%s: nrep must be 1..%d (got %d)", what, GBDMC_MAX_REPLICAS, nrep);
+    return GBDMC_ERR_CAPACITY;
+  }
+  const int tpb = pick_tpb(S, reps, nrep);
+  if (tpb < kMinTPB || tpb > kMaxTPB || tpb % 32) {
+    set_error("%s: block_threads must be a multiple of 32 in [32, 256] (got %d)", what, tpb);
+    return GBDMC_ERR_ARG;
+  }
+  T.nrep = nrep;
+  T.tpb = tpb;
+  int64_t tiles = 0;
+  for (int r = 0; r < nrep; ++r) {
+    const gbdmc_replica_t& R = reps[r];
+    if (R.off < 0 || R.cap < 1 || R.off + R.cap > S.ld || R.n0 < 1) {
+      set_error("%s: replica %d has bad off/cap/n0 (%lld/%lld/%lld, ld %lld)", what, r, (long long)R.off,
+                (long long)R.cap, (long long)R.n0, (long long)S.ld);
+      return GBDMC_ERR_ARG;
+    }
+    T.tile_off[r] = (int32_t)tiles;
+    T.off[r] = R.off;
+    T.cap[r] = R.cap;
+    T.n0[r] = R.n0;
+    T.stream[r] = R.stream;
+    tiles += (R.cap + tpb - 1) / tpb;
+    if (tiles > INT32_MAX / 2) {
+      set_error("%s: too many tiles", what);
+      return GBDMC_ERR_CAPACITY;
+    }
+  }
+  T.tile_off[nrep] = (int32_t)tiles;
+  return GBDMC_OK;
+}
+
+static int grid_for(const RepTable& T) {
+  const int tiles = T.tile_off[T.nrep];
+  const int resident = num_sms() * (2048 / T.tpb);
+  return tiles < resident ? tiles : resident;
+}
+
 template <int PK, int A, int TK>
-static int run_init(const gbdmc_sim_t& S, const gbdmc_walkers_t& W, gbdmc_ctrl_t* ctrl, const ScratchLayout& L,
-                    cudaStream_t s) {
-  k_init<PK, A, TK><<<grid_for(S.ld), kTPB, 0, s>>>(S, W, ctrl, L.part);
-  return check_launch("gbdmc_sim_init");
+static int run_init(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& W, gbdmc_ctrl_t* ctrl,
+                    const ScratchLayout& L, cudaStream_t s) {
+  k_init<PK, A, TK><<<grid_for(T), T.tpb, 0, s>>>(S, T, W, ctrl, L.part);
+  return check_launch("gbdmc init");
 }
 
-template <int A, bool IS>
-static void launch_scatter(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const gbdmc_walkers_t& dst,
-                           gbdmc_ctrl_t* ctrl, const ScratchLayout& L, cudaStream_t s) {
-  const int G = grid_for(S.ld);
-  if (S.track_who)
-    k_scatter<A, IS, true><<<G, kTPB, 0, s>>>(S, src, dst, ctrl, L.prefix, L.counts);
-  else
-    k_scatter<A, IS, false><<<G, kTPB, 0, s>>>(S, src, dst, ctrl, L.prefix, L.counts);
-}
-
-template <int A, bool IS>
-static void launch_cont(const gbdmc_sim_t& S, const gbdmc_walkers_t& W, gbdmc_ctrl_t* ctrl, const ScratchLayout& L,
-                        cudaStream_t s) {
-  if (S.track_who)
-    k_cont_branch<A, IS, true><<<1, kCTA, 0, s>>>(S, W, ctrl, L.list, L.flags);
-  else
-    k_cont_branch<A, IS, false><<<1, kCTA, 0, s>>>(S, W, ctrl, L.list, L.flags);
-}
-
-template <int PK, int A, int TK, int NM>
-static int run_step(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const gbdmc_walkers_t& dst, gbdmc_ctrl_t* ctrl,
-                    const ScratchLayout& L, const gbdmc_noise_t& nz, cudaStream_t s) {
-  const int G = grid_for(S.ld);
+template <int PK, int A, int TK, int NM, bool STATS>
+static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& src,
+                        const gbdmc_walkers_t& dst, gbdmc_ctrl_t* ctrl, const ScratchLayout& L,
+                        const gbdmc_noise_t& nz, cudaStream_t s) {
+  const int G = grid_for(T);
   constexpr bool IS = TK != GBDMC_TRIAL_NONE;
+  const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
+  cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
+  if (prof) cudaEventRecord(ev[0], s);
   if constexpr (!IS) {
     if (S.weighting == GBDMC_DISCRETE) {
-      const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
-      cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
-      if (prof) cudaEventRecord(ev[0], s);
-      k_move<PK, A, NM, true><<<G, kTPB, 0, s>>>(S, src, ctrl, L.part, L.prefix, L.counts, nz);
+      k_move<PK, A, NM, true, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      launch_scatter<A, false>(S, src, dst, ctrl, L, s);
-      if (prof) {
-        cudaEventRecord(ev[2], s);
-        ++g_prof.count;
-      }
+      k_branch<<<G, T.tpb, 0, s>>>(T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
-      k_move<PK, A, NM, false><<<G, kTPB, 0, s>>>(S, src, ctrl, L.part, L.prefix, L.counts, nz);
-      launch_cont<A, false>(S, src, ctrl, L, s);
+      k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
+      if (prof) cudaEventRecord(ev[1], s);
+      k_cont_branch<A, false><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
     }
   } else {
-    k_is_move<PK, A, TK, NM><<<G, kTPB, 0, s>>>(S, src, ctrl, L.part, nz);
+    k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
+    if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
-      k_count<NM><<<G, kTPB, 0, s>>>(S, src, ctrl, L.part, L.prefix, L.counts, nz);
-      launch_scatter<A, true>(S, src, dst, ctrl, L, s);
+      k_count<NM><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
+      k_branch<<<G, T.tpb, 0, s>>>(T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
-      launch_cont<A, true>(S, src, ctrl, L, s);
+      k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
     }
   }
-  return check_launch("gbdmc_sim_step");
+  if (prof) {
+    cudaEventRecord(ev[2], s);
+    ++g_prof.count;
+  }
 }
 
 template <int PK, int A, int TK>
-static int step_noise(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const gbdmc_walkers_t& dst,
-                      gbdmc_ctrl_t* ctrl, const ScratchLayout& L, const gbdmc_noise_t& nz, cudaStream_t s) {
-  switch (S.noise_mode) {
-    case GBDMC_NOISE_PHILOX32: return run_step<PK, A, TK, GBDMC_NOISE_PHILOX32>(S, src, dst, ctrl, L, nz, s);
-    case GBDMC_NOISE_PHILOX64: return run_step<PK, A, TK, GBDMC_NOISE_PHILOX64>(S, src, dst, ctrl, L, nz, s);
-    case GBDMC_NOISE_INJECTED: return run_step<PK, A, TK, GBDMC_NOISE_INJECTED>(S, src, dst, ctrl, L, nz, s);
+static int run_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& src, const gbdmc_walkers_t& dst,
+                    gbdmc_ctrl_t* ctrl, const ScratchLayout& L, const gbdmc_noise_t& nz, cudaStream_t s) {
+  const bool stats = S.hist.vmin || S.hist.vmax || S.hist.vmean;
+#define GBDMC_NM(nm)                                                     \
+  if (S.noise_mode == nm) {                                              \
+    if (stats)                                                           \
+      launch_step<PK, A, TK, nm, true>(S, T, src, dst, ctrl, L, nz, s);  \
+    else                                                                 \
+      launch_step<PK, A, TK, nm, false>(S, T, src, dst, ctrl, L, nz, s); \
+    return check_launch("gbdmc step");                                   \
   }
-  set_error("gbdmc_sim_step: unknown noise mode %d", S.noise_mode);
+  GBDMC_NM(GBDMC_NOISE_PHILOX32)
+  GBDMC_NM(GBDMC_NOISE_PHILOX64)
+  GBDMC_NM(GBDMC_NOISE_INJECTED)
+#undef GBDMC_NM
+  set_error("gbdmc step: unknown noise mode %d", S.noise_mode);
   return GBDMC_ERR_ARG;
 }
+
+template <int A>
+static int run_compact(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& in,
+                       const gbdmc_walkers_t& out, const gbdmc_ctrl_t* ctrl, cudaStream_t s) {
+  if (in.f && out.f)
+    k_compact<A, true><<<grid_for(T), T.tpb, 0, s>>>(S, T, in, out, ctrl);
+  else
+    k_compact<A, false><<<grid_for(T), T.tpb, 0, s>>>(S, T, in, out, ctrl);
+  return check_launch("gbdmc_walkers_compact");
+}
+
+struct InitF {
+  const gbdmc_sim_t& S;
+  const RepTable& T;
+  const gbdmc_walkers_t& W;
+  gbdmc_ctrl_t* ctrl;
+  const ScratchLayout& L;
+  cudaStream_t s;
+  template <int PK, int A, int TK>
+  int operator()() {
+    return run_init<PK, A, TK>(S, T, W, ctrl, L, s);
+  }
+};
+
+struct StepF {
+  const gbdmc_sim_t& S;
+  const RepTable& T;
+  const gbdmc_walkers_t& src;
+  const gbdmc_walkers_t& dst;
+  gbdmc_ctrl_t* ctrl;
+  const ScratchLayout& L;
+  const gbdmc_noise_t& nz;
+  cudaStream_t s;
+  template <int PK, int A, int TK>
+  int operator()() {
+    return run_step<PK, A, TK>(S, T, src, dst, ctrl, L, nz, s);
+  }
+};
 
 // Supported (PES, atoms, trial) systems.
 template <typename F>
@@ -835,8 +1034,8 @@ static int validate(const gbdmc_sim_t* S, const gbdmc_walkers_t* W, const void* 
     set_error("%s: null argument", what);
     return GBDMC_ERR_ARG;
   }
-  if (S->natoms < 1 || S->natoms > GBDMC_MAX_ATOMS || S->ld < 1 || S->n0 < 1) {
-    set_error("%s: bad sizes (natoms=%d ld=%lld n0=%lld)", what, S->natoms, (long long)S->ld, (long long)S->n0);
+  if (S->natoms < 1 || S->natoms > GBDMC_MAX_ATOMS || S->ld < 1) {
+    set_error("%s: bad sizes (natoms=%d ld=%lld)", what, S->natoms, (long long)S->ld);
     return GBDMC_ERR_ARG;
   }
   if (S->ld > (int64_t)INT32_MAX) {
@@ -862,71 +1061,152 @@ static int validate(const gbdmc_sim_t* S, const gbdmc_walkers_t* W, const void* 
   return GBDMC_OK;
 }
 
-
-struct InitF {
-  const gbdmc_sim_t& S;
-  const gbdmc_walkers_t& W;
-  gbdmc_ctrl_t* ctrl;
-  const ScratchLayout& L;
-  cudaStream_t s;
-  template <int PK, int A, int TK>
-  int operator()() {
-    return run_init<PK, A, TK>(S, W, ctrl, L, s);
+static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep, const gbdmc_walkers_t* src,
+                       const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl, void* scratch, const gbdmc_noise_t* noise,
+                       void* stream, const char* what) {
+  int rc = validate(S, src, ctrl, scratch, what);
+  if (rc) return rc;
+  rc = validate(S, dst, ctrl, scratch, what);
+  if (rc) return rc;
+  if (src->x == dst->x || src->v == dst->v || (src->who && src->who == dst->who)) {
+    set_error("%s: src and dst must use different arrays", what);
+    return GBDMC_ERR_ARG;
   }
-};
-
-struct StepF {
-  const gbdmc_sim_t& S;
-  const gbdmc_walkers_t& src;
-  const gbdmc_walkers_t& dst;
-  gbdmc_ctrl_t* ctrl;
-  const ScratchLayout& L;
-  const gbdmc_noise_t& nz;
-  cudaStream_t s;
-  template <int PK, int A, int TK>
-  int operator()() {
-    return step_noise<PK, A, TK>(S, src, dst, ctrl, L, nz, s);
+  if (S->weighting == GBDMC_DISCRETE && !dst->idx) {
+    set_error("%s: discrete weighting writes the branch index: dst->idx is required", what);
+    return GBDMC_ERR_ARG;
   }
-};
+  if (S->weighting == GBDMC_CONTINUOUS && (dst->idx || src->idx)) {
+    set_error("%s: continuous weighting works on compact walkers (idx must be NULL)", what);
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_noise_t nz{};
+  if (S->noise_mode == GBDMC_NOISE_INJECTED) {
+    if (!noise || !noise->normal || (S->weighting == GBDMC_DISCRETE && !noise->u_branch) ||
+        (S->trial.kind != GBDMC_TRIAL_NONE && !noise->u_accept) || noise->ld_noise < 1) {
+      set_error("%s: injected noise buffers missing", what);
+      return GBDMC_ERR_ARG;
+    }
+    nz = *noise;
+  }
+  RepTable T;
+  rc = build_table(*S, reps, nrep, T, what);
+  if (rc) return rc;
+  const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(reps, nrep));
+  StepF f{*S, T, *src, *dst, ctrl, L, nz, (cudaStream_t)stream};
+  return dispatch_system(*S, what, f);
+}
+
+static int init_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep, const gbdmc_walkers_t* W,
+                       gbdmc_ctrl_t* ctrl, void* scratch, void* stream, const char* what) {
+  int rc = validate(S, W, ctrl, scratch, what);
+  if (rc) return rc;
+  RepTable T;
+  rc = build_table(*S, reps, nrep, T, what);
+  if (rc) return rc;
+  const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(reps, nrep));
+  InitF f{*S, T, *W, ctrl, L, (cudaStream_t)stream};
+  return dispatch_system(*S, what, f);
+}
+
+static gbdmc_replica_t single_replica(const gbdmc_sim_t* S) {
+  gbdmc_replica_t r{};
+  r.off = 0;
+  r.cap = S->ld;
+  r.n0 = S->n0;
+  r.stream = S->replica_id;
+  return r;
+}
 
 }  // namespace gbdmc
 
 using namespace gbdmc;
 
+extern "C" size_t gbdmc_scratch_bytes(int64_t ld) {
+  if (ld <= 0) return 0;
+  return scratch_layout(nullptr, ld, (ld + kMinTPB - 1) / kMinTPB).bytes;
+}
+
+extern "C" size_t gbdmc_batch_scratch_bytes(const gbdmc_replica_t* reps, int32_t nrep) {
+  if (!reps || nrep < 1) return 0;
+  int64_t ld = 0;
+  for (int r = 0; r < nrep; ++r) ld = reps[r].off + reps[r].cap > ld ? reps[r].off + reps[r].cap : ld;
+  return scratch_layout(nullptr, ld, max_tiles_for(reps, nrep)).bytes;
+}
+
 extern "C" int gbdmc_sim_init(const gbdmc_sim_t* S, const gbdmc_walkers_t* W, gbdmc_ctrl_t* ctrl, void* scratch,
                               void* stream) {
-  int rc = validate(S, W, ctrl, scratch, "gbdmc_sim_init");
-  if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld);
-  cudaStream_t s = (cudaStream_t)stream;
-  InitF f{*S, *W, ctrl, L, s};
-  return dispatch_system(*S, "gbdmc_sim_init", f);
+  if (!S) {
+    set_error("gbdmc_sim_init: null sim");
+    return GBDMC_ERR_ARG;
+  }
+  if (S->n0 < 1) {
+    set_error("gbdmc_sim_init: n0 must be >= 1");
+    return GBDMC_ERR_ARG;
+  }
+  const gbdmc_replica_t r = single_replica(S);
+  return init_common(S, &r, 1, W, ctrl, scratch, stream, "gbdmc_sim_init");
 }
 
 extern "C" int gbdmc_sim_step(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
                               gbdmc_ctrl_t* ctrl, void* scratch, const gbdmc_noise_t* noise, void* stream) {
-  int rc = validate(S, src, ctrl, scratch, "gbdmc_sim_step");
+  if (!S || !dst) {
+    set_error("gbdmc_sim_step: null argument");
+    return GBDMC_ERR_ARG;
+  }
+  if (S->n0 < 1) {
+    set_error("gbdmc_sim_step: n0 must be >= 1");
+    return GBDMC_ERR_ARG;
+  }
+  const gbdmc_replica_t r = single_replica(S);
+  return step_common(S, &r, 1, src, dst, ctrl, scratch, noise, stream, "gbdmc_sim_step");
+}
+
+extern "C" int gbdmc_batch_init(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                const gbdmc_walkers_t* W, gbdmc_ctrl_t* ctrl, void* scratch, void* stream) {
+  if (!reps) {
+    set_error("gbdmc_batch_init: null replica table");
+    return GBDMC_ERR_ARG;
+  }
+  return init_common(S, reps, nrep, W, ctrl, scratch, stream, "gbdmc_batch_init");
+}
+
+extern "C" int gbdmc_batch_step(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl,
+                                void* scratch, const gbdmc_noise_t* noise, void* stream) {
+  if (!reps || !dst) {
+    set_error("gbdmc_batch_step: null argument");
+    return GBDMC_ERR_ARG;
+  }
+  return step_common(S, reps, nrep, src, dst, ctrl, scratch, noise, stream, "gbdmc_batch_step");
+}
+
+extern "C" int gbdmc_walkers_compact(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                     const gbdmc_walkers_t* in, const gbdmc_walkers_t* out,
+                                     const gbdmc_ctrl_t* ctrl, void* stream) {
+  if (!S || !in || !out || !ctrl || !in->x || !in->v || !out->x || !out->v || in->x == out->x) {
+    set_error("gbdmc_walkers_compact: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_replica_t one;
+  if (nrep == 0) {
+    one = single_replica(S);
+    one.n0 = S->n0 > 0 ? S->n0 : 1;
+    reps = &one;
+    nrep = 1;
+  }
+  RepTable T;
+  int rc = build_table(*S, reps, nrep, T, "gbdmc_walkers_compact");
   if (rc) return rc;
-  if (S->weighting == GBDMC_DISCRETE) {
-    if (!dst || !dst->x || !dst->v || dst->x == src->x) {
-      set_error("gbdmc_sim_step: discrete weighting needs a distinct dst buffer");
-      return GBDMC_ERR_ARG;
-    }
-  }
-  gbdmc_noise_t nz{};
-  if (S->noise_mode == GBDMC_NOISE_INJECTED) {
-    if (!noise || !noise->normal || !noise->u_branch ||
-        (S->trial.kind != GBDMC_TRIAL_NONE && !noise->u_accept) || noise->ld_noise < 1) {
-      set_error("gbdmc_sim_step: injected noise buffers missing");
-      return GBDMC_ERR_ARG;
-    }
-    nz = *noise;
-  }
-  const ScratchLayout L = scratch_layout(scratch, S->ld);
   cudaStream_t s = (cudaStream_t)stream;
-  const gbdmc_walkers_t d = dst ? *dst : *src;
-  StepF f{*S, *src, d, ctrl, L, nz, s};
-  return dispatch_system(*S, "gbdmc_sim_step", f);
+  switch (S->natoms) {
+    case 1: return run_compact<1>(*S, T, *in, *out, ctrl, s);
+    case 2: return run_compact<2>(*S, T, *in, *out, ctrl, s);
+    case 3: return run_compact<3>(*S, T, *in, *out, ctrl, s);
+    case 6: return run_compact<6>(*S, T, *in, *out, ctrl, s);
+  }
+  set_error("gbdmc_walkers_compact: unsupported natoms %d", S->natoms);
+  return GBDMC_ERR_ARG;
 }
 
 extern "C" int gbdmc_desc_weights(const int32_t* who, const double* w, const int64_t* n_dev, int64_t n_parent,
@@ -943,7 +1223,7 @@ extern "C" int gbdmc_desc_weights(const int32_t* who, const double* w, const int
       return GBDMC_ERR_CUDA;
     }
   }
-  k_desc<<<304, 256, 0, s>>>(who, w, n_dev, n_parent, desc);
+  k_desc<<<2 * num_sms(), 256, 0, s>>>(who, w, n_dev, n_parent, desc);
   return check_launch("gbdmc_desc_weights");
 }
 
@@ -952,6 +1232,6 @@ extern "C" int gbdmc_desc_begin(int32_t* who, const int64_t* n_dev, void* stream
     set_error("gbdmc_desc_begin: invalid arguments");
     return GBDMC_ERR_ARG;
   }
-  k_iota<<<304, 256, 0, (cudaStream_t)stream>>>(who, n_dev);
+  k_iota<<<2 * num_sms(), 256, 0, (cudaStream_t)stream>>>(who, n_dev);
   return check_launch("gbdmc_desc_begin");
 }

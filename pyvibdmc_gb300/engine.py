@@ -13,7 +13,9 @@ Extra keywords (after ``*``): ``seed`` (Philox key), ``rng`` ('philox32',
 that supplies the deviates on the host in the reference's call order),
 ``capacity`` (walker buffer size, default ``floor(1.5 N0) + 1`` rounded up to
 256), ``graph_steps`` (steps per captured CUDA graph), ``device``,
-``write_files``.
+``write_files``, ``training_sink`` (callable receiving device walkers at the
+``DEBUG_save_training_every`` steps), ``replica_id`` (Philox stream) and
+``block_threads`` (tile width; 0 = chosen from the population).
 """
 import copy
 import ctypes as C
@@ -43,7 +45,7 @@ class DMC_Sim:
                  adiabatic_dmc=None, fixed_node=None, DEBUG_alpha=None, DEBUG_save_desc_wt_tracker=None,
                  DEBUG_save_training_every=None, DEBUG_save_before_bod=False, DEBUG_mass_change=None,
                  *, seed=0, rng="philox32", capacity=None, graph_steps=32, device=None, write_files=True,
-                 training_sink=None):
+                 training_sink=None, replica_id=0, block_threads=0):
         unsupported = {"imp_samp_oned": imp_samp_oned, "second_impsamp_displacement": second_impsamp_displacement,
                        "excited_state_imp_samp": excited_state_imp_samp, "adiabatic_dmc": adiabatic_dmc,
                        "fixed_node": fixed_node, "DEBUG_mass_change": DEBUG_mass_change,
@@ -84,6 +86,8 @@ class DMC_Sim:
         self.graph_steps = max(2, int(graph_steps) // 2 * 2)
         self.write_files = write_files
         self.training_sink = training_sink
+        self.replica_id = int(replica_id)
+        self.block_threads = int(block_threads)
         self.device = torch.device(device) if device is not None else default_device()
         self.masses = masses
         self._initialize(capacity)
@@ -189,20 +193,24 @@ class DMC_Sim:
         dev, ld, A = self.device, self.capacity, self.natoms
         f64 = dict(dtype=torch.float64, device=dev)
         IS = self.impsamp_manager is not None
+        cont = self.weighting == "continuous"
         self._bufs = []
-        for _ in range(2 if self.weighting == "discrete" else 1):
+        for _ in range(2):
             b = dict(x=torch.zeros(3 * A, ld, **f64), v=torch.zeros(ld, **f64),
                      who=torch.zeros(ld, dtype=torch.int32, device=dev))
             if IS:
                 b.update(f=torch.zeros(3 * A, ld, **f64), psi=torch.zeros(ld, **f64), ke=torch.zeros(ld, **f64))
+            if cont:
+                b["w"] = torch.zeros(ld, **f64)
+            else:
+                b["idx"] = torch.zeros(ld, dtype=torch.int32, device=dev)
             self._bufs.append(b)
-        self._w = None
-        if self.weighting == "continuous":
-            self._w = torch.zeros(ld, **f64)
+        if cont:
             w0 = np.ones(len(coords)) if self.start_cont_wts is None else np.asarray(self.start_cont_wts, float)
-            self._w[:len(coords)] = torch.as_tensor(w0, **f64)
+            self._bufs[0]["w"][:len(coords)] = torch.as_tensor(w0, **f64)
         self._bufs[0]["x"][:, :len(coords)] = to_soa(coords, dev)
         self._cur = 0
+        self._lazy = False  # current buffer holds its walkers through a gather index
         self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
         L = _capi.load()
         self._scratch = torch.zeros(L.gbdmc_scratch_bytes(ld), dtype=torch.uint8, device=dev)
@@ -215,7 +223,6 @@ class DMC_Sim:
                           eff_ts=torch.zeros(T, **f64))
         self._n_start = len(coords)
         self._sim = self._make_sim()
-        self._walkers = [self._walker_struct(b) for b in self._bufs]
 
     def _make_sim(self):
         s = _capi.Sim()
@@ -233,6 +240,8 @@ class DMC_Sim:
         s.thresh_lower = float(self._thresh_lower) if self._thresh_lower is not None else 0.0
         s.thresh_upper = float(self._thresh_upper) if self._thresh_upper is not None else -1.0
         s.seed = self.seed & 0xFFFFFFFFFFFFFFFF
+        s.block_threads = self.block_threads
+        s.replica_id = self.replica_id
         s.pes = self.potential.pes_struct()
         if self.impsamp_manager is not None:
             s.trial = self.impsamp_manager.trial_struct()
@@ -248,13 +257,15 @@ class DMC_Sim:
         s.hist.len = self.num_timesteps
         return s
 
-    def _walker_struct(self, b):
+    def _walker_struct(self, b, with_idx):
         w = _capi.Walkers()
         w.x, w.v, w.who = b["x"].data_ptr(), b["v"].data_ptr(), b["who"].data_ptr()
         if "f" in b:
             w.f, w.psi, w.ke = b["f"].data_ptr(), b["psi"].data_ptr(), b["ke"].data_ptr()
-        if self._w is not None:
-            w.w = self._w.data_ptr()
+        if "w" in b:
+            w.w = b["w"].data_ptr()
+        if with_idx and "idx" in b:
+            w.idx = b["idx"].data_ptr()
         return w
 
     # ------------------------------------------------------- device calls
@@ -270,41 +281,57 @@ class DMC_Sim:
 
     def _init_device(self):
         """Step-0 potential / local energy and vref (pyvibdmc.py:760-769)."""
+        self._compact()
         c = _capi.Ctrl()
         c.n = self._n_start if self.cur_timestep == 0 or not hasattr(self, "_n_now") else self._n_now
         c.step = self.cur_timestep
         c.eff_ts = self._eff_ts[self.cur_timestep - 1] if self.cur_timestep > 0 else 0.0
         self._write_ctrl(c)
         L = _capi.load()
-        _capi.check(L.gbdmc_sim_init(C.byref(self._sim), C.byref(self._walkers[self._cur]),
+        _capi.check(L.gbdmc_sim_init(C.byref(self._sim), C.byref(self._walker_struct(self._bufs[self._cur], False)),
                                      C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
                                      self._stream()), "gbdmc_sim_init")
 
-    def _launch_step(self, cur, noise=None):
+    def _launch_step(self, cur, lazy, noise=None):
+        """Queue one step reading buffer `cur` (through its gather index when
+        `lazy`) and writing the other buffer; returns the new (cur, lazy)."""
         L = _capi.load()
-        dst = self._walkers[1 - cur] if self.weighting == "discrete" else self._walkers[cur]
-        rc = L.gbdmc_sim_step(C.byref(self._sim), C.byref(self._walkers[cur]), C.byref(dst),
+        src = self._walker_struct(self._bufs[cur], lazy)
+        dst = self._walker_struct(self._bufs[1 - cur], True)
+        rc = L.gbdmc_sim_step(C.byref(self._sim), C.byref(src), C.byref(dst),
                               C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
                               C.byref(noise) if noise is not None else None, self._stream())
         _capi.check(rc, "gbdmc_sim_step")
-        return 1 - cur if self.weighting == "discrete" else cur
+        return 1 - cur, self.weighting == "discrete"
 
-    def _graph_for(self, cur):
-        key = cur
+    def _compact(self):
+        """Materialise the current walkers contiguously (gbdmc_walkers_compact)."""
+        if not self._lazy:
+            return
+        L = _capi.load()
+        src = self._walker_struct(self._bufs[self._cur], True)
+        dst = self._walker_struct(self._bufs[1 - self._cur], False)
+        _capi.check(L.gbdmc_walkers_compact(C.byref(self._sim), None, 0, C.byref(src), C.byref(dst),
+                                            C.c_void_p(self._ctrl.data_ptr()), self._stream()),
+                    "gbdmc_walkers_compact")
+        self._cur, self._lazy = 1 - self._cur, False
+
+    def _graph_for(self, cur, lazy):
+        key = (cur, lazy)
         g = self._graphs.get(key)
         if g is None:
             g = torch.cuda.CUDAGraph()
             side = torch.cuda.Stream(device=self.device)
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.graph(g, stream=side):
-                c = cur
+                c, lz = cur, lazy
                 for _ in range(self.graph_steps):
-                    c = self._launch_step(c)
+                    c, lz = self._launch_step(c, lz)
             torch.cuda.current_stream().wait_stream(side)
             self._graphs[key] = g
         return g
 
-    def _injected_step(self, cur, n):
+    def _injected_step(self, n):
         """Host-supplied deviates in the reference's draw order (pyvibdmc.py:544, :556, :601, :392)."""
         A = self.natoms
         z = np.asarray(self.rng.standard_normal((n, 3, A)), dtype=np.float64)
@@ -319,23 +346,26 @@ class DMC_Sim:
         nz.u_accept = ua.data_ptr() if ua is not None else None
         nz.ld_noise = n
         self._keep = (zs, ub, ua)
-        return self._launch_step(cur, nz)
+        self._cur, self._lazy = self._launch_step(self._cur, self._lazy, nz)
 
     def _run_steps(self, nsteps):
-        """Run nsteps steps on the device; returns after queueing (no sync) in Philox modes."""
+        """Queue nsteps steps (no host sync in the Philox modes)."""
         if self._noise_mode == _capi.NOISE_INJECTED:
             for _ in range(nsteps):
                 c = self._read_ctrl()
                 if c.status:
                     return
-                self._cur = self._injected_step(self._cur, c.n)
+                self._injected_step(c.n)
             return
         done = 0
+        if nsteps and self.weighting == "discrete" and not self._lazy:
+            self._cur, self._lazy = self._launch_step(self._cur, self._lazy)
+            done = 1
         while nsteps - done >= self.graph_steps:
-            self._graph_for(self._cur).replay()
+            self._graph_for(self._cur, self._lazy).replay()
             done += self.graph_steps
         while done < nsteps:
-            self._cur = self._launch_step(self._cur)
+            self._cur, self._lazy = self._launch_step(self._cur, self._lazy)
             done += 1
 
     # ------------------------------------------------------------ events
@@ -348,15 +378,17 @@ class DMC_Sim:
         return int(self._read_ctrl().n)
 
     def _coords_host(self, n=None):
+        self._compact()
         n = self._n_device() if n is None else n
         return from_soa(self._bufs[self._cur]["x"], n, self.natoms)
 
     def _begin_desc(self, t):
         """pyvibdmc.py:739-747."""
         L = _capi.load()
+        self._compact()
         n = self._n_device()
         self._parent = self._coords_host(n)
-        self._parent_wts = None if self._w is None else self._w[:n].cpu().numpy().copy()
+        self._parent_wts = None if "w" not in self._bufs[0] else self._bufs[self._cur]["w"][:n].cpu().numpy().copy()
         _capi.check(L.gbdmc_desc_begin(C.c_void_p(self._bufs[self._cur]["who"].data_ptr()),
                                        C.c_void_p(self._ctrl.data_ptr()), self._stream()), "gbdmc_desc_begin")
         self._desc_open = t
@@ -364,9 +396,11 @@ class DMC_Sim:
     def _end_desc(self, t):
         """pyvibdmc.py:856-872."""
         L = _capi.load()
+        self._compact()
         npar = len(self._parent)
         desc = torch.zeros(max(npar, 1), dtype=torch.float64, device=self.device)
-        wptr = C.c_void_p(self._w.data_ptr()) if self._w is not None else None
+        wb = self._bufs[self._cur].get("w")
+        wptr = C.c_void_p(wb.data_ptr()) if wb is not None else None
         _capi.check(L.gbdmc_desc_weights(C.c_void_p(self._bufs[self._cur]["who"].data_ptr()), wptr,
                                          C.c_void_p(self._ctrl.data_ptr()), npar, C.c_void_p(desc.data_ptr()),
                                          self._stream()), "gbdmc_desc_weights")
@@ -385,6 +419,7 @@ class DMC_Sim:
         self._desc_open = None
 
     def _harvest(self, t):
+        self._compact()
         n = self._n_device()
         b = self._bufs[self._cur]
         if self.training_sink is not None:
@@ -434,14 +469,16 @@ class DMC_Sim:
             t_end = min(t_end, T)
             self._pop_before = self._n_device() if self.impsamp_manager is not None else 0
             cur0 = self._cur
+            if self.weighting == "discrete" and not self._lazy and self._noise_mode != _capi.NOISE_INJECTED:
+                cur0 = self._cur  # the first step of the batch is a direct launch from this buffer
             t_start = time.perf_counter()
             self._run_steps(t_end - t)
             c = self._read_ctrl()
             secs = time.perf_counter() - t_start
             if c.status:
                 done = int(c.err_step) - t
-                if self.weighting == "discrete":
-                    self._cur = cur0 ^ (done & 1)
+                # the failing step moved its walkers into its dst buffer and did not branch
+                self._cur, self._lazy = cur0 ^ (done & 1) ^ 1, False
                 h = self._sync_history(t, int(c.err_step))
                 self.cur_timestep = int(c.err_step)
                 self._n_now = int(c.n)
@@ -502,7 +539,7 @@ class DMC_Sim:
             "potential", "impsamp_manager", "potential_info", "training_sink", "device", "rng")}
         st.update(_coords=self._coords_host(n), _vref_vs_tau=self._vref_vs_tau.copy(),
                   _pop_vs_tau=self._pop_vs_tau.copy(), _eff_ts=self._eff_ts.copy(),
-                  _cont_wts=None if self._w is None else self._w[:n].cpu().numpy(),
+                  _cont_wts=None if "w" not in self._bufs[0] else self._bufs[self._cur]["w"][:n].cpu().numpy(),
                   _masses=np.asarray(self.masses), _atm_nums=self._atm_nums,
                   _rng=self.rng if isinstance(self.rng, str) else "philox32",
                   _vref=float(self._read_ctrl().vref))
@@ -522,7 +559,7 @@ class DMC_Sim:
     def walkers(self):
         x = self._coords_host()
         if self.weighting == "continuous":
-            return x, self._w[:len(x)].cpu().numpy()
+            return x, self._bufs[self._cur]["w"][:len(x)].cpu().numpy()
         return x
 
     def zpe(self, onwards=None, ret_cm=True):
