@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
         x[k] = __dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k]));
         out.x[k * ld + dst] = x[k];
       }
-      if (out.who) out.who[dst] = in.who[src];
+      if (out.who && in.who) out.who[dst] = in.who[src];
       const double v = pes<PK, A, false>(x, S.pes, g);
       out.v[dst] = v;
       if (STATS) {
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
       }
       out.psi[dst] = psi;
       out.ke[dst] = ke;
-      if (out.who) out.who[dst] = in.who[src];
+      if (out.who && in.who) out.who[dst] = in.who[src];
       if (S.weighting == GBDMC_CONTINUOUS) out.w[dst] = in.w[src];
       const double v = pes<PK, A, false>(x, S.pes, g);
       out.v[dst] = v + ke;
