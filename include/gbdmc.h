@@ -241,8 +241,84 @@ int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);
 
 /* sizeof() of the ABI structs, for binding self-checks:
  * 0 gbdmc_sim_t, 1 gbdmc_walkers_t, 2 gbdmc_ctrl_t, 3 gbdmc_noise_t,
- * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t, 7 gbdmc_replica_t; 0 for unknown ids. */
+ * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t, 7 gbdmc_replica_t, 8 gbdmc_mlp_t,
+ * 9 gbdmc_walkers_f32_t; 0 for unknown ids. */
 size_t gbdmc_struct_size(int32_t which);
+
+/* ---- MLP surrogate of the water-dimer PES (BF16 tensor cores, FP32 accumulation) ----
+ * Replaces the user model behind NN_Potential.getpot
+ * (simulation_utilities/potential_manager.py:177-214) and the distance
+ * descriptor of DistIt (tensorflow_descriptors/distance_descriptors.py:102-113,
+ * method 'distance' inverted): 15 inverse O/H distances -> 3 x 128 SiLU -> 1.
+ * Weight matrices are bf16 and stored transposed (n-major): wNt[n*K + k]. */
+#define GBDMC_MLP_HIDDEN 128
+#define GBDMC_MLP_INPUT 16 /* 15 features, padded */
+typedef struct {
+  const uint16_t* w1t; /* [128][16]  */
+  const uint16_t* w2t; /* [128][128] */
+  const uint16_t* w3t; /* [128][128] */
+  const float* b1;
+  const float* b2;
+  const float* b3;     /* [128] each */
+  const float* w4;     /* [128] output weights (fp32) */
+  float b4;
+  float e_mean;        /* V = e_mean + e_scale * network output (hartree) */
+  float e_scale;
+  float hull_margin;   /* walkers with a normalised feature outside [lo-m, hi+m] use the analytic PES */
+  float feat_mu[16];
+  float feat_inv_sd[16];
+  float feat_lo[16];
+  float feat_hi[16];
+  int32_t audit_every; /* walker audited (analytic PES, error recorded) when hash % audit_every == 0; 0 = off */
+  int32_t reserved;
+} gbdmc_mlp_t;
+
+/* fp32-coordinate walkers of the surrogate path (SoA [18][ld]) */
+typedef struct {
+  float* x;
+  double* v;
+  int32_t* who;
+  int32_t* idx;
+} gbdmc_walkers_f32_t;
+
+/* Training kernels.  Y[M x 128] = X[M x K] W + b (K = 16 or 128; X fp32 rounded to bf16). */
+int gbdmc_mlp_gemm(const float* x_dev, int64_t m, int32_t k, const uint16_t* wt_dev, const float* bias_dev,
+                   float* y_dev, void* stream);
+/* G[K x 128] += X^T D over the m rows (fp32 atomics). */
+int gbdmc_mlp_gemm_tn(const float* x_dev, const float* d_dev, int64_t m, int32_t k, float* g_dev, void* stream);
+/* H = silu(Z), Ht = silu'(Z) Zt (Zt/Ht may be NULL). */
+int gbdmc_mlp_silu_fwd(const float* z_dev, const float* zt_dev, float* h_dev, float* ht_dev, int64_t n, void* stream);
+/* Zb = silu'(Z) Hb + silu''(Z) Zt Htb, Ztb = silu'(Z) Htb (Zt/Htb/Ztb may be NULL). */
+int gbdmc_mlp_silu_bwd(const float* z_dev, const float* zt_dev, const float* hb_dev, const float* htb_dev,
+                       float* zb_dev, float* ztb_dev, int64_t n, void* stream);
+/* Output layer + loss wE<(E-e)^2> + wF<(Et-et)^2>; writes dL/dH3, dL/dHt3 and accumulates dL/dw4, dL/db4,
+ * loss[0] = sum (E-e)^2, loss[1] = sum (Et-et)^2. */
+int gbdmc_mlp_head(const float* h3_dev, const float* ht3_dev, const float* w4_dev, float b4, const float* e_dev,
+                   const float* et_dev, int64_t m, float w_e, float w_f, float* h3b_dev, float* ht3b_dev,
+                   float* gw4_dev, float* gb4_dev, double* loss_dev, void* stream);
+/* Adam step (t >= 1) on fp32 parameters; for a K x 128 weight matrix also refreshes its bf16 copies:
+ * wt transposed (n-major, forward GEMM) and wn row-major (backward GEMM); either may be NULL. */
+int gbdmc_mlp_adam(float* p_dev, const float* g_dev, float* m_dev, float* v_dev, int64_t n, float lr, float beta1,
+                   float beta2, float eps, int32_t t, uint16_t* wt_dev, uint16_t* wn_dev, int32_t k, void* stream);
+/* Normalised descriptors of n dimers (fp64 SoA [18][ld]); with vdir (SoA, may be NULL) also the normalised
+ * directional derivative of the descriptors and et = (dV/dx . v) / e_scale from grad (SoA). */
+int gbdmc_dimer_features(const double* x_dev, int64_t ld, int64_t n, const float* mu_dev, const float* inv_sd_dev,
+                         const double* vdir_dev, const double* grad_dev, float e_scale, float* feat_dev,
+                         float* tang_dev, float* et_dev, void* stream);
+/* Surrogate energies of n walkers (fp32 SoA [18][ld]); outside_dev[i] = 1 for walkers outside the training box
+ * (may be NULL; not cleared). */
+int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int64_t n, double* v_dev,
+                     int32_t* outside_dev, void* stream);
+/* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
+ * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[4] accumulates: audited
+ * walkers, sum (V_nn - V_analytic), sum (V_nn - V_analytic)^2, fallbacks. */
+int gbdmc_mlp_sim_init(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
+                       gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
+int gbdmc_mlp_sim_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,
+                       const gbdmc_walkers_f32_t* dst, gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, double* audit_dev,
+                       const gbdmc_noise_t* noise, void* stream);
+int gbdmc_mlp_compact(const gbdmc_sim_t* sim, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
+                      const gbdmc_ctrl_t* ctrl_dev, void* stream);
 
 /* ---- measurement aids (no counterpart in the reference; used by bench.py) ----
  * gbdmc_prof_enable(1) makes every later gbdmc_sim_step record CUDA events

@@ -6,3 +6,4 @@ and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` use it,
 and only as the checker or as the timed CPU baseline.
 """
 from .dmc_oracle import *  # noqa: F401,F403
+from . import mlp_oracle  # noqa: F401,E402

@@ -620,20 +620,12 @@ def dimer_config():
 
 
 def dimer_equilibrium():
-    """Minimum of :func:`pes_dimer` found once with scipy from a
-    donor/acceptor start; stored to keep start structures fixed."""
-    return np.array(_DIMER_EQ)
-
-
-_DIMER_EQ = None  # filled in below by _load_dimer_eq()
-
-
-def _load_dimer_eq():
-    global _DIMER_EQ
-    import os
-    path = os.path.join(os.path.dirname(__file__), "dimer_eq.npy")
-    if os.path.exists(path):
-        _DIMER_EQ = np.load(path)
-
-
-_load_dimer_eq()
+    """Minimum of :func:`pes_dimer` (E = -0.0108784 Eh, R_OO = 5.152 bohr),
+    found once with scipy BFGS from random donor/acceptor starts."""
+    return np.array([
+    [0.000000000000, 0.000000000000, 0.000000000000],
+    [1.427477952458, -0.371496091643, 1.058267415716],
+    [-0.475355230876, -1.624174243271, -0.657060123398],
+    [-0.890893874743, 4.517468473284, -2.310760800984],
+    [-2.231456348667, 5.100851802863, -1.249695023025],
+    [-0.483907575038, 2.882598047543, -1.568314000679]])

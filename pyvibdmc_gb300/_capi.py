@@ -67,7 +67,19 @@ class Noise(C.Structure):
                 ("ld_noise", C.c_int64)]
 
 
-_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica]
+class MLP(C.Structure):
+    _fields_ = [("w1t", C.c_void_p), ("w2t", C.c_void_p), ("w3t", C.c_void_p), ("b1", C.c_void_p),
+                ("b2", C.c_void_p), ("b3", C.c_void_p), ("w4", C.c_void_p), ("b4", C.c_float),
+                ("e_mean", C.c_float), ("e_scale", C.c_float), ("hull_margin", C.c_float),
+                ("feat_mu", C.c_float * 16), ("feat_inv_sd", C.c_float * 16), ("feat_lo", C.c_float * 16),
+                ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("reserved", C.c_int32)]
+
+
+class WalkersF32(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("idx", C.c_void_p)]
+
+
+_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32]
 
 _lib = None
 
@@ -105,6 +117,19 @@ def load():
         "gbdmc_batch_scratch_bytes": ([C.POINTER(Replica), C.c_int32], C.c_size_t),
         "gbdmc_walkers_compact": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers),
                                    C.POINTER(Walkers), P, P], C.c_int),
+        "gbdmc_mlp_gemm": ([P, C.c_int64, C.c_int32, P, P, P, P], C.c_int),
+        "gbdmc_mlp_gemm_tn": ([P, P, C.c_int64, C.c_int32, P, P], C.c_int),
+        "gbdmc_mlp_silu_fwd": ([P, P, P, P, C.c_int64, P], C.c_int),
+        "gbdmc_mlp_silu_bwd": ([P, P, P, P, P, P, C.c_int64, P], C.c_int),
+        "gbdmc_mlp_head": ([P, P, P, C.c_float, P, P, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P], C.c_int),
+        "gbdmc_mlp_adam": ([P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P, P,
+                            C.c_int32, P], C.c_int),
+        "gbdmc_dimer_features": ([P, C.c_int64, C.c_int64, P, P, P, P, C.c_float, P, P, P, P], C.c_int),
+        "gbdmc_mlp_energy": ([C.POINTER(MLP), P, C.c_int64, C.c_int64, P, P, P], C.c_int),
+        "gbdmc_mlp_sim_init": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), P, P, P], C.c_int),
+        "gbdmc_mlp_sim_step": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P,
+                                P, C.POINTER(Noise), P], C.c_int),
+        "gbdmc_mlp_compact": ([C.POINTER(Sim), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P], C.c_int),
         "gbdmc_prof_enable": ([C.c_int32], C.c_int),
         "gbdmc_prof_read": ([C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                              C.POINTER(C.c_int64)], C.c_int),

@@ -164,6 +164,8 @@ extern "C" size_t gbdmc_struct_size(int32_t which) {
     case 5: return sizeof(gbdmc_trial_t);
     case 6: return sizeof(gbdmc_history_t);
     case 7: return sizeof(gbdmc_replica_t);
+    case 8: return sizeof(gbdmc_mlp_t);
+    case 9: return sizeof(gbdmc_walkers_f32_t);
   }
   return 0;
 }

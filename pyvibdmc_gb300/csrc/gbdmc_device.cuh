@@ -83,6 +83,14 @@ struct Rng {
   }
 };
 
+// 32-bit integer hash (SplitMix32-style finaliser) for audit sampling.
+__device__ __forceinline__ uint32_t splitmix32(uint32_t z) {
+  z += 0x9E3779B9u;
+  z = (z ^ (z >> 16)) * 0x85EBCA6Bu;
+  z = (z ^ (z >> 13)) * 0xC2B2AE35u;
+  return z ^ (z >> 16);
+}
+
 // Fill z[0..n) with standard normals for the chosen noise mode.
 template <int NM, int N>
 __device__ __forceinline__ void gen_normals(Rng& g, double (&z)[N]) {

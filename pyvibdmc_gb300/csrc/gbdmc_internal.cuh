@@ -86,4 +86,10 @@ extern ProfState g_prof;
 
 int num_sms();
 
+// Host helpers of the step launchers shared between translation units.
+int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, RepTable& T, const char* what);
+int grid_for(const RepTable& T);
+void launch_branch(const RepTable& T, int32_t* idx, const gbdmc_ctrl_t* ctrl, const long long* prefix,
+                   const int* counts, cudaStream_t s);
+
 }  // namespace gbdmc

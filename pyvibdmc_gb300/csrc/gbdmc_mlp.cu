@@ -1,0 +1,866 @@
+// MLP surrogate of the water-dimer PES on BF16 tensor cores (mma.sync
+// m16n8k16, FP32 accumulation).
+//
+// Network: 15 inverse O/H distances (normalised, padded to 16) -> 128 -> 128
+// -> 128 (SiLU) -> 1.  Inference keeps a warp's 16 walkers' activations in
+// registers from layer to layer: the m16n8 accumulator fragments of one layer
+// are repacked as the m16k16 A fragments of the next, and the weights stay in
+// shared memory for the whole persistent CTA.
+//
+// Training (force matching) uses the same fragments in three generic kernels:
+// Y = X W (+b), G += X^T D, and fused SiLU forward/backward with a tangent
+// (directional-derivative) stream, so that d(E . u)/dW -- the gradient of the
+// force residual -- is one more pass of the same GEMMs.
+#include <cuda_bf16.h>
+#include "gbdmc_stepcore.cuh"
+
+namespace gbdmc {
+
+constexpr int kH = 128;    // hidden width
+constexpr int kIn = 16;    // padded input width (15 features)
+constexpr int kPadH = 136; // smem row stride (bf16) of 128-wide weights
+constexpr int kPadI = 24;  // smem row stride (bf16) of 16-wide weights
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
+
+// Copy a transposed bf16 weight matrix Wt[128][K] from global into smem rows of stride P.
+__device__ __forceinline__ void load_wt(uint16_t* dst, const uint16_t* __restrict__ src, int K, int P) {
+  for (int e = threadIdx.x; e < kH * K / 2; e += blockDim.x) {
+    const int n = (2 * e) / K, k = (2 * e) % K;
+    *reinterpret_cast<uint32_t*>(dst + n * P + k) = __ldg(reinterpret_cast<const uint32_t*>(src) + e);
+  }
+}
+
+// acc[16 n-tiles][4] += A(16 x 16 k-chunk) * W(k-chunk x 128), W from smem Wt rows of stride P.
+__device__ __forceinline__ void mma_row16(float (&acc)[16][4], const uint32_t (&a)[4], const uint16_t* Ws, int P,
+                                          int kc) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const uint16_t* row = Ws + (8 * j + g) * P + 16 * kc + 2 * t;
+    const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
+    const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
+    mma16816(acc[j], a[0], a[1], a[2], a[3], b0, b1);
+  }
+}
+
+// --------------------------------------------------------- training GEMMs
+// Y[M x 128] = X[M x K] W[K x 128] (+ bias); X fp32 row-major, Wt bf16 [128][K].
+template <int K>
+__global__ void __launch_bounds__(256) k_gemm_xw(const float* __restrict__ X, long long M,
+                                                  const uint16_t* __restrict__ Wt, const float* __restrict__ bias,
+                                                  float* __restrict__ Y) {
+  constexpr int P = K == kH ? kPadH : kPadI;
+  __shared__ __align__(16) uint16_t Ws[kH * P];
+  load_wt(Ws, Wt, K, P);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  for (long long r0 = (long long)blockIdx.x * 128 + 16 * w; r0 < M; r0 += (long long)gridDim.x * 128) {
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const long long ra = r0 + g, rb = r0 + g + 8;
+#pragma unroll
+    for (int kc = 0; kc < K / 16; ++kc) {
+      const int c = 16 * kc + 2 * t;
+      float2 xa0 = make_float2(0.f, 0.f), xa1 = xa0, xb0 = xa0, xb1 = xa0;
+      if (ra < M) {
+        xa0 = *reinterpret_cast<const float2*>(X + ra * K + c);
+        xa1 = *reinterpret_cast<const float2*>(X + ra * K + c + 8);
+      }
+      if (rb < M) {
+        xb0 = *reinterpret_cast<const float2*>(X + rb * K + c);
+        xb1 = *reinterpret_cast<const float2*>(X + rb * K + c + 8);
+      }
+      const uint32_t a[4] = {pack_bf16(xa0.x, xa0.y), pack_bf16(xb0.x, xb0.y), pack_bf16(xa1.x, xa1.y),
+                             pack_bf16(xb1.x, xb1.y)};
+      mma_row16(acc, a, Ws, P, kc);
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int col = 8 * j + 2 * t;
+      const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+      if (ra < M) *reinterpret_cast<float2*>(Y + ra * kH + col) = make_float2(acc[j][0] + b0, acc[j][1] + b1);
+      if (rb < M) *reinterpret_cast<float2*>(Y + rb * kH + col) = make_float2(acc[j][2] + b0, acc[j][3] + b1);
+    }
+  }
+}
+
+// G[K x 128] += X[M x K]^T D[M x 128]: chunks of 64 rows staged transposed in
+// smem (bf16), reduced over M in registers, then one fp32 atomicAdd per element.
+template <int K>
+__global__ void __launch_bounds__(256) k_gemm_tn(const float* __restrict__ X, const float* __restrict__ D,
+                                                  long long M, float* __restrict__ G) {
+  constexpr int CH = 64, PC = CH + 8;
+  __shared__ __align__(16) uint16_t Xt[K * PC];
+  __shared__ __align__(16) uint16_t Dt[kH * PC];
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  constexpr int NTW = K == kH ? 16 : 2;  // n-tiles per warp
+  const int mt = K == kH ? w : 0;         // m-tile (rows of K) of this warp
+  const int nt0 = K == kH ? 0 : 2 * w;
+  float acc[NTW][4];
+#pragma unroll
+  for (int j = 0; j < NTW; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  for (long long c0 = (long long)blockIdx.x * CH; c0 < M; c0 += (long long)gridDim.x * CH) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < CH * K; e += blockDim.x) {
+      const int r = e / K, c = e % K;
+      const float v = (c0 + r < M) ? X[(c0 + r) * K + c] : 0.f;
+      const __nv_bfloat16 b = __float2bfloat16_rn(v);
+      Xt[c * PC + r] = *reinterpret_cast<const uint16_t*>(&b);
+    }
+    for (int e = threadIdx.x; e < CH * kH; e += blockDim.x) {
+      const int r = e / kH, c = e % kH;
+      const float v = (c0 + r < M) ? D[(c0 + r) * kH + c] : 0.f;
+      const __nv_bfloat16 b = __float2bfloat16_rn(v);
+      Dt[c * PC + r] = *reinterpret_cast<const uint16_t*>(&b);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < CH; ks += 16) {
+      const uint16_t* xa = Xt + (16 * mt + g) * PC + ks + 2 * t;
+      const uint16_t* xb = Xt + (16 * mt + g + 8) * PC + ks + 2 * t;
+      const uint32_t a0 = *reinterpret_cast<const uint32_t*>(xa);
+      const uint32_t a1 = *reinterpret_cast<const uint32_t*>(xb);
+      const uint32_t a2 = *reinterpret_cast<const uint32_t*>(xa + 8);
+      const uint32_t a3 = *reinterpret_cast<const uint32_t*>(xb + 8);
+#pragma unroll
+      for (int j = 0; j < NTW; ++j) {
+        const uint16_t* db = Dt + (8 * (nt0 + j) + g) * PC + ks + 2 * t;
+        mma16816(acc[j], a0, a1, a2, a3, *reinterpret_cast<const uint32_t*>(db),
+                 *reinterpret_cast<const uint32_t*>(db + 8));
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NTW; ++j) {
+    const int col = 8 * (nt0 + j) + 2 * t;
+    const int ra = 16 * mt + g, rb = ra + 8;
+    atomicAdd(G + ra * kH + col, acc[j][0]);
+    atomicAdd(G + ra * kH + col + 1, acc[j][1]);
+    atomicAdd(G + rb * kH + col, acc[j][2]);
+    atomicAdd(G + rb * kH + col + 1, acc[j][3]);
+  }
+}
+
+// ------------------------------------------------------------ elementwise
+// H = silu(Z); Ht = silu'(Z) Zt  (tangent stream, may be NULL)
+__global__ void k_silu_fwd(const float* __restrict__ Z, const float* __restrict__ Zt, float* __restrict__ H,
+                           float* __restrict__ Ht, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float z = Z[i];
+    const float s = sigmoidf_(z);
+    H[i] = z * s;
+    if (Ht) Ht[i] = s * (1.f + z * (1.f - s)) * Zt[i];
+  }
+}
+
+// Zb = silu'(Z) Hb + silu''(Z) Zt Htb ;  Ztb = silu'(Z) Htb
+__global__ void k_silu_bwd(const float* __restrict__ Z, const float* __restrict__ Zt, const float* __restrict__ Hb,
+                           const float* __restrict__ Htb, float* __restrict__ Zb, float* __restrict__ Ztb,
+                           long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float z = Z[i];
+    const float s = sigmoidf_(z);
+    const float d1 = s * (1.f + z * (1.f - s));
+    const float d2 = s * (1.f - s) * (2.f + z * (1.f - 2.f * s));
+    const float hb = Hb[i];
+    if (Zt) {
+      const float htb = Htb[i];
+      Zb[i] = d1 * hb + d2 * Zt[i] * htb;
+      Ztb[i] = d1 * htb;
+    } else {
+      Zb[i] = d1 * hb;
+    }
+  }
+}
+
+// Output layer and loss, one warp per sample:
+//   E = H3 w4 + b4, Et = Ht3 w4;  L = wE (E - e)^2 + wF (Et - et)^2 (mean over samples)
+//   writes dL/dH3, dL/dHt3, accumulates dL/dw4, dL/db4 and the loss terms.
+__global__ void k_head(const float* __restrict__ H3, const float* __restrict__ Ht3, const float* __restrict__ w4,
+                       float b4, const float* __restrict__ e_true, const float* __restrict__ et_true, long long M,
+                       float wE, float wF, float* __restrict__ H3b, float* __restrict__ Ht3b, float* __restrict__ gw4,
+                       float* __restrict__ gb4, double* __restrict__ loss) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  float gw[4] = {0.f, 0.f, 0.f, 0.f}, gb = 0.f;
+  double lE = 0.0, lF = 0.0;
+  for (long long s = warp; s < M; s += nw) {
+    float e = 0.f, et = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = lane + 32 * q;
+      e += H3[s * kH + c] * w4[c];
+      if (Ht3) et += Ht3[s * kH + c] * w4[c];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      e += __shfl_xor_sync(0xffffffffu, e, o);
+      et += __shfl_xor_sync(0xffffffffu, et, o);
+    }
+    e += b4;
+    const float de = 2.f * wE * (e - e_true[s]) / (float)M;
+    const float det = Ht3 ? 2.f * wF * (et - et_true[s]) / (float)M : 0.f;
+    if (lane == 0) {
+      lE += (double)(e - e_true[s]) * (double)(e - e_true[s]);
+      if (Ht3) lF += (double)(et - et_true[s]) * (double)(et - et_true[s]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = lane + 32 * q;
+      H3b[s * kH + c] = de * w4[c];
+      if (Ht3) {
+        Ht3b[s * kH + c] = det * w4[c];
+        gw[q] += de * H3[s * kH + c] + det * Ht3[s * kH + c];
+      } else {
+        gw[q] += de * H3[s * kH + c];
+      }
+    }
+    gb += de;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) atomicAdd(gw4 + lane + 32 * q, gw[q]);
+  if (lane == 0) {
+    atomicAdd(gb4, gb);
+    atomicAdd(loss, lE);
+    atomicAdd(loss + 1, lF);
+  }
+}
+
+// Adam on fp32 master parameters; optionally refreshes the bf16 copies used
+// by the GEMMs: transposed wt[n*K + k] = p[k*128 + n] (forward) and row-major
+// wn[k*128 + n] = p[k*128 + n] (backward through the layer).
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2, uint16_t* __restrict__ wt, uint16_t* __restrict__ wn, int K) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float g = gr[i];
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    p[i] = pi;
+    if (wt || wn) {
+      const long long k = i / kH, nn = i % kH;
+      const __nv_bfloat16 b = __float2bfloat16_rn(pi);
+      if (wt) wt[nn * K + k] = *reinterpret_cast<const uint16_t*>(&b);
+      if (wn) wn[i] = *reinterpret_cast<const uint16_t*>(&b);
+    }
+  }
+}
+
+// ------------------------------------------------------------- features
+// Inverse distances of the 15 atom pairs (i<j, combinations order of the
+// reference's descriptor, tensorflow_descriptors/distance_descriptors.py:66-68)
+// normalised (d - mu) * inv_sd; with a direction v, also the normalised
+// directional derivative u = (dd/dx) v, and et = (dV/dx . v) / e_scale.
+template <typename T>
+__global__ void k_features(const T* __restrict__ x, long long ldx, long long n, const float* __restrict__ mu,
+                           const float* __restrict__ inv_sd, const T* __restrict__ vdir, const double* __restrict__ grad,
+                           float e_scale, float* __restrict__ feat, float* __restrict__ tang, float* __restrict__ et) {
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (long long)gridDim.x * blockDim.x) {
+    float xs[18], vs[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+      xs[k] = (float)x[k * ldx + s];
+      vs[k] = vdir ? (float)vdir[k * ldx + s] : 0.f;
+    }
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+      for (int j = i + 1; j < 6; ++j) {
+        const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
+        const float ir = rsqrtf(dx * dx + dy * dy + dz * dz);
+        feat[s * kIn + q] = (ir - mu[q]) * inv_sd[q];
+        if (tang) {
+          const float dvx = vs[3 * i] - vs[3 * j], dvy = vs[3 * i + 1] - vs[3 * j + 1], dvz = vs[3 * i + 2] - vs[3 * j + 2];
+          tang[s * kIn + q] = -(dx * dvx + dy * dvy + dz * dvz) * ir * ir * ir * inv_sd[q];
+        }
+        ++q;
+      }
+    }
+    feat[s * kIn + 15] = 0.f;
+    if (tang) tang[s * kIn + 15] = 0.f;
+    if (et) {
+      double d = 0.0;
+#pragma unroll
+      for (int k = 0; k < 18; ++k) d += grad[k * ldx + s] * (double)vs[k];
+      et[s] = (float)(d / (double)e_scale);
+    }
+  }
+}
+
+// ------------------------------------------------------------ inference
+// Layer l of one warp's 16 rows: acc = A(h, 16 x K) W_l, then bias + SiLU and
+// repack into next-layer A fragments.
+__device__ __forceinline__ void hidden_layer(uint32_t (&a)[8][4], const uint16_t* Ws, const float* bs) {
+  const int lane = threadIdx.x & 31, t = lane & 3;
+  float acc[16][4];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) mma_row16(acc, a[kc], Ws, kPadH, kc);
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) {
+    const int c0 = 16 * kc + 2 * t, c1 = c0 + 8;
+    const float* u = acc[2 * kc];
+    const float* v = acc[2 * kc + 1];
+    a[kc][0] = pack_bf16(silu(u[0] + bs[c0]), silu(u[1] + bs[c0 + 1]));
+    a[kc][1] = pack_bf16(silu(u[2] + bs[c0]), silu(u[3] + bs[c0 + 1]));
+    a[kc][2] = pack_bf16(silu(v[0] + bs[c1]), silu(v[1] + bs[c1 + 1]));
+    a[kc][3] = pack_bf16(silu(v[2] + bs[c1]), silu(v[3] + bs[c1 + 1]));
+  }
+}
+
+struct MlpSmem {
+  uint16_t w1[kH * kPadI];
+  uint16_t w2[kH * kPadH];
+  uint16_t w3[kH * kPadH];
+  float b1[kH], b2[kH], b3[kH], w4[kH];
+  float feat[8][16][17];  // per warp: 16 walkers x 16 features (+1 pad)
+};
+
+__device__ void load_net(MlpSmem& sm, const gbdmc_mlp_t& net) {
+  load_wt(sm.w1, net.w1t, kIn, kPadI);
+  load_wt(sm.w2, net.w2t, kH, kPadH);
+  load_wt(sm.w3, net.w3t, kH, kPadH);
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    sm.b1[i] = net.b1[i];
+    sm.b2[i] = net.b2[i];
+    sm.b3[i] = net.b3[i];
+    sm.w4[i] = net.w4[i];
+  }
+}
+
+// Network output (normalised units) for the 16 feature rows of warp w; on
+// return every lane of quad g holds rows g (e_lo) and g + 8 (e_hi).
+__device__ __forceinline__ void mlp_forward16(const MlpSmem& sm, const gbdmc_mlp_t& net, int w, float& e_lo,
+                                              float& e_hi) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t a[8][4];
+  {
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const float* fa = sm.feat[w][g];
+    const float* fb = sm.feat[w][g + 8];
+    const uint32_t a0[4] = {pack_bf16(fa[2 * t], fa[2 * t + 1]), pack_bf16(fb[2 * t], fb[2 * t + 1]),
+                            pack_bf16(fa[2 * t + 8], fa[2 * t + 9]), pack_bf16(fb[2 * t + 8], fb[2 * t + 9])};
+    mma_row16(acc, a0, sm.w1, kPadI, 0);
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc) {
+      const int c0 = 16 * kc + 2 * t, c1 = c0 + 8;
+      const float* u = acc[2 * kc];
+      const float* v = acc[2 * kc + 1];
+      a[kc][0] = pack_bf16(silu(u[0] + sm.b1[c0]), silu(u[1] + sm.b1[c0 + 1]));
+      a[kc][1] = pack_bf16(silu(u[2] + sm.b1[c0]), silu(u[3] + sm.b1[c0 + 1]));
+      a[kc][2] = pack_bf16(silu(v[0] + sm.b1[c1]), silu(v[1] + sm.b1[c1 + 1]));
+      a[kc][3] = pack_bf16(silu(v[2] + sm.b1[c1]), silu(v[3] + sm.b1[c1 + 1]));
+    }
+  }
+  hidden_layer(a, sm.w2, sm.b2);
+  // layer 3 + head (fp32 dot with w4)
+  float acc[16][4];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) mma_row16(acc, a[kc], sm.w3, kPadH, kc);
+  float lo = 0.f, hi = 0.f;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int c = 8 * j + 2 * t;
+    lo += silu(acc[j][0] + sm.b3[c]) * sm.w4[c] + silu(acc[j][1] + sm.b3[c + 1]) * sm.w4[c + 1];
+    hi += silu(acc[j][2] + sm.b3[c]) * sm.w4[c] + silu(acc[j][3] + sm.b3[c + 1]) * sm.w4[c + 1];
+  }
+  lo += __shfl_xor_sync(0xffffffffu, lo, 1);
+  lo += __shfl_xor_sync(0xffffffffu, lo, 2);
+  hi += __shfl_xor_sync(0xffffffffu, hi, 1);
+  hi += __shfl_xor_sync(0xffffffffu, hi, 2);
+  e_lo = lo + net.b4;
+  e_hi = hi + net.b4;
+}
+
+// Descriptors of one walker into the warp's feature row; returns true when
+// the walker lies outside the training box (normalised range +- margin).
+__device__ __forceinline__ bool walker_features(const float (&xs)[18], const gbdmc_mlp_t& net, float* row) {
+  int q = 0;
+  bool out = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = i + 1; j < 6; ++j) {
+      const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
+      const float f = (rsqrtf(dx * dx + dy * dy + dz * dz) - net.feat_mu[q]) * net.feat_inv_sd[q];
+      out |= (f < net.feat_lo[q] - net.hull_margin) || (f > net.feat_hi[q] + net.hull_margin);
+      row[q] = f;
+      ++q;
+    }
+  }
+  row[15] = 0.f;
+  return out;
+}
+
+// Energies of n walkers (coordinates SoA, fp32 or fp64) from the surrogate.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mlp_energy(const __grid_constant__ gbdmc_mlp_t net, const T* __restrict__ x,
+                                                     long long ld, long long n, double* __restrict__ v,
+                                                     int* __restrict__ outside) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
+  load_net(sm, net);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  for (long long base = (long long)blockIdx.x * 128 + 16 * w; base < n; base += (long long)gridDim.x * 128) {
+    bool oob = false;
+    if (lane < 16) {
+      const long long i = base + lane;
+      float xs[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) xs[k] = i < n ? (float)x[k * ld + i] : (k < 3 ? 0.f : 1.f + k);
+      oob = walker_features(xs, net, sm.feat[w][lane]) && i < n;
+    }
+    __syncwarp();
+    float e_lo, e_hi;
+    mlp_forward16(sm, net, w, e_lo, e_hi);
+    const int row = g + 8 * t;
+    if (t < 2) {
+      const long long i = base + row;
+      if (i < n) v[i] = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi);
+    }
+    const unsigned ob = __ballot_sync(0xffffffffu, oob);
+    if (outside && lane < 16 && ((ob >> lane) & 1u)) outside[base + lane] = 1;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------- surrogate step
+// One DMC step of the water dimer on the surrogate, discrete weighting, fp32
+// walker coordinates: gather through idx, move (lanes 0-15 of each warp own
+// one walker), descriptors, MLP energy (whole warp), FP64 analytic energy for
+// the audit subset and for walkers outside the training box, weights, counts,
+// tile partials and the per-replica finalisation.  Tiles are 128 walkers
+// (8 warps x 16), so k_branch runs with tpb = 128.
+__global__ void __launch_bounds__(256) k_mlp_step(const __grid_constant__ gbdmc_sim_t S,
+                                                   const __grid_constant__ RepTable T,
+                                                   const __grid_constant__ gbdmc_mlp_t net,
+                                                   const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
+                                                   gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
+                                                   int* counts, double* audit, const gbdmc_noise_t nz) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
+  __shared__ double u_sh[8][16];
+  __shared__ unsigned char flag_sh[8][16];
+  load_net(sm, net);
+  __syncthreads();
+  const int64_t ld = S.ld;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const double vref = ctrl->vref;
+    const int64_t base = T.off[r];
+    const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * 128 + 16 * w;
+    // --- move + descriptors (lanes 0..15)
+    if (lane < 16) {
+      const int64_t i = i0 + lane;
+      float xs[18];
+      unsigned char fl = 0;
+      if (i < n) {
+        const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+        const int64_t dst = base + i;
+        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+        float z[18];
+        if (S.noise_mode == GBDMC_NOISE_INJECTED) {
+#pragma unroll
+          for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 18; k += 2) rng.normal2_f32(z[k], z[k + 1]);
+        }
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+          xs[k] = in.x[k * ld + src] + (float)S.sigma[k / 3] * z[k];
+          out.x[k * ld + dst] = xs[k];
+        }
+        if (out.who && in.who) out.who[dst] = in.who[src];
+        u_sh[w][lane] = S.noise_mode == GBDMC_NOISE_INJECTED ? nz.u_branch[dst] : rng.uniform53();
+        const bool oob = walker_features(xs, net, sm.feat[w][lane]);
+        const bool aud = net.audit_every > 0 &&
+                         ((uint32_t)(splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ T.stream[r] * 0x85EBCA6Bu)) %
+                          (uint32_t)net.audit_every) == 0;
+        fl = (oob ? 1 : 0) | (aud ? 2 : 0);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
+        walker_features(xs, net, sm.feat[w][lane]);
+      }
+      flag_sh[w][lane] = fl;
+    }
+    __syncwarp();
+    float e_lo, e_hi;
+    mlp_forward16(sm, net, w, e_lo, e_hi);
+    // --- weights and counts (lanes with t < 2 own rows g and g + 8)
+    Partial p = partial_zero();
+    int flag = 0;
+    const int row = g + 8 * t;
+    const int64_t i = i0 + row;
+    if (t < 2 && i < n) {
+      const int64_t dst = base + i;
+      double v = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi);
+      const unsigned char fl = flag_sh[w][row];
+      if (fl) {
+        double xd[18], gd[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
+        const double va = pes_dimer<false>(xd, S.pes.p, gd);
+        if (fl & 2) {
+          const double d = v - va;
+          atomicAdd(audit + 0, 1.0);
+          atomicAdd(audit + 1, d);
+          atomicAdd(audit + 2, d * d);
+        }
+        if (fl & 1) atomicAdd(audit + 3, 1.0);
+        v = va;
+      }
+      out.v[dst] = v;
+      const double n0 = (double)T.n0[r];
+      const double w_hi = (n0 + n0 * 0.5) + 1.0;
+      const int c = branch_count(v, vref, S.dt, u_sh[w][row], w_hi, flag, p.births, p.deaths);
+      counts[dst] = c;
+      p.c = c;
+      p.s0 = c == 1 ? v : (double)c * v;
+    }
+    if (__syncthreads_or(flag)) {
+      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
+    }
+    p = block_reduce_partial<false>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial tt = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
+      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, tt);
+    }
+  }
+}
+
+// Step 0 of the surrogate run: energies (with audit/fallback) and vref.
+__global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_sim_t S,
+                                                   const __grid_constant__ RepTable T,
+                                                   const __grid_constant__ gbdmc_mlp_t net, gbdmc_walkers_f32_t W,
+                                                   gbdmc_ctrl_t* ctrls, Partial* part) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
+  load_net(sm, net);
+  __syncthreads();
+  const int64_t ld = S.ld;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    const long long n = ctrl->n;
+    const int64_t base = T.off[r];
+    const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * 128 + 16 * w;
+    if (lane < 16) {
+      const int64_t i = i0 + lane;
+      float xs[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) xs[k] = i < n ? W.x[k * ld + base + i] : (k < 3 ? 0.f : 1.f + k);
+      walker_features(xs, net, sm.feat[w][lane]);
+    }
+    __syncwarp();
+    float e_lo, e_hi;
+    mlp_forward16(sm, net, w, e_lo, e_hi);
+    Partial p = partial_zero();
+    const int row = g + 8 * t;
+    const int64_t i = i0 + row;
+    if (t < 2 && i < n) {
+      double xd[18], gd[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) xd[k] = (double)W.x[k * ld + base + i];
+      // step 0 uses the analytic energy for every walker (start structures are not yet sampled)
+      const double v = pes_dimer<false>(xd, S.pes.p, gd);
+      (void)e_lo;
+      (void)e_hi;
+      W.v[base + i] = v;
+      p.s0 = v;
+      p.c = 1;
+    }
+    p = block_reduce_partial<false>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial tt = reduce_partials<false>(part, T.tile_off[r], nt, nullptr);
+      if (threadIdx.x == 0) {
+        const double n0 = (double)T.n0[r];
+        ctrl->vref = tt.s0 / (double)n - S.alpha * ((double)(n - T.n0[r]) / n0);
+        ctrl->ticket = 0;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kMaxTPB) k_compact_f32(const __grid_constant__ gbdmc_sim_t S,
+                                                          const __grid_constant__ RepTable T,
+                                                          const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
+                                                          const gbdmc_ctrl_t* ctrls) {
+  const int64_t ld = S.ld;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    const long long n = ctrls[r].n;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    if (i >= n) continue;
+    const int64_t b = T.off[r];
+    const int64_t src = b + (in.idx ? (int64_t)in.idx[b + i] : i);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) out.x[k * ld + b + i] = in.x[k * ld + src];
+    out.v[b + i] = in.v[src];
+    if (in.who && out.who) out.who[b + i] = in.who[src];
+  }
+}
+
+// ============================================================ host side
+static int ew_grid(long long n) {
+  long long g = (n + 255) / 256;
+  const long long cap = 8LL * num_sms();
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+static int mlp_smem_bytes() { return (int)sizeof(MlpSmem); }
+
+static int set_mlp_smem(const void* fn) {
+  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp_smem_bytes());
+  if (e != cudaSuccess) {
+    set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  return GBDMC_OK;
+}
+
+static bool valid_net(const gbdmc_mlp_t* net) {
+  return net && net->w1t && net->w2t && net->w3t && net->b1 && net->b2 && net->b3 && net->w4;
+}
+
+}  // namespace gbdmc
+
+using namespace gbdmc;
+
+extern "C" int gbdmc_mlp_gemm(const float* x, int64_t m, int32_t k, const uint16_t* wt, const float* bias, float* y,
+                              void* stream) {
+  if (!x || !wt || !y || m < 0 || (k != 16 && k != 128)) {
+    set_error("gbdmc_mlp_gemm: invalid arguments (k must be 16 or 128)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  long long g = (m + 127) / 128;
+  if (g > 4LL * num_sms()) g = 4LL * num_sms();
+  if (k == 16)
+    k_gemm_xw<16><<<(int)g, 256, 0, s>>>(x, m, wt, bias, y);
+  else
+    k_gemm_xw<128><<<(int)g, 256, 0, s>>>(x, m, wt, bias, y);
+  return check_launch("gbdmc_mlp_gemm");
+}
+
+extern "C" int gbdmc_mlp_gemm_tn(const float* x, const float* d, int64_t m, int32_t k, float* g, void* stream) {
+  if (!x || !d || !g || m < 0 || (k != 16 && k != 128)) {
+    set_error("gbdmc_mlp_gemm_tn: invalid arguments (k must be 16 or 128)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  long long grid = (m + 63) / 64;
+  if (grid > 2LL * num_sms()) grid = 2LL * num_sms();
+  if (k == 16)
+    k_gemm_tn<16><<<(int)grid, 256, 0, s>>>(x, d, m, g);
+  else
+    k_gemm_tn<128><<<(int)grid, 256, 0, s>>>(x, d, m, g);
+  return check_launch("gbdmc_mlp_gemm_tn");
+}
+
+extern "C" int gbdmc_mlp_silu_fwd(const float* z, const float* zt, float* h, float* ht, int64_t n, void* stream) {
+  if (!z || !h || n < 0 || ((zt == nullptr) != (ht == nullptr))) {
+    set_error("gbdmc_mlp_silu_fwd: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (n == 0) return GBDMC_OK;
+  k_silu_fwd<<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(z, zt, h, ht, n);
+  return check_launch("gbdmc_mlp_silu_fwd");
+}
+
+extern "C" int gbdmc_mlp_silu_bwd(const float* z, const float* zt, const float* hb, const float* htb, float* zb,
+                                  float* ztb, int64_t n, void* stream) {
+  if (!z || !hb || !zb || n < 0 || (zt && (!htb || !ztb))) {
+    set_error("gbdmc_mlp_silu_bwd: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (n == 0) return GBDMC_OK;
+  k_silu_bwd<<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(z, zt, hb, htb, zb, ztb, n);
+  return check_launch("gbdmc_mlp_silu_bwd");
+}
+
+extern "C" int gbdmc_mlp_head(const float* h3, const float* ht3, const float* w4, float b4, const float* e,
+                              const float* et, int64_t m, float w_e, float w_f, float* h3b, float* ht3b, float* gw4,
+                              float* gb4, double* loss, void* stream) {
+  if (!h3 || !w4 || !e || !h3b || !gw4 || !gb4 || !loss || m < 1 || (ht3 && (!et || !ht3b))) {
+    set_error("gbdmc_mlp_head: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  long long warps = m < 8LL * 256 * num_sms() / 32 ? m : 8LL * 256 * num_sms() / 32;
+  const int grid = (int)((warps * 32 + 255) / 256);
+  k_head<<<grid, 256, 0, (cudaStream_t)stream>>>(h3, ht3, w4, b4, e, et, m, w_e, w_f, h3b, ht3b, gw4, gb4, loss);
+  return check_launch("gbdmc_mlp_head");
+}
+
+extern "C" int gbdmc_mlp_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
+                              float eps, int32_t t, uint16_t* wt, uint16_t* wn, int32_t k, void* stream) {
+  if (!p || !g || !m || !v || n < 1 || t < 1 || ((wt || wn) && n != (int64_t)k * kH)) {
+    set_error("gbdmc_mlp_adam: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  const float c1 = 1.0f / (1.0f - powf(b1, (float)t)), c2 = 1.0f / (1.0f - powf(b2, (float)t));
+  k_adam<<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2, wt, wn, k);
+  return check_launch("gbdmc_mlp_adam");
+}
+
+extern "C" int gbdmc_dimer_features(const double* x, int64_t ld, int64_t n, const float* mu, const float* inv_sd,
+                                    const double* vdir, const double* grad, float e_scale, float* feat, float* tang,
+                                    float* et, void* stream) {
+  if (!x || !mu || !inv_sd || !feat || n < 0 || ld < n || (vdir && !tang) || (et && (!vdir || !grad))) {
+    set_error("gbdmc_dimer_features: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (n == 0) return GBDMC_OK;
+  k_features<double><<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(x, ld, n, mu, inv_sd, vdir, grad, e_scale, feat,
+                                                                     vdir ? tang : nullptr, et);
+  return check_launch("gbdmc_dimer_features");
+}
+
+extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t ld, int64_t n, double* v,
+                                int32_t* outside, void* stream) {
+  if (!valid_net(net) || !x || !v || n < 0 || ld < n) {
+    set_error("gbdmc_mlp_energy: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (n == 0) return GBDMC_OK;
+  int rc = set_mlp_smem((const void*)k_mlp_energy<float>);
+  if (rc) return rc;
+  long long g = (n + 127) / 128;
+  if (g > 2LL * num_sms()) g = 2LL * num_sms();
+  k_mlp_energy<float><<<(int)g, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*net, x, ld, n, v, outside);
+  return check_launch("gbdmc_mlp_energy");
+}
+
+static int mlp_table(const gbdmc_sim_t* S, RepTable& T, const char* what) {
+  if (!S || S->natoms != 6 || S->pes.kind != GBDMC_PES_DIMER || S->weighting != GBDMC_DISCRETE ||
+      S->trial.kind != GBDMC_TRIAL_NONE || S->n0 < 1 || S->ld < 1 || S->ld > (int64_t)INT32_MAX) {
+    set_error("%s: the surrogate path runs the 6-atom dimer, discrete weighting, no trial psi", what);
+    return GBDMC_ERR_ARG;
+  }
+  if (S->noise_mode == GBDMC_NOISE_PHILOX64) {
+    set_error("%s: the surrogate path draws fp32 deviates (PHILOX32 or INJECTED)", what);
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_replica_t r{};
+  r.off = 0;
+  r.cap = S->ld;
+  r.n0 = S->n0;
+  r.stream = S->replica_id;
+  gbdmc_sim_t S2 = *S;
+  S2.block_threads = 128;  // tile = 8 warps x 16 walkers
+  return build_table(S2, &r, 1, T, what);
+}
+
+extern "C" int gbdmc_mlp_sim_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
+                                  gbdmc_ctrl_t* ctrl, void* scratch, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, T, "gbdmc_mlp_sim_init");
+  if (rc) return rc;
+  if (!valid_net(net) || !w || !w->x || !w->v || !ctrl || !scratch) {
+    set_error("gbdmc_mlp_sim_init: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  rc = set_mlp_smem((const void*)k_mlp_init);
+  if (rc) return rc;
+  const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
+  int grid = T.tile_off[1];
+  if (grid > 2 * num_sms()) grid = 2 * num_sms();
+  k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part);
+  return check_launch("gbdmc_mlp_sim_init");
+}
+
+extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,
+                                  const gbdmc_walkers_f32_t* dst, gbdmc_ctrl_t* ctrl, void* scratch, double* audit,
+                                  const gbdmc_noise_t* noise, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, T, "gbdmc_mlp_sim_step");
+  if (rc) return rc;
+  if (!valid_net(net) || !src || !dst || !src->x || !dst->x || !dst->v || !dst->idx || src->x == dst->x || !ctrl ||
+      !scratch || !audit) {
+    set_error("gbdmc_mlp_sim_step: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_noise_t nz{};
+  if (S->noise_mode == GBDMC_NOISE_INJECTED) {
+    if (!noise || !noise->normal || !noise->u_branch || noise->ld_noise < 1) {
+      set_error("gbdmc_mlp_sim_step: injected noise buffers missing");
+      return GBDMC_ERR_ARG;
+    }
+    nz = *noise;
+  }
+  rc = set_mlp_smem((const void*)k_mlp_step);
+  if (rc) return rc;
+  const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
+  cudaStream_t s = (cudaStream_t)stream;
+  int grid = T.tile_off[1];
+  if (grid > 2 * num_sms()) grid = 2 * num_sms();
+  const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
+  cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
+  if (prof) cudaEventRecord(ev[0], s);
+  k_mlp_step<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.part, L.prefix, L.counts, audit,
+                                                  nz);
+  if (prof) cudaEventRecord(ev[1], s);
+  launch_branch(T, dst->idx, ctrl, L.prefix, L.counts, s);
+  if (prof) {
+    cudaEventRecord(ev[2], s);
+    ++g_prof.count;
+  }
+  return check_launch("gbdmc_mlp_sim_step");
+}
+
+extern "C" int gbdmc_mlp_compact(const gbdmc_sim_t* S, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
+                                 const gbdmc_ctrl_t* ctrl, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, T, "gbdmc_mlp_compact");
+  if (rc) return rc;
+  if (!in || !out || !in->x || !out->x || !in->v || !out->v || in->x == out->x || !ctrl) {
+    set_error("gbdmc_mlp_compact: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  k_compact_f32<<<grid_for(T), T.tpb, 0, (cudaStream_t)stream>>>(*S, T, *in, *out, ctrl);
+  return check_launch("gbdmc_mlp_compact");
+}

@@ -1,0 +1,217 @@
+// Building blocks shared by the step kernels: per-tile partials, the
+// last-tile election, the fixed-order partial reduction and prefix scan, the
+// discrete branch count and the finalisation of a branching pass.
+#pragma once
+#include "gbdmc_device.cuh"
+#include "gbdmc_internal.cuh"
+
+namespace gbdmc {
+
+__device__ __forceinline__ Partial partial_zero() {
+  Partial p;
+  p.c = p.births = p.deaths = p.aux = 0;
+  p.s0 = p.s1 = 0.0;
+  p.vmin = CUDART_INF;
+  p.vmax = -CUDART_INF;
+  return p;
+}
+
+// Deterministic block reduction of a Partial (fixed shuffle/shared tree).
+// STATS: also the fp64 sum/min/max of V.  Result valid in thread 0.
+template <bool STATS>
+__device__ Partial block_reduce_partial(Partial p) {
+  __shared__ Partial sh[kMaxTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  p.c = warp_sum(p.c);
+  p.births = warp_sum(p.births);
+  p.deaths = warp_sum(p.deaths);
+  p.aux = warp_sum(p.aux);
+  p.s0 = warp_sum(p.s0);
+  if (STATS) {
+    p.s1 = warp_sum(p.s1);
+    p.vmin = warp_min(p.vmin);
+    p.vmax = warp_max(p.vmax);
+  }
+  if (lane == 0) sh[wid] = p;
+  __syncthreads();
+  if (wid == 0) {
+    p = lane < nw ? sh[lane] : partial_zero();
+    p.c = warp_sum(p.c);
+    p.births = warp_sum(p.births);
+    p.deaths = warp_sum(p.deaths);
+    p.aux = warp_sum(p.aux);
+    p.s0 = warp_sum(p.s0);
+    if (STATS) {
+      p.s1 = warp_sum(p.s1);
+      p.vmin = warp_min(p.vmin);
+      p.vmax = warp_max(p.vmax);
+    }
+  }
+  __syncthreads();
+  return p;
+}
+
+__device__ __forceinline__ Partial load_partial(const Partial* p) {
+  Partial r;
+  const long long* q = (const long long*)p;
+  long long* o = (long long*)&r;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) o[k] = __ldcg(q + k);
+  return r;
+}
+
+__device__ __forceinline__ void accumulate(Partial& a, const Partial& b) {
+  a.c += b.c;
+  a.births += b.births;
+  a.deaths += b.deaths;
+  a.aux += b.aux;
+  a.s0 += b.s0;
+  a.s1 += b.s1;
+  a.vmin = fmin(a.vmin, b.vmin);
+  a.vmax = fmax(a.vmax, b.vmax);
+}
+
+__device__ __forceinline__ int replica_of(const RepTable& T, int tile) {
+  int lo = 0, hi = T.nrep - 1;
+  while (lo < hi) {  // last r with tile_off[r] <= tile
+    const int mid = (lo + hi + 1) >> 1;
+    if (T.tile_off[mid] <= tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Elects the last tile of replica `ctrl` to finish (threadFenceReduction
+// pattern, no waiting).  Every thread of the block calls it after the tile's
+// partial is written; returns true in all threads of the electing block.
+__device__ __forceinline__ bool last_tile(gbdmc_ctrl_t* ctrl, int ntiles) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(&ctrl->ticket, 1u);
+    am_last = (t == (unsigned)ntiles - 1u);
+  }
+  __syncthreads();
+  const bool r = am_last;
+  if (r) __threadfence();
+  __syncthreads();
+  return r;
+}
+
+// Fixed-order reduction of the partials of tiles [t0, t0+nt) (and, when
+// prefix != NULL, an exclusive scan of their counts into prefix[]).
+template <bool STATS>
+__device__ Partial reduce_partials(const Partial* part, int t0, int nt, long long* prefix) {
+  const int per = (nt + blockDim.x - 1) / blockDim.x;
+  const int beg = min(nt, (int)threadIdx.x * per), end = min(nt, beg + per);
+  Partial acc = partial_zero();
+  for (int j = beg; j < end; ++j) accumulate(acc, load_partial(part + t0 + j));
+  if (prefix) {
+    __shared__ long long wsum[kMaxTPB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long v = acc.c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane == 31) wsum[wid] = v;
+    __syncthreads();
+    long long base = 0;
+    for (int w = 0; w < wid; ++w) base += wsum[w];
+    long long run = base + v - acc.c;
+    for (int j = beg; j < end; ++j) {
+      prefix[t0 + j] = run;
+      run += __ldcg(&part[t0 + j].c);
+    }
+    __syncthreads();
+  }
+  return block_reduce_partial<STATS>(acc);
+}
+
+// Discrete weight and branch count of one walker (pyvibdmc.py:392-403).
+__device__ __forceinline__ int branch_count(double v, double vref, double dt, double u, double w_hi, int& flag,
+                                            long long& births, long long& deaths) {
+  const double w = exp(__dmul_rn(-__dsub_rn(v, vref), dt));
+  if (!isfinite(w)) {
+    flag |= GBDMC_ST_NONFINITE_WEIGHT;
+    return 0;
+  }
+  if (w > w_hi) {
+    flag |= GBDMC_ST_HUGE_WEIGHT;
+    return 0;
+  }
+  const double fl = floor(w);
+  const int c = (int)fl + (u < __dsub_rn(w, fl) ? 1 : 0);
+  births += c > 1 ? c - 1 : 0;
+  deaths += c == 0 ? 1 : 0;
+  return c;
+}
+
+__device__ __forceinline__ int64_t hidx(const gbdmc_sim_t& S, int r, long long step) {
+  return (int64_t)r * S.hist.len + step;
+}
+
+// Finalisation of a discrete branching pass of replica r (thread 0).
+__device__ __noinline__ static void finalize_discrete(const gbdmc_sim_t& S, const RepTable& T, int r, gbdmc_ctrl_t* ctrl,
+                                  const Partial& tot) {
+  const long long n = ctrl->n;
+  const long long step = ctrl->step;
+  const long long nn = tot.c;
+  const long long n0 = T.n0[r];
+  int st = ctrl->status | *(volatile int*)&ctrl->flags;
+  ctrl->flags = 0;
+  if (!st) {
+    const double d0 = (double)n0;
+    if ((double)nn < d0 - d0 * 0.5) st |= GBDMC_ST_POP_LOW;
+    if ((double)nn > d0 + d0 * 0.5) st |= GBDMC_ST_POP_HIGH;
+    if (nn > T.cap[r]) st |= GBDMC_ST_OVERFLOW;
+  }
+  if (st) {
+    ctrl->status = st;
+    ctrl->err_step = (int)step;
+  } else {
+    const double vbar = tot.s0 / (double)nn;
+    const double corr = (double)(nn - n0) / (double)n0;
+    const double vref = vbar - S.alpha * corr;
+    if (step < S.hist.len) {
+      const int64_t h = hidx(S, r, step);
+      if (S.hist.vref) S.hist.vref[h] = vref;
+      if (S.hist.pop) S.hist.pop[h] = (double)nn;
+      if (S.hist.births) S.hist.births[h] = (int)tot.births;
+      if (S.hist.deaths) S.hist.deaths[h] = (int)tot.deaths;
+    }
+    ctrl->n_prev = n;
+    ctrl->n = nn;
+    ctrl->vref = vref;
+    ctrl->step = step + 1;
+  }
+  ctrl->ticket = 0;
+}
+
+template <bool STATS>
+__device__ __forceinline__ void record_vstats(const gbdmc_sim_t& S, int r, long long step, long long n,
+                                              const Partial& t) {
+  if (STATS && step < S.hist.len) {
+    const int64_t h = hidx(S, r, step);
+    if (S.hist.vmin) S.hist.vmin[h] = t.vmin;
+    if (S.hist.vmax) S.hist.vmax[h] = t.vmax;
+    if (S.hist.vmean) S.hist.vmean[h] = t.s1 / (double)n;
+  }
+}
+
+template <int A>
+__device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&d2)[3 * A]) {
+  // -1/2 sum_d sum_a (1/m_a) d2psi/psi (imp_samp.py:49-53: atoms first, then dims)
+  double s = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double t = 0.0;
+#pragma unroll
+    for (int a = 0; a < A; ++a) t = t + S.inv_mass[a] * d2[3 * a + d];
+    s = s + t;
+  }
+  return -0.5 * s;
+}
+
+}  // namespace gbdmc

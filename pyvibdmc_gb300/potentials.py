@@ -21,7 +21,7 @@ import torch
 from . import _capi
 from .constants import Constants
 
-__all__ = ["Potential_GPU", "PESFunction", "harmonic_oscillator", "h2o_local_mode", "water_dimer",
+__all__ = ["Potential_GPU", "PESFunction", "harmonic_oscillator", "h2o_local_mode", "water_dimer", "WATER_DIMER_EQ",
            "to_soa", "from_soa", "default_device"]
 
 
@@ -153,6 +153,16 @@ def h2o_local_mode(De=0.1869, a=1.2, re=1.81, ktheta=0.16, theta_e_deg=104.5, kr
     1/2 k_theta (theta - theta_e)^2 and a k_rr (r1-re)(r2-re) coupling."""
     return Potential_GPU("h2o_local_mode", dict(De=De, a=a, re=re, ktheta=ktheta,
                                                 theta_e=np.deg2rad(theta_e_deg), krr=krr), device=device)
+
+
+# Minimum of the default water_dimer surface (O,H,H,O,H,H; bohr; E = -0.0108784 Eh).
+WATER_DIMER_EQ = np.array([
+    [0.000000000000, 0.000000000000, 0.000000000000],
+    [1.427477952458, -0.371496091643, 1.058267415716],
+    [-0.475355230876, -1.624174243271, -0.657060123398],
+    [-0.890893874743, 4.517468473284, -2.310760800984],
+    [-2.231456348667, 5.100851802863, -1.249695023025],
+    [-0.483907575038, 2.882598047543, -1.568314000679]])
 
 
 def water_dimer(eps=2.4e-4, sigma=5.95, qH=0.417, qO=-0.834, device=None, **monomer):

@@ -1,0 +1,427 @@
+"""MLP surrogate of the water-dimer PES: training, inference and DMC.
+
+* :class:`MLPSurrogate` -- 15 inverse O/H distances -> 3 x 128 SiLU -> 1,
+  BF16 tensor-core kernels with FP32 accumulation (libgbdmc ``gbdmc_mlp_*``).
+  Trained on geometries, energies and adjoint forces (``gbdmc_pes_eval``
+  gradients) harvested from a plain FP64 run.  Force matching uses a random
+  direction v per sample: the network's directional derivative
+  dE/dx . v = (dE/dD)(dD/dx v) is a forward tangent through the same layers,
+  and the loss gradient of that tangent is one more pass of the same GEMMs
+  (SiLU'' enters through ``gbdmc_mlp_silu_bwd``).
+* :class:`NN_Potential_GPU` -- the ``getpot`` plug-in of the reference's
+  ``NN_Potential`` (simulation_utilities/potential_manager.py:177-214).
+* :class:`NNDMC` -- discrete-weighting DMC of the dimer with fp32 walker
+  coordinates on the surrogate; a random 1/``audit_every`` of the walkers and
+  every walker outside the training box get the analytic FP64 energy, and the
+  audited differences are accumulated as the surrogate's error estimate.
+"""
+import ctypes as C
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _capi
+from .constants import Constants
+from .potentials import Potential_GPU, default_device, to_soa, from_soa
+
+__all__ = ["MLPSurrogate", "NN_Potential_GPU", "NNDMC", "harvest_training_data"]
+
+H = 128
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _s():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _bf16_bits(t):
+    """fp32 tensor -> int16 tensor holding its round-to-nearest-even bf16 bits."""
+    return t.to(torch.bfloat16).contiguous().view(torch.int16)
+
+
+class MLPSurrogate:
+    def __init__(self, device=None, seed=0):
+        self.device = torch.device(device) if device is not None else default_device()
+        g = torch.Generator().manual_seed(seed)
+        f32 = dict(dtype=torch.float32)
+
+        def rnd(*shape, std):
+            return (torch.randn(*shape, generator=g, **f32) * std).to(self.device)
+
+        W1 = rnd(16, H, std=math.sqrt(1.0 / 15))
+        W1[15].zero_()
+        self.P = dict(W1=W1, b1=torch.zeros(H, device=self.device), W2=rnd(H, H, std=math.sqrt(1.0 / H)),
+                      b2=torch.zeros(H, device=self.device), W3=rnd(H, H, std=math.sqrt(1.0 / H)),
+                      b3=torch.zeros(H, device=self.device), w4=rnd(H, std=0.1 / math.sqrt(H)),
+                      b4=torch.zeros(1, device=self.device))
+        self.M = {k: torch.zeros_like(v) for k, v in self.P.items()}
+        self.V = {k: torch.zeros_like(v) for k, v in self.P.items()}
+        self.t = 0
+        self.bf = {}
+        self._refresh_bf16()
+        self.mu = torch.zeros(16, device=self.device)
+        self.inv_sd = torch.ones(16, device=self.device)
+        self.lo = torch.full((16,), -1e30)
+        self.hi = torch.full((16,), 1e30)
+        self.e_mean, self.e_scale = 0.0, 1.0
+        self.hull_margin = 0.5
+        self.history = []
+
+    def _refresh_bf16(self):
+        P = self.P
+        self.bf = dict(W1t=_bf16_bits(P["W1"].t()), W2t=_bf16_bits(P["W2"].t()), W3t=_bf16_bits(P["W3"].t()),
+                       W2n=_bf16_bits(P["W2"]), W3n=_bf16_bits(P["W3"]))
+
+    # ---------------------------------------------------------- inference
+    def net_struct(self, audit_every=0):
+        n = _capi.MLP()
+        n.w1t, n.w2t, n.w3t = self.bf["W1t"].data_ptr(), self.bf["W2t"].data_ptr(), self.bf["W3t"].data_ptr()
+        n.b1, n.b2, n.b3 = self.P["b1"].data_ptr(), self.P["b2"].data_ptr(), self.P["b3"].data_ptr()
+        n.w4 = self.P["w4"].data_ptr()
+        n.b4 = float(self.P["b4"].item())
+        n.e_mean, n.e_scale, n.hull_margin = float(self.e_mean), float(self.e_scale), float(self.hull_margin)
+        mu, isd, lo, hi = (t.detach().cpu().numpy() for t in (self.mu, self.inv_sd, self.lo, self.hi))
+        for q in range(16):
+            n.feat_mu[q], n.feat_inv_sd[q], n.feat_lo[q], n.feat_hi[q] = mu[q], isd[q], lo[q], hi[q]
+        n.audit_every = int(audit_every)
+        return n
+
+    def energy_soa(self, x32, n, ld=None):
+        """Surrogate energies (float64 tensor) of fp32 SoA walkers; also the out-of-box mask."""
+        L = _capi.load()
+        ld = x32.shape[1] if ld is None else ld
+        v = torch.empty(max(n, 1), dtype=torch.float64, device=self.device)
+        out = torch.zeros(max(n, 1), dtype=torch.int32, device=self.device)
+        _capi.check(L.gbdmc_mlp_energy(C.byref(self.net_struct()), _p(x32), ld, n, _p(v), _p(out), _s()),
+                    "gbdmc_mlp_energy")
+        return v[:n], out[:n]
+
+    def energy(self, cds):
+        cds = np.asarray(cds, dtype=np.float64)
+        x32 = to_soa(cds, self.device, dtype=torch.float32)
+        return self.energy_soa(x32, len(cds))[0].cpu().numpy()
+
+    # ----------------------------------------------------------- training
+    def set_normalisation(self, x, v):
+        """Descriptor mean/scale and energy mean/scale from training data (x fp64 SoA (18, M))."""
+        L = _capi.load()
+        m = x.shape[1]
+        feat = torch.empty(m, 16, dtype=torch.float32, device=self.device)
+        zeros, ones = torch.zeros(16, device=self.device), torch.ones(16, device=self.device)
+        _capi.check(L.gbdmc_dimer_features(_p(x), m, m, _p(zeros), _p(ones), None, None, 1.0, _p(feat), None, None,
+                                           _s()), "gbdmc_dimer_features")
+        mu = feat.mean(0)
+        sd = feat.std(0).clamp_min(1e-6)
+        mu[15], sd[15] = 0.0, 1.0
+        self.mu, self.inv_sd = mu, 1.0 / sd
+        fn = (feat - mu) / sd
+        self.lo, self.hi = fn.min(0).values, fn.max(0).values
+        self.e_mean = float(v.mean())
+        self.e_scale = float(v.std())
+
+    def _features(self, xb, gb, vdir, feat, tang, et):
+        L = _capi.load()
+        n = xb.shape[1]
+        _capi.check(L.gbdmc_dimer_features(_p(xb), n, n, _p(self.mu), _p(self.inv_sd), _p(vdir), _p(gb),
+                                           float(self.e_scale), _p(feat), _p(tang), _p(et), _s()),
+                    "gbdmc_dimer_features")
+
+    def _alloc(self, B):
+        f = lambda *s: torch.empty(*s, dtype=torch.float32, device=self.device)  # noqa: E731
+        self.buf = dict(feat=f(B, 16), tang=f(B, 16), et=f(B), e=f(B), ones=torch.ones(B, 16, device=self.device),
+                        **{f"{k}{l}": f(B, H) for k in ("Z", "Zt", "H", "Ht", "Zb", "Ztb", "Hb", "Htb")
+                           for l in (1, 2, 3)},
+                        loss=torch.zeros(2, dtype=torch.float64, device=self.device))
+        self.grads = {k: torch.zeros_like(v) for k, v in self.P.items()}
+        self.g16 = torch.zeros(16, H, device=self.device)
+
+    def train_batch(self, xb, vb, gb, lr, w_e=1.0, w_f=0.5):
+        """One Adam step on a minibatch (x (18, B) fp64, V (B,), dV/dx (18, B)); returns (mse_E, mse_F)."""
+        L = _capi.load()
+        B = xb.shape[1]
+        if getattr(self, "buf", None) is None or self.buf["feat"].shape[0] != B:
+            self._alloc(B)
+        b, P, bf, G = self.buf, self.P, self.bf, self.grads
+        vdir = torch.randn(18, B, dtype=torch.float64, device=self.device)
+        vdir /= vdir.norm(dim=0, keepdim=True)
+        self._features(xb, gb, vdir, b["feat"], b["tang"], b["et"])
+        b["e"].copy_(((vb - self.e_mean) / self.e_scale).float())
+        s = _s()
+        ck = _capi.check
+        # forward: primal and tangent streams
+        ck(L.gbdmc_mlp_gemm(_p(b["feat"]), B, 16, _p(bf["W1t"]), _p(P["b1"]), _p(b["Z1"]), s), "gemm")
+        ck(L.gbdmc_mlp_gemm(_p(b["tang"]), B, 16, _p(bf["W1t"]), None, _p(b["Zt1"]), s), "gemm")
+        ck(L.gbdmc_mlp_silu_fwd(_p(b["Z1"]), _p(b["Zt1"]), _p(b["H1"]), _p(b["Ht1"]), B * H, s), "silu")
+        for l, (wt, bias) in ((2, ("W2t", "b2")), (3, ("W3t", "b3"))):
+            ck(L.gbdmc_mlp_gemm(_p(b[f"H{l-1}"]), B, H, _p(bf[wt]), _p(P[bias]), _p(b[f"Z{l}"]), s), "gemm")
+            ck(L.gbdmc_mlp_gemm(_p(b[f"Ht{l-1}"]), B, H, _p(bf[wt]), None, _p(b[f"Zt{l}"]), s), "gemm")
+            ck(L.gbdmc_mlp_silu_fwd(_p(b[f"Z{l}"]), _p(b[f"Zt{l}"]), _p(b[f"H{l}"]), _p(b[f"Ht{l}"]), B * H, s),
+               "silu")
+        for g in G.values():
+            g.zero_()
+        b["loss"].zero_()
+        ck(L.gbdmc_mlp_head(_p(b["H3"]), _p(b["Ht3"]), _p(P["w4"]), float(P["b4"].item()), _p(b["e"]), _p(b["et"]),
+                            B, w_e, w_f, _p(b["Hb3"]), _p(b["Htb3"]), _p(G["w4"]), _p(G["b4"]), _p(b["loss"]), s),
+           "head")
+        # backward
+        for l in (3, 2, 1):
+            ck(L.gbdmc_mlp_silu_bwd(_p(b[f"Z{l}"]), _p(b[f"Zt{l}"]), _p(b[f"Hb{l}"]), _p(b[f"Htb{l}"]),
+                                    _p(b[f"Zb{l}"]), _p(b[f"Ztb{l}"]), B * H, s), "silu_bwd")
+            K = H if l > 1 else 16
+            xin, xtin = (b[f"H{l-1}"], b[f"Ht{l-1}"]) if l > 1 else (b["feat"], b["tang"])
+            ck(L.gbdmc_mlp_gemm_tn(_p(xin), _p(b[f"Zb{l}"]), B, K, _p(G[f"W{l}"]), s), "gemm_tn")
+            ck(L.gbdmc_mlp_gemm_tn(_p(xtin), _p(b[f"Ztb{l}"]), B, K, _p(G[f"W{l}"]), s), "gemm_tn")
+            self.g16.zero_()
+            ck(L.gbdmc_mlp_gemm_tn(_p(b["ones"]), _p(b[f"Zb{l}"]), B, 16, _p(self.g16), s), "gemm_tn")
+            G[f"b{l}"].copy_(self.g16[0])
+            if l > 1:
+                wn = bf[f"W{l}n"]
+                ck(L.gbdmc_mlp_gemm(_p(b[f"Zb{l}"]), B, H, _p(wn), None, _p(b[f"Hb{l-1}"]), s), "gemm")
+                ck(L.gbdmc_mlp_gemm(_p(b[f"Ztb{l}"]), B, H, _p(wn), None, _p(b[f"Htb{l-1}"]), s), "gemm")
+        G["W1"][15].zero_()
+        self.t += 1
+        for k, p in P.items():
+            wt = bf.get(f"{k}t") if k in ("W1", "W2", "W3") else None
+            wn = bf.get(f"{k}n") if k in ("W2", "W3") else None
+            K = 16 if k == "W1" else H
+            ck(L.gbdmc_mlp_adam(_p(p), _p(G[k]), _p(self.M[k]), _p(self.V[k]), p.numel(), lr, 0.9, 0.999, 1e-8,
+                                self.t, _p(wt), _p(wn), K, s), "adam")
+        return b["loss"] / B
+
+    def fit(self, x, v, g, epochs=20, batch=4096, lr=2e-3, lr_final=5e-5, w_f=0.5, seed=0, verbose=False):
+        """Train on harvested data: x, g fp64 SoA (18, M) device tensors, v (M,) fp64."""
+        self.set_normalisation(x, v)
+        M = x.shape[1]
+        steps = epochs * (M // batch)
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        k = 0
+        t0 = time.perf_counter()
+        for ep in range(epochs):
+            perm = torch.randperm(M, device=self.device, generator=gen)
+            tot = torch.zeros(2, dtype=torch.float64, device=self.device)
+            nb = M // batch
+            for i in range(nb):
+                idx = perm[i * batch:(i + 1) * batch]
+                lr_k = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps, 1)))
+                tot += self.train_batch(x[:, idx].contiguous(), v[idx], g[:, idx].contiguous(), lr_k, w_f=w_f)
+                k += 1
+            rec = dict(epoch=ep, mse_e=float(tot[0] / nb), mse_f=float(tot[1] / nb),
+                       rmse_e_cm=math.sqrt(float(tot[0] / nb)) * self.e_scale / Constants.atomic_units["wavenumbers"])
+            self.history.append(rec)
+            if verbose:
+                print(rec, flush=True)
+        torch.cuda.synchronize()
+        self.train_seconds = time.perf_counter() - t0
+        return self
+
+    def state_dict(self):
+        return dict(P={k: v.detach().cpu() for k, v in self.P.items()}, mu=self.mu.cpu(), inv_sd=self.inv_sd.cpu(),
+                    lo=self.lo.cpu(), hi=self.hi.cpu(), e_mean=self.e_mean, e_scale=self.e_scale,
+                    hull_margin=self.hull_margin)
+
+    def load_state_dict(self, st):
+        for k, v in st["P"].items():
+            self.P[k] = v.to(self.device)
+        self.mu, self.inv_sd = st["mu"].to(self.device), st["inv_sd"].to(self.device)
+        self.lo, self.hi = st["lo"], st["hi"]
+        self.e_mean, self.e_scale, self.hull_margin = st["e_mean"], st["e_scale"], st["hull_margin"]
+        self._refresh_bf16()
+        return self
+
+
+class NN_Potential_GPU:
+    """``getpot(cds, timeit=False)`` of a trained surrogate (the NN_Potential
+    contract of potential_manager.py:177-214, model held by the object)."""
+
+    def __init__(self, surrogate):
+        self.model = surrogate
+        self.natoms = 6
+
+    def getpot(self, cds, timeit=False):
+        t0 = time.time()
+        v = self.model.energy(cds)
+        return (v, time.time() - t0) if timeit else v
+
+
+def harvest_training_data(potential, num_walkers, nsteps, every, start, masses, delta_t=10.0, seed=0, equil=0):
+    """Plain FP64 DMC of `potential` (the analytic dimer); every `every` steps
+    after `equil` the walkers, their energies and adjoint gradients are kept
+    on the device.  Returns x (18, M), v (M,), g (18, M) fp64 tensors."""
+    from .engine import DMC_Sim
+    xs, vs, gs = [], [], []
+
+    def sink(t, x, v, n):
+        if t < equil:
+            return
+        xx = x[:, :n].clone()
+        vv, gg = potential.eval_soa(xx, n, grad=True)
+        xs.append(xx)
+        vs.append(vv.clone())
+        gs.append(gg)
+
+    sim = DMC_Sim(num_walkers=num_walkers, num_timesteps=nsteps, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                  masses=list(masses), delta_t=delta_t, potential=potential, start_structures=start, seed=seed,
+                  DEBUG_save_training_every=every, training_sink=sink, write_files=False)
+    sim.run()
+    return torch.cat(xs, 1), torch.cat(vs), torch.cat(gs, 1), sim
+
+
+class NNDMC:
+    """Surrogate DMC of the water dimer (discrete weighting, fp32 coordinates)."""
+
+    def __init__(self, surrogate, potential, num_walkers, start_structures, masses, delta_t, num_timesteps, seed=0,
+                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0):
+        if not isinstance(potential, Potential_GPU) or potential.kind != "water_dimer":
+            raise TypeError("the audit/fallback potential must be the analytic water_dimer Potential_GPU")
+        self.model, self.potential = surrogate, potential
+        self.device = surrogate.device
+        self.n0 = int(num_walkers)
+        self.T = int(num_timesteps)
+        self.dt = float(delta_t)
+        self.masses = np.asarray(masses, dtype=np.float64)
+        self.audit_every = int(audit_every)
+        self.graph_steps = max(2, int(graph_steps) // 2 * 2)
+        self.rng = rng
+        ss = np.asarray(start_structures, dtype=np.float64)
+        x0 = np.repeat(ss, self.n0, axis=0) if ss.shape[0] == 1 else ss
+        cap = ((int(np.floor(self.n0 + self.n0 * 0.5)) + 1) + 127) // 128 * 128
+        self.ld = cap
+        dev = self.device
+        self._bufs = [dict(x=torch.zeros(18, cap, dtype=torch.float32, device=dev),
+                           v=torch.zeros(cap, dtype=torch.float64, device=dev),
+                           who=torch.zeros(cap, dtype=torch.int32, device=dev),
+                           idx=torch.zeros(cap, dtype=torch.int32, device=dev)) for _ in range(2)]
+        self._bufs[0]["x"][:, :len(x0)] = to_soa(x0, dev, dtype=torch.float32)
+        self._cur, self._lazy = 0, False
+        L = _capi.load()
+        self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
+        self._scratch = torch.zeros(L.gbdmc_scratch_bytes(cap), dtype=torch.uint8, device=dev)
+        self._audit = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._hist = dict(vref=torch.zeros(self.T, dtype=torch.float64, device=dev),
+                          pop=torch.zeros(self.T, dtype=torch.float64, device=dev))
+        s = _capi.Sim()
+        s.natoms, s.weighting, s.track_who, s.ld, s.n0 = 6, _capi.DISCRETE, 1, cap, self.n0
+        s.noise_mode = _capi.NOISE_PHILOX32 if isinstance(rng, str) else _capi.NOISE_INJECTED
+        s.dt, s.alpha = self.dt, 1.0 / (2.0 * self.dt)
+        for a in range(6):
+            s.sigma[a] = float(np.sqrt(self.dt / self.masses[a]))
+            s.inv_mass[a] = float(1.0 / self.masses[a])
+        s.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        s.replica_id = int(replica_id)
+        s.pes = potential.pes_struct()
+        s.trial.kind, s.trial.natoms = _capi.TRIAL_NONE, 6
+        s.hist.vref, s.hist.pop, s.hist.len = self._hist["vref"].data_ptr(), self._hist["pop"].data_ptr(), self.T
+        self._sim = s
+        self._net = surrogate.net_struct(audit_every)
+        self._n_start = len(x0)
+        self._graphs = {}
+        self.step = 0
+
+    def _w(self, b, with_idx):
+        w = _capi.WalkersF32()
+        w.x, w.v, w.who = b["x"].data_ptr(), b["v"].data_ptr(), b["who"].data_ptr()
+        if with_idx:
+            w.idx = b["idx"].data_ptr()
+        return w
+
+    def ctrl(self):
+        return _capi.Ctrl.from_buffer_copy(self._ctrl.cpu().numpy().tobytes())
+
+    def init(self):
+        c = _capi.Ctrl()
+        c.n = self._n_start
+        self._ctrl.copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
+        L = _capi.load()
+        _capi.check(L.gbdmc_mlp_sim_init(C.byref(self._sim), C.byref(self._net),
+                                         C.byref(self._w(self._bufs[self._cur], False)), _p(self._ctrl),
+                                         _p(self._scratch), _s()), "gbdmc_mlp_sim_init")
+        return self
+
+    def _launch(self, cur, lazy, noise=None):
+        L = _capi.load()
+        _capi.check(L.gbdmc_mlp_sim_step(C.byref(self._sim), C.byref(self._net),
+                                         C.byref(self._w(self._bufs[cur], lazy)),
+                                         C.byref(self._w(self._bufs[1 - cur], True)), _p(self._ctrl),
+                                         _p(self._scratch), _p(self._audit),
+                                         C.byref(noise) if noise is not None else None, _s()), "gbdmc_mlp_sim_step")
+        return 1 - cur, True
+
+    def _graph(self, cur):
+        g = self._graphs.get(cur)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                c, lz = cur, True
+                for _ in range(self.graph_steps):
+                    c, lz = self._launch(c, lz)
+            torch.cuda.current_stream().wait_stream(side)
+            self._graphs[cur] = g
+        return g
+
+    def run(self, nsteps):
+        if not isinstance(self.rng, str):
+            for _ in range(nsteps):
+                n = int(self.ctrl().n)
+                z = np.asarray(self.rng.standard_normal((n, 3, 6)), dtype=np.float64)
+                zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(18, n)), device=self.device)
+                ub = torch.as_tensor(self.rng.uniform(n), device=self.device)
+                nz = _capi.Noise()
+                nz.normal, nz.u_branch, nz.ld_noise = zs.data_ptr(), ub.data_ptr(), n
+                self._cur, self._lazy = self._launch(self._cur, self._lazy, nz)
+                torch.cuda.synchronize()
+            self.step += nsteps
+            return self._check()
+        done = 0
+        if nsteps and not self._lazy:
+            self._cur, self._lazy = self._launch(self._cur, self._lazy)
+            done = 1
+        while nsteps - done >= self.graph_steps:
+            self._graph(self._cur).replay()
+            done += self.graph_steps
+        while done < nsteps:
+            self._cur, self._lazy = self._launch(self._cur, True)
+            done += 1
+        self.step += nsteps
+        return self._check()
+
+    def _check(self):
+        c = self.ctrl()
+        if c.status:
+            raise ValueError(f"Massive walker birth or death event!!!!!!! Dying... (status {c.status})")
+        return self
+
+    def vref_history(self):
+        return self._hist["vref"][:self.step].cpu().numpy()
+
+    def pop_history(self):
+        return self._hist["pop"][:self.step].cpu().numpy()
+
+    def zpe(self, start=None, nblocks=20):
+        from .batch import blocking_error
+        v = Constants.convert(self.vref_history(), "wavenumbers", to_AU=False)
+        start = len(v) // 4 if start is None else start
+        return blocking_error(v[start:], nblocks)
+
+    def audit(self):
+        """(audited walkers, mean and RMS of V_nn - V_analytic in cm^-1, fallbacks)."""
+        a = self._audit.cpu().numpy()
+        n = max(a[0], 1.0)
+        w = Constants.atomic_units["wavenumbers"]
+        return dict(audited=int(a[0]), mean_cm=a[1] / n / w, rms_cm=math.sqrt(a[2] / n) / w, fallbacks=int(a[3]))
+
+    def walkers(self):
+        if self._lazy:
+            L = _capi.load()
+            _capi.check(L.gbdmc_mlp_compact(C.byref(self._sim), C.byref(self._w(self._bufs[self._cur], True)),
+                                            C.byref(self._w(self._bufs[1 - self._cur], False)), _p(self._ctrl),
+                                            _s()), "gbdmc_mlp_compact")
+            self._cur, self._lazy = 1 - self._cur, False
+        n = int(self.ctrl().n)
+        return from_soa(self._bufs[self._cur]["x"], n, 6)

@@ -1,0 +1,138 @@
+"""MLP surrogate kernels (BF16 tensor cores, FP32 accumulation) against a
+plain PyTorch fp32 reference and the NumPy oracle of the force-matching loss.
+
+Tolerances: GEMMs with bf16-rounded operands agree with torch fp32 on the same
+rounded operands to 1e-4 relative; quantities that round activations to bf16
+between layers agree with the fp64 oracle to a few 1e-2 relative (bf16 keeps
+8 mantissa bits)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from oracle import mlp_oracle as mo
+import pyvibdmc_gb300 as pg
+from pyvibdmc_gb300 import _capi
+from pyvibdmc_gb300.surrogate import MLPSurrogate, NNDMC, harvest_training_data, _p, _s
+
+pytestmark = pytest.mark.gpu
+
+
+def bf(t):
+    return t.to(torch.bfloat16).float()
+
+
+@pytest.mark.parametrize("K", [16, 128])
+@pytest.mark.parametrize("M", [1, 37, 1000, 4096])
+def test_gemm_xw_matches_torch(K, M):
+    L = _capi.load()
+    g = torch.Generator(device="cuda").manual_seed(K + M)
+    X = torch.randn(M, K, device="cuda", generator=g)
+    W = torch.randn(K, 128, device="cuda", generator=g) / np.sqrt(K)
+    b = torch.randn(128, device="cuda", generator=g)
+    Wt = W.t().contiguous().to(torch.bfloat16).view(torch.int16)
+    Y = torch.empty(M, 128, device="cuda")
+    _capi.check(L.gbdmc_mlp_gemm(_p(X), M, K, _p(Wt), _p(b), _p(Y), _s()))
+    ref = bf(X) @ bf(W) + b
+    torch.testing.assert_close(Y, ref, rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.parametrize("K", [16, 128])
+@pytest.mark.parametrize("M", [5, 64, 3001])
+def test_gemm_tn_matches_torch(K, M):
+    L = _capi.load()
+    g = torch.Generator(device="cuda").manual_seed(7 * K + M)
+    X = torch.randn(M, K, device="cuda", generator=g)
+    D = torch.randn(M, 128, device="cuda", generator=g)
+    G = torch.ones(K, 128, device="cuda")
+    _capi.check(L.gbdmc_mlp_gemm_tn(_p(X), _p(D), M, K, _p(G), _s()))
+    ref = 1.0 + bf(X).t() @ bf(D)
+    torch.testing.assert_close(G, ref, rtol=1e-4, atol=1e-3)
+
+
+def test_features_match_oracle():
+    x = oracle.dimer_equilibrium()[None] + 0.1 * oracle.InjectedNoise(3).standard_normal((300, 6, 3))
+    v = oracle.InjectedNoise(4).standard_normal((300, 6, 3))
+    p, _ = oracle.dimer_config()
+    grad = oracle.grad_dimer(x, p)
+    f_ref, t_ref = mo.inv_dist_features(x, v)
+    mu = torch.linspace(0.1, 0.3, 16, device="cuda")
+    isd = torch.linspace(1.0, 2.0, 16, device="cuda")
+    L = _capi.load()
+    xs, vs, gs = (pg.to_soa(a, "cuda") for a in (x, v, grad))
+    feat = torch.empty(300, 16, device="cuda")
+    tang = torch.empty(300, 16, device="cuda")
+    et = torch.empty(300, device="cuda")
+    _capi.check(L.gbdmc_dimer_features(_p(xs), 300, 300, _p(mu), _p(isd), _p(vs), _p(gs), 0.01, _p(feat), _p(tang),
+                                       _p(et), _s()))
+    mu_, isd_ = mu.cpu().numpy()[:15], isd.cpu().numpy()[:15]
+    np.testing.assert_allclose(feat.cpu().numpy()[:, :15], (f_ref - mu_) * isd_, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(tang.cpu().numpy()[:, :15], t_ref * isd_, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(et.cpu().numpy(), (grad * v).sum((1, 2)) / 0.01, rtol=1e-4, atol=1e-4)
+
+
+def _small_model(seed=0):
+    m = MLPSurrogate(seed=seed)
+    x = oracle.dimer_equilibrium()[None] + 0.1 * oracle.InjectedNoise(seed + 10).standard_normal((2048, 6, 3))
+    p, _ = oracle.dimer_config()
+    xs = pg.to_soa(x, "cuda")
+    v = torch.as_tensor(oracle.pes_dimer(x, p), device="cuda")
+    g = pg.to_soa(oracle.grad_dimer(x, p), "cuda")
+    m.set_normalisation(xs, v)
+    return m, x, xs, v, g
+
+
+def test_training_gradients_match_oracle():
+    m, x, xs, v, g = _small_model(1)
+    P0 = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
+    torch.manual_seed(0)
+    torch.cuda.manual_seed(0)
+    m.train_batch(xs, v, g, lr=0.0)  # lr 0: gradients only (Adam with lr 0 leaves the parameters)
+    Gg = {k: t.detach().cpu().double().numpy() for k, t in m.grads.items()}
+    b = m.buf
+    D = b["feat"].cpu().double().numpy()
+    U = b["tang"].cpu().double().numpy()
+    e = b["e"].cpu().double().numpy()
+    et = b["et"].cpu().double().numpy()
+    P0["b4"] = P0["b4"][0]
+    Go, loss = mo.mlp_loss_grads(P0, D, U, e, et, 1.0, 0.5)
+    Go["W1"][15] = 0.0
+    for k in Go:
+        a, r = Gg[k].ravel(), np.ravel(Go[k])
+        rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+        assert rel < 5e-2, (k, rel)
+    for k, t in m.P.items():
+        np.testing.assert_array_equal(t.detach().cpu().double().numpy().ravel(), np.ravel(P0[k]))
+
+
+def test_inference_kernel_matches_oracle_forward():
+    m, x, xs, v, g = _small_model(2)
+    for _ in range(30):
+        m.train_batch(xs, v, g, lr=2e-3)
+    P = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
+    P["b4"] = P["b4"][0]
+    f, _ = mo.inv_dist_features(x)
+    mu, isd = m.mu.cpu().double().numpy(), m.inv_sd.cpu().double().numpy()
+    D = np.zeros((len(x), 16))
+    D[:, :15] = (f - mu[:15]) * isd[:15]
+    E, _, _ = mo.mlp_forward(P, D)
+    ref = m.e_mean + m.e_scale * E
+    got = m.energy(x)
+    err = np.abs(got - ref) / m.e_scale
+    assert np.median(err) < 1e-2 and err.max() < 5e-2, (np.median(err), err.max())
+
+
+def test_training_reduces_loss_and_surrogate_dmc_runs():
+    p, masses = oracle.dimer_config()
+    pot = pg.water_dimer()
+    x, v, g, _ = harvest_training_data(pot, 4000, 120, 10, pg.WATER_DIMER_EQ[None], masses, seed=3, equil=20)
+    m = MLPSurrogate(seed=0).fit(x, v, g, epochs=12, batch=2048, lr=3e-3)
+    h = m.history
+    assert h[-1]["mse_e"] < 0.2 * h[0]["mse_e"]
+    assert h[-1]["mse_f"] < 0.5 * h[0]["mse_f"]
+    nd = NNDMC(m, pot, 3000, pg.WATER_DIMER_EQ[None], masses, 10.0, 200, seed=1, audit_every=10).init()
+    nd.run(200)
+    a = nd.audit()
+    assert a["audited"] > 0
+    assert np.isfinite(nd.vref_history()).all()
+    assert len(nd.walkers()) == int(nd.ctrl().n)
