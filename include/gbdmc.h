@@ -230,6 +230,24 @@ int gbdmc_walkers_compact(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, i
                           const gbdmc_walkers_t* in, const gbdmc_walkers_t* out,
                           const gbdmc_ctrl_t* ctrl_dev, void* stream);
 
+/* Allocation-free step (no counterpart in the reference).  For callers that
+ * cannot allocate device memory -- e.g. code running while a CUDA graph is
+ * being captured, or a plug-in that is handed only its input and output
+ * buffers -- this is gbdmc_sim_step with its scratch taken from a static
+ * device array of GBDMC_STATIC_SCRATCH_BYTES (1 MiB) inside the library, so
+ * sim->ld is limited to gbdmc_sim_step_static_max_ld() walkers (larger ld
+ * returns GBDMC_ERR_CAPACITY).  It calls no allocator.  The array is held
+ * by every GPU that loads the library until the process exits.  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller.  The
+ * scratch needs no zeroing between calls; every word a step reads is written
+ * earlier in the same step. */
+int gbdmc_sim_step_static(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                          gbdmc_ctrl_t* ctrl_dev, const gbdmc_noise_t* noise, void* stream);
+size_t gbdmc_sim_step_static_max_ld(void);
+
 /* Descendant weights: desc_dev[q] = #walkers (or sum of weights, w_dev != NULL)
  * whose ancestor id is q; desc_dev has n_parent entries and is overwritten. */
 int gbdmc_desc_weights(const int32_t* who_dev, const double* w_dev, const int64_t* n_dev,

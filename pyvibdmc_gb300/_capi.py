@@ -130,6 +130,9 @@ def load():
         "gbdmc_mlp_sim_step": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P,
                                 P, C.POINTER(Noise), P], C.c_int),
         "gbdmc_mlp_compact": ([C.POINTER(Sim), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P], C.c_int),
+        "gbdmc_sim_step_static": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, C.POINTER(Noise), P],
+                                  C.c_int),
+        "gbdmc_sim_step_static_max_ld": ([], C.c_size_t),
         "gbdmc_prof_enable": ([C.c_int32], C.c_int),
         "gbdmc_prof_read": ([C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                              C.POINTER(C.c_int64)], C.c_int),

@@ -22,6 +22,7 @@
 // dt_eff = dt * accepted/N) and k_branch.  Continuous weighting replaces
 // count/branch by k_cont_branch, one CTA per replica (sequential argmax
 // cloning, pyvibdmc.py:340-356, :432-454).
+#include <mutex>
 #include "gbdmc_device.cuh"
 #include "gbdmc_internal.cuh"
 
@@ -1034,4 +1035,71 @@ extern "C" int gbdmc_desc_begin(int32_t* who, const int64_t* n_dev, void* stream
   }
   k_iota<<<2 * num_sms(), 256, 0, (cudaStream_t)stream>>>(who, n_dev);
   return check_launch("gbdmc_desc_begin");
+}
+
+// ------------------------------------------------ allocation-free variant
+// Step scratch for callers that cannot allocate device memory.  The array
+// lives in the library's own device image: every GPU that loads libgbdmc.so
+// holds these bytes until the process exits, and every call shares them.
+#define GBDMC_STATIC_SCRATCH_BYTES (1u << 20)
+static __device__ __align__(256) unsigned char g_static_scratch[GBDMC_STATIC_SCRATCH_BYTES];
+
+namespace gbdmc {
+// Device address of g_static_scratch, looked up once per device.
+static void* g_static_scratch_ptr[64] = {nullptr};
+static std::mutex g_static_scratch_mu;
+
+static int static_scratch_ptr(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error("gbdmc_sim_step_static: cudaGetDevice: %s", e != cudaSuccess ? cudaGetErrorString(e) : "device id >= 64");
+    return GBDMC_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_static_scratch_mu);
+  if (!g_static_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("gbdmc_sim_step_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+      return GBDMC_ERR_CUDA;
+    }
+    g_static_scratch_ptr[dev] = p;
+  }
+  *out = g_static_scratch_ptr[dev];
+  return GBDMC_OK;
+}
+}  // namespace gbdmc
+
+extern "C" size_t gbdmc_sim_step_static_max_ld(void) {
+  // largest capacity whose step scratch fits the static array
+  int64_t lo = 1, hi = (int64_t)GBDMC_STATIC_SCRATCH_BYTES;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) / 2;
+    if (gbdmc_scratch_bytes(mid) <= GBDMC_STATIC_SCRATCH_BYTES) lo = mid; else hi = mid - 1;
+  }
+  return (size_t)lo;
+}
+
+extern "C" int gbdmc_sim_step_static(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                                     gbdmc_ctrl_t* ctrl, const gbdmc_noise_t* noise, void* stream) {
+  if (!S || !dst) {
+    set_error("gbdmc_sim_step_static: null argument");
+    return GBDMC_ERR_ARG;
+  }
+  if (S->n0 < 1) {
+    set_error("gbdmc_sim_step_static: n0 must be >= 1");
+    return GBDMC_ERR_ARG;
+  }
+  if (S->ld < 1 || gbdmc_scratch_bytes(S->ld) > GBDMC_STATIC_SCRATCH_BYTES) {
+    set_error("gbdmc_sim_step_static: ld %lld needs %zu scratch bytes; the static scratch holds %u (ld <= %zu)",
+              (long long)S->ld, gbdmc_scratch_bytes(S->ld), GBDMC_STATIC_SCRATCH_BYTES,
+              gbdmc_sim_step_static_max_ld());
+    return GBDMC_ERR_CAPACITY;
+  }
+  void* scratch = nullptr;
+  const int rc = static_scratch_ptr(&scratch);
+  if (rc) return rc;
+  const gbdmc_replica_t r = single_replica(S);
+  return step_common(S, &r, 1, src, dst, ctrl, scratch, noise, stream, "gbdmc_sim_step_static");
 }
