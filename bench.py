@@ -349,6 +349,11 @@ def run_ours(args):
                          "kernel_avg_us": move_avg_s * 1e6, "scatter_avg_us": sc_ms.value / max(sc_n.value, 1) * 1e3,
                          "fp64_fma_probe_tflops": fp64_tflops},
             "e2e": e2e}
+    if not args.no_extras and world == 1:
+        try:
+            line["extras"] = run_extras(max(64, min(K, 400)))
+        except Exception as exc:  # the headline line must still print
+            line["extras"] = {"error": repr(exc)[:300]}
     if rank == 0 and world == 1:
         rate, secs = cpu_reference_rate(N_WALKERS, 150, 1)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
@@ -359,6 +364,90 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _timed_graph_rate(run_steps, pop_of, steps):
+    """walker-steps/s of `steps` queued steps (CUDA events around them)."""
+    import torch
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = pop_of()
+    e0.record(s)
+    run_steps(steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return t0, e0.elapsed_time(e1) / 1e3
+
+
+def run_extras(steps):
+    """The other workloads of the metric, measured on the same GPU (walkers
+    resident on the device, back-to-back graph-captured steps)."""
+    import torch
+    import pyvibdmc_gb300 as pg
+    out = {}
+    masses = [pg.Constants.mass("O"), pg.Constants.mass("H"), pg.Constants.mass("H")]
+    # importance-sampled H2O, 50000 walkers
+    sim = pg.DMC_Sim(num_walkers=50000, num_timesteps=steps + 64, equil_steps=10 ** 9, atoms=["O", "H", "H"],
+                     masses=masses, delta_t=DT, potential=pg.h2o_local_mode(), imp_samp=pg.h2o_gaussian_trial(),
+                     start_structures=start_structures(50000, 7), seed=11, write_files=False, graph_steps=16)
+    sim._init_device()
+    sim._run_steps(32)
+    torch.cuda.synchronize()
+    s0 = int(sim._read_ctrl().step)
+    _, secs = _timed_graph_rate(sim._run_steps, lambda: 0, steps)
+    pop = sim._hist["pop"][s0 - 1:s0 - 1 + steps].cpu().numpy()
+    rej = sim._hist["rejected"][s0:s0 + steps].cpu().numpy()
+    out["is_h2o_50k"] = {"walker_steps_per_s": float(pop.sum()) / secs, "us_per_step": secs / steps * 1e6,
+                         "acceptance": float(1 - rej.sum() / pop.sum())}
+    # batched ensemble: 64 replicas, N_r ~ U[1000, 65536] (seeded)
+    ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
+    th = np.deg2rad(104.5)
+    eq = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [1.81 * np.cos(th), 1.81 * np.sin(th), 0.0]])
+    b = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, steps + 64, seed=3, start_noise=0.05,
+                     graph_steps=16)
+    b.init()
+    tune = b.autotune(steps_per_candidate=3)
+    b.run(16)
+    torch.cuda.synchronize()
+    t0 = b.step
+    _, secs = _timed_graph_rate(lambda k: b.run(k, check=False), lambda: 0, steps)
+    b.check()
+    ws = b.walker_steps(t0, t0 + steps)
+    out["batched_64_replicas"] = {"walkers_total": int(sum(ns)), "walker_steps_per_s": ws / secs,
+                                  "us_per_step": secs / steps * 1e6,
+                                  "tile_width_per_bucket": {str(k): v[0] for k, v in tune.items()}}
+    # surrogate dimer (200000 walkers) vs the analytic fp64 dimer
+    dm = [pg.Constants.mass(a) for a in ("O", "H", "H", "O", "H", "H")]
+    pot = pg.water_dimer()
+    t_h = time.perf_counter()
+    x, v, g, _ = pg.harvest_training_data(pot, 200000, 210, 20, pg.WATER_DIMER_EQ[None], dm, seed=1, equil=20)
+    torch.cuda.synchronize()
+    t_h = time.perf_counter() - t_h
+    t_t = time.perf_counter()
+    m = pg.MLPSurrogate(seed=0).fit(x, v, g, epochs=10, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
+    t_t = time.perf_counter() - t_t
+    nd = pg.NNDMC(m, pot, 200000, pg.WATER_DIMER_EQ[None], dm, DT, steps + 64, seed=5, audit_every=100).init()
+    nd.run(32)
+    torch.cuda.synchronize()
+    s0 = nd.step
+    _, secs = _timed_graph_rate(nd.run, lambda: 0, steps)
+    ph = nd._hist["pop"][s0 - 1:s0 - 1 + steps].cpu().numpy()
+    fp = pg.DMC_Sim(num_walkers=200000, num_timesteps=steps + 64, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                    masses=dm, delta_t=DT, potential=pot, start_structures=pg.WATER_DIMER_EQ[None], seed=5,
+                    write_files=False)
+    fp._init_device()
+    fp._run_steps(32)
+    torch.cuda.synchronize()
+    f0 = int(fp._read_ctrl().step)
+    _, fsecs = _timed_graph_rate(fp._run_steps, lambda: 0, steps)
+    pf = fp._hist["pop"][f0 - 1:f0 - 1 + steps].cpu().numpy()
+    out["surrogate_dimer_200k"] = {"walker_steps_per_s": float(ph.sum()) / secs, "us_per_step": secs / steps * 1e6,
+                                   "fp64_analytic_walker_steps_per_s": float(pf.sum()) / fsecs,
+                                   "fp64_analytic_us_per_step": fsecs / steps * 1e6,
+                                   "harvest_s": t_h, "train_s": t_t, "train_samples": int(x.shape[1]),
+                                   "train_rmse_cm": m.history[-1]["rmse_e_cm"], "audit": nd.audit()}
+    return out
 
 
 def run_e2e(sim, L, dev, steps):
@@ -408,6 +497,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extras", dest="no_extras", action="store_true",
+                    help="skip the IS / batched / surrogate workloads reported under 'extras'")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

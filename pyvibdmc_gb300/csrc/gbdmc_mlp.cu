@@ -35,7 +35,14 @@ __device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// sigmoid(z) = (1 + tanh(z/2)) / 2 with the single-instruction tanh.approx.f32
+// (|error| ~ 1e-3 relative, below the bf16 rounding of the activations).
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
 __device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
 
 // Copy a transposed bf16 weight matrix Wt[128][K] from global into smem rows of stride P.
@@ -453,22 +460,21 @@ __global__ void __launch_bounds__(256) k_mlp_energy(const __grid_constant__ gbdm
 }
 
 // ------------------------------------------------------- surrogate step
-// One DMC step of the water dimer on the surrogate, discrete weighting, fp32
-// walker coordinates: gather through idx, move (lanes 0-15 of each warp own
-// one walker), descriptors, MLP energy (whole warp), FP64 analytic energy for
-// the audit subset and for walkers outside the training box, weights, counts,
-// tile partials and the per-replica finalisation.  Tiles are 128 walkers
-// (8 warps x 16), so k_branch runs with tpb = 128.
-__global__ void __launch_bounds__(256) k_mlp_step(const __grid_constant__ gbdmc_sim_t S,
-                                                   const __grid_constant__ RepTable T,
-                                                   const __grid_constant__ gbdmc_mlp_t net,
-                                                   const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
-                                                   gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
-                                                   int* counts, double* audit, const gbdmc_noise_t nz) {
+// Phase 1 of a surrogate DMC step (water dimer, fp32 walker coordinates):
+// gather through idx and move (lanes 0-15 of each warp own one walker),
+// descriptors, then the warp's 16-walker MLP forward on the tensor cores;
+// writes V (hartree, fp64).  Walkers selected for the audit or outside the
+// training box are appended to a per-step list (scratch) with their flag;
+// k_mlp_audit gives them the analytic energy, so this kernel has no
+// divergent fp64 work.  Tiles are 128 walkers (8 warps x 16).
+__global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__ gbdmc_sim_t S,
+                                                          const __grid_constant__ RepTable T,
+                                                          const __grid_constant__ gbdmc_mlp_t net,
+                                                          const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
+                                                          gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
+                                                          const gbdmc_noise_t nz) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
-  __shared__ double u_sh[8][16];
-  __shared__ unsigned char flag_sh[8][16];
   load_net(sm, net);
   __syncthreads();
   const int64_t ld = S.ld;
@@ -480,14 +486,12 @@ __global__ void __launch_bounds__(256) k_mlp_step(const __grid_constant__ gbdmc_
     if (*(volatile int*)&ctrl->status) continue;
     const long long n = ctrl->n;
     const long long step = ctrl->step;
-    const double vref = ctrl->vref;
     const int64_t base = T.off[r];
     const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * 128 + 16 * w;
-    // --- move + descriptors (lanes 0..15)
+    if (i0 >= n) continue;  // warp-uniform: no walkers in this warp's rows
     if (lane < 16) {
       const int64_t i = i0 + lane;
       float xs[18];
-      unsigned char fl = 0;
       if (i < n) {
         const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
         const int64_t dst = base + i;
@@ -506,62 +510,62 @@ __global__ void __launch_bounds__(256) k_mlp_step(const __grid_constant__ gbdmc_
           out.x[k * ld + dst] = xs[k];
         }
         if (out.who && in.who) out.who[dst] = in.who[src];
-        u_sh[w][lane] = S.noise_mode == GBDMC_NOISE_INJECTED ? nz.u_branch[dst] : rng.uniform53();
         const bool oob = walker_features(xs, net, sm.feat[w][lane]);
         const bool aud = net.audit_every > 0 &&
-                         ((uint32_t)(splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ T.stream[r] * 0x85EBCA6Bu)) %
+                         (splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)) %
                           (uint32_t)net.audit_every) == 0;
-        fl = (oob ? 1 : 0) | (aud ? 2 : 0);
+        const unsigned char fl = (oob ? 1 : 0) | (aud ? 2 : 0);
+        if (fl) {
+          const unsigned long long q = atomicAdd((unsigned long long*)&ctrl->reserved[2], 1ull);
+          list[base + (int64_t)q] = (int)i;
+          flags[dst] = fl;
+        }
       } else {
 #pragma unroll
         for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
         walker_features(xs, net, sm.feat[w][lane]);
       }
-      flag_sh[w][lane] = fl;
     }
     __syncwarp();
     float e_lo, e_hi;
     mlp_forward16(sm, net, w, e_lo, e_hi);
-    // --- weights and counts (lanes with t < 2 own rows g and g + 8)
-    Partial p = partial_zero();
-    int flag = 0;
     const int row = g + 8 * t;
     const int64_t i = i0 + row;
-    if (t < 2 && i < n) {
-      const int64_t dst = base + i;
-      double v = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi);
-      const unsigned char fl = flag_sh[w][row];
-      if (fl) {
-        double xd[18], gd[18];
+    if (t < 2 && i < n)
+      out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi);
+    __syncwarp();
+  }
+}
+
+// Phase 2: analytic fp64 energy for the listed walkers (audit subset and
+// out-of-box fallback); audited differences V_nn - V_analytic are
+// accumulated in audit[0..2], fallbacks in audit[3].
+__global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
+                                                    const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
+                                                    const gbdmc_ctrl_t* ctrls, const int* list,
+                                                    const unsigned char* flags, double* audit) {
+  const int64_t ld = S.ld;
+  for (int r = 0; r < T.nrep; ++r) {
+    const gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile const int*)&ctrl->status) continue;
+    const long long cnt = *(volatile const long long*)&ctrl->reserved[2];
+    const int64_t base = T.off[r];
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < cnt && j < T.cap[r];
+         j += (long long)gridDim.x * blockDim.x) {
+      const int64_t dst = base + list[base + j];
+      double xd[18], gd[18];
 #pragma unroll
-        for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
-        const double va = pes_dimer<false>(xd, S.pes.p, gd);
-        if (fl & 2) {
-          const double d = v - va;
-          atomicAdd(audit + 0, 1.0);
-          atomicAdd(audit + 1, d);
-          atomicAdd(audit + 2, d * d);
-        }
-        if (fl & 1) atomicAdd(audit + 3, 1.0);
-        v = va;
+      for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
+      const double va = pes_dimer<false>(xd, S.pes.p, gd);
+      const unsigned char fl = flags[dst];
+      if (fl & 2) {
+        const double d = out.v[dst] - va;
+        atomicAdd(audit + 0, 1.0);
+        atomicAdd(audit + 1, d);
+        atomicAdd(audit + 2, d * d);
       }
-      out.v[dst] = v;
-      const double n0 = (double)T.n0[r];
-      const double w_hi = (n0 + n0 * 0.5) + 1.0;
-      const int c = branch_count(v, vref, S.dt, u_sh[w][row], w_hi, flag, p.births, p.deaths);
-      counts[dst] = c;
-      p.c = c;
-      p.s0 = c == 1 ? v : (double)c * v;
-    }
-    if (__syncthreads_or(flag)) {
-      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-    }
-    p = block_reduce_partial<false>(p);
-    if (threadIdx.x == 0) part[tile] = p;
-    const int nt = T.tile_off[r + 1] - T.tile_off[r];
-    if (last_tile(ctrl, nt)) {
-      const Partial tt = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
-      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, tt);
+      if (fl & 1) atomicAdd(audit + 3, 1.0);
+      out.v[dst] = va;
     }
   }
 }
@@ -617,6 +621,8 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
       if (threadIdx.x == 0) {
         const double n0 = (double)T.n0[r];
         ctrl->vref = tt.s0 / (double)n - S.alpha * ((double)(n - T.n0[r]) / n0);
+        ctrl->dt_eff = S.dt;  // k_count weights with dt_eff
+        ctrl->reserved[2] = 0;
         ctrl->ticket = 0;
       }
     }
@@ -832,7 +838,7 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
     }
     nz = *noise;
   }
-  rc = set_mlp_smem((const void*)k_mlp_step);
+  rc = set_mlp_smem((const void*)k_mlp_move_energy);
   if (rc) return rc;
   const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
   cudaStream_t s = (cudaStream_t)stream;
@@ -841,9 +847,17 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
   cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
   if (prof) cudaEventRecord(ev[0], s);
-  k_mlp_step<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.part, L.prefix, L.counts, audit,
-                                                  nz);
+  k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz);
   if (prof) cudaEventRecord(ev[1], s);
+  k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit);
+  gbdmc_walkers_t wv{};
+  wv.v = dst->v;
+  if (S->noise_mode == GBDMC_NOISE_INJECTED)
+    k_count<GBDMC_NOISE_INJECTED, true><<<grid_for(T), T.tpb, 0, s>>>(*S, T, wv, ctrl, L.part, L.prefix, L.counts,
+                                                                       nz);
+  else
+    k_count<GBDMC_NOISE_PHILOX32, true><<<grid_for(T), T.tpb, 0, s>>>(*S, T, wv, ctrl, L.part, L.prefix, L.counts,
+                                                                       nz);
   launch_branch(T, dst->idx, ctrl, L.prefix, L.counts, s);
   if (prof) {
     cudaEventRecord(ev[2], s);

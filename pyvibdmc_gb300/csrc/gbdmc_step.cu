@@ -293,55 +293,6 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
   }
 }
 
-// Discrete weights and counts from stored energies with dt_eff (importance sampling).
-template <int NM>
-__global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
-                                                    const __grid_constant__ RepTable T, gbdmc_walkers_t out,
-                                                    gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
-                                                    int* counts, const gbdmc_noise_t nz) {
-  const int ntile = T.tile_off[T.nrep];
-  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-    const int r = replica_of(T, tile);
-    gbdmc_ctrl_t* ctrl = ctrls + r;
-    if (*(volatile int*)&ctrl->status) continue;
-    const long long n = ctrl->n;
-    const long long step = ctrl->step;
-    const double vref = ctrl->vref;
-    const double dt = ctrl->dt_eff;
-    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
-    const int64_t dst = T.off[r] + i;
-    Partial p = partial_zero();
-    int flag = 0;
-    if (i < n) {
-      const double v = out.v[dst];
-      double u;
-      if constexpr (NM == GBDMC_NOISE_INJECTED) {
-        u = nz.u_branch[dst];
-      } else {
-        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
-        rng.slot = 64;  // stream disjoint from the move's draws
-        u = rng.uniform53();
-      }
-      const double n0 = (double)T.n0[r];
-      const double w_hi = (n0 + n0 * 0.5) + 1.0;
-      const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
-      counts[dst] = c;
-      p.c = c;
-      p.s0 = c == 1 ? v : (double)c * v;
-    }
-    if (__syncthreads_or(flag)) {
-      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-    }
-    p = block_reduce_partial<false>(p);
-    if (threadIdx.x == 0) part[tile] = p;
-    const int nt = T.tile_off[r + 1] - T.tile_off[r];
-    if (last_tile(ctrl, nt)) {
-      const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
-      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, t);
-    }
-  }
-}
-
 // ----------------------------------------------------------- branching
 // Walker j (pre-branch order) writes j into idx[prefix[tile] + scan .. + c):
 // the np.repeat(arange(N), counts) order of pyvibdmc.py:417-430.
@@ -737,7 +688,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
     if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
-      k_count<NM><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
+      k_count<NM, false><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
       k_branch<<<G, T.tpb, 0, s>>>(T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
       k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);

@@ -186,6 +186,7 @@ __device__ __noinline__ static void finalize_discrete(const gbdmc_sim_t& S, cons
     ctrl->vref = vref;
     ctrl->step = step + 1;
   }
+  ctrl->reserved[2] = 0;  // surrogate path: analytic-energy list of the step
   ctrl->ticket = 0;
 }
 
@@ -212,6 +213,75 @@ __device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&
     s = s + t;
   }
   return -0.5 * s;
+}
+
+// Discrete weights and counts from stored energies with dt = ctrl->dt_eff
+// (importance sampling; the surrogate path sets it to dt).  F32W: the weight
+// exp(-(V-vref) dt) is evaluated in fp32 from the fp64 exponent (surrogate
+// path, whose energies carry ~1e-4 relative error); sums stay fp64.
+template <int NM, bool F32W>
+__global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
+                                                    const __grid_constant__ RepTable T, gbdmc_walkers_t out,
+                                                    gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
+                                                    int* counts, const gbdmc_noise_t nz) {
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const double vref = ctrl->vref;
+    const double dt = ctrl->dt_eff;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t dst = T.off[r] + i;
+    Partial p = partial_zero();
+    int flag = 0;
+    if (i < n) {
+      const double v = out.v[dst];
+      double u;
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
+        u = nz.u_branch[dst];
+      } else {
+        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+        rng.slot = 64;  // stream disjoint from the move's draws
+        u = rng.uniform53();
+      }
+      const double n0 = (double)T.n0[r];
+      const double w_hi = (n0 + n0 * 0.5) + 1.0;
+      int c;
+      if constexpr (F32W) {
+        const float wf = expf((float)__dmul_rn(-__dsub_rn(v, vref), dt));
+        if (!isfinite(wf)) {
+          flag |= GBDMC_ST_NONFINITE_WEIGHT;
+          c = 0;
+        } else if ((double)wf > w_hi) {
+          flag |= GBDMC_ST_HUGE_WEIGHT;
+          c = 0;
+        } else {
+          const float fl = floorf(wf);
+          c = (int)fl + (u < (double)(wf - fl) ? 1 : 0);
+          p.births += c > 1 ? c - 1 : 0;
+          p.deaths += c == 0 ? 1 : 0;
+        }
+      } else {
+        c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
+      }
+      counts[dst] = c;
+      p.c = c;
+      p.s0 = c == 1 ? v : (double)c * v;
+    }
+    if (__syncthreads_or(flag)) {
+      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
+    }
+    p = block_reduce_partial<false>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    if (last_tile(ctrl, nt)) {
+      const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
+      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, t);
+    }
+  }
 }
 
 }  // namespace gbdmc
