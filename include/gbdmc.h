@@ -54,7 +54,8 @@ enum {
   GBDMC_ST_HUGE_WEIGHT = 2,      /* pyvibdmc.py:397 weight > 1.5 N0 + 1        */
   GBDMC_ST_POP_LOW = 4,          /* pyvibdmc.py:409,716 population < 0.5 N0    */
   GBDMC_ST_POP_HIGH = 8,         /* pyvibdmc.py:409,716 population > 1.5 N0    */
-  GBDMC_ST_OVERFLOW = 16         /* population would exceed the capacity ld    */
+  GBDMC_ST_OVERFLOW = 16,        /* population would exceed the capacity ld    */
+  GBDMC_ST_TIMEOUT = 32          /* a bounded wait inside a kernel gave up     */
 };
 
 /* potential energy surfaces */
@@ -288,7 +289,7 @@ typedef struct {
   float feat_lo[16];
   float feat_hi[16];
   int32_t audit_every; /* walker audited (analytic PES, error recorded) when hash % audit_every == 0; 0 = off */
-  int32_t reserved;
+  int32_t engine;      /* 0: mma.sync BF16 kernels; 1: tcgen05 (TMEM accumulators, one thread per walker) */
 } gbdmc_mlp_t;
 
 /* fp32-coordinate walkers of the surrogate path (SoA [18][ld]) */
@@ -324,9 +325,10 @@ int gbdmc_dimer_features(const double* x_dev, int64_t ld, int64_t n, const float
                          const double* vdir_dev, const double* grad_dev, float e_scale, float* feat_dev,
                          float* tang_dev, float* et_dev, void* stream);
 /* Surrogate energies of n walkers (fp32 SoA [18][ld]); outside_dev[i] = 1 for walkers outside the training box
- * (may be NULL; not cleared). */
+ * (may be NULL; not cleared).  With net->engine == 1 (tcgen05) status_dev (device int, required) is set to 1 if a
+ * bounded wait for the tensor cores gave up. */
 int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int64_t n, double* v_dev,
-                     int32_t* outside_dev, void* stream);
+                     int32_t* outside_dev, int32_t* status_dev, void* stream);
 /* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
  * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[4] accumulates: audited
  * walkers, sum (V_nn - V_analytic), sum (V_nn - V_analytic)^2, fallbacks. */

@@ -12,7 +12,7 @@ from . import _build
 MAX_ATOMS = 8
 
 OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY = 0, 1, 2, 3
-ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW = 1, 2, 4, 8, 16
+ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW, ST_TIMEOUT = 1, 2, 4, 8, 16, 32
 PES_HO, PES_H2O_LM, PES_DIMER = 1, 2, 3
 TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS = 0, 1, 2
 NOISE_PHILOX32, NOISE_PHILOX64, NOISE_INJECTED = 0, 1, 2
@@ -72,7 +72,7 @@ class MLP(C.Structure):
                 ("b2", C.c_void_p), ("b3", C.c_void_p), ("w4", C.c_void_p), ("b4", C.c_float),
                 ("e_mean", C.c_float), ("e_scale", C.c_float), ("hull_margin", C.c_float),
                 ("feat_mu", C.c_float * 16), ("feat_inv_sd", C.c_float * 16), ("feat_lo", C.c_float * 16),
-                ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("reserved", C.c_int32)]
+                ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("engine", C.c_int32)]
 
 
 class WalkersF32(C.Structure):
@@ -125,7 +125,7 @@ def load():
         "gbdmc_mlp_adam": ([P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P, P,
                             C.c_int32, P], C.c_int),
         "gbdmc_dimer_features": ([P, C.c_int64, C.c_int64, P, P, P, P, C.c_float, P, P, P, P], C.c_int),
-        "gbdmc_mlp_energy": ([C.POINTER(MLP), P, C.c_int64, C.c_int64, P, P, P], C.c_int),
+        "gbdmc_mlp_energy": ([C.POINTER(MLP), P, C.c_int64, C.c_int64, P, P, P, P], C.c_int),
         "gbdmc_mlp_sim_init": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), P, P, P], C.c_int),
         "gbdmc_mlp_sim_step": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P,
                                 P, C.POINTER(Noise), P], C.c_int),

@@ -92,4 +92,11 @@ int grid_for(const RepTable& T);
 void launch_branch(const RepTable& T, int32_t* idx, const gbdmc_ctrl_t* ctrl, const long long* prefix,
                    const int* counts, cudaStream_t s);
 
+// tcgen05 surrogate kernels (gbdmc_mlp_tc.cu)
+int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, long long n, double* v, int* outside,
+                         int* err, cudaStream_t s);
+int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_mlp_t& net,
+                              const gbdmc_walkers_f32_t& in, const gbdmc_walkers_f32_t& out, gbdmc_ctrl_t* ctrl,
+                              int* list, unsigned char* flags, const gbdmc_noise_t& nz, cudaStream_t s);
+
 }  // namespace gbdmc

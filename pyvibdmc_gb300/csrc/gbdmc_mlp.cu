@@ -11,8 +11,7 @@
 // Y = X W (+b), G += X^T D, and fused SiLU forward/backward with a tangent
 // (directional-derivative) stream, so that d(E . u)/dW -- the gradient of the
 // force residual -- is one more pass of the same GEMMs.
-#include <cuda_bf16.h>
-#include "gbdmc_stepcore.cuh"
+#include "gbdmc_mlp_common.cuh"
 
 namespace gbdmc {
 
@@ -20,11 +19,6 @@ constexpr int kH = 128;    // hidden width
 constexpr int kIn = 16;    // padded input width (15 features)
 constexpr int kPadH = 136; // smem row stride (bf16) of 128-wide weights
 constexpr int kPadI = 24;  // smem row stride (bf16) of 16-wide weights
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t*>(&v);
-}
 
 __device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1) {
@@ -34,16 +28,6 @@ __device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
-
-// sigmoid(z) = (1 + tanh(z/2)) / 2 with the single-instruction tanh.approx.f32
-// (|error| ~ 1e-3 relative, below the bf16 rounding of the activations).
-__device__ __forceinline__ float tanh_approx(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
-__device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
 
 // Copy a transposed bf16 weight matrix Wt[128][K] from global into smem rows of stride P.
 __device__ __forceinline__ void load_wt(uint16_t* dst, const uint16_t* __restrict__ src, int K, int P) {
@@ -406,26 +390,6 @@ __device__ __forceinline__ void mlp_forward16(const MlpSmem& sm, const gbdmc_mlp
   e_hi = hi + net.b4;
 }
 
-// Descriptors of one walker into the warp's feature row; returns true when
-// the walker lies outside the training box (normalised range +- margin).
-__device__ __forceinline__ bool walker_features(const float (&xs)[18], const gbdmc_mlp_t& net, float* row) {
-  int q = 0;
-  bool out = false;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-#pragma unroll
-    for (int j = i + 1; j < 6; ++j) {
-      const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
-      const float f = (rsqrtf(dx * dx + dy * dy + dz * dz) - net.feat_mu[q]) * net.feat_inv_sd[q];
-      out |= (f < net.feat_lo[q] - net.hull_margin) || (f > net.feat_hi[q] + net.hull_margin);
-      row[q] = f;
-      ++q;
-    }
-  }
-  row[15] = 0.f;
-  return out;
-}
-
 // Energies of n walkers (coordinates SoA, fp32 or fp64) from the surrogate.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mlp_energy(const __grid_constant__ gbdmc_mlp_t net, const T* __restrict__ x,
@@ -767,12 +731,14 @@ extern "C" int gbdmc_dimer_features(const double* x, int64_t ld, int64_t n, cons
 }
 
 extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t ld, int64_t n, double* v,
-                                int32_t* outside, void* stream) {
-  if (!valid_net(net) || !x || !v || n < 0 || ld < n) {
+                                int32_t* outside, int32_t* status, void* stream) {
+  if (!valid_net(net) || !x || !v || n < 0 || ld < n || (net->engine == 1 && !status) || net->engine < 0 ||
+      net->engine > 1) {
     set_error("gbdmc_mlp_energy: invalid arguments");
     return GBDMC_ERR_ARG;
   }
   if (n == 0) return GBDMC_OK;
+  if (net->engine == 1) return launch_mlp_tc_energy(*net, x, ld, n, v, outside, status, (cudaStream_t)stream);
   int rc = set_mlp_smem((const void*)k_mlp_energy<float>);
   if (rc) return rc;
   long long g = (n + 127) / 128;
@@ -838,6 +804,10 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
     }
     nz = *noise;
   }
+  if (net->engine < 0 || net->engine > 1) {
+    set_error("gbdmc_mlp_sim_step: engine must be 0 (mma.sync) or 1 (tcgen05)");
+    return GBDMC_ERR_ARG;
+  }
   rc = set_mlp_smem((const void*)k_mlp_move_energy);
   if (rc) return rc;
   const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
@@ -847,7 +817,12 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
   cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
   if (prof) cudaEventRecord(ev[0], s);
-  k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz);
+  if (net->engine == 1) {
+    rc = launch_mlp_tc_move_energy(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz, s);
+    if (rc) return rc;
+  } else {
+    k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz);
+  }
   if (prof) cudaEventRecord(ev[1], s);
   k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit);
   gbdmc_walkers_t wv{};

@@ -1,0 +1,357 @@
+// MLP surrogate forward on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// One CTA of 128 threads processes tiles of 128 walkers, one walker per
+// thread.  The hidden layers are M=128 x N=128 x K tcgen05.mma instructions
+// (kind::f16, BF16 operands, FP32 accumulation) issued by one thread:
+//   A = activations of the tile, B = transposed weights, both in shared memory
+//       in the canonical K-major no-swizzle layout (8-row x 16-byte core
+//       matrices; K-adjacent cores contiguous, LBO = 128 B, SBO = KG*128 B);
+//   D = a 128-lane x 128-column FP32 accumulator in tensor memory.
+// Completion is signalled by tcgen05.commit to an mbarrier; every thread then
+// reads its own walker's row (TMEM lane = thread) with tcgen05.ld, applies
+// bias + SiLU and writes the BF16 row back as the next layer's A operand.
+// Waits are bounded: a timeout sets GBDMC_ST_TIMEOUT, the CTA stops issuing,
+// frees its tensor memory and returns.
+#include "gbdmc_mlp_common.cuh"
+
+namespace gbdmc {
+namespace tc {
+
+constexpr int kRows = 128;       // walkers per tile = MMA M = TMEM lanes
+constexpr int kN = 128;          // hidden width = MMA N = TMEM columns
+constexpr uint32_t kCols = 128;  // TMEM columns allocated per CTA
+constexpr int kCore = 128;       // bytes of one 8 x 16-byte core matrix
+constexpr int kThreads = 128;
+
+// Instruction descriptor, kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N>>3 at 17, M>>4 at 24.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(kRows >> 4) << 24);
+
+struct TcSmem {
+  alignas(128) unsigned char w1[kN * 16 * 2];    // N=128 x K=16 (KG = 2)
+  alignas(128) unsigned char w2[kN * kN * 2];    // N=128 x K=128 (KG = 16)
+  alignas(128) unsigned char w3[kN * kN * 2];
+  alignas(128) unsigned char a[kRows * kN * 2];  // M=128 x K=128 (KG = 16)
+  float b1[kN], b2[kN], b3[kN], w4[kN];
+  alignas(8) unsigned long long mbar;
+  uint32_t tmem_base;
+};
+
+// byte offset of element (row, k) of a canonical K-major operand with KG core columns
+__device__ __forceinline__ uint32_t canon_off(int row, int k, int KG) {
+  return (uint32_t)(((row >> 3) * KG + (k >> 3)) * kCore + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// tcgen05 shared-memory descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29),
+// SBO >> 4 (32-45), version 1 (46-47), no swizzle (61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Bounded wait for the mbarrier phase `parity` to complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 32 consecutive fp32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32]) {
+  uint32_t u[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+        "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
+        "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
+        "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) r[j] = __uint_as_float(u[j]);
+}
+
+__device__ void load_weights(TcSmem& sm, const gbdmc_mlp_t& net) {
+  // Wt is n-major [128][K] in global; 16-byte chunks = 8 consecutive k of one row n
+  for (int c = threadIdx.x; c < kN * 2; c += blockDim.x) {
+    const int n = c >> 1, kg = c & 1;
+    *reinterpret_cast<uint4*>(sm.w1 + canon_off(n, 8 * kg, 2)) =
+        __ldg(reinterpret_cast<const uint4*>(net.w1t + n * 16 + 8 * kg));
+  }
+  for (int c = threadIdx.x; c < kN * 16; c += blockDim.x) {
+    const int n = c >> 4, kg = c & 15;
+    *reinterpret_cast<uint4*>(sm.w2 + canon_off(n, 8 * kg, 16)) =
+        __ldg(reinterpret_cast<const uint4*>(net.w2t + n * kN + 8 * kg));
+    *reinterpret_cast<uint4*>(sm.w3 + canon_off(n, 8 * kg, 16)) =
+        __ldg(reinterpret_cast<const uint4*>(net.w3t + n * kN + 8 * kg));
+  }
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) {
+    sm.b1[i] = net.b1[i];
+    sm.b2[i] = net.b2[i];
+    sm.b3[i] = net.b3[i];
+    sm.w4[i] = net.w4[i];
+  }
+}
+
+// Bias + SiLU of this thread's accumulator row, written as BF16 A row (KG = 16).
+__device__ __forceinline__ void epilogue_to_a(TcSmem& sm, uint32_t trow, const float* bias) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float r[32];
+    tmem_ld32(trow + 32 * c, r);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t p[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int j = 8 * q + 2 * e, n = 32 * c + j;
+        p[e] = pack_bf16(silu(r[j] + bias[n]), silu(r[j + 1] + bias[n + 1]));
+      }
+      *reinterpret_cast<uint4*>(sm.a + canon_off(t, 32 * c + 8 * q, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
+    }
+  }
+}
+
+// Issue the K/16 MMAs of one layer (thread 0) and wait for them.
+__device__ __forceinline__ bool run_layer(TcSmem& sm, uint32_t tmem, uint32_t mbar, uint32_t& phase,
+                                          const unsigned char* w, int KG) {
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    const uint32_t a0 = saddr(sm.a), b0 = saddr(w);
+    for (int s = 0; s < KG / 2; ++s)
+      umma(tmem, smem_desc(a0 + 256u * s, kCore, 16 * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
+           s > 0 ? 1u : 0u);
+    umma_commit(mbar);
+  }
+  const bool ok = mbar_wait(mbar, phase);
+  phase ^= 1u;
+  tc_fence_after();
+  return ok;
+}
+
+// Network output (normalised, without b4) of this thread's feature row f.
+__device__ __forceinline__ float forward_tile(TcSmem& sm, uint32_t tmem, uint32_t mbar, uint32_t& phase,
+                                              const float (&f)[16], bool& ok) {
+  const int t = threadIdx.x;
+  const uint32_t trow = tmem + ((uint32_t)(32 * (t >> 5)) << 16);
+  {
+    uint32_t p[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) p[q] = pack_bf16(f[2 * q], f[2 * q + 1]);
+    *reinterpret_cast<uint4*>(sm.a + canon_off(t, 0, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(sm.a + canon_off(t, 8, 16)) = make_uint4(p[4], p[5], p[6], p[7]);
+  }
+  ok &= run_layer(sm, tmem, mbar, phase, sm.w1, 2);
+  epilogue_to_a(sm, trow, sm.b1);
+  tc_fence_before();
+  ok &= run_layer(sm, tmem, mbar, phase, sm.w2, 16);
+  epilogue_to_a(sm, trow, sm.b2);
+  tc_fence_before();
+  ok &= run_layer(sm, tmem, mbar, phase, sm.w3, 16);
+  float e = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float r[32];
+    tmem_ld32(trow + 32 * c, r);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) e += silu(r[j] + sm.b3[32 * c + j]) * sm.w4[32 * c + j];
+  }
+  tc_fence_before();
+  __syncthreads();  // TMEM rows read and A free before the next tile
+  return e;
+}
+
+__device__ __forceinline__ void setup(TcSmem& sm, const gbdmc_mlp_t& net, uint32_t& tmem, uint32_t& mbar) {
+  load_weights(sm, net);
+  mbar = saddr(&sm.mbar);
+  if (threadIdx.x == 0) mbar_init(mbar);
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&sm.tmem_base)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  tmem = sm.tmem_base;
+}
+
+__device__ __forceinline__ void teardown(uint32_t tmem) {
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
+
+// Energies of n walkers (fp32 SoA coordinates) -- the tcgen05 twin of k_mlp_energy.
+__global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constant__ gbdmc_mlp_t net,
+                                                             const float* __restrict__ x, long long ld, long long n,
+                                                             double* __restrict__ v, int* __restrict__ outside,
+                                                             int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
+  uint32_t tmem, mbar, phase = 0;
+  setup(sm, net, tmem, mbar);
+  bool ok = true;
+  for (long long base = (long long)blockIdx.x * kRows; base < n; base += (long long)gridDim.x * kRows) {
+    const long long i = base + threadIdx.x;
+    float xs[18], f[16];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) xs[k] = i < n ? x[k * ld + i] : (k < 3 ? 0.f : 1.f + k);
+    const bool oob = walker_features(xs, net, f) && i < n;
+    const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
+    if (i < n) v[i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4);
+    if (oob && outside) outside[i] = 1;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      break;
+    }
+  }
+  teardown(tmem);
+}
+
+// Phase 1 of a surrogate DMC step on tcgen05: gather + move + descriptors
+// (one walker per thread), MLP forward, V; audit/out-of-box walkers are
+// listed for k_mlp_audit exactly like the mma.sync path.
+__global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_constant__ gbdmc_sim_t S,
+                                                                  const __grid_constant__ RepTable T,
+                                                                  const __grid_constant__ gbdmc_mlp_t net,
+                                                                  const gbdmc_walkers_f32_t in,
+                                                                  gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls,
+                                                                  int* list, unsigned char* flags,
+                                                                  const gbdmc_noise_t nz) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
+  uint32_t tmem, mbar, phase = 0;
+  setup(sm, net, tmem, mbar);
+  bool ok = true;
+  const int64_t ld = S.ld;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const long long step = ctrl->step;
+    const int64_t base = T.off[r];
+    const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * kRows;
+    if (i0 >= n) continue;  // block-uniform
+    const int64_t i = i0 + threadIdx.x;
+    float xs[18], f[16];
+    if (i < n) {
+      const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+      const int64_t dst = base + i;
+      Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+      float z[18];
+      if (S.noise_mode == GBDMC_NOISE_INJECTED) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 18; k += 2) rng.normal2_f32(z[k], z[k + 1]);
+      }
+#pragma unroll
+      for (int k = 0; k < 18; ++k) {
+        xs[k] = in.x[k * ld + src] + (float)S.sigma[k / 3] * z[k];
+        out.x[k * ld + dst] = xs[k];
+      }
+      if (out.who && in.who) out.who[dst] = in.who[src];
+      const bool oob = walker_features(xs, net, f);
+      const bool aud = net.audit_every > 0 &&
+                       (splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)) %
+                        (uint32_t)net.audit_every) == 0;
+      const unsigned char fl = (oob ? 1 : 0) | (aud ? 2 : 0);
+      if (fl) {
+        const unsigned long long q = atomicAdd((unsigned long long*)&ctrl->reserved[2], 1ull);
+        list[base + (int64_t)q] = (int)i;
+        flags[dst] = fl;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
+      walker_features(xs, net, f);
+    }
+    const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
+    if (i < n) out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+      break;
+    }
+  }
+  teardown(tmem);
+}
+
+}  // namespace tc
+
+int tc_smem_bytes() { return (int)sizeof(tc::TcSmem) + 1024; }
+
+int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, long long n, double* v, int* outside,
+                         int* err, cudaStream_t s) {
+  const cudaError_t e =
+      cudaFuncSetAttribute((const void*)tc::k_mlp_tc_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes());
+  if (e != cudaSuccess) {
+    set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  long long g = (n + tc::kRows - 1) / tc::kRows;
+  if (g > 2LL * num_sms()) g = 2LL * num_sms();
+  tc::k_mlp_tc_energy<<<(int)g, tc::kThreads, tc_smem_bytes(), s>>>(net, x, ld, n, v, outside, err);
+  return check_launch("gbdmc_mlp_energy (tcgen05)");
+}
+
+int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_mlp_t& net,
+                              const gbdmc_walkers_f32_t& in, const gbdmc_walkers_f32_t& out, gbdmc_ctrl_t* ctrl,
+                              int* list, unsigned char* flags, const gbdmc_noise_t& nz, cudaStream_t s) {
+  const cudaError_t e = cudaFuncSetAttribute((const void*)tc::k_mlp_tc_move_energy,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes());
+  if (e != cudaSuccess) {
+    set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  int g = T.tile_off[T.nrep];
+  if (g > 2 * num_sms()) g = 2 * num_sms();
+  tc::k_mlp_tc_move_energy<<<g, tc::kThreads, tc_smem_bytes(), s>>>(S, T, net, in, out, ctrl, list, flags, nz);
+  return check_launch("gbdmc_mlp_sim_step (tcgen05)");
+}
+
+}  // namespace gbdmc

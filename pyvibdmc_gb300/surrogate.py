@@ -45,8 +45,10 @@ def _bf16_bits(t):
 
 
 class MLPSurrogate:
-    def __init__(self, device=None, seed=0):
+    def __init__(self, device=None, seed=0, engine=1):
+        """engine: 1 = tcgen05 inference kernels (default), 0 = mma.sync kernels."""
         self.device = torch.device(device) if device is not None else default_device()
+        self.engine = int(engine)
         g = torch.Generator().manual_seed(seed)
         f32 = dict(dtype=torch.float32)
 
@@ -78,7 +80,7 @@ class MLPSurrogate:
                        W2n=_bf16_bits(P["W2"]), W3n=_bf16_bits(P["W3"]))
 
     # ---------------------------------------------------------- inference
-    def net_struct(self, audit_every=0):
+    def net_struct(self, audit_every=0, engine=None):
         n = _capi.MLP()
         n.w1t, n.w2t, n.w3t = self.bf["W1t"].data_ptr(), self.bf["W2t"].data_ptr(), self.bf["W3t"].data_ptr()
         n.b1, n.b2, n.b3 = self.P["b1"].data_ptr(), self.P["b2"].data_ptr(), self.P["b3"].data_ptr()
@@ -89,22 +91,26 @@ class MLPSurrogate:
         for q in range(16):
             n.feat_mu[q], n.feat_inv_sd[q], n.feat_lo[q], n.feat_hi[q] = mu[q], isd[q], lo[q], hi[q]
         n.audit_every = int(audit_every)
+        n.engine = int(self.engine if engine is None else engine)
         return n
 
-    def energy_soa(self, x32, n, ld=None):
+    def energy_soa(self, x32, n, ld=None, engine=None):
         """Surrogate energies (float64 tensor) of fp32 SoA walkers; also the out-of-box mask."""
         L = _capi.load()
         ld = x32.shape[1] if ld is None else ld
         v = torch.empty(max(n, 1), dtype=torch.float64, device=self.device)
         out = torch.zeros(max(n, 1), dtype=torch.int32, device=self.device)
-        _capi.check(L.gbdmc_mlp_energy(C.byref(self.net_struct()), _p(x32), ld, n, _p(v), _p(out), _s()),
-                    "gbdmc_mlp_energy")
+        st = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _capi.check(L.gbdmc_mlp_energy(C.byref(self.net_struct(engine=engine)), _p(x32), ld, n, _p(v), _p(out),
+                                       _p(st), _s()), "gbdmc_mlp_energy")
+        if int(st.item()):
+            raise RuntimeError("gbdmc_mlp_energy: a bounded tensor-core wait timed out")
         return v[:n], out[:n]
 
-    def energy(self, cds):
+    def energy(self, cds, engine=None):
         cds = np.asarray(cds, dtype=np.float64)
         x32 = to_soa(cds, self.device, dtype=torch.float32)
-        return self.energy_soa(x32, len(cds))[0].cpu().numpy()
+        return self.energy_soa(x32, len(cds), engine=engine)[0].cpu().numpy()
 
     # ----------------------------------------------------------- training
     def set_normalisation(self, x, v):

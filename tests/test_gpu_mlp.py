@@ -136,3 +136,16 @@ def test_training_reduces_loss_and_surrogate_dmc_runs():
     assert a["audited"] > 0
     assert np.isfinite(nd.vref_history()).all()
     assert len(nd.walkers()) == int(nd.ctrl().n)
+
+
+def test_tcgen05_forward_matches_mma_sync_forward():
+    """The tcgen05/TMEM inference kernel computes the same BF16 network as the
+    mma.sync kernel (same operand rounding; fp32 accumulation order differs)."""
+    m, x, xs, v, g = _small_model(3)
+    for _ in range(20):
+        m.train_batch(xs, v, g, lr=2e-3)
+    xx = oracle.dimer_equilibrium()[None] + 0.1 * oracle.InjectedNoise(77).standard_normal((1000, 6, 3))
+    e0 = m.energy(xx, engine=0)
+    e1 = m.energy(xx, engine=1)
+    rel = np.abs(e1 - e0) / m.e_scale
+    assert np.median(rel) < 2e-4 and rel.max() < 5e-3, (np.median(rel), rel.max())
