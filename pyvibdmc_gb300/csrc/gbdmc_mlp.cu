@@ -501,35 +501,83 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
   }
 }
 
+// One eighth of the analytic dimer energy (same terms as pes_dimer): part 0/1
+// the two monomers, part 2 the O-O Lennard-Jones plus the O-O charge pair,
+// parts 3..7 the remaining eight intermolecular charge pairs.
+__device__ __forceinline__ double dimer_part(const double (&x)[18], const double* p, int part) {
+  double g[18];
+  if (part == 0) return h2o_lm<false, 6>(x, p, 0, 1, 2, g);
+  if (part == 1) return h2o_lm<false, 6>(x, p, 3, 4, 5, g);
+  const double q[3] = {p[9], p[8], p[8]};  // O, H, H
+  double v = 0.0;
+  if (part == 2) {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
+    const double ir2 = 1.0 / (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double s2 = p[7] * p[7] * ir2;
+    const double s6 = s2 * s2 * s2;
+    v = 4.0 * p[6] * (s6 * s6 - s6);
+  }
+  // charge pairs (i of monomer A, j of monomer B) owned by this part
+  const int pairs[6][2] = {{0, 0}, {1, 2}, {3, 4}, {5, 6}, {7, 7}, {8, 8}};  // [part-2] -> pair range
+  const int lo = pairs[part - 2][0], hi = pairs[part - 2][1];
+  for (int k = lo; k <= hi; ++k) {
+    const int i = k / 3, j = k % 3;
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) d[c] = x[3 * (3 + j) + c] - x[3 * i + c];
+    v += q[i] * q[j] * rsqrt_guard(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  }
+  return v;
+}
+
 // Phase 2: analytic fp64 energy for the listed walkers (audit subset and
-// out-of-box fallback); audited differences V_nn - V_analytic are
-// accumulated in audit[0..2], fallbacks in audit[3].
+// out-of-box fallback), 8 lanes per walker (one part each, summed in a fixed
+// shuffle order); audited differences V_nn - V_analytic are accumulated in
+// audit[0..2], fallbacks in audit[3].
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     const gbdmc_ctrl_t* ctrls, const int* list,
                                                     const unsigned char* flags, double* audit) {
   const int64_t ld = S.ld;
+  const int part = threadIdx.x & 7;
   for (int r = 0; r < T.nrep; ++r) {
     const gbdmc_ctrl_t* ctrl = ctrls + r;
     if (*(volatile const int*)&ctrl->status) continue;
-    const long long cnt = *(volatile const long long*)&ctrl->reserved[2];
+    long long cnt = *(volatile const long long*)&ctrl->reserved[2];
+    if (cnt > T.cap[r]) cnt = T.cap[r];
     const int64_t base = T.off[r];
-    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < cnt && j < T.cap[r];
-         j += (long long)gridDim.x * blockDim.x) {
-      const int64_t dst = base + list[base + j];
-      double xd[18], gd[18];
+    // a warp takes 4 walkers per iteration (lanes 8k..8k+7 -> walker jb + k); the
+    // loop bound is warp-uniform, so the shuffles below see all 32 lanes
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long jb = 4 * gw; jb < cnt; jb += 4 * nw) {
+      const long long j = jb + ((threadIdx.x & 31) >> 3);
+      const bool live = j < cnt;
+      double v = 0.0;
+      int64_t dst = 0;
+      if (live) {
+        dst = base + list[base + j];
+        double xd[18];
 #pragma unroll
-      for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
-      const double va = pes_dimer<false>(xd, S.pes.p, gd);
-      const unsigned char fl = flags[dst];
-      if (fl & 2) {
-        const double d = out.v[dst] - va;
-        atomicAdd(audit + 0, 1.0);
-        atomicAdd(audit + 1, d);
-        atomicAdd(audit + 2, d * d);
+        for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
+        v = dimer_part(xd, S.pes.p, part);
       }
-      if (fl & 1) atomicAdd(audit + 3, 1.0);
-      out.v[dst] = va;
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (live && part == 0) {
+        const unsigned char fl = flags[dst];
+        if (fl & 2) {
+          const double d = out.v[dst] - v;
+          atomicAdd(audit + 0, 1.0);
+          atomicAdd(audit + 1, d);
+          atomicAdd(audit + 2, d * d);
+        }
+        if (fl & 1) atomicAdd(audit + 3, 1.0);
+        out.v[dst] = v;
+      }
     }
   }
 }
@@ -747,7 +795,9 @@ extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t 
   return check_launch("gbdmc_mlp_energy");
 }
 
-static int mlp_table(const gbdmc_sim_t* S, RepTable& T, const char* what) {
+// Replica table of the surrogate path: tiles of `tpb` walkers (128 for the
+// MLP kernels: 8 warps x 16 or 128 threads x 1; 256 for counts and branching).
+static int mlp_table(const gbdmc_sim_t* S, RepTable& T, const char* what, int tpb = 128) {
   if (!S || S->natoms != 6 || S->pes.kind != GBDMC_PES_DIMER || S->weighting != GBDMC_DISCRETE ||
       S->trial.kind != GBDMC_TRIAL_NONE || S->n0 < 1 || S->ld < 1 || S->ld > (int64_t)INT32_MAX) {
     set_error("%s: the surrogate path runs the 6-atom dimer, discrete weighting, no trial psi", what);
@@ -763,7 +813,7 @@ static int mlp_table(const gbdmc_sim_t* S, RepTable& T, const char* what) {
   r.n0 = S->n0;
   r.stream = S->replica_id;
   gbdmc_sim_t S2 = *S;
-  S2.block_threads = 128;  // tile = 8 warps x 16 walkers
+  S2.block_threads = tpb;
   return build_table(S2, &r, 1, T, what);
 }
 
@@ -825,15 +875,18 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   }
   if (prof) cudaEventRecord(ev[1], s);
   k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit);
+  RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
+  rc = mlp_table(S, T2, "gbdmc_mlp_sim_step", 256);
+  if (rc) return rc;
   gbdmc_walkers_t wv{};
   wv.v = dst->v;
   if (S->noise_mode == GBDMC_NOISE_INJECTED)
-    k_count<GBDMC_NOISE_INJECTED, true><<<grid_for(T), T.tpb, 0, s>>>(*S, T, wv, ctrl, L.part, L.prefix, L.counts,
-                                                                       nz);
+    k_count<GBDMC_NOISE_INJECTED, true><<<grid_for(T2), T2.tpb, 0, s>>>(*S, T2, wv, ctrl, L.part, L.prefix,
+                                                                         L.counts, nz);
   else
-    k_count<GBDMC_NOISE_PHILOX32, true><<<grid_for(T), T.tpb, 0, s>>>(*S, T, wv, ctrl, L.part, L.prefix, L.counts,
-                                                                       nz);
-  launch_branch(T, dst->idx, ctrl, L.prefix, L.counts, s);
+    k_count<GBDMC_NOISE_PHILOX32, true><<<grid_for(T2), T2.tpb, 0, s>>>(*S, T2, wv, ctrl, L.part, L.prefix,
+                                                                         L.counts, nz);
+  launch_branch(T2, dst->idx, ctrl, L.prefix, L.counts, s);
   if (prof) {
     cudaEventRecord(ev[2], s);
     ++g_prof.count;

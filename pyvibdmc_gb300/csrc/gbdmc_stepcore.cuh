@@ -105,7 +105,16 @@ __device__ Partial reduce_partials(const Partial* part, int t0, int nt, long lon
   const int per = (nt + blockDim.x - 1) / blockDim.x;
   const int beg = min(nt, (int)threadIdx.x * per), end = min(nt, beg + per);
   Partial acc = partial_zero();
-  for (int j = beg; j < end; ++j) accumulate(acc, load_partial(part + t0 + j));
+  int j = beg;
+  for (; j + 4 <= end; j += 4) {  // four independent loads in flight
+    const Partial p0 = load_partial(part + t0 + j), p1 = load_partial(part + t0 + j + 1);
+    const Partial p2 = load_partial(part + t0 + j + 2), p3 = load_partial(part + t0 + j + 3);
+    accumulate(acc, p0);
+    accumulate(acc, p1);
+    accumulate(acc, p2);
+    accumulate(acc, p3);
+  }
+  for (; j < end; ++j) accumulate(acc, load_partial(part + t0 + j));
   if (prefix) {
     __shared__ long long wsum[kMaxTPB / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

@@ -431,3 +431,40 @@ class NNDMC:
             self._cur, self._lazy = 1 - self._cur, False
         n = int(self.ctrl().n)
         return from_soa(self._bufs[self._cur]["x"], n, 6)
+
+
+def _main(argv=None):
+    """Harvest -> train -> surrogate DMC of the water dimer, printing timings.
+
+    python -m pyvibdmc_gb300.surrogate --walkers 200000 --steps 200 --epochs 10
+    """
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--walkers", type=int, default=200000)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--harvest-walkers", type=int, default=200000)
+    ap.add_argument("--harvest-steps", type=int, default=210)
+    ap.add_argument("--engine", type=int, default=1)
+    a = ap.parse_args(argv)
+    from .potentials import water_dimer, WATER_DIMER_EQ
+    masses = [Constants.mass(s) for s in ("O", "H", "H", "O", "H", "H")]
+    pot = water_dimer()
+    t0 = time.perf_counter()
+    x, v, g, _ = harvest_training_data(pot, a.harvest_walkers, a.harvest_steps, 20, WATER_DIMER_EQ[None], masses,
+                                       seed=1, equil=min(20, a.harvest_steps // 2))
+    t1 = time.perf_counter()
+    m = MLPSurrogate(seed=0, engine=a.engine).fit(x, v, g, epochs=a.epochs)
+    t2 = time.perf_counter()
+    nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps + 1, seed=5, audit_every=100).init()
+    nd.run(a.steps)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    print(json.dumps(dict(samples=int(x.shape[1]), harvest_s=t1 - t0, train_s=t2 - t1, dmc_s=t3 - t2,
+                          rmse_cm=m.history[-1]["rmse_e_cm"] if m.history else None, audit=nd.audit(),
+                          population=int(nd.ctrl().n))))
+
+
+if __name__ == "__main__":
+    _main()
