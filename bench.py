@@ -199,6 +199,17 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------- ours
+def reduce_over_ranks(ms, walker_steps, dist, device):
+    """Whole-job figures of N independent replicas: the slowest rank's time
+    (max) and the walker-steps of all ranks (sum)."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ws = torch.tensor([walker_steps], dtype=torch.float64, device=device)
+    dist.all_reduce(ws, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(ws.item())
+
+
 def run_ours(args):
     import torch
     import pyvibdmc_gb300 as pg
@@ -273,12 +284,7 @@ def run_ours(args):
     pop = sim._hist["pop"][step0 - 1:step0 - 1 + K].cpu().numpy()
     walker_steps = float(pop.sum())  # population entering each timed step
     if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        ws = torch.tensor([walker_steps], device=dev, dtype=torch.float64)
-        dist.all_reduce(ws)
-        walker_steps = float(ws.item())
+        ms, walker_steps = reduce_over_ranks(ms, walker_steps, dist, dev)
     value = walker_steps / (ms / 1e3)
     ms_per_step = ms / K
 
@@ -399,6 +405,24 @@ def run_extras(steps):
     rej = sim._hist["rejected"][s0:s0 + steps].cpu().numpy()
     out["is_h2o_50k"] = {"walker_steps_per_s": float(pop.sum()) / secs, "us_per_step": secs / steps * 1e6,
                          "acceptance": float(1 - rej.sum() / pop.sum())}
+    # variance-normalised efficiency of importance sampling: ZPE error bar per unit time, 20000 walkers each
+    eff = {}
+    for tag, trial in (("plain", None), ("is", pg.h2o_gaussian_trial())):
+        T = 12000
+        sm = pg.DMC_Sim(num_walkers=20000, num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"],
+                        masses=masses, delta_t=DT, potential=pg.h2o_local_mode(), imp_samp=trial,
+                        start_structures=start_structures(20000, 9), seed=21, write_files=False, graph_steps=32)
+        sm._init_device()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sm._run_steps(T)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        vr = pg.Constants.convert(sm._hist["vref"].cpu().numpy()[T // 4:], "wavenumbers", to_AU=False)
+        z, e = pg.blocking_error(vr, 30)
+        eff[tag] = {"zpe_cm": z, "err_cm": e, "seconds": secs, "steps": T, "efficiency": 1.0 / (e * e * secs)}
+    eff["is_gain_at_equal_error"] = eff["is"]["efficiency"] / eff["plain"]["efficiency"]
+    out["is_vs_plain_h2o_20k"] = eff
     # batched ensemble: 64 replicas, N_r ~ U[1000, 65536] (seeded)
     ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
     th = np.deg2rad(104.5)

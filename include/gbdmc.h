@@ -290,6 +290,9 @@ typedef struct {
   float feat_hi[16];
   int32_t audit_every; /* walker audited (analytic PES, error recorded) when hash % audit_every == 0; 0 = off */
   int32_t engine;      /* 0: mma.sync BF16 kernels; 1: tcgen05 (TMEM accumulators, one thread per walker) */
+  float bias_beta;     /* online bias control: c <- (1-b) c + b <V_nn - V_analytic>_audit each step, and the
+                          next step's surrogate energies are V_nn - c (0 = off) */
+  int32_t pad;
 } gbdmc_mlp_t;
 
 /* fp32-coordinate walkers of the surrogate path (SoA [18][ld]) */
@@ -330,8 +333,9 @@ int gbdmc_dimer_features(const double* x_dev, int64_t ld, int64_t n, const float
 int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int64_t n, double* v_dev,
                      int32_t* outside_dev, int32_t* status_dev, void* stream);
 /* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
- * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[4] accumulates: audited
- * walkers, sum (V_nn - V_analytic), sum (V_nn - V_analytic)^2, fallbacks. */
+ * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[8] (zeroed by the caller before
+ * the first step): [0] audited walkers, [1] sum (V_nn - V_analytic), [2] sum (V_nn - V_analytic)^2,
+ * [3] fallbacks, [4] current bias correction c (hartree), [5..7] bookkeeping of the bias control. */
 int gbdmc_mlp_sim_init(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
                        gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
 int gbdmc_mlp_sim_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,

@@ -72,7 +72,8 @@ class MLP(C.Structure):
                 ("b2", C.c_void_p), ("b3", C.c_void_p), ("w4", C.c_void_p), ("b4", C.c_float),
                 ("e_mean", C.c_float), ("e_scale", C.c_float), ("hull_margin", C.c_float),
                 ("feat_mu", C.c_float * 16), ("feat_inv_sd", C.c_float * 16), ("feat_lo", C.c_float * 16),
-                ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("engine", C.c_int32)]
+                ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("engine", C.c_int32),
+                ("bias_beta", C.c_float), ("pad", C.c_int32)]
 
 
 class WalkersF32(C.Structure):

@@ -97,6 +97,7 @@ int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, l
                          int* err, cudaStream_t s);
 int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_mlp_t& net,
                               const gbdmc_walkers_f32_t& in, const gbdmc_walkers_f32_t& out, gbdmc_ctrl_t* ctrl,
-                              int* list, unsigned char* flags, const gbdmc_noise_t& nz, cudaStream_t s);
+                              int* list, unsigned char* flags, const double* audit, const gbdmc_noise_t& nz,
+                              cudaStream_t s);
 
 }  // namespace gbdmc

@@ -436,9 +436,10 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
                                                           const __grid_constant__ gbdmc_mlp_t net,
                                                           const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
                                                           gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
-                                                          const gbdmc_noise_t nz) {
+                                                          const double* audit, const gbdmc_noise_t nz) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
+  const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
   load_net(sm, net);
   __syncthreads();
   const int64_t ld = S.ld;
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
     const int row = g + 8 * t;
     const int64_t i = i0 + row;
     if (t < 2 && i < n)
-      out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi);
+      out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(t == 0 ? e_lo : e_hi) - corr;
     __syncwarp();
   }
 }
@@ -539,8 +540,9 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     const gbdmc_ctrl_t* ctrls, const int* list,
-                                                    const unsigned char* flags, double* audit) {
+                                                    const unsigned char* flags, double* audit, float beta) {
   const int64_t ld = S.ld;
+  const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
   const int part = threadIdx.x & 7;
   for (int r = 0; r < T.nrep; ++r) {
     const gbdmc_ctrl_t* ctrl = ctrls + r;
@@ -570,7 +572,7 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
       if (live && part == 0) {
         const unsigned char fl = flags[dst];
         if (fl & 2) {
-          const double d = out.v[dst] - v;
+          const double d = (out.v[dst] + c_used) - v;  // error of the raw network energy
           atomicAdd(audit + 0, 1.0);
           atomicAdd(audit + 1, d);
           atomicAdd(audit + 2, d * d);
@@ -579,6 +581,24 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
         out.v[dst] = v;
       }
     }
+  }
+  // last block: c <- (1 - beta) c + beta * (mean audited error of this step)
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned long long t = atomicAdd(reinterpret_cast<unsigned long long*>(audit + 7), 1ull);
+    am_last = (t == (unsigned long long)gridDim.x - 1ull);
+  }
+  __syncthreads();
+  if (am_last && threadIdx.x == 0) {
+    __threadfence();
+    const double cnt = *(volatile double*)(audit + 0) - audit[5];
+    const double sum = *(volatile double*)(audit + 1) - audit[6];
+    if (beta > 0.f && cnt > 0.0) audit[4] = (1.0 - (double)beta) * c_used + (double)beta * (sum / cnt);
+    audit[5] = audit[0];
+    audit[6] = audit[1];
+    *reinterpret_cast<unsigned long long*>(audit + 7) = 0ull;
   }
 }
 
@@ -868,13 +888,14 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
   if (prof) cudaEventRecord(ev[0], s);
   if (net->engine == 1) {
-    rc = launch_mlp_tc_move_energy(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz, s);
+    rc = launch_mlp_tc_move_energy(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, audit, nz, s);
     if (rc) return rc;
   } else {
-    k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, nz);
+    k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, audit,
+                                                          nz);
   }
   if (prof) cudaEventRecord(ev[1], s);
-  k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit);
+  k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
   rc = mlp_table(S, T2, "gbdmc_mlp_sim_step", 256);
   if (rc) return rc;

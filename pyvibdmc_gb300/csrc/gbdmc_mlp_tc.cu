@@ -259,9 +259,10 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
                                                                   const gbdmc_walkers_f32_t in,
                                                                   gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls,
                                                                   int* list, unsigned char* flags,
-                                                                  const gbdmc_noise_t nz) {
+                                                                  const double* audit, const gbdmc_noise_t nz) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
+  const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
   uint32_t tmem, mbar, phase = 0;
   setup(sm, net, tmem, mbar);
   bool ok = true;
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
       walker_features(xs, net, f);
     }
     const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
-    if (i < n) out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4);
+    if (i < n) out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4) - corr;
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
       break;
@@ -341,7 +342,8 @@ int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, l
 
 int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_mlp_t& net,
                               const gbdmc_walkers_f32_t& in, const gbdmc_walkers_f32_t& out, gbdmc_ctrl_t* ctrl,
-                              int* list, unsigned char* flags, const gbdmc_noise_t& nz, cudaStream_t s) {
+                              int* list, unsigned char* flags, const double* audit, const gbdmc_noise_t& nz,
+                              cudaStream_t s) {
   const cudaError_t e = cudaFuncSetAttribute((const void*)tc::k_mlp_tc_move_energy,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes());
   if (e != cudaSuccess) {
@@ -350,7 +352,8 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   }
   int g = T.tile_off[T.nrep];
   if (g > 2 * num_sms()) g = 2 * num_sms();
-  tc::k_mlp_tc_move_energy<<<g, tc::kThreads, tc_smem_bytes(), s>>>(S, T, net, in, out, ctrl, list, flags, nz);
+  tc::k_mlp_tc_move_energy<<<g, tc::kThreads, tc_smem_bytes(), s>>>(S, T, net, in, out, ctrl, list, flags, audit,
+                                                                     nz);
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 

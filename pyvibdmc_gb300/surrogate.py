@@ -13,7 +13,11 @@
 * :class:`NNDMC` -- discrete-weighting DMC of the dimer with fp32 walker
   coordinates on the surrogate; a random 1/``audit_every`` of the walkers and
   every walker outside the training box get the analytic FP64 energy, and the
-  audited differences are accumulated as the surrogate's error estimate.
+  audited differences are accumulated as the surrogate's error estimate.  With
+  ``bias_control`` = b > 0 the mean audited error of each step updates an
+  exponential moving average c <- (1-b) c + b <V_nn - V>, and the surrogate
+  energies of the next step are V_nn - c: the analytic PES, which judges the
+  surrogate, also removes its mean error on the current walker distribution.
 """
 import ctypes as C
 import math
@@ -80,7 +84,7 @@ class MLPSurrogate:
                        W2n=_bf16_bits(P["W2"]), W3n=_bf16_bits(P["W3"]))
 
     # ---------------------------------------------------------- inference
-    def net_struct(self, audit_every=0, engine=None):
+    def net_struct(self, audit_every=0, engine=None, bias_beta=0.0):
         n = _capi.MLP()
         n.w1t, n.w2t, n.w3t = self.bf["W1t"].data_ptr(), self.bf["W2t"].data_ptr(), self.bf["W3t"].data_ptr()
         n.b1, n.b2, n.b3 = self.P["b1"].data_ptr(), self.P["b2"].data_ptr(), self.P["b3"].data_ptr()
@@ -92,6 +96,7 @@ class MLPSurrogate:
             n.feat_mu[q], n.feat_inv_sd[q], n.feat_lo[q], n.feat_hi[q] = mu[q], isd[q], lo[q], hi[q]
         n.audit_every = int(audit_every)
         n.engine = int(self.engine if engine is None else engine)
+        n.bias_beta = float(bias_beta)
         return n
 
     def energy_soa(self, x32, n, ld=None, engine=None):
@@ -281,7 +286,7 @@ class NNDMC:
     """Surrogate DMC of the water dimer (discrete weighting, fp32 coordinates)."""
 
     def __init__(self, surrogate, potential, num_walkers, start_structures, masses, delta_t, num_timesteps, seed=0,
-                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0):
+                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0, bias_control=0.02):
         if not isinstance(potential, Potential_GPU) or potential.kind != "water_dimer":
             raise TypeError("the audit/fallback potential must be the analytic water_dimer Potential_GPU")
         self.model, self.potential = surrogate, potential
@@ -307,7 +312,7 @@ class NNDMC:
         L = _capi.load()
         self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
         self._scratch = torch.zeros(L.gbdmc_scratch_bytes(cap), dtype=torch.uint8, device=dev)
-        self._audit = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._audit = torch.zeros(8, dtype=torch.float64, device=dev)
         self._hist = dict(vref=torch.zeros(self.T, dtype=torch.float64, device=dev),
                           pop=torch.zeros(self.T, dtype=torch.float64, device=dev))
         s = _capi.Sim()
@@ -323,7 +328,7 @@ class NNDMC:
         s.trial.kind, s.trial.natoms = _capi.TRIAL_NONE, 6
         s.hist.vref, s.hist.pop, s.hist.len = self._hist["vref"].data_ptr(), self._hist["pop"].data_ptr(), self.T
         self._sim = s
-        self._net = surrogate.net_struct(audit_every)
+        self._net = surrogate.net_struct(audit_every, bias_beta=bias_control)
         self._n_start = len(x0)
         self._graphs = {}
         self.step = 0
@@ -420,7 +425,8 @@ class NNDMC:
         a = self._audit.cpu().numpy()
         n = max(a[0], 1.0)
         w = Constants.atomic_units["wavenumbers"]
-        return dict(audited=int(a[0]), mean_cm=a[1] / n / w, rms_cm=math.sqrt(a[2] / n) / w, fallbacks=int(a[3]))
+        return dict(audited=int(a[0]), mean_cm=a[1] / n / w, rms_cm=math.sqrt(a[2] / n) / w, fallbacks=int(a[3]),
+                    bias_correction_cm=a[4] / w)
 
     def walkers(self):
         if self._lazy:
@@ -437,18 +443,27 @@ def _main(argv=None):
     """Harvest -> train -> surrogate DMC of the water dimer, printing timings.
 
     python -m pyvibdmc_gb300.surrogate --walkers 200000 --steps 200 --epochs 10
+    python -m pyvibdmc_gb300.surrogate --steps 6000 --compare   # ZPE: surrogate (with and
+        without bias control) against the analytic FP64 dimer DMC, same walkers, steps, seed
     """
     import argparse
     import json
-    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap = argparse.ArgumentParser(description=_main.__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--walkers", type=int, default=200000)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--harvest-walkers", type=int, default=200000)
     ap.add_argument("--harvest-steps", type=int, default=210)
     ap.add_argument("--engine", type=int, default=1)
+    ap.add_argument("--bias-control", type=float, default=0.02)
+    ap.add_argument("--audit-every", type=int, default=100)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--compare", action="store_true",
+                    help="also run without bias control and the FP64 analytic DMC; report ZPEs")
     a = ap.parse_args(argv)
     from .potentials import water_dimer, WATER_DIMER_EQ
+    from .engine import DMC_Sim
+    from .batch import blocking_error
     masses = [Constants.mass(s) for s in ("O", "H", "H", "O", "H", "H")]
     pot = water_dimer()
     t0 = time.perf_counter()
@@ -457,13 +472,37 @@ def _main(argv=None):
     t1 = time.perf_counter()
     m = MLPSurrogate(seed=0, engine=a.engine).fit(x, v, g, epochs=a.epochs)
     t2 = time.perf_counter()
-    nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps + 1, seed=5, audit_every=100).init()
-    nd.run(a.steps)
-    torch.cuda.synchronize()
-    t3 = time.perf_counter()
-    print(json.dumps(dict(samples=int(x.shape[1]), harvest_s=t1 - t0, train_s=t2 - t1, dmc_s=t3 - t2,
-                          rmse_cm=m.history[-1]["rmse_e_cm"] if m.history else None, audit=nd.audit(),
-                          population=int(nd.ctrl().n))))
+    out = dict(samples=int(x.shape[1]), harvest_s=t1 - t0, train_s=t2 - t1,
+               rmse_cm=m.history[-1]["rmse_e_cm"] if m.history else None)
+    start = a.steps // 4
+    warm = min(32, a.steps // 2)
+
+    def timed(run):
+        run(warm)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run(a.steps - warm)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e3 / max(a.steps - warm, 1)
+
+    for label, beta in (("nn", a.bias_control),) + ((("nn_uncorrected", 0.0),) if a.compare else ()):
+        nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps, seed=a.seed,
+                   audit_every=a.audit_every, bias_control=beta).init()
+        us = timed(nd.run)
+        out[label] = dict(us_per_step=us, audit=nd.audit(), population=int(nd.ctrl().n),
+                          zpe_cm=nd.zpe(start=start) if a.steps >= 40 else None)
+    if a.compare:
+        sim = DMC_Sim(num_walkers=a.walkers, num_timesteps=a.steps, equil_steps=10 ** 9,
+                      atoms=["O", "H", "H"] * 2, masses=masses, delta_t=10.0, potential=pot,
+                      start_structures=WATER_DIMER_EQ[None], seed=a.seed, write_files=False)
+        sim._init_device()
+        us = timed(sim._run_steps)
+        vv = Constants.convert(sim._hist["vref"][:a.steps].cpu().numpy(), "wavenumbers", to_AU=False)
+        out["fp64"] = dict(us_per_step=us, population=int(sim._read_ctrl().n),
+                           zpe_cm=blocking_error(vv[start:], 20) if a.steps >= 40 else None)
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

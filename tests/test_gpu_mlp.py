@@ -137,6 +137,19 @@ def test_training_reduces_loss_and_surrogate_dmc_runs():
     assert np.isfinite(nd.vref_history()).all()
     assert len(nd.walkers()) == int(nd.ctrl().n)
 
+    # online bias control: a network shifted by +d converges to a correction larger by d
+    w = pg.Constants.atomic_units["wavenumbers"]
+    corr = []
+    for shift in (0.0, 150.0):
+        nb = NNDMC(m, pot, 3000, pg.WATER_DIMER_EQ[None], masses, 10.0, 200, seed=5, audit_every=10,
+                   bias_control=0.2)
+        nb._net.e_mean += shift * w
+        nb.init().run(200)
+        a = nb.audit()
+        assert abs(a["bias_correction_cm"] - a["mean_cm"]) < 15.0, a
+        corr.append(a["bias_correction_cm"])
+    assert abs((corr[1] - corr[0]) - 150.0) < 10.0, corr
+
 
 def test_tcgen05_forward_matches_mma_sync_forward():
     """The tcgen05/TMEM inference kernel computes the same BF16 network as the
