@@ -91,6 +91,18 @@ __device__ __forceinline__ uint32_t splitmix32(uint32_t z) {
   return z ^ (z >> 16);
 }
 
+// Exact float -> double widening with integer operations only (the FP64 pipe
+// of GB300 is narrow; a conversion costs about two DFMA slots there).  Valid
+// for zero and normal floats, which is everything the fp32 Box-Muller below
+// produces: |z| is either 0 or >= 2^-11.5 * |cospi(0.5 - 2^-23)| > 1e-10.
+__device__ __forceinline__ double widen_f32(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  const uint64_t mag = ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)(sign | (e ? mag : 0ull)));
+}
+
 // Fill z[0..n) with standard normals for the chosen noise mode.
 template <int NM, int N>
 __device__ __forceinline__ void gen_normals(Rng& g, double (&z)[N]) {
@@ -99,8 +111,8 @@ __device__ __forceinline__ void gen_normals(Rng& g, double (&z)[N]) {
     for (int k = 0; k < N; k += 2) {
       float a, b;
       g.normal2_f32(a, b);
-      z[k] = (double)a;
-      if (k + 1 < N) z[k + 1] = (double)b;
+      z[k] = widen_f32(a);
+      if (k + 1 < N) z[k + 1] = widen_f32(b);
     }
   } else {
 #pragma unroll
@@ -347,6 +359,39 @@ __device__ __forceinline__ T warp_sum(T v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
+// Order-preserving map of a double onto int64 (total order of the non-NaN
+// values, -0 < +0); min/max then run on the integer pipes.  Self-inverse.
+__device__ __forceinline__ long long dkey(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ double dkey_inv(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
+}
+__device__ __forceinline__ long long warp_min_key(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, (long long)__shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ long long warp_max_key(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+// Warp sums of a and b with five fp64 adds per lane instead of ten: after one
+// exchange lanes 0-15 reduce a and lanes 16-31 reduce b.  Fixed order; the
+// sums are returned in every lane.
+__device__ __forceinline__ void warp_sum2(double& a, double& b) {
+  const bool hi = (threadIdx.x & 16) != 0;
+  double keep = hi ? b : a;
+  const double send = hi ? a : b;
+  keep += __shfl_xor_sync(0xffffffffu, send, 16);
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+  a = __shfl_sync(0xffffffffu, keep, 0);
+  b = __shfl_sync(0xffffffffu, keep, 16);
+}
+
 __device__ __forceinline__ double warp_min(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));

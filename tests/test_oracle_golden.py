@@ -128,3 +128,24 @@ def test_pes_gradients_match_finite_differences():
             xm[:, a, d] -= h
             fdd[:, a, d] = (oracle.pes_dimer(xp, pd) - oracle.pes_dimer(xm, pd)) / (2 * h)
     np.testing.assert_allclose(gd, fdd, atol=1e-8)
+
+
+def test_philox_restatement_known_answers():
+    """Philox4x32-10 against the published known-answer vectors (Salmon et al., SC'11)."""
+    from oracle.philox_oracle import philox4x32_10
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+           ((0xFFFFFFFF,) * 4, (0xFFFFFFFF, 0xFFFFFFFF), (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+           ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+            (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, want in kat:
+        got = philox4x32_10(*[np.array([v], dtype=np.uint64) for v in ctr], *key)
+        assert tuple(int(g[0]) for g in got) == want
+
+
+def test_philox_normals_are_standard_normal():
+    from oracle.philox_oracle import philox_normals, philox_branch_uniform
+    for mode in ("philox32", "philox64"):
+        z, _ = philox_normals(99, 3, np.arange(200000), 9, mode)
+        assert abs(z.mean()) < 3e-3 and abs(z.std() - 1.0) < 3e-3
+        u = philox_branch_uniform(99, 3, np.arange(200000), 9, mode)
+        assert u.min() >= 0.0 and u.max() < 1.0 and abs(u.mean() - 0.5) < 3e-3
