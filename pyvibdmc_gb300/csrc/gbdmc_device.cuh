@@ -83,6 +83,15 @@ struct Rng {
   }
 };
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialisation may start while the previous kernel of its stream is still
+// running; griddepcontrol.wait returns once that kernel has completed and its
+// memory is visible (immediately when there is no programmatic dependency).
+// Every such kernel calls pdl_wait() before its first global-memory access,
+// then pdl_trigger() so that its own successor can be launched early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // 32-bit integer hash (SplitMix32-style finaliser) for audit sampling.
 __device__ __forceinline__ uint32_t splitmix32(uint32_t z) {
   z += 0x9E3779B9u;

@@ -99,6 +99,8 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
                                                    const __grid_constant__ RepTable T, const gbdmc_walkers_t in,
                                                    gbdmc_walkers_t out, gbdmc_ctrl_t* ctrls, Partial* part,
                                                    long long* prefix, int* counts, const gbdmc_noise_t nz) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t ld = S.ld;
   const int ntile = T.tile_off[T.nrep];
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
@@ -305,6 +307,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
 __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepTable T, int32_t* __restrict__ idx,
                                                      const gbdmc_ctrl_t* ctrls, const long long* prefix,
                                                      const int* counts) {
+  pdl_wait();
   const int ntile = T.tile_off[T.nrep];
   __shared__ int wsum[kMaxTPB / 32];
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
@@ -665,7 +668,7 @@ int grid_for(const RepTable& T) {
 
 void launch_branch(const RepTable& T, int32_t* idx, const gbdmc_ctrl_t* ctrl, const long long* prefix,
                    const int* counts, cudaStream_t s) {
-  k_branch<<<grid_for(T), T.tpb, 0, s>>>(T, idx, ctrl, prefix, counts);
+  launch_pdl(k_branch, grid_for(T), T.tpb, s, T, idx, ctrl, prefix, counts);
 }
 
 template <int PK, int A, int TK>
@@ -686,9 +689,11 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
   if (prof) cudaEventRecord(ev[0], s);
   if constexpr (!IS) {
     if (S.weighting == GBDMC_DISCRETE) {
+      // k_move is launched in stream order (its CTAs then spread one per SM, which
+      // its fp64 pipes need); k_branch may be launched while k_move finishes
       k_move<PK, A, NM, true, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      k_branch<<<G, T.tpb, 0, s>>>(T, dst.idx, ctrl, L.prefix, L.counts);
+      launch_pdl(k_branch, G, T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
       k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
@@ -699,7 +704,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
       k_count<NM, false><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
-      k_branch<<<G, T.tpb, 0, s>>>(T, dst.idx, ctrl, L.prefix, L.counts);
+      launch_pdl(k_branch, G, T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
       k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
     }
