@@ -231,6 +231,20 @@ int gbdmc_walkers_compact(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, i
                           const gbdmc_walkers_t* in, const gbdmc_walkers_t* out,
                           const gbdmc_ctrl_t* ctrl_dev, void* stream);
 
+/* One step of walkers held in page-locked host memory: the reference's
+ * propagate iteration (pyvibdmc.py:710-848) seen from the FFI, NumPy-style
+ * walker arrays in, the branched population out.  `host` holds the compact
+ * walkers [3A][sim->ld] -- x and v, plus who / f, psi, ke / w as the
+ * configuration uses them, no idx -- in memory from cudaHostAlloc or
+ * cudaHostRegister; the kernels read and write it directly over the host
+ * link (no staging copies).  `work` is a device walker set with idx.  The
+ * step runs host -> work, the compaction work -> host, and the control block
+ * is copied to ctrl_host (page-locked).  After the stream is synchronised,
+ * host holds the ctrl_host->n walkers of the next step in columns 0..n-1. */
+int gbdmc_sim_step_host(const gbdmc_sim_t* sim, const gbdmc_walkers_t* host, const gbdmc_walkers_t* work,
+                        gbdmc_ctrl_t* ctrl_dev, gbdmc_ctrl_t* ctrl_host, void* scratch_dev,
+                        const gbdmc_noise_t* noise, void* stream);
+
 /* Allocation-free step (no counterpart in the reference).  For callers that
  * cannot allocate device memory -- e.g. code running while a CUDA graph is
  * being captured, or a plug-in that is handed only its input and output

@@ -109,6 +109,8 @@ def load():
         "gbdmc_sim_init": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, P], C.c_int),
         "gbdmc_sim_step": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P,
                             C.POINTER(Noise), P], C.c_int),
+        "gbdmc_sim_step_host": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, P,
+                                 C.POINTER(Noise), P], C.c_int),
         "gbdmc_desc_weights": ([P, P, P, C.c_int64, P, P], C.c_int),
         "gbdmc_desc_begin": ([P, P, P], C.c_int),
         "gbdmc_batch_init": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers), P, P, P],

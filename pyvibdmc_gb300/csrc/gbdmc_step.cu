@@ -976,6 +976,54 @@ extern "C" int gbdmc_walkers_compact(const gbdmc_sim_t* S, const gbdmc_replica_t
   return GBDMC_ERR_ARG;
 }
 
+// Device alias of a page-locked host pointer (NULL stays NULL); false when p
+// is not host memory the device can address.
+static bool host_alias(const void* p, void** d) {
+  *d = nullptr;
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+  *d = a.devicePointer;
+  return true;
+}
+
+extern "C" int gbdmc_sim_step_host(const gbdmc_sim_t* S, const gbdmc_walkers_t* host, const gbdmc_walkers_t* work,
+                                   gbdmc_ctrl_t* ctrl, gbdmc_ctrl_t* ctrl_host, void* scratch,
+                                   const gbdmc_noise_t* noise, void* stream) {
+  if (!S || !host || !work || !ctrl || !ctrl_host || !host->x || !host->v || host->idx || !work->x || !work->v) {
+    set_error("gbdmc_sim_step_host: invalid arguments (host walkers need x and v and no idx)");
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_walkers_t h = {};
+  void* d[7];
+  const void* hp[7] = {host->x, host->v, host->who, host->f, host->psi, host->ke, host->w};
+  for (int k = 0; k < 7; ++k) {
+    if (!host_alias(hp[k], &d[k])) {
+      set_error("gbdmc_sim_step_host: host walker array %d is not page-locked host memory", k);
+      return GBDMC_ERR_ARG;
+    }
+  }
+  h.x = (double*)d[0];
+  h.v = (double*)d[1];
+  h.who = (int32_t*)d[2];
+  h.f = (double*)d[3];
+  h.psi = (double*)d[4];
+  h.ke = (double*)d[5];
+  h.w = (double*)d[6];
+  int rc = gbdmc_sim_step(S, &h, work, ctrl, scratch, noise, stream);
+  if (rc) return rc;
+  rc = gbdmc_walkers_compact(S, nullptr, 0, work, &h, ctrl, stream);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(ctrl_host, ctrl, sizeof(gbdmc_ctrl_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream) !=
+      cudaSuccess)
+    return check_launch("gbdmc_sim_step_host: control block copy");
+  return GBDMC_OK;
+}
+
 extern "C" int gbdmc_desc_weights(const int32_t* who, const double* w, const int64_t* n_dev, int64_t n_parent,
                                   double* desc, void* stream) {
   if (!who || !n_dev || !desc || n_parent < 0) {

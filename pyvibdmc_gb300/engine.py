@@ -31,7 +31,7 @@ from . import archive
 from .constants import Constants, get_atomic_num
 from .potentials import Potential_GPU, default_device, to_soa, from_soa
 
-__all__ = ["DMC_Sim", "dmc_restart"]
+__all__ = ["DMC_Sim", "HostWalkers", "dmc_restart"]
 
 _MASSIVE = "Massive walker birth or death event!!!!!!! Dying..."
 
@@ -568,6 +568,92 @@ class DMC_Sim:
         o = len(v) // 4 if onwards is None else onwards
         z = np.average(v[o:])
         return Constants.convert(z, "wavenumbers", to_AU=False) if ret_cm else z
+
+
+class HostWalkers:
+    """The walkers of a :class:`DMC_Sim` held in page-locked host memory and
+    stepped there with ``gbdmc_sim_step_host``.
+
+    The kernels read the walkers from host memory and write the branched
+    population back over the host link, so every step starts and ends with
+    the walkers on the host -- the way the reference's ``propagate`` loop
+    holds them in NumPy arrays (``pyvibdmc.py:710-848``).  ``step()`` queues
+    one step, waits for it and returns the new population; ``x``, ``v`` (and
+    ``who``, IS and continuous-weight arrays) are the pinned SoA arrays
+    ``[3A][ld]`` whose first ``n`` columns are valid.  Philox noise only.
+    With ``graph`` the step's launches are captured once into a CUDA graph
+    and replayed.  While in use, the simulation is stepped only through this
+    object; ``close()`` puts the walkers back into the simulation's device
+    buffers.
+    """
+
+    def __init__(self, sim, graph=True):
+        self.graph = bool(graph)
+        self._graph = None
+        if sim._noise_mode == _capi.NOISE_INJECTED:
+            raise ValueError("HostWalkers steps with Philox deviates (rng='philox32' or 'philox64')")
+        sim._compact()
+        torch.cuda.synchronize()
+        self.sim = sim
+        b = sim._bufs[sim._cur]
+        self.host = {k: torch.empty(t.shape, dtype=t.dtype).pin_memory() for k, t in b.items() if k != "idx"}
+        for k, t in self.host.items():
+            t.copy_(b[k])
+        self.work = sim._bufs[1 - sim._cur]
+        self.ctrl_host = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8).pin_memory()
+        self._h = sim._walker_struct(self.host, False)
+        self._w = sim._walker_struct(self.work, True)
+        self.n = int(sim._read_ctrl().n)
+        torch.cuda.synchronize()
+
+    def __getattr__(self, name):
+        host = self.__dict__.get("host", {})
+        if name in host:
+            return host[name]
+        raise AttributeError(name)
+
+    def ctrl(self):
+        return _capi.Ctrl.from_address(self.ctrl_host.data_ptr())
+
+    def _queue(self):
+        sim = self.sim
+        rc = _capi.load().gbdmc_sim_step_host(
+            C.byref(sim._sim), C.byref(self._h), C.byref(self._w), C.c_void_p(sim._ctrl.data_ptr()),
+            C.c_void_p(self.ctrl_host.data_ptr()), C.c_void_p(sim._scratch.data_ptr()), None, sim._stream())
+        _capi.check(rc, "gbdmc_sim_step_host")
+
+    def step(self):
+        if not self.graph:
+            self._queue()
+        else:
+            # the step's launches and copies are captured once and replayed: the walker
+            # arrays and the control block never move, and every launch reads N from
+            # the device control block
+            if self._graph is None:
+                g = torch.cuda.CUDAGraph()
+                side = torch.cuda.Stream(device=self.sim.device)
+                side.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.graph(g, stream=side):
+                    self._queue()
+                torch.cuda.current_stream().wait_stream(side)
+                self._graph = g
+            self._graph.replay()
+        torch.cuda.current_stream().synchronize()
+        c = self.ctrl()
+        if c.status:
+            raise ValueError(f"Massive walker birth or death event!!!!!!! Dying... (status {c.status})")
+        self.n = int(c.n)
+        return self.n
+
+    def close(self):
+        """Copy the walkers back into the simulation's device buffers."""
+        sim = self.sim
+        b = sim._bufs[sim._cur]
+        for k, t in self.host.items():
+            b[k].copy_(t)
+        sim._lazy = False
+        sim.cur_timestep = int(sim._read_ctrl().step)
+        torch.cuda.synchronize()
 
 
 def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsamp=None, **kw):

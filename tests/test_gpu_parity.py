@@ -191,6 +191,38 @@ def test_philox_graph_batching_is_deterministic():
     assert np.array_equal(runs[0][1], runs[1][1])
 
 
+@pytest.mark.parametrize("imp,graph", [(False, False), (False, True), (True, True)])
+def test_host_resident_step_matches_device_step(imp, graph):
+    """gbdmc_sim_step_host (walkers in page-locked host memory, read and written by
+    the kernels) reproduces the device-resident step bit for bit."""
+    _, m = oracle.h2o_config()
+    x0 = geoms(3000, seed=8, scale=0.05)
+
+    def mk():
+        return pg.DMC_Sim(num_walkers=3000, num_timesteps=50, equil_steps=1000, atoms=["O", "H", "H"], masses=m,
+                          delta_t=10.0, potential=pg.h2o_local_mode(),
+                          imp_samp=pg.h2o_gaussian_trial() if imp else None, start_structures=x0, seed=77,
+                          write_files=False)
+
+    a, b = mk(), mk()
+    a._init_device()
+    b._init_device()
+    hw = pg.HostWalkers(b, graph=graph)
+    for _ in range(20):
+        a._cur, a._lazy = a._launch_step(a._cur, a._lazy)
+        n = hw.step()
+    a._compact()
+    na = int(a._read_ctrl().n)
+    assert n == na
+    ba = a._bufs[a._cur]
+    for k in ("x", "v", "who") + (("f", "psi", "ke") if imp else ()):
+        got = hw.host[k][..., :n].numpy()
+        want = ba[k][..., :n].cpu().numpy()
+        assert np.array_equal(got, want), k
+    hw.close()
+    assert b.cur_timestep == 20 and np.array_equal(b._coords_host(), a._coords_host())
+
+
 @pytest.mark.parametrize("rng", ["philox32", "philox64"])
 def test_philox_noise_and_branching_match_oracle_stream(rng):
     """Two steps of water in a Philox mode.  Each step's moved walkers (pre-branch
