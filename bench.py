@@ -427,6 +427,31 @@ def run_extras(steps):
         eff[tag] = {"zpe_cm": z, "err_cm": e, "seconds": secs, "steps": T, "efficiency": 1.0 / (e * e * secs)}
     eff["is_gain_at_equal_error"] = eff["is"]["efficiency"] / eff["plain"]["efficiency"]
     out["is_vs_plain_h2o_20k"] = eff
+    # importance sampling + batching: 64 IS replicas (N_r ~ U[1000, 65536]); the ensemble
+    # estimate is the N0-weighted mean of the replicas' vref at each step
+    ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
+    th = np.deg2rad(104.5)
+    eq = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [1.81 * np.cos(th), 1.81 * np.sin(th), 0.0]])
+    Tb = 4000
+    bi = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, Tb + 16, imp_samp=pg.h2o_gaussian_trial(),
+                      seed=5, start_noise=0.05, graph_steps=16)
+    bi.init()
+    bi.autotune(steps_per_candidate=2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bi.run(Tb)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0 + 0.0
+    s0 = bi.step - Tb
+    w = np.asarray(ns, dtype=float)
+    vr = pg.Constants.convert(bi.vref_history()[:, s0:bi.step], "wavenumbers", to_AU=False)
+    ens = (w[:, None] * vr).sum(0) / w.sum()
+    z, e = pg.blocking_error(ens[Tb // 4:], 30)
+    ws = bi.walker_steps(s0, bi.step)
+    isb = {"replicas": len(ns), "walkers_total": int(sum(ns)), "steps": Tb, "seconds": secs,
+           "walker_steps_per_s": ws / secs, "zpe_cm": z, "err_cm": e, "efficiency": 1.0 / (e * e * secs)}
+    isb["gain_vs_plain_h2o_20k_at_equal_error"] = isb["efficiency"] / eff["plain"]["efficiency"]
+    out["is_batched_64_replicas_h2o"] = isb
     # batched ensemble: 64 replicas, N_r ~ U[1000, 65536] (seeded)
     ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
     th = np.deg2rad(104.5)
