@@ -485,7 +485,7 @@ def run_extras(steps):
     torch.cuda.synchronize()
     s0 = nd.step
     _, secs = _timed_graph_rate(nd.run, lambda: 0, steps)
-    ph = nd._hist["pop"][s0 - 1:s0 - 1 + steps].cpu().numpy()
+    nn_ws = nd.walker_steps(s0, s0 + steps)
     fp = pg.DMC_Sim(num_walkers=200000, num_timesteps=steps + 64, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
                     masses=dm, delta_t=DT, potential=pot, start_structures=pg.WATER_DIMER_EQ[None], seed=5,
                     write_files=False)
@@ -495,7 +495,7 @@ def run_extras(steps):
     f0 = int(fp._read_ctrl().step)
     _, fsecs = _timed_graph_rate(fp._run_steps, lambda: 0, steps)
     pf = fp._hist["pop"][f0 - 1:f0 - 1 + steps].cpu().numpy()
-    out["surrogate_dimer_200k"] = {"walker_steps_per_s": float(ph.sum()) / secs, "us_per_step": secs / steps * 1e6,
+    out["surrogate_dimer_200k"] = {"walker_steps_per_s": nn_ws / secs, "us_per_step": secs / steps * 1e6,
                                    "fp64_analytic_walker_steps_per_s": float(pf.sum()) / fsecs,
                                    "fp64_analytic_us_per_step": fsecs / steps * 1e6,
                                    "harvest_s": t_h, "train_s": t_t, "train_samples": int(x.shape[1]),

@@ -75,7 +75,9 @@ typedef struct {
 enum {
   GBDMC_TRIAL_NONE = 0,
   GBDMC_TRIAL_HO_GAUSS = 1,  /* p[a] = alpha of atom a; separable Cartesian Gaussian        */
-  GBDMC_TRIAL_H2O_GAUSS = 2  /* O,H,H; p = alpha_r1, alpha_r2, alpha_th, r1e, r2e, theta_e  */
+  GBDMC_TRIAL_H2O_GAUSS = 2, /* O,H,H; p = alpha_r1, alpha_r2, alpha_th, r1e, r2e, theta_e  */
+  GBDMC_TRIAL_DIMER_GAUSS = 3 /* O,H,H,O,H,H: the H2O trial of each monomer times a Gaussian in
+                                 R_OO; p = the six H2O parameters, alpha_R, R_e                */
 };
 
 typedef struct {
@@ -309,12 +311,18 @@ typedef struct {
   int32_t pad;
 } gbdmc_mlp_t;
 
-/* fp32-coordinate walkers of the surrogate path (SoA [18][ld]) */
+/* fp32-coordinate walkers of the surrogate path (SoA [18][ld]).  With a trial
+ * wave function (sim->trial.kind = GBDMC_TRIAL_DIMER_GAUSS) the walkers also
+ * carry the drift d ln psi/dx (f, [18][ld]), ln psi and the local kinetic
+ * energy, all fp32, and v holds the local energy V + KE. */
 typedef struct {
   float* x;
   double* v;
   int32_t* who;
   int32_t* idx;
+  float* f;
+  float* lnpsi;
+  float* ke;
 } gbdmc_walkers_f32_t;
 
 /* Training kernels.  Y[M x 128] = X[M x K] W + b (K = 16 or 128; X fp32 rounded to bf16). */
@@ -349,7 +357,12 @@ int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int
 /* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
  * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[8] (zeroed by the caller before
  * the first step): [0] audited walkers, [1] sum (V_nn - V_analytic), [2] sum (V_nn - V_analytic)^2,
- * [3] fallbacks, [4] current bias correction c (hartree), [5..7] bookkeeping of the bias control. */
+ * [3] fallbacks, [4] current bias correction c (hartree), [5..7] bookkeeping of the bias control.
+ * With sim->trial.kind = GBDMC_TRIAL_DIMER_GAUSS (tcgen05 engine only) the step is importance sampled
+ * (pyvibdmc.py:549-612 in fp32: drift-diffusion proposal, trial at the proposal, Metropolis test, local
+ * energy V_nn + KE, weights with dt_eff = dt * accepted / N).  The batch_ forms run nrep replicas laid out
+ * as gbdmc_replica_t slot ranges, one control block each (scratch: gbdmc_batch_scratch_bytes); the audit
+ * statistics and the bias correction are shared by all replicas. */
 int gbdmc_mlp_sim_init(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
                        gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
 int gbdmc_mlp_sim_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,
@@ -357,6 +370,14 @@ int gbdmc_mlp_sim_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbd
                        const gbdmc_noise_t* noise, void* stream);
 int gbdmc_mlp_compact(const gbdmc_sim_t* sim, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
                       const gbdmc_ctrl_t* ctrl_dev, void* stream);
+int gbdmc_mlp_batch_init(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps, int32_t nrep,
+                         const gbdmc_walkers_f32_t* w, gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
+int gbdmc_mlp_batch_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps, int32_t nrep,
+                         const gbdmc_walkers_f32_t* src, const gbdmc_walkers_f32_t* dst, gbdmc_ctrl_t* ctrl_dev,
+                         void* scratch_dev, double* audit_dev, const gbdmc_noise_t* noise, void* stream);
+int gbdmc_mlp_batch_compact(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                            const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
+                            const gbdmc_ctrl_t* ctrl_dev, void* stream);
 
 /* ---- measurement aids (no counterpart in the reference; used by bench.py) ----
  * gbdmc_prof_enable(1) makes every later gbdmc_sim_step record CUDA events

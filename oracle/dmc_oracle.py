@@ -19,7 +19,7 @@ __all__ = [
     "WAVENUMBERS", "ANGSTROMS", "AMU", "MASS_H", "MASS_O", "mass_au",
     "InjectedNoise", "splitmix64",
     "pes_ho", "pes_h2o_lm", "pes_dimer", "grad_ho", "grad_h2o_lm", "grad_dimer",
-    "h2o_internals", "TrialH2OGauss", "TrialHOGauss", "finite_diff",
+    "h2o_internals", "TrialH2OGauss", "TrialHOGauss", "TrialDimerGauss", "finite_diff",
     "metropolis", "local_kin", "move_randomly", "birth_or_death_discrete",
     "continuous_update_and_branch", "calc_vref", "calc_desc_wts",
     "OracleDMC", "ho_config", "h2o_config", "h2o_equilibrium", "h2o_trial_config", "dimer_config",
@@ -293,6 +293,48 @@ class TrialH2OGauss:
             first[:, atom] = f
             sec[:, atom] = f * f + t
         return first, sec
+
+
+class TrialDimerGauss:
+    """Trial for the water dimer (O,H,H,O,H,H) of the GPU engine: the
+    TrialH2OGauss of each monomer times (alpha_R/pi)^(1/4)
+    exp(-alpha_R (R_OO - R_e)^2 / 2).  The reference ships no dimer trial;
+    this restates the engine's, with the same derivative contract as
+    TrialH2OGauss (imp_samp_manager.py:202-224).  alpha = (a_r1, a_r2,
+    a_theta, a_R), qe = (r1e, r2e, theta_e, R_e)."""
+
+    def __init__(self, alpha, qe):
+        self.mono = (TrialH2OGauss(alpha[:3], qe[:3], 0, 1, 2), TrialH2OGauss(alpha[:3], qe[:3], 3, 4, 5))
+        self.aR, self.Re = float(alpha[3]), float(qe[3])
+
+    def _oo(self, x):
+        v = x[:, 3] - x[:, 0]
+        R = np.sqrt((v * v).sum(1))
+        return v, R
+
+    def psi(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        _, R = self._oo(x)
+        g = (self.aR / np.pi) ** 0.25 * np.exp(-self.aR * (R - self.Re) ** 2 / 2)
+        return self.mono[0].psi(x) * self.mono[1].psi(x) * g
+
+    def derivs(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        f = np.zeros_like(x)
+        t = np.zeros_like(x)
+        for m in self.mono:
+            fm, sm = m.derivs(x)
+            f += fm
+            t += sm - fm * fm  # d2 ln psi_m / dx2 (zero outside the monomer)
+        v, R = self._oo(x)
+        e = v / R[:, None]
+        L = (-self.aR * (R - self.Re))[:, None]
+        too = -self.aR * e * e + L * (1 - e * e) / R[:, None]
+        f[:, 3] += L * e
+        f[:, 0] -= L * e
+        t[:, 3] += too
+        t[:, 0] += too
+        return f, f * f + t
 
 
 class TrialHOGauss:

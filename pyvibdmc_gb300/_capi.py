@@ -14,7 +14,7 @@ MAX_ATOMS = 8
 OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY = 0, 1, 2, 3
 ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW, ST_TIMEOUT = 1, 2, 4, 8, 16, 32
 PES_HO, PES_H2O_LM, PES_DIMER = 1, 2, 3
-TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS = 0, 1, 2
+TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS, TRIAL_DIMER_GAUSS = 0, 1, 2, 3
 NOISE_PHILOX32, NOISE_PHILOX64, NOISE_INJECTED = 0, 1, 2
 DISCRETE, CONTINUOUS = 0, 1
 
@@ -77,7 +77,8 @@ class MLP(C.Structure):
 
 
 class WalkersF32(C.Structure):
-    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("idx", C.c_void_p)]
+    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("idx", C.c_void_p),
+                ("f", C.c_void_p), ("lnpsi", C.c_void_p), ("ke", C.c_void_p)]
 
 
 _STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32]
@@ -133,6 +134,12 @@ def load():
         "gbdmc_mlp_sim_step": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P,
                                 P, C.POINTER(Noise), P], C.c_int),
         "gbdmc_mlp_compact": ([C.POINTER(Sim), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P], C.c_int),
+        "gbdmc_mlp_batch_init": ([C.POINTER(Sim), C.POINTER(MLP), P, C.c_int32, C.POINTER(WalkersF32), P, P, P],
+                                 C.c_int),
+        "gbdmc_mlp_batch_step": ([C.POINTER(Sim), C.POINTER(MLP), P, C.c_int32, C.POINTER(WalkersF32),
+                                  C.POINTER(WalkersF32), P, P, P, C.POINTER(Noise), P], C.c_int),
+        "gbdmc_mlp_batch_compact": ([C.POINTER(Sim), P, C.c_int32, C.POINTER(WalkersF32), C.POINTER(WalkersF32),
+                                     P, P], C.c_int),
         "gbdmc_sim_step_static": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, C.POINTER(Noise), P],
                                   C.c_int),
         "gbdmc_sim_step_static_max_ld": ([], C.c_size_t),

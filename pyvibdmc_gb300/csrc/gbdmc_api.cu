@@ -147,6 +147,12 @@ extern "C" int gbdmc_trial_eval(const gbdmc_trial_t* t, const double* x, int64_t
       return GBDMC_ERR_ARG;
     }
     k_trial_eval<GBDMC_TRIAL_H2O_GAUSS, 3><<<G, kEvalTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
+  } else if (t->kind == GBDMC_TRIAL_DIMER_GAUSS) {
+    if (A != 6) {
+      set_error("gbdmc_trial_eval: dimer trial needs 6 atoms (got %d)", A);
+      return GBDMC_ERR_ARG;
+    }
+    k_trial_eval<GBDMC_TRIAL_DIMER_GAUSS, 6><<<G, kEvalTPB, 0, s>>>(*t, x, n, ld, psi, d1, d2);
   } else {
     set_error("gbdmc_trial_eval: unknown trial kind %d", t->kind);
     return GBDMC_ERR_ARG;

@@ -280,74 +280,122 @@ __device__ __forceinline__ double trial_ho(const double (&x)[3 * A], const doubl
 //   d1_k = sum_q L_q dq/dx_k
 //   d2_k = d1_k^2 + sum_q [ -alpha_q (dq/dx_k)^2 + L_q d2q/dx_k^2 ]
 // which equals the ChainRuleHelper d2psidx2 sum for a direct-product psi.
+// h2o_trial_terms adds the water's d ln psi / dx_k to f[] and its
+// d2 ln psi / dx_k^2 to t[] for the atoms (o, h1, h2) of x, and returns the
+// exponent -1/2 sum_q alpha_q (q - q_e)^2.  T is float (surrogate walkers)
+// or double.
+template <typename T>
+__device__ __forceinline__ T rsqrt_guard_t(T y) {
+  return y > T(0) ? T(1) / sqrt(y) : T(0);
+}
+
+template <typename T, int N>
+__device__ __forceinline__ T h2o_trial_terms(const T (&x)[N], const double* p, int o, int h1, int h2, T (&f)[N],
+                                             T (&t)[N]) {
+  const T a1 = (T)p[0], a2 = (T)p[1], ath = (T)p[2], r1e = (T)p[3], r2e = (T)p[4], the = (T)p[5];
+  T v1[3], v2[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v1[d] = x[3 * h1 + d] - x[3 * o + d];
+    v2[d] = x[3 * h2 + d] - x[3 * o + d];
+  }
+  const T r1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const T r2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const T ir1 = T(1) / r1, ir2 = T(1) / r2;
+  const T g = ir1 * ir2;
+  T c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) * g;
+  c = fmin(T(1), fmax(T(-1), c));
+  const T th = acos(c);
+  const T one_m_c2 = T(1) - c * c;
+  const T s = -rsqrt_guard_t(one_m_c2);  // dtheta/dcos
+  const T s2 = c * s * s * s;            // d2theta/dcos2 = -c/(1-c^2)^1.5
+  const T L1 = -a1 * (r1 - r1e), L2 = -a2 * (r2 - r2e), Lt = -ath * (th - the);
+  const T ir1s = ir1 * ir1, ir2s = ir2 * ir2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const T e1 = v1[d] * ir1, e2 = v2[d] * ir2;
+    // cos(theta) first derivatives
+    const T dch1 = v2[d] * g - c * ir1 * e1;
+    const T dch2 = v1[d] * g - c * ir2 * e2;
+    const T dco = -(dch1 + dch2);
+    // cos(theta) diagonal second derivatives
+    const T d2ch1 = c * (T(3) * e1 * e1 - T(1)) * ir1s - T(2) * v2[d] * e1 * ir1s * ir2;
+    const T d2ch2 = c * (T(3) * e2 * e2 - T(1)) * ir2s - T(2) * v1[d] * e2 * ir2s * ir1;
+    const T h = e1 * ir1 + e2 * ir2;
+    const T d2co = T(2) * g - T(2) * (v1[d] + v2[d]) * g * h +
+                   c * (h * h + (T(2) * e1 * e1 - T(1)) * ir1s + (T(2) * e2 * e2 - T(1)) * ir2s);
+    // theta derivatives
+    const T dth_o = s * dco, dth_1 = s * dch1, dth_2 = s * dch2;
+    const T d2th_o = s2 * dco * dco + s * d2co;
+    const T d2th_1 = s2 * dch1 * dch1 + s * d2ch1;
+    const T d2th_2 = s2 * dch2 * dch2 + s * d2ch2;
+    // r derivatives
+    const T d2r1 = (T(1) - e1 * e1) * ir1, d2r2 = (T(1) - e2 * e2) * ir2;
+    // O: depends on r1 (-e1), r2 (-e2), theta
+    f[3 * o + d] += -L1 * e1 - L2 * e2 + Lt * dth_o;
+    t[3 * o + d] += -a1 * e1 * e1 - a2 * e2 * e2 - ath * dth_o * dth_o + L1 * d2r1 + L2 * d2r2 + Lt * d2th_o;
+    // H1: r1 (+e1), theta
+    f[3 * h1 + d] += L1 * e1 + Lt * dth_1;
+    t[3 * h1 + d] += -a1 * e1 * e1 - ath * dth_1 * dth_1 + L1 * d2r1 + Lt * d2th_1;
+    // H2: r2 (+e2), theta
+    f[3 * h2 + d] += L2 * e2 + Lt * dth_2;
+    t[3 * h2 + d] += -a2 * e2 * e2 - ath * dth_2 * dth_2 + L2 * d2r2 + Lt * d2th_2;
+  }
+  return T(-0.5) * (a1 * (r1 - r1e) * (r1 - r1e) + a2 * (r2 - r2e) * (r2 - r2e) + ath * (th - the) * (th - the));
+}
+
 template <int A>
 __device__ __forceinline__ double trial_h2o(const double (&x)[3 * A], const double* p, double (&d1o)[3 * A],
                                             double (&d2o)[3 * A]) {
-  const double a1 = p[0], a2 = p[1], ath = p[2], r1e = p[3], r2e = p[4], the = p[5];
-  double v1[3], v2[3];
+  double t[3 * A];
+#pragma unroll
+  for (int k = 0; k < 3 * A; ++k) d1o[k] = t[k] = 0.0;
+  const double e = h2o_trial_terms(x, p, 0, 1, 2, d1o, t);
+  const double n = sqrt(sqrt(p[0] * p[1] * p[2] * (1.0 / (CUDART_PI * CUDART_PI * CUDART_PI))));
+#pragma unroll
+  for (int k = 0; k < 3 * A; ++k) d2o[k] = d1o[k] * d1o[k] + t[k];
+  return n * exp(e);
+}
+
+// Water dimer (O,H,H,O,H,H): the water trial of each monomer times a Gaussian
+// in the O-O distance, exp(-1/2 alpha_R (R - R_e)^2);
+// p = alpha_r1, alpha_r2, alpha_th, r1e, r2e, theta_e, alpha_R, R_e.
+// Returns ln psi without the normalisation; d1 = d ln psi/dx,
+// d2 = (d2 psi/dx2)/psi = d1^2 + d2 ln psi/dx2 per Cartesian component.
+template <typename T>
+__device__ __forceinline__ T dimer_trial_log(const T (&x)[18], const double* p, T (&d1)[18], T (&d2)[18]) {
+  T t[18];
+#pragma unroll
+  for (int k = 0; k < 18; ++k) d1[k] = t[k] = T(0);
+  T e = h2o_trial_terms(x, p, 0, 1, 2, d1, t) + h2o_trial_terms(x, p, 3, 4, 5, d1, t);
+  const T aR = (T)p[6], Re = (T)p[7];
+  T v[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = x[9 + d] - x[d];
+  const T R = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  const T iR = T(1) / R;
+  const T LR = -aR * (R - Re);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    v1[d] = x[3 + d] - x[d];
-    v2[d] = x[6 + d] - x[d];
+    const T ed = v[d] * iR;
+    const T tt = -aR * ed * ed + LR * (T(1) - ed * ed) * iR;
+    d1[9 + d] += LR * ed;
+    d1[d] -= LR * ed;
+    t[9 + d] += tt;
+    t[d] += tt;
   }
-  const double r1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
-  const double r2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
-  const double ir1 = 1.0 / r1, ir2 = 1.0 / r2;
-  const double g = ir1 * ir2;
-  double c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) * g;
-  c = fmin(1.0, fmax(-1.0, c));
-  const double th = acos(c);
-  const double one_m_c2 = 1.0 - c * c;
-  const double s = -rsqrt_guard(one_m_c2);      // dtheta/dcos
-  const double s2 = c * s * s * s;              // d2theta/dcos2 = -c/(1-c^2)^1.5
-  const double L1 = -a1 * (r1 - r1e), L2 = -a2 * (r2 - r2e), Lt = -ath * (th - the);
-  const double n = sqrt(sqrt(a1 * a2 * ath * (1.0 / (CUDART_PI * CUDART_PI * CUDART_PI))));
-  const double psi = n * exp(-0.5 * (a1 * (r1 - r1e) * (r1 - r1e) + a2 * (r2 - r2e) * (r2 - r2e) +
-                                     ath * (th - the) * (th - the)));
-  const double ir1s = ir1 * ir1, ir2s = ir2 * ir2;
+  e += T(-0.5) * aR * (R - Re) * (R - Re);
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const double e1 = v1[d] * ir1, e2 = v2[d] * ir2;
-    // cos(theta) first derivatives
-    const double dch1 = v2[d] * g - c * ir1 * e1;
-    const double dch2 = v1[d] * g - c * ir2 * e2;
-    const double dco = -(dch1 + dch2);
-    // cos(theta) diagonal second derivatives
-    const double d2ch1 = c * (3.0 * e1 * e1 - 1.0) * ir1s - 2.0 * v2[d] * e1 * ir1s * ir2;
-    const double d2ch2 = c * (3.0 * e2 * e2 - 1.0) * ir2s - 2.0 * v1[d] * e2 * ir2s * ir1;
-    const double h = e1 * ir1 + e2 * ir2;
-    const double d2co = 2.0 * g - 2.0 * (v1[d] + v2[d]) * g * h +
-                        c * (h * h + (2.0 * e1 * e1 - 1.0) * ir1s + (2.0 * e2 * e2 - 1.0) * ir2s);
-    // theta derivatives
-    const double dth_o = s * dco, dth_1 = s * dch1, dth_2 = s * dch2;
-    const double d2th_o = s2 * dco * dco + s * d2co;
-    const double d2th_1 = s2 * dch1 * dch1 + s * d2ch1;
-    const double d2th_2 = s2 * dch2 * dch2 + s * d2ch2;
-    // r derivatives
-    const double d2r1 = (1.0 - e1 * e1) * ir1, d2r2 = (1.0 - e2 * e2) * ir2;
-    // O: depends on r1 (-e1), r2 (-e2), theta
-    {
-      const double f = -L1 * e1 - L2 * e2 + Lt * dth_o;
-      const double t = -a1 * e1 * e1 - a2 * e2 * e2 - ath * dth_o * dth_o + L1 * d2r1 + L2 * d2r2 + Lt * d2th_o;
-      d1o[d] = f;
-      d2o[d] = f * f + t;
-    }
-    // H1: r1 (+e1), theta
-    {
-      const double f = L1 * e1 + Lt * dth_1;
-      const double t = -a1 * e1 * e1 - ath * dth_1 * dth_1 + L1 * d2r1 + Lt * d2th_1;
-      d1o[3 + d] = f;
-      d2o[3 + d] = f * f + t;
-    }
-    // H2: r2 (+e2), theta
-    {
-      const double f = L2 * e2 + Lt * dth_2;
-      const double t = -a2 * e2 * e2 - ath * dth_2 * dth_2 + L2 * d2r2 + Lt * d2th_2;
-      d1o[6 + d] = f;
-      d2o[6 + d] = f * f + t;
-    }
-  }
-  return psi;
+  for (int k = 0; k < 18; ++k) d2[k] = d1[k] * d1[k] + t[k];
+  return e;
+}
+
+template <int A>
+__device__ __forceinline__ double trial_dimer(const double (&x)[3 * A], const double* p, double (&d1)[3 * A],
+                                              double (&d2)[3 * A]) {
+  const double e = dimer_trial_log(x, p, d1, d2);
+  const double n1 = sqrt(sqrt(p[0] * p[1] * p[2] * (1.0 / (CUDART_PI * CUDART_PI * CUDART_PI))));
+  return n1 * n1 * sqrt(sqrt(p[6] * (1.0 / CUDART_PI))) * exp(e);
 }
 
 template <int TK, int A>
@@ -355,6 +403,9 @@ __device__ __forceinline__ double trial(const double (&x)[3 * A], const gbdmc_tr
                                         double (&d2)[3 * A]) {
   if constexpr (TK == GBDMC_TRIAL_HO_GAUSS) {
     return trial_ho<A>(x, T.p, d1, d2);
+  } else if constexpr (TK == GBDMC_TRIAL_DIMER_GAUSS) {
+    static_assert(A == 6, "dimer trial has 6 atoms");
+    return trial_dimer<A>(x, T.p, d1, d2);
   } else {
     static_assert(A == 3, "H2O trial has 3 atoms");
     return trial_h2o<A>(x, T.p, d1, d2);

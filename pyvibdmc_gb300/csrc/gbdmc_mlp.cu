@@ -539,7 +539,7 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
 // audit[0..2], fallbacks in audit[3].
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
-                                                    const gbdmc_ctrl_t* ctrls, const int* list,
+                                                    gbdmc_ctrl_t* ctrls, const int* list,
                                                     const unsigned char* flags, double* audit, float beta) {
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
@@ -571,14 +571,15 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
       v += __shfl_xor_sync(0xffffffffu, v, 1);
       if (live && part == 0) {
         const unsigned char fl = flags[dst];
+        const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
         if (fl & 2) {
-          const double d = (out.v[dst] + c_used) - v;  // error of the raw network energy
+          const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
           atomicAdd(audit + 0, 1.0);
           atomicAdd(audit + 1, d);
           atomicAdd(audit + 2, d * d);
         }
         if (fl & 1) atomicAdd(audit + 3, 1.0);
-        out.v[dst] = v;
+        out.v[dst] = v + ke;
       }
     }
   }
@@ -599,6 +600,24 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     audit[5] = audit[0];
     audit[6] = audit[1];
     *reinterpret_cast<unsigned long long*>(audit + 7) = 0ull;
+    if (S.trial.kind != GBDMC_TRIAL_NONE) {
+      // dt_factor = accepted / N (pyvibdmc.py:603) for the weights of this step; effective time (:372-378)
+      for (int r = 0; r < T.nrep; ++r) {
+        gbdmc_ctrl_t* c = ctrls + r;
+        if (*(volatile int*)&c->status) continue;
+        const long long n = c->n, step = c->step;
+        const long long na = *(volatile long long*)&c->n_acc;
+        const double dte = S.dt * ((double)na / (double)n);
+        c->dt_eff = dte;
+        c->eff_ts = (step == 0) ? dte : c->eff_ts + dte;
+        if (step < S.hist.len) {
+          const int64_t h = (int64_t)r * S.hist.len + step;
+          if (S.hist.rejected) S.hist.rejected[h] = (int)(n - na);
+          if (S.hist.eff_ts) S.hist.eff_ts[h] = c->eff_ts;
+        }
+        c->n_acc = 0;
+      }
+    }
   }
 }
 
@@ -638,9 +657,21 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
 #pragma unroll
       for (int k = 0; k < 18; ++k) xd[k] = (double)W.x[k * ld + base + i];
       // step 0 uses the analytic energy for every walker (start structures are not yet sampled)
-      const double v = pes_dimer<false>(xd, S.pes.p, gd);
+      double v = pes_dimer<false>(xd, S.pes.p, gd);
       (void)e_lo;
       (void)e_hi;
+      if (S.trial.kind == GBDMC_TRIAL_DIMER_GAUSS) {  // psi_T, drift and local KE at the start (pyvibdmc.py:760-769)
+        float xs[18], fx[18], d2[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) xs[k] = W.x[k * ld + base + i];
+        const float lp = dimer_trial_log(xs, S.trial.p, fx, d2);
+        const float ke = local_ke_f32(S, d2);
+#pragma unroll
+        for (int k = 0; k < 18; ++k) W.f[k * ld + base + i] = fx[k];
+        W.lnpsi[base + i] = lp;
+        W.ke[base + i] = ke;
+        v += (double)ke;
+      }
       W.v[base + i] = v;
       p.s0 = v;
       p.c = 1;
@@ -655,6 +686,7 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
         ctrl->vref = tt.s0 / (double)n - S.alpha * ((double)(n - T.n0[r]) / n0);
         ctrl->dt_eff = S.dt;  // k_count weights with dt_eff
         ctrl->reserved[2] = 0;
+        ctrl->n_acc = 0;
         ctrl->ticket = 0;
       }
     }
@@ -678,6 +710,12 @@ __global__ void __launch_bounds__(kMaxTPB) k_compact_f32(const __grid_constant__
     for (int k = 0; k < 18; ++k) out.x[k * ld + b + i] = in.x[k * ld + src];
     out.v[b + i] = in.v[src];
     if (in.who && out.who) out.who[b + i] = in.who[src];
+    if (in.f && out.f) {
+#pragma unroll
+      for (int k = 0; k < 18; ++k) out.f[k * ld + b + i] = in.f[k * ld + src];
+      out.lnpsi[b + i] = in.lnpsi[src];
+      out.ke[b + i] = in.ke[src];
+    }
   }
 }
 
@@ -817,72 +855,110 @@ extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t 
 
 // Replica table of the surrogate path: tiles of `tpb` walkers (128 for the
 // MLP kernels: 8 warps x 16 or 128 threads x 1; 256 for counts and branching).
-static int mlp_table(const gbdmc_sim_t* S, RepTable& T, const char* what, int tpb = 128) {
+// Replica table of a surrogate run: the 6-atom dimer, discrete weighting,
+// fp32 deviates, optionally the dimer trial; nrep == 0 means one replica
+// spanning the whole ld.
+static int mlp_table(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep, RepTable& T, const char* what,
+                     int tpb = 128) {
   if (!S || S->natoms != 6 || S->pes.kind != GBDMC_PES_DIMER || S->weighting != GBDMC_DISCRETE ||
-      S->trial.kind != GBDMC_TRIAL_NONE || S->n0 < 1 || S->ld < 1 || S->ld > (int64_t)INT32_MAX) {
-    set_error("%s: the surrogate path runs the 6-atom dimer, discrete weighting, no trial psi", what);
+      (S->trial.kind != GBDMC_TRIAL_NONE && S->trial.kind != GBDMC_TRIAL_DIMER_GAUSS) || S->ld < 1 ||
+      S->ld > (int64_t)INT32_MAX || (nrep == 0 && S->n0 < 1) || nrep < 0 || (nrep > 0 && !reps)) {
+    set_error("%s: the surrogate path runs the 6-atom dimer, discrete weighting, no trial or the dimer trial",
+              what);
     return GBDMC_ERR_ARG;
   }
   if (S->noise_mode == GBDMC_NOISE_PHILOX64) {
     set_error("%s: the surrogate path draws fp32 deviates (PHILOX32 or INJECTED)", what);
     return GBDMC_ERR_ARG;
   }
-  gbdmc_replica_t r{};
-  r.off = 0;
-  r.cap = S->ld;
-  r.n0 = S->n0;
-  r.stream = S->replica_id;
+  gbdmc_replica_t one{};
+  if (nrep == 0) {
+    one.off = 0;
+    one.cap = S->ld;
+    one.n0 = S->n0;
+    one.stream = S->replica_id;
+    reps = &one;
+    nrep = 1;
+  }
   gbdmc_sim_t S2 = *S;
   S2.block_threads = tpb;
-  return build_table(S2, &r, 1, T, what);
+  return build_table(S2, reps, nrep, T, what);
 }
 
-extern "C" int gbdmc_mlp_sim_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
-                                  gbdmc_ctrl_t* ctrl, void* scratch, void* stream) {
+// Tiles of the scratch layout: enough for any tile width >= kMinTPB.
+static int64_t mlp_scratch_tiles(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep) {
+  if (nrep == 0) return (S->ld + kMinTPB - 1) / kMinTPB;
+  int64_t t = 0;
+  for (int r = 0; r < nrep; ++r) t += (reps[r].cap + kMinTPB - 1) / kMinTPB;
+  return t;
+}
+
+extern "C" int gbdmc_mlp_batch_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps,
+                                    int32_t nrep, const gbdmc_walkers_f32_t* w, gbdmc_ctrl_t* ctrl, void* scratch,
+                                    void* stream) {
   RepTable T;
-  int rc = mlp_table(S, T, "gbdmc_mlp_sim_init");
+  int rc = mlp_table(S, reps, nrep, T, "gbdmc_mlp_batch_init");
   if (rc) return rc;
   if (!valid_net(net) || !w || !w->x || !w->v || !ctrl || !scratch) {
-    set_error("gbdmc_mlp_sim_init: invalid arguments");
+    set_error("gbdmc_mlp_batch_init: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (S->trial.kind != GBDMC_TRIAL_NONE && (!w->f || !w->lnpsi || !w->ke)) {
+    set_error("gbdmc_mlp_batch_init: a trial needs f/lnpsi/ke walker arrays");
     return GBDMC_ERR_ARG;
   }
   rc = set_mlp_smem((const void*)k_mlp_init);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
-  int grid = T.tile_off[1];
+  const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
+  int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();
   k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part);
-  return check_launch("gbdmc_mlp_sim_init");
+  return check_launch("gbdmc_mlp_batch_init");
 }
 
-extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,
-                                  const gbdmc_walkers_f32_t* dst, gbdmc_ctrl_t* ctrl, void* scratch, double* audit,
-                                  const gbdmc_noise_t* noise, void* stream) {
+extern "C" int gbdmc_mlp_sim_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* w,
+                                  gbdmc_ctrl_t* ctrl, void* scratch, void* stream) {
+  return gbdmc_mlp_batch_init(S, net, nullptr, 0, w, ctrl, scratch, stream);
+}
+
+extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps,
+                                    int32_t nrep, const gbdmc_walkers_f32_t* src, const gbdmc_walkers_f32_t* dst,
+                                    gbdmc_ctrl_t* ctrl, void* scratch, double* audit, const gbdmc_noise_t* noise,
+                                    void* stream) {
+  const char* what = "gbdmc_mlp_batch_step";
   RepTable T;
-  int rc = mlp_table(S, T, "gbdmc_mlp_sim_step");
+  int rc = mlp_table(S, reps, nrep, T, what);
   if (rc) return rc;
   if (!valid_net(net) || !src || !dst || !src->x || !dst->x || !dst->v || !dst->idx || src->x == dst->x || !ctrl ||
       !scratch || !audit) {
-    set_error("gbdmc_mlp_sim_step: invalid arguments");
+    set_error("%s: invalid arguments", what);
     return GBDMC_ERR_ARG;
   }
   gbdmc_noise_t nz{};
   if (S->noise_mode == GBDMC_NOISE_INJECTED) {
-    if (!noise || !noise->normal || !noise->u_branch || noise->ld_noise < 1) {
-      set_error("gbdmc_mlp_sim_step: injected noise buffers missing");
+    if (!noise || !noise->normal || !noise->u_branch || noise->ld_noise < 1 || T.nrep != 1) {
+      set_error("%s: injected noise needs normal/u_branch buffers and one replica", what);
       return GBDMC_ERR_ARG;
     }
     nz = *noise;
   }
   if (net->engine < 0 || net->engine > 1) {
-    set_error("gbdmc_mlp_sim_step: engine must be 0 (mma.sync) or 1 (tcgen05)");
+    set_error("%s: engine must be 0 (mma.sync) or 1 (tcgen05)", what);
     return GBDMC_ERR_ARG;
+  }
+  if (S->trial.kind != GBDMC_TRIAL_NONE) {
+    if (net->engine != 1 || !src->f || !src->lnpsi || !src->ke || !dst->f || !dst->lnpsi || !dst->ke ||
+        (S->noise_mode == GBDMC_NOISE_INJECTED && !nz.u_accept)) {
+      set_error("%s: importance sampling needs engine 1 (tcgen05), f/lnpsi/ke walker arrays and, with "
+                "injected noise, acceptance uniforms", what);
+      return GBDMC_ERR_ARG;
+    }
   }
   rc = set_mlp_smem((const void*)k_mlp_move_energy);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, (S->ld + kMinTPB - 1) / kMinTPB);
+  const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
   cudaStream_t s = (cudaStream_t)stream;
-  int grid = T.tile_off[1];
+  int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();
   const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
   cudaEvent_t* ev = prof ? g_prof.ev[g_prof.count] : nullptr;
@@ -897,7 +973,7 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   if (prof) cudaEventRecord(ev[1], s);
   k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
-  rc = mlp_table(S, T2, "gbdmc_mlp_sim_step", 256);
+  rc = mlp_table(S, reps, nrep, T2, what, 256);
   if (rc) return rc;
   gbdmc_walkers_t wv{};
   wv.v = dst->v;
@@ -912,18 +988,30 @@ extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
     cudaEventRecord(ev[2], s);
     ++g_prof.count;
   }
-  return check_launch("gbdmc_mlp_sim_step");
+  return check_launch(what);
+}
+
+extern "C" int gbdmc_mlp_sim_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_walkers_f32_t* src,
+                                  const gbdmc_walkers_f32_t* dst, gbdmc_ctrl_t* ctrl, void* scratch, double* audit,
+                                  const gbdmc_noise_t* noise, void* stream) {
+  return gbdmc_mlp_batch_step(S, net, nullptr, 0, src, dst, ctrl, scratch, audit, noise, stream);
+}
+
+extern "C" int gbdmc_mlp_batch_compact(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                       const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
+                                       const gbdmc_ctrl_t* ctrl, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, reps, nrep, T, "gbdmc_mlp_batch_compact");
+  if (rc) return rc;
+  if (!in || !out || !in->x || !out->x || !in->v || !out->v || in->x == out->x || !ctrl) {
+    set_error("gbdmc_mlp_batch_compact: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  k_compact_f32<<<grid_for(T), T.tpb, 0, (cudaStream_t)stream>>>(*S, T, *in, *out, ctrl);
+  return check_launch("gbdmc_mlp_batch_compact");
 }
 
 extern "C" int gbdmc_mlp_compact(const gbdmc_sim_t* S, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
                                  const gbdmc_ctrl_t* ctrl, void* stream) {
-  RepTable T;
-  int rc = mlp_table(S, T, "gbdmc_mlp_compact");
-  if (rc) return rc;
-  if (!in || !out || !in->x || !out->x || !in->v || !out->v || in->x == out->x || !ctrl) {
-    set_error("gbdmc_mlp_compact: invalid arguments");
-    return GBDMC_ERR_ARG;
-  }
-  k_compact_f32<<<grid_for(T), T.tpb, 0, (cudaStream_t)stream>>>(*S, T, *in, *out, ctrl);
-  return check_launch("gbdmc_mlp_compact");
+  return gbdmc_mlp_batch_compact(S, nullptr, 0, in, out, ctrl, stream);
 }

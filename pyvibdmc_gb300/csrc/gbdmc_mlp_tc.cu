@@ -279,6 +279,8 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
     if (i0 >= n) continue;  // block-uniform
     const int64_t i = i0 + threadIdx.x;
     float xs[18], f[16];
+    bool acc = false;
+    float ke = 0.f;
     if (i < n) {
       const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
       const int64_t dst = base + i;
@@ -291,10 +293,30 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
 #pragma unroll
         for (int k = 0; k < 18; k += 2) rng.normal2_f32(z[k], z[k + 1]);
       }
+      if (S.trial.kind == GBDMC_TRIAL_DIMER_GAUSS) {
+        float fx[18];
 #pragma unroll
-      for (int k = 0; k < 18; ++k) {
-        xs[k] = in.x[k * ld + src] + (float)S.sigma[k / 3] * z[k];
-        out.x[k * ld + dst] = xs[k];
+        for (int k = 0; k < 18; ++k) {
+          xs[k] = in.x[k * ld + src];
+          fx[k] = in.f[k * ld + src];
+        }
+        float lp = in.lnpsi[src];
+        ke = in.ke[src];
+        const double u = S.noise_mode == GBDMC_NOISE_INJECTED ? nz.u_accept[dst] : rng.uniform53();
+        acc = is_move_f32(S, xs, fx, lp, ke, z, u);
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+          out.x[k * ld + dst] = xs[k];
+          out.f[k * ld + dst] = fx[k];
+        }
+        out.lnpsi[dst] = lp;
+        out.ke[dst] = ke;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+          xs[k] = in.x[k * ld + src] + (float)S.sigma[k / 3] * z[k];
+          out.x[k * ld + dst] = xs[k];
+        }
       }
       if (out.who && in.who) out.who[dst] = in.who[src];
       const bool oob = walker_features(xs, net, f);
@@ -312,8 +334,13 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
       for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
       walker_features(xs, net, f);
     }
+    if (S.trial.kind != GBDMC_TRIAL_NONE) {  // accepted moves of the replica (dt_eff = dt * accepted / N)
+      const int nacc = __syncthreads_count(acc);
+      if (threadIdx.x == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
+    }
     const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
-    if (i < n) out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4) - corr;
+    if (i < n)
+      out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4) - corr + (double)ke;
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
       break;

@@ -790,6 +790,7 @@ static int dispatch_system(const gbdmc_sim_t& S, const char* what, F&& f) {
   GBDMC_SYS(GBDMC_PES_HO, 1, GBDMC_TRIAL_HO_GAUSS)
   GBDMC_SYS(GBDMC_PES_HO, 3, GBDMC_TRIAL_HO_GAUSS)
   GBDMC_SYS(GBDMC_PES_H2O_LM, 3, GBDMC_TRIAL_H2O_GAUSS)
+  GBDMC_SYS(GBDMC_PES_DIMER, 6, GBDMC_TRIAL_DIMER_GAUSS)
 #undef GBDMC_SYS
   set_error("%s: unsupported system (pes %d, atoms %d, trial %d)", what, PK, A, TK);
   return GBDMC_ERR_ARG;

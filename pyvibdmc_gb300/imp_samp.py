@@ -20,27 +20,33 @@ from . import _capi
 from .constants import Constants
 from .potentials import to_soa, from_soa, default_device, _ptr, _stream
 
-__all__ = ["ImpSampManager_GPU", "TrialFunction", "h2o_gaussian_trial", "ho_gaussian_trial"]
+__all__ = ["ImpSampManager_GPU", "TrialFunction", "h2o_gaussian_trial", "ho_gaussian_trial",
+           "dimer_gaussian_trial"]
 
 
 class ImpSampManager_GPU:
     """Trial wave function evaluated on the GPU.
 
     :param kind: 'h2o_gauss' (product of Gaussians in r1, r2, theta of an
-        O,H,H water) or 'ho_gauss' (separable Cartesian Gaussian)
-    :param alpha: Gaussian exponents (3 for h2o_gauss, one per atom for ho_gauss)
-    :param qe: centres (r1e, r2e, theta_e) for h2o_gauss
+        O,H,H water), 'dimer_gauss' (the h2o_gauss trial of both monomers of an
+        O,H,H,O,H,H dimer times a Gaussian in the O-O distance) or 'ho_gauss'
+        (separable Cartesian Gaussian)
+    :param alpha: Gaussian exponents (3 for h2o_gauss, 4 for dimer_gauss --
+        the monomer's three and alpha_R -- one per atom for ho_gauss)
+    :param qe: centres (r1e, r2e, theta_e) for h2o_gauss, plus R_e for dimer_gauss
     """
 
     def __init__(self, kind, alpha, qe=None, natoms=None, device=None):
-        if kind not in ("h2o_gauss", "ho_gauss"):
+        if kind not in ("h2o_gauss", "dimer_gauss", "ho_gauss"):
             raise ValueError(f"unknown trial kind {kind!r}")
         self.kind = kind
         self.alpha = [float(a) for a in alpha]
         self.qe = None if qe is None else [float(q) for q in qe]
-        self.natoms = 3 if kind == "h2o_gauss" else (natoms or len(self.alpha))
+        self.natoms = {"h2o_gauss": 3, "dimer_gauss": 6}.get(kind) or natoms or len(self.alpha)
         if kind == "h2o_gauss" and (len(self.alpha) != 3 or self.qe is None or len(self.qe) != 3):
             raise ValueError("h2o_gauss needs 3 alphas and 3 centres")
+        if kind == "dimer_gauss" and (len(self.alpha) != 4 or self.qe is None or len(self.qe) != 4):
+            raise ValueError("dimer_gauss needs 4 alphas and 4 centres")
         if kind == "ho_gauss" and len(self.alpha) != self.natoms:
             raise ValueError("ho_gauss needs one alpha per atom")
         self.device = device
@@ -51,6 +57,10 @@ class ImpSampManager_GPU:
         if self.kind == "h2o_gauss":
             t.kind = _capi.TRIAL_H2O_GAUSS
             for i, v in enumerate(self.alpha + self.qe):
+                t.p[i] = v
+        elif self.kind == "dimer_gauss":
+            t.kind = _capi.TRIAL_DIMER_GAUSS
+            for i, v in enumerate(self.alpha[:3] + self.qe[:3] + [self.alpha[3], self.qe[3]]):
                 t.p[i] = v
         else:
             t.kind = _capi.TRIAL_HO_GAUSS
@@ -112,6 +122,18 @@ def h2o_gaussian_trial(omega_r=3800.0, omega_theta=1600.0, re=1.81, theta_e_deg=
     w = Constants.atomic_units["wavenumbers"]
     alpha = [mu * omega_r * w, mu * omega_r * w, omega_theta * w / g]
     return ImpSampManager_GPU("h2o_gauss", alpha, [re, re, th], device=device)
+
+
+def dimer_gaussian_trial(omega_r=3800.0, omega_theta=1600.0, re=1.81, theta_e_deg=104.5, omega_R=180.0,
+                         R_e=5.152, device=None):
+    """The water trial of each monomer (as :func:`h2o_gaussian_trial`) times
+    exp(-1/2 alpha_R (R_OO - R_e)^2) with alpha_R = mu omega_R, mu the reduced
+    mass of the two waters; R_e = 5.152 bohr is the O-O distance at the
+    minimum of the dimer PES."""
+    mono = h2o_gaussian_trial(omega_r, omega_theta, re, theta_e_deg)
+    mw = Constants.mass("O") + 2 * Constants.mass("H")
+    aR = 0.5 * mw * omega_R * Constants.atomic_units["wavenumbers"]
+    return ImpSampManager_GPU("dimer_gauss", mono.alpha + [aR], mono.qe + [R_e], device=device)
 
 
 def ho_gaussian_trial(masses, omega_wavenumbers, device=None):

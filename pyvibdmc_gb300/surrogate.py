@@ -283,40 +283,80 @@ def harvest_training_data(potential, num_walkers, nsteps, every, start, masses, 
 
 
 class NNDMC:
-    """Surrogate DMC of the water dimer (discrete weighting, fp32 coordinates)."""
+    """Surrogate DMC of the water dimer (discrete weighting, fp32 coordinates).
+
+    ``num_walkers`` is one walker count, or a list of them for a batch of
+    independent replicas stepped together (one replica table, one control
+    block per replica; the audit statistics and the bias correction are
+    shared).  With ``imp_samp`` (:func:`dimer_gaussian_trial`) every step is
+    importance sampled on the tensor-core engine: drift-diffusion proposal,
+    trial psi at the proposal and Metropolis test in fp32, local energy
+    V_nn + KE, weights with dt_eff = dt * accepted / N (pyvibdmc.py:549-612).
+    """
 
     def __init__(self, surrogate, potential, num_walkers, start_structures, masses, delta_t, num_timesteps, seed=0,
-                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0, bias_control=0.02):
+                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0, bias_control=0.02, imp_samp=None):
         if not isinstance(potential, Potential_GPU) or potential.kind != "water_dimer":
             raise TypeError("the audit/fallback potential must be the analytic water_dimer Potential_GPU")
         self.model, self.potential = surrogate, potential
         self.device = surrogate.device
-        self.n0 = int(num_walkers)
+        self.ns = [int(num_walkers)] if np.ndim(num_walkers) == 0 else [int(v) for v in num_walkers]
+        self.R = len(self.ns)
+        self.n0 = self.ns[0] if self.R == 1 else list(self.ns)
         self.T = int(num_timesteps)
         self.dt = float(delta_t)
         self.masses = np.asarray(masses, dtype=np.float64)
         self.audit_every = int(audit_every)
         self.graph_steps = max(2, int(graph_steps) // 2 * 2)
         self.rng = rng
+        self.imp_samp = imp_samp
+        if imp_samp is not None and (surrogate.engine != 1 or getattr(imp_samp, "kind", None) != "dimer_gauss"):
+            raise ValueError("importance sampling on the surrogate needs the tcgen05 engine and the dimer trial")
+        if self.R > 1 and not isinstance(rng, str):
+            raise ValueError("replica batches draw Philox deviates")
         ss = np.asarray(start_structures, dtype=np.float64)
-        x0 = np.repeat(ss, self.n0, axis=0) if ss.shape[0] == 1 else ss
-        cap = ((int(np.floor(self.n0 + self.n0 * 0.5)) + 1) + 127) // 128 * 128
+        self.caps = [((int(np.floor(n + n * 0.5)) + 1) + 127) // 128 * 128 for n in self.ns]
+        self.offs = list(np.cumsum([0] + self.caps[:-1]))
+        cap = int(sum(self.caps))
         self.ld = cap
         dev = self.device
-        self._bufs = [dict(x=torch.zeros(18, cap, dtype=torch.float32, device=dev),
-                           v=torch.zeros(cap, dtype=torch.float64, device=dev),
-                           who=torch.zeros(cap, dtype=torch.int32, device=dev),
-                           idx=torch.zeros(cap, dtype=torch.int32, device=dev)) for _ in range(2)]
-        self._bufs[0]["x"][:, :len(x0)] = to_soa(x0, dev, dtype=torch.float32)
+        IS = imp_samp is not None
+
+        def bufset():
+            b = dict(x=torch.zeros(18, cap, dtype=torch.float32, device=dev),
+                     v=torch.zeros(cap, dtype=torch.float64, device=dev),
+                     who=torch.zeros(cap, dtype=torch.int32, device=dev),
+                     idx=torch.zeros(cap, dtype=torch.int32, device=dev))
+            if IS:
+                b.update(f=torch.zeros(18, cap, dtype=torch.float32, device=dev),
+                         lnpsi=torch.zeros(cap, dtype=torch.float32, device=dev),
+                         ke=torch.zeros(cap, dtype=torch.float32, device=dev))
+            return b
+
+        self._bufs = [bufset(), bufset()]
+        for r, (n, off) in enumerate(zip(self.ns, self.offs)):
+            x0 = np.repeat(ss, n, axis=0) if ss.shape[0] == 1 else ss
+            if len(x0) != n:
+                raise ValueError("start_structures: one geometry, or one per walker of a single replica")
+            self._bufs[0]["x"][:, off:off + n] = to_soa(x0, dev, dtype=torch.float32)
         self._cur, self._lazy = 0, False
         L = _capi.load()
-        self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
-        self._scratch = torch.zeros(L.gbdmc_scratch_bytes(cap), dtype=torch.uint8, device=dev)
+        self._reps = None
+        if self.R > 1:
+            self._reps = (_capi.Replica * self.R)()
+            for r in range(self.R):
+                self._reps[r].off, self._reps[r].cap = int(self.offs[r]), self.caps[r]
+                self._reps[r].n0, self._reps[r].stream = self.ns[r], int(replica_id) + r
+            nbytes = L.gbdmc_batch_scratch_bytes(self._reps, self.R)
+        else:
+            nbytes = L.gbdmc_scratch_bytes(cap)
+        self._ctrl = torch.zeros(self.R * C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
+        self._scratch = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
         self._audit = torch.zeros(8, dtype=torch.float64, device=dev)
-        self._hist = dict(vref=torch.zeros(self.T, dtype=torch.float64, device=dev),
-                          pop=torch.zeros(self.T, dtype=torch.float64, device=dev))
+        self._hist = dict(vref=torch.zeros(self.R, self.T, dtype=torch.float64, device=dev),
+                          pop=torch.zeros(self.R, self.T, dtype=torch.float64, device=dev))
         s = _capi.Sim()
-        s.natoms, s.weighting, s.track_who, s.ld, s.n0 = 6, _capi.DISCRETE, 1, cap, self.n0
+        s.natoms, s.weighting, s.track_who, s.ld, s.n0 = 6, _capi.DISCRETE, 1, cap, self.ns[0]
         s.noise_mode = _capi.NOISE_PHILOX32 if isinstance(rng, str) else _capi.NOISE_INJECTED
         s.dt, s.alpha = self.dt, 1.0 / (2.0 * self.dt)
         for a in range(6):
@@ -325,11 +365,13 @@ class NNDMC:
         s.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
         s.replica_id = int(replica_id)
         s.pes = potential.pes_struct()
-        s.trial.kind, s.trial.natoms = _capi.TRIAL_NONE, 6
+        if IS:
+            s.trial = imp_samp.trial_struct()
+        else:
+            s.trial.kind, s.trial.natoms = _capi.TRIAL_NONE, 6
         s.hist.vref, s.hist.pop, s.hist.len = self._hist["vref"].data_ptr(), self._hist["pop"].data_ptr(), self.T
         self._sim = s
         self._net = surrogate.net_struct(audit_every, bias_beta=bias_control)
-        self._n_start = len(x0)
         self._graphs = {}
         self.step = 0
 
@@ -338,28 +380,45 @@ class NNDMC:
         w.x, w.v, w.who = b["x"].data_ptr(), b["v"].data_ptr(), b["who"].data_ptr()
         if with_idx:
             w.idx = b["idx"].data_ptr()
+        if "f" in b:
+            w.f, w.lnpsi, w.ke = b["f"].data_ptr(), b["lnpsi"].data_ptr(), b["ke"].data_ptr()
         return w
 
-    def ctrl(self):
-        return _capi.Ctrl.from_buffer_copy(self._ctrl.cpu().numpy().tobytes())
+    def _rep_args(self):
+        return (C.cast(self._reps, C.c_void_p), self.R) if self._reps is not None else (None, 0)
+
+    def ctrls(self):
+        raw = self._ctrl.cpu().numpy().tobytes()
+        n = C.sizeof(_capi.Ctrl)
+        return [_capi.Ctrl.from_buffer_copy(raw[r * n:(r + 1) * n]) for r in range(self.R)]
+
+    def ctrl(self, r=0):
+        return self.ctrls()[r]
 
     def init(self):
-        c = _capi.Ctrl()
-        c.n = self._n_start
-        self._ctrl.copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
+        n = C.sizeof(_capi.Ctrl)
+        raw = bytearray(self.R * n)
+        for r in range(self.R):
+            c = _capi.Ctrl()
+            c.n = self.ns[r]
+            raw[r * n:(r + 1) * n] = bytes(c)
+        self._ctrl.copy_(torch.frombuffer(raw, dtype=torch.uint8))
         L = _capi.load()
-        _capi.check(L.gbdmc_mlp_sim_init(C.byref(self._sim), C.byref(self._net),
-                                         C.byref(self._w(self._bufs[self._cur], False)), _p(self._ctrl),
-                                         _p(self._scratch), _s()), "gbdmc_mlp_sim_init")
+        reps, nrep = self._rep_args()
+        _capi.check(L.gbdmc_mlp_batch_init(C.byref(self._sim), C.byref(self._net), reps, nrep,
+                                           C.byref(self._w(self._bufs[self._cur], False)), _p(self._ctrl),
+                                           _p(self._scratch), _s()), "gbdmc_mlp_batch_init")
         return self
 
     def _launch(self, cur, lazy, noise=None):
         L = _capi.load()
-        _capi.check(L.gbdmc_mlp_sim_step(C.byref(self._sim), C.byref(self._net),
-                                         C.byref(self._w(self._bufs[cur], lazy)),
-                                         C.byref(self._w(self._bufs[1 - cur], True)), _p(self._ctrl),
-                                         _p(self._scratch), _p(self._audit),
-                                         C.byref(noise) if noise is not None else None, _s()), "gbdmc_mlp_sim_step")
+        reps, nrep = self._rep_args()
+        _capi.check(L.gbdmc_mlp_batch_step(C.byref(self._sim), C.byref(self._net), reps, nrep,
+                                           C.byref(self._w(self._bufs[cur], lazy)),
+                                           C.byref(self._w(self._bufs[1 - cur], True)), _p(self._ctrl),
+                                           _p(self._scratch), _p(self._audit),
+                                           C.byref(noise) if noise is not None else None, _s()),
+                    "gbdmc_mlp_batch_step")
         return 1 - cur, True
 
     def _graph(self, cur):
@@ -376,19 +435,22 @@ class NNDMC:
             self._graphs[cur] = g
         return g
 
-    def run(self, nsteps):
+    def run(self, nsteps, check=True):
         if not isinstance(self.rng, str):
             for _ in range(nsteps):
                 n = int(self.ctrl().n)
                 z = np.asarray(self.rng.standard_normal((n, 3, 6)), dtype=np.float64)
                 zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(18, n)), device=self.device)
+                ua = torch.as_tensor(self.rng.uniform(n), device=self.device) if self.imp_samp is not None else None
                 ub = torch.as_tensor(self.rng.uniform(n), device=self.device)
                 nz = _capi.Noise()
                 nz.normal, nz.u_branch, nz.ld_noise = zs.data_ptr(), ub.data_ptr(), n
+                if ua is not None:
+                    nz.u_accept = ua.data_ptr()
                 self._cur, self._lazy = self._launch(self._cur, self._lazy, nz)
                 torch.cuda.synchronize()
             self.step += nsteps
-            return self._check()
+            return self._check() if check else self
         done = 0
         if nsteps and not self._lazy:
             self._cur, self._lazy = self._launch(self._cur, self._lazy)
@@ -400,25 +462,39 @@ class NNDMC:
             self._cur, self._lazy = self._launch(self._cur, True)
             done += 1
         self.step += nsteps
-        return self._check()
+        return self._check() if check else self
 
     def _check(self):
-        c = self.ctrl()
-        if c.status:
-            raise ValueError(f"Massive walker birth or death event!!!!!!! Dying... (status {c.status})")
+        for r, c in enumerate(self.ctrls()):
+            if c.status:
+                where = f"replica {r}: " if self.R > 1 else ""
+                raise ValueError(f"{where}Massive walker birth or death event!!!!!!! Dying... (status {c.status})")
         return self
 
     def vref_history(self):
-        return self._hist["vref"][:self.step].cpu().numpy()
+        """vref per step (hartree): (T,) for one replica, (R, T) for a batch."""
+        h = self._hist["vref"][:, :self.step].cpu().numpy()
+        return h[0] if self.R == 1 else h
 
     def pop_history(self):
-        return self._hist["pop"][:self.step].cpu().numpy()
+        h = self._hist["pop"][:, :self.step].cpu().numpy()
+        return h[0] if self.R == 1 else h
 
     def zpe(self, start=None, nblocks=20):
+        """ZPE (cm^-1) and its blocking error; for a batch, of the N0-weighted mean of
+        the replicas' vref at each step."""
         from .batch import blocking_error
-        v = Constants.convert(self.vref_history(), "wavenumbers", to_AU=False)
-        start = len(v) // 4 if start is None else start
-        return blocking_error(v[start:], nblocks)
+        v = Constants.convert(self._hist["vref"][:, :self.step].cpu().numpy(), "wavenumbers", to_AU=False)
+        w = np.asarray(self.ns, dtype=float)
+        ens = (w[:, None] * v).sum(0) / w.sum()
+        start = len(ens) // 4 if start is None else start
+        return blocking_error(ens[start:], nblocks)
+
+    def walker_steps(self, t0, t1):
+        """Walkers moved in steps [t0, t1), summed over replicas."""
+        p = self._hist["pop"].cpu().numpy()
+        prev = np.concatenate([np.asarray(self.ns, dtype=float)[:, None], p[:, :-1]], axis=1)
+        return float(prev[:, t0:t1].sum())
 
     def audit(self):
         """(audited walkers, mean and RMS of V_nn - V_analytic in cm^-1, fallbacks)."""
@@ -428,15 +504,18 @@ class NNDMC:
         return dict(audited=int(a[0]), mean_cm=a[1] / n / w, rms_cm=math.sqrt(a[2] / n) / w, fallbacks=int(a[3]),
                     bias_correction_cm=a[4] / w)
 
-    def walkers(self):
+    def walkers(self, r=0):
         if self._lazy:
             L = _capi.load()
-            _capi.check(L.gbdmc_mlp_compact(C.byref(self._sim), C.byref(self._w(self._bufs[self._cur], True)),
-                                            C.byref(self._w(self._bufs[1 - self._cur], False)), _p(self._ctrl),
-                                            _s()), "gbdmc_mlp_compact")
+            reps, nrep = self._rep_args()
+            _capi.check(L.gbdmc_mlp_batch_compact(C.byref(self._sim), reps, nrep,
+                                                  C.byref(self._w(self._bufs[self._cur], True)),
+                                                  C.byref(self._w(self._bufs[1 - self._cur], False)),
+                                                  _p(self._ctrl), _s()), "gbdmc_mlp_batch_compact")
             self._cur, self._lazy = 1 - self._cur, False
-        n = int(self.ctrl().n)
-        return from_soa(self._bufs[self._cur]["x"], n, 6)
+        n = int(self.ctrl(r).n)
+        off = int(self.offs[r])
+        return from_soa(self._bufs[self._cur]["x"][:, off:off + n], n, 6)
 
 
 def _main(argv=None):

@@ -173,3 +173,79 @@ def test_tcgen05_forward_matches_mma_sync_forward():
     e1 = m.energy(xx, engine=1)
     rel = np.abs(e1 - e0) / m.e_scale
     assert np.median(rel) < 2e-4 and rel.max() < 5e-3, (np.median(rel), rel.max())
+
+
+@pytest.fixture(scope="module")
+def dimer_model():
+    """A surrogate fitted well enough for ZPE comparisons (about 1M harvested samples)."""
+    p, masses = oracle.dimer_config()
+    pot = pg.water_dimer()
+    x, v, g, _ = harvest_training_data(pot, 100000, 210, 20, pg.WATER_DIMER_EQ[None], masses, seed=3, equil=20)
+    m = MLPSurrogate(seed=0).fit(x, v, g, epochs=15, batch=8192, lr=2e-3)
+    return m, pot, masses
+
+
+def test_surrogate_is_start_state_matches_fp64_trial(dimer_model):
+    """The fp32 trial of the surrogate IS path (ln psi, drift, local KE written at step 0)
+    against the FP64 oracle trial at the same (fp32-rounded) coordinates."""
+    m, pot, masses = dimer_model
+    t = pg.dimer_gaussian_trial()
+    x0 = (oracle.dimer_equilibrium()[None] + 0.05 * oracle.InjectedNoise(4).standard_normal((3000, 6, 3)))
+    x0 = x0.astype(np.float32).astype(np.float64)
+    nd = NNDMC(m, pot, 3000, x0, masses, 10.0, 4, seed=1, imp_samp=t).init()
+    torch.cuda.synchronize()
+    b = nd._bufs[nd._cur]
+    tr = oracle.TrialDimerGauss(t.alpha, t.qe)
+    d1, d2 = tr.derivs(x0)
+    lnorm = 2 * 0.25 * np.log(np.prod(t.alpha[:3]) / np.pi ** 3) + 0.25 * np.log(t.alpha[3] / np.pi)
+    lp = np.log(tr.psi(x0)) - lnorm
+    ke = -0.5 * (d2 / np.asarray(masses)[None, :, None]).sum((1, 2))
+    got_f = b["f"][:, :3000].cpu().numpy().T.reshape(3000, 6, 3)
+    np.testing.assert_allclose(b["lnpsi"][:3000].cpu().numpy(), lp, rtol=1e-4, atol=1e-4)
+    np.testing.assert_allclose(got_f, d1, rtol=1e-3, atol=2e-3)
+    np.testing.assert_allclose(b["ke"][:3000].cpu().numpy(), ke, rtol=1e-3, atol=1e-5)
+    v = b["v"][:3000].cpu().numpy()
+    np.testing.assert_allclose(v - b["ke"][:3000].cpu().numpy(), oracle.pes_dimer(x0, oracle.dimer_config()[0]),
+                               rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("imp", [False, True])
+def test_surrogate_replica_batch_equals_single_runs(dimer_model, imp):
+    """Replica r of a batch reproduces a single run with replica_id = r bit for bit
+    (bias control off, so no statistic is shared between replicas)."""
+    m, pot, masses = dimer_model
+    t = pg.dimer_gaussian_trial() if imp else None
+    ns = [700, 3000, 1500]
+    b = NNDMC(m, pot, ns, pg.WATER_DIMER_EQ[None], masses, 10.0, 40, seed=9, bias_control=0.0, imp_samp=t)
+    b.init().run(40)
+    for r, n in enumerate(ns):
+        s = NNDMC(m, pot, n, pg.WATER_DIMER_EQ[None], masses, 10.0, 40, seed=9, bias_control=0.0, imp_samp=t,
+                  replica_id=r)
+        s.init().run(40)
+        np.testing.assert_array_equal(b.pop_history()[r], s.pop_history())
+        np.testing.assert_array_equal(b.vref_history()[r], s.vref_history())
+        assert np.array_equal(b.walkers(r), s.walkers())
+
+
+def test_surrogate_is_zpe_agrees_with_fp64_is(dimer_model):
+    """Importance-sampled surrogate DMC against importance-sampled FP64 analytic DMC of
+    the dimer (same trial, dt, walkers)."""
+    m, pot, masses = dimer_model
+    t = pg.dimer_gaussian_trial()
+    nd = NNDMC(m, pot, 50000, pg.WATER_DIMER_EQ[None], masses, 10.0, 3000, seed=3, imp_samp=t).init()
+    nd.run(3000)
+    z_nn = nd.zpe(start=750)
+    acc = 1.0  # the acceptance is checked through the FP64 run's rejected counts below
+    fp = pg.DMC_Sim(num_walkers=50000, num_timesteps=3000, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                    masses=masses, delta_t=10.0, potential=pot, imp_samp=t, start_structures=pg.WATER_DIMER_EQ[None],
+                    seed=3, write_files=False)
+    fp._init_device()
+    fp._run_steps(3000)
+    torch.cuda.synchronize()
+    vv = pg.Constants.convert(fp._hist["vref"].cpu().numpy()[750:3000], "wavenumbers", to_AU=False)
+    z_fp = pg.blocking_error(vv, 20)
+    rej = fp._hist["rejected"].cpu().numpy()[:3000].sum() / (50000.0 * 3000)
+    assert rej < 0.2 and acc > 0
+    d = z_nn[0] - z_fp[0]
+    err = float(np.hypot(z_nn[1], z_fp[1]))
+    assert abs(d) < 3.0 + 4.0 * err, (z_nn, z_fp, nd.audit())

@@ -107,6 +107,18 @@ def test_trial_adjoint_matches_chain_rule_helper_golden():
     np.testing.assert_allclose(xg.grad.cpu().numpy(), d1 * g["psi"][:, None, None], rtol=1e-10, atol=1e-14)
 
 
+def test_dimer_trial_matches_oracle():
+    """gbdmc_trial_eval with the dimer trial (FP64) against the oracle's restatement."""
+    t = pg.dimer_gaussian_trial()
+    tr = oracle.TrialDimerGauss(t.alpha, t.qe)
+    x = oracle.dimer_equilibrium()[None] + 0.08 * oracle.InjectedNoise(6).standard_normal((1025, 6, 3))
+    np.testing.assert_allclose(t.call_trial(x), tr.psi(x), rtol=1e-12)
+    d1, d2 = t.call_derivs(x)
+    o1, o2 = tr.derivs(x)
+    np.testing.assert_allclose(d1, o1, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(d2, o2, rtol=0, atol=1e-8)
+
+
 # ----------------------------------------------------------------- engine
 def _sim(x0, masses, atoms, pot, seed, nsteps, **kw):
     return pg.DMC_Sim(sim_name="t", output_folder="/tmp/gbdmc_test", num_walkers=len(x0), num_timesteps=nsteps,
@@ -165,6 +177,22 @@ def test_engine_importance_sampling_vs_reference():
     np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-10)
     np.testing.assert_allclose(sim._eff_ts, g["eff_ts"], rtol=0, atol=1e-10)
     np.testing.assert_allclose(sim.walkers, g["x_final"], rtol=0, atol=1e-10)
+
+
+def test_engine_dimer_importance_sampling_vs_oracle():
+    """Importance-sampled dimer DMC (dimer trial) against the oracle step loop on the same
+    injected deviates; tolerances as for the water IS case."""
+    p, m = oracle.dimer_config()
+    t = pg.dimer_gaussian_trial()
+    x0 = oracle.dimer_equilibrium()[None] + 0.03 * oracle.InjectedNoise(17).standard_normal((600, 6, 3))
+    nsteps = 12
+    ref = oracle.OracleDMC(x0, m, 10.0, lambda c: oracle.pes_dimer(c, p), oracle.InjectedNoise(23),
+                           trial=oracle.TrialDimerGauss(t.alpha, t.qe)).run(nsteps)
+    sim = _sim(x0, m, ["O", "H", "H", "O", "H", "H"], pg.water_dimer(), 23, nsteps, imp_samp=t)
+    sim.run()
+    np.testing.assert_array_equal(sim._pop_vs_tau, np.array(ref.pop_hist))
+    np.testing.assert_allclose(sim._vref_vs_tau, np.array(ref.vref_hist), rtol=0, atol=1e-10)
+    np.testing.assert_allclose(sim.walkers, ref.x, rtol=0, atol=1e-10)
 
 
 def test_population_guard_raises_value_error():

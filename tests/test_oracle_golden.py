@@ -149,3 +149,22 @@ def test_philox_normals_are_standard_normal():
         assert abs(z.mean()) < 3e-3 and abs(z.std() - 1.0) < 3e-3
         u = philox_branch_uniform(99, 3, np.arange(200000), 9, mode)
         assert u.min() >= 0.0 and u.max() < 1.0 and abs(u.mean() - 0.5) < 3e-3
+
+
+def test_dimer_trial_derivatives_match_finite_differences():
+    """The dimer trial's analytic d psi/psi and d2 psi/psi against central differences."""
+    from pyvibdmc_gb300.imp_samp import dimer_gaussian_trial
+    t = dimer_gaussian_trial()
+    tr = oracle.TrialDimerGauss(t.alpha, t.qe)
+    x = oracle.dimer_equilibrium()[None] + 0.05 * oracle.InjectedNoise(5).standard_normal((40, 6, 3))
+    f, d2 = tr.derivs(x)
+    h = 1e-4
+    psi0 = tr.psi(x)
+    for a in range(6):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[:, a, d] += h
+            xm[:, a, d] -= h
+            pp, pm = tr.psi(xp), tr.psi(xm)
+            np.testing.assert_allclose(f[:, a, d], (pp - pm) / (2 * h) / psi0, rtol=1e-6, atol=1e-6)
+            np.testing.assert_allclose(d2[:, a, d], (pp - 2 * psi0 + pm) / (h * h) / psi0, rtol=1e-4, atol=1e-3)
