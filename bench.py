@@ -500,7 +500,60 @@ def run_extras(steps):
                                    "fp64_analytic_us_per_step": fsecs / steps * 1e6,
                                    "harvest_s": t_h, "train_s": t_t, "train_samples": int(x.shape[1]),
                                    "train_rmse_cm": m.history[-1]["rmse_e_cm"], "audit": nd.audit()}
+    del nd, fp
+    out["is_nn_batched_dimer"] = run_combined_dimer(m, pot, dm)
     return out
+
+
+def run_combined_dimer(m, pot, dm, T=3000):
+    """The engine with all three accelerations on one system, the water dimer:
+    importance sampling (dimer trial), the tcgen05 surrogate PES and 64
+    batched replicas (N_r ~ U[1000, 65536]), against the plain FP64 dimer
+    path (200000 walkers, one replica) at equal ZPE error bar (efficiency =
+    1 / (error^2 x seconds)), and its ZPE against the FP64 importance-sampled
+    dimer (same trial, dt)."""
+    import torch
+    import pyvibdmc_gb300 as pg
+    trial = pg.dimer_gaussian_trial()
+    res = {}
+
+    def fp64(tag, imp):
+        sm = pg.DMC_Sim(num_walkers=200000, num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                        masses=dm, delta_t=DT, potential=pot, imp_samp=imp, start_structures=pg.WATER_DIMER_EQ[None],
+                        seed=13, write_files=False, graph_steps=32)
+        sm._init_device()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sm._run_steps(T)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        vr = pg.Constants.convert(sm._hist["vref"].cpu().numpy()[T // 4:T], "wavenumbers", to_AU=False)
+        z, e = pg.blocking_error(vr, 30)
+        pop = sm._hist["pop"].cpu().numpy()[:T]
+        ws = float(200000 + pop[:-1].sum())
+        res[tag] = {"walkers": 200000, "steps": T, "seconds": secs, "walker_steps_per_s": ws / secs, "zpe_cm": z,
+                    "err_cm": e, "efficiency": 1.0 / (e * e * secs)}
+
+    fp64("plain_fp64_200k", None)
+    fp64("is_fp64_200k", trial)
+    ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
+    nd = pg.NNDMC(m, pot, ns, pg.WATER_DIMER_EQ[None], dm, DT, T + 16, seed=13, audit_every=100, imp_samp=trial,
+                  graph_steps=16).init()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nd.run(T)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    z, e = nd.zpe(start=T // 4)
+    res["is_nn_64_replicas"] = {"replicas": len(ns), "walkers": int(sum(ns)), "steps": T, "seconds": secs,
+                                "walker_steps_per_s": nd.walker_steps(0, T) / secs, "zpe_cm": z, "err_cm": e,
+                                "efficiency": 1.0 / (e * e * secs), "audit": nd.audit()}
+    base = res["plain_fp64_200k"]["efficiency"]
+    res["is_gain_fp64_at_equal_error"] = res["is_fp64_200k"]["efficiency"] / base
+    res["gain_vs_plain_fp64_at_equal_error"] = res["is_nn_64_replicas"]["efficiency"] / base
+    d = z - res["is_fp64_200k"]["zpe_cm"]
+    res["zpe_minus_fp64_is_cm"] = [d, float(np.hypot(e, res["is_fp64_200k"]["err_cm"]))]
+    return res
 
 
 def run_e2e(sim, L, dev, steps):
