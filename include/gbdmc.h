@@ -62,7 +62,10 @@ enum {
 enum {
   GBDMC_PES_HO = 1,     /* p[0]=k : V = 1/2 k |x|^2                              */
   GBDMC_PES_H2O_LM = 2, /* O,H,H; p = De, a, re, ktheta, theta_e, krr            */
-  GBDMC_PES_DIMER = 3   /* O,H,H,O,H,H; p = De,a,re,ktheta,theta_e,krr,eps,sigma,qH,qO */
+  GBDMC_PES_DIMER = 3,  /* O,H,H,O,H,H; p = De,a,re,ktheta,theta_e,krr,eps,sigma,qH,qO */
+  GBDMC_PES_H2O_PS = 4  /* Partridge-Schwenke water (J. Chem. Phys. 106, 4618 (1997)), the reference's
+                           sample Fortran PES (h2opes_v2.f).  p[0] = 0: atoms O,H,H; p[0] = 1: H,H,O (the
+                           order of the reference's calc_hoh_pot, calc_h2o_pot.f:1-30)            */
 };
 
 typedef struct {

@@ -8,6 +8,7 @@ the C ABI of ``include/gbdmc.h``.
 """
 from .constants import Constants, get_atomic_num, get_atomic_string
 from .potentials import (Potential_GPU, PESFunction, harmonic_oscillator, h2o_local_mode, water_dimer,
+                         partridge_schwenke,
                          WATER_DIMER_EQ, to_soa, from_soa)
 from .imp_samp import ImpSampManager_GPU, TrialFunction, h2o_gaussian_trial, ho_gaussian_trial, \
     dimer_gaussian_trial
@@ -17,7 +18,7 @@ from .surrogate import MLPSurrogate, NN_Potential_GPU, NNDMC, harvest_training_d
 from . import _capi
 
 __all__ = ["HostWalkers", "Constants", "get_atomic_num", "get_atomic_string", "Potential_GPU", "PESFunction",
-           "harmonic_oscillator", "h2o_local_mode", "water_dimer", "ImpSampManager_GPU", "TrialFunction",
+           "harmonic_oscillator", "h2o_local_mode", "water_dimer", "partridge_schwenke", "ImpSampManager_GPU", "TrialFunction",
            "h2o_gaussian_trial", "ho_gaussian_trial", "dimer_gaussian_trial", "DMC_Sim", "dmc_restart", "DMC_Batch", "blocking_error",
            "MLPSurrogate", "NN_Potential_GPU", "NNDMC", "harvest_training_data", "WATER_DIMER_EQ",
            "to_soa", "from_soa"]

@@ -13,7 +13,7 @@ MAX_ATOMS = 8
 
 OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY = 0, 1, 2, 3
 ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW, ST_TIMEOUT = 1, 2, 4, 8, 16, 32
-PES_HO, PES_H2O_LM, PES_DIMER = 1, 2, 3
+PES_HO, PES_H2O_LM, PES_DIMER, PES_H2O_PS = 1, 2, 3, 4
 TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS, TRIAL_DIMER_GAUSS = 0, 1, 2, 3
 NOISE_PHILOX32, NOISE_PHILOX64, NOISE_INJECTED = 0, 1, 2
 DISCRETE, CONTINUOUS = 0, 1

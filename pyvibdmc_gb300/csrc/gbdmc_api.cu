@@ -110,6 +110,13 @@ extern "C" int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x, int64_t n
       }
       launch_pes<GBDMC_PES_H2O_LM, 3>(*pes, x, n, ld, v, grad, s);
       break;
+    case GBDMC_PES_H2O_PS:
+      if (pes->natoms != 3) {
+        set_error("gbdmc_pes_eval: the Partridge-Schwenke PES has 3 atoms");
+        return GBDMC_ERR_ARG;
+      }
+      launch_pes<GBDMC_PES_H2O_PS, 3>(*pes, x, n, ld, v, grad, s);
+      break;
     case GBDMC_PES_DIMER:
       if (A != 6) {
         set_error("gbdmc_pes_eval: dimer PES needs 6 atoms (got %d)", A);

@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <math_constants.h>
 #include "gbdmc.h"
+#include "gbdmc_ps_pes.cuh"
 
 namespace gbdmc {
 
@@ -244,6 +245,60 @@ __device__ __forceinline__ double pes_dimer(const double (&x)[18], const double*
   return v;
 }
 
+// Partridge-Schwenke water (vibpot, h2opes_v2.f:393-492, with the internal
+// coordinates of calc_hoh_pot, calc_h2o_pot.f:13-27).  V = P(x1, x2, x3)
+// exp(-b1 (dr1^2 + dr2^2)) + c1 + V_OH(r1) + V_OH(r2) + V_HH(r_HH) with
+// x_k = (r_k - re)/re, x3 = cos(theta) - cos(theta_e); cos(theta) is taken
+// from the bond vectors directly (the reference evaluates acos, then cos),
+// and r_HH is the H-H distance (the reference's law of cosines).  The
+// polynomial P and its partial derivatives are generated code
+// (gbdmc_ps_pes.cuh).  With G: adds dV/dx to g.
+template <bool G, int A>
+__device__ __forceinline__ double h2o_ps(const double (&x)[3 * A], int o, int h1, int h2, double (&g)[3 * A]) {
+  using namespace ps;
+  double v1[3], v2[3], u[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v1[d] = x[3 * h1 + d] - x[3 * o + d];
+    v2[d] = x[3 * h2 + d] - x[3 * o + d];
+    u[d] = x[3 * h1 + d] - x[3 * h2 + d];
+  }
+  const double r1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const double r2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const double rhh = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const double ir12 = 1.0 / (r1 * r2);
+  const double c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) * ir12;
+  const double dr1 = r1 - k_reoh, dr2 = r2 - k_reoh;
+  const double x1 = dr1 / k_reoh, x2 = dr2 / k_reoh, x3 = c - k_ce;
+  const double vhh = k_phh1 * exp(-k_phh2 * rhh);
+  const double ex1 = exp(-k_alphaoh * (r1 - k_roh)), ex2 = exp(-k_alphaoh * (r2 - k_roh));
+  const double voh1 = k_deoh * ex1 * (ex1 - 2.0), voh2 = k_deoh * ex2 * (ex2 - 2.0);
+  const double E = exp(-k_b1 * (dr1 * dr1 + dr2 * dr2));
+  const double P = poly(x1, x2, x3);
+  const double v = P * E + kC1 + voh1 + voh2 + vhh;
+  if constexpr (G) {
+    const double ire = 1.0 / k_reoh;
+    const double vr1 = (dpoly1(x1, x2, x3) * ire - 2.0 * k_b1 * dr1 * P) * E +
+                       k_deoh * (-k_alphaoh * ex1) * (2.0 * ex1 - 2.0);
+    const double vr2 = (dpoly2(x1, x2, x3) * ire - 2.0 * k_b1 * dr2 * P) * E +
+                       k_deoh * (-k_alphaoh * ex2) * (2.0 * ex2 - 2.0);
+    const double vc = dpoly3(x1, x2, x3) * E;
+    const double vrh = -k_phh2 * vhh / rhh;  // (dV/dr_HH) / r_HH
+    const double ir1 = 1.0 / r1, ir2 = 1.0 / r2;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double e1 = v1[d] * ir1, e2 = v2[d] * ir2;
+      const double dc1 = (e2 - c * e1) * ir1, dc2 = (e1 - c * e2) * ir2;  // dcos/dx_h1, dcos/dx_h2
+      const double gh1 = vr1 * e1 + vc * dc1 + vrh * u[d];
+      const double gh2 = vr2 * e2 + vc * dc2 - vrh * u[d];
+      g[3 * h1 + d] += gh1;
+      g[3 * h2 + d] += gh2;
+      g[3 * o + d] -= vr1 * e1 + vr2 * e2 + vc * (dc1 + dc2);
+    }
+  }
+  return v;
+}
+
 template <int PK, int A, bool G>
 __device__ __forceinline__ double pes(const double (&x)[3 * A], const gbdmc_pes_t& P, double (&g)[3 * A]) {
   if constexpr (PK == GBDMC_PES_HO) {
@@ -251,6 +306,9 @@ __device__ __forceinline__ double pes(const double (&x)[3 * A], const gbdmc_pes_
   } else if constexpr (PK == GBDMC_PES_H2O_LM) {
     static_assert(A == 3, "H2O local-mode PES has 3 atoms");
     return h2o_lm<G, 3>(x, P.p, 0, 1, 2, g);
+  } else if constexpr (PK == GBDMC_PES_H2O_PS) {
+    static_assert(A == 3, "Partridge-Schwenke PES has 3 atoms");
+    return P.p[0] != 0.0 ? h2o_ps<G, 3>(x, 2, 0, 1, g) : h2o_ps<G, 3>(x, 0, 1, 2, g);
   } else {
     static_assert(A == 6, "dimer PES has 6 atoms");
     return pes_dimer<G>(x, P.p, g);

@@ -787,6 +787,8 @@ static int dispatch_system(const gbdmc_sim_t& S, const char* what, F&& f) {
   GBDMC_SYS(GBDMC_PES_HO, 3, GBDMC_TRIAL_NONE)
   GBDMC_SYS(GBDMC_PES_H2O_LM, 3, GBDMC_TRIAL_NONE)
   GBDMC_SYS(GBDMC_PES_DIMER, 6, GBDMC_TRIAL_NONE)
+  GBDMC_SYS(GBDMC_PES_H2O_PS, 3, GBDMC_TRIAL_NONE)
+  GBDMC_SYS(GBDMC_PES_H2O_PS, 3, GBDMC_TRIAL_H2O_GAUSS)
   GBDMC_SYS(GBDMC_PES_HO, 1, GBDMC_TRIAL_HO_GAUSS)
   GBDMC_SYS(GBDMC_PES_HO, 3, GBDMC_TRIAL_HO_GAUSS)
   GBDMC_SYS(GBDMC_PES_H2O_LM, 3, GBDMC_TRIAL_H2O_GAUSS)

@@ -21,7 +21,8 @@ import torch
 from . import _capi
 from .constants import Constants
 
-__all__ = ["Potential_GPU", "PESFunction", "harmonic_oscillator", "h2o_local_mode", "water_dimer", "WATER_DIMER_EQ",
+__all__ = ["Potential_GPU", "PESFunction", "harmonic_oscillator", "h2o_local_mode", "water_dimer",
+           "partridge_schwenke", "WATER_DIMER_EQ",
            "to_soa", "from_soa", "default_device"]
 
 
@@ -54,23 +55,25 @@ def _stream():
 class Potential_GPU:
     """Built-in analytic PES evaluated on the GPU.
 
-    :param kind: 'harmonic_oscillator' | 'h2o_local_mode' | 'water_dimer'
+    :param kind: 'harmonic_oscillator' | 'h2o_local_mode' | 'water_dimer' |
+        'partridge_schwenke'
     :param params: dict of the PES parameters (see the factory functions)
     :param natoms: number of atoms (fixed for the water PESs)
     """
 
     KINDS = {"harmonic_oscillator": _capi.PES_HO, "h2o_local_mode": _capi.PES_H2O_LM,
-             "water_dimer": _capi.PES_DIMER}
+             "water_dimer": _capi.PES_DIMER, "partridge_schwenke": _capi.PES_H2O_PS}
     ORDER = {"harmonic_oscillator": ["k"],
              "h2o_local_mode": ["De", "a", "re", "ktheta", "theta_e", "krr"],
-             "water_dimer": ["De", "a", "re", "ktheta", "theta_e", "krr", "eps", "sigma", "qH", "qO"]}
+             "water_dimer": ["De", "a", "re", "ktheta", "theta_e", "krr", "eps", "sigma", "qH", "qO"],
+             "partridge_schwenke": ["hho"]}
 
     def __init__(self, kind, params, natoms=None, device=None):
         if kind not in self.KINDS:
             raise ValueError(f"unknown PES kind {kind!r}; choose one of {sorted(self.KINDS)}")
         self.kind = kind
         self.params = dict(params)
-        fixed = {"h2o_local_mode": 3, "water_dimer": 6}
+        fixed = {"h2o_local_mode": 3, "water_dimer": 6, "partridge_schwenke": 3}
         self.natoms = fixed.get(kind, natoms if natoms is not None else 1)
         if natoms is not None and natoms != self.natoms:
             raise ValueError(f"{kind} has {self.natoms} atoms, got natoms={natoms}")
@@ -146,6 +149,17 @@ def harmonic_oscillator(omega_wavenumbers=3000.0, mass_amu=1.00782505, natoms=1,
     m = mass_amu * Constants.atomic_units["amu"]
     w = Constants.convert(omega_wavenumbers, "wavenumbers")
     return Potential_GPU("harmonic_oscillator", {"k": m * w * w}, natoms=natoms, device=device)
+
+
+def partridge_schwenke(atom_order="OHH", device=None):
+    """The Partridge-Schwenke water PES (J. Chem. Phys. 106, 4618 (1997)) that
+    the reference ships as its Fortran sample potential
+    (sample_potentials/FortPots/Partridge_Schwenke_H2O), as a GPU kernel.
+    ``atom_order`` 'HHO' takes the reference's calc_hoh_pot coordinate order
+    (H, H, O); 'OHH' the order of the other water PESs here."""
+    if atom_order not in ("OHH", "HHO"):
+        raise ValueError("atom_order must be 'OHH' or 'HHO'")
+    return Potential_GPU("partridge_schwenke", {"hho": 1.0 if atom_order == "HHO" else 0.0}, device=device)
 
 
 def h2o_local_mode(De=0.1869, a=1.2, re=1.81, ktheta=0.16, theta_e_deg=104.5, krr=0.01, device=None):

@@ -119,6 +119,65 @@ def test_dimer_trial_matches_oracle():
     np.testing.assert_allclose(d2, o2, rtol=0, atol=1e-8)
 
 
+def ps_geoms(n, seed=7, scale=0.08):
+    from oracle.ps_oracle import ps_data
+    d = ps_data()
+    re_, th = float(d["reoh"]), np.arccos(float(d["ce"]))
+    eq = np.array([[0, 0, 0], [re_, 0, 0], [re_ * np.cos(th), re_ * np.sin(th), 0]], dtype=float)
+    return eq[None] + scale * oracle.InjectedNoise(seed).standard_normal((n, 3, 3))
+
+
+@pytest.mark.parametrize("order", ["OHH", "HHO"])
+@pytest.mark.parametrize("n", [1, 33, 4097])
+def test_partridge_schwenke_matches_oracle(order, n):
+    """The Partridge-Schwenke kernel (nested-Horner polynomial, cos(theta) and r_HH from
+    the bond vectors) against the term-by-term restatement of vibpot, and its adjoint
+    against central differences of the oracle."""
+    from oracle.ps_oracle import pes_ps
+    x = ps_geoms(n)
+    if order == "HHO":
+        x = x[:, [1, 2, 0]]
+    pot = pg.partridge_schwenke(atom_order=order)
+    np.testing.assert_allclose(pot.getpot(x), pes_ps(x, order), rtol=0, atol=1e-12)
+    v, g = pot.getgrad(x)
+    h = 1e-5
+    fd = np.zeros_like(x)
+    for a in range(3):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[:, a, d] += h
+            xm[:, a, d] -= h
+            fd[:, a, d] = (pes_ps(xp, order) - pes_ps(xm, order)) / (2 * h)
+    np.testing.assert_allclose(g, fd, rtol=0, atol=2e-7)
+
+
+def test_partridge_schwenke_dmc_reproduces_the_reference_sample_runs():
+    """The reference's own sample runs on this PES (tutorial_water_0..4: 8000 walkers,
+    dt = 5, 5000 steps, discrete) print the ensemble's mean potential after each move;
+    its average over steps 500-4999, over five runs, against five GPU runs."""
+    import json
+    ref = json.load(open(os.path.join(G, "ps_tutorial_reference.json")))
+    r0 = ref["runs"][0]
+    mref = np.array([r["mean_v_cm"] for r in ref["runs"]])
+    x0 = ps_geoms(1, scale=0.0)[:, [1, 2, 0]]
+    ours = []
+    for seed in range(5):
+        sim = pg.DMC_Sim(num_walkers=r0["walkers"], num_timesteps=r0["steps"], equil_steps=10 ** 9,
+                         atoms=["H", "H", "O"], masses=r0["masses"], delta_t=r0["dt"],
+                         potential=pg.partridge_schwenke(atom_order="HHO"), start_structures=x0, seed=100 + seed,
+                         write_files=False, graph_steps=32)
+        sim._init_device()
+        sim._run_steps(r0["steps"])
+        torch.cuda.synchronize()
+        assert int(sim._read_ctrl().status) == 0
+        vm = sim._hist["vmean"].cpu().numpy()[ref["first_step"]:r0["steps"]]
+        ours.append(pg.Constants.convert(vm, "wavenumbers", to_AU=False).mean())
+    ours = np.array(ours)
+    d = ours.mean() - mref.mean()
+    err = np.hypot(ours.std(ddof=1) / np.sqrt(len(ours)), mref.std(ddof=1) / np.sqrt(len(mref)))
+    assert abs(d) < 0.5 + 4.0 * err, (ours, mref, d, err)
+
+
 # ----------------------------------------------------------------- engine
 def _sim(x0, masses, atoms, pot, seed, nsteps, **kw):
     return pg.DMC_Sim(sim_name="t", output_folder="/tmp/gbdmc_test", num_walkers=len(x0), num_timesteps=nsteps,

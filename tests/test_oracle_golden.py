@@ -168,3 +168,36 @@ def test_dimer_trial_derivatives_match_finite_differences():
             pp, pm = tr.psi(xp), tr.psi(xm)
             np.testing.assert_allclose(f[:, a, d], (pp - pm) / (2 * h) / psi0, rtol=1e-6, atol=1e-6)
             np.testing.assert_allclose(d2[:, a, d], (pp - 2 * psi0 + pm) / (h * h) / psi0, rtol=1e-4, atol=1e-3)
+
+
+REF_PS = "/root/reference/pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_PS), reason="the reference source is not present")
+def test_ps_coefficients_match_the_fortran_source():
+    """The committed Partridge-Schwenke tables against an independent read of the
+    Fortran DATA statements and vibpot's first-call scaling (h2opes_v2.f:420-458)."""
+    import re
+    from oracle.ps_oracle import ps_data
+    src = open(REF_PS).read()
+
+    def block(name):
+        m = re.search(r"data \(" + name + r"\(i\),i=1,245\)/(.*?)/", src, re.S)
+        return np.array([float(t.replace("D", "e")) for t in re.findall(r"-?\d\.\d+D[-+]\d+", m.group(1))])
+
+    c5z, cb, cc, cr = (block(n) for n in ("c5z", "cbasis", "ccore", "crest"))
+    c = (0.99967788500000 * c5z + 0.15860145369897 * cb - 1.6351695982132 * cc + 1.0 * cr) * 4.556335e-6
+    c[0] *= 2.0
+    d = ps_data()
+    np.testing.assert_allclose(d["c"], c, rtol=1e-14, atol=1e-20)
+    assert d["idx"].shape == (245, 3) and d["idx"].min() == 1 and d["idx"][:, 2].max() <= 15
+
+
+def test_ps_oracle_is_near_zero_at_its_expansion_centre():
+    from oracle.ps_oracle import pes_ps, ps_data
+    d = ps_data()
+    re_, th = float(d["reoh"]), np.arccos(float(d["ce"]))
+    ohh = np.array([[0, 0, 0], [re_, 0, 0], [re_ * np.cos(th), re_ * np.sin(th), 0]], dtype=float)[None]
+    v = pes_ps(ohh)
+    assert abs(v[0]) < 1.0 * oracle.WAVENUMBERS
+    np.testing.assert_allclose(pes_ps(ohh[:, [1, 2, 0]], order="HHO"), v, rtol=0, atol=1e-15)
