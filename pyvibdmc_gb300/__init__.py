@@ -13,11 +13,12 @@ from .potentials import (Potential_GPU, PESFunction, harmonic_oscillator, h2o_lo
 from .imp_samp import ImpSampManager_GPU, TrialFunction, h2o_gaussian_trial, ho_gaussian_trial, \
     dimer_gaussian_trial
 from .engine import DMC_Sim, HostWalkers, dmc_restart
+from .initial import HarmonicAnalysis, InitialConditioner
 from .batch import DMC_Batch, blocking_error
 from .surrogate import MLPSurrogate, NN_Potential_GPU, NNDMC, harvest_training_data
 from . import _capi
 
-__all__ = ["HostWalkers", "Constants", "get_atomic_num", "get_atomic_string", "Potential_GPU", "PESFunction",
+__all__ = ["HostWalkers", "HarmonicAnalysis", "InitialConditioner", "Constants", "get_atomic_num", "get_atomic_string", "Potential_GPU", "PESFunction",
            "harmonic_oscillator", "h2o_local_mode", "water_dimer", "partridge_schwenke", "ImpSampManager_GPU", "TrialFunction",
            "h2o_gaussian_trial", "ho_gaussian_trial", "dimer_gaussian_trial", "DMC_Sim", "dmc_restart", "DMC_Batch", "blocking_error",
            "MLPSurrogate", "NN_Potential_GPU", "NNDMC", "harvest_training_data", "WATER_DIMER_EQ",
