@@ -337,6 +337,15 @@ def run_ours(args):
     e_b.record(stream)
     torch.cuda.synchronize()
     fp64_tflops = flops.value / (e_a.elapsed_time(e_b) / 1e3) / 1e12
+    # the bound that binds: FP64 FLOPs of k_move per walker (ncu DADD/DMUL/DFMA counts) over its event time
+    fp64_roof = None
+    fp_path = os.path.join(ROOT, "profiles", "k_move_h2o_20k_fp64.json")
+    if os.path.exists(fp_path):
+        fpw = json.load(open(fp_path))["fp64_flops_per_walker"]
+        ach = fpw * float(popp.mean()) / move_avg_s / 1e12
+        fp64_roof = {"bound": "fp64", "achieved": ach, "peak": fp64_tflops, "unit": "TFLOP/s",
+                     "frac": ach / fp64_tflops, "peak_kind": "measured (gbdmc_fp64_fma_probe, this run)",
+                     "flops_per_walker": fpw}
 
     # ---- e2e through the C ABI with host buffers
     e2e_steps = max(50, min(K, 500))
@@ -357,7 +366,7 @@ def run_ours(args):
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "bytes_per_walker": BYTES_MOVE_KERNEL,
                          "kernel_avg_us": move_avg_s * 1e6, "scatter_avg_us": sc_ms.value / max(sc_n.value, 1) * 1e3,
-                         "fp64_fma_probe_tflops": fp64_tflops},
+                         "fp64_fma_probe_tflops": fp64_tflops, "fp64": fp64_roof},
             "e2e": e2e}
     if not args.no_extras and world == 1:
         try:
@@ -477,7 +486,7 @@ def run_extras(steps):
     torch.cuda.synchronize()
     t_h = time.perf_counter() - t_h
     t_t = time.perf_counter()
-    m = pg.MLPSurrogate(seed=0).fit(x, v, g, epochs=10, batch=8192, lr=2e-3)
+    m = pg.MLPSurrogate(seed=0).fit(x, v, g, epochs=30, batch=8192, lr=2e-3)
     torch.cuda.synchronize()
     t_t = time.perf_counter() - t_t
     nd = pg.NNDMC(m, pot, 200000, pg.WATER_DIMER_EQ[None], dm, DT, steps + 64, seed=5, audit_every=100).init()
