@@ -249,3 +249,28 @@ def test_surrogate_is_zpe_agrees_with_fp64_is(dimer_model):
     d = z_nn[0] - z_fp[0]
     err = float(np.hypot(z_nn[1], z_fp[1]))
     assert abs(d) < 3.0 + 4.0 * err, (z_nn, z_fp, nd.audit())
+
+
+def test_trained_surrogate_gains_over_the_fp64_pes(dimer_model):
+    """What the trained network gains over the method without it: one surrogate DMC
+    step of 200000 dimer walkers against one step of the FP64 analytic PES, same
+    walkers, dt and branching (graph-replayed steps, CUDA events).  The ZPE agreement
+    of the two is checked in the statistical tests above and in the bench extras."""
+    m, pot, masses = dimer_model
+    nd = NNDMC(m, pot, 200000, pg.WATER_DIMER_EQ[None], masses, 10.0, 200, seed=4).init()
+    fp = pg.DMC_Sim(num_walkers=200000, num_timesteps=200, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                    masses=masses, delta_t=10.0, potential=pot, start_structures=pg.WATER_DIMER_EQ[None], seed=4,
+                    write_files=False, graph_steps=16)
+    fp._init_device()
+    nd.run(32)
+    fp._run_steps(32)
+    torch.cuda.synchronize()
+    times = []
+    for run in (nd.run, fp._run_steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run(64)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 64)
+    assert times[0] < 0.85 * times[1], times
