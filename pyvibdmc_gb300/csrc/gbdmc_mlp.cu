@@ -535,8 +535,11 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
 
 // Phase 2: analytic fp64 energy for the listed walkers (audit subset and
 // out-of-box fallback), 8 lanes per walker (one part each, summed in a fixed
-// shuffle order); audited differences V_nn - V_analytic are accumulated in
-// audit[0..2], fallbacks in audit[3].
+// shuffle order).  The replicas are processed side by side: the grid is cut
+// into units of (replica, share of that replica's list), so a batch of many
+// replicas does not walk its replicas one after another.  Audited differences
+// V_nn - V_analytic are summed per block and added to audit[0..2] (fallbacks
+// to audit[3]) with one atomic each per block.
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     gbdmc_ctrl_t* ctrls, const int* list,
@@ -544,7 +547,13 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
   const int part = threadIdx.x & 7;
-  for (int r = 0; r < T.nrep; ++r) {
+  const int nrep = T.nrep;
+  const int per_rep = gridDim.x >= (unsigned)nrep ? (int)(gridDim.x / nrep) : 1;  // blocks per replica
+  const int units = nrep * per_rep;
+  const int wpb = blockDim.x >> 5;
+  double s_n = 0.0, s_d = 0.0, s_d2 = 0.0, s_fb = 0.0;
+  for (int u = blockIdx.x; u < units; u += gridDim.x) {
+    const int r = u / per_rep, sub = u % per_rep;
     const gbdmc_ctrl_t* ctrl = ctrls + r;
     if (*(volatile const int*)&ctrl->status) continue;
     long long cnt = *(volatile const long long*)&ctrl->reserved[2];
@@ -552,8 +561,8 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     const int64_t base = T.off[r];
     // a warp takes 4 walkers per iteration (lanes 8k..8k+7 -> walker jb + k); the
     // loop bound is warp-uniform, so the shuffles below see all 32 lanes
-    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long gw = (long long)sub * wpb + (threadIdx.x >> 5);
+    const long long nw = (long long)per_rep * wpb;
     for (long long jb = 4 * gw; jb < cnt; jb += 4 * nw) {
       const long long j = jb + ((threadIdx.x & 31) >> 3);
       const bool live = j < cnt;
@@ -574,13 +583,33 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
         const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
         if (fl & 2) {
           const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
-          atomicAdd(audit + 0, 1.0);
-          atomicAdd(audit + 1, d);
-          atomicAdd(audit + 2, d * d);
+          s_n += 1.0;
+          s_d += d;
+          s_d2 += d * d;
         }
-        if (fl & 1) atomicAdd(audit + 3, 1.0);
+        if (fl & 1) s_fb += 1.0;
         out.v[dst] = v + ke;
       }
+    }
+  }
+  {  // block sums of the audit statistics, one atomic per quantity
+    __shared__ double red[4][4];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    s_n = warp_sum(s_n);
+    s_d = warp_sum(s_d);
+    s_d2 = warp_sum(s_d2);
+    s_fb = warp_sum(s_fb);
+    if (lane == 0) {
+      red[w][0] = s_n;
+      red[w][1] = s_d;
+      red[w][2] = s_d2;
+      red[w][3] = s_fb;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      double t = 0.0;
+      for (int k = 0; k < wpb; ++k) t += red[k][threadIdx.x];
+      if (t != 0.0) atomicAdd(audit + threadIdx.x, t);
     }
   }
   // last block: c <- (1 - beta) c + beta * (mean audited error of this step)
@@ -600,23 +629,23 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     audit[5] = audit[0];
     audit[6] = audit[1];
     *reinterpret_cast<unsigned long long*>(audit + 7) = 0ull;
-    if (S.trial.kind != GBDMC_TRIAL_NONE) {
-      // dt_factor = accepted / N (pyvibdmc.py:603) for the weights of this step; effective time (:372-378)
-      for (int r = 0; r < T.nrep; ++r) {
-        gbdmc_ctrl_t* c = ctrls + r;
-        if (*(volatile int*)&c->status) continue;
-        const long long n = c->n, step = c->step;
-        const long long na = *(volatile long long*)&c->n_acc;
-        const double dte = S.dt * ((double)na / (double)n);
-        c->dt_eff = dte;
-        c->eff_ts = (step == 0) ? dte : c->eff_ts + dte;
-        if (step < S.hist.len) {
-          const int64_t h = (int64_t)r * S.hist.len + step;
-          if (S.hist.rejected) S.hist.rejected[h] = (int)(n - na);
-          if (S.hist.eff_ts) S.hist.eff_ts[h] = c->eff_ts;
-        }
-        c->n_acc = 0;
+  }
+  if (am_last && S.trial.kind != GBDMC_TRIAL_NONE) {
+    // dt_factor = accepted / N (pyvibdmc.py:603) for the weights of this step; effective time (:372-378)
+    for (int r = threadIdx.x; r < T.nrep; r += blockDim.x) {
+      gbdmc_ctrl_t* c = ctrls + r;
+      if (*(volatile int*)&c->status) continue;
+      const long long n = c->n, step = c->step;
+      const long long na = *(volatile long long*)&c->n_acc;
+      const double dte = S.dt * ((double)na / (double)n);
+      c->dt_eff = dte;
+      c->eff_ts = (step == 0) ? dte : c->eff_ts + dte;
+      if (step < S.hist.len) {
+        const int64_t h = (int64_t)r * S.hist.len + step;
+        if (S.hist.rejected) S.hist.rejected[h] = (int)(n - na);
+        if (S.hist.eff_ts) S.hist.eff_ts[h] = c->eff_ts;
       }
+      c->n_acc = 0;
     }
   }
 }
