@@ -514,7 +514,7 @@ def run_extras(steps):
     return out
 
 
-def run_combined_dimer(m, pot, dm, T=3000):
+def run_combined_dimer(m, pot, dm, T=6000):
     """The engine with all three accelerations on one system, the water dimer:
     importance sampling (dimer trial), the tcgen05 surrogate PES and 64
     batched replicas (N_r ~ U[1000, 65536]), against the plain FP64 dimer

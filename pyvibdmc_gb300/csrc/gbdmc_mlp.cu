@@ -534,19 +534,23 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
 }
 
 // Phase 2: analytic fp64 energy for the listed walkers (audit subset and
-// out-of-box fallback), 8 lanes per walker (one part each, summed in a fixed
-// shuffle order).  The replicas are processed side by side: the grid is cut
+// out-of-box fallback).  LANES = 8: 8 lanes per walker (one part each, summed
+// in a fixed shuffle order) -- short lists, where the latency of one walker's
+// PES matters; LANES = 1: one walker per thread -- long lists (large batches),
+// where the FP64 pipe's throughput matters and 8 lanes would issue 6x the FP64
+// warp instructions.  The replicas are processed side by side: the grid is cut
 // into units of (replica, share of that replica's list), so a batch of many
 // replicas does not walk its replicas one after another.  Audited differences
 // V_nn - V_analytic are summed per block and added to audit[0..2] (fallbacks
 // to audit[3]) with one atomic each per block.
+template <int LANES>
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     gbdmc_ctrl_t* ctrls, const int* list,
                                                     const unsigned char* flags, double* audit, float beta) {
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
-  const int part = threadIdx.x & 7;
+  const int part = threadIdx.x & (LANES - 1);
   const int nrep = T.nrep;
   const int per_rep = gridDim.x >= (unsigned)nrep ? (int)(gridDim.x / nrep) : 1;  // blocks per replica
   const int units = nrep * per_rep;
@@ -559,12 +563,13 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     long long cnt = *(volatile const long long*)&ctrl->reserved[2];
     if (cnt > T.cap[r]) cnt = T.cap[r];
     const int64_t base = T.off[r];
-    // a warp takes 4 walkers per iteration (lanes 8k..8k+7 -> walker jb + k); the
-    // loop bound is warp-uniform, so the shuffles below see all 32 lanes
+    // a warp takes 32/LANES walkers per iteration (lanes LANES*k .. LANES*k+LANES-1 ->
+    // walker jb + k); the loop bound is warp-uniform, so the shuffles see all 32 lanes
+    constexpr int WPW = 32 / LANES;  // walkers per warp and iteration
     const long long gw = (long long)sub * wpb + (threadIdx.x >> 5);
     const long long nw = (long long)per_rep * wpb;
-    for (long long jb = 4 * gw; jb < cnt; jb += 4 * nw) {
-      const long long j = jb + ((threadIdx.x & 31) >> 3);
+    for (long long jb = WPW * gw; jb < cnt; jb += WPW * nw) {
+      const long long j = jb + ((threadIdx.x & 31) / LANES);
       const bool live = j < cnt;
       double v = 0.0;
       int64_t dst = 0;
@@ -573,11 +578,18 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
         double xd[18];
 #pragma unroll
         for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
-        v = dimer_part(xd, S.pes.p, part);
+        if constexpr (LANES == 1) {
+          double gd[18];
+          v = pes_dimer<false>(xd, S.pes.p, gd);
+        } else {
+          v = dimer_part(xd, S.pes.p, part);
+        }
       }
-      v += __shfl_xor_sync(0xffffffffu, v, 4);
-      v += __shfl_xor_sync(0xffffffffu, v, 2);
-      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if constexpr (LANES == 8) {
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 2);
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+      }
       if (live && part == 0) {
         const unsigned char fl = flags[dst];
         const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
@@ -1000,7 +1012,14 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
                                                           nz);
   }
   if (prof) cudaEventRecord(ev[1], s);
-  k_mlp_audit<<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+  // expected list length: the audit share of the walkers (the out-of-box fallbacks are few)
+  long long slots = 0;
+  for (int r = 0; r < T.nrep; ++r) slots += T.cap[r];
+  const long long expect = net->audit_every > 0 ? slots / net->audit_every : 0;
+  if (expect > 16384)
+    k_mlp_audit<1><<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+  else
+    k_mlp_audit<8><<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
   rc = mlp_table(S, reps, nrep, T2, what, 256);
   if (rc) return rc;
