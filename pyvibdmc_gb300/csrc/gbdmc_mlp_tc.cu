@@ -1,7 +1,9 @@
 // MLP surrogate forward on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// One CTA of 128 threads processes tiles of 128 walkers, one walker per
-// thread.  The hidden layers are M=128 x N=128 x K tcgen05.mma instructions
+// A tile group of 128 threads processes tiles of 128 walkers, one walker per
+// thread; a CTA holds G groups (G = 4 in the DMC step: 16 warps on the SM
+// sharing one copy of the weights in shared memory, each group with its own
+// activation buffer, mbarrier, named barrier and 128 TMEM columns).  The hidden layers are M=128 x N=128 x K tcgen05.mma instructions
 // (kind::f16, BF16 operands, FP32 accumulation) issued by one thread:
 //   A = activations of the tile, B = transposed weights, both in shared memory
 //       in the canonical K-major no-swizzle layout (8-row x 16-byte core
@@ -28,15 +30,48 @@ constexpr int kThreads = 128;
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
                             ((uint32_t)(kRows >> 4) << 24);
 
-struct TcSmem {
-  alignas(128) unsigned char w1[kN * 16 * 2];    // N=128 x K=16 (KG = 2)
-  alignas(128) unsigned char w2[kN * kN * 2];    // N=128 x K=128 (KG = 16)
+template <int G>
+struct TcSmemG {
+  alignas(128) unsigned char w1[kN * 16 * 2];       // N=128 x K=16 (KG = 2)
+  alignas(128) unsigned char w2[kN * kN * 2];       // N=128 x K=128 (KG = 16)
   alignas(128) unsigned char w3[kN * kN * 2];
-  alignas(128) unsigned char a[kRows * kN * 2];  // M=128 x K=128 (KG = 16)
+  alignas(128) unsigned char a[G][kRows * kN * 2];  // per group: M=128 x K=128 (KG = 16)
   float b1[kN], b2[kN], b3[kN], w4[kN];
-  alignas(8) unsigned long long mbar;
+  alignas(8) unsigned long long mbar[G];
   uint32_t tmem_base;
 };
+constexpr int kGroups = 4;  // tile groups per CTA of the DMC step kernel
+using TcSmem = TcSmemG<1>;
+
+// What one tile group owns: its activation buffer, mbarrier, TMEM columns,
+// named barrier (bar.sync id over the group's 128 threads) and its thread index.
+struct Grp {
+  unsigned char* a;
+  uint32_t mbar;
+  uint32_t tmem;
+  int bar;
+  int lt;
+};
+
+__device__ __forceinline__ void group_sync(int bar) { asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory"); }
+// OR / population count of a predicate over the group (one barrier; the result is group-uniform)
+__device__ __forceinline__ bool group_any(bool v, int bar) {
+  int r;
+  asm volatile(
+      "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, %2, 128, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((int)v), "r"(bar)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ int group_count(bool v, int bar) {
+  int r;
+  asm volatile("{\n.reg .pred p;\nsetp.ne.s32 p, %1, 0;\nbar.red.popc.u32 %0, %2, 128, p;\n}\n"
+               : "=r"(r)
+               : "r"((int)v), "r"(bar)
+               : "memory");
+  return r;
+}
 
 // byte offset of element (row, k) of a canonical K-major operand with KG core columns
 __device__ __forceinline__ uint32_t canon_off(int row, int k, int KG) {
@@ -104,7 +139,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32]) {
   for (int j = 0; j < 32; ++j) r[j] = __uint_as_float(u[j]);
 }
 
-__device__ void load_weights(TcSmem& sm, const gbdmc_mlp_t& net) {
+template <int G>
+__device__ void load_weights(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
   // Wt is n-major [128][K] in global; 16-byte chunks = 8 consecutive k of one row n
   for (int c = threadIdx.x; c < kN * 2; c += blockDim.x) {
     const int n = c >> 1, kg = c & 1;
@@ -127,8 +163,8 @@ __device__ void load_weights(TcSmem& sm, const gbdmc_mlp_t& net) {
 }
 
 // Bias + SiLU of this thread's accumulator row, written as BF16 A row (KG = 16).
-__device__ __forceinline__ void epilogue_to_a(TcSmem& sm, uint32_t trow, const float* bias) {
-  const int t = threadIdx.x;
+__device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow, const float* bias) {
+  const int t = gp.lt;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float r[32];
@@ -141,50 +177,52 @@ __device__ __forceinline__ void epilogue_to_a(TcSmem& sm, uint32_t trow, const f
         const int j = 8 * q + 2 * e, n = 32 * c + j;
         p[e] = pack_bf16(silu(r[j] + bias[n]), silu(r[j + 1] + bias[n + 1]));
       }
-      *reinterpret_cast<uint4*>(sm.a + canon_off(t, 32 * c + 8 * q, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
+      *reinterpret_cast<uint4*>(gp.a + canon_off(t, 32 * c + 8 * q, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
     }
   }
 }
 
 // Issue the K/16 MMAs of one layer (thread 0) and wait for them.
-__device__ __forceinline__ bool run_layer(TcSmem& sm, uint32_t tmem, uint32_t mbar, uint32_t& phase,
-                                          const unsigned char* w, int KG) {
+__device__ __forceinline__ bool run_layer(const Grp& gp, uint32_t& phase, const unsigned char* w, int KG) {
   fence_proxy_async();
   tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  group_sync(gp.bar);
+  if (gp.lt == 0) {
     tc_fence_after();
-    const uint32_t a0 = saddr(sm.a), b0 = saddr(w);
+    const uint32_t a0 = saddr(gp.a), b0 = saddr(w);
     for (int s = 0; s < KG / 2; ++s)
-      umma(tmem, smem_desc(a0 + 256u * s, kCore, 16 * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
+      umma(gp.tmem, smem_desc(a0 + 256u * s, kCore, 16 * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
            s > 0 ? 1u : 0u);
-    umma_commit(mbar);
+    umma_commit(gp.mbar);
   }
-  const bool ok = mbar_wait(mbar, phase);
+  const bool ok = mbar_wait(gp.mbar, phase);
   phase ^= 1u;
   tc_fence_after();
   return ok;
 }
 
 // Network output (normalised, without b4) of this thread's feature row f.
-__device__ __forceinline__ float forward_tile(TcSmem& sm, uint32_t tmem, uint32_t mbar, uint32_t& phase,
-                                              const float (&f)[16], bool& ok) {
-  const int t = threadIdx.x;
-  const uint32_t trow = tmem + ((uint32_t)(32 * (t >> 5)) << 16);
+// TMEM lane quarter of a warp = its warp index mod 4, which for a group of four
+// aligned warps is the warp's index within the group.
+template <int G>
+__device__ __forceinline__ float forward_tile(TcSmemG<G>& sm, const Grp& gp, uint32_t& phase, const float (&f)[16],
+                                              bool& ok) {
+  const int t = gp.lt;
+  const uint32_t trow = gp.tmem + ((uint32_t)(32 * (t >> 5)) << 16);
   {
     uint32_t p[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) p[q] = pack_bf16(f[2 * q], f[2 * q + 1]);
-    *reinterpret_cast<uint4*>(sm.a + canon_off(t, 0, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
-    *reinterpret_cast<uint4*>(sm.a + canon_off(t, 8, 16)) = make_uint4(p[4], p[5], p[6], p[7]);
+    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 0, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 8, 16)) = make_uint4(p[4], p[5], p[6], p[7]);
   }
-  ok &= run_layer(sm, tmem, mbar, phase, sm.w1, 2);
-  epilogue_to_a(sm, trow, sm.b1);
+  ok &= run_layer(gp, phase, sm.w1, 2);
+  epilogue_to_a(gp, trow, sm.b1);
   tc_fence_before();
-  ok &= run_layer(sm, tmem, mbar, phase, sm.w2, 16);
-  epilogue_to_a(sm, trow, sm.b2);
+  ok &= run_layer(gp, phase, sm.w2, 16);
+  epilogue_to_a(gp, trow, sm.b2);
   tc_fence_before();
-  ok &= run_layer(sm, tmem, mbar, phase, sm.w3, 16);
+  ok &= run_layer(gp, phase, sm.w3, 16);
   float e = 0.f;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
@@ -194,17 +232,21 @@ __device__ __forceinline__ float forward_tile(TcSmem& sm, uint32_t tmem, uint32_
     for (int j = 0; j < 32; ++j) e += silu(r[j] + sm.b3[32 * c + j]) * sm.w4[32 * c + j];
   }
   tc_fence_before();
-  __syncthreads();  // TMEM rows read and A free before the next tile
+  group_sync(gp.bar);  // TMEM rows read and A free before the group's next tile
   return e;
 }
 
-__device__ __forceinline__ void setup(TcSmem& sm, const gbdmc_mlp_t& net, uint32_t& tmem, uint32_t& mbar) {
+// Weights into shared memory, G mbarriers, G x 128 TMEM columns (warp 0);
+// returns the TMEM base address.
+template <int G>
+__device__ __forceinline__ uint32_t setup(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
+  static_assert(G == 1 || G == 2 || G == 4, "TMEM allocations are powers of two of at least 32 columns");
   load_weights(sm, net);
-  mbar = saddr(&sm.mbar);
-  if (threadIdx.x == 0) mbar_init(mbar);
+  if (threadIdx.x == 0)
+    for (int g = 0; g < G; ++g) mbar_init(saddr(&sm.mbar[g]));
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&sm.tmem_base)),
-                 "r"(kCols)
+                 "r"(kCols * G)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -212,15 +254,16 @@ __device__ __forceinline__ void setup(TcSmem& sm, const gbdmc_mlp_t& net, uint32
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  tmem = sm.tmem_base;
+  return sm.tmem_base;
 }
 
+template <int G>
 __device__ __forceinline__ void teardown(uint32_t tmem) {
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (threadIdx.x < 32)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols * G) : "memory");
 }
 
 // Energies of n walkers (fp32 SoA coordinates) -- the tcgen05 twin of k_mlp_energy.
@@ -230,8 +273,9 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
                                                              int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
-  uint32_t tmem, mbar, phase = 0;
-  setup(sm, net, tmem, mbar);
+  uint32_t phase = 0;
+  const uint32_t tmem = setup(sm, net);
+  const Grp gp{sm.a[0], saddr(&sm.mbar[0]), tmem, 0, (int)threadIdx.x};
   bool ok = true;
   for (long long base = (long long)blockIdx.x * kRows; base < n; base += (long long)gridDim.x * kRows) {
     const long long i = base + threadIdx.x;
@@ -239,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
 #pragma unroll
     for (int k = 0; k < 18; ++k) xs[k] = i < n ? x[k * ld + i] : (k < 3 ? 0.f : 1.f + k);
     const bool oob = walker_features(xs, net, f) && i < n;
-    const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
+    const float e = forward_tile(sm, gp, phase, f, ok);
     if (i < n) v[i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4);
     if (oob && outside) outside[i] = 1;
     if (__syncthreads_or(!ok)) {
@@ -247,37 +291,41 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
       break;
     }
   }
-  teardown(tmem);
+  teardown<1>(tmem);
 }
 
 // Phase 1 of a surrogate DMC step on tcgen05: gather + move + descriptors
 // (one walker per thread), MLP forward, V; audit/out-of-box walkers are
 // listed for k_mlp_audit exactly like the mma.sync path.
-__global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_constant__ gbdmc_sim_t S,
-                                                                  const __grid_constant__ RepTable T,
-                                                                  const __grid_constant__ gbdmc_mlp_t net,
-                                                                  const gbdmc_walkers_f32_t in,
-                                                                  gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls,
-                                                                  int* list, unsigned char* flags,
-                                                                  const double* audit, const gbdmc_noise_t nz) {
+// The CTA holds kGroups tile groups; group g takes tiles blockIdx.x * kGroups + g,
+// + gridDim.x * kGroups, ...  Every decision that skips or ends a group's tile
+// (replica stopped, tile beyond N, tensor-core timeout) is made uniform over
+// the group with a barrier reduction, so the group's named barriers always
+// see all of its 128 threads.
+__global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
+    const __grid_constant__ gbdmc_sim_t S, const __grid_constant__ RepTable T, const __grid_constant__ gbdmc_mlp_t net,
+    const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
+    const double* audit, const gbdmc_noise_t nz) {
   extern __shared__ __align__(1024) unsigned char smraw[];
-  TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
+  TcSmemG<kGroups>& sm = *reinterpret_cast<TcSmemG<kGroups>*>(smraw);
   const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
-  uint32_t tmem, mbar, phase = 0;
-  setup(sm, net, tmem, mbar);
+  uint32_t phase = 0;
+  const uint32_t tmem = setup(sm, net);
+  const int g = threadIdx.x >> 7;
+  const Grp gp{sm.a[g], saddr(&sm.mbar[g]), tmem + (uint32_t)(g * kN), 1 + g, (int)(threadIdx.x & 127)};
   bool ok = true;
   const int64_t ld = S.ld;
   const int ntile = T.tile_off[T.nrep];
-  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+  for (int tile = blockIdx.x * kGroups + g; tile < ntile; tile += gridDim.x * kGroups) {
     const int r = replica_of(T, tile);
     gbdmc_ctrl_t* ctrl = ctrls + r;
-    if (*(volatile int*)&ctrl->status) continue;
+    if (group_any(*(volatile int*)&ctrl->status != 0, gp.bar)) continue;  // replica stopped
     const long long n = ctrl->n;
     const long long step = ctrl->step;
     const int64_t base = T.off[r];
     const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * kRows;
-    if (i0 >= n) continue;  // block-uniform
-    const int64_t i = i0 + threadIdx.x;
+    if (i0 >= n) continue;  // group-uniform: n and the tile are the same for the whole group
+    const int64_t i = i0 + gp.lt;
     float xs[18], f[16];
     bool acc = false;
     float ke = 0.f;
@@ -335,23 +383,24 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_move_energy(const __grid_co
       walker_features(xs, net, f);
     }
     if (S.trial.kind != GBDMC_TRIAL_NONE) {  // accepted moves of the replica (dt_eff = dt * accepted / N)
-      const int nacc = __syncthreads_count(acc);
-      if (threadIdx.x == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
+      const int nacc = group_count(acc, gp.bar);
+      if (gp.lt == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
     }
-    const float e = forward_tile(sm, tmem, mbar, phase, f, ok);
+    const float e = forward_tile(sm, gp, phase, f, ok);
     if (i < n)
       out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4) - corr + (double)ke;
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+    if (group_any(!ok, gp.bar)) {
+      if (gp.lt == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
       break;
     }
   }
-  teardown(tmem);
+  teardown<kGroups>(tmem);
 }
 
 }  // namespace tc
 
 int tc_smem_bytes() { return (int)sizeof(tc::TcSmem) + 1024; }
+static int tc_group_smem_bytes() { return (int)sizeof(tc::TcSmemG<tc::kGroups>) + 1024; }
 
 int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, long long n, double* v, int* outside,
                          int* err, cudaStream_t s) {
@@ -372,15 +421,16 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
                               int* list, unsigned char* flags, const double* audit, const gbdmc_noise_t& nz,
                               cudaStream_t s) {
   const cudaError_t e = cudaFuncSetAttribute((const void*)tc::k_mlp_tc_move_energy,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes());
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, tc_group_smem_bytes());
   if (e != cudaSuccess) {
     set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
     return GBDMC_ERR_CUDA;
   }
-  int g = T.tile_off[T.nrep];
-  if (g > 2 * num_sms()) g = 2 * num_sms();
-  tc::k_mlp_tc_move_energy<<<g, tc::kThreads, tc_smem_bytes(), s>>>(S, T, net, in, out, ctrl, list, flags, audit,
-                                                                     nz);
+  // one CTA per SM (its shared memory and its 4 x 128 TMEM columns fill the SM)
+  int g = (T.tile_off[T.nrep] + tc::kGroups - 1) / tc::kGroups;
+  if (g > num_sms()) g = num_sms();
+  tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(S, T, net, in, out, ctrl,
+                                                                                         list, flags, audit, nz);
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 

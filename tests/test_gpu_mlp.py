@@ -274,3 +274,22 @@ def test_trained_surrogate_gains_over_the_fp64_pes(dimer_model):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 64)
     assert times[0] < 0.85 * times[1], times
+
+
+@pytest.mark.parametrize("nwalk", [300, 70000])
+def test_step_kernel_energies_equal_the_energy_kernel(dimer_model, nwalk):
+    """The DMC step kernel (move + descriptors + network in 128-walker tile groups, four
+    groups per CTA) gives each moved walker the same surrogate energy as the energy
+    kernel evaluated on the moved coordinates (audit and bias correction off)."""
+    m, pot, masses = dimer_model
+    nd = NNDMC(m, pot, nwalk, pg.WATER_DIMER_EQ[None], masses, 10.0, 4, seed=8, audit_every=0,
+               bias_control=0.0).init()
+    nd.run(1)
+    torch.cuda.synchronize()
+    b = nd._bufs[nd._cur]  # pre-branch moved walkers in slots 0..N-1
+    x = b["x"][:, :nwalk].contiguous()
+    v_step = b["v"][:nwalk].cpu().numpy()
+    v_ref, outside = m.energy_soa(x, nwalk, engine=1)
+    keep = outside.cpu().numpy() == 0
+    assert keep.mean() > 0.5
+    np.testing.assert_array_equal(v_step[keep], v_ref.cpu().numpy()[keep])
