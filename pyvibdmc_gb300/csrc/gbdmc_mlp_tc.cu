@@ -297,8 +297,9 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
 // Phase 1 of a surrogate DMC step on tcgen05: gather + move + descriptors
 // (one walker per thread), MLP forward, V; audit/out-of-box walkers are
 // listed for k_mlp_audit exactly like the mma.sync path.
-// The CTA holds kGroups tile groups; group g takes tiles blockIdx.x * kGroups + g,
-// + gridDim.x * kGroups, ...  Every decision that skips or ends a group's tile
+// The CTA holds kGroups tile groups; group g takes tiles blockIdx.x + g * gridDim.x,
+// + gridDim.x * kGroups, ... (so a run of fewer tiles than 4 x SMs still spreads
+// over all SMs).  Every decision that skips or ends a group's tile
 // (replica stopped, tile beyond N, tensor-core timeout) is made uniform over
 // the group with a barrier reduction, so the group's named barriers always
 // see all of its 128 threads.
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
   bool ok = true;
   const int64_t ld = S.ld;
   const int ntile = T.tile_off[T.nrep];
-  for (int tile = blockIdx.x * kGroups + g; tile < ntile; tile += gridDim.x * kGroups) {
+  for (int tile = blockIdx.x + g * gridDim.x; tile < ntile; tile += gridDim.x * kGroups) {
     const int r = replica_of(T, tile);
     gbdmc_ctrl_t* ctrl = ctrls + r;
     if (group_any(*(volatile int*)&ctrl->status != 0, gp.bar)) continue;  // replica stopped
@@ -427,7 +428,7 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
     return GBDMC_ERR_CUDA;
   }
   // one CTA per SM (its shared memory and its 4 x 128 TMEM columns fill the SM)
-  int g = (T.tile_off[T.nrep] + tc::kGroups - 1) / tc::kGroups;
+  int g = T.tile_off[T.nrep];
   if (g > num_sms()) g = num_sms();
   tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(S, T, net, in, out, ctrl,
                                                                                          list, flags, audit, nz);
