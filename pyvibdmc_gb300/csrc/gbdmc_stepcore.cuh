@@ -260,17 +260,18 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int r = replica_of(T, tile);
     gbdmc_ctrl_t* ctrl = ctrls + r;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t dst = T.off[r] + i;
+    // the energy load is issued with the control-block loads (slot i < cap is inside the replica)
+    const double v = i < T.cap[r] ? out.v[dst] : 0.0;
     if (*(volatile int*)&ctrl->status) continue;
     const long long n = ctrl->n;
     const long long step = ctrl->step;
     const double vref = ctrl->vref;
     const double dt = ctrl->dt_eff;
-    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
-    const int64_t dst = T.off[r] + i;
     Partial p = partial_zero();
     int flag = 0;
     if (i < n) {
-      const double v = out.v[dst];
       double u;
       if constexpr (NM == GBDMC_NOISE_INJECTED) {
         u = nz.u_branch[dst];
