@@ -1031,6 +1031,7 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   else
     k_count<GBDMC_NOISE_PHILOX32, true><<<grid_for(T2), T2.tpb, 0, s>>>(*S, T2, wv, ctrl, L.part, L.prefix,
                                                                          L.counts, nz);
+  k_count_finalize<<<T2.nrep, kMaxTPB, 0, s>>>(*S, T2, ctrl, L.part, L.prefix);
   launch_branch(T2, dst->idx, ctrl, L.prefix, L.counts, s);
   if (prof) {
     cudaEventRecord(ev[2], s);

@@ -704,6 +704,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
       k_count<NM, false><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
+      k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_pdl(k_branch, G, T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
     } else {
       k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);

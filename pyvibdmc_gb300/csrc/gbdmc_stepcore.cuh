@@ -309,11 +309,25 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     }
     p = block_reduce_partial<false>(p);
     if (threadIdx.x == 0) part[tile] = p;
+  }
+}
+
+// Finalisation of a counting pass, one CTA per replica: the partial
+// reduction, the tile-count scan into prefix[] and finalize_discrete.  The
+// kernel boundary after k_count makes every tile's partial visible, so the
+// counting tiles need no fence and no last-tile election.
+static __global__ void __launch_bounds__(kMaxTPB) k_count_finalize(const __grid_constant__ gbdmc_sim_t S,
+                                                                    const __grid_constant__ RepTable T,
+                                                                    gbdmc_ctrl_t* ctrls, const Partial* part,
+                                                                    long long* prefix) {
+  for (int r = blockIdx.x; r < T.nrep; r += gridDim.x) {
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile int*)&ctrl->status) continue;  // block-uniform: only this block writes this replica's status
+    const long long n = ctrl->n, step = ctrl->step;
     const int nt = T.tile_off[r + 1] - T.tile_off[r];
-    if (last_tile(ctrl, nt)) {
-      const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
-      if (threadIdx.x < 32) finalize_discrete<false>(S, T, r, ctrl, t, n, step);
-    }
+    const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
+    if (threadIdx.x < 32) finalize_discrete<false>(S, T, r, ctrl, t, n, step);
+    __syncthreads();  // the next replica reuses reduce_partials' shared memory
   }
 }
 
