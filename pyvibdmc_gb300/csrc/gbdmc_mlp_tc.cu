@@ -163,9 +163,12 @@ __device__ void load_weights(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
 }
 
 // Bias + SiLU of this thread's accumulator row, written as BF16 A row (KG = 16).
+// The 32-column chunks are a rolled loop: sixteen warps at different points of
+// the tile pipeline share the SM's instruction caches, and the fully unrolled
+// epilogues tripled the kernel's code.
 __device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow, const float* bias) {
   const int t = gp.lt;
-#pragma unroll
+#pragma unroll 1
   for (int c = 0; c < 4; ++c) {
     float r[32];
     tmem_ld32(trow + 32 * c, r);
@@ -224,7 +227,7 @@ __device__ __forceinline__ float forward_tile(TcSmemG<G>& sm, const Grp& gp, uin
   tc_fence_before();
   ok &= run_layer(gp, phase, sm.w3, 16);
   float e = 0.f;
-#pragma unroll
+#pragma unroll 1
   for (int c = 0; c < 4; ++c) {
     float r[32];
     tmem_ld32(trow + 32 * c, r);
