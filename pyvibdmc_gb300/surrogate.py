@@ -539,6 +539,10 @@ def _main(argv=None):
     ap.add_argument("--seeds", default="5", help="comma-separated DMC seeds (one run per seed and variant)")
     ap.add_argument("--compare", action="store_true",
                     help="also run without bias control and the FP64 analytic DMC; report ZPEs")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="run R replicas with N_r ~ U[1000, 65536] (seeded) instead of one of --walkers")
+    ap.add_argument("--imp-samp", dest="imp_samp", action="store_true",
+                    help="importance sampling with the dimer trial (dimer_gaussian_trial)")
     a = ap.parse_args(argv)
     from .potentials import water_dimer, WATER_DIMER_EQ
     from .engine import DMC_Sim
@@ -568,18 +572,25 @@ def _main(argv=None):
 
     seeds = [int(v) for v in a.seeds.split(",")]
     variants = [("nn", a.bias_control)] + ([("nn_uncorrected", 0.0)] if a.compare else [])
+    walkers = a.walkers
+    if a.replicas:
+        walkers = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=a.replicas)]
+    trial = None
+    if a.imp_samp:
+        from .imp_samp import dimer_gaussian_trial
+        trial = dimer_gaussian_trial()
     runs = {}
     for seed in seeds:
         for label, beta in variants:
-            nd = NNDMC(m, pot, a.walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps, seed=seed,
-                       audit_every=a.audit_every, bias_control=beta).init()
+            nd = NNDMC(m, pot, walkers, WATER_DIMER_EQ[None], masses, 10.0, a.steps, seed=seed,
+                       audit_every=a.audit_every, bias_control=beta, imp_samp=trial).init()
             us = timed(nd.run)
             runs.setdefault(label, []).append(dict(
-                seed=seed, us_per_step=us, audit=nd.audit(), population=int(nd.ctrl().n),
+                seed=seed, us_per_step=us, audit=nd.audit(), population=int(sum(c.n for c in nd.ctrls())),
                 zpe_cm=nd.zpe(start=start) if a.steps >= 40 else None))
             del nd
         if a.compare:
-            sim = DMC_Sim(num_walkers=a.walkers, num_timesteps=a.steps, equil_steps=10 ** 9,
+            sim = DMC_Sim(num_walkers=a.walkers, imp_samp=trial, num_timesteps=a.steps, equil_steps=10 ** 9,
                           atoms=["O", "H", "H"] * 2, masses=masses, delta_t=10.0, potential=pot,
                           start_structures=WATER_DIMER_EQ[None], seed=seed, write_files=False)
             sim._init_device()
