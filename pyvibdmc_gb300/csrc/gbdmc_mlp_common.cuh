@@ -47,14 +47,19 @@ __device__ __forceinline__ bool is_move_f32(const gbdmc_sim_t& S, float (&x)[18]
 #pragma unroll
   for (int k = 0; k < 18; ++k) y[k] = x[k] + (float)S.sigma[k / 3] * z[k] + (float)S.inv_mass[k / 3] * f[k] * dt;
   const float lpy = dimer_trial_log(y, S.trial.p, fy, d2y);
+  float h[6];  // 1 / (2 sigma_a^2), one division per atom
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const float sg = (float)S.sigma[a];
+    h[a] = 0.5f / (sg * sg);
+  }
   float expo = 0.f;
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
     const float im = (float)S.inv_mass[k / 3];
-    const float s2 = (float)(S.sigma[k / 3] * S.sigma[k / 3]);
     const float a = x[k] - y[k] - im * fy[k] * dt;
     const float b = y[k] - x[k] - im * f[k] * dt;
-    expo += (b * b - a * a) / (2.f * s2);
+    expo += (b * b - a * a) * h[k / 3];
   }
   const float met = expf(expo + 2.f * (lpy - lnpsi));
   const bool acc = (double)met > u;

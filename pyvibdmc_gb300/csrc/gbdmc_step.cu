@@ -229,14 +229,16 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
         y[k] = __dadd_rn(__dadd_rn(x[k], __dmul_rn(S.sigma[k / 3], z[k])), __dmul_rn(dx, dt));
       }
       const double psi_y = trial<TK, A>(y, S.trial, fy, sdy);
+      double h[A];  // 1 / (2 sigma_a^2), one division per atom
+#pragma unroll
+      for (int a = 0; a < A; ++a) h[a] = 0.5 / (S.sigma[a] * S.sigma[a]);
       double expo = 0.0;
 #pragma unroll
       for (int k = 0; k < 3 * A; ++k) {
         const double im = S.inv_mass[k / 3];
-        const double s2 = S.sigma[k / 3] * S.sigma[k / 3];
         const double a = x[k] - y[k] - im * fy[k] * dt;
         const double b = y[k] - x[k] - im * fx[k] * dt;
-        expo += (b * b - a * a) / (2.0 * s2);
+        expo += (b * b - a * a) * h[k / 3];
       }
       const double rr = psi_y / psi_x;
       double met = exp(expo) * (rr * rr);
