@@ -582,9 +582,9 @@ def run_e2e(sim, L, dev, steps):
     """The walkers in page-locked host memory, stepped through the public
     host-resident API (``pyvibdmc_gb300.HostWalkers`` ->
     ``gbdmc_sim_step_host``): every step the move kernel reads the walkers
-    from host memory, the compaction kernel writes the branched population,
-    its potentials and ancestor ids back to host memory, the control block is
-    copied back, and the host waits for the step and reads N'."""
+    from host memory, the branching kernel writes the branched population,
+    its potentials, ancestor ids and the control block back to host memory,
+    and the host waits for the step and reads N'."""
     import torch
     import pyvibdmc_gb300 as pg
     from pyvibdmc_gb300 import _capi
@@ -598,7 +598,7 @@ def run_e2e(sim, L, dev, steps):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        h2d += A3 * sim.capacity * 8 + 4 * n  # coordinates of every slot (speculative gather) + ancestor ids
+        h2d += (A3 * 8 + 4) * n  # coordinates and ancestor ids of the N walkers
         total += n
         n = hw.step()
         d2h += (A3 * 8 + 8 + 4) * n + C.sizeof(_capi.Ctrl)
@@ -606,9 +606,10 @@ def run_e2e(sim, L, dev, steps):
     hw.close()
     return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
             "d2h_bytes_per_step": d2h // steps, "steps": steps,
-            "path": "walkers in page-locked host memory; per step one gbdmc_sim_step_host call (C ABI): move "
-                    "kernel reads the walkers from host memory, branch, compaction kernel writes the branched "
-                    "walkers, V and ancestor ids to host memory, control block copied back; host sync per step"}
+            "path": "walkers in page-locked host memory; per step one gbdmc_sim_step_host call (C ABI, "
+                    "graph-replayed): the move kernel reads the N walkers from host memory, the branching kernel "
+                    "writes the branched walkers, V, ancestor ids and the control block to host memory; host "
+                    "sync per step"}
 
 
 def run_e2e_staged(sim, L, dev, steps):

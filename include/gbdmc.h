@@ -242,10 +242,14 @@ int gbdmc_walkers_compact(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, i
  * walkers [3A][sim->ld] -- x and v, plus who / f, psi, ke / w as the
  * configuration uses them, no idx -- in memory from cudaHostAlloc or
  * cudaHostRegister; the kernels read and write it directly over the host
- * link (no staging copies).  `work` is a device walker set with idx.  The
- * step runs host -> work, the compaction work -> host, and the control block
- * is copied to ctrl_host (page-locked).  After the stream is synchronised,
- * host holds the ctrl_host->n walkers of the next step in columns 0..n-1. */
+ * link (no staging copies).  `work` is a device walker set.  The step runs
+ * host -> work; with discrete weighting the branching pass then writes the
+ * branched walkers (each copied c times, the np.repeat order) and the
+ * control block straight into host and ctrl_host (page-locked); continuous
+ * weighting compacts work -> host and copies the control block.  After the
+ * stream is synchronised, host holds the ctrl_host->n walkers of the next
+ * step in columns 0..n-1; after a failed step (ctrl_host->status set) it
+ * still holds the walkers of before the step. */
 int gbdmc_sim_step_host(const gbdmc_sim_t* sim, const gbdmc_walkers_t* host, const gbdmc_walkers_t* work,
                         gbdmc_ctrl_t* ctrl_dev, gbdmc_ctrl_t* ctrl_host, void* scratch_dev,
                         const gbdmc_noise_t* noise, void* stream);

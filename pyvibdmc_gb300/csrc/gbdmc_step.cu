@@ -108,18 +108,24 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
     gbdmc_ctrl_t* ctrl = ctrls + r;
     const int64_t base = T.off[r];
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
-    // The gather is issued before the control block arrives (its loads overlap):
-    // slot i < cap lies inside the replica and the index is clamped into it, so
-    // the walkers of slots i >= N are read harmlessly and then ignored.
+    // A gather through the index is issued before the control block arrives
+    // (their loads overlap): slot i < cap lies inside the replica and the index
+    // is clamped into it, so the walkers of slots i >= N are read harmlessly
+    // and then ignored.  Compact sources (possibly host memory) are read after
+    // N is known, walkers i < N only.
     double x[3 * A];
     int64_t src = base + i;
-    if (i < T.cap[r]) {
-      if (in.idx) src = base + min(max((int64_t)__ldg(in.idx + base + i), (int64_t)0), T.cap[r] - 1);
+    if (in.idx && i < T.cap[r]) {
+      src = base + min(max((int64_t)__ldg(in.idx + base + i), (int64_t)0), T.cap[r] - 1);
 #pragma unroll
       for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
     }
     if (*(volatile int*)&ctrl->status) continue;  // replica stopped by a previous kernel
     const long long n = ctrl->n;
+    if (!in.idx && i < n) {
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
+    }
     const long long step = ctrl->step;
     const double vref = ctrl->vref;
     Partial p = partial_zero();
@@ -336,6 +342,71 @@ __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepT
     for (int q = 0; q < c; ++q)
       if (dest + q < cap) idx[base + dest + q] = (int32_t)i;
   }
+}
+
+// Branching straight into compact walkers, for the host-resident step:
+// walker i (pre-branch, in `in`) is copied c_i times to slots prefix + scan
+// .. + c_i of `out` -- the np.repeat(arange(N), counts) order of
+// pyvibdmc.py:417-430 -- so no gather index and no compaction pass are needed;
+// block 0 then copies the control block to ctrl_out.  A replica whose step
+// failed (status set) is not written: `out` keeps the walkers it had.
+template <int A, bool IS>
+__global__ void __launch_bounds__(kMaxTPB) k_branch_scatter(const __grid_constant__ RepTable T, int64_t ld,
+                                                             const gbdmc_walkers_t in, gbdmc_walkers_t out,
+                                                             const gbdmc_ctrl_t* ctrls, const long long* prefix,
+                                                             const int* counts, gbdmc_ctrl_t* ctrl_out) {
+  pdl_wait();
+  const int ntile = T.tile_off[T.nrep];
+  __shared__ int wsum[kMaxTPB / 32];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    const gbdmc_ctrl_t* ctrl = ctrls + r;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    const int64_t base = T.off[r];
+    const long long cap = T.cap[r];
+    const int c_raw = i < cap ? counts[base + i] : 0;
+    const long long pre = prefix[tile];
+    if (*(volatile const int*)&ctrl->status) continue;  // block-uniform: not written by this kernel
+    const long long n = ctrl->n_prev;
+    const int c = i < n ? c_raw : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int inc = warp_incl_scan(c);
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    int off = 0;
+    for (int w = 0; w < wid; ++w) off += wsum[w];
+    __syncthreads();
+    if (c > 0) {
+      const int64_t src = base + i;
+      const long long dest = pre + off + inc - c;
+      double x[3 * A], f[3 * A];
+#pragma unroll
+      for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
+      if constexpr (IS) {
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) f[k] = in.f[k * ld + src];
+      }
+      const double v = in.v[src];
+      const int32_t who = in.who ? in.who[src] : 0;
+      const double psi = IS ? in.psi[src] : 0.0, ke = IS ? in.ke[src] : 0.0;
+      for (int q = 0; q < c; ++q) {
+        if (dest + q >= cap) break;
+        const int64_t d = base + dest + q;
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) out.x[k * ld + d] = x[k];
+        out.v[d] = v;
+        if (out.who) out.who[d] = who;
+        if constexpr (IS) {
+#pragma unroll
+          for (int k = 0; k < 3 * A; ++k) out.f[k * ld + d] = f[k];
+          out.psi[d] = psi;
+          out.ke[d] = ke;
+        }
+      }
+    }
+  }
+  if (ctrl_out && blockIdx.x == 0 && threadIdx.x < (int)(sizeof(gbdmc_ctrl_t) / 8))
+    reinterpret_cast<long long*>(ctrl_out)[threadIdx.x] = reinterpret_cast<const long long*>(ctrls)[threadIdx.x];
 }
 
 // ---------------------------------------------------------- compaction
@@ -680,10 +751,28 @@ static int run_init(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers
   return check_launch("gbdmc init");
 }
 
+// Where a discrete branching pass puts its result: the gather index of dst
+// (out == nullptr) or compact walkers in `out` plus a copy of the control
+// block in `ctrl_out` (the host-resident step).
+struct BranchTarget {
+  const gbdmc_walkers_t* out;
+  gbdmc_ctrl_t* ctrl_out;
+};
+
+template <int A, bool IS>
+static void launch_branch_to(const RepTable& T, const gbdmc_sim_t& S, const gbdmc_walkers_t& dst, gbdmc_ctrl_t* ctrl,
+                             const ScratchLayout& L, const BranchTarget& bt, cudaStream_t s) {
+  if (bt.out)
+    launch_pdl(k_branch_scatter<A, IS>, grid_for(T), T.tpb, s, T, S.ld, dst, *bt.out, ctrl, L.prefix, L.counts,
+               bt.ctrl_out);
+  else
+    launch_pdl(k_branch, grid_for(T), T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
+}
+
 template <int PK, int A, int TK, int NM, bool STATS>
 static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& src,
                         const gbdmc_walkers_t& dst, gbdmc_ctrl_t* ctrl, const ScratchLayout& L,
-                        const gbdmc_noise_t& nz, cudaStream_t s) {
+                        const gbdmc_noise_t& nz, const BranchTarget& bt, cudaStream_t s) {
   const int G = grid_for(T);
   constexpr bool IS = TK != GBDMC_TRIAL_NONE;
   const bool prof = g_prof.on && g_prof.count < ProfState::kSlots;
@@ -695,7 +784,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
       // its fp64 pipes need); k_branch may be launched while k_move finishes
       k_move<PK, A, NM, true, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      launch_pdl(k_branch, G, T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
+      launch_branch_to<A, false>(T, S, dst, ctrl, L, bt, s);
     } else {
       k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
@@ -707,7 +796,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     if (S.weighting == GBDMC_DISCRETE) {
       k_count<NM, false><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
-      launch_pdl(k_branch, G, T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
+      launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {
       k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
     }
@@ -720,15 +809,16 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
 
 template <int PK, int A, int TK>
 static int run_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& src, const gbdmc_walkers_t& dst,
-                    gbdmc_ctrl_t* ctrl, const ScratchLayout& L, const gbdmc_noise_t& nz, cudaStream_t s) {
+                    gbdmc_ctrl_t* ctrl, const ScratchLayout& L, const gbdmc_noise_t& nz, const BranchTarget& bt,
+                    cudaStream_t s) {
   const bool stats = S.hist.vmin || S.hist.vmax || S.hist.vmean;
-#define GBDMC_NM(nm)                                                     \
-  if (S.noise_mode == nm) {                                              \
-    if (stats)                                                           \
-      launch_step<PK, A, TK, nm, true>(S, T, src, dst, ctrl, L, nz, s);  \
-    else                                                                 \
-      launch_step<PK, A, TK, nm, false>(S, T, src, dst, ctrl, L, nz, s); \
-    return check_launch("gbdmc step");                                   \
+#define GBDMC_NM(nm)                                                         \
+  if (S.noise_mode == nm) {                                                  \
+    if (stats)                                                               \
+      launch_step<PK, A, TK, nm, true>(S, T, src, dst, ctrl, L, nz, bt, s);  \
+    else                                                                     \
+      launch_step<PK, A, TK, nm, false>(S, T, src, dst, ctrl, L, nz, bt, s); \
+    return check_launch("gbdmc step");                                       \
   }
   GBDMC_NM(GBDMC_NOISE_PHILOX32)
   GBDMC_NM(GBDMC_NOISE_PHILOX64)
@@ -769,10 +859,11 @@ struct StepF {
   gbdmc_ctrl_t* ctrl;
   const ScratchLayout& L;
   const gbdmc_noise_t& nz;
+  const BranchTarget& bt;
   cudaStream_t s;
   template <int PK, int A, int TK>
   int operator()() {
-    return run_step<PK, A, TK>(S, T, src, dst, ctrl, L, nz, s);
+    return run_step<PK, A, TK>(S, T, src, dst, ctrl, L, nz, bt, s);
   }
 };
 
@@ -836,7 +927,7 @@ static int validate(const gbdmc_sim_t* S, const gbdmc_walkers_t* W, const void* 
 
 static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep, const gbdmc_walkers_t* src,
                        const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl, void* scratch, const gbdmc_noise_t* noise,
-                       void* stream, const char* what) {
+                       void* stream, const char* what, const BranchTarget& bt = BranchTarget{nullptr, nullptr}) {
   int rc = validate(S, src, ctrl, scratch, what);
   if (rc) return rc;
   rc = validate(S, dst, ctrl, scratch, what);
@@ -845,7 +936,7 @@ static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
     set_error("%s: src and dst must use different arrays", what);
     return GBDMC_ERR_ARG;
   }
-  if (S->weighting == GBDMC_DISCRETE && !dst->idx) {
+  if (S->weighting == GBDMC_DISCRETE && !dst->idx && !bt.out) {
     set_error("%s: discrete weighting writes the branch index: dst->idx is required", what);
     return GBDMC_ERR_ARG;
   }
@@ -866,7 +957,7 @@ static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
   rc = build_table(*S, reps, nrep, T, what);
   if (rc) return rc;
   const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(reps, nrep));
-  StepF f{*S, T, *src, *dst, ctrl, L, nz, (cudaStream_t)stream};
+  StepF f{*S, T, *src, *dst, ctrl, L, nz, bt, (cudaStream_t)stream};
   return dispatch_system(*S, what, f);
 }
 
@@ -1020,6 +1111,21 @@ extern "C" int gbdmc_sim_step_host(const gbdmc_sim_t* S, const gbdmc_walkers_t* 
   h.psi = (double*)d[4];
   h.ke = (double*)d[5];
   h.w = (double*)d[6];
+  if (S->weighting == GBDMC_DISCRETE) {
+    // the branching pass writes the branched walkers and the control block straight into host memory
+    void* ch;
+    if (!host_alias(ctrl_host, &ch)) {
+      set_error("gbdmc_sim_step_host: ctrl_host is not page-locked host memory");
+      return GBDMC_ERR_ARG;
+    }
+    if (S->n0 < 1) {
+      set_error("gbdmc_sim_step_host: n0 must be >= 1");
+      return GBDMC_ERR_ARG;
+    }
+    const gbdmc_replica_t r = single_replica(S);
+    return step_common(S, &r, 1, &h, work, ctrl, scratch, noise, stream, "gbdmc_sim_step_host",
+                       BranchTarget{&h, (gbdmc_ctrl_t*)ch});
+  }
   int rc = gbdmc_sim_step(S, &h, work, ctrl, scratch, noise, stream);
   if (rc) return rc;
   rc = gbdmc_walkers_compact(S, nullptr, 0, work, &h, ctrl, stream);
