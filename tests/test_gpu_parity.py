@@ -382,3 +382,56 @@ def test_is_and_plain_converge_at_small_time_step():
     d = z["is"][0] - z["plain"][0]
     err = float(np.hypot(z["is"][1], z["plain"][1]))
     assert abs(d) < 1.0 + 4.0 * err, (z, d, err)
+
+
+def test_full_size_workload_step_properties():
+    """The benchmark workload at its full size (water, 20000 walkers, Philox32, dt = 10),
+    three consecutive steps, checked through size-independent properties: every deviate
+    equals the oracle's Philox restatement (8 fp32 ulps), every branch count equals
+    floor(w) + [u < w - floor(w)] with the oracle's uniform, the branch index is
+    np.repeat(arange(N), counts), and vref equals the mean potential of the branched
+    population minus the population term (1e-12 relative)."""
+    from oracle.philox_oracle import philox_normals, philox_branch_uniform
+    _, m = oracle.h2o_config()
+    n, seed, dt = 20000, 20240611, 10.0
+    sim = pg.DMC_Sim(num_walkers=n, num_timesteps=10, equil_steps=1000, atoms=["O", "H", "H"], masses=m,
+                     delta_t=dt, potential=pg.h2o_local_mode(), start_structures=geoms(n, seed=19, scale=0.05),
+                     seed=seed, rng="philox32", write_files=False)
+    sim._init_device()
+    sig = np.repeat([sim._sim.sigma[a] for a in range(3)], 3)[:, None]
+    alpha = 1.0 / (2.0 * dt)
+    prev = sim._bufs[sim._cur]["x"][:, :n].cpu().numpy()
+    for step in range(3):
+        c = sim._read_ctrl()
+        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
+        b = sim._bufs[sim._cur]
+        moved = b["x"][:, :n].cpu().numpy()
+        z, _ = philox_normals(seed, step, np.arange(n), 9, "philox32")
+        np.testing.assert_allclose((moved - prev) / sig, z, rtol=1e-6, atol=1e-6)
+        v = b["v"][:n].cpu().numpy()
+        w = np.exp(-(v - c.vref) * dt)
+        u = philox_branch_uniform(seed, step, np.arange(n), 9, "philox32")
+        counts = np.floor(w).astype(np.int64) + (u < w - np.floor(w))
+        c2 = sim._read_ctrl()
+        n2 = int(c2.n)
+        idx = b["idx"][:n2].cpu().numpy()
+        np.testing.assert_array_equal(idx, np.repeat(np.arange(n), counts))
+        vref = v[idx].mean() - alpha * (n2 - 20000) / 20000
+        np.testing.assert_allclose(c2.vref, vref, rtol=1e-12, atol=0)
+        n, prev = n2, moved[:, idx]
+
+
+def test_host_resident_step_failure_keeps_the_host_walkers():
+    """A step that trips the weight guard raises the reference's ValueError and leaves
+    the host walkers as they were before the step."""
+    ho = oracle.ho_config()
+    x0 = np.zeros((100, 1, 3))
+    x0[50:, 0, 0] = np.sqrt(2 * 2.0 / ho["k"])  # V = 2 Eh for half the walkers -> w ~ e^10
+    sim = pg.DMC_Sim(num_walkers=100, num_timesteps=5, equil_steps=1000, atoms=["H"], masses=ho["masses"],
+                     delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=3, write_files=False)
+    sim._init_device()
+    hw = pg.HostWalkers(sim)
+    before = hw.host["x"][:, :100].clone()
+    with pytest.raises(ValueError, match="Massive walker"):
+        hw.step()
+    assert torch.equal(hw.host["x"][:, :100], before)
