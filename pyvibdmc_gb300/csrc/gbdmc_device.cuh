@@ -57,10 +57,13 @@ struct Rng {
     return v;
   }
   // uniform in [0,1) with 53 random bits
-  __device__ __forceinline__ double uniform53() {
+  // the 53 random bits m of uniform53() = m * 2^-53
+  __device__ __forceinline__ uint64_t bits53() {
     const uint64_t hi = next32(), lo = next32();
-    return (double)((hi << 21) | (lo >> 11)) * 0x1.0p-53;
+    return (hi << 21) | (lo >> 11);
   }
+  // uniform in [0,1) with 53 random bits
+  __device__ __forceinline__ double uniform53() { return (double)bits53() * 0x1.0p-53; }
   // two standard normals, Box-Muller in fp32 (u1 in (0,1] from 32 bits)
   __device__ __forceinline__ void normal2_f32(float& z0, float& z1) {
     const uint32_t a = next32(), b = next32();
@@ -83,6 +86,22 @@ struct Rng {
     z1 = rad * s;
   }
 };
+
+// m * 2^-53 < f for the 53-bit integer m of Rng::bits53 and a float f, with
+// integer operations only: the exact value of (double)uniform53() < (double)f.
+// For 0 < f < 1, f = F * 2^(e - 150) with F the 24-bit significand and e the
+// biased exponent, so m * 2^-53 < f  <=>  m * 2^(97 - e) < F.
+__device__ __forceinline__ bool u53_below(uint64_t m, float f) {
+  if (!(f > 0.f)) return false;  // uniforms are >= 0; NaN compares false
+  if (f >= 1.f) return true;     // uniforms are < 1
+  const uint32_t b = __float_as_uint(f);
+  const int e = (int)(b >> 23);
+  const uint64_t F = e ? ((b & 0x7FFFFFu) | 0x800000u) : b;
+  const int s = (e ? e : 1) - 97;
+  if (s >= 0) return m < (F << s);                       // s <= 29 since f < 1: F << s < 2^53
+  if (m >= (1ull << 24) || -s >= 24) return m == 0;      // otherwise m * 2^-s >= 2^24 > F
+  return (m << -s) < F;
+}
 
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialisation may start while the previous kernel of its stream is still
@@ -343,14 +362,15 @@ __device__ __forceinline__ double trial_ho(const double (&x)[3 * A], const doubl
 // h2o_trial_terms adds the water's d ln psi / dx_k to f[] and its
 // d2 ln psi / dx_k^2 to t[] for the atoms (o, h1, h2) of x, and returns the
 // exponent -1/2 sum_q alpha_q (q - q_e)^2.  T is float (surrogate walkers)
-// or double.
+// or double; the parameters p come as double, or as their fp32 copies for
+// float walkers (no per-walker conversion).
 template <typename T>
 __device__ __forceinline__ T rsqrt_guard_t(T y) {
   return y > T(0) ? rsqrt(y) : T(0);
 }
 
-template <typename T, int N>
-__device__ __forceinline__ T h2o_trial_terms(const T (&x)[N], const double* p, int o, int h1, int h2, T (&f)[N],
+template <typename T, int N, typename P>
+__device__ __forceinline__ T h2o_trial_terms(const T (&x)[N], const P* p, int o, int h1, int h2, T (&f)[N],
                                              T (&t)[N]) {
   const T a1 = (T)p[0], a2 = (T)p[1], ath = (T)p[2], r1e = (T)p[3], r2e = (T)p[4], the = (T)p[5];
   T v1[3], v2[3];
@@ -422,8 +442,8 @@ __device__ __forceinline__ double trial_h2o(const double (&x)[3 * A], const doub
 // p = alpha_r1, alpha_r2, alpha_th, r1e, r2e, theta_e, alpha_R, R_e.
 // Returns ln psi without the normalisation; d1 = d ln psi/dx,
 // d2 = (d2 psi/dx2)/psi = d1^2 + d2 ln psi/dx2 per Cartesian component.
-template <typename T>
-__device__ __forceinline__ T dimer_trial_log(const T (&x)[18], const double* p, T (&d1)[18], T (&d2)[18]) {
+template <typename T, typename P>
+__device__ __forceinline__ T dimer_trial_log(const T (&x)[18], const P* p, T (&d1)[18], T (&d2)[18]) {
   T t[18];
 #pragma unroll
   for (int k = 0; k < 18; ++k) d1[k] = t[k] = T(0);

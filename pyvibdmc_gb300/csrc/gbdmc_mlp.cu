@@ -538,70 +538,94 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
 // in a fixed shuffle order) -- short lists, where the latency of one walker's
 // PES matters; LANES = 1: one walker per thread -- long lists (large batches),
 // where the FP64 pipe's throughput matters and 8 lanes would issue 6x the FP64
-// warp instructions.  The replicas are processed side by side: the grid is cut
-// into units of (replica, share of that replica's list), so a batch of many
-// replicas does not walk its replicas one after another.  Audited differences
-// V_nn - V_analytic are summed per block and added to audit[0..2] (fallbacks
-// to audit[3]) with one atomic each per block.
+// warp instructions.  The lists of all replicas are walked as one: every
+// block scans the replicas' list lengths into shared memory and the grid
+// strides over the concatenated list, so each SM gets the same share of the
+// fp64 work however the replicas' lists differ in length.  Audited
+// differences V_nn - V_analytic are summed per block and added to
+// audit[0..2] (fallbacks to audit[3]) with one atomic each per block.
 template <int LANES>
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     gbdmc_ctrl_t* ctrls, const int* list,
                                                     const unsigned char* flags, double* audit, float beta) {
+  static_assert(GBDMC_MAX_REPLICAS <= 64, "two replicas per lane in the list-length scan");
+  __shared__ long long pre[GBDMC_MAX_REPLICAS + 1];  // exclusive prefix of the list lengths
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
   const int part = threadIdx.x & (LANES - 1);
   const int nrep = T.nrep;
-  const int per_rep = gridDim.x >= (unsigned)nrep ? (int)(gridDim.x / nrep) : 1;  // blocks per replica
-  const int units = nrep * per_rep;
   const int wpb = blockDim.x >> 5;
-  double s_n = 0.0, s_d = 0.0, s_d2 = 0.0, s_fb = 0.0;
-  for (int u = blockIdx.x; u < units; u += gridDim.x) {
-    const int r = u / per_rep, sub = u % per_rep;
-    const gbdmc_ctrl_t* ctrl = ctrls + r;
-    if (*(volatile const int*)&ctrl->status) continue;
-    long long cnt = *(volatile const long long*)&ctrl->reserved[2];
-    if (cnt > T.cap[r]) cnt = T.cap[r];
-    const int64_t base = T.off[r];
-    // a warp takes 32/LANES walkers per iteration (lanes LANES*k .. LANES*k+LANES-1 ->
-    // walker jb + k); the loop bound is warp-uniform, so the shuffles see all 32 lanes
-    constexpr int WPW = 32 / LANES;  // walkers per warp and iteration
-    const long long gw = (long long)sub * wpb + (threadIdx.x >> 5);
-    const long long nw = (long long)per_rep * wpb;
-    for (long long jb = WPW * gw; jb < cnt; jb += WPW * nw) {
-      const long long j = jb + ((threadIdx.x & 31) / LANES);
-      const bool live = j < cnt;
-      double v = 0.0;
-      int64_t dst = 0;
-      if (live) {
-        dst = base + list[base + j];
-        double xd[18];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    long long c[2] = {0, 0};
 #pragma unroll
-        for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
-        if constexpr (LANES == 1) {
-          double gd[18];
-          v = pes_dimer<false>(xd, S.pes.p, gd);
-        } else {
-          v = dimer_part(xd, S.pes.p, part);
-        }
+    for (int h = 0; h < 2; ++h) {
+      const int r = lane + 32 * h;
+      if (r < nrep && *(volatile const int*)&ctrls[r].status == 0) {
+        const long long m = *(volatile const long long*)&ctrls[r].reserved[2];
+        c[h] = m < T.cap[r] ? m : T.cap[r];
       }
-      if constexpr (LANES == 8) {
-        v += __shfl_xor_sync(0xffffffffu, v, 4);
-        v += __shfl_xor_sync(0xffffffffu, v, 2);
-        v += __shfl_xor_sync(0xffffffffu, v, 1);
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, c[h], o);
+        if (lane >= o) c[h] += t;
       }
-      if (live && part == 0) {
-        const unsigned char fl = flags[dst];
-        const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
-        if (fl & 2) {
-          const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
-          s_n += 1.0;
-          s_d += d;
-          s_d2 += d * d;
-        }
-        if (fl & 1) s_fb += 1.0;
-        out.v[dst] = v + ke;
+    }
+    const long long lo_total = __shfl_sync(0xffffffffu, c[0], 31);
+    if (lane == 0) pre[0] = 0;
+    if (lane < nrep) pre[lane + 1] = c[0];
+    if (lane + 32 < nrep) pre[lane + 33] = c[1] + lo_total;
+  }
+  __syncthreads();
+  const long long total = pre[nrep];
+  double s_n = 0.0, s_d = 0.0, s_d2 = 0.0, s_fb = 0.0;
+  // a warp takes 32/LANES walkers per iteration (lanes LANES*k .. LANES*k+LANES-1 ->
+  // walker jb + k); the loop bound is warp-uniform, so the shuffles see all 32 lanes
+  // (warp w of block b takes chunk w * gridDim + b: a short list still spreads over every SM)
+  constexpr int WPW = 32 / LANES;  // walkers per warp and iteration
+  const long long gw = (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const long long nw = (long long)gridDim.x * wpb;
+  for (long long jb = WPW * gw; jb < total; jb += WPW * nw) {
+    const long long j = jb + ((threadIdx.x & 31) / LANES);
+    const bool live = j < total;
+    double v = 0.0;
+    int64_t dst = 0;
+    if (live) {
+      int r = 0, hi = nrep;  // largest r with pre[r] <= j (then j < pre[r + 1])
+      while (hi - r > 1) {
+        const int mid = (r + hi) >> 1;
+        if (pre[mid] <= j) r = mid;
+        else hi = mid;
       }
+      const int64_t base = T.off[r];
+      dst = base + list[base + (j - pre[r])];
+      double xd[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
+      if constexpr (LANES == 1) {
+        double gd[18];
+        v = pes_dimer<false>(xd, S.pes.p, gd);
+      } else {
+        v = dimer_part(xd, S.pes.p, part);
+      }
+    }
+    if constexpr (LANES == 8) {
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+    }
+    if (live && part == 0) {
+      const unsigned char fl = flags[dst];
+      const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
+      if (fl & 2) {
+        const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
+        s_n += 1.0;
+        s_d += d;
+        s_d2 += d * d;
+      }
+      if (fl & 1) s_fb += 1.0;
+      out.v[dst] = v + ke;
     }
   }
   {  // block sums of the audit statistics, one atomic per quantity
@@ -666,7 +690,8 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
 __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_sim_t S,
                                                    const __grid_constant__ RepTable T,
                                                    const __grid_constant__ gbdmc_mlp_t net, gbdmc_walkers_f32_t W,
-                                                   gbdmc_ctrl_t* ctrls, Partial* part) {
+                                                   gbdmc_ctrl_t* ctrls, Partial* part,
+                                                   const __grid_constant__ StepF32 P) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
   load_net(sm, net);
@@ -705,8 +730,8 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
         float xs[18], fx[18], d2[18];
 #pragma unroll
         for (int k = 0; k < 18; ++k) xs[k] = W.x[k * ld + base + i];
-        const float lp = dimer_trial_log(xs, S.trial.p, fx, d2);
-        const float ke = local_ke_f32(S, d2);
+        const float lp = dimer_trial_log(xs, P.trial, fx, d2);
+        const float ke = local_ke_f32(P, d2);
 #pragma unroll
         for (int k = 0; k < 18; ++k) W.f[k * ld + base + i] = fx[k];
         W.lnpsi[base + i] = lp;
@@ -953,7 +978,7 @@ extern "C" int gbdmc_mlp_batch_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
   int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();
-  k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part);
+  k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part, step_f32(*S));
   return check_launch("gbdmc_mlp_batch_init");
 }
 

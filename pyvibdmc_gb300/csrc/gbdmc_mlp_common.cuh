@@ -10,59 +10,93 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// sigmoid(z) = (1 + tanh(z/2)) / 2 with the single-instruction tanh.approx.f32
-// (|error| ~ 1e-3 relative, below the bf16 rounding of the activations).
+// SiLU through the single-instruction tanh.approx.f32 (|error| ~ 1e-3
+// relative, below the bf16 rounding of the activations):
+//   silu(z) = z (1 + tanh(z/2)) / 2 = h + h tanh(h),  h = z/2.
+// silu_half takes h; the tcgen05 path pre-scales its hidden-layer weights and
+// biases by 1/2 (exact in bf16 / fp32), so its accumulator already holds h.
 __device__ __forceinline__ float tanh_approx(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
-__device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
+__device__ __forceinline__ float silu_half(float h) { return fmaf(h, tanh_approx(h), h); }
+__device__ __forceinline__ float silu(float z) { return silu_half(0.5f * z); }
+
+// fp32 copies of the step parameters that the surrogate kernels use,
+// converted once on the host (round to nearest, the device conversion), so
+// that the per-walker code issues no fp64 conversion.
+struct StepF32 {
+  float sigma[6];     // sqrt(dt / m_a)
+  float inv_mass[6];  // 1 / m_a
+  float h[6];         // 1 / (2 sigma_a^2), fp32 arithmetic on the fp32 sigma
+  float dt;
+  float trial[8];     // dimer trial parameters (gbdmc_trial_t.p[0..7])
+};
+
+inline StepF32 step_f32(const gbdmc_sim_t& S) {
+  StepF32 P{};
+  for (int a = 0; a < 6; ++a) {
+    P.sigma[a] = (float)S.sigma[a];
+    P.inv_mass[a] = (float)S.inv_mass[a];
+    const float sg = P.sigma[a];
+    P.h[a] = 0.5f / (sg * sg);
+  }
+  P.dt = (float)S.dt;
+  for (int k = 0; k < 8; ++k) P.trial[k] = (float)S.trial.p[k];
+  return P;
+}
 
 // -1/2 sum_d sum_a (1/m_a) (d2 psi/dx2)/psi in fp32, the summation order of
 // local_ke (imp_samp.py:49-53).
-__device__ __forceinline__ float local_ke_f32(const gbdmc_sim_t& S, const float (&d2)[18]) {
+__device__ __forceinline__ float local_ke_f32(const StepF32& P, const float (&d2)[18]) {
   float s = 0.f;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     float t = 0.f;
 #pragma unroll
-    for (int a = 0; a < 6; ++a) t += (float)S.inv_mass[a] * d2[3 * a + d];
+    for (int a = 0; a < 6; ++a) t += P.inv_mass[a] * d2[3 * a + d];
     s += t;
   }
   return -0.5f * s;
 }
+
+// Metropolis decisions met > u: the Philox uniform as its 53-bit integer
+// (integer pipes) or an injected fp64 uniform.
+struct AcceptU53 {
+  uint64_t m;
+  __device__ __forceinline__ bool operator()(float met) const { return u53_below(m, met); }
+};
+struct AcceptF64 {
+  double u;
+  __device__ __forceinline__ bool operator()(float met) const { return (double)met > u; }
+};
 
 // Importance-sampled move of one fp32 dimer walker (pyvibdmc.py:549-612 with
 // ImpSamp.metropolis, imp_samp.py:28-47): proposal y = x + sigma z + (f_x/m) dt,
 // trial at y, acceptance min(1, G(y->x)/G(x->y) (psi_y/psi_x)^2) with the
 // psi ratio folded into one exponent through ln psi.  On return x, f, lnpsi
 // and ke hold the walker's state after the Metropolis test; returns whether
-// the proposal was accepted.  u is the acceptance uniform.
-__device__ __forceinline__ bool is_move_f32(const gbdmc_sim_t& S, float (&x)[18], float (&f)[18], float& lnpsi,
-                                            float& ke, const float (&z)[18], double u) {
-  const float dt = (float)S.dt;
+// the proposal was accepted.
+template <typename Acc>
+__device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], float (&f)[18], float& lnpsi,
+                                            float& ke, const float (&z)[18], const Acc& accept) {
+  const float dt = P.dt;
   float y[18], fy[18], d2y[18];
 #pragma unroll
-  for (int k = 0; k < 18; ++k) y[k] = x[k] + (float)S.sigma[k / 3] * z[k] + (float)S.inv_mass[k / 3] * f[k] * dt;
-  const float lpy = dimer_trial_log(y, S.trial.p, fy, d2y);
-  float h[6];  // 1 / (2 sigma_a^2), one division per atom
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    const float sg = (float)S.sigma[a];
-    h[a] = 0.5f / (sg * sg);
-  }
+  for (int k = 0; k < 18; ++k) y[k] = x[k] + P.sigma[k / 3] * z[k] + P.inv_mass[k / 3] * f[k] * dt;
+  const float lpy = dimer_trial_log(y, P.trial, fy, d2y);
   float expo = 0.f;
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
-    const float im = (float)S.inv_mass[k / 3];
+    const float im = P.inv_mass[k / 3];
     const float a = x[k] - y[k] - im * fy[k] * dt;
     const float b = y[k] - x[k] - im * f[k] * dt;
-    expo += (b * b - a * a) * h[k / 3];
+    expo += (b * b - a * a) * P.h[k / 3];
   }
   const float met = expf(expo + 2.f * (lpy - lnpsi));
-  const bool acc = (double)met > u;
+  const bool acc = accept(met);
   if (acc) {
 #pragma unroll
     for (int k = 0; k < 18; ++k) {
@@ -70,7 +104,7 @@ __device__ __forceinline__ bool is_move_f32(const gbdmc_sim_t& S, float (&x)[18]
       f[k] = fy[k];
     }
     lnpsi = lpy;
-    ke = local_ke_f32(S, d2y);
+    ke = local_ke_f32(P, d2y);
   }
   return acc;
 }

@@ -139,30 +139,46 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32]) {
   for (int j = 0; j < 32; ++j) r[j] = __uint_as_float(u[j]);
 }
 
+// 8 bf16 weights times 1/2 (exact: a power of two on normal bf16 values)
+__device__ __forceinline__ uint4 half_bf16x8(uint4 v) {
+  const __nv_bfloat162 h = __float2bfloat162_rn(0.5f);
+  uint32_t* w = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w[k]);
+    b = __hmul2(b, h);
+    w[k] = *reinterpret_cast<uint32_t*>(&b);
+  }
+  return v;
+}
+
+// The hidden layers' weights and biases are stored halved, so that each
+// accumulator row plus bias is h = z/2 and the epilogue is silu_half(h).
 template <int G>
 __device__ void load_weights(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
   // Wt is n-major [128][K] in global; 16-byte chunks = 8 consecutive k of one row n
   for (int c = threadIdx.x; c < kN * 2; c += blockDim.x) {
     const int n = c >> 1, kg = c & 1;
     *reinterpret_cast<uint4*>(sm.w1 + canon_off(n, 8 * kg, 2)) =
-        __ldg(reinterpret_cast<const uint4*>(net.w1t + n * 16 + 8 * kg));
+        half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w1t + n * 16 + 8 * kg)));
   }
   for (int c = threadIdx.x; c < kN * 16; c += blockDim.x) {
     const int n = c >> 4, kg = c & 15;
     *reinterpret_cast<uint4*>(sm.w2 + canon_off(n, 8 * kg, 16)) =
-        __ldg(reinterpret_cast<const uint4*>(net.w2t + n * kN + 8 * kg));
+        half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w2t + n * kN + 8 * kg)));
     *reinterpret_cast<uint4*>(sm.w3 + canon_off(n, 8 * kg, 16)) =
-        __ldg(reinterpret_cast<const uint4*>(net.w3t + n * kN + 8 * kg));
+        half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w3t + n * kN + 8 * kg)));
   }
   for (int i = threadIdx.x; i < kN; i += blockDim.x) {
-    sm.b1[i] = net.b1[i];
-    sm.b2[i] = net.b2[i];
-    sm.b3[i] = net.b3[i];
+    sm.b1[i] = 0.5f * net.b1[i];
+    sm.b2[i] = 0.5f * net.b2[i];
+    sm.b3[i] = 0.5f * net.b3[i];
     sm.w4[i] = net.w4[i];
   }
 }
 
-// Bias + SiLU of this thread's accumulator row, written as BF16 A row (KG = 16).
+// Bias + SiLU of this thread's accumulator row (h = z/2, see load_weights),
+// written as BF16 A row (KG = 16).
 // The 32-column chunks are a rolled loop: sixteen warps at different points of
 // the tile pipeline share the SM's instruction caches, and the fully unrolled
 // epilogues tripled the kernel's code.
@@ -178,7 +194,7 @@ __device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow, cons
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int j = 8 * q + 2 * e, n = 32 * c + j;
-        p[e] = pack_bf16(silu(r[j] + bias[n]), silu(r[j + 1] + bias[n + 1]));
+        p[e] = pack_bf16(silu_half(r[j] + bias[n]), silu_half(r[j + 1] + bias[n + 1]));
       }
       *reinterpret_cast<uint4*>(gp.a + canon_off(t, 32 * c + 8 * q, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
     }
@@ -232,7 +248,7 @@ __device__ __forceinline__ float forward_tile(TcSmemG<G>& sm, const Grp& gp, uin
     float r[32];
     tmem_ld32(trow + 32 * c, r);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) e += silu(r[j] + sm.b3[32 * c + j]) * sm.w4[32 * c + j];
+    for (int j = 0; j < 32; ++j) e += silu_half(r[j] + sm.b3[32 * c + j]) * sm.w4[32 * c + j];
   }
   tc_fence_before();
   group_sync(gp.bar);  // TMEM rows read and A free before the group's next tile
@@ -309,10 +325,12 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
 __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
     const __grid_constant__ gbdmc_sim_t S, const __grid_constant__ RepTable T, const __grid_constant__ gbdmc_mlp_t net,
     const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
-    const double* audit, const gbdmc_noise_t nz) {
+    const double* audit, const gbdmc_noise_t nz, const __grid_constant__ StepF32 P) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmemG<kGroups>& sm = *reinterpret_cast<TcSmemG<kGroups>*>(smraw);
   const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
+  // V = (e_mean - corr) + e_scale (e + b4) (+ KE): the fp64 constants once per thread
+  const double v_off = (double)net.e_mean - corr, v_scale = (double)net.e_scale;
   uint32_t phase = 0;
   const uint32_t tmem = setup(sm, net);
   const int g = threadIdx.x >> 7;
@@ -354,8 +372,10 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
         }
         float lp = in.lnpsi[src];
         ke = in.ke[src];
-        const double u = S.noise_mode == GBDMC_NOISE_INJECTED ? nz.u_accept[dst] : rng.uniform53();
-        acc = is_move_f32(S, xs, fx, lp, ke, z, u);
+        if (S.noise_mode == GBDMC_NOISE_INJECTED)
+          acc = is_move_f32(P, xs, fx, lp, ke, z, AcceptF64{nz.u_accept[dst]});
+        else
+          acc = is_move_f32(P, xs, fx, lp, ke, z, AcceptU53{rng.bits53()});
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
           out.x[k * ld + dst] = xs[k];
@@ -366,7 +386,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
       } else {
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
-          xs[k] = in.x[k * ld + src] + (float)S.sigma[k / 3] * z[k];
+          xs[k] = in.x[k * ld + src] + P.sigma[k / 3] * z[k];
           out.x[k * ld + dst] = xs[k];
         }
       }
@@ -391,8 +411,10 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
       if (gp.lt == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
     }
     const float e = forward_tile(sm, gp, phase, f, ok);
-    if (i < n)
-      out.v[base + i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4) - corr + (double)ke;
+    if (i < n) {
+      const double v = v_off + v_scale * (double)(e + net.b4);
+      out.v[base + i] = S.trial.kind != GBDMC_TRIAL_NONE ? v + (double)ke : v;
+    }
     if (group_any(!ok, gp.bar)) {
       if (gp.lt == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
       break;
@@ -433,8 +455,8 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   // one CTA per SM (its shared memory and its 4 x 128 TMEM columns fill the SM)
   int g = T.tile_off[T.nrep];
   if (g > num_sms()) g = num_sms();
-  tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(S, T, net, in, out, ctrl,
-                                                                                         list, flags, audit, nz);
+  tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(
+      S, T, net, in, out, ctrl, list, flags, audit, nz, step_f32(S));
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 

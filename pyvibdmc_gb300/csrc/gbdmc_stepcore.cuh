@@ -247,10 +247,45 @@ __device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&
   return -0.5 * s;
 }
 
+// Block sums of a counting tile (valid in thread 0) with a fixed
+// shuffle / shared-memory order: count, births, deaths (int) and sf (fp32).
+__device__ __forceinline__ void block_reduce_count_f32(int& c, int& b, int& d, float& sf) {
+  __shared__ int4 sh[kMaxTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c += __shfl_down_sync(0xffffffffu, c, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    d += __shfl_down_sync(0xffffffffu, d, o);
+    sf += __shfl_down_sync(0xffffffffu, sf, o);
+  }
+  if (lane == 0) sh[wid] = make_int4(c, b, d, __float_as_int(sf));
+  __syncthreads();
+  if (wid == 0) {
+    const int4 q = lane < nw ? sh[lane] : make_int4(0, 0, 0, 0);
+    c = q.x;
+    b = q.y;
+    d = q.z;
+    sf = __int_as_float(q.w);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      c += __shfl_down_sync(0xffffffffu, c, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      d += __shfl_down_sync(0xffffffffu, d, o);
+      sf += __shfl_down_sync(0xffffffffu, sf, o);
+    }
+  }
+  __syncthreads();
+}
+
 // Discrete weights and counts from stored energies with dt = ctrl->dt_eff
-// (importance sampling; the surrogate path sets it to dt).  F32W: the weight
-// exp(-(V-vref) dt) is evaluated in fp32 from the fp64 exponent (surrogate
-// path, whose energies carry ~1e-4 relative error); sums stay fp64.
+// (importance sampling; the surrogate path sets it to dt).
+// F32W (surrogate path, whose energies carry ~1e-4 relative error): the
+// weight exp(-(V-vref) dt) is evaluated in fp32 from the fp64 exponent, the
+// branching uniform is compared with the fractional weight on the integer
+// pipes (u53_below), and the tile's sum of c V is formed as
+// vref * sum c + sum c (V - vref) with the second sum in fp32 -- three fp64
+// instructions per walker instead of ~20 (the fp64 pipe bounded the kernel).
 template <int NM, bool F32W>
 __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_t out,
@@ -269,46 +304,71 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     const long long step = ctrl->step;
     const double vref = ctrl->vref;
     const double dt = ctrl->dt_eff;
-    Partial p = partial_zero();
+    const double n0 = (double)T.n0[r];
+    const double w_hi = (n0 + n0 * 0.5) + 1.0;
     int flag = 0;
-    if (i < n) {
-      double u;
-      if constexpr (NM == GBDMC_NOISE_INJECTED) {
-        u = nz.u_branch[dst];
-      } else {
-        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
-        rng.slot = 64;  // stream disjoint from the move's draws
-        u = rng.uniform53();
-      }
-      const double n0 = (double)T.n0[r];
-      const double w_hi = (n0 + n0 * 0.5) + 1.0;
-      int c;
-      if constexpr (F32W) {
-        const float wf = expf((float)__dmul_rn(-__dsub_rn(v, vref), dt));
+    if constexpr (F32W) {
+      int c = 0, nb = 0, nd = 0;
+      float sf = 0.f;
+      if (i < n) {
+        const float w_hi_f = __double2float_rd(w_hi);  // float wf > w_hi  <=>  wf > rd(w_hi)
+        const double dv = __dsub_rn(v, vref);
+        const float wf = expf((float)__dmul_rn(-dv, dt));
         if (!isfinite(wf)) {
           flag |= GBDMC_ST_NONFINITE_WEIGHT;
-          c = 0;
-        } else if ((double)wf > w_hi) {
+        } else if (wf > w_hi_f) {
           flag |= GBDMC_ST_HUGE_WEIGHT;
-          c = 0;
         } else {
-          const float fl = floorf(wf);
-          c = (int)fl + (u < (double)(wf - fl) ? 1 : 0);
-          p.births += c > 1 ? c - 1 : 0;
-          p.deaths += c == 0 ? 1 : 0;
+          const float fl = floorf(wf), fr = wf - fl;
+          bool up;
+          if constexpr (NM == GBDMC_NOISE_INJECTED) {
+            up = nz.u_branch[dst] < (double)fr;
+          } else {
+            Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+            rng.slot = 64;  // stream disjoint from the move's draws
+            up = u53_below(rng.bits53(), fr);
+          }
+          c = (int)fl + (up ? 1 : 0);
+          nb = c > 1 ? c - 1 : 0;
+          nd = c == 0 ? 1 : 0;
+          sf = (float)c * (float)dv;
         }
-      } else {
-        c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
+        counts[dst] = c;
       }
-      counts[dst] = c;
-      p.c = c;
-      p.s0 = c == 1 ? v : (double)c * v;
+      if (__syncthreads_or(flag)) {
+        if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
+      }
+      block_reduce_count_f32(c, nb, nd, sf);
+      if (threadIdx.x == 0) {
+        Partial p = partial_zero();
+        p.c = c;
+        p.births = nb;
+        p.deaths = nd;
+        p.s0 = fma(vref, (double)c, (double)sf);
+        part[tile] = p;
+      }
+    } else {
+      Partial p = partial_zero();
+      if (i < n) {
+        double u;
+        if constexpr (NM == GBDMC_NOISE_INJECTED) {
+          u = nz.u_branch[dst];
+        } else {
+          Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+          rng.slot = 64;  // stream disjoint from the move's draws
+          u = rng.uniform53();
+        }
+        const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
+        counts[dst] = c;
+        p.c = c;
+        p.s0 = c == 1 ? v : (double)c * v;
+      }
+      if (__syncthreads_or(flag)) {
+        if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
+      }
+      p = block_reduce_partial<false>(p);
+      if (threadIdx.x == 0) part[tile] = p;
     }
-    if (__syncthreads_or(flag)) {
-      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-    }
-    p = block_reduce_partial<false>(p);
-    if (threadIdx.x == 0) part[tile] = p;
   }
 }
 

@@ -293,3 +293,42 @@ def test_step_kernel_energies_equal_the_energy_kernel(dimer_model, nwalk):
     keep = outside.cpu().numpy() == 0
     assert keep.mean() > 0.5
     np.testing.assert_array_equal(v_step[keep], v_ref.cpu().numpy()[keep])
+
+
+def test_surrogate_branch_counts_match_the_oracle_draws(dimer_model):
+    """The surrogate path's counting kernel (fp32 weight from the fp64 exponent, the
+    Philox branching uniform compared with the fractional weight on the integer pipes,
+    per-tile sums of c (V - vref) in fp32) against the oracle: fp64 weights from the
+    same energies and the oracle's 53-bit uniforms of the same Philox stream.  The
+    counts are read back from the branching index; walkers whose uniform lies within
+    1e-5 of the fractional weight (fp32 exp) may go either way.  vref to 1e-9 hartree."""
+    from oracle.philox_oracle import PhiloxStream
+    m, pot, masses = dimer_model
+    n0, seed, dt = 20000, 21, 10.0
+    nd = NNDMC(m, pot, n0, pg.WATER_DIMER_EQ[None], masses, dt, 8, seed=seed, audit_every=0,
+               bias_control=0.0).init()
+    nd.run(3)
+    torch.cuda.synchronize()
+    c0 = nd.ctrl()
+    n, step, vref = int(c0.n), int(c0.step), float(c0.vref)
+    assert c0.dt_eff == dt
+    nd.run(1)
+    torch.cuda.synchronize()
+    c1 = nd.ctrl()
+    b = nd._bufs[nd._cur]
+    v = b["v"][:n].cpu().numpy()
+    idx = b["idx"][:int(c1.n)].cpu().numpy()
+    cnt = np.bincount(idx, minlength=n)
+    assert len(cnt) == n and cnt.sum() == c1.n
+    st = PhiloxStream(seed, step, np.arange(n), replica=0)
+    st.slot = 64
+    u = st.uniform53()
+    w = np.exp(-(v - vref) * dt)
+    fl = np.floor(w)
+    want = fl.astype(np.int64) + (u < w - fl)
+    amb = (np.abs(u - (w - fl)) < 1e-5) | (np.abs(w - np.round(w)) < 1e-5)
+    assert amb.sum() < 0.002 * n
+    np.testing.assert_array_equal(cnt[~amb], want[~amb])
+    nn = int(c1.n)
+    vref_want = (cnt * v).sum() / nn - (1.0 / (2.0 * dt)) * (nn - n0) / n0
+    assert abs(c1.vref - vref_want) < 1e-9, (c1.vref, vref_want)
