@@ -75,6 +75,23 @@ struct Rng {
     z0 = rad * c;
     z1 = rad * s;
   }
+  // two standard normals, Box-Muller from the same draws with the special-
+  // function unit's approximations (lg2.approx, sqrt.approx, sin/cos.approx on
+  // the angle reduced to [-pi, pi)): ~1e-6 absolute error, for the fp32
+  // surrogate walkers, whose moves need no more
+  __device__ __forceinline__ void normal2_f32_fast(float& z0, float& z1) {
+    const uint32_t a = next32(), b = next32();
+    const float u1 = fmaf((float)a, 0x1.0p-32f, 0x1.0p-33f);  // (0, 1]
+    const float u2 = (float)(b >> 8) * 0x1.0p-24f;             // [0, 1)
+    const float r2 = -1.38629436f * __log2f(u1);               // -2 ln u1 >= 0
+    float rad;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(rad) : "f"(r2));
+    const float th = fmaf(6.28318531f, u2, -3.14159265f);  // the angle 2 pi u2 - pi
+    float s, c;
+    __sincosf(th, &s, &c);
+    z0 = -rad * c;  // cos(2 pi u2) = -cos(th)
+    z1 = -rad * s;
+  }
   // two standard normals, Box-Muller in fp64 (53-bit uniforms)
   __device__ __forceinline__ void normal2_f64(double& z0, double& z1) {
     const double u1 = 1.0 - uniform53();  // (0,1]
@@ -86,6 +103,25 @@ struct Rng {
     z1 = rad * s;
   }
 };
+
+// fp64 -> fp32 with round-to-nearest-even on the integer pipes only (the
+// fp64 pipe runs a conversion at about the cost of two FMAs per warp).  Equal
+// to the (float) conversion except that results below the normal fp32 range
+// flush to a signed zero; overflow gives a signed infinity, NaN a quiet NaN.
+__device__ __forceinline__ float d2f_rn_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu);
+  const uint32_t m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // the top 23 of 52 mantissa bits
+  const uint32_t rest = lo & 0x1FFFFFFFu;                    // the 29 dropped bits
+  uint32_t f = sign | ((uint32_t)(e - 1023 + 127) << 23) | m;
+  f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry moves into the exponent
+  const bool nan = e == 0x7FF && ((hi & 0xFFFFFu) | lo) != 0u;
+  f = e < 1023 - 126 ? sign : f;                               // below the normal range
+  f = e > 1023 + 127 ? (nan ? (sign | 0x7FC00000u) : (sign | 0x7F800000u)) : f;
+  return __uint_as_float(f);
+}
 
 // m * 2^-53 < f for the 53-bit integer m of Rng::bits53 and a float f, with
 // integer operations only: the exact value of (double)uniform53() < (double)f.

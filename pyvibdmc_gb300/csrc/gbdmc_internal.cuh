@@ -32,6 +32,7 @@ struct RepTable {
   int64_t cap[GBDMC_MAX_REPLICAS];
   int64_t n0[GBDMC_MAX_REPLICAS];
   uint32_t stream[GBDMC_MAX_REPLICAS];
+  float w_hi_f[GBDMC_MAX_REPLICAS];  // (n0 + n0/2) + 1 rounded down to fp32: float w > w_hi <=> w > w_hi_f
 };
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -106,6 +107,11 @@ int num_sms();
 // Host helpers of the step launchers shared between translation units.
 int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, RepTable& T, const char* what);
 int grid_for(const RepTable& T);
+// Tiles per block iteration of the tile-batched passes (k_count_f32, k_branch) and their grid.
+struct TileBatch {
+  int tpi, grid;
+};
+TileBatch tile_batch(const RepTable& T);
 void launch_branch(const RepTable& T, int32_t* idx, const gbdmc_ctrl_t* ctrl, const long long* prefix,
                    const int* counts, cudaStream_t s);
 

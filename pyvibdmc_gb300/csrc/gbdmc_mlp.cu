@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
           for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
         } else {
 #pragma unroll
-          for (int k = 0; k < 18; k += 2) rng.normal2_f32(z[k], z[k + 1]);
+          for (int k = 0; k < 18; k += 2) rng.normal2_f32_fast(z[k], z[k + 1]);
         }
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
@@ -533,12 +533,51 @@ __device__ __forceinline__ double dimer_part(const double (&x)[18], const double
   return v;
 }
 
+// Half of the analytic dimer energy (the terms of pes_dimer) for the 2-lane
+// audit: lane h takes monomer h; of the intermolecular terms lane 0 takes the
+// O-O Lennard-Jones and the charge pairs (i of A, j of B) (0,0) (0,1) (0,2)
+// (1,0), lane 1 the pairs (1,1) (1,2) (2,0) (2,1) (2,2).  Both lanes run the
+// same instructions on operands selected by h, so a warp issues each fp64
+// instruction once for its 16 walkers.
+__device__ __forceinline__ double dimer_half(const double (&x)[18], const double* p, int h) {
+  double xm[9], gm[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) xm[k] = h ? x[9 + k] : x[k];
+  double v = h2o_lm<false, 3>(xm, p, 0, 1, 2, gm);
+  {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
+    const double ir2 = 1.0 / (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double s2 = p[7] * p[7] * ir2;
+    const double s6 = s2 * s2 * s2;
+    const double lj = 4.0 * p[6] * (s6 * s6 - s6);
+    v += h ? 0.0 : lj;
+  }
+  const double q[3] = {p[9], p[8], p[8]};  // O, H, H
+  constexpr int ia[5] = {0, 0, 0, 1, 0}, ja[5] = {0, 1, 2, 0, 0};  // lane 0 (four pairs)
+  constexpr int ib[5] = {1, 1, 2, 2, 2}, jb[5] = {1, 2, 0, 1, 2};  // lane 1
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      d[c] = (h ? x[3 * (3 + jb[k]) + c] : x[3 * (3 + ja[k]) + c]) - (h ? x[3 * ib[k] + c] : x[3 * ia[k] + c]);
+    const double ir = rsqrt_guard(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double qq = h ? q[ib[k]] * q[jb[k]] : q[ia[k]] * q[ja[k]];
+    v += (k < 4 || h) ? qq * ir : 0.0;
+  }
+  return v;
+}
+
 // Phase 2: analytic fp64 energy for the listed walkers (audit subset and
 // out-of-box fallback).  LANES = 8: 8 lanes per walker (one part each, summed
 // in a fixed shuffle order) -- short lists, where the latency of one walker's
-// PES matters; LANES = 1: one walker per thread -- long lists (large batches),
-// where the FP64 pipe's throughput matters and 8 lanes would issue 6x the FP64
-// warp instructions.  The lists of all replicas are walked as one: every
+// PES matters; LANES = 2: two lanes per walker on one instruction stream
+// (dimer_half; ~1.2x the fp64 warp instructions of one lane per walker, twice
+// the warps in flight) -- lists of ~10^4 to 10^5; LANES = 1: one walker per
+// thread -- longer lists, where the FP64 pipe's throughput matters and 8
+// lanes would issue 6x the FP64 warp instructions.  The lists of all replicas are walked as one: every
 // block scans the replicas' list lengths into shared memory and the grid
 // strides over the concatenated list, so each SM gets the same share of the
 // fp64 work however the replicas' lists differ in length.  Audited
@@ -606,6 +645,8 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
       if constexpr (LANES == 1) {
         double gd[18];
         v = pes_dimer<false>(xd, S.pes.p, gd);
+      } else if constexpr (LANES == 2) {
+        v = dimer_half(xd, S.pes.p, part);
       } else {
         v = dimer_part(xd, S.pes.p, part);
       }
@@ -613,8 +654,8 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     if constexpr (LANES == 8) {
       v += __shfl_xor_sync(0xffffffffu, v, 4);
       v += __shfl_xor_sync(0xffffffffu, v, 2);
-      v += __shfl_xor_sync(0xffffffffu, v, 1);
     }
+    if constexpr (LANES >= 2) v += __shfl_xor_sync(0xffffffffu, v, 1);
     if (live && part == 0) {
       const unsigned char fl = flags[dst];
       const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
@@ -1041,21 +1082,34 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   long long slots = 0;
   for (int r = 0; r < T.nrep; ++r) slots += T.cap[r];
   const long long expect = net->audit_every > 0 ? slots / net->audit_every : 0;
-  if (expect > 16384)
-    k_mlp_audit<1><<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+  // lanes per walker by the expected list length; the grid holds one pass of
+  // the expected list (two to four 128-thread blocks per SM)
+  const int lanes = expect > 131072 ? 1 : (expect > 8192 ? 2 : 8);
+  long long ab = (expect * lanes + 127) / 128;
+  if (ab < 2LL * num_sms()) ab = 2LL * num_sms();
+  if (ab > 4LL * num_sms()) ab = 4LL * num_sms();
+  if (lanes == 1)
+    k_mlp_audit<1><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+  else if (lanes == 2)
+    k_mlp_audit<2><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
   else
-    k_mlp_audit<8><<<2 * num_sms(), 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+    k_mlp_audit<8><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
   rc = mlp_table(S, reps, nrep, T2, what, 256);
   if (rc) return rc;
-  gbdmc_walkers_t wv{};
-  wv.v = dst->v;
-  if (S->noise_mode == GBDMC_NOISE_INJECTED)
-    k_count<GBDMC_NOISE_INJECTED, true><<<grid_for(T2), T2.tpb, 0, s>>>(*S, T2, wv, ctrl, L.part, L.prefix,
-                                                                         L.counts, nz);
-  else
-    k_count<GBDMC_NOISE_PHILOX32, true><<<grid_for(T2), T2.tpb, 0, s>>>(*S, T2, wv, ctrl, L.part, L.prefix,
-                                                                         L.counts, nz);
+  const TileBatch tb = tile_batch(T2);
+  const bool inj = S->noise_mode == GBDMC_NOISE_INJECTED;
+  if (tb.tpi == 4) {
+    if (inj)
+      k_count_f32<GBDMC_NOISE_INJECTED, 4><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+    else
+      k_count_f32<GBDMC_NOISE_PHILOX32, 4><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+  } else {
+    if (inj)
+      k_count_f32<GBDMC_NOISE_INJECTED, 1><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+    else
+      k_count_f32<GBDMC_NOISE_PHILOX32, 1><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+  }
   k_count_finalize<<<T2.nrep, kMaxTPB, 0, s>>>(*S, T2, ctrl, L.part, L.prefix);
   launch_branch(T2, dst->idx, ctrl, L.prefix, L.counts, s);
   if (prof) {

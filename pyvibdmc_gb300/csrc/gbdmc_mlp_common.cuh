@@ -95,7 +95,7 @@ __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], fl
     const float b = y[k] - x[k] - im * f[k] * dt;
     expo += (b * b - a * a) * P.h[k / 3];
   }
-  const float met = expf(expo + 2.f * (lpy - lnpsi));
+  const float met = __expf(expo + 2.f * (lpy - lnpsi));
   const bool acc = accept(met);
   if (acc) {
 #pragma unroll

@@ -9,6 +9,10 @@
 //       in the canonical K-major no-swizzle layout (8-row x 16-byte core
 //       matrices; K-adjacent cores contiguous, LBO = 128 B, SBO = KG*128 B);
 //   D = a 128-lane x 128-column FP32 accumulator in tensor memory.
+// The biases ride in the MMA: every A row ends in a constant block of 16
+// columns (1, 1, 0, ..., 0) and every weight row in (b_hi, b_lo, 0, ..., 0),
+// the bias split into two bf16 parts (~16 significant bits), so the
+// accumulator holds W a + b and the epilogue adds nothing.
 // Completion is signalled by tcgen05.commit to an mbarrier; every thread then
 // reads its own walker's row (TMEM lane = thread) with tcgen05.ld, applies
 // bias + SiLU and writes the BF16 row back as the next layer's A operand.
@@ -24,6 +28,9 @@ constexpr int kN = 128;          // hidden width = MMA N = TMEM columns
 constexpr uint32_t kCols = 128;  // TMEM columns allocated per CTA
 constexpr int kCore = 128;       // bytes of one 8 x 16-byte core matrix
 constexpr int kThreads = 128;
+constexpr int kKH = kN + 16;  // hidden-layer K: 128 activations + the constant block
+constexpr int kKG = kKH / 8;  // core columns of an A buffer and of W2/W3 (18)
+constexpr int kK1G = 4;       // core columns of W1: 16 features + the bias block
 
 // Instruction descriptor, kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N>>3 at 17, M>>4 at 24.
@@ -32,16 +39,18 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN 
 
 template <int G>
 struct TcSmemG {
-  alignas(128) unsigned char w1[kN * 16 * 2];       // N=128 x K=16 (KG = 2)
-  alignas(128) unsigned char w2[kN * kN * 2];       // N=128 x K=128 (KG = 16)
-  alignas(128) unsigned char w3[kN * kN * 2];
-  alignas(128) unsigned char a[G][kRows * kN * 2];  // per group: M=128 x K=128 (KG = 16)
-  float b1[kN], b2[kN], b3[kN], w4[kN];
+  alignas(128) unsigned char w1[kN * 8 * kK1G * 2];  // N=128 x K=32: W1 | bias block
+  alignas(128) unsigned char w2[kN * kKH * 2];       // N=128 x K=144: W2 | bias block
+  alignas(128) unsigned char w3[kN * kKH * 2];
+  alignas(128) unsigned char a[G][kRows * kKH * 2];  // per group: M=128 x K=144: activations | constants
+  float w4[kN];
   alignas(8) unsigned long long mbar[G];
   uint32_t tmem_base;
 };
 constexpr int kGroups = 4;  // tile groups per CTA of the DMC step kernel
 using TcSmem = TcSmemG<1>;
+// the step kernel's shared memory (+1 KB alignment slack) within the 227 KB a CTA may use
+static_assert(sizeof(TcSmemG<kGroups>) + 1024 <= 227 * 1024, "tile-group shared memory exceeds 227 KB");
 
 // What one tile group owns: its activation buffer, mbarrier, TMEM columns,
 // named barrier (bar.sync id over the group's 128 threads) and its thread index.
@@ -152,37 +161,61 @@ __device__ __forceinline__ uint4 half_bf16x8(uint4 v) {
   return v;
 }
 
+// bf16 bits of x (round to nearest even)
+__device__ __forceinline__ uint32_t bf16_bits(float x) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(x);
+  return (uint32_t)*reinterpret_cast<const uint16_t*>(&b);
+}
+
+// The bias block of weight row n: (b_hi, b_lo, 0, ..., 0) with b = hb the
+// halved bias, b_hi = bf16(hb) and b_lo = bf16(hb - b_hi) (the difference is
+// exact in fp32).  Two 16-byte chunks at columns kc .. kc + 15.
+__device__ __forceinline__ void store_bias_block(unsigned char* w, int n, int kc, int KG, float hb) {
+  const uint32_t hi = bf16_bits(hb);
+  const uint32_t lo = bf16_bits(hb - __uint_as_float(hi << 16));
+  *reinterpret_cast<uint4*>(w + canon_off(n, kc, KG)) = make_uint4(hi | (lo << 16), 0u, 0u, 0u);
+  *reinterpret_cast<uint4*>(w + canon_off(n, kc + 8, KG)) = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // The hidden layers' weights and biases are stored halved, so that each
-// accumulator row plus bias is h = z/2 and the epilogue is silu_half(h).
+// accumulator row is h = z/2 and the epilogue is silu_half(h).
 template <int G>
 __device__ void load_weights(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
   // Wt is n-major [128][K] in global; 16-byte chunks = 8 consecutive k of one row n
   for (int c = threadIdx.x; c < kN * 2; c += blockDim.x) {
     const int n = c >> 1, kg = c & 1;
-    *reinterpret_cast<uint4*>(sm.w1 + canon_off(n, 8 * kg, 2)) =
+    *reinterpret_cast<uint4*>(sm.w1 + canon_off(n, 8 * kg, kK1G)) =
         half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w1t + n * 16 + 8 * kg)));
   }
   for (int c = threadIdx.x; c < kN * 16; c += blockDim.x) {
     const int n = c >> 4, kg = c & 15;
-    *reinterpret_cast<uint4*>(sm.w2 + canon_off(n, 8 * kg, 16)) =
+    *reinterpret_cast<uint4*>(sm.w2 + canon_off(n, 8 * kg, kKG)) =
         half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w2t + n * kN + 8 * kg)));
-    *reinterpret_cast<uint4*>(sm.w3 + canon_off(n, 8 * kg, 16)) =
+    *reinterpret_cast<uint4*>(sm.w3 + canon_off(n, 8 * kg, kKG)) =
         half_bf16x8(__ldg(reinterpret_cast<const uint4*>(net.w3t + n * kN + 8 * kg)));
   }
-  for (int i = threadIdx.x; i < kN; i += blockDim.x) {
-    sm.b1[i] = 0.5f * net.b1[i];
-    sm.b2[i] = 0.5f * net.b2[i];
-    sm.b3[i] = 0.5f * net.b3[i];
-    sm.w4[i] = net.w4[i];
+  for (int n = threadIdx.x; n < kN; n += blockDim.x) {
+    store_bias_block(sm.w1, n, 16, kK1G, 0.5f * net.b1[n]);
+    store_bias_block(sm.w2, n, kN, kKG, 0.5f * net.b2[n]);
+    store_bias_block(sm.w3, n, kN, kKG, 0.5f * net.b3[n]);
+    sm.w4[n] = net.w4[n];
   }
 }
 
-// Bias + SiLU of this thread's accumulator row (h = z/2, see load_weights),
-// written as BF16 A row (KG = 16).
+// The constant block (1, 1, 0, ..., 0) of row `row` of an A buffer (written
+// once; the epilogues only write columns 0 .. 127).
+__device__ __forceinline__ void store_const_block(unsigned char* a, int row) {
+  const uint32_t one = bf16_bits(1.f);
+  *reinterpret_cast<uint4*>(a + canon_off(row, kN, kKG)) = make_uint4(one | (one << 16), 0u, 0u, 0u);
+  *reinterpret_cast<uint4*>(a + canon_off(row, kN + 8, kKG)) = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// SiLU of this thread's accumulator row (h = z/2 with the bias, see
+// load_weights), written as the BF16 A row (columns 0 .. 127).
 // The 32-column chunks are a rolled loop: sixteen warps at different points of
 // the tile pipeline share the SM's instruction caches, and the fully unrolled
 // epilogues tripled the kernel's code.
-__device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow, const float* bias) {
+__device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow) {
   const int t = gp.lt;
 #pragma unroll 1
   for (int c = 0; c < 4; ++c) {
@@ -193,25 +226,34 @@ __device__ __forceinline__ void epilogue_to_a(const Grp& gp, uint32_t trow, cons
       uint32_t p[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int j = 8 * q + 2 * e, n = 32 * c + j;
-        p[e] = pack_bf16(silu_half(r[j] + bias[n]), silu_half(r[j + 1] + bias[n + 1]));
+        const int j = 8 * q + 2 * e;
+        p[e] = pack_bf16(silu_half(r[j]), silu_half(r[j + 1]));
       }
-      *reinterpret_cast<uint4*>(gp.a + canon_off(t, 32 * c + 8 * q, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
+      *reinterpret_cast<uint4*>(gp.a + canon_off(t, 32 * c + 8 * q, kKG)) = make_uint4(p[0], p[1], p[2], p[3]);
     }
   }
 }
 
-// Issue the K/16 MMAs of one layer (thread 0) and wait for them.
-__device__ __forceinline__ bool run_layer(const Grp& gp, uint32_t& phase, const unsigned char* w, int KG) {
+// Issue the MMAs of one layer (thread 0) and wait for them.  A K-block of 16
+// columns is 256 bytes further along a row of core matrices.  Layer 1 reads
+// A's feature block (columns 0-15) and its constant block (128-143) against
+// W1's two blocks; the hidden layers read all nine blocks.
+__device__ __forceinline__ bool run_layer(const Grp& gp, uint32_t& phase, const unsigned char* w, bool first) {
   fence_proxy_async();
   tc_fence_before();
   group_sync(gp.bar);
   if (gp.lt == 0) {
     tc_fence_after();
     const uint32_t a0 = saddr(gp.a), b0 = saddr(w);
-    for (int s = 0; s < KG / 2; ++s)
-      umma(gp.tmem, smem_desc(a0 + 256u * s, kCore, 16 * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
-           s > 0 ? 1u : 0u);
+    if (first) {
+      umma(gp.tmem, smem_desc(a0, kCore, kKG * kCore), smem_desc(b0, kCore, kK1G * kCore), 0u);
+      umma(gp.tmem, smem_desc(a0 + 256u * (kN / 16), kCore, kKG * kCore), smem_desc(b0 + 256u, kCore, kK1G * kCore),
+           1u);
+    } else {
+      for (int s = 0; s < kKG / 2; ++s)
+        umma(gp.tmem, smem_desc(a0 + 256u * s, kCore, kKG * kCore), smem_desc(b0 + 256u * s, kCore, kKG * kCore),
+             s > 0 ? 1u : 0u);
+    }
     umma_commit(gp.mbar);
   }
   const bool ok = mbar_wait(gp.mbar, phase);
@@ -232,23 +274,23 @@ __device__ __forceinline__ float forward_tile(TcSmemG<G>& sm, const Grp& gp, uin
     uint32_t p[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) p[q] = pack_bf16(f[2 * q], f[2 * q + 1]);
-    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 0, 16)) = make_uint4(p[0], p[1], p[2], p[3]);
-    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 8, 16)) = make_uint4(p[4], p[5], p[6], p[7]);
+    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 0, kKG)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(gp.a + canon_off(t, 8, kKG)) = make_uint4(p[4], p[5], p[6], p[7]);
   }
-  ok &= run_layer(gp, phase, sm.w1, 2);
-  epilogue_to_a(gp, trow, sm.b1);
+  ok &= run_layer(gp, phase, sm.w1, true);
+  epilogue_to_a(gp, trow);
   tc_fence_before();
-  ok &= run_layer(gp, phase, sm.w2, 16);
-  epilogue_to_a(gp, trow, sm.b2);
+  ok &= run_layer(gp, phase, sm.w2, false);
+  epilogue_to_a(gp, trow);
   tc_fence_before();
-  ok &= run_layer(gp, phase, sm.w3, 16);
+  ok &= run_layer(gp, phase, sm.w3, false);
   float e = 0.f;
 #pragma unroll 1
   for (int c = 0; c < 4; ++c) {
     float r[32];
     tmem_ld32(trow + 32 * c, r);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) e += silu_half(r[j] + sm.b3[32 * c + j]) * sm.w4[32 * c + j];
+    for (int j = 0; j < 32; ++j) e += silu_half(r[j]) * sm.w4[32 * c + j];
   }
   tc_fence_before();
   group_sync(gp.bar);  // TMEM rows read and A free before the group's next tile
@@ -261,6 +303,7 @@ template <int G>
 __device__ __forceinline__ uint32_t setup(TcSmemG<G>& sm, const gbdmc_mlp_t& net) {
   static_assert(G == 1 || G == 2 || G == 4, "TMEM allocations are powers of two of at least 32 columns");
   load_weights(sm, net);
+  for (int i = threadIdx.x; i < G * kRows; i += blockDim.x) store_const_block(sm.a[i / kRows], i % kRows);
   if (threadIdx.x == 0)
     for (int g = 0; g < G; ++g) mbar_init(saddr(&sm.mbar[g]));
   if (threadIdx.x < 32) {
@@ -361,7 +404,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
         for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
       } else {
 #pragma unroll
-        for (int k = 0; k < 18; k += 2) rng.normal2_f32(z[k], z[k + 1]);
+        for (int k = 0; k < 18; k += 2) rng.normal2_f32_fast(z[k], z[k + 1]);
       }
       if (S.trial.kind == GBDMC_TRIAL_DIMER_GAUSS) {
         float fx[18];

@@ -22,10 +22,10 @@
 // dt_eff = dt * accepted/N) and k_branch.  Continuous weighting replaces
 // count/branch by k_cont_branch, one CTA per replica (sequential argmax
 // cloning, pyvibdmc.py:340-356, :432-454).
+#include <cmath>
 #include <mutex>
 #include "gbdmc_device.cuh"
 #include "gbdmc_internal.cuh"
-
 #include "gbdmc_stepcore.cuh"
 
 namespace gbdmc {
@@ -170,9 +170,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
         out.w[dst] = in.w[src];
       }
     }
-    if (COUNT && __syncthreads_or(flag)) {
-      if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-    }
+    if (COUNT) flag_weights(ctrl, flag);
     p = block_reduce_partial<STATS>(p);
     if (threadIdx.x == 0) part[tile] = p;
     const int nt = T.tile_off[r + 1] - T.tile_off[r];
@@ -311,37 +309,72 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
 
 // ----------------------------------------------------------- branching
 // Walker j (pre-branch order) writes j into idx[prefix[tile] + scan .. + c):
-// the np.repeat(arange(N), counts) order of pyvibdmc.py:417-430.
+// the np.repeat(arange(N), counts) order of pyvibdmc.py:417-430.  A block
+// takes TPI consecutive tiles per iteration (their loads in flight together,
+// one pair of barriers for all TPI scans); TPI = 1 when the tiles fit the
+// resident blocks.  Tiles at or beyond the pre-branch N are skipped.
+template <int TPI>
 __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepTable T, int32_t* __restrict__ idx,
                                                      const gbdmc_ctrl_t* ctrls, const long long* prefix,
                                                      const int* counts) {
   pdl_wait();
   const int ntile = T.tile_off[T.nrep];
-  __shared__ int wsum[kMaxTPB / 32];
-  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-    const int r = replica_of(T, tile);
-    const gbdmc_ctrl_t* ctrl = ctrls + r;
-    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
-    const int64_t base = T.off[r];
-    const long long cap = T.cap[r];
-    // counts, the tile prefix and the control block are loaded together; the
-    // counts of slots >= N are masked once N is known
-    const int c_raw = i < cap ? counts[base + i] : 0;
-    const long long pre = prefix[tile];
-    if (*(volatile const int*)&ctrl->status) continue;
-    const long long n = ctrl->n_prev;
-    const int c = i < n ? c_raw : 0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int inc = warp_incl_scan(c);
-    if (lane == 31) wsum[wid] = inc;
+  __shared__ int wsum[TPI][kMaxTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int tb = blockIdx.x * TPI; tb < ntile; tb += gridDim.x * TPI) {
+    int r[TPI], c[TPI], inc[TPI];
+    int64_t i[TPI];
+    long long pre[TPI], np[TPI];
+    // the control blocks first: tiles at or beyond N (whose prefix was not
+    // written) and stopped replicas load nothing else
+    int rr = replica_of(T, tb);
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      const int tile = min(tb + u, ntile - 1);  // a clamped duplicate is masked below
+      while (rr + 1 < T.nrep && tile >= T.tile_off[rr + 1]) ++rr;
+      r[u] = rr;
+      i[u] = (int64_t)(tile - T.tile_off[rr]) * blockDim.x + threadIdx.x;
+      const gbdmc_ctrl_t* ctrl = ctrls + rr;
+      np[u] = tb + u < ntile && *(volatile const int*)&ctrl->status == 0 ? ctrl->n_prev : 0;
+      any |= i[u] - threadIdx.x < np[u];
+    }
+    if (!any) continue;  // block-uniform
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      const bool tile_live = i[u] - threadIdx.x < np[u];
+      c[u] = i[u] < np[u] ? counts[T.off[r[u]] + i[u]] : 0;
+      pre[u] = tile_live ? prefix[tb + u] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      inc[u] = warp_incl_scan(c[u]);
+      if (lane == 31) wsum[u][wid] = inc[u];
+    }
     __syncthreads();
-    int off = 0;
-    for (int w = 0; w < wid; ++w) off += wsum[w];
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      int off = 0;
+      for (int w = 0; w < wid; ++w) off += wsum[u][w];
+      const long long dest = pre[u] + off + inc[u] - c[u];
+      const int64_t base = T.off[r[u]];
+      const long long cap = T.cap[r[u]];
+      for (int q = 0; q < c[u]; ++q)
+        if (dest + q < cap) idx[base + dest + q] = (int32_t)i[u];
+    }
     __syncthreads();
-    const long long dest = pre + off + inc - c;
-    for (int q = 0; q < c; ++q)
-      if (dest + q < cap) idx[base + dest + q] = (int32_t)i;
   }
+}
+
+// TPI = 4 once there are more than two tiles per resident block.
+TileBatch tile_batch(const RepTable& T) {
+  const int tiles = T.tile_off[T.nrep];
+  const int resident = num_sms() * (2048 / T.tpb);
+  if (tiles > 2 * resident && T.tpb >= 128) {
+    const int g = (tiles + 3) / 4;
+    return {4, g < resident ? g : resident};
+  }
+  return {1, tiles < resident ? tiles : resident};
 }
 
 // Branching straight into compact walkers, for the host-resident step:
@@ -723,6 +756,10 @@ int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, Rep
     T.cap[r] = R.cap;
     T.n0[r] = R.n0;
     T.stream[r] = R.stream;
+    const double d0 = (double)R.n0, w_hi = (d0 + d0 * 0.5) + 1.0;
+    float wf = (float)w_hi;
+    if ((double)wf > w_hi) wf = std::nextafter(wf, -INFINITY);
+    T.w_hi_f[r] = wf;
     tiles += (R.cap + tpb - 1) / tpb;
     if (tiles > INT32_MAX / 2) {
       set_error("%s: too many tiles", what);
@@ -741,7 +778,11 @@ int grid_for(const RepTable& T) {
 
 void launch_branch(const RepTable& T, int32_t* idx, const gbdmc_ctrl_t* ctrl, const long long* prefix,
                    const int* counts, cudaStream_t s) {
-  launch_pdl(k_branch, grid_for(T), T.tpb, s, T, idx, ctrl, prefix, counts);
+  const TileBatch tb = tile_batch(T);
+  if (tb.tpi == 4)
+    launch_pdl(k_branch<4>, tb.grid, T.tpb, s, T, idx, ctrl, prefix, counts);
+  else
+    launch_pdl(k_branch<1>, tb.grid, T.tpb, s, T, idx, ctrl, prefix, counts);
 }
 
 template <int PK, int A, int TK>
@@ -766,7 +807,7 @@ static void launch_branch_to(const RepTable& T, const gbdmc_sim_t& S, const gbdm
     launch_pdl(k_branch_scatter<A, IS>, grid_for(T), T.tpb, s, T, S.ld, dst, *bt.out, ctrl, L.prefix, L.counts,
                bt.ctrl_out);
   else
-    launch_pdl(k_branch, grid_for(T), T.tpb, s, T, dst.idx, ctrl, L.prefix, L.counts);
+    launch_branch(T, dst.idx, ctrl, L.prefix, L.counts, s);
 }
 
 template <int PK, int A, int TK, int NM, bool STATS>
@@ -794,7 +835,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
     if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
-      k_count<NM, false><<<G, T.tpb, 0, s>>>(S, T, dst, ctrl, L.part, L.prefix, L.counts, nz);
+      k_count<NM><<<G, T.tpb, 0, s>>>(S, T, dst.v, ctrl, L.part, L.counts, nz);
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {

@@ -80,6 +80,18 @@ __device__ __forceinline__ int replica_of(const RepTable& T, int tile) {
   return lo;
 }
 
+// The weight-guard bits (GBDMC_ST_NONFINITE_WEIGHT, GBDMC_ST_HUGE_WEIGHT)
+// raised by any thread of the block, ORed into ctrl->flags by thread 0.
+// Called by every thread; one barrier when no walker of the block tripped a
+// guard (the common case), three when one did.
+__device__ __forceinline__ void flag_weights(gbdmc_ctrl_t* ctrl, int flag) {
+  if (__syncthreads_or(flag)) {
+    const int f = (__syncthreads_or(flag & GBDMC_ST_NONFINITE_WEIGHT) ? GBDMC_ST_NONFINITE_WEIGHT : 0) |
+                  (__syncthreads_or(flag & GBDMC_ST_HUGE_WEIGHT) ? GBDMC_ST_HUGE_WEIGHT : 0);
+    if (threadIdx.x == 0) atomicOr(&ctrl->flags, f);
+  }
+}
+
 // Elects the last tile of replica `ctrl` to finish (threadFenceReduction
 // pattern, no waiting).  Every thread of the block calls it after the tile's
 // partial is written; returns true in all threads of the electing block.
@@ -247,50 +259,13 @@ __device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&
   return -0.5 * s;
 }
 
-// Block sums of a counting tile (valid in thread 0) with a fixed
-// shuffle / shared-memory order: count, births, deaths (int) and sf (fp32).
-__device__ __forceinline__ void block_reduce_count_f32(int& c, int& b, int& d, float& sf) {
-  __shared__ int4 sh[kMaxTPB / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    c += __shfl_down_sync(0xffffffffu, c, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-    d += __shfl_down_sync(0xffffffffu, d, o);
-    sf += __shfl_down_sync(0xffffffffu, sf, o);
-  }
-  if (lane == 0) sh[wid] = make_int4(c, b, d, __float_as_int(sf));
-  __syncthreads();
-  if (wid == 0) {
-    const int4 q = lane < nw ? sh[lane] : make_int4(0, 0, 0, 0);
-    c = q.x;
-    b = q.y;
-    d = q.z;
-    sf = __int_as_float(q.w);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      c += __shfl_down_sync(0xffffffffu, c, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
-      d += __shfl_down_sync(0xffffffffu, d, o);
-      sf += __shfl_down_sync(0xffffffffu, sf, o);
-    }
-  }
-  __syncthreads();
-}
-
-// Discrete weights and counts from stored energies with dt = ctrl->dt_eff
-// (importance sampling; the surrogate path sets it to dt).
-// F32W (surrogate path, whose energies carry ~1e-4 relative error): the
-// weight exp(-(V-vref) dt) is evaluated in fp32 from the fp64 exponent, the
-// branching uniform is compared with the fractional weight on the integer
-// pipes (u53_below), and the tile's sum of c V is formed as
-// vref * sum c + sum c (V - vref) with the second sum in fp32 -- three fp64
-// instructions per walker instead of ~20 (the fp64 pipe bounded the kernel).
-template <int NM, bool F32W>
+// Discrete weights and counts from stored fp64 energies with dt =
+// ctrl->dt_eff (the importance-sampled fp64 path).
+template <int NM>
 __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
-                                                    const __grid_constant__ RepTable T, gbdmc_walkers_t out,
-                                                    gbdmc_ctrl_t* ctrls, Partial* part, long long* prefix,
-                                                    int* counts, const gbdmc_noise_t nz) {
+                                                    const __grid_constant__ RepTable T, const double* __restrict__ V,
+                                                    gbdmc_ctrl_t* ctrls, Partial* part, int* counts,
+                                                    const gbdmc_noise_t nz) {
   const int ntile = T.tile_off[T.nrep];
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int r = replica_of(T, tile);
@@ -298,7 +273,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     const int64_t dst = T.off[r] + i;
     // the energy load is issued with the control-block loads (slot i < cap is inside the replica)
-    const double v = i < T.cap[r] ? out.v[dst] : 0.0;
+    const double v = i < T.cap[r] ? V[dst] : 0.0;
     if (*(volatile int*)&ctrl->status) continue;
     const long long n = ctrl->n;
     const long long step = ctrl->step;
@@ -307,68 +282,147 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     const double n0 = (double)T.n0[r];
     const double w_hi = (n0 + n0 * 0.5) + 1.0;
     int flag = 0;
-    if constexpr (F32W) {
-      int c = 0, nb = 0, nd = 0;
-      float sf = 0.f;
-      if (i < n) {
-        const float w_hi_f = __double2float_rd(w_hi);  // float wf > w_hi  <=>  wf > rd(w_hi)
-        const double dv = __dsub_rn(v, vref);
-        const float wf = expf((float)__dmul_rn(-dv, dt));
+    Partial p = partial_zero();
+    if (i < n) {
+      double u;
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
+        u = nz.u_branch[dst];
+      } else {
+        Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+        rng.slot = 64;  // stream disjoint from the move's draws
+        u = rng.uniform53();
+      }
+      const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
+      counts[dst] = c;
+      p.c = c;
+      p.s0 = c == 1 ? v : (double)c * v;
+    }
+    flag_weights(ctrl, flag);
+    p = block_reduce_partial<false>(p);
+    if (threadIdx.x == 0) part[tile] = p;
+  }
+}
+
+// Counting for the surrogate path (fp32 walkers, energies with ~1e-4
+// relative error), with no fp64 instruction per walker -- the fp64 pipe
+// bounded the fp64 version of this pass:
+//   dv = fp32(V) - fp32(vref), both converted on the integer pipes;
+//   w = exp(-dv dt) in fp32 (ex2.approx, ~2 ulp); the weight cap as the fp32
+//   w_hi_f of the table;
+//   the branching uniform compared with the fractional weight as its 53-bit
+//   integer (u53_below);
+//   the tile's sum of c V as fp32(vref) sum c + sum c dv, the second sum in
+//   fp32 (the rounding of vref cancels); births = sum c - live + deaths.
+// A block takes TPI consecutive tiles per iteration (their loads in flight
+// together, one pair of barriers for all TPI reductions; TPI = 1 when the
+// tiles fit the resident blocks).  Tiles at or beyond N write nothing:
+// k_count_finalize reduces the first ceil(N / tile) partials only.
+template <int NM, int TPI>
+__global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ gbdmc_sim_t S,
+                                                        const __grid_constant__ RepTable T,
+                                                        const double* __restrict__ V, gbdmc_ctrl_t* ctrls,
+                                                        Partial* part, int* counts, const gbdmc_noise_t nz) {
+  static_assert(TPI >= 1 && TPI <= 4, "warp u of the block reduces tile u: launched with >= 4 warps per block");
+  __shared__ int4 sh[TPI][kMaxTPB / 32];  // per warp: sum c, deaths, guard bits, sum c dv
+  const int ntile = T.tile_off[T.nrep];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int tb = blockIdx.x * TPI; tb < ntile; tb += gridDim.x * TPI) {
+    int r[TPI];
+    int64_t i[TPI];
+    double v[TPI];
+    int rr = replica_of(T, tb);
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      const int tile = min(tb + u, ntile - 1);  // a clamped duplicate is masked below
+      while (rr + 1 < T.nrep && tile >= T.tile_off[rr + 1]) ++rr;
+      r[u] = rr;
+      i[u] = (int64_t)(tile - T.tile_off[rr]) * blockDim.x + threadIdx.x;
+      v[u] = i[u] < T.cap[rr] ? V[T.off[rr] + i[u]] : 0.0;
+    }
+    int c[TPI], nd[TPI], fl[TPI];
+    long long nn[TPI];
+    float sf[TPI], vr[TPI];
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+      c[u] = nd[u] = fl[u] = 0;
+      sf[u] = 0.f;
+      const gbdmc_ctrl_t* ctrl = ctrls + r[u];
+      const int st = *(volatile const int*)&ctrl->status;
+      nn[u] = st == 0 && tb + u < ntile ? ctrl->n : 0;  // 0: nothing of this tile is counted
+      vr[u] = d2f_rn_int(ctrl->vref);
+      if (i[u] < nn[u]) {
+        const int64_t dst = T.off[r[u]] + i[u];
+        const float dv = d2f_rn_int(v[u]) - vr[u];
+        const float wf = __expf(-dv * d2f_rn_int(ctrl->dt_eff));
         if (!isfinite(wf)) {
-          flag |= GBDMC_ST_NONFINITE_WEIGHT;
-        } else if (wf > w_hi_f) {
-          flag |= GBDMC_ST_HUGE_WEIGHT;
+          fl[u] = GBDMC_ST_NONFINITE_WEIGHT;
+        } else if (wf > T.w_hi_f[r[u]]) {
+          fl[u] = GBDMC_ST_HUGE_WEIGHT;
         } else {
-          const float fl = floorf(wf), fr = wf - fl;
+          const float w0 = floorf(wf), fr = wf - w0;
           bool up;
           if constexpr (NM == GBDMC_NOISE_INJECTED) {
             up = nz.u_branch[dst] < (double)fr;
           } else {
-            Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+            Rng rng(S.seed, (uint64_t)ctrl->step, (uint64_t)i[u], T.stream[r[u]]);
             rng.slot = 64;  // stream disjoint from the move's draws
             up = u53_below(rng.bits53(), fr);
           }
-          c = (int)fl + (up ? 1 : 0);
-          nb = c > 1 ? c - 1 : 0;
-          nd = c == 0 ? 1 : 0;
-          sf = (float)c * (float)dv;
+          c[u] = (int)w0 + (up ? 1 : 0);
+          nd[u] = c[u] == 0 ? 1 : 0;
+          sf[u] = (float)c[u] * dv;
         }
-        counts[dst] = c;
+        counts[dst] = c[u];
       }
-      if (__syncthreads_or(flag)) {
-        if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-      }
-      block_reduce_count_f32(c, nb, nd, sf);
-      if (threadIdx.x == 0) {
-        Partial p = partial_zero();
-        p.c = c;
-        p.births = nb;
-        p.deaths = nd;
-        p.s0 = fma(vref, (double)c, (double)sf);
-        part[tile] = p;
-      }
-    } else {
-      Partial p = partial_zero();
-      if (i < n) {
-        double u;
-        if constexpr (NM == GBDMC_NOISE_INJECTED) {
-          u = nz.u_branch[dst];
-        } else {
-          Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
-          rng.slot = 64;  // stream disjoint from the move's draws
-          u = rng.uniform53();
-        }
-        const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);
-        counts[dst] = c;
-        p.c = c;
-        p.s0 = c == 1 ? v : (double)c * v;
-      }
-      if (__syncthreads_or(flag)) {
-        if (threadIdx.x == 0) atomicOr(&ctrl->flags, flag);
-      }
-      p = block_reduce_partial<false>(p);
-      if (threadIdx.x == 0) part[tile] = p;
     }
+#pragma unroll
+    for (int u = 0; u < TPI; ++u) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        c[u] += __shfl_down_sync(0xffffffffu, c[u], o);
+        nd[u] += __shfl_down_sync(0xffffffffu, nd[u], o);
+        sf[u] += __shfl_down_sync(0xffffffffu, sf[u], o);
+      }
+      fl[u] = __reduce_or_sync(0xffffffffu, fl[u]);
+      if (lane == 0) sh[u][wid] = make_int4(c[u], nd[u], fl[u], __float_as_int(sf[u]));
+    }
+    __syncthreads();
+    if (wid < TPI) {  // warp u: the fixed-order sums of tile tb + u
+      int ru = r[0];
+      long long nu = nn[0];
+      int64_t i0 = i[0] - threadIdx.x;
+      float vu = vr[0];
+#pragma unroll
+      for (int u = 1; u < TPI; ++u)
+        if (wid == u) {
+          ru = r[u];
+          nu = nn[u];
+          i0 = i[u] - threadIdx.x;
+          vu = vr[u];
+        }
+      if (i0 < nu) {  // a live tile of a running replica (warp-uniform)
+        int4 q = lane < nw ? sh[wid][lane] : make_int4(0, 0, 0, 0);
+        float t = __int_as_float(q.w);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          q.x += __shfl_down_sync(0xffffffffu, q.x, o);
+          q.y += __shfl_down_sync(0xffffffffu, q.y, o);
+          t += __shfl_down_sync(0xffffffffu, t, o);
+        }
+        const int f = __reduce_or_sync(0xffffffffu, q.z);
+        if (lane == 0) {
+          if (f) atomicOr(&ctrls[ru].flags, f);
+          const long long live = nu - i0 < (long long)blockDim.x ? nu - i0 : (long long)blockDim.x;
+          Partial p = partial_zero();
+          p.c = q.x;
+          p.births = (long long)q.x - live + q.y;
+          p.deaths = q.y;
+          p.s0 = fma((double)vu, (double)q.x, (double)t);
+          part[tb + wid] = p;
+        }
+      }
+    }
+    __syncthreads();  // sh is reused by the next iteration
   }
 }
 
@@ -384,7 +438,7 @@ static __global__ void __launch_bounds__(kMaxTPB) k_count_finalize(const __grid_
     gbdmc_ctrl_t* ctrl = ctrls + r;
     if (*(volatile int*)&ctrl->status) continue;  // block-uniform: only this block writes this replica's status
     const long long n = ctrl->n, step = ctrl->step;
-    const int nt = T.tile_off[r + 1] - T.tile_off[r];
+    const int nt = (int)((n + T.tpb - 1) / T.tpb);  // the tiles below N (the counting passes' live tiles)
     const Partial t = reduce_partials<false>(part, T.tile_off[r], nt, prefix);
     if (threadIdx.x < 32) finalize_discrete<false>(S, T, r, ctrl, t, n, step);
     __syncthreads();  // the next replica reuses reduce_partials' shared memory

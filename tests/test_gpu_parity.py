@@ -264,6 +264,23 @@ def test_population_guard_raises_value_error():
     assert sim.cur_timestep == 0
 
 
+@pytest.mark.parametrize("imp", [False, True])
+def test_weight_guard_sees_every_walker_of_a_tile(imp):
+    """A single walker with a huge weight trips the weight guard (pyvibdmc.py:397) when it
+    is not the first walker of its tile: every thread's guard bits reach the control
+    block.  Plain step (counting in the move kernel) and importance-sampled step (the
+    counting pass), 100 HO walkers at V = 2 Eh except walker 37 at V = 0."""
+    ho = oracle.ho_config()
+    x0 = np.zeros((100, 1, 3))
+    x0[:, 0, 0] = np.sqrt(2 * 2.0 / ho["k"])
+    x0[37, 0, 0] = 0.0  # w_37 ~ exp(vref dt) with vref ~ 2 Eh
+    kw = dict(imp_samp=pg.ho_gaussian_trial(ho["masses"], 1500.0)) if imp else {}
+    sim = _sim(x0, ho["masses"], ["H"], pg.harmonic_oscillator(), 3, 20, **kw)
+    with pytest.raises(ValueError, match="Massive walker"):
+        sim.run()
+    assert sim.cur_timestep == 0
+
+
 def test_philox_graph_batching_is_deterministic():
     _, m = oracle.h2o_config()
     x0 = geoms(4000, seed=11, scale=0.05)
