@@ -311,7 +311,8 @@ typedef struct {
   float feat_inv_sd[16];
   float feat_lo[16];
   float feat_hi[16];
-  int32_t audit_every; /* walker audited (analytic PES, error recorded) when hash % audit_every == 0; 0 = off */
+  int32_t audit_every; /* walker audited (analytic PES, error recorded) with probability 1/audit_every
+                          (32-bit hash h of walker, step, replica: h * audit_every < 2^32); 0 = off */
   int32_t engine;      /* 0: mma.sync BF16 kernels; 1: tcgen05 (TMEM accumulators, one thread per walker) */
   float bias_beta;     /* online bias control: c <- (1-b) c + b <V_nn - V_analytic>_audit each step, and the
                           next step's surrogate energies are V_nn - c (0 = off) */

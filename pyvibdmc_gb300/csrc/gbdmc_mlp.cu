@@ -394,7 +394,7 @@ __device__ __forceinline__ void mlp_forward16(const MlpSmem& sm, const gbdmc_mlp
 template <typename T>
 __global__ void __launch_bounds__(256) k_mlp_energy(const __grid_constant__ gbdmc_mlp_t net, const T* __restrict__ x,
                                                      long long ld, long long n, double* __restrict__ v,
-                                                     int* __restrict__ outside) {
+                                                     int* __restrict__ outside, const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
   load_net(sm, net);
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) k_mlp_energy(const __grid_constant__ gbdm
       float xs[18];
 #pragma unroll
       for (int k = 0; k < 18; ++k) xs[k] = i < n ? (float)x[k * ld + i] : (k < 3 ? 0.f : 1.f + k);
-      oob = walker_features(xs, net, sm.feat[w][lane]) && i < n;
+      oob = walker_features(xs, B, sm.feat[w][lane]) && i < n;
     }
     __syncwarp();
     float e_lo, e_hi;
@@ -436,7 +436,8 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
                                                           const __grid_constant__ gbdmc_mlp_t net,
                                                           const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out,
                                                           gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
-                                                          const double* audit, const gbdmc_noise_t nz) {
+                                                          const double* audit, const gbdmc_noise_t nz,
+                                                          const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
   const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
@@ -454,6 +455,7 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
     const int64_t base = T.off[r];
     const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * 128 + 16 * w;
     if (i0 >= n) continue;  // warp-uniform: no walkers in this warp's rows
+    if (i0 == 0 && lane == 0) store_count_params(ctrl);
     if (lane < 16) {
       const int64_t i = i0 + lane;
       float xs[18];
@@ -475,10 +477,9 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
           out.x[k * ld + dst] = xs[k];
         }
         if (out.who && in.who) out.who[dst] = in.who[src];
-        const bool oob = walker_features(xs, net, sm.feat[w][lane]);
-        const bool aud = net.audit_every > 0 &&
-                         (splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)) %
-                          (uint32_t)net.audit_every) == 0;
+        const bool oob = walker_features(xs, B, sm.feat[w][lane]);
+        const bool aud = audit_pick(
+            splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)), net.audit_every);
         const unsigned char fl = (oob ? 1 : 0) | (aud ? 2 : 0);
         if (fl) {
           const unsigned long long q = atomicAdd((unsigned long long*)&ctrl->reserved[2], 1ull);
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
       } else {
 #pragma unroll
         for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
-        walker_features(xs, net, sm.feat[w][lane]);
+        walker_features(xs, B, sm.feat[w][lane]);
       }
     }
     __syncwarp();
@@ -716,6 +717,7 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
       const long long na = *(volatile long long*)&c->n_acc;
       const double dte = S.dt * ((double)na / (double)n);
       c->dt_eff = dte;
+      count_params(c)->y = (float)dte;
       c->eff_ts = (step == 0) ? dte : c->eff_ts + dte;
       if (step < S.hist.len) {
         const int64_t h = (int64_t)r * S.hist.len + step;
@@ -732,7 +734,7 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
                                                    const __grid_constant__ RepTable T,
                                                    const __grid_constant__ gbdmc_mlp_t net, gbdmc_walkers_f32_t W,
                                                    gbdmc_ctrl_t* ctrls, Partial* part,
-                                                   const __grid_constant__ StepF32 P) {
+                                                   const __grid_constant__ StepF32 P, const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
   load_net(sm, net);
@@ -751,7 +753,7 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
       float xs[18];
 #pragma unroll
       for (int k = 0; k < 18; ++k) xs[k] = i < n ? W.x[k * ld + base + i] : (k < 3 ? 0.f : 1.f + k);
-      walker_features(xs, net, sm.feat[w][lane]);
+      walker_features(xs, B, sm.feat[w][lane]);
     }
     __syncwarp();
     float e_lo, e_hi;
@@ -956,7 +958,8 @@ extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t 
   if (rc) return rc;
   long long g = (n + 127) / 128;
   if (g > 2LL * num_sms()) g = 2LL * num_sms();
-  k_mlp_energy<float><<<(int)g, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*net, x, ld, n, v, outside);
+  k_mlp_energy<float><<<(int)g, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*net, x, ld, n, v, outside,
+                                                                                 feat_box(*net));
   return check_launch("gbdmc_mlp_energy");
 }
 
@@ -1019,7 +1022,8 @@ extern "C" int gbdmc_mlp_batch_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
   int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();
-  k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part, step_f32(*S));
+  k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part, step_f32(*S),
+                                                                     feat_box(*net));
   return check_launch("gbdmc_mlp_batch_init");
 }
 
@@ -1075,7 +1079,7 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
     if (rc) return rc;
   } else {
     k_mlp_move_energy<<<grid, 256, mlp_smem_bytes(), s>>>(*S, T, *net, *src, *dst, ctrl, L.list, L.flags, audit,
-                                                          nz);
+                                                          nz, feat_box(*net));
   }
   if (prof) cudaEventRecord(ev[1], s);
   // expected list length: the audit share of the walkers (the out-of-box fallbacks are few)

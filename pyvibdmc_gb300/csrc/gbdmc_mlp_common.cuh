@@ -62,6 +62,17 @@ __device__ __forceinline__ float local_ke_f32(const StepF32& P, const float (&d2
   return -0.5f * s;
 }
 
+// fp32 copies of the replica's vref and dt_eff for the surrogate counting
+// pass (k_count_f32), kept in ctrl->reserved[3]: written by the step's first
+// kernel from the replica's first tile (vref as of the step's start; dt_eff
+// is rewritten by the audit when a trial changes it).
+__device__ __forceinline__ float2* count_params(gbdmc_ctrl_t* ctrl) {
+  return reinterpret_cast<float2*>(&ctrl->reserved[3]);
+}
+__device__ __forceinline__ void store_count_params(gbdmc_ctrl_t* ctrl) {
+  *count_params(ctrl) = make_float2((float)ctrl->vref, (float)ctrl->dt_eff);
+}
+
 // Metropolis decisions met > u: the Philox uniform as its 53-bit integer
 // (integer pipes) or an injected fp64 uniform.
 struct AcceptU53 {
@@ -109,9 +120,28 @@ __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], fl
   return acc;
 }
 
-// Descriptors of one walker into the warp's feature row; returns true when
-// the walker lies outside the training box (normalised range +- margin).
-__device__ __forceinline__ bool walker_features(const float (&xs)[18], const gbdmc_mlp_t& net, float* row) {
+// The descriptor normalisation and training box of a network, prepared on
+// the host: f_q = r_q scale_q + shift_q (scale = 1/sd, shift = -mu/sd) and
+// the box [lo_q - margin, hi_q + margin].
+struct FeatBox {
+  float scale[15], shift[15], lo[15], hi[15];
+};
+
+inline FeatBox feat_box(const gbdmc_mlp_t& net) {
+  FeatBox B{};
+  for (int q = 0; q < 15; ++q) {
+    B.scale[q] = net.feat_inv_sd[q];
+    B.shift[q] = -net.feat_mu[q] * net.feat_inv_sd[q];
+    B.lo[q] = net.feat_lo[q] - net.hull_margin;
+    B.hi[q] = net.feat_hi[q] + net.hull_margin;
+  }
+  return B;
+}
+
+// Descriptors of one walker into the warp's feature row (15 normalised inverse
+// pair distances, then a zero pad); returns true when the walker lies outside
+// the training box.
+__device__ __forceinline__ bool walker_features(const float (&xs)[18], const FeatBox& B, float* row) {
   int q = 0;
   bool out = false;
 #pragma unroll
@@ -119,14 +149,21 @@ __device__ __forceinline__ bool walker_features(const float (&xs)[18], const gbd
 #pragma unroll
     for (int j = i + 1; j < 6; ++j) {
       const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
-      const float f = (rsqrtf(dx * dx + dy * dy + dz * dz) - net.feat_mu[q]) * net.feat_inv_sd[q];
-      out |= (f < net.feat_lo[q] - net.hull_margin) || (f > net.feat_hi[q] + net.hull_margin);
+      const float f = fmaf(rsqrtf(dx * dx + dy * dy + dz * dz), B.scale[q], B.shift[q]);
+      out |= (f < B.lo[q]) || (f > B.hi[q]);
       row[q] = f;
       ++q;
     }
   }
   row[15] = 0.f;
   return out;
+}
+
+// Audit selection of a walker from its 32-bit hash h of (walker, step,
+// replica stream): h * audit_every < 2^32, probability 1/audit_every
+// (every walker for 1, none for 0) with one wide multiply.
+__device__ __forceinline__ bool audit_pick(uint32_t h, int audit_every) {
+  return audit_every > 0 && (uint64_t)h * (uint64_t)(uint32_t)audit_every < (1ull << 32);
 }
 
 }  // namespace gbdmc

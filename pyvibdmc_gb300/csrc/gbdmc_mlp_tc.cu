@@ -332,7 +332,7 @@ __device__ __forceinline__ void teardown(uint32_t tmem) {
 __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constant__ gbdmc_mlp_t net,
                                                              const float* __restrict__ x, long long ld, long long n,
                                                              double* __restrict__ v, int* __restrict__ outside,
-                                                             int* __restrict__ err) {
+                                                             int* __restrict__ err, const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
   uint32_t phase = 0;
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
     float xs[18], f[16];
 #pragma unroll
     for (int k = 0; k < 18; ++k) xs[k] = i < n ? x[k * ld + i] : (k < 3 ? 0.f : 1.f + k);
-    const bool oob = walker_features(xs, net, f) && i < n;
+    const bool oob = walker_features(xs, B, f) && i < n;
     const float e = forward_tile(sm, gp, phase, f, ok);
     if (i < n) v[i] = (double)net.e_mean + (double)net.e_scale * (double)(e + net.b4);
     if (oob && outside) outside[i] = 1;
@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(kThreads) k_mlp_tc_energy(const __grid_constan
 __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
     const __grid_constant__ gbdmc_sim_t S, const __grid_constant__ RepTable T, const __grid_constant__ gbdmc_mlp_t net,
     const gbdmc_walkers_f32_t in, gbdmc_walkers_f32_t out, gbdmc_ctrl_t* ctrls, int* list, unsigned char* flags,
-    const double* audit, const gbdmc_noise_t nz, const __grid_constant__ StepF32 P) {
+    const double* audit, const gbdmc_noise_t nz, const __grid_constant__ StepF32 P,
+    const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmemG<kGroups>& sm = *reinterpret_cast<TcSmemG<kGroups>*>(smraw);
   const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
     const int64_t base = T.off[r];
     const int64_t i0 = (int64_t)(tile - T.tile_off[r]) * kRows;
     if (i0 >= n) continue;  // group-uniform: n and the tile are the same for the whole group
+    if (i0 == 0 && gp.lt == 0) store_count_params(ctrl);
     const int64_t i = i0 + gp.lt;
     float xs[18], f[16];
     bool acc = false;
@@ -434,10 +436,9 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
         }
       }
       if (out.who && in.who) out.who[dst] = in.who[src];
-      const bool oob = walker_features(xs, net, f);
-      const bool aud = net.audit_every > 0 &&
-                       (splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)) %
-                        (uint32_t)net.audit_every) == 0;
+      const bool oob = walker_features(xs, B, f);
+      const bool aud = audit_pick(
+          splitmix32((uint32_t)i ^ (uint32_t)(step * 0x9E3779B9u) ^ (T.stream[r] * 0x85EBCA6Bu)), net.audit_every);
       const unsigned char fl = (oob ? 1 : 0) | (aud ? 2 : 0);
       if (fl) {
         const unsigned long long q = atomicAdd((unsigned long long*)&ctrl->reserved[2], 1ull);
@@ -447,7 +448,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
     } else {
 #pragma unroll
       for (int k = 0; k < 18; ++k) xs[k] = (k < 3 ? 0.f : 1.f + k);
-      walker_features(xs, net, f);
+      walker_features(xs, B, f);
     }
     if (S.trial.kind != GBDMC_TRIAL_NONE) {  // accepted moves of the replica (dt_eff = dt * accepted / N)
       const int nacc = group_count(acc, gp.bar);
@@ -481,7 +482,7 @@ int launch_mlp_tc_energy(const gbdmc_mlp_t& net, const float* x, long long ld, l
   }
   long long g = (n + tc::kRows - 1) / tc::kRows;
   if (g > 2LL * num_sms()) g = 2LL * num_sms();
-  tc::k_mlp_tc_energy<<<(int)g, tc::kThreads, tc_smem_bytes(), s>>>(net, x, ld, n, v, outside, err);
+  tc::k_mlp_tc_energy<<<(int)g, tc::kThreads, tc_smem_bytes(), s>>>(net, x, ld, n, v, outside, err, feat_box(net));
   return check_launch("gbdmc_mlp_energy (tcgen05)");
 }
 
@@ -499,7 +500,7 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   int g = T.tile_off[T.nrep];
   if (g > num_sms()) g = num_sms();
   tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(
-      S, T, net, in, out, ctrl, list, flags, audit, nz, step_f32(S));
+      S, T, net, in, out, ctrl, list, flags, audit, nz, step_f32(S), feat_box(net));
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 

@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
 // Counting for the surrogate path (fp32 walkers, energies with ~1e-4
 // relative error), with no fp64 instruction per walker -- the fp64 pipe
 // bounded the fp64 version of this pass:
-//   dv = fp32(V) - fp32(vref), both converted on the integer pipes;
+//   dv = fp32(V) - fp32(vref), V converted on the integer pipes, fp32(vref)
+//   and fp32(dt_eff) from ctrl->reserved[3] (written by the step's first
+//   kernel, and by the audit for dt_eff);
 //   w = exp(-dv dt) in fp32 (ex2.approx, ~2 ulp); the weight cap as the fp32
 //   w_hi_f of the table;
 //   the branching uniform compared with the fractional weight as its 53-bit
@@ -349,11 +351,12 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ g
       const gbdmc_ctrl_t* ctrl = ctrls + r[u];
       const int st = *(volatile const int*)&ctrl->status;
       nn[u] = st == 0 && tb + u < ntile ? ctrl->n : 0;  // 0: nothing of this tile is counted
-      vr[u] = d2f_rn_int(ctrl->vref);
+      const float2 vd = *reinterpret_cast<const float2*>(&ctrl->reserved[3]);  // fp32 vref, dt_eff
+      vr[u] = vd.x;
       if (i[u] < nn[u]) {
         const int64_t dst = T.off[r[u]] + i[u];
-        const float dv = d2f_rn_int(v[u]) - vr[u];
-        const float wf = __expf(-dv * d2f_rn_int(ctrl->dt_eff));
+        const float dv = d2f_rn_int(v[u]) - vd.x;
+        const float wf = __expf(-dv * vd.y);
         if (!isfinite(wf)) {
           fl[u] = GBDMC_ST_NONFINITE_WEIGHT;
         } else if (wf > T.w_hi_f[r[u]]) {
@@ -377,12 +380,10 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ g
     }
 #pragma unroll
     for (int u = 0; u < TPI; ++u) {
+      c[u] = __reduce_add_sync(0xffffffffu, c[u]);
+      nd[u] = __reduce_add_sync(0xffffffffu, nd[u]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        c[u] += __shfl_down_sync(0xffffffffu, c[u], o);
-        nd[u] += __shfl_down_sync(0xffffffffu, nd[u], o);
-        sf[u] += __shfl_down_sync(0xffffffffu, sf[u], o);
-      }
+      for (int o = 16; o > 0; o >>= 1) sf[u] += __shfl_down_sync(0xffffffffu, sf[u], o);
       fl[u] = __reduce_or_sync(0xffffffffu, fl[u]);
       if (lane == 0) sh[u][wid] = make_int4(c[u], nd[u], fl[u], __float_as_int(sf[u]));
     }
@@ -403,12 +404,10 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ g
       if (i0 < nu) {  // a live tile of a running replica (warp-uniform)
         int4 q = lane < nw ? sh[wid][lane] : make_int4(0, 0, 0, 0);
         float t = __int_as_float(q.w);
+        q.x = __reduce_add_sync(0xffffffffu, q.x);
+        q.y = __reduce_add_sync(0xffffffffu, q.y);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          q.x += __shfl_down_sync(0xffffffffu, q.x, o);
-          q.y += __shfl_down_sync(0xffffffffu, q.y, o);
-          t += __shfl_down_sync(0xffffffffu, t, o);
-        }
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
         const int f = __reduce_or_sync(0xffffffffu, q.z);
         if (lane == 0) {
           if (f) atomicOr(&ctrls[ru].flags, f);
