@@ -73,23 +73,13 @@ __device__ __forceinline__ void store_count_params(gbdmc_ctrl_t* ctrl) {
   *count_params(ctrl) = make_float2((float)ctrl->vref, (float)ctrl->dt_eff);
 }
 
-// Metropolis decisions met > u: the Philox uniform as its 53-bit integer
-// (integer pipes) or an injected fp64 uniform.
-struct AcceptU53 {
-  uint64_t m;
-  __device__ __forceinline__ bool operator()(float met) const { return u53_below(m, met); }
-};
-struct AcceptF64 {
-  double u;
-  __device__ __forceinline__ bool operator()(float met) const { return (double)met > u; }
-};
-
 // Importance-sampled move of one fp32 dimer walker (pyvibdmc.py:549-612 with
 // ImpSamp.metropolis, imp_samp.py:28-47): proposal y = x + sigma z + (f_x/m) dt,
 // trial at y, acceptance min(1, G(y->x)/G(x->y) (psi_y/psi_x)^2) with the
-// psi ratio folded into one exponent through ln psi.  On return x, f, lnpsi
-// and ke hold the walker's state after the Metropolis test; returns whether
-// the proposal was accepted.
+// psi ratio folded into one exponent through ln psi; accept(met) decides
+// met > u (it may draw u, after the deviates z).  On return x, f, lnpsi and ke
+// hold the walker's state after the Metropolis test; returns whether the
+// proposal was accepted.
 template <typename Acc>
 __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], float (&f)[18], float& lnpsi,
                                             float& ke, const float (&z)[18], const Acc& accept) {

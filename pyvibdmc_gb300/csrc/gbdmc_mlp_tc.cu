@@ -400,15 +400,18 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
       const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
       const int64_t dst = base + i;
       Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+      const bool inj = S.noise_mode == GBDMC_NOISE_INJECTED;
       float z[18];
-      if (S.noise_mode == GBDMC_NOISE_INJECTED) {
-#pragma unroll
-        for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
-      } else {
-#pragma unroll
-        for (int k = 0; k < 18; k += 2) rng.normal2_f32_fast(z[k], z[k + 1]);
-      }
       if (S.trial.kind == GBDMC_TRIAL_DIMER_GAUSS) {
+        // deviates first, then the walker's loads (measured faster here: the
+        // trial's registers leave no room to hold both across the deviates)
+        if (inj) {
+#pragma unroll
+          for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 18; k += 2) rng.normal2_f32_fast(z[k], z[k + 1]);
+        }
         float fx[18];
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
@@ -417,10 +420,11 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
         }
         float lp = in.lnpsi[src];
         ke = in.ke[src];
-        if (S.noise_mode == GBDMC_NOISE_INJECTED)
-          acc = is_move_f32(P, xs, fx, lp, ke, z, AcceptF64{nz.u_accept[dst]});
-        else
-          acc = is_move_f32(P, xs, fx, lp, ke, z, AcceptU53{rng.bits53()});
+        // the acceptance uniform is drawn after the deviates (the stream order of the move)
+        auto accept = [&](float met) {
+          return inj ? (double)met > nz.u_accept[dst] : u53_below(rng.bits53(), met);
+        };
+        acc = is_move_f32(P, xs, fx, lp, ke, z, accept);
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
           out.x[k * ld + dst] = xs[k];
@@ -429,9 +433,19 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
         out.lnpsi[dst] = lp;
         out.ke[dst] = ke;
       } else {
+        // the walker's loads first: their latency overlaps the deviates' arithmetic
+#pragma unroll
+        for (int k = 0; k < 18; ++k) xs[k] = in.x[k * ld + src];
+        if (inj) {
+#pragma unroll
+          for (int k = 0; k < 18; ++k) z[k] = (float)nz.normal[k * nz.ld_noise + dst];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 18; k += 2) rng.normal2_f32_fast(z[k], z[k + 1]);
+        }
 #pragma unroll
         for (int k = 0; k < 18; ++k) {
-          xs[k] = in.x[k * ld + src] + P.sigma[k / 3] * z[k];
+          xs[k] += P.sigma[k / 3] * z[k];
           out.x[k * ld + dst] = xs[k];
         }
       }
