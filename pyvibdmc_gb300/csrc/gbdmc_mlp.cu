@@ -503,97 +503,23 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
   }
 }
 
-// One eighth of the analytic dimer energy (same terms as pes_dimer): part 0/1
-// the two monomers, part 2 the O-O Lennard-Jones plus the O-O charge pair,
-// parts 3..7 the remaining eight intermolecular charge pairs.
-__device__ __forceinline__ double dimer_part(const double (&x)[18], const double* p, int part) {
-  double g[18];
-  if (part == 0) return h2o_lm<false, 6>(x, p, 0, 1, 2, g);
-  if (part == 1) return h2o_lm<false, 6>(x, p, 3, 4, 5, g);
-  const double q[3] = {p[9], p[8], p[8]};  // O, H, H
-  double v = 0.0;
-  if (part == 2) {
-    double d[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
-    const double ir2 = 1.0 / (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double s2 = p[7] * p[7] * ir2;
-    const double s6 = s2 * s2 * s2;
-    v = 4.0 * p[6] * (s6 * s6 - s6);
-  }
-  // charge pairs (i of monomer A, j of monomer B) owned by this part
-  const int pairs[6][2] = {{0, 0}, {1, 2}, {3, 4}, {5, 6}, {7, 7}, {8, 8}};  // [part-2] -> pair range
-  const int lo = pairs[part - 2][0], hi = pairs[part - 2][1];
-  for (int k = lo; k <= hi; ++k) {
-    const int i = k / 3, j = k % 3;
-    double d[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) d[c] = x[3 * (3 + j) + c] - x[3 * i + c];
-    v += q[i] * q[j] * rsqrt_guard(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-  }
-  return v;
-}
-
-// Half of the analytic dimer energy (the terms of pes_dimer) for the 2-lane
-// audit: lane h takes monomer h; of the intermolecular terms lane 0 takes the
-// O-O Lennard-Jones and the charge pairs (i of A, j of B) (0,0) (0,1) (0,2)
-// (1,0), lane 1 the pairs (1,1) (1,2) (2,0) (2,1) (2,2).  Both lanes run the
-// same instructions on operands selected by h, so a warp issues each fp64
-// instruction once for its 16 walkers.
-__device__ __forceinline__ double dimer_half(const double (&x)[18], const double* p, int h) {
-  double xm[9], gm[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) xm[k] = h ? x[9 + k] : x[k];
-  double v = h2o_lm<false, 3>(xm, p, 0, 1, 2, gm);
-  {
-    double d[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
-    const double ir2 = 1.0 / (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double s2 = p[7] * p[7] * ir2;
-    const double s6 = s2 * s2 * s2;
-    const double lj = 4.0 * p[6] * (s6 * s6 - s6);
-    v += h ? 0.0 : lj;
-  }
-  const double q[3] = {p[9], p[8], p[8]};  // O, H, H
-  constexpr int ia[5] = {0, 0, 0, 1, 0}, ja[5] = {0, 1, 2, 0, 0};  // lane 0 (four pairs)
-  constexpr int ib[5] = {1, 1, 2, 2, 2}, jb[5] = {1, 2, 0, 1, 2};  // lane 1
-#pragma unroll
-  for (int k = 0; k < 5; ++k) {
-    double d[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-      d[c] = (h ? x[3 * (3 + jb[k]) + c] : x[3 * (3 + ja[k]) + c]) - (h ? x[3 * ib[k] + c] : x[3 * ia[k] + c]);
-    const double ir = rsqrt_guard(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double qq = h ? q[ib[k]] * q[jb[k]] : q[ia[k]] * q[ja[k]];
-    v += (k < 4 || h) ? qq * ir : 0.0;
-  }
-  return v;
-}
-
-// Phase 2: analytic fp64 energy for the listed walkers (audit subset and
-// out-of-box fallback).  LANES = 8: 8 lanes per walker (one part each, summed
-// in a fixed shuffle order) -- short lists, where the latency of one walker's
-// PES matters; LANES = 2: two lanes per walker on one instruction stream
-// (dimer_half; ~1.2x the fp64 warp instructions of one lane per walker, twice
-// the warps in flight) -- lists of ~10^4 to 10^5; LANES = 1: one walker per
-// thread -- longer lists, where the FP64 pipe's throughput matters and 8
-// lanes would issue 6x the FP64 warp instructions.  The lists of all replicas are walked as one: every
-// block scans the replicas' list lengths into shared memory and the grid
-// strides over the concatenated list, so each SM gets the same share of the
-// fp64 work however the replicas' lists differ in length.  Audited
-// differences V_nn - V_analytic are summed per block and added to
-// audit[0..2] (fallbacks to audit[3]) with one atomic each per block.
-template <int LANES>
+// Phase 2: the analytic energy (dimer_energy_f32) of the listed walkers:
+// the audit subset and the out-of-box fallback, one walker per thread.  The
+// lists of all replicas are walked as one: every block scans the replicas'
+// list lengths into shared memory and the grid strides over the
+// concatenated list (warp w of block b takes chunk w * gridDim + b, so a
+// short list still spreads over every SM).  Audited differences
+// V_nn - V_analytic are summed per block and added to audit[0..2]
+// (fallbacks to audit[3]) with one atomic each per block.
 __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     gbdmc_ctrl_t* ctrls, const int* list,
-                                                    const unsigned char* flags, double* audit, float beta) {
+                                                    const unsigned char* flags, double* audit, float beta,
+                                                    const __grid_constant__ StepF32 P) {
   static_assert(GBDMC_MAX_REPLICAS <= 64, "two replicas per lane in the list-length scan");
   __shared__ long long pre[GBDMC_MAX_REPLICAS + 1];  // exclusive prefix of the list lengths
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
-  const int part = threadIdx.x & (LANES - 1);
   const int nrep = T.nrep;
   const int wpb = blockDim.x >> 5;
   if (threadIdx.x < 32) {
@@ -620,55 +546,33 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
   __syncthreads();
   const long long total = pre[nrep];
   double s_n = 0.0, s_d = 0.0, s_d2 = 0.0, s_fb = 0.0;
-  // a warp takes 32/LANES walkers per iteration (lanes LANES*k .. LANES*k+LANES-1 ->
-  // walker jb + k); the loop bound is warp-uniform, so the shuffles see all 32 lanes
-  // (warp w of block b takes chunk w * gridDim + b: a short list still spreads over every SM)
-  constexpr int WPW = 32 / LANES;  // walkers per warp and iteration
   const long long gw = (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
   const long long nw = (long long)gridDim.x * wpb;
-  for (long long jb = WPW * gw; jb < total; jb += WPW * nw) {
-    const long long j = jb + ((threadIdx.x & 31) / LANES);
-    const bool live = j < total;
-    double v = 0.0;
-    int64_t dst = 0;
-    if (live) {
-      int r = 0, hi = nrep;  // largest r with pre[r] <= j (then j < pre[r + 1])
-      while (hi - r > 1) {
-        const int mid = (r + hi) >> 1;
-        if (pre[mid] <= j) r = mid;
-        else hi = mid;
-      }
-      const int64_t base = T.off[r];
-      dst = base + list[base + (j - pre[r])];
-      double xd[18];
+  for (long long jb = 32 * gw; jb < total; jb += 32 * nw) {
+    const long long j = jb + (threadIdx.x & 31);
+    if (j >= total) break;
+    int r = 0, hi = nrep;  // largest r with pre[r] <= j (then j < pre[r + 1])
+    while (hi - r > 1) {
+      const int mid = (r + hi) >> 1;
+      if (pre[mid] <= j) r = mid;
+      else hi = mid;
+    }
+    const int64_t base = T.off[r];
+    const int64_t dst = base + list[base + (j - pre[r])];
+    float xs[18];
 #pragma unroll
-      for (int k = 0; k < 18; ++k) xd[k] = (double)out.x[k * ld + dst];
-      if constexpr (LANES == 1) {
-        double gd[18];
-        v = pes_dimer<false>(xd, S.pes.p, gd);
-      } else if constexpr (LANES == 2) {
-        v = dimer_half(xd, S.pes.p, part);
-      } else {
-        v = dimer_part(xd, S.pes.p, part);
-      }
+    for (int k = 0; k < 18; ++k) xs[k] = out.x[k * ld + dst];
+    const double v = (double)dimer_energy_f32(xs, P.pes);
+    const unsigned char fl = flags[dst];
+    const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
+    if (fl & 2) {
+      const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
+      s_n += 1.0;
+      s_d += d;
+      s_d2 += d * d;
     }
-    if constexpr (LANES == 8) {
-      v += __shfl_xor_sync(0xffffffffu, v, 4);
-      v += __shfl_xor_sync(0xffffffffu, v, 2);
-    }
-    if constexpr (LANES >= 2) v += __shfl_xor_sync(0xffffffffu, v, 1);
-    if (live && part == 0) {
-      const unsigned char fl = flags[dst];
-      const double ke = out.ke ? (double)out.ke[dst] : 0.0;  // v holds V + KE with a trial
-      if (fl & 2) {
-        const double d = (out.v[dst] - ke + c_used) - v;  // error of the raw network energy
-        s_n += 1.0;
-        s_d += d;
-        s_d2 += d * d;
-      }
-      if (fl & 1) s_fb += 1.0;
-      out.v[dst] = v + ke;
-    }
+    if (fl & 1) s_fb += 1.0;
+    out.v[dst] = v + ke;
   }
   {  // block sums of the audit statistics, one atomic per quantity
     __shared__ double red[4][4];
@@ -1082,22 +986,15 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
                                                           nz, feat_box(*net));
   }
   if (prof) cudaEventRecord(ev[1], s);
-  // expected list length: the audit share of the walkers (the out-of-box fallbacks are few)
+  // expected list length: the audit share of the walkers (the out-of-box fallbacks are few);
+  // the grid holds one pass of it (two to four 128-thread blocks per SM)
   long long slots = 0;
   for (int r = 0; r < T.nrep; ++r) slots += T.cap[r];
   const long long expect = net->audit_every > 0 ? slots / net->audit_every : 0;
-  // lanes per walker by the expected list length; the grid holds one pass of
-  // the expected list (two to four 128-thread blocks per SM)
-  const int lanes = expect > 131072 ? 1 : (expect > 8192 ? 2 : 8);
-  long long ab = (expect * lanes + 127) / 128;
+  long long ab = (expect + 127) / 128;
   if (ab < 2LL * num_sms()) ab = 2LL * num_sms();
   if (ab > 4LL * num_sms()) ab = 4LL * num_sms();
-  if (lanes == 1)
-    k_mlp_audit<1><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
-  else if (lanes == 2)
-    k_mlp_audit<2><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
-  else
-    k_mlp_audit<8><<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta);
+  k_mlp_audit<<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta, step_f32(*S));
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
   rc = mlp_table(S, reps, nrep, T2, what, 256);
   if (rc) return rc;

@@ -33,6 +33,7 @@ struct StepF32 {
   float h[6];         // 1 / (2 sigma_a^2), fp32 arithmetic on the fp32 sigma
   float dt;
   float trial[8];     // dimer trial parameters (gbdmc_trial_t.p[0..7])
+  float pes[10];      // dimer PES parameters (gbdmc_pes_t.p[0..9])
 };
 
 inline StepF32 step_f32(const gbdmc_sim_t& S) {
@@ -45,6 +46,7 @@ inline StepF32 step_f32(const gbdmc_sim_t& S) {
   }
   P.dt = (float)S.dt;
   for (int k = 0; k < 8; ++k) P.trial[k] = (float)S.trial.p[k];
+  for (int k = 0; k < 10; ++k) P.pes[k] = (float)S.pes.p[k];
   return P;
 }
 
@@ -108,6 +110,55 @@ __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], fl
     ke = local_ke_f32(P, d2y);
   }
   return acc;
+}
+
+// The analytic dimer energy in fp32: the terms of pes_dimer (two local-mode
+// monomers, the O-O Lennard-Jones, nine intermolecular charge pairs) in its
+// summation order, p = De, a, re, k_theta, theta_e, k_rr, eps, sigma, q_H,
+// q_O.  About 1e-7 relative (~1e-2 cm^-1 per walker), far below the
+// surrogate error that the audit measures; used for the audit and the
+// out-of-box fallback of the fp32 surrogate walkers.
+__device__ __forceinline__ float dimer_energy_f32(const float (&x)[18], const float (&p)[10]) {
+  float v = 0.f;
+#pragma unroll
+  for (int m = 0; m < 2; ++m) {
+    const int o = 3 * m, h1 = o + 1, h2 = o + 2;
+    float d1[3], d2[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      d1[d] = x[3 * h1 + d] - x[3 * o + d];
+      d2[d] = x[3 * h2 + d] - x[3 * o + d];
+    }
+    const float r1 = sqrtf(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
+    const float r2 = sqrtf(d2[0] * d2[0] + d2[1] * d2[1] + d2[2] * d2[2]);
+    const float dot = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2];
+    const float c = fminf(1.f, fmaxf(-1.f, dot / (r1 * r2)));
+    const float dth = acosf(c) - p[4];
+    const float dr1 = r1 - p[2], dr2 = r2 - p[2];
+    const float e1 = 1.f - expf(-p[1] * dr1), e2 = 1.f - expf(-p[1] * dr2);
+    v += p[0] * e1 * e1 + p[0] * e2 * e2 + 0.5f * p[3] * dth * dth + p[5] * dr1 * dr2;
+  }
+  {
+    float d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = x[9 + k] - x[k];
+    const float s2 = p[7] * p[7] / (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const float s6 = s2 * s2 * s2;
+    v += 4.f * p[6] * (s6 * s6 - s6);
+  }
+  const float q[3] = {p[9], p[8], p[8]};  // O, H, H
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float d[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[k] = x[3 * (3 + j) + k] - x[3 * i + k];
+      const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      v += q[i] * q[j] * (r2 > 0.f ? rsqrtf(r2) : 0.f);
+    }
+  }
+  return v;
 }
 
 // The descriptor normalisation and training box of a network, prepared on
