@@ -127,22 +127,35 @@ def _pool_pes(chunk):
     return oracle.pes_h2o_lm(chunk, p)
 
 
-def cpu_reference_rate(n_walkers, steps, cores):
-    """Oracle port of DMC_Sim.propagate on the host: walker-steps/s.  With
+def _pool_pes_dimer(chunk):
+    import oracle
+    p, _ = oracle.dimer_config()
+    return oracle.pes_dimer(chunk, p)
+
+
+def cpu_reference_rate(n_walkers, steps, cores, system="h2o"):
+    """Oracle port of DMC_Sim.propagate on the host: walker-steps/s of the
+    local-mode water (system "h2o") or the water dimer ("dimer").  With
     cores > 1 the PES is sharded over a spawn pool the way
     potential_manager.Potential.getpot does (np.array_split, pool.map,
     np.concatenate)."""
     import oracle
-    p, m = oracle.h2o_config()
-    x0 = start_structures(n_walkers, 5)
+    if system == "dimer":
+        p, m = oracle.dimer_config()
+        x0 = oracle.dimer_equilibrium()[None] + 0.02 * np.random.default_rng(5).standard_normal((n_walkers, 6, 3))
+        pes1, poolf = (lambda c: oracle.pes_dimer(c, p)), _pool_pes_dimer
+    else:
+        p, m = oracle.h2o_config()
+        x0 = start_structures(n_walkers, 5)
+        pes1, poolf = (lambda c: oracle.pes_h2o_lm(c, p)), _pool_pes
     if cores > 1:
         import multiprocessing as mp
         ctx = mp.get_context("spawn")
         pool = ctx.Pool(cores)
-        pes = lambda c: np.concatenate(pool.map(_pool_pes, np.array_split(c, cores)))  # noqa: E731
+        pes = lambda c: np.concatenate(pool.map(poolf, np.array_split(c, cores)))  # noqa: E731
     else:
         pool = None
-        pes = lambda c: oracle.pes_h2o_lm(c, p)  # noqa: E731
+        pes = pes1
     try:
         sim = oracle.OracleDMC(x0, m, DT, pes, _NumpyNoise(1))
         sim.run(3)  # warm-up (step 0 potential + vref)
@@ -573,6 +586,24 @@ def run_combined_dimer(m, pot, dm, T=6000):
     base = res["plain_fp64_200k"]["efficiency"]
     res["is_gain_fp64_at_equal_error"] = res["is_fp64_200k"]["efficiency"] / base
     res["gain_vs_plain_fp64_at_equal_error"] = res["is_nn_64_replicas"]["efficiency"] / base
+    # the reference's CPU path on the same dimer (oracle port, plain discrete), a bounded
+    # sample: its error per walker-step is the plain FP64 run's (same algorithm), so the
+    # gain at equal error scales with the throughput ratio
+    cores = os.cpu_count() or 1
+    cpu, ccores = cpu_reference_rate(20000, 20, 1, "dimer")[0], 1
+    if cores > 1:
+        try:
+            cp = cpu_reference_rate(20000, 10, cores, "dimer")[0]
+            if cp > cpu:
+                cpu, ccores = cp, cores
+        except Exception:
+            pass
+    res["cpu_reference_dimer"] = {"walker_steps_per_s": cpu, "cores": ccores,
+                                  "sample": "oracle restatement of DMC_Sim.propagate (plain, discrete), "
+                                            "20000 dimer walkers, numpy; best of 1 process and a "
+                                            f"{cores}-process PES pool"}
+    res["gain_vs_cpu_reference_at_equal_error"] = (res["gain_vs_plain_fp64_at_equal_error"] *
+                                                   res["plain_fp64_200k"]["walker_steps_per_s"] / cpu)
     d = z - res["is_fp64_200k"]["zpe_cm"]
     res["zpe_minus_fp64_is_cm"] = [d, float(np.hypot(e, res["is_fp64_200k"]["err_cm"]))]
     return res
