@@ -613,13 +613,17 @@ def run_e2e(sim, L, dev, steps):
     """The walkers in page-locked host memory, stepped through the public
     host-resident API (``pyvibdmc_gb300.HostWalkers`` ->
     ``gbdmc_sim_step_host``): every step the move kernel reads the walkers
-    from host memory, the branching kernel writes the branched population,
-    its potentials, ancestor ids and the control block back to host memory,
-    and the host waits for the step and reads N'."""
+    from host memory, and the branching kernel writes the branched
+    population, its potentials, ancestor ids and the control block back to
+    host memory.  The headline value queues the timed steps back to back
+    (``HostWalkers.run``, one wait at the end; the kernels take N from the
+    device control block); ``per_step_sync`` waits for every step and reads
+    N' on the host (``HostWalkers.step``)."""
     import torch
     import pyvibdmc_gb300 as pg
     from pyvibdmc_gb300 import _capi
     A3 = 3 * sim.natoms
+    cb = C.sizeof(_capi.Ctrl)
     hw = pg.HostWalkers(sim)
     n = hw.n
     for _ in range(3):
@@ -632,15 +636,27 @@ def run_e2e(sim, L, dev, steps):
         h2d += (A3 * 8 + 4) * n  # coordinates and ancestor ids of the N walkers
         total += n
         n = hw.step()
-        d2h += (A3 * 8 + 8 + 4) * n + C.sizeof(_capi.Ctrl)
+        d2h += (A3 * 8 + 8 + 4) * n + cb
     secs = time.perf_counter() - t0
+    sync = {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
+            "d2h_bytes_per_step": d2h // steps, "steps": steps}
+    # the same steps queued back to back; the populations come from the device history
+    s0, n0 = int(hw.ctrl().step), hw.n
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hw.run(steps)
+    secs = time.perf_counter() - t0
+    after = sim._hist["pop"][s0:s0 + steps].cpu().numpy().astype(np.int64)
+    before = np.concatenate([[n0], after[:-1]])
     hw.close()
-    return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
-            "d2h_bytes_per_step": d2h // steps, "steps": steps,
+    return {"value": float(before.sum()) / secs, "unit": UNIT,
+            "h2d_bytes_per_step": int((A3 * 8 + 4) * before.sum()) // steps,
+            "d2h_bytes_per_step": int((A3 * 8 + 8 + 4) * after.sum() + cb * steps) // steps, "steps": steps,
             "path": "walkers in page-locked host memory; per step one gbdmc_sim_step_host call (C ABI, "
                     "graph-replayed): the move kernel reads the N walkers from host memory, the branching kernel "
-                    "writes the branched walkers, V, ancestor ids and the control block to host memory; host "
-                    "sync per step"}
+                    "writes the branched walkers, V, ancestor ids and the control block to host memory; the steps "
+                    "are queued back to back (HostWalkers.run) with one host wait at the end",
+            "per_step_sync": sync}
 
 
 def run_e2e_staged(sim, L, dev, steps):

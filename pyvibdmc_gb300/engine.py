@@ -578,7 +578,8 @@ class HostWalkers:
     population back over the host link, so every step starts and ends with
     the walkers on the host -- the way the reference's ``propagate`` loop
     holds them in NumPy arrays (``pyvibdmc.py:710-848``).  ``step()`` queues
-    one step, waits for it and returns the new population; ``x``, ``v`` (and
+    one step, waits for it and returns the new population; ``run(k)`` queues
+    k steps and waits once; ``x``, ``v`` (and
     ``who``, IS and continuous-weight arrays) are the pinned SoA arrays
     ``[3A][ld]`` whose first ``n`` columns are valid.  Philox noise only.
     With ``graph`` the step's launches are captured once into a CUDA graph
@@ -622,28 +623,43 @@ class HostWalkers:
             C.c_void_p(self.ctrl_host.data_ptr()), C.c_void_p(sim._scratch.data_ptr()), None, sim._stream())
         _capi.check(rc, "gbdmc_sim_step_host")
 
-    def step(self):
+    def _launch(self):
         if not self.graph:
             self._queue()
-        else:
-            # the step's launches and copies are captured once and replayed: the walker
-            # arrays and the control block never move, and every launch reads N from
-            # the device control block
-            if self._graph is None:
-                g = torch.cuda.CUDAGraph()
-                side = torch.cuda.Stream(device=self.sim.device)
-                side.wait_stream(torch.cuda.current_stream())
-                with torch.cuda.graph(g, stream=side):
-                    self._queue()
-                torch.cuda.current_stream().wait_stream(side)
-                self._graph = g
-            self._graph.replay()
+            return
+        # the step's launches and copies are captured once and replayed: the walker
+        # arrays and the control block never move, and every launch reads N from
+        # the device control block
+        if self._graph is None:
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.sim.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                self._queue()
+            torch.cuda.current_stream().wait_stream(side)
+            self._graph = g
+        self._graph.replay()
+
+    def run(self, nsteps):
+        """Queue ``nsteps`` host-resident steps back to back and wait once.
+        Every step still reads the walkers from, and writes the branched
+        population, V and the control block to, page-locked host memory; the
+        kernels take N from the device control block, so the host needs no
+        value between steps.  A step whose guard trips stops the steps after
+        it on the device (the host walkers keep the last good population) and
+        raises the reference's ValueError here.  Returns the population."""
+        for _ in range(int(nsteps)):
+            self._launch()
         torch.cuda.current_stream().synchronize()
         c = self.ctrl()
         if c.status:
             raise ValueError(f"Massive walker birth or death event!!!!!!! Dying... (status {c.status})")
         self.n = int(c.n)
         return self.n
+
+    def step(self):
+        """One host-resident step; waits for it and returns the new population."""
+        return self.run(1)
 
     def close(self):
         """Copy the walkers back into the simulation's device buffers."""

@@ -295,10 +295,12 @@ def test_philox_graph_batching_is_deterministic():
     assert np.array_equal(runs[0][1], runs[1][1])
 
 
-@pytest.mark.parametrize("imp,graph", [(False, False), (False, True), (True, True)])
-def test_host_resident_step_matches_device_step(imp, graph):
+@pytest.mark.parametrize("imp,graph,pipelined", [(False, False, False), (False, True, False), (True, True, False),
+                                                 (False, True, True), (True, True, True)])
+def test_host_resident_step_matches_device_step(imp, graph, pipelined):
     """gbdmc_sim_step_host (walkers in page-locked host memory, read and written by
-    the kernels) reproduces the device-resident step bit for bit."""
+    the kernels) reproduces the device-resident step bit for bit, one step per call
+    (step) and with the 20 steps queued back to back (run)."""
     _, m = oracle.h2o_config()
     x0 = geoms(3000, seed=8, scale=0.05)
 
@@ -314,7 +316,10 @@ def test_host_resident_step_matches_device_step(imp, graph):
     hw = pg.HostWalkers(b, graph=graph)
     for _ in range(20):
         a._cur, a._lazy = a._launch_step(a._cur, a._lazy)
-        n = hw.step()
+        if not pipelined:
+            n = hw.step()
+    if pipelined:
+        n = hw.run(20)
     a._compact()
     na = int(a._read_ctrl().n)
     assert n == na
@@ -451,4 +456,8 @@ def test_host_resident_step_failure_keeps_the_host_walkers():
     before = hw.host["x"][:, :100].clone()
     with pytest.raises(ValueError, match="Massive walker"):
         hw.step()
+    assert torch.equal(hw.host["x"][:, :100], before)
+    # queued steps: the first trips the guard, the device skips the rest
+    with pytest.raises(ValueError, match="Massive walker"):
+        hw.run(4)
     assert torch.equal(hw.host["x"][:, :100], before)
