@@ -674,11 +674,11 @@ __global__ void __launch_bounds__(256) k_mlp_init(const __grid_constant__ gbdmc_
       (void)e_lo;
       (void)e_hi;
       if (S.trial.kind == GBDMC_TRIAL_DIMER_GAUSS) {  // psi_T, drift and local KE at the start (pyvibdmc.py:760-769)
-        float xs[18], fx[18], d2[18];
+        float xs[18], fx[18], lap;
 #pragma unroll
         for (int k = 0; k < 18; ++k) xs[k] = W.x[k * ld + base + i];
-        const float lp = dimer_trial_log(xs, P.trial, fx, d2);
-        const float ke = local_ke_f32(P, d2);
+        const float lp = dimer_trial_f32(xs, P, fx, lap);
+        const float ke = -0.5f * lap;
 #pragma unroll
         for (int k = 0; k < 18; ++k) W.f[k * ld + base + i] = fx[k];
         W.lnpsi[base + i] = lp;

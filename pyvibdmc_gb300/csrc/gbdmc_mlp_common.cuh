@@ -50,20 +50,6 @@ inline StepF32 step_f32(const gbdmc_sim_t& S) {
   return P;
 }
 
-// -1/2 sum_d sum_a (1/m_a) (d2 psi/dx2)/psi in fp32, the summation order of
-// local_ke (imp_samp.py:49-53).
-__device__ __forceinline__ float local_ke_f32(const StepF32& P, const float (&d2)[18]) {
-  float s = 0.f;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    float t = 0.f;
-#pragma unroll
-    for (int a = 0; a < 6; ++a) t += P.inv_mass[a] * d2[3 * a + d];
-    s += t;
-  }
-  return -0.5f * s;
-}
-
 // fp32 copies of the replica's vref and dt_eff for the surrogate counting
 // pass (k_count_f32), kept in ctrl->reserved[3]: written by the step's first
 // kernel from the replica's first tile (vref as of the step's start; dt_eff
@@ -73,6 +59,91 @@ __device__ __forceinline__ float2* count_params(gbdmc_ctrl_t* ctrl) {
 }
 __device__ __forceinline__ void store_count_params(gbdmc_ctrl_t* ctrl) {
   *count_params(ctrl) = make_float2((float)ctrl->vref, (float)ctrl->dt_eff);
+}
+
+// The dimer trial in fp32 for the surrogate move: ln psi at x (without the
+// normalisation), the drift d1 = d ln psi/dx, and the mass-weighted
+// Laplacian sum lap = sum_k (1/m_k) (d2 psi/dx_k^2)/psi, so that the local
+// kinetic energy is -lap/2 (imp_samp.py:49-53) -- the terms of
+// dimer_trial_log, with the second derivatives summed as they are produced
+// instead of kept per Cartesian component (18 fewer live registers).
+__device__ __forceinline__ void h2o_trial_f32(const float (&x)[18], const float* p, int o, float imo, float imh1,
+                                              float imh2, float (&f)[18], float& lnpsi, float& tsum) {
+  const float a1 = p[0], a2 = p[1], ath = p[2], r1e = p[3], r2e = p[4], the = p[5];
+  const int h1 = o + 1, h2 = o + 2;
+  float v1[3], v2[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v1[d] = x[3 * h1 + d] - x[3 * o + d];
+    v2[d] = x[3 * h2 + d] - x[3 * o + d];
+  }
+  const float r1 = sqrtf(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const float r2 = sqrtf(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const float ir1 = 1.f / r1, ir2 = 1.f / r2;
+  const float g = ir1 * ir2;
+  float c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) * g;
+  c = fminf(1.f, fmaxf(-1.f, c));
+  const float th = acosf(c);
+  const float one_m_c2 = 1.f - c * c;
+  const float s = one_m_c2 > 0.f ? -rsqrtf(one_m_c2) : 0.f;  // dtheta/dcos
+  const float s2 = c * s * s * s;                            // d2theta/dcos2
+  const float L1 = -a1 * (r1 - r1e), L2 = -a2 * (r2 - r2e), Lt = -ath * (th - the);
+  const float ir1s = ir1 * ir1, ir2s = ir2 * ir2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float e1 = v1[d] * ir1, e2 = v2[d] * ir2;
+    const float dch1 = v2[d] * g - c * ir1 * e1;
+    const float dch2 = v1[d] * g - c * ir2 * e2;
+    const float dco = -(dch1 + dch2);
+    const float d2ch1 = c * (3.f * e1 * e1 - 1.f) * ir1s - 2.f * v2[d] * e1 * ir1s * ir2;
+    const float d2ch2 = c * (3.f * e2 * e2 - 1.f) * ir2s - 2.f * v1[d] * e2 * ir2s * ir1;
+    const float h = e1 * ir1 + e2 * ir2;
+    const float d2co = 2.f * g - 2.f * (v1[d] + v2[d]) * g * h +
+                       c * (h * h + (2.f * e1 * e1 - 1.f) * ir1s + (2.f * e2 * e2 - 1.f) * ir2s);
+    const float dth_o = s * dco, dth_1 = s * dch1, dth_2 = s * dch2;
+    const float d2th_o = s2 * dco * dco + s * d2co;
+    const float d2th_1 = s2 * dch1 * dch1 + s * d2ch1;
+    const float d2th_2 = s2 * dch2 * dch2 + s * d2ch2;
+    const float d2r1 = (1.f - e1 * e1) * ir1, d2r2 = (1.f - e2 * e2) * ir2;
+    f[3 * o + d] += -L1 * e1 - L2 * e2 + Lt * dth_o;
+    f[3 * h1 + d] += L1 * e1 + Lt * dth_1;
+    f[3 * h2 + d] += L2 * e2 + Lt * dth_2;
+    tsum += imo * (-a1 * e1 * e1 - a2 * e2 * e2 - ath * dth_o * dth_o + L1 * d2r1 + L2 * d2r2 + Lt * d2th_o) +
+            imh1 * (-a1 * e1 * e1 - ath * dth_1 * dth_1 + L1 * d2r1 + Lt * d2th_1) +
+            imh2 * (-a2 * e2 * e2 - ath * dth_2 * dth_2 + L2 * d2r2 + Lt * d2th_2);
+  }
+  lnpsi += -0.5f * (a1 * (r1 - r1e) * (r1 - r1e) + a2 * (r2 - r2e) * (r2 - r2e) + ath * (th - the) * (th - the));
+}
+
+__device__ __forceinline__ float dimer_trial_f32(const float (&x)[18], const StepF32& P, float (&d1)[18],
+                                                 float& lap) {
+  const float* p = P.trial;
+#pragma unroll
+  for (int k = 0; k < 18; ++k) d1[k] = 0.f;
+  float lnpsi = 0.f, tsum = 0.f;
+  h2o_trial_f32(x, p, 0, P.inv_mass[0], P.inv_mass[1], P.inv_mass[2], d1, lnpsi, tsum);
+  h2o_trial_f32(x, p, 3, P.inv_mass[3], P.inv_mass[4], P.inv_mass[5], d1, lnpsi, tsum);
+  const float aR = p[6], Re = p[7];
+  float v[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = x[9 + d] - x[d];
+  const float R = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  const float iR = 1.f / R;
+  const float LR = -aR * (R - Re);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float ed = v[d] * iR;
+    const float tt = -aR * ed * ed + LR * (1.f - ed * ed) * iR;
+    d1[9 + d] += LR * ed;
+    d1[d] -= LR * ed;
+    tsum += (P.inv_mass[3] + P.inv_mass[0]) * tt;
+  }
+  lnpsi += -0.5f * aR * (R - Re) * (R - Re);
+  float q = 0.f;
+#pragma unroll
+  for (int k = 0; k < 18; ++k) q += P.inv_mass[k / 3] * d1[k] * d1[k];
+  lap = q + tsum;
+  return lnpsi;
 }
 
 // Importance-sampled move of one fp32 dimer walker (pyvibdmc.py:549-612 with
@@ -86,10 +157,10 @@ template <typename Acc>
 __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], float (&f)[18], float& lnpsi,
                                             float& ke, const float (&z)[18], const Acc& accept) {
   const float dt = P.dt;
-  float y[18], fy[18], d2y[18];
+  float y[18], fy[18], lap;
 #pragma unroll
   for (int k = 0; k < 18; ++k) y[k] = x[k] + P.sigma[k / 3] * z[k] + P.inv_mass[k / 3] * f[k] * dt;
-  const float lpy = dimer_trial_log(y, P.trial, fy, d2y);
+  const float lpy = dimer_trial_f32(y, P, fy, lap);
   float expo = 0.f;
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
@@ -107,7 +178,7 @@ __device__ __forceinline__ bool is_move_f32(const StepF32& P, float (&x)[18], fl
       f[k] = fy[k];
     }
     lnpsi = lpy;
-    ke = local_ke_f32(P, d2y);
+    ke = -0.5f * lap;
   }
   return acc;
 }
