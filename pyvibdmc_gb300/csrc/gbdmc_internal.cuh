@@ -75,14 +75,16 @@ inline int64_t max_tiles_for(const gbdmc_replica_t* reps, int nrep) {
 void set_error(const char* fmt, ...);
 int check_launch(const char* what);
 
-// Launch with programmatic stream serialisation (the kernel must begin with
-// pdl_wait()); a failed launch is reported by the next check_launch.
+// Launch with programmatic stream serialisation: the kernel may start while
+// its predecessor drains and must call pdl_wait() before it reads anything the
+// predecessor writes; a failed launch is reported by the next check_launch.
 template <typename... P, typename... Args>
-inline void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, Args&&... args) {
+inline void launch_pdl_smem(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s,
+                            Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -90,6 +92,10 @@ inline void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s
   cfg.attrs = at;
   cfg.numAttrs = 1;
   (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+template <typename... P, typename... Args>
+inline void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, Args&&... args) {
+  launch_pdl_smem(kernel, grid, block, 0, s, static_cast<Args&&>(args)...);
 }
 
 // Event-pair timing of the step kernels (gbdmc_prof_enable / gbdmc_prof_read).

@@ -518,6 +518,7 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
                                                     const __grid_constant__ StepF32 P) {
   static_assert(GBDMC_MAX_REPLICAS <= 64, "two replicas per lane in the list-length scan");
   __shared__ long long pre[GBDMC_MAX_REPLICAS + 1];  // exclusive prefix of the list lengths
+  pdl_wait();
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
   const int nrep = T.nrep;
@@ -994,24 +995,25 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   long long ab = (expect + 127) / 128;
   if (ab < 2LL * num_sms()) ab = 2LL * num_sms();
   if (ab > 4LL * num_sms()) ab = 4LL * num_sms();
-  k_mlp_audit<<<(int)ab, 128, 0, s>>>(*S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta, step_f32(*S));
+  launch_pdl(k_mlp_audit, (int)ab, 128, s, *S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta, step_f32(*S));
   RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
   rc = mlp_table(S, reps, nrep, T2, what, 256);
   if (rc) return rc;
   const TileBatch tb = tile_batch(T2);
   const bool inj = S->noise_mode == GBDMC_NOISE_INJECTED;
+  const double* vv = dst->v;
   if (tb.tpi == 4) {
     if (inj)
-      k_count_f32<GBDMC_NOISE_INJECTED, 4><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+      launch_pdl(k_count_f32<GBDMC_NOISE_INJECTED, 4>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
     else
-      k_count_f32<GBDMC_NOISE_PHILOX32, 4><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+      launch_pdl(k_count_f32<GBDMC_NOISE_PHILOX32, 4>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
   } else {
     if (inj)
-      k_count_f32<GBDMC_NOISE_INJECTED, 1><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+      launch_pdl(k_count_f32<GBDMC_NOISE_INJECTED, 1>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
     else
-      k_count_f32<GBDMC_NOISE_PHILOX32, 1><<<tb.grid, T2.tpb, 0, s>>>(*S, T2, dst->v, ctrl, L.part, L.counts, nz);
+      launch_pdl(k_count_f32<GBDMC_NOISE_PHILOX32, 1>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
   }
-  k_count_finalize<<<T2.nrep, kMaxTPB, 0, s>>>(*S, T2, ctrl, L.part, L.prefix);
+  launch_pdl(k_count_finalize, T2.nrep, kMaxTPB, s, *S, T2, ctrl, L.part, L.prefix);
   launch_branch(T2, dst->idx, ctrl, L.prefix, L.counts, s);
   if (prof) {
     cudaEventRecord(ev[2], s);

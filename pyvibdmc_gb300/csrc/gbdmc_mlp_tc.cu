@@ -372,11 +372,14 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
     const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmemG<kGroups>& sm = *reinterpret_cast<TcSmemG<kGroups>*>(smraw);
+  uint32_t phase = 0;
+  // weights, mbarriers and TMEM first (inputs no kernel of the step writes),
+  // then wait for the previous step's kernels (programmatic launch)
+  const uint32_t tmem = setup(sm, net);
+  pdl_wait();
   const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
   // V = (e_mean - corr) + e_scale (e + b4) (+ KE): the fp64 constants once per thread
   const double v_off = (double)net.e_mean - corr, v_scale = (double)net.e_scale;
-  uint32_t phase = 0;
-  const uint32_t tmem = setup(sm, net);
   const int g = threadIdx.x >> 7;
   const Grp gp{sm.a[g], saddr(&sm.mbar[g]), tmem + (uint32_t)(g * kN), 1 + g, (int)(threadIdx.x & 127)};
   bool ok = true;
@@ -513,8 +516,8 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   // one CTA per SM (its shared memory and its 4 x 128 TMEM columns fill the SM)
   int g = T.tile_off[T.nrep];
   if (g > num_sms()) g = num_sms();
-  tc::k_mlp_tc_move_energy<<<g, tc::kThreads * tc::kGroups, tc_group_smem_bytes(), s>>>(
-      S, T, net, in, out, ctrl, list, flags, audit, nz, step_f32(S), feat_box(net));
+  launch_pdl_smem(tc::k_mlp_tc_move_energy, g, tc::kThreads * tc::kGroups, (size_t)tc_group_smem_bytes(), s, S, T,
+                  net, in, out, ctrl, list, flags, audit, nz, step_f32(S), feat_box(net));
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 

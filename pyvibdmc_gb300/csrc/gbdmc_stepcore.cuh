@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ g
                                                         Partial* part, int* counts, const gbdmc_noise_t nz) {
   static_assert(TPI >= 1 && TPI <= 4, "warp u of the block reduces tile u: launched with >= 4 warps per block");
   __shared__ int4 sh[TPI][kMaxTPB / 32];  // per warp: sum c, deaths, guard bits, sum c dv
+  pdl_wait();
   const int ntile = T.tile_off[T.nrep];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int tb = blockIdx.x * TPI; tb < ntile; tb += gridDim.x * TPI) {
@@ -433,6 +434,7 @@ static __global__ void __launch_bounds__(kMaxTPB) k_count_finalize(const __grid_
                                                                     const __grid_constant__ RepTable T,
                                                                     gbdmc_ctrl_t* ctrls, const Partial* part,
                                                                     long long* prefix) {
+  pdl_wait();  // (a no-op when launched without programmatic serialisation)
   for (int r = blockIdx.x; r < T.nrep; r += gridDim.x) {
     gbdmc_ctrl_t* ctrl = ctrls + r;
     if (*(volatile int*)&ctrl->status) continue;  // block-uniform: only this block writes this replica's status
