@@ -38,12 +38,15 @@ struct RepTable {
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // scratch layout: [Partial x tiles][int64 prefix x tiles][int32 counts x ld][int32 list x ld][uint8 flags x ld]
+// [uint32 sync x 64]; the surrogate step's single-pass counting uses prefix[] as its tile status words and
+// sync[0..1] as its tile ticket and exit counters
 struct ScratchLayout {
   Partial* part;
   long long* prefix;
   int* counts;
   int* list;
   unsigned char* flags;
+  unsigned int* sync;
   size_t bytes;
 };
 
@@ -61,6 +64,8 @@ inline ScratchLayout scratch_layout(void* base, int64_t ld, int64_t max_tiles) {
   off += align256(sizeof(int) * (size_t)ld);
   L.flags = (unsigned char*)(b + off);
   off += align256((size_t)ld);
+  L.sync = (unsigned int*)(b + off);
+  off += align256(64 * sizeof(unsigned int));
   L.bytes = off;
   return L;
 }

@@ -515,10 +515,14 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
                                                     const __grid_constant__ RepTable T, gbdmc_walkers_f32_t out,
                                                     gbdmc_ctrl_t* ctrls, const int* list,
                                                     const unsigned char* flags, double* audit, float beta,
-                                                    const __grid_constant__ StepF32 P) {
+                                                    const __grid_constant__ StepF32 P, unsigned long long* tstat,
+                                                    int ntile2, unsigned int* sync) {
   static_assert(GBDMC_MAX_REPLICAS <= 64, "two replicas per lane in the list-length scan");
   __shared__ long long pre[GBDMC_MAX_REPLICAS + 1];  // exclusive prefix of the list lengths
   pdl_wait();
+  // the tile status words and tickets of this step's counting pass start cleared
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntile2; t += gridDim.x * blockDim.x) tstat[t] = 0ull;
+  if (blockIdx.x == 0 && threadIdx.x < 2) sync[threadIdx.x] = 0u;
   const int64_t ld = S.ld;
   const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
   const int nrep = T.nrep;
@@ -937,6 +941,22 @@ extern "C" int gbdmc_mlp_sim_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, 
   return gbdmc_mlp_batch_init(S, net, nullptr, 0, w, ctrl, scratch, stream);
 }
 
+// Blocks of the single-pass counting kernel: at most the resident blocks
+// (the tiles are taken by ticket, so the grid need not cover them).
+static int count_branch_grid(int ntile, bool injected) {
+  static int occ[2] = {0, 0};
+  int& o = occ[injected ? 1 : 0];
+  if (o == 0) {
+    const cudaError_t e = injected ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                         &o, k_count_branch_f32<GBDMC_NOISE_INJECTED>, kMaxTPB, 0)
+                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                         &o, k_count_branch_f32<GBDMC_NOISE_PHILOX32>, kMaxTPB, 0);
+    if (e != cudaSuccess || o < 1) o = 1;
+  }
+  const int g = num_sms() * o;
+  return ntile < g ? ntile : g;
+}
+
 extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps,
                                     int32_t nrep, const gbdmc_walkers_f32_t* src, const gbdmc_walkers_f32_t* dst,
                                     gbdmc_ctrl_t* ctrl, void* scratch, double* audit, const gbdmc_noise_t* noise,
@@ -995,26 +1015,25 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   long long ab = (expect + 127) / 128;
   if (ab < 2LL * num_sms()) ab = 2LL * num_sms();
   if (ab > 4LL * num_sms()) ab = 4LL * num_sms();
-  launch_pdl(k_mlp_audit, (int)ab, 128, s, *S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta, step_f32(*S));
-  RepTable T2;  // counts and branching on 256-walker tiles (fewer partials for the last-tile reduction)
-  rc = mlp_table(S, reps, nrep, T2, what, 256);
+  RepTable T2;  // counting and branching on kCBW-walker tiles (256 threads per tile)
+  rc = mlp_table(S, reps, nrep, T2, what, kMaxTPB);
   if (rc) return rc;
-  const TileBatch tb = tile_batch(T2);
-  const bool inj = S->noise_mode == GBDMC_NOISE_INJECTED;
-  const double* vv = dst->v;
-  if (tb.tpi == 4) {
-    if (inj)
-      launch_pdl(k_count_f32<GBDMC_NOISE_INJECTED, 4>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
-    else
-      launch_pdl(k_count_f32<GBDMC_NOISE_PHILOX32, 4>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
-  } else {
-    if (inj)
-      launch_pdl(k_count_f32<GBDMC_NOISE_INJECTED, 1>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
-    else
-      launch_pdl(k_count_f32<GBDMC_NOISE_PHILOX32, 1>, tb.grid, T2.tpb, s, *S, T2, vv, ctrl, L.part, L.counts, nz);
+  int ntile2 = 0;
+  for (int r = 0; r < T2.nrep; ++r) {
+    T2.tile_off[r] = ntile2;
+    ntile2 += (int)((T2.cap[r] + kCBW - 1) / kCBW);
   }
-  launch_pdl(k_count_finalize, T2.nrep, kMaxTPB, s, *S, T2, ctrl, L.part, L.prefix);
-  launch_branch(T2, dst->idx, ctrl, L.prefix, L.counts, s);
+  T2.tile_off[T2.nrep] = ntile2;
+  unsigned long long* tstat = reinterpret_cast<unsigned long long*>(L.prefix);
+  launch_pdl(k_mlp_audit, (int)ab, 128, s, *S, T, *dst, ctrl, L.list, L.flags, audit, net->bias_beta, step_f32(*S),
+             tstat, ntile2, L.sync);
+  // counting, finalisation and branching in one pass (tile tickets, decoupled look-back)
+  if (S->noise_mode == GBDMC_NOISE_INJECTED)
+    launch_pdl(k_count_branch_f32<GBDMC_NOISE_INJECTED>, count_branch_grid(ntile2, true), T2.tpb, s, *S, T2, dst->v,
+               ctrl, L.part, tstat, L.sync, dst->idx, nz);
+  else
+    launch_pdl(k_count_branch_f32<GBDMC_NOISE_PHILOX32>, count_branch_grid(ntile2, false), T2.tpb, s, *S, T2,
+               dst->v, ctrl, L.part, tstat, L.sync, dst->idx, nz);
   if (prof) {
     cudaEventRecord(ev[2], s);
     ++g_prof.count;

@@ -303,9 +303,13 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
   }
 }
 
-// Counting for the surrogate path (fp32 walkers, energies with ~1e-4
-// relative error), with no fp64 instruction per walker -- the fp64 pipe
-// bounded the fp64 version of this pass:
+// The surrogate step's counting, finalisation and branching in one pass
+// (decoupled look-back): the discrete counts, then the gather index that
+// k_branch writes for the fp64 path, with the tile prefixes found on the fly
+// instead of by a separate finalisation kernel.  Tiles are kCBW walkers,
+// kCBW / blockDim consecutive walkers per thread (the table T is cut at that
+// width).  No fp64 instruction per walker (the fp64 pipe bounded the fp64
+// counting of this path):
 //   dv = fp32(V) - fp32(vref), V converted on the integer pipes, fp32(vref)
 //   and fp32(dt_eff) from ctrl->reserved[3] (written by the step's first
 //   kernel, and by the audit for dt_eff);
@@ -315,114 +319,195 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
 //   integer (u53_below);
 //   the tile's sum of c V as fp32(vref) sum c + sum c dv, the second sum in
 //   fp32 (the rounding of vref cancels); births = sum c - live + deaths.
-// A block takes TPI consecutive tiles per iteration (their loads in flight
-// together, one pair of barriers for all TPI reductions; TPI = 1 when the
-// tiles fit the resident blocks).  Tiles at or beyond N write nothing:
-// k_count_finalize reduces the first ceil(N / tile) partials only.
-template <int NM, int TPI>
-__global__ void __launch_bounds__(kMaxTPB) k_count_f32(const __grid_constant__ gbdmc_sim_t S,
-                                                        const __grid_constant__ RepTable T,
-                                                        const double* __restrict__ V, gbdmc_ctrl_t* ctrls,
-                                                        Partial* part, int* counts, const gbdmc_noise_t nz) {
-  static_assert(TPI >= 1 && TPI <= 4, "warp u of the block reduces tile u: launched with >= 4 warps per block");
-  __shared__ int4 sh[TPI][kMaxTPB / 32];  // per warp: sum c, deaths, guard bits, sum c dv
+// - Blocks take tiles in ticket order (sync[0]); a tile's predecessors in its
+//   replica hold earlier tickets, so they are running or done.
+// - A tile publishes its count total as an aggregate (state A) in its status
+//   word, then warp 0 looks back over its predecessors 32 at a time (bounded
+//   waits) until it meets an inclusive prefix (state P), and the tile
+//   publishes its own inclusive prefix.  The words carry the replica's step,
+//   so a word left from an earlier step never counts; the audit kernel
+//   zeroes them and the tickets every step.
+// - Each walker then writes its ancestor index c times from the tile's
+//   prefix plus its place in the tile's scan (np.repeat(arange(N), counts),
+//   pyvibdmc.py:417-430).
+// - Live tiles write their partial (c, births, deaths, sum c V) before they
+//   publish; the replica's last tile, once its look-back has seen every
+//   earlier tile, reduces the live partials in the fixed order of
+//   reduce_partials and finalises N', vref and the guards.
+// A wait that runs out sets GBDMC_ST_TIMEOUT on the replica (its later tiles
+// then skip, and their own waits run out too) and the kernel returns.
+constexpr int kCBW = 1024;  // walkers per tile of the single-pass counting kernel
+template <int NM>
+__global__ void __launch_bounds__(kMaxTPB) k_count_branch_f32(const __grid_constant__ gbdmc_sim_t S,
+                                                               const __grid_constant__ RepTable T,
+                                                               const double* __restrict__ V, gbdmc_ctrl_t* ctrls,
+                                                               Partial* part, unsigned long long* tstat,
+                                                               unsigned int* sync, int32_t* __restrict__ idx,
+                                                               const gbdmc_noise_t nz) {
+  constexpr unsigned long long kA = 1ull << 30, kP = 2ull << 30, kVal = (1ull << 30) - 1;
+  constexpr int kSpin = 1 << 22;
+  constexpr int WPT = kCBW / kMaxTPB;  // launched with kMaxTPB threads
+  __shared__ int s_tile, s_st;
+  __shared__ long long s_n, s_step, s_prefix;
+  __shared__ float2 s_vd;
+  __shared__ int wsum[kMaxTPB / 32];
+  __shared__ int4 sh[kMaxTPB / 32];  // per warp: deaths, guard bits, sum c dv (bits)
   pdl_wait();
   const int ntile = T.tile_off[T.nrep];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int tb = blockIdx.x * TPI; tb < ntile; tb += gridDim.x * TPI) {
-    int r[TPI];
-    int64_t i[TPI];
-    double v[TPI];
-    int rr = replica_of(T, tb);
-#pragma unroll
-    for (int u = 0; u < TPI; ++u) {
-      const int tile = min(tb + u, ntile - 1);  // a clamped duplicate is masked below
-      while (rr + 1 < T.nrep && tile >= T.tile_off[rr + 1]) ++rr;
-      r[u] = rr;
-      i[u] = (int64_t)(tile - T.tile_off[rr]) * blockDim.x + threadIdx.x;
-      v[u] = i[u] < T.cap[rr] ? V[T.off[rr] + i[u]] : 0.0;
-    }
-    int c[TPI], nd[TPI], fl[TPI];
-    long long nn[TPI];
-    float sf[TPI], vr[TPI];
-#pragma unroll
-    for (int u = 0; u < TPI; ++u) {
-      c[u] = nd[u] = fl[u] = 0;
-      sf[u] = 0.f;
-      const gbdmc_ctrl_t* ctrl = ctrls + r[u];
-      const int st = *(volatile const int*)&ctrl->status;
-      nn[u] = st == 0 && tb + u < ntile ? ctrl->n : 0;  // 0: nothing of this tile is counted
-      const float2 vd = *reinterpret_cast<const float2*>(&ctrl->reserved[3]);  // fp32 vref, dt_eff
-      vr[u] = vd.x;
-      if (i[u] < nn[u]) {
-        const int64_t dst = T.off[r[u]] + i[u];
-        const float dv = d2f_rn_int(v[u]) - vd.x;
-        const float wf = __expf(-dv * vd.y);
-        if (!isfinite(wf)) {
-          fl[u] = GBDMC_ST_NONFINITE_WEIGHT;
-        } else if (wf > T.w_hi_f[r[u]]) {
-          fl[u] = GBDMC_ST_HUGE_WEIGHT;
-        } else {
-          const float w0 = floorf(wf), fr = wf - w0;
-          bool up;
-          if constexpr (NM == GBDMC_NOISE_INJECTED) {
-            up = nz.u_branch[dst] < (double)fr;
-          } else {
-            Rng rng(S.seed, (uint64_t)ctrl->step, (uint64_t)i[u], T.stream[r[u]]);
-            rng.slot = 64;  // stream disjoint from the move's draws
-            up = u53_below(rng.bits53(), fr);
-          }
-          c[u] = (int)w0 + (up ? 1 : 0);
-          nd[u] = c[u] == 0 ? 1 : 0;
-          sf[u] = (float)c[u] * dv;
-        }
-        counts[dst] = c[u];
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int t = (int)atomicAdd(&sync[0], 1u);
+      s_tile = t;
+      if (t < ntile) {
+        const gbdmc_ctrl_t* ctrl = ctrls + replica_of(T, t);
+        s_st = *(volatile const int*)&ctrl->status;
+        s_n = ctrl->n;
+        s_step = ctrl->step;
+        s_vd = *reinterpret_cast<const float2*>(&ctrl->reserved[3]);  // fp32 vref, dt_eff
       }
-    }
-#pragma unroll
-    for (int u = 0; u < TPI; ++u) {
-      c[u] = __reduce_add_sync(0xffffffffu, c[u]);
-      nd[u] = __reduce_add_sync(0xffffffffu, nd[u]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sf[u] += __shfl_down_sync(0xffffffffu, sf[u], o);
-      fl[u] = __reduce_or_sync(0xffffffffu, fl[u]);
-      if (lane == 0) sh[u][wid] = make_int4(c[u], nd[u], fl[u], __float_as_int(sf[u]));
     }
     __syncthreads();
-    if (wid < TPI) {  // warp u: the fixed-order sums of tile tb + u
-      int ru = r[0];
-      long long nu = nn[0];
-      int64_t i0 = i[0] - threadIdx.x;
-      float vu = vr[0];
+    const int tile = s_tile;
+    if (tile >= ntile) break;  // block-uniform
+    const int r = replica_of(T, tile);
+    gbdmc_ctrl_t* ctrl = ctrls + r;
+    const int t0 = T.tile_off[r], t1 = T.tile_off[r + 1];
+    const long long n = s_n, step = s_step;
+    if (s_st == 0) {  // block-uniform (read once by thread 0)
+      const int64_t i0 = (int64_t)(tile - t0) * kCBW;
+      const int64_t ib = i0 + (int64_t)threadIdx.x * WPT;  // this thread's first walker
+      const int64_t base = T.off[r];
+      double v[WPT];
 #pragma unroll
-      for (int u = 1; u < TPI; ++u)
-        if (wid == u) {
-          ru = r[u];
-          nu = nn[u];
-          i0 = i[u] - threadIdx.x;
-          vu = vr[u];
+      for (int k = 0; k < WPT; ++k) v[k] = ib + k < n ? V[base + ib + k] : 0.0;
+      int c[WPT], csum = 0, nd = 0, fl = 0;
+      float sf = 0.f;
+#pragma unroll
+      for (int k = 0; k < WPT; ++k) {
+        c[k] = 0;
+        const int64_t i = ib + k;
+        if (i < n) {
+          const float dv = d2f_rn_int(v[k]) - s_vd.x;
+          const float wf = __expf(-dv * s_vd.y);
+          if (!isfinite(wf)) {
+            fl |= GBDMC_ST_NONFINITE_WEIGHT;
+          } else if (wf > T.w_hi_f[r]) {
+            fl |= GBDMC_ST_HUGE_WEIGHT;
+          } else {
+            const float w0 = floorf(wf), fr = wf - w0;
+            bool up;
+            if constexpr (NM == GBDMC_NOISE_INJECTED) {
+              up = nz.u_branch[base + i] < (double)fr;
+            } else {
+              Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
+              rng.slot = 64;  // stream disjoint from the move's draws
+              up = u53_below(rng.bits53(), fr);
+            }
+            c[k] = (int)w0 + (up ? 1 : 0);
+            nd += c[k] == 0 ? 1 : 0;
+            sf += (float)c[k] * dv;
+          }
         }
-      if (i0 < nu) {  // a live tile of a running replica (warp-uniform)
-        int4 q = lane < nw ? sh[wid][lane] : make_int4(0, 0, 0, 0);
-        float t = __int_as_float(q.w);
-        q.x = __reduce_add_sync(0xffffffffu, q.x);
-        q.y = __reduce_add_sync(0xffffffffu, q.y);
+        csum += c[k];
+      }
+      // the tile's scan of the thread totals and its sums (fixed order)
+      const int inc = warp_incl_scan(csum);
+      nd = __reduce_add_sync(0xffffffffu, nd);
+      fl = __reduce_or_sync(0xffffffffu, fl);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        const int f = __reduce_or_sync(0xffffffffu, q.z);
+      for (int o = 16; o > 0; o >>= 1) sf += __shfl_down_sync(0xffffffffu, sf, o);
+      if (lane == 31) wsum[wid] = inc;
+      if (lane == 0) sh[wid] = make_int4(nd, fl, __float_as_int(sf), 0);
+      __syncthreads();
+      int off = 0;
+      for (int w = 0; w < wid; ++w) off += wsum[w];
+      if (wid == 0) {  // warp 0: totals, partial, publication and look-back
+        long long ctot = 0, dtot = 0;
+        int ftot = 0;
+        float stot = 0.f;
+        for (int w = 0; w < nw; ++w) {
+          ctot += wsum[w];
+          dtot += sh[w].x;
+          ftot |= sh[w].y;
+          stot += __int_as_float(sh[w].z);
+        }
+        const unsigned long long ep = (unsigned long long)(uint32_t)step << 32;
+        const unsigned long long agg = (unsigned long long)(ctot < (long long)kVal ? ctot : (long long)kVal);
         if (lane == 0) {
-          if (f) atomicOr(&ctrls[ru].flags, f);
-          const long long live = nu - i0 < (long long)blockDim.x ? nu - i0 : (long long)blockDim.x;
-          Partial p = partial_zero();
-          p.c = q.x;
-          p.births = (long long)q.x - live + q.y;
-          p.deaths = q.y;
-          p.s0 = fma((double)vu, (double)q.x, (double)t);
-          part[tb + wid] = p;
+          if (i0 < n) {  // a live tile: its partial for the finalisation
+            const long long live = n - i0 < (long long)kCBW ? n - i0 : (long long)kCBW;
+            Partial p = partial_zero();
+            p.c = ctot;
+            p.births = ctot - live + dtot;
+            p.deaths = dtot;
+            p.s0 = fma((double)s_vd.x, (double)ctot, (double)stot);
+            part[tile] = p;
+          }
+          if (ftot) atomicOr(&ctrl->flags, ftot);
+          __threadfence();  // partial and guard bits before the status word
+          atomicExch(&tstat[tile], ep | (tile == t0 ? kP : kA) | agg);
+        }
+        long long prefix = 0;
+        bool timeout = false;
+        for (int jt = tile - 1; jt >= t0; jt -= 32) {  // 32 predecessors per round (warp-uniform)
+          const int j = jt - lane;
+          unsigned long long w = 0;
+          bool ready = j < t0;  // lanes before the replica's first tile add nothing
+          for (int it = 0;; ++it) {
+            if (!ready) {
+              w = *(volatile unsigned long long*)&tstat[j];
+              ready = (w >> 32) == (uint32_t)step && (w & (kA | kP)) != 0;
+            }
+            if (__all_sync(0xffffffffu, ready)) break;
+            if (it >= kSpin) {
+              timeout = true;
+              break;
+            }
+            if (it > 64) __nanosleep(64);
+          }
+          if (timeout) break;
+          const unsigned pm = __ballot_sync(0xffffffffu, j >= t0 && (w & kP) != 0);
+          const int stop = pm ? __ffs(pm) - 1 : 32;  // the nearest inclusive prefix
+          long long val = (j >= t0 && lane <= stop) ? (long long)(w & kVal) : 0;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+          prefix += val;
+          if (pm) break;
+        }
+        if (lane == 0) {
+          if (timeout) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+          if (tile != t0) {
+            const long long inclusive = prefix + ctot;
+            atomicExch(&tstat[tile],
+                       ep | kP | (unsigned long long)(inclusive < (long long)kVal ? inclusive : (long long)kVal));
+          }
+          __threadfence();  // what the predecessors published, before the finalisation reads it
+          s_prefix = prefix;
         }
       }
+      __syncthreads();
+      // the ancestor index of each copy
+      long long dest = s_prefix + off + inc - csum;
+      const long long cap = T.cap[r];
+#pragma unroll
+      for (int k = 0; k < WPT; ++k) {
+        for (int q = 0; q < c[k]; ++q)
+          if (dest + q < cap) idx[base + dest + q] = (int32_t)(ib + k);
+        dest += c[k];
+      }
+      // the replica's last tile finalises it (block-uniform)
+      if (tile == t1 - 1) {
+        const int nt = (int)((n + kCBW - 1) / kCBW);
+        const Partial tot = reduce_partials<false>(part, t0, nt, nullptr);
+        if (threadIdx.x < 32) finalize_discrete<false>(S, T, r, ctrl, tot, n, step);
+      }
     }
-    __syncthreads();  // sh is reused by the next iteration
+    __syncthreads();  // the shared words are rewritten by the next ticket
+  }
+  if (threadIdx.x == 0 && atomicAdd(&sync[1], 1u) == gridDim.x - 1) {  // the last block out resets the tickets
+    sync[0] = 0;
+    sync[1] = 0;
   }
 }
 
