@@ -118,7 +118,7 @@ int num_sms();
 // Host helpers of the step launchers shared between translation units.
 int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, RepTable& T, const char* what);
 int grid_for(const RepTable& T);
-// Tiles per block iteration of the tile-batched passes (k_count_f32, k_branch) and their grid.
+// Tiles per block iteration of the tile-batched branching pass (k_branch) and its grid.
 struct TileBatch {
   int tpi, grid;
 };

@@ -51,7 +51,7 @@ inline StepF32 step_f32(const gbdmc_sim_t& S) {
 }
 
 // fp32 copies of the replica's vref and dt_eff for the surrogate counting
-// pass (k_count_f32), kept in ctrl->reserved[3]: written by the step's first
+// pass (k_count_branch_f32), kept in ctrl->reserved[3]: written by the step's first
 // kernel from the replica's first tile (vref as of the step's start; dt_eff
 // is rewritten by the audit when a trial changes it).
 __device__ __forceinline__ float2* count_params(gbdmc_ctrl_t* ctrl) {
