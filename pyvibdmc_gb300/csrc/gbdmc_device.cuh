@@ -397,9 +397,9 @@ __device__ __forceinline__ double trial_ho(const double (&x)[3 * A], const doubl
 // which equals the ChainRuleHelper d2psidx2 sum for a direct-product psi.
 // h2o_trial_terms adds the water's d ln psi / dx_k to f[] and its
 // d2 ln psi / dx_k^2 to t[] for the atoms (o, h1, h2) of x, and returns the
-// exponent -1/2 sum_q alpha_q (q - q_e)^2.  T is float (surrogate walkers)
-// or double; the parameters p come as double, or as their fp32 copies for
-// float walkers (no per-walker conversion).
+// exponent -1/2 sum_q alpha_q (q - q_e)^2.  The fp64 path instantiates it
+// with T = double and double parameters; the fp32 surrogate move has its own
+// form (dimer_trial_f32), which sums the second derivatives as it goes.
 template <typename T>
 __device__ __forceinline__ T rsqrt_guard_t(T y) {
   return y > T(0) ? rsqrt(y) : T(0);
