@@ -535,7 +535,9 @@ def run_combined_dimer(m, pot, dm, T=6000):
     (efficiency = 1 / (error^2 x seconds)), and its ZPE against the FP64
     importance-sampled dimer (same trial, dt).  The batch's error bar is the
     scatter of its 64 independent replica ZPEs (N0-weighted); the single runs'
-    are blocking errors."""
+    are blocking errors.  The replicas' own blocking errors, combined with
+    the same weights, give a second (less noisy, correlation-dependent)
+    estimate of the batch's error bar, reported beside it."""
     import torch
     import pyvibdmc_gb300 as pg
     trial = pg.dimer_gaussian_trial()
@@ -579,13 +581,17 @@ def run_combined_dimer(m, pot, dm, T=6000):
     zr = v.mean(1)
     z = float((w * zr).sum() / w.sum())
     e = float(np.sqrt((w * w * (zr - z) ** 2).sum() * len(w) / (len(w) - 1)) / w.sum())
+    # a second error estimate: each replica's own blocking error, combined with the same weights
+    eb = np.array([pg.blocking_error(v[r], 30)[1] for r in range(len(ns))])
+    e_rb = float(np.sqrt(np.sum((w * eb) ** 2)) / w.sum())
     res["is_nn_64_replicas"] = {"replicas": len(ns), "walkers": int(sum(ns)), "steps": T, "seconds": secs,
                                 "walker_steps_per_s": nd.walker_steps(0, T) / secs, "zpe_cm": z, "err_cm": e,
-                                "err_blocking_cm": nd.zpe(start=T // 4)[1], "efficiency": 1.0 / (e * e * secs),
-                                "audit": nd.audit()}
+                                "err_blocking_cm": nd.zpe(start=T // 4)[1], "err_replica_blocking_cm": e_rb,
+                                "efficiency": 1.0 / (e * e * secs), "audit": nd.audit()}
     base = res["plain_fp64_200k"]["efficiency"]
     res["is_gain_fp64_at_equal_error"] = res["is_fp64_200k"]["efficiency"] / base
     res["gain_vs_plain_fp64_at_equal_error"] = res["is_nn_64_replicas"]["efficiency"] / base
+    res["gain_vs_plain_fp64_at_equal_error_replica_blocking"] = 1.0 / (e_rb * e_rb * secs) / base
     # the reference's CPU path on the same dimer (oracle port, plain discrete), a bounded
     # sample: its error per walker-step is the plain FP64 run's (same algorithm), so the
     # gain at equal error scales with the throughput ratio
