@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
 //   reduce_partials and finalises N', vref and the guards.
 // A wait that runs out sets GBDMC_ST_TIMEOUT on the replica (its later tiles
 // then skip, and their own waits run out too) and the kernel returns.
-constexpr int kCBW = 1024;  // walkers per tile of the single-pass counting kernel
+constexpr int kCBW = 2048;  // walkers per tile of the single-pass counting kernel (measured: 1024, 2048, 4096)
 template <int NM>
 __global__ void __launch_bounds__(kMaxTPB) k_count_branch_f32(const __grid_constant__ gbdmc_sim_t S,
                                                                const __grid_constant__ RepTable T,
