@@ -351,3 +351,42 @@ def test_audit_energies_match_the_fp64_oracle(dimer_model):
     v = b["v"][:n].cpu().numpy()
     np.testing.assert_allclose(v, oracle.pes_dimer(x, p), rtol=0, atol=2e-7)
     assert nd.audit()["audited"] >= n
+
+
+@pytest.mark.parametrize("n0", [100, 5000])
+def test_surrogate_injected_step_matches_the_oracle(dimer_model, n0):
+    """One surrogate step with injected deviates and uniforms (a one-tile replica of 100
+    walkers and one of 5000): every moved walker is x + sigma z in fp32, and the gather
+    index expands the counts floor(w) + [u < w - floor(w)] of the oracle's fp64 weights
+    from the step's own energies and the injected uniforms (walkers whose uniform lies
+    within 1e-5 of the fractional weight may go either way); vref to 1e-9 hartree."""
+    m, pot, masses = dimer_model
+    seed, dt = 31, 10.0
+    nd = NNDMC(m, pot, n0, pg.WATER_DIMER_EQ[None], masses, dt, 4, rng=oracle.InjectedNoise(seed), audit_every=0,
+               bias_control=0.0).init()
+    torch.cuda.synchronize()
+    c0 = nd.ctrl()
+    n, vref = int(c0.n), float(c0.vref)
+    x_old = nd._bufs[nd._cur]["x"][:, :n].cpu().numpy()
+    twin = oracle.InjectedNoise(seed)
+    z = np.asarray(twin.standard_normal((n, 3, 6)), dtype=np.float64).transpose(2, 1, 0).reshape(18, n)
+    u = twin.uniform(n)
+    nd.run(1)
+    torch.cuda.synchronize()
+    c1 = nd.ctrl()
+    b = nd._bufs[nd._cur]
+    sig = np.repeat(np.sqrt(dt / np.asarray(masses)), 3).astype(np.float32)[:, None]
+    want_x = x_old + sig * z.astype(np.float32)
+    np.testing.assert_allclose(b["x"][:, :n].cpu().numpy(), want_x, rtol=0, atol=2e-6)
+    v = b["v"][:n].cpu().numpy()
+    nn = int(c1.n)
+    cnt = np.bincount(b["idx"][:nn].cpu().numpy(), minlength=n)
+    assert len(cnt) == n and cnt.sum() == nn
+    w = np.exp(-(v - vref) * dt)
+    fl = np.floor(w)
+    want = fl.astype(np.int64) + (u < w - fl)
+    amb = (np.abs(u - (w - fl)) < 1e-5) | (np.abs(w - np.round(w)) < 1e-5)
+    assert amb.sum() < max(3, 0.002 * n)
+    np.testing.assert_array_equal(cnt[~amb], want[~amb])
+    vref_want = (cnt * v).sum() / nn - (1.0 / (2.0 * dt)) * (nn - n0) / n0
+    assert abs(c1.vref - vref_want) < 1e-9, (c1.vref, vref_want)
