@@ -468,8 +468,8 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
       walker_features(xs, B, f);
     }
     if (S.trial.kind != GBDMC_TRIAL_NONE) {  // accepted moves of the replica (dt_eff = dt * accepted / N)
-      const int nacc = group_count(acc, gp.bar);
-      if (gp.lt == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
+      const int nacc = __popc(__ballot_sync(0xffffffffu, acc));
+      if ((gp.lt & 31) == 0 && nacc) atomicAdd((unsigned long long*)&ctrl->n_acc, (unsigned long long)nacc);
     }
     const float e = forward_tile(sm, gp, phase, f, ok);
     if (i < n) {
