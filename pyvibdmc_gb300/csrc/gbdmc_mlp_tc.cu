@@ -63,7 +63,7 @@ struct Grp {
 };
 
 __device__ __forceinline__ void group_sync(int bar) { asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory"); }
-// OR / population count of a predicate over the group (one barrier; the result is group-uniform)
+// OR of a predicate over the group (one barrier; the result is group-uniform)
 __device__ __forceinline__ bool group_any(bool v, int bar) {
   int r;
   asm volatile(
@@ -73,15 +73,6 @@ __device__ __forceinline__ bool group_any(bool v, int bar) {
       : "memory");
   return r != 0;
 }
-__device__ __forceinline__ int group_count(bool v, int bar) {
-  int r;
-  asm volatile("{\n.reg .pred p;\nsetp.ne.s32 p, %1, 0;\nbar.red.popc.u32 %0, %2, 128, p;\n}\n"
-               : "=r"(r)
-               : "r"((int)v), "r"(bar)
-               : "memory");
-  return r;
-}
-
 // byte offset of element (row, k) of a canonical K-major operand with KG core columns
 __device__ __forceinline__ uint32_t canon_off(int row, int k, int KG) {
   return (uint32_t)(((row >> 3) * KG + (k >> 3)) * kCore + (row & 7) * 16 + (k & 7) * 2);
