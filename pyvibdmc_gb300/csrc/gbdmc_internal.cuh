@@ -70,6 +70,17 @@ inline ScratchLayout scratch_layout(void* base, int64_t ld, int64_t max_tiles) {
   return L;
 }
 
+// Slot extent of a replica table: the largest off + cap (the sim's ld for a
+// single simulation, nrep == 0).  The scratch of a call is laid out over this
+// extent, as the *_scratch_bytes functions size it, not over sim->ld: a batch
+// may step a subset of the slots with a smaller scratch.
+inline int64_t slot_extent(int64_t ld, const gbdmc_replica_t* reps, int nrep) {
+  if (!reps || nrep < 1) return ld;
+  int64_t e = 0;
+  for (int r = 0; r < nrep; ++r) e = reps[r].off + reps[r].cap > e ? reps[r].off + reps[r].cap : e;
+  return e;
+}
+
 // Upper bound of the tile count for any tile width >= kMinTPB.
 inline int64_t max_tiles_for(const gbdmc_replica_t* reps, int nrep) {
   int64_t t = 0;

@@ -928,7 +928,7 @@ extern "C" int gbdmc_mlp_batch_init(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   }
   rc = set_mlp_smem((const void*)k_mlp_init);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
+  const ScratchLayout L = scratch_layout(scratch, slot_extent(S->ld, reps, nrep), mlp_scratch_tiles(S, reps, nrep));
   int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();
   k_mlp_init<<<grid, 256, mlp_smem_bytes(), (cudaStream_t)stream>>>(*S, T, *net, *w, ctrl, L.part, step_f32(*S),
@@ -992,7 +992,7 @@ extern "C" int gbdmc_mlp_batch_step(const gbdmc_sim_t* S, const gbdmc_mlp_t* net
   }
   rc = set_mlp_smem((const void*)k_mlp_move_energy);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, mlp_scratch_tiles(S, reps, nrep));
+  const ScratchLayout L = scratch_layout(scratch, slot_extent(S->ld, reps, nrep), mlp_scratch_tiles(S, reps, nrep));
   cudaStream_t s = (cudaStream_t)stream;
   int grid = T.tile_off[T.nrep];
   if (grid > 2 * num_sms()) grid = 2 * num_sms();

@@ -997,7 +997,7 @@ static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
   RepTable T;
   rc = build_table(*S, reps, nrep, T, what);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(reps, nrep));
+  const ScratchLayout L = scratch_layout(scratch, slot_extent(S->ld, reps, nrep), max_tiles_for(reps, nrep));
   StepF f{*S, T, *src, *dst, ctrl, L, nz, bt, (cudaStream_t)stream};
   return dispatch_system(*S, what, f);
 }
@@ -1009,7 +1009,7 @@ static int init_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
   RepTable T;
   rc = build_table(*S, reps, nrep, T, what);
   if (rc) return rc;
-  const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(reps, nrep));
+  const ScratchLayout L = scratch_layout(scratch, slot_extent(S->ld, reps, nrep), max_tiles_for(reps, nrep));
   InitF f{*S, T, *W, ctrl, L, (cudaStream_t)stream};
   return dispatch_system(*S, what, f);
 }
@@ -1034,9 +1034,7 @@ extern "C" size_t gbdmc_scratch_bytes(int64_t ld) {
 
 extern "C" size_t gbdmc_batch_scratch_bytes(const gbdmc_replica_t* reps, int32_t nrep) {
   if (!reps || nrep < 1) return 0;
-  int64_t ld = 0;
-  for (int r = 0; r < nrep; ++r) ld = reps[r].off + reps[r].cap > ld ? reps[r].off + reps[r].cap : ld;
-  return scratch_layout(nullptr, ld, max_tiles_for(reps, nrep)).bytes;
+  return scratch_layout(nullptr, slot_extent(0, reps, nrep), max_tiles_for(reps, nrep)).bytes;
 }
 
 extern "C" int gbdmc_sim_init(const gbdmc_sim_t* S, const gbdmc_walkers_t* W, gbdmc_ctrl_t* ctrl, void* scratch,

@@ -477,12 +477,12 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_branch_f32(const __grid_const
         }
         if (lane == 0) {
           if (timeout) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+          __threadfence();  // what the predecessors published, before this tile's word and the finalisation
           if (tile != t0) {
             const long long inclusive = prefix + ctot;
             atomicExch(&tstat[tile],
                        ep | kP | (unsigned long long)(inclusive < (long long)kVal ? inclusive : (long long)kVal));
           }
-          __threadfence();  // what the predecessors published, before the finalisation reads it
           s_prefix = prefix;
         }
       }
