@@ -4,7 +4,8 @@
   simulation_utilities/sim_archive.py:12-23).  With h5py installed it writes
   HDF5; otherwise the same keys go to ``<fname>.npz`` next to the requested
   name (h5py is optional here).
-* ``create_filesystem`` / ``delete_older_checkpoints`` mirror FileManager
+* ``create_filesystem`` / ``delete_older_checkpoints`` /
+  ``delete_future_checkpoints`` mirror FileManager
   (simulation_utilities/file_manager.py:7-54).
 * The text log follows SimLogger's lines (simulation_utilities/sim_logger.py).
 """
@@ -15,7 +16,8 @@ import numpy as np
 
 from .constants import Constants
 
-__all__ = ["save_h5", "load_h5", "create_filesystem", "delete_older_checkpoints", "SimLogger"]
+__all__ = ["save_h5", "load_h5", "create_filesystem", "delete_older_checkpoints", "delete_future_checkpoints",
+           "checkpoint_step", "SimLogger"]
 
 try:  # optional dependency
     import h5py as _h5py
@@ -49,13 +51,39 @@ def create_filesystem(output_folder):
         os.makedirs(output_folder + sub, exist_ok=True)
 
 
+def checkpoint_step(path):
+    """Step number of a ``{sim_name}_{t}.pickle`` checkpoint (None if the name has none)."""
+    try:
+        return int(os.path.basename(path).split("_")[-1].split(".")[0])
+    except ValueError:
+        return None
+
+
+def _wfn_step(path):
+    try:  # {sim_name}_wfn_{t}ts.hdf5 (or .hdf5.npz)
+        return int(os.path.basename(path).split("_")[-1].split("ts")[0])
+    except ValueError:
+        return None
+
+
 def delete_older_checkpoints(sim_folder, sim_name, time_step):
+    """Remove the checkpoints of steps before ``time_step`` (file_manager.py:29-38)."""
     for p in glob.glob(f"{sim_folder}/chkpts/{sim_name}_*.pickle"):
-        try:
-            t = int(p.split("_")[-1].split(".")[0])
-        except ValueError:
-            continue
-        if t < time_step:
+        t = checkpoint_step(p)
+        if t is not None and t < time_step:
+            os.remove(p)
+
+
+def delete_future_checkpoints(sim_folder, sim_name, time_step):
+    """Remove the checkpoints and wave-function files of steps after
+    ``time_step`` (file_manager.py:11-26), before a restart from it."""
+    for p in glob.glob(f"{sim_folder}/chkpts/{sim_name}_*.pickle"):
+        t = checkpoint_step(p)
+        if t is not None and t > time_step:
+            os.remove(p)
+    for p in glob.glob(f"{sim_folder}/wfns/{sim_name}_*.hdf5*"):
+        t = _wfn_step(p)
+        if t is not None and t > time_step:
             os.remove(p)
 
 
@@ -93,7 +121,7 @@ class SimLogger:
         cv = lambda e: Constants.convert(e, "wavenumbers", to_AU=False)  # noqa: E731
         w = self.fl.write
         w(f"Time step {t}\n")
-        if "rejected" in h:
+        if "pop_before" in h:  # importance sampling: Metropolis rejections of the step's proposals
             tot = h["pop_before"][t]
             w(f"Metropolis rejected {h['rejected'][t]} of {tot} walkers "
               f"({(h['rejected'][t] / max(tot, 1)) * 100:0.2f} %)\n")

@@ -460,6 +460,8 @@ class DMC_Sim:
         self._init_device()
         bounds = [b for b in self._boundaries() if b > t] + [T]
         while t < T:
+            # as pyvibdmc.py:710-711: a checkpoint at step t holds the walkers before step t
+            self.cur_timestep = self._next_step = t
             if t in self._chkpt_step and self.write_files:
                 archive.delete_older_checkpoints(self.output_folder, self.sim_name, t)
                 self._chkpt(t)
@@ -480,7 +482,7 @@ class DMC_Sim:
                 # the failing step moved its walkers into its dst buffer and did not branch
                 self._cur, self._lazy = cur0 ^ (done & 1) ^ 1, False
                 h = self._sync_history(t, int(c.err_step))
-                self.cur_timestep = int(c.err_step)
+                self.cur_timestep = self._next_step = int(c.err_step)
                 self._n_now = int(c.n)
                 raise ValueError(_MASSIVE)
             self._n_now = int(c.n)
@@ -494,6 +496,7 @@ class DMC_Sim:
                 self._harvest(last)
             t = t_end
         self.cur_timestep = T - 1
+        self._next_step = T  # the final checkpoint continues with step T
 
     def run(self):
         """pyvibdmc.py:878-932: propagate, final checkpoint, ZPE, sim_info."""
@@ -542,7 +545,8 @@ class DMC_Sim:
                   _cont_wts=None if "w" not in self._bufs[0] else self._bufs[self._cur]["w"][:n].cpu().numpy(),
                   _masses=np.asarray(self.masses), _atm_nums=self._atm_nums,
                   _rng=self.rng if isinstance(self.rng, str) else "philox32",
-                  _vref=float(self._read_ctrl().vref))
+                  _vref=float(self._read_ctrl().vref),
+                  _next_step=getattr(self, "_next_step", self.cur_timestep))
         return st
 
     def _chkpt(self, t):
@@ -673,22 +677,36 @@ class HostWalkers:
 
 
 def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsamp=None, **kw):
-    """Reload the first checkpoint of ``sim_name`` and extend the run
-    (pyvibdmc.py:949-965).  The Philox streams are keyed by step index, so a
-    restarted run continues the same trajectory."""
+    """Reload the checkpoint of ``sim_name`` and extend the run by
+    ``additional_timesteps`` (pyvibdmc.py:949-965).  A run keeps one
+    checkpoint (older ones are deleted as it goes); if there are several, the
+    latest step is taken.  The run continues with the step after the saved
+    walkers: step t for the checkpoint written before step t, step T for the
+    final checkpoint of a T-step run.  Checkpoints and wave functions of later
+    steps are deleted first, as FileManager.delete_future_checkpoints does.
+    A checkpoint taken inside a descendant-weighting window restarts without
+    that window's parents, so its wave function is not written.
+    The Philox streams are keyed by step index, so a restarted run continues
+    the trajectory of the uninterrupted one."""
     import glob
-    files = sorted(glob.glob(f"{chkpt_folder}/chkpts/{sim_name}_*.pickle"))
+    files = [p for p in glob.glob(f"{chkpt_folder}/chkpts/{sim_name}_*.pickle")
+             if archive.checkpoint_step(p) is not None]
     if not files:
         raise FileNotFoundError(f"no checkpoint for {sim_name} in {chkpt_folder}/chkpts")
-    with open(files[0], "rb") as fh:
+    with open(max(files, key=archive.checkpoint_step), "rb") as fh:
         st = pickle.load(fh)
+    nxt = int(st.get("_next_step", st["cur_timestep"]))
+    archive.delete_future_checkpoints(chkpt_folder, sim_name, nxt)
     T = st["num_timesteps"] + additional_timesteps
+    for k in ("replica_id", "block_threads"):  # the Philox stream and the reduction order of the saved run
+        if k in st:
+            kw.setdefault(k, st[k])
     sim = DMC_Sim(sim_name=st["sim_name"], output_folder=st["output_folder"], weighting=st["weighting"],
                   num_walkers=st["num_walkers"], num_timesteps=T, equil_steps=st["equil_steps"],
                   chkpt_every=st["chkpt_every"], wfn_every=st["wfn_every"], desc_wt_steps=st["desc_wt_time_steps"],
                   atoms=st["atoms"], delta_t=st["delta_t"], potential=potential, masses=list(st["_masses"]),
                   start_structures=st["_coords"], start_cont_wts=st["_cont_wts"], log_every=st["log_every"],
-                  cur_timestep=st["cur_timestep"], cont_wt_thresh=st["cont_wt_thresh"], imp_samp=impsamp,
+                  cur_timestep=nxt, cont_wt_thresh=st["cont_wt_thresh"], imp_samp=impsamp,
                   seed=st["seed"], rng=st["_rng"], **kw)
     n = len(st["_vref_vs_tau"])
     sim._vref_vs_tau[:n] = st["_vref_vs_tau"]

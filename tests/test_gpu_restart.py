@@ -1,0 +1,63 @@
+"""Checkpoint and restart (pyvibdmc.py:892-965): a run written to disk,
+reloaded with dmc_restart and extended, follows the trajectory of the same
+run done in one go.  The deviates are keyed by (seed, step, walker), so the
+populations and walkers agree bit for bit; vref agrees to 1e-12 Eh (the
+restart recomputes the first vref from the saved walkers, which sums them in
+another order)."""
+import numpy as np
+import pytest
+
+import oracle
+import pyvibdmc_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+T = 60
+
+
+def _kw(tmp_path, name, nsteps, **kw):
+    p, m = oracle.h2o_config()
+    x0 = oracle.h2o_equilibrium(p)[None] + 0.08 * oracle.InjectedNoise(11).standard_normal((3000, 3, 3))
+    return dict(sim_name=name, output_folder=str(tmp_path / name), num_walkers=3000, num_timesteps=nsteps,
+                equil_steps=10 ** 6, wfn_every=10 ** 6, desc_wt_steps=1, atoms=["O", "H", "H"], masses=m,
+                delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=7, **kw)
+
+
+def _same(c, a):
+    np.testing.assert_array_equal(c._pop_vs_tau, a._pop_vs_tau)
+    np.testing.assert_allclose(c._vref_vs_tau, a._vref_vs_tau, rtol=0, atol=1e-12)
+    assert np.array_equal(c.walkers, a.walkers)
+
+
+@pytest.fixture(scope="module")
+def whole(tmp_path_factory):
+    a = pg.DMC_Sim(**_kw(tmp_path_factory.mktemp("a"), "a", T, chkpt_every=10 ** 6, write_files=False))
+    a.run()
+    return a
+
+
+def test_restart_after_a_finished_run(tmp_path, whole):
+    b = pg.DMC_Sim(**_kw(tmp_path, "b", 25, chkpt_every=10 ** 6, write_files=True))
+    b.run()
+    c = pg.dmc_restart(pg.h2o_local_mode(), str(tmp_path / "b"), "b", additional_timesteps=T - 25)
+    assert c.cur_timestep == 25 and c.num_timesteps == T
+    c.run()
+    _same(c, whole)
+
+
+def test_restart_from_a_checkpoint_of_an_interrupted_run(tmp_path, whole, monkeypatch):
+    b = pg.DMC_Sim(**_kw(tmp_path, "b", T, chkpt_every=20, write_files=True))
+    run_steps = b._run_steps
+
+    def crash_at_40(n):  # the host side fails before step 40 (after the checkpoint of step 40)
+        if b.cur_timestep == 40:
+            raise RuntimeError("interrupted")
+        return run_steps(n)
+
+    monkeypatch.setattr(b, "_run_steps", crash_at_40)
+    with pytest.raises(RuntimeError, match="interrupted"):
+        b.run()
+    c = pg.dmc_restart(pg.h2o_local_mode(), str(tmp_path / "b"), "b")
+    assert c.cur_timestep == 40
+    c.run()
+    _same(c, whole)
