@@ -85,11 +85,12 @@ extern "C" const char* gbdmc_last_error(void) { return g_err; }
 
 extern "C" int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x, int64_t n, int64_t ld, double* v,
                               double* grad, void* stream) {
+  // no walkers: nothing is read or written (an empty array may have no address)
+  if (pes && n == 0 && ld >= 0) return GBDMC_OK;
   if (!pes || !x || !v || n < 0 || ld < n) {
     set_error("gbdmc_pes_eval: invalid arguments (n=%lld ld=%lld)", (long long)n, (long long)ld);
     return GBDMC_ERR_ARG;
   }
-  if (n == 0) return GBDMC_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const int A = pes->natoms;
   switch (pes->kind) {
@@ -133,11 +134,11 @@ extern "C" int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x, int64_t n
 
 extern "C" int gbdmc_trial_eval(const gbdmc_trial_t* t, const double* x, int64_t n, int64_t ld, double* psi,
                                 double* d1, double* d2, void* stream) {
+  if (t && n == 0 && ld >= 0) return GBDMC_OK;  // no walkers: nothing is read or written
   if (!t || !x || !psi || n < 0 || ld < n) {
     set_error("gbdmc_trial_eval: invalid arguments");
     return GBDMC_ERR_ARG;
   }
-  if (n == 0) return GBDMC_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const int G = eval_grid(n);
   const int A = t->natoms;

@@ -35,8 +35,8 @@ def default_device():
 def to_soa(cds, device, dtype=torch.float64):
     """(N, A, 3) host or device array -> contiguous (3A, N) device tensor."""
     t = torch.as_tensor(np.asarray(cds) if not torch.is_tensor(cds) else cds, dtype=dtype)
-    n = t.shape[0]
-    return t.reshape(n, -1).t().contiguous().to(device)
+    n, m = t.shape[0], int(np.prod(t.shape[1:]))  # explicit width: N may be 0
+    return t.reshape(n, m).t().contiguous().to(device)
 
 
 def from_soa(x, n, natoms):

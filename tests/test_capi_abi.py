@@ -53,3 +53,7 @@ def test_error_reporting_without_gpu():
     rc = L.gbdmc_pes_eval(None, None, 1, 1, None, None, None)
     assert rc == _capi.ERR_ARG
     assert b"invalid" in L.gbdmc_last_error()
+    # no walkers: nothing to read, so no buffers are needed and no kernel runs
+    pes = _capi.PES(kind=_capi.PES_H2O_LM, natoms=3)
+    assert L.gbdmc_pes_eval(ctypes.byref(pes), None, 0, 0, None, None, None) == _capi.OK
+    assert L.gbdmc_pes_eval(ctypes.byref(pes), None, 2, 1, None, None, None) == _capi.ERR_ARG  # ld < n

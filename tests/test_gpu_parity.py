@@ -42,6 +42,18 @@ def test_h2o_pes_matches_oracle(n):
     np.testing.assert_allclose(v, oracle.pes_h2o_lm(x, p), rtol=0, atol=1e-12)
 
 
+def test_getpot_keeps_the_plugin_contract():
+    # potential_manager.py:71-99: (N, A, 3) bohr -> (N,) float64 hartree, or (v, seconds) with timeit
+    pot = pg.h2o_local_mode()
+    x = geoms(100)
+    v = pot.getpot(x)
+    v2, secs = pot.getpot(x, timeit=True)
+    assert v.shape == (100,) and v.dtype == np.float64
+    assert np.array_equal(v, v2) and secs >= 0.0
+    assert pot.getpot(np.zeros((0, 3, 3))).shape == (0,)  # no walkers
+    assert vars(pot)["kind"] == "h2o_local_mode"  # the reference engine logs vars(potential)
+
+
 def test_ho_and_dimer_pes_match_oracle():
     ho = oracle.ho_config()
     x1 = 0.3 * oracle.InjectedNoise(5).standard_normal((777, 1, 3))

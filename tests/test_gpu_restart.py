@@ -61,3 +61,34 @@ def test_restart_from_a_checkpoint_of_an_interrupted_run(tmp_path, whole, monkey
     assert c.cur_timestep == 40
     c.run()
     _same(c, whole)
+
+
+@pytest.mark.parametrize("weighting", ["discrete", "continuous"])
+def test_run_writes_the_reference_files(tmp_path, weighting):
+    """sim_info, wave functions, checkpoint and log under output_folder, with
+    the reference's names and keys (pyvibdmc.py:856-872, 897-922)."""
+    import os
+
+    from pyvibdmc_gb300 import archive
+
+    kw = _kw(tmp_path, "f", 30, chkpt_every=15, write_files=True)
+    kw.update(equil_steps=10, wfn_every=10, desc_wt_steps=5, weighting=weighting)
+    s = pg.DMC_Sim(**kw)
+    s.run()
+    out = str(tmp_path / "f")
+    info = archive.load_h5(f"{out}/f_sim_info.hdf5")
+    assert sorted(info) == ["atomic_masses", "atomic_nums", "pop_vs_tau", "vref_vs_tau"]
+    np.testing.assert_array_equal(info["vref_vs_tau"][:, 0], np.arange(30) * 10.0)
+    np.testing.assert_array_equal(info["vref_vs_tau"][:, 1], s._vref_vs_tau)
+    np.testing.assert_array_equal(info["pop_vs_tau"][:, 1], s._pop_vs_tau)
+    assert [w["start"] for w in s.wfns] == [10, 20]
+    keys = ["coords", "desc_wts"] + (["parent_wts"] if weighting == "continuous" else [])
+    for w in s.wfns:
+        f = archive.load_h5(f"{out}/wfns/f_wfn_{w['start']}ts.hdf5")
+        assert sorted(f) == sorted(keys)
+        for k in keys:
+            np.testing.assert_array_equal(f[k], w[k])
+        if weighting == "discrete":  # every walker at the window's end descends from one parent
+            assert w["desc_wts"].sum() == s._pop_vs_tau[w["start"] + 4]
+    assert sorted(os.listdir(f"{out}/chkpts")) == ["f_29.pickle"]
+    assert "Simulation has finished." in open(f"{out}/f_log.txt").read()

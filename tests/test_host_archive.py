@@ -94,6 +94,21 @@ def test_potential_must_be_a_gpu_potential():
                    write_files=False)
 
 
+def test_walker_layout_round_trip_and_empty_input():
+    from pyvibdmc_gb300.potentials import from_soa, to_soa
+    x = np.arange(2 * 3 * 3, dtype=np.float64).reshape(2, 3, 3)
+    s = to_soa(x, "cpu")
+    assert s.shape == (9, 2) and s[4, 1].item() == x[1, 1, 1]  # component 3*atom + dim of walker i
+    assert np.array_equal(from_soa(s, 2, 3), x)
+    e = to_soa(np.zeros((0, 3, 3)), "cpu")
+    assert e.shape == (9, 0) and from_soa(e, 0, 3).shape == (0, 3, 3)
+
+
+def test_getpot_checks_the_walker_shape_first():
+    with pytest.raises(ValueError, match="cds must be"):
+        pg.h2o_local_mode().getpot(np.zeros((5, 2, 3)))
+
+
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the behaviour without a CUDA device")
 def test_engine_fails_loudly_without_cuda():
     with pytest.raises(RuntimeError, match="CUDA device"):
