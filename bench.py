@@ -133,12 +133,13 @@ def _pool_pes_dimer(chunk):
     return oracle.pes_dimer(chunk, p)
 
 
-def cpu_reference_rate(n_walkers, steps, cores, system="h2o"):
+def cpu_reference_rate(n_walkers, steps, cores, system="h2o", min_s=0.0, max_steps=100000):
     """Oracle port of DMC_Sim.propagate on the host: walker-steps/s of the
     local-mode water (system "h2o") or the water dimer ("dimer").  With
     cores > 1 the PES is sharded over a spawn pool the way
     potential_manager.Potential.getpot does (np.array_split, pool.map,
-    np.concatenate)."""
+    np.concatenate).  Runs at least `steps` steps and at least `min_s`
+    seconds (at most `max_steps` steps); returns (rate, seconds, steps)."""
     import oracle
     if system == "dimer":
         p, m = oracle.dimer_config()
@@ -161,7 +162,7 @@ def cpu_reference_rate(n_walkers, steps, cores, system="h2o"):
         sim.run(3)  # warm-up (step 0 potential + vref)
         pops = []
         t0 = time.perf_counter()
-        for _ in range(steps):
+        while len(pops) < max_steps and (len(pops) < steps or time.perf_counter() - t0 < min_s):
             pops.append(len(sim.x))
             _single_step(sim)
         dt = time.perf_counter() - t0
@@ -169,7 +170,7 @@ def cpu_reference_rate(n_walkers, steps, cores, system="h2o"):
         if pool is not None:
             pool.close()
             pool.join()
-    return float(np.sum(pops)) / dt, dt
+    return float(np.sum(pops)) / dt, dt, len(pops)
 
 
 def _single_step(sim):
@@ -190,13 +191,13 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    rate1, t1 = cpu_reference_rate(N_WALKERS, max(args.steps // 10, 20), 1)
-    best, kind_cores = rate1, 1
+    rate1, t1, k1 = cpu_reference_rate(N_WALKERS, max(args.steps // 10, 20), 1, min_s=10.0)
+    best, kind_cores, sample = rate1, 1, f"{k1} steps in {t1:.1f} s"
     if cores > 1:
         try:
-            ratep, tp = cpu_reference_rate(N_WALKERS, max(args.steps // 20, 10), cores)
+            ratep, tp, kp = cpu_reference_rate(N_WALKERS, max(args.steps // 20, 10), cores, min_s=10.0)
             if ratep > best:
-                best, kind_cores = ratep, cores
+                best, kind_cores, sample = ratep, cores, f"{kp} steps in {tp:.1f} s"
         except Exception:
             pass
     line = {"impl": "reference", "metric": METRIC, "value": best, "unit": UNIT, "n_gpus": args.gpus,
@@ -206,7 +207,7 @@ def run_reference(args):
             "cpu_baseline": {"value": best, "unit": UNIT, "cores": kind_cores, "kind": "port",
                              "sample": f"oracle restatement of DMC_Sim.propagate (plain, discrete), "
                                        f"{N_WALKERS} walkers, numpy; best of 1-process and "
-                                       f"{cores}-process PES pool"},
+                                       f"{cores}-process PES pool ({sample})"},
             "e2e": {"value": best, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -387,10 +388,10 @@ def run_ours(args):
         except Exception as exc:  # the headline line must still print
             line["extras"] = {"error": repr(exc)[:300]}
     if rank == 0 and world == 1:
-        rate, secs = cpu_reference_rate(N_WALKERS, 150, 1)
+        rate, secs, ksteps = cpu_reference_rate(N_WALKERS, 20, 1, min_s=10.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": f"oracle restatement of DMC_Sim.propagate (plain, discrete), "
-                                          f"{N_WALKERS} walkers x 150 steps, numpy, {secs:.1f} s"}
+                                          f"{N_WALKERS} walkers x {ksteps} steps, numpy, {secs:.1f} s"}
     line["clocks"] = clk.summary()
     if rank == 0:
         print(json.dumps(line), flush=True)
