@@ -856,12 +856,12 @@ extern "C" int gbdmc_dimer_features(const double* x, int64_t ld, int64_t n, cons
 
 extern "C" int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x, int64_t ld, int64_t n, double* v,
                                 int32_t* outside, int32_t* status, void* stream) {
+  if (valid_net(net) && n == 0 && ld >= 0) return GBDMC_OK;  // no walkers: nothing is read or written
   if (!valid_net(net) || !x || !v || n < 0 || ld < n || (net->engine == 1 && !status) || net->engine < 0 ||
       net->engine > 1) {
     set_error("gbdmc_mlp_energy: invalid arguments");
     return GBDMC_ERR_ARG;
   }
-  if (n == 0) return GBDMC_OK;
   if (net->engine == 1) return launch_mlp_tc_energy(*net, x, ld, n, v, outside, status, (cudaStream_t)stream);
   int rc = set_mlp_smem((const void*)k_mlp_energy<float>);
   if (rc) return rc;
