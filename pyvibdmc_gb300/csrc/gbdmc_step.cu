@@ -751,6 +751,12 @@ int build_table(const gbdmc_sim_t& S, const gbdmc_replica_t* reps, int nrep, Rep
                 (long long)R.cap, (long long)R.n0, (long long)S.ld);
       return GBDMC_ERR_ARG;
     }
+    for (int q = 0; q < r; ++q) {  // replicas own disjoint slot ranges (their kernels write them concurrently)
+      if (R.off < reps[q].off + reps[q].cap && reps[q].off < R.off + R.cap) {
+        set_error("%s: replicas %d and %d overlap", what, q, r);
+        return GBDMC_ERR_ARG;
+      }
+    }
     T.tile_off[r] = (int32_t)tiles;
     T.off[r] = R.off;
     T.cap[r] = R.cap;

@@ -57,3 +57,26 @@ def test_error_reporting_without_gpu():
     pes = _capi.PES(kind=_capi.PES_H2O_LM, natoms=3)
     assert L.gbdmc_pes_eval(ctypes.byref(pes), None, 0, 0, None, None, None) == _capi.OK
     assert L.gbdmc_pes_eval(ctypes.byref(pes), None, 2, 1, None, None, None) == _capi.ERR_ARG  # ld < n
+
+
+def test_replica_table_is_checked_before_any_launch():
+    """Bad replica tables are refused on the host (no pointer is touched)."""
+    from pyvibdmc_gb300 import _capi
+    L = _capi.load()
+    s = _capi.Sim(natoms=3, weighting=_capi.DISCRETE, ld=1000, n0=100, block_threads=64)
+    s.pes.kind, s.pes.natoms = _capi.PES_H2O_LM, 3
+    s.trial.kind, s.trial.natoms = _capi.TRIAL_NONE, 3
+    w = _capi.Walkers(x=16, v=16, idx=16)
+    fake = ctypes.c_void_p(16)
+
+    def init(pairs):
+        reps = (_capi.Replica * len(pairs))()
+        for k, (off, cap) in enumerate(pairs):
+            reps[k].off, reps[k].cap, reps[k].n0 = off, cap, 50
+        return L.gbdmc_batch_init(ctypes.byref(s), reps, len(pairs), ctypes.byref(w), fake, fake, None)
+
+    assert init([(0, 400), (300, 400)]) == _capi.ERR_ARG
+    assert b"overlap" in L.gbdmc_last_error()
+    assert init([(0, 400), (600, 500)]) == _capi.ERR_ARG  # past ld
+    assert b"bad off/cap" in L.gbdmc_last_error()
+    assert init([(0, 10)] * 65) == _capi.ERR_CAPACITY  # more than 64 replicas
