@@ -167,7 +167,8 @@ typedef struct {
 } gbdmc_sim_t;
 
 /* One replica of a batched ensemble: its walkers occupy slots
- * [off, off + cap) of every SoA array of the batch. */
+ * [off, off + cap) of every SoA array of the batch.  The ranges of one
+ * batch must not overlap and must lie inside [0, sim->ld). */
 #define GBDMC_MAX_REPLICAS 64
 typedef struct {
   int64_t off;     /* first slot                                    */
@@ -192,11 +193,13 @@ const char* gbdmc_last_error(void);
 /* Bytes of device scratch the step calls need for capacity ld (block partials). */
 size_t gbdmc_scratch_bytes(int64_t ld);
 
-/* V(x) for n walkers; grad_dev (SoA like x, may be NULL) receives dV/dx. */
+/* V(x) for n walkers; grad_dev (SoA like x, may be NULL) receives dV/dx.
+ * n = 0 reads and writes nothing (the buffers may then be NULL). */
 int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x_dev, int64_t n, int64_t ld,
                    double* v_dev, double* grad_dev, void* stream);
 
-/* psi, (dpsi/dx)/psi and (d2psi/dx2)/psi per Cartesian component. */
+/* psi, (dpsi/dx)/psi and (d2psi/dx2)/psi per Cartesian component.
+ * n = 0 reads and writes nothing (the buffers may then be NULL). */
 int gbdmc_trial_eval(const gbdmc_trial_t* trial, const double* x_dev, int64_t n, int64_t ld,
                      double* psi_dev, double* d1_dev, double* d2_dev, void* stream);
 
@@ -221,7 +224,9 @@ int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbd
  * one launch per phase (persistent grid over all replicas' tiles).  sim->ld
  * is the total slot count, sim->n0 is ignored (per replica in reps), ctrl_dev
  * holds nrep control blocks and the history arrays are replica-major with
- * stride sim->hist.len.  Scratch: gbdmc_batch_scratch_bytes(reps, nrep). */
+ * stride sim->hist.len.  Scratch: gbdmc_batch_scratch_bytes(reps, nrep),
+ * laid out over the table's slot extent (the largest off + cap), so a call
+ * may step a subset of a larger batch with a scratch sized for that subset. */
 int gbdmc_batch_init(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
                      const gbdmc_walkers_t* w, gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
 int gbdmc_batch_step(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
@@ -359,7 +364,7 @@ int gbdmc_dimer_features(const double* x_dev, int64_t ld, int64_t n, const float
                          float* tang_dev, float* et_dev, void* stream);
 /* Surrogate energies of n walkers (fp32 SoA [18][ld]); outside_dev[i] = 1 for walkers outside the training box
  * (may be NULL; not cleared).  With net->engine == 1 (tcgen05) status_dev (device int, required) is set to 1 if a
- * bounded wait for the tensor cores gave up. */
+ * bounded wait for the tensor cores gave up.  n = 0 reads and writes nothing. */
 int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int64_t n, double* v_dev,
                      int32_t* outside_dev, int32_t* status_dev, void* stream);
 /* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
