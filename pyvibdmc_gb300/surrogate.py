@@ -16,7 +16,7 @@
   audited differences are accumulated as the surrogate's error estimate.  With
   ``bias_control`` = b > 0 the mean audited error of each step updates an
   exponential moving average c <- (1-b) c + b <V_nn - V>, and the surrogate
-  energies of the next step are V_nn - c: the analytic PES, which judges the
+  energies of the next step are V_nn - c: the analytic PES, which audits the
   surrogate, also removes its mean error on the current walker distribution.
 """
 import ctypes as C
