@@ -2,7 +2,7 @@
 
 Run from the repository root with the reference checkout available::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [fixture,fixture,...]
 
 What it does:
 
@@ -167,7 +167,7 @@ def run_reference(pv, out_dir, name, x0, atoms, masses, dt, nsteps, pes, seed, w
     return out
 
 
-def main(ref_path):
+def main(ref_path, only=None):
     pv = _import_reference(ref_path)
     tmp = tempfile.mkdtemp(prefix="gbdmc_golden_")
     fixtures = {}
@@ -196,6 +196,20 @@ def main(ref_path):
     r = run_reference(pv, tmp, "h2o_cont", x0, ["O", "H", "H"], masses, 10.0, 40, pes, seed=3,
                       weighting="continuous", thresh=0.2)
     fixtures["h2o_continuous"] = dict(x0=x0, seed=3, dt=10.0, nsteps=40, thresh=0.2, **r)
+
+    # --- continuous weights with both thresholds, one step.  The reference picks the
+    # walkers to replace above the upper threshold with np.argpartition, whose order is
+    # unspecified, so this fixture pins the branched walkers as a set.  The thresholds are
+    # the 2 % and 90 % quantiles of the step's weights (a few walkers below, and more
+    # above than the lower branching halves).
+    n = 192
+    x0 = eq[None] + 0.05 * oracle.InjectedNoise(707).standard_normal((n, 3, 3))
+    probe = oracle.OracleDMC(x0, masses, 10.0, pes, oracle.InjectedNoise(7), weighting="continuous",
+                             cont_wt_thresh=[1e-300, 1e300]).run(1)
+    thr = [float(q) for q in np.quantile(probe.w, [0.02, 0.9])]
+    r = run_reference(pv, tmp, "h2o_cont_upper", x0, ["O", "H", "H"], masses, 10.0, 1, pes, seed=7,
+                      weighting="continuous", thresh=thr)
+    fixtures["h2o_cont_upper"] = dict(x0=x0, seed=7, dt=10.0, nsteps=1, thresh=np.array(thr), **r)
 
     # --- config-3 family: importance sampling with the Gaussian internal trial
     alpha, qe = oracle.h2o_trial_config(p)
@@ -236,10 +250,14 @@ def main(ref_path):
     fixtures["h2o_metropolis"] = dict(xa=xa, xb=xb, met=met, ke=ke, masses=np.asarray(masses))
 
     for name, d in fixtures.items():
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
         print(f"wrote {path} ({os.path.getsize(path)} bytes)")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # optional second argument: comma-separated fixture names to write (default: all)
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference",
+         set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)

@@ -62,6 +62,31 @@ def test_h2o_continuous_matches_reference():
     assert sum(c[0] for c in sim.counters) > 0  # branching happened
 
 
+def _rows(x, v, w):
+    r = np.column_stack([x.reshape(len(x), -1), v, w])
+    return r[np.lexsort(r.T[::-1])]
+
+
+def test_h2o_continuous_upper_threshold_matches_reference_as_a_set():
+    # the reference orders the walkers it replaces above the upper threshold by
+    # np.argpartition (unspecified); the oracle takes them in ascending slot order, so
+    # the branched walkers agree as a set of (x, V, w) rows
+    g = load("h2o_cont_upper")
+    p, m = oracle.h2o_config()
+    pes = lambda c: oracle.pes_h2o_lm(c, p)  # noqa: E731
+
+    def run(thresh):
+        return oracle.OracleDMC(g["x0"], m, float(g["dt"]), pes, oracle.InjectedNoise(int(g["seed"])),
+                                weighting="continuous", cont_wt_thresh=thresh).run(int(g["nsteps"]))
+
+    sim = run(list(g["thresh"]))
+    assert np.array_equal(_rows(sim.x, sim.v, sim.w), _rows(g["x_final"], g["v_final"], g["w_final"]))
+    np.testing.assert_allclose(sim.vref_hist, g["vref"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sim.pop_hist, g["pop"], rtol=1e-14, atol=0)
+    low = run(float(g["thresh"][0]))  # the upper threshold changed the walkers
+    assert not np.array_equal(_rows(low.x, low.v, low.w), _rows(sim.x, sim.v, sim.w))
+
+
 def test_h2o_importance_sampling_matches_reference():
     g = load("h2o_is")
     p, m = oracle.h2o_config()
