@@ -473,3 +473,23 @@ def test_host_resident_step_failure_keeps_the_host_walkers():
     with pytest.raises(ValueError, match="Massive walker"):
         hw.run(4)
     assert torch.equal(hw.host["x"][:, :100], before)
+
+
+def test_engine_continuous_upper_threshold_vs_oracle():
+    # both thresholds (pyvibdmc.py:432-454): the walkers replaced above the upper
+    # threshold are taken in ascending slot order, as the oracle does (the reference's
+    # np.argpartition order is unspecified; the oracle is pinned on it as a set)
+    g = load("h2o_cont_upper")
+    p, m = oracle.h2o_config()
+    thr = [float(t) for t in g["thresh"]]
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pg.h2o_local_mode(), int(g["seed"]), int(g["nsteps"]),
+               weighting="continuous", cont_wt_thresh=thr)
+    sim.run()
+    ref = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), weighting="continuous",
+                           cont_wt_thresh=thr).run(int(g["nsteps"]))
+    x, w = sim.walkers
+    assert np.array_equal(x, ref.x)
+    np.testing.assert_allclose(w, ref.w, rtol=1e-12)
+    np.testing.assert_allclose(sim._vref_vs_tau, ref.vref_hist, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sim._pop_vs_tau, ref.pop_hist, rtol=1e-13)
