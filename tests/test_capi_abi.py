@@ -80,3 +80,38 @@ def test_replica_table_is_checked_before_any_launch():
     assert init([(0, 400), (600, 500)]) == _capi.ERR_ARG  # past ld
     assert b"bad off/cap" in L.gbdmc_last_error()
     assert init([(0, 10)] * 65) == _capi.ERR_CAPACITY  # more than 64 replicas
+
+
+def _prototypes():
+    """name -> list of parameter declarations, from every header in include/."""
+    out = {}
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+        for m in re.finditer(r"\b(gbdmc_\w+)\s*\(([^;{]*?)\)\s*;", text):
+            params = [p.strip() for p in m.group(2).split(",")]
+            out[m.group(1)] = [] if params == ["void"] else params
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every function the Python host binds has the header's parameter count,
+    and pointers where the header has pointers."""
+    from pyvibdmc_gb300 import _capi
+    L = _capi.load()
+    protos = _prototypes()
+    scalars = (ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_double, ctypes.c_uint32, ctypes.c_size_t,
+               ctypes.c_int)
+    checked = 0
+    for name, params in protos.items():
+        fn = getattr(L, name)
+        if fn.argtypes is None:
+            continue
+        assert len(fn.argtypes) == len(params), f"{name}: ctypes {len(fn.argtypes)} args, header {len(params)}"
+        for decl, ct in zip(params, fn.argtypes):
+            if "*" in decl:
+                assert ct not in scalars, f"{name}: '{decl}' bound as {ct.__name__}"
+            else:
+                assert ct in scalars, f"{name}: '{decl}' bound as {ct.__name__}"
+        checked += 1
+    assert checked >= 30
