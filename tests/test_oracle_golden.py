@@ -87,6 +87,20 @@ def test_h2o_continuous_upper_threshold_matches_reference_as_a_set():
     assert not np.array_equal(_rows(low.x, low.v, low.w), _rows(sim.x, sim.v, sim.w))
 
 
+def test_continuous_replacement_rules_by_hand():
+    # pyvibdmc.py:340-356, 432-454 with the oracle's order above the upper threshold:
+    # below `lower` in slot order, then the n_up smallest weights in slot order, each
+    # replaced by a copy of the current largest weight (first slot on ties), both halved
+    x = np.arange(5.0)[:, None, None] * np.ones((5, 1, 3))
+    st = dict(x=x, v=np.arange(5.0), w=np.array([0.1, 3.0, 0.5, 3.0, 2.0]), vref=0.0)
+    nb, wmax, wmin = oracle.continuous_update_and_branch(st, 0.0, 0.2, 1.4)
+    # slot 0 <- 1 (w 1.5 each); then n_up = 4 of {1.5, 1.5, 3, 2}: slots 0, 1, 2, 4 <- 3, 4, 0, 3
+    assert (nb, wmax, wmin) == (5, 1.0, 0.75)
+    assert np.array_equal(st["w"], [0.75, 1.0, 0.75, 0.75, 0.75])
+    assert np.array_equal(st["x"][:, 0, 0], [3.0, 4.0, 3.0, 3.0, 3.0])
+    assert np.array_equal(st["v"], [3.0, 4.0, 3.0, 3.0, 3.0])
+
+
 def test_h2o_importance_sampling_matches_reference():
     g = load("h2o_is")
     p, m = oracle.h2o_config()
