@@ -1,6 +1,8 @@
 """bench.py's host side without a GPU: the timed CPU baseline loop is the
-oracle's step, and the clock record is read the way the timing rules need
-(median SM clock under load, maximum clock, throttle reasons seen)."""
+oracle's step, the clock record is read the way the timing rules need
+(median SM clock under load, maximum clock, throttle reasons seen), and the
+blocking error behind the ZPE error bars recovers the known standard error
+of a correlated series."""
 import numpy as np
 
 import bench
@@ -39,3 +41,21 @@ def test_clock_record_summary(tmp_path):
         s = c.summary()
     assert s == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
     assert bench.ClockSampler(0).summary()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_blocking_error_of_a_correlated_series():
+    # AR(1), phi = 0.9: the standard error of the mean is sqrt(var * tau / n) with
+    # var = 1 / (1 - phi^2) and tau = (1 + phi) / (1 - phi) = 19, 4.4x the naive iid value
+    import pyvibdmc_gb300 as pg
+    phi, n = 0.9, 200000
+    e = np.random.default_rng(3).standard_normal(n)
+    x = np.empty(n)
+    x[0] = e[0]
+    for t in range(1, n):
+        x[t] = phi * x[t - 1] + e[t]
+    mean, err = pg.blocking_error(x, 20)
+    true = np.sqrt(1 / (1 - phi ** 2) * (1 + phi) / (1 - phi) / n)
+    assert abs(mean) < 5 * true
+    assert 0.5 * true < err < 1.5 * true
+    assert err > 2.5 * x.std() / np.sqrt(n)
+    assert pg.blocking_error([1.0, 2.0, 3.0])[0] == 2.0  # short series: two blocks
