@@ -262,7 +262,8 @@ class NN_Potential_GPU:
 def harvest_training_data(potential, num_walkers, nsteps, every, start, masses, delta_t=10.0, seed=0, equil=0):
     """Plain FP64 DMC of `potential` (the analytic dimer); every `every` steps
     after `equil` the walkers, their energies and adjoint gradients are kept
-    on the device.  Returns x (18, M), v (M,), g (18, M) fp64 tensors."""
+    on the device.  Returns x (18, M), v (M,), g (18, M) fp64 tensors and the
+    FP64 simulation that produced them."""
     from .engine import DMC_Sim
     xs, vs, gs = [], [], []
 
