@@ -127,3 +127,26 @@ def test_documented_python_snippets_parse():
             compile(block, f"{doc}[{k}]", "exec")
             n += 1
     assert n >= 4
+
+
+# DMC_Sim keywords, defaults and order of pyvibdmc.py:67-98
+REFERENCE_KEYWORDS = [
+    ("sim_name", "DMC_Sim"), ("output_folder", "exSimResults"), ("weighting", "discrete"), ("num_walkers", 10000),
+    ("num_timesteps", 20000), ("equil_steps", 2000), ("chkpt_every", 1000), ("wfn_every", 1000),
+    ("desc_wt_steps", 100), ("atoms", []), ("delta_t", 1), ("potential", None), ("masses", None),
+    ("start_structures", None), ("start_cont_wts", None), ("branch_every", 1), ("log_every", 1),
+    ("cur_timestep", 0), ("cont_wt_thresh", None), ("imp_samp", None), ("imp_samp_oned", False),
+    ("second_impsamp_displacement", False), ("excited_state_imp_samp", False), ("adiabatic_dmc", None),
+    ("fixed_node", None), ("DEBUG_alpha", None), ("DEBUG_save_desc_wt_tracker", None),
+    ("DEBUG_save_training_every", None), ("DEBUG_save_before_bod", False), ("DEBUG_mass_change", None)]
+
+
+def test_dmc_sim_keeps_the_reference_constructor():
+    import inspect
+    params = list(inspect.signature(pg.DMC_Sim.__init__).parameters.values())[1:]
+    positional = [p for p in params if p.kind == p.POSITIONAL_OR_KEYWORD]
+    assert [(p.name, p.default) for p in positional] == REFERENCE_KEYWORDS
+    assert all(p.kind == p.KEYWORD_ONLY for p in params[len(positional):])  # extras only by keyword
+    for name in ("DMC_Sim", "dmc_restart", "Constants", "Potential_GPU", "ImpSampManager_GPU", "NN_Potential_GPU",
+                 "HarmonicAnalysis", "InitialConditioner"):
+        assert hasattr(pg, name), name
