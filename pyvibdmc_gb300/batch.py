@@ -13,7 +13,6 @@ Each replica is the same simulation ``DMC_Sim`` would run with
 same tiles), so a replica can be re-run on its own and compared step by step.
 """
 import ctypes as C
-import time
 
 import numpy as np
 import torch

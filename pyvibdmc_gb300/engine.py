@@ -17,9 +17,7 @@ that supplies the deviates on the host in the reference's call order),
 ``DEBUG_save_training_every`` steps), ``replica_id`` (Philox stream) and
 ``block_threads`` (tile width; 0 = chosen from the population).
 """
-import copy
 import ctypes as C
-import os
 import pickle
 import time
 

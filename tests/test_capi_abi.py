@@ -4,7 +4,6 @@ import ctypes
 import os
 import re
 
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
