@@ -282,6 +282,18 @@ size_t gbdmc_sim_step_static_max_ld(void);
 int gbdmc_desc_weights(const int32_t* who_dev, const double* w_dev, const int64_t* n_dev,
                        int64_t n_parent, double* desc_dev, void* stream);
 
+/* np.argpartition(w, kth) (pyvibdmc.py:443-445, the walkers replaced above
+ * the upper continuous-weight threshold) in the order of NumPy's portable
+ * introselect, run by one 1024-thread block as inside the continuous-weight
+ * step: perm_dev (n int32) receives the permutation, whose first kth entries
+ * are the kth smallest weights in NumPy's order; for kth >= 3 the whole
+ * permutation is NumPy's (for kth < 3 the entries from kth on may differ).
+ * lpos_dev (n int32) and flags_dev (n bytes) are scratch.  0 <= kth < n.
+ * perm_dev[0] = -1 reports the (unreachable below 5^16 elements) overflow of
+ * the nested median-of-medians stack. */
+int gbdmc_argpartition(const double* w_dev, int64_t n, int64_t kth, int32_t* perm_dev, int32_t* lpos_dev,
+                       uint8_t* flags_dev, void* stream);
+
 /* Start of a descendant-weighting window: who_dev[i] = i for i < *n_dev
  * (pyvibdmc.py:739-745, `_who_from = np.arange(len(coords))`). */
 int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);

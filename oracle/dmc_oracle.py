@@ -21,7 +21,7 @@ __all__ = [
     "pes_ho", "pes_h2o_lm", "pes_dimer", "grad_ho", "grad_h2o_lm", "grad_dimer",
     "h2o_internals", "TrialH2OGauss", "TrialHOGauss", "TrialDimerGauss", "finite_diff",
     "metropolis", "local_kin", "move_randomly", "birth_or_death_discrete",
-    "continuous_update_and_branch", "calc_vref", "calc_desc_wts",
+    "continuous_update_and_branch", "argpartition_introselect", "introselect_adversary", "calc_vref", "calc_desc_wts",
     "OracleDMC", "ho_config", "h2o_config", "h2o_equilibrium", "h2o_trial_config", "dimer_config",
     "dimer_equilibrium", "inv_dist_descriptors",
 ]
@@ -412,12 +412,202 @@ def birth_or_death_discrete(pots, vref, dt, rand_nums, pop_hi):
     return np.repeat(np.arange(len(counts)), counts), counts, births, deaths
 
 
+def _msb(n):
+    """npy_get_msb: index of the highest set bit of n > 0."""
+    d = 0
+    while n > 1:
+        n >>= 1
+        d += 1
+    return d
+
+
+def argpartition_introselect(v, kth, less=None, stats=None):
+    """``np.argpartition(v, kth)`` as NumPy's portable introselect computes it.
+
+    The reference picks the walkers to replace above the upper weight
+    threshold with ``np.argpartition(w, k)[:k]`` (pyvibdmc.py:443-445), so the
+    ORDER of that list -- which decides which walker is cloned into which slot
+    by the sequential ``_branch`` -- is NumPy's.  NumPy (numpy/_core/src/
+    npysort/selection.cpp, functions ``introselect_``, ``dumb_select_``,
+    ``median3_swap_``, ``unguarded_partition_``, ``median_of_median5_`` and
+    ``median5_``; same algorithm in NumPy 1.x and 2.x) runs this introselect
+    on every platform without a SIMD select kernel, e.g. aarch64, and on x86
+    when the x86-simd-sort dispatch targets are switched off
+    (``NPY_DISABLE_CPU_FEATURES``); on x86 with AVX2/AVX-512 NumPy 2.x
+    substitutes a SIMD select whose order differs.  The algorithm:
+
+    * kth - low < 3: selection sort of positions 0..kth (first minimum wins);
+    * kth == num - 1: swap the last maximum into the last position;
+    * otherwise quickselect with a median-of-3 pivot (median3_swap_: the
+      median to ``low``, the smallest to ``low + 1``, the largest to
+      ``high``), Hoare's unguarded partition and, once ``2 * msb(num)``
+      partitions have not finished, a median-of-medians-of-5 pivot.
+
+    ``less`` overrides the comparison (used by the adversary test);
+    ``stats`` (a dict) counts the median-of-medians pivots taken.
+    Returns the permutation as a list.
+    """
+    t = list(range(len(v)))
+    if less is None:
+        vals = list(v)
+
+        def lt(i, j):
+            return vals[t[i]] < vals[t[j]]
+
+        def lt_val(i, pv):
+            return vals[t[i]] < pv
+
+        def val_lt(pv, i):
+            return pv < vals[t[i]]
+
+        def val(i):
+            return vals[t[i]]
+    else:
+        def lt(i, j):
+            return less(t[i], t[j])
+
+        def lt_val(i, pv):
+            return less(t[i], pv)
+
+        def val_lt(pv, i):
+            return less(pv, t[i])
+
+        def val(i):  # the element id stands for its value
+            return t[i]
+
+    def swap(i, j):
+        t[i], t[j] = t[j], t[i]
+
+    def dumb_select(off, num, k):
+        for i in range(k + 1):
+            mi = i
+            for q in range(i + 1, num):
+                if lt(off + q, off + mi):
+                    mi = q
+            swap(off + i, off + mi)
+
+    def median3_swap(low, mid, high):
+        if lt(high, mid):
+            swap(high, mid)
+        if lt(high, low):
+            swap(high, low)
+        if lt(low, mid):
+            swap(low, mid)
+        swap(mid, low + 1)
+
+    def median5(off):
+        if lt(off + 1, off + 0):
+            swap(off + 1, off + 0)
+        if lt(off + 4, off + 3):
+            swap(off + 4, off + 3)
+        if lt(off + 3, off + 0):
+            swap(off + 3, off + 0)
+        if lt(off + 4, off + 1):
+            swap(off + 4, off + 1)
+        if lt(off + 2, off + 1):
+            swap(off + 2, off + 1)
+        if lt(off + 3, off + 2):
+            return 1 if lt(off + 3, off + 1) else 3
+        return 2
+
+    def median_of_median5(off, num):
+        nmed = num // 5
+        for i in range(nmed):
+            m = median5(off + 5 * i)
+            swap(off + 5 * i + m, off + i)
+        if nmed > 2:
+            introselect(off, nmed, nmed // 2, top=False)
+        return nmed // 2
+
+    def introselect(off, num, kth, top):
+        low, high = 0, num - 1
+        if kth - low < 3:
+            dumb_select(off + low, high - low + 1, kth - low)
+            return
+        if kth == num - 1:  # inexact types only (float64 weights)
+            mi = low
+            for q in range(low + 1, num):
+                if not lt(off + q, off + mi):  # !(v[q] < max): the last maximum wins
+                    mi = q
+            swap(off + kth, off + mi)
+            return
+        depth = _msb(num) * 2
+        while low + 1 < high:
+            ll, hh = low + 1, high
+            if depth > 0 or hh - ll < 5:
+                median3_swap(off + low, off + low + (high - low) // 2, off + high)
+            else:
+                mid = ll + median_of_median5(off + ll, hh - ll)
+                swap(off + mid, off + low)
+                ll -= 1
+                hh += 1
+                if stats is not None:
+                    stats["mom5"] = stats.get("mom5", 0) + 1
+            depth -= 1
+            pv = val(off + low)
+            while True:  # unguarded_partition_
+                ll += 1
+                while lt_val(off + ll, pv):
+                    ll += 1
+                hh -= 1
+                while val_lt(pv, off + hh):
+                    hh -= 1
+                if hh < ll:
+                    break
+                swap(off + ll, off + hh)
+            swap(off + low, off + hh)
+            if hh >= kth:
+                high = hh - 1
+            if hh <= kth:
+                low = ll
+        if high == low + 1 and lt(off + high, off + low):
+            swap(off + high, off + low)
+
+    n = len(t)
+    if not 0 <= kth < n:
+        raise ValueError(f"kth(={kth}) out of bounds ({n})")
+    introselect(0, n, kth, top=True)
+    return t
+
+
+def introselect_adversary(n, kth):
+    """Weights on which :func:`argpartition_introselect` takes poor median-of-3
+    pivots until it falls back to median-of-medians pivots: McIlroy's "killer
+    adversary" (Software: Practice and Experience 29, 341 (1999)) fixes the
+    values lazily while the select runs -- of two undecided elements compared,
+    the pivot candidate is frozen to the next smallest value -- and the frozen
+    values then replay the same path.  Test input for the selection's rare
+    branch."""
+    gas = 1 << 40
+    val = [gas] * n
+    st = {"solid": 0, "cand": 0}
+
+    def less(a, b):
+        if val[a] == gas and val[b] == gas:
+            z = a if a == st["cand"] else b
+            val[z] = st["solid"]
+            st["solid"] += 1
+        if val[a] == gas:
+            st["cand"] = a
+        elif val[b] == gas:
+            st["cand"] = b
+        return val[a] < val[b]
+
+    argpartition_introselect(list(range(n)), kth, less=less)
+    nxt = st["solid"]
+    for i in range(n):
+        if val[i] == gas:
+            val[i] = nxt
+            nxt += 1
+    return np.array(val, dtype=np.float64)
+
+
 def continuous_update_and_branch(st, dt, thresh_lower, thresh_upper=None):
     """pyvibdmc.py:432-454 with _branch :340-356.  ``st`` is a dict of
     walker-aligned arrays with at least 'x', 'v', 'w' (and optionally 'who',
-    'f', 'psi', 'ke').  Upper-threshold kill order: the reference takes
-    ``np.argpartition(...)[:k]`` whose order is unspecified; here it is the
-    k smallest weights in ascending-index order."""
+    'f', 'psi', 'ke').  The walkers replaced above the upper threshold are
+    ``np.argpartition(w, k)[:k]`` in the order of NumPy's portable
+    introselect (:func:`argpartition_introselect`)."""
     w = st["w"]
     w *= np.exp(-1.0 * (st["v"] - st["vref"]) * dt)
     keys = [k for k in ("x", "v", "who", "f", "psi", "ke") if st.get(k) is not None]
@@ -436,8 +626,7 @@ def continuous_update_and_branch(st, dt, thresh_lower, thresh_upper=None):
     if thresh_upper is not None:
         n_up = int(np.sum(w > thresh_upper))
         if n_up:
-            order = np.argsort(w, kind="stable")[:n_up]
-            _branch(np.sort(order))
+            _branch(argpartition_introselect(w, n_up)[:n_up])
     return len(kill) + n_up, float(np.amax(w)), float(np.amin(w))
 
 

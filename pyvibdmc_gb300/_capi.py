@@ -114,6 +114,7 @@ def load():
                                  C.POINTER(Noise), P], C.c_int),
         "gbdmc_desc_weights": ([P, P, P, C.c_int64, P, P], C.c_int),
         "gbdmc_desc_begin": ([P, P, P], C.c_int),
+        "gbdmc_argpartition": ([P, C.c_int64, C.c_int64, P, P, P, P], C.c_int),
         "gbdmc_batch_init": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers), P, P, P],
                              C.c_int),
         "gbdmc_batch_step": ([C.POINTER(Sim), C.POINTER(Replica), C.c_int32, C.POINTER(Walkers),

@@ -27,6 +27,7 @@
 #include "gbdmc_device.cuh"
 #include "gbdmc_internal.cuh"
 #include "gbdmc_stepcore.cuh"
+#include "gbdmc_select.cuh"
 
 namespace gbdmc {
 
@@ -475,10 +476,11 @@ __global__ void __launch_bounds__(kMaxTPB) k_compact(const __grid_constant__ gbd
 // One CTA of 1024 threads per replica: w *= exp(-(V-vref) dt); clone the
 // current argmax into every walker below the lower threshold, in index order,
 // halving the argmax each time (pyvibdmc.py:340-356, :432-438); the optional
-// upper threshold branches the k smallest weights (k = #w > upper) in
-// ascending index order; then vref from the weighted mean (:659-661).
-// Works in place on compact walkers.
+// upper threshold branches the k smallest weights (k = #w > upper) in the
+// order of np.argpartition(w, k)[:k] (:439-445, block_argpartition); then
+// vref from the weighted mean (:659-661).  Works in place on compact walkers.
 constexpr int kCTA = 1024;
+static_assert(kCTA == kSelCTA, "k_cont_branch runs the block-wide select");
 
 struct ArgBest {
   double v;
@@ -575,7 +577,8 @@ __device__ long long block_compact_flags(const unsigned char* flag, long long n,
 template <int A, bool IS>
 __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gbdmc_sim_t S,
                                                        const __grid_constant__ RepTable T, gbdmc_walkers_t W,
-                                                       gbdmc_ctrl_t* ctrls, int* list_all, unsigned char* flags_all) {
+                                                       gbdmc_ctrl_t* ctrls, int* list_all, int* aux_all,
+                                                       unsigned char* flags_all) {
   const int r = blockIdx.x;
   gbdmc_ctrl_t* ctrl = ctrls + r;
   if (*(volatile int*)&ctrl->status) return;
@@ -621,20 +624,26 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
     if (threadIdx.x == 0) s_nb = 0;
     __syncthreads();
     long long cnt = 0;
-    for (long long i = threadIdx.x; i < n; i += kCTA) {
-      cnt += w[i] > S.thresh_upper ? 1 : 0;
-      flags[i] = 0;
-    }
+    for (long long i = threadIdx.x; i < n; i += kCTA) cnt += w[i] > S.thresh_upper ? 1 : 0;
     cnt = warp_sum(cnt);
     if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long*)&s_nb, (unsigned long long)cnt);
     __syncthreads();
     const long long nup = s_nb;
-    for (long long j = 0; j < nup; ++j) {
-      const long long m = block_arg<false>(w, n, flags);
-      if (threadIdx.x == 0 && m >= 0) flags[m] = 1;
-      __syncthreads();
+    if (nup >= n && nup > 0) {  // np.argpartition raises: kth out of bounds
+      if (threadIdx.x == 0) {
+        ctrl->status |= GBDMC_ST_HUGE_WEIGHT;
+        ctrl->err_step = (int)step;
+      }
+      return;
     }
-    const long long nk2 = block_compact_flags(flags, n, list);
+    if (nup > 0 && !block_argpartition(w, list, n, nup, aux_all + base, flags)) {
+      if (threadIdx.x == 0) {
+        ctrl->status |= GBDMC_ST_OVERFLOW;
+        ctrl->err_step = (int)step;
+      }
+      return;
+    }
+    const long long nk2 = nup;
     for (long long j = 0; j < nk2; ++j) {
       const long long to = list[j];
       const long long m = block_arg<true>(w, n, nullptr);
@@ -691,6 +700,12 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
       ctrl->reserved[1] = __double_as_longlong(wmn);
     }
   }
+}
+
+// np.argpartition of one weight array by one CTA (gbdmc_argpartition).
+__global__ void __launch_bounds__(kSelCTA) k_argpartition(const double* w, long long n, long long kth, int* perm,
+                                                          int* lpos, unsigned char* fl) {
+  if (!block_argpartition(w, perm, n, kth, lpos, fl) && threadIdx.x == 0) perm[0] = -1;
 }
 
 // -------------------------------------------------------- descendants
@@ -835,7 +850,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     } else {
       k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      k_cont_branch<A, false><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
+      k_cont_branch<A, false><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.counts, L.flags);
     }
   } else {
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
@@ -845,7 +860,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {
-      k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.flags);
+      k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.counts, L.flags);
     }
   }
   if (prof) {
@@ -1197,6 +1212,17 @@ extern "C" int gbdmc_desc_weights(const int32_t* who, const double* w, const int
   }
   k_desc<<<2 * num_sms(), 256, 0, s>>>(who, w, n_dev, n_parent, desc);
   return check_launch("gbdmc_desc_weights");
+}
+
+extern "C" int gbdmc_argpartition(const double* w, int64_t n, int64_t kth, int32_t* perm, int32_t* lpos,
+                                  uint8_t* flags, void* stream) {
+  if (!w || !perm || !lpos || !flags || n < 1 || n > (int64_t)INT32_MAX || kth < 0 || kth >= n) {
+    set_error("gbdmc_argpartition: need 0 <= kth < n <= 2^31-1 and non-null buffers (n=%lld kth=%lld)",
+              (long long)n, (long long)kth);
+    return GBDMC_ERR_ARG;
+  }
+  k_argpartition<<<1, kSelCTA, 0, (cudaStream_t)stream>>>(w, n, kth, perm, lpos, flags);
+  return check_launch("gbdmc_argpartition");
 }
 
 extern "C" int gbdmc_desc_begin(int32_t* who, const int64_t* n_dev, void* stream) {

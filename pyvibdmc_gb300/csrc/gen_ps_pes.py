@@ -2,7 +2,7 @@
 Fortran source (run once, in the container that has the reference):
 
     python pyvibdmc_gb300/csrc/gen_ps_pes.py \
-        /root/reference/pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f
+        <reference checkout>/pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f
 
 The PES (H. Partridge and D. W. Schwenke, J. Chem. Phys. 106, 4618 (1997))
 is defined by its fitted coefficients, which are data: this script parses
@@ -160,5 +160,6 @@ def main(path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else
-         "/root/reference/pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f")
+    if len(sys.argv) < 2:
+        sys.exit("usage: gen_ps_pes.py <path of the reference's h2opes_v2.f>")
+    main(sys.argv[1])

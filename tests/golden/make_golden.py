@@ -2,7 +2,9 @@
 
 Run from the repository root with the reference checkout available::
 
-    python tests/golden/make_golden.py /root/reference [fixture,fixture,...]
+    python tests/golden/make_golden.py <reference checkout> [fixture,fixture,...]
+
+(or set GBDMC_REFERENCE to the checkout and omit the first argument).
 
 What it does:
 
@@ -21,14 +23,36 @@ What it does:
   the reference test geometry;
 * writes ``tests/golden/*.npz``.
 
+NumPy's SIMD select is switched off (``NPY_DISABLE_CPU_FEATURES`` set to every
+dispatch target of the running NumPy, before NumPy is imported), so the
+reference's ``np.argpartition`` (pyvibdmc.py:443-445) runs NumPy's portable
+introselect, the algorithm NumPy uses on every platform without a SIMD
+select kernel (aarch64 among them).  On x86 with AVX2/AVX-512 NumPy 2.x would
+otherwise substitute a SIMD select whose output order differs.
+
 The fixtures hold the seeds, the inputs and the reference outputs.
 """
 import os
+import subprocess
 import sys
 import tempfile
 import types
 
-import numpy as np
+
+def _numpy_dispatch_targets():
+    r = subprocess.run([sys.executable, "-c", "import numpy._core._multiarray_umath as m; "
+                        "print(' '.join(getattr(m, '__cpu_dispatch__', [])))"],
+                       capture_output=True, text=True, check=True)
+    return r.stdout.strip()
+
+
+if __name__ == "__main__" and "NPY_DISABLE_CPU_FEATURES" not in os.environ:
+    feats = _numpy_dispatch_targets()
+    if feats:
+        os.environ["NPY_DISABLE_CPU_FEATURES"] = feats
+        os.execv(sys.executable, [sys.executable] + sys.argv)
+
+import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -197,19 +221,27 @@ def main(ref_path, only=None):
                       weighting="continuous", thresh=0.2)
     fixtures["h2o_continuous"] = dict(x0=x0, seed=3, dt=10.0, nsteps=40, thresh=0.2, **r)
 
-    # --- continuous weights with both thresholds, one step.  The reference picks the
-    # walkers to replace above the upper threshold with np.argpartition, whose order is
-    # unspecified, so this fixture pins the branched walkers as a set.  The thresholds are
-    # the 2 % and 90 % quantiles of the step's weights (a few walkers below, and more
-    # above than the lower branching halves).
-    n = 192
-    x0 = eq[None] + 0.05 * oracle.InjectedNoise(707).standard_normal((n, 3, 3))
-    probe = oracle.OracleDMC(x0, masses, 10.0, pes, oracle.InjectedNoise(7), weighting="continuous",
-                             cont_wt_thresh=[1e-300, 1e300]).run(1)
-    thr = [float(q) for q in np.quantile(probe.w, [0.02, 0.9])]
-    r = run_reference(pv, tmp, "h2o_cont_upper", x0, ["O", "H", "H"], masses, 10.0, 1, pes, seed=7,
-                      weighting="continuous", thresh=thr)
-    fixtures["h2o_cont_upper"] = dict(x0=x0, seed=7, dt=10.0, nsteps=1, thresh=np.array(thr), **r)
+    # --- continuous weights with both thresholds.  The reference replaces the walkers
+    # above the upper threshold in np.argpartition order (portable introselect, see the
+    # module docstring), so these fixtures pin which walker is cloned into which slot.
+    # The thresholds are the 2 % and 90 % (85 %) quantiles of the first step's weights,
+    # so every step branches a few walkers below and more above than the lower
+    # branching halves; a descendant-weighting window follows the walkers' ancestors
+    # through the replacements.  The 1500-walker case spans two 1024-walker chunks
+    # of the GPU's block-wide select.
+    for name, n, nsteps, seed, q_hi in (("h2o_cont_upper", 192, 6, 7, 0.9),
+                                         ("h2o_cont_upper_1500", 1500, 3, 8, 0.85)):
+        x0 = eq[None] + 0.05 * oracle.InjectedNoise(700 + seed).standard_normal((n, 3, 3))
+        probe = oracle.OracleDMC(x0, masses, 10.0, pes, oracle.InjectedNoise(seed), weighting="continuous",
+                                 cont_wt_thresh=[1e-300, 1e300]).run(1)
+        thr = [float(q) for q in np.quantile(probe.w, [0.02, q_hi])]
+        r = run_reference(pv, tmp, name, x0, ["O", "H", "H"], masses, 10.0, nsteps, pes, seed=seed,
+                          weighting="continuous", thresh=thr, equil=1, wfn_every=10 ** 6, desc=nsteps - 2)
+        if n > 1000:  # kept small: x0 is regenerated from its seed, the parents are x after step 1
+            r.pop("wfn0_coords")
+        fixtures[name] = dict(x0=x0 if n <= 1000 else np.zeros(0), seed=seed, dt=10.0, nsteps=nsteps,
+                              thresh=np.array(thr), equil=1, desc=nsteps - 2, numpy_version=np.__version__,
+                              npy_disable_cpu_features=os.environ.get("NPY_DISABLE_CPU_FEATURES", ""), **r)
 
     # --- config-3 family: importance sampling with the Gaussian internal trial
     alpha, qe = oracle.h2o_trial_config(p)
@@ -259,5 +291,7 @@ def main(ref_path, only=None):
 
 if __name__ == "__main__":
     # optional second argument: comma-separated fixture names to write (default: all)
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference",
-         set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBDMC_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> [fixture,...]  (or set GBDMC_REFERENCE)")
+    main(ref, set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)

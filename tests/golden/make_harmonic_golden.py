@@ -2,7 +2,7 @@
 the UNMODIFIED reference (``HarmonicAnalysis``, ``InitialConditioner``) with
 the oracle's NumPy PESs plugged in through ``Potential_Direct``:
 
-    python tests/golden/make_harmonic_golden.py /root/reference
+    python tests/golden/make_harmonic_golden.py <reference checkout>   (or set GBDMC_REFERENCE)
 
 Writes ``tests/golden/harmonic.npz``: Hessians, frequencies and normal modes
 of the local-mode water (O,H,H at its minimum) and of the Partridge-Schwenke
@@ -58,4 +58,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBDMC_REFERENCE")
+    if not ref:
+        sys.exit("usage: %s <reference checkout>  (or set GBDMC_REFERENCE)" % sys.argv[0])
+    main(ref)

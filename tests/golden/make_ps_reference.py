@@ -5,7 +5,7 @@ discrete weighting).  Each log prints, per step, the mean potential energy of
 the ensemble after the move (cm^-1) and the population.  This script keeps,
 per run, the average over steps 500-4999 of that mean and of the population.
 
-    python tests/golden/make_ps_reference.py /root/reference
+    python tests/golden/make_ps_reference.py <reference checkout>   (or set GBDMC_REFERENCE)
 """
 import json
 import os
@@ -36,4 +36,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBDMC_REFERENCE")
+    if not ref:
+        sys.exit("usage: %s <reference checkout>  (or set GBDMC_REFERENCE)" % sys.argv[0])
+    main(ref)

@@ -5,6 +5,7 @@ Tolerances: coordinates, populations, branch counts and descendant weights
 bit-exact; potentials 1e-12 Eh; vref 1e-12 Eh; importance-sampled runs 1e-10
 (the adjoint derivatives differ from the reference's NumPy chain rule in
 the last bits, which moves proposals by ~1e-16 bohr)."""
+import ctypes as C
 import os
 
 import numpy as np
@@ -391,10 +392,17 @@ def test_ho_zpe_analytic(rng):
                      delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=7, rng=rng,
                      write_files=False)
     sim.run()
+    # The walk is exact for the Trotter-split propagator exp(-dt V) exp(-dt T),
+    # whose ground-state growth rate for this oscillator is known in closed form:
+    # E(dt) = 3/(2 dt) arccosh(1 + (omega dt)^2 / 2) = 4496.5 cm^-1 at dt = 10
+    # (4500 cm^-1 as dt -> 0).  Bar: 3 standard errors of 20 block means.
+    w = pg.Constants.convert(3000.0, "wavenumbers")
+    e_dt = pg.Constants.convert(1.5 / 10.0 * np.arccosh(1.0 + (w * 10.0) ** 2 / 2.0), "wavenumbers", to_AU=False)
     v = pg.Constants.convert(sim._vref_vs_tau[1000:], "wavenumbers", to_AU=False)
-    blocks = v.reshape(10, -1).mean(1)
+    blocks = v.reshape(20, -1).mean(1)
     err = blocks.std(ddof=1) / np.sqrt(len(blocks))
-    assert abs(v.mean() - 4500.0) < max(5 * err, 15.0), (v.mean(), err)
+    assert abs(e_dt - 4496.5) < 0.1
+    assert abs(v.mean() - e_dt) < 3 * err, (v.mean(), e_dt, err)
 
 
 def test_is_and_plain_converge_at_small_time_step():
@@ -475,21 +483,70 @@ def test_host_resident_step_failure_keeps_the_host_walkers():
     assert torch.equal(hw.host["x"][:, :100], before)
 
 
-def test_engine_continuous_upper_threshold_vs_oracle():
-    # both thresholds (pyvibdmc.py:432-454): the walkers replaced above the upper
-    # threshold are taken in ascending slot order, as the oracle does (the reference's
-    # np.argpartition order is unspecified; the oracle is pinned on it as a set)
-    g = load("h2o_cont_upper")
+def _cont_upper(name):
+    g = load(name)
     p, m = oracle.h2o_config()
+    if g["x0"].size == 0:  # regenerated from its seed (make_golden.py keeps the large fixture small)
+        n = len(g["wfn0_desc_wts"])
+        g["x0"] = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(700 + int(g["seed"])).standard_normal(
+            (n, 3, 3))
+    return g, p, m
+
+
+@pytest.mark.parametrize("name", ["h2o_cont_upper", "h2o_cont_upper_1500"])
+def test_engine_continuous_upper_threshold_vs_reference(name):
+    # both thresholds (pyvibdmc.py:432-454): the walkers replaced above the upper
+    # threshold come in np.argpartition order (block_argpartition), so which walker
+    # is cloned into which slot is the reference's.  Walkers bit-exact; weights,
+    # weight sums, vref and descendant weights within 1e-12 (CUDA's exp vs NumPy's)
+    g, p, m = _cont_upper(name)
     thr = [float(t) for t in g["thresh"]]
     sim = _sim(g["x0"], m, ["O", "H", "H"], pg.h2o_local_mode(), int(g["seed"]), int(g["nsteps"]),
-               weighting="continuous", cont_wt_thresh=thr)
+               weighting="continuous", cont_wt_thresh=thr, equil=int(g["equil"]), desc=int(g["desc"]))
     sim.run()
-    ref = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
-                           oracle.InjectedNoise(int(g["seed"])), weighting="continuous",
-                           cont_wt_thresh=thr).run(int(g["nsteps"]))
     x, w = sim.walkers
-    assert np.array_equal(x, ref.x)
-    np.testing.assert_allclose(w, ref.w, rtol=1e-12)
-    np.testing.assert_allclose(sim._vref_vs_tau, ref.vref_hist, rtol=0, atol=1e-12)
-    np.testing.assert_allclose(sim._pop_vs_tau, ref.pop_hist, rtol=1e-13)
+    assert np.array_equal(x, g["x_final"])
+    np.testing.assert_allclose(w, g["w_final"], rtol=1e-12)
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sim._pop_vs_tau, g["pop"], rtol=1e-12)
+    assert len(sim.wfns) == 1
+    np.testing.assert_allclose(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(sim.wfns[0]["parent_wts"], g["wfn0_parent_wts"], rtol=1e-12, atol=0)
+
+
+def _argpartition_cases():
+    rng = np.random.default_rng(3)
+    cases = []
+    for n in (1, 2, 3, 5, 31, 1023, 1024, 1025, 3000, 20000):
+        for k in sorted({0, 1, 2, 3, 4, n // 2, n - 2, n - 1} & set(range(n))):
+            v = rng.random(n)
+            cases.append((f"rand{n}/{k}", v, k))
+            cases.append((f"ties{n}/{k}", np.round(v * 8) / 8, k))
+    cases.append(("equal5000", np.full(5000, 0.5), 2500))
+    for n, k in ((200, 100), (1000, 37), (2500, 1250), (777, 700)):
+        cases.append((f"adversary{n}/{k}", oracle.introselect_adversary(n, k), k))
+    return cases
+
+
+def test_argpartition_kernel_matches_numpy_introselect():
+    # the block-wide select against the oracle's restatement of NumPy's
+    # introselect (itself pinned on np.argpartition): random weights, heavy ties,
+    # a constant array, several 1024-element chunks, kth in every branch of the
+    # algorithm (selection sort, last element, quickselect) and adversarial inputs
+    # that take the median-of-medians pivots
+    L = pg._capi.load()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for label, v, k in _argpartition_cases():
+        n = len(v)
+        w = torch.as_tensor(v, device="cuda")
+        perm = torch.empty(n, dtype=torch.int32, device="cuda")
+        lpos = torch.empty(n, dtype=torch.int32, device="cuda")
+        fl = torch.empty(n, dtype=torch.uint8, device="cuda")
+        pg._capi.check(L.gbdmc_argpartition(C.c_void_p(w.data_ptr()), n, k, C.c_void_p(perm.data_ptr()),
+                                            C.c_void_p(lpos.data_ptr()), C.c_void_p(fl.data_ptr()), st),
+                       "gbdmc_argpartition")
+        got = perm.cpu().numpy()
+        ref = np.array(oracle.argpartition_introselect(v, k))
+        assert np.array_equal(got[:k], ref[:k]), label
+        if k >= 3:
+            assert np.array_equal(got, ref), label

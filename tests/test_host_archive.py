@@ -116,19 +116,6 @@ def test_engine_fails_loudly_without_cuda():
                    start_structures=np.zeros((1, 3, 3)), write_files=False)
 
 
-def test_documented_python_snippets_parse():
-    """The Python examples of the integration guide and the README are valid syntax."""
-    import re
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    n = 0
-    for doc in ("INTEGRATION.md", "README.md"):
-        text = open(os.path.join(root, doc)).read()
-        for k, block in enumerate(re.findall(r"```python\n(.*?)```", text, flags=re.S)):
-            compile(block, f"{doc}[{k}]", "exec")
-            n += 1
-    assert n >= 4
-
-
 # DMC_Sim keywords, defaults and order of pyvibdmc.py:67-98
 REFERENCE_KEYWORDS = [
     ("sim_name", "DMC_Sim"), ("output_folder", "exSimResults"), ("weighting", "discrete"), ("num_walkers", 10000),

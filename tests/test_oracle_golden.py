@@ -62,43 +62,141 @@ def test_h2o_continuous_matches_reference():
     assert sum(c[0] for c in sim.counters) > 0  # branching happened
 
 
-def _rows(x, v, w):
-    r = np.column_stack([x.reshape(len(x), -1), v, w])
-    return r[np.lexsort(r.T[::-1])]
-
-
-def test_h2o_continuous_upper_threshold_matches_reference_as_a_set():
-    # the reference orders the walkers it replaces above the upper threshold by
-    # np.argpartition (unspecified); the oracle takes them in ascending slot order, so
-    # the branched walkers agree as a set of (x, V, w) rows
-    g = load("h2o_cont_upper")
+def _cont_upper_fixture(name):
+    g = load(name)
     p, m = oracle.h2o_config()
+    if g["x0"].size == 0:  # regenerated from its seed (make_golden.py keeps the large fixture small)
+        n = len(g["wfn0_desc_wts"])
+        g["x0"] = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(700 + int(g["seed"])).standard_normal(
+            (n, 3, 3))
+    return g, p, m
+
+
+def _numpy_without_simd_env():
+    """Environment that switches NumPy's SIMD dispatch off, as make_golden.py does
+    when it runs the reference for the upper-threshold fixtures (the SIMD kernels
+    also change the association of NumPy's float sums in the last bits)."""
+    import subprocess
+    import sys
+    feats = subprocess.run([sys.executable, "-c", "import numpy._core._multiarray_umath as m; "
+                            "print(' '.join(getattr(m, '__cpu_dispatch__', [])))"],
+                           capture_output=True, text=True, check=True).stdout.strip()
+    return dict(os.environ, NPY_DISABLE_CPU_FEATURES=feats)
+
+
+def _in_numpy_without_simd(code, timeout=600):
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-c", f"import sys; sys.path[:0] = [{os.path.dirname(here)!r}, {here!r}]\n"
+                        + code], capture_output=True, text=True, env=_numpy_without_simd_env(), timeout=timeout)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    return r.stdout
+
+
+@pytest.mark.parametrize("name", ["h2o_cont_upper", "h2o_cont_upper_1500"])
+def test_h2o_continuous_upper_threshold_matches_reference(name):
+    # both thresholds: the walkers replaced above the upper threshold come in
+    # np.argpartition order (portable introselect); walkers, weights, potentials,
+    # vref, the weight sums and the descendant weights of a window spanning the
+    # replacements are all bit-equal to the unmodified reference's, with NumPy's
+    # arithmetic set up as it was when the fixture was made
+    out = _in_numpy_without_simd(f"import test_oracle_golden as t; t.check_cont_upper({name!r}); print('OK')")
+    assert out.strip().endswith("OK")
+
+
+def check_cont_upper(name):
+    g, p, m = _cont_upper_fixture(name)
     pes = lambda c: oracle.pes_h2o_lm(c, p)  # noqa: E731
 
     def run(thresh):
         return oracle.OracleDMC(g["x0"], m, float(g["dt"]), pes, oracle.InjectedNoise(int(g["seed"])),
-                                weighting="continuous", cont_wt_thresh=thresh).run(int(g["nsteps"]))
+                                weighting="continuous", cont_wt_thresh=thresh, equil_steps=int(g["equil"]),
+                                wfn_every=10 ** 6, desc_wt_steps=int(g["desc"])).run(int(g["nsteps"]))
 
     sim = run(list(g["thresh"]))
-    assert np.array_equal(_rows(sim.x, sim.v, sim.w), _rows(g["x_final"], g["v_final"], g["w_final"]))
-    np.testing.assert_allclose(sim.vref_hist, g["vref"], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(sim.pop_hist, g["pop"], rtol=1e-14, atol=0)
+    assert np.array_equal(sim.x, g["x_final"])
+    assert np.array_equal(sim.w, g["w_final"])
+    assert np.array_equal(sim.v, g["v_final"])
+    assert np.array_equal(np.array(sim.vref_hist), g["vref"])
+    assert np.array_equal(np.array(sim.pop_hist), g["pop"])
+    assert len(sim.wfns) == 1
+    assert np.array_equal(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"])
+    assert np.array_equal(sim.wfns[0]["parent_wts"], g["wfn0_parent_wts"])
+    if "wfn0_coords" in g:
+        assert np.array_equal(sim.wfns[0]["coords"], g["wfn0_coords"])
+    assert min(c[0] for c in sim.counters) > 5  # every step branched above the upper threshold
     low = run(float(g["thresh"][0]))  # the upper threshold changed the walkers
-    assert not np.array_equal(_rows(low.x, low.v, low.w), _rows(sim.x, sim.v, sim.w))
+    assert not np.array_equal(low.x, sim.x)
 
 
 def test_continuous_replacement_rules_by_hand():
-    # pyvibdmc.py:340-356, 432-454 with the oracle's order above the upper threshold:
-    # below `lower` in slot order, then the n_up smallest weights in slot order, each
-    # replaced by a copy of the current largest weight (first slot on ties), both halved
+    # pyvibdmc.py:340-356, 432-454: below `lower` in slot order, then
+    # np.argpartition(w, n_up)[:n_up], each replaced by a copy of the current
+    # largest weight (first slot on ties), both halved
     x = np.arange(5.0)[:, None, None] * np.ones((5, 1, 3))
     st = dict(x=x, v=np.arange(5.0), w=np.array([0.1, 3.0, 0.5, 3.0, 2.0]), vref=0.0)
     nb, wmax, wmin = oracle.continuous_update_and_branch(st, 0.0, 0.2, 1.4)
-    # slot 0 <- 1 (w 1.5 each); then n_up = 4 of {1.5, 1.5, 3, 2}: slots 0, 1, 2, 4 <- 3, 4, 0, 3
+    # slot 0 <- 1 (w 1.5 each); then n_up = 4 = N - 1: argpartition swaps the first
+    # maximum (slot 3) to the end, so slots 0, 1, 2, 4 <- 3, 4, 0, 3
     assert (nb, wmax, wmin) == (5, 1.0, 0.75)
     assert np.array_equal(st["w"], [0.75, 1.0, 0.75, 0.75, 0.75])
     assert np.array_equal(st["x"][:, 0, 0], [3.0, 4.0, 3.0, 3.0, 3.0])
     assert np.array_equal(st["v"], [3.0, 4.0, 3.0, 3.0, 3.0])
+
+
+def test_upper_threshold_order_is_introselect_not_ascending():
+    # seven weights, three above the threshold: argpartition(w, 3)[:3] = [6, 1, 4]
+    # by dumb_select_ (kth < 3 is not the case: kth = 3 takes the quickselect loop)
+    w = np.array([5.0, 0.9, 4.0, 6.0, 0.8, 7.0, 0.7])
+    order = oracle.argpartition_introselect(w, 3)[:3]
+    assert sorted(order) == [1, 4, 6]
+    assert order != sorted(order)
+
+
+_PIN_SCRIPT = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from oracle import argpartition_introselect as aps, introselect_adversary as adversary
+rng = np.random.default_rng(11)
+bad = []
+for trial in range(600):
+    n = int(rng.integers(1, 1500))
+    v = rng.random(n)
+    if trial % 3 == 0:
+        v = np.round(v * 8) / 8          # many ties
+    if trial % 13 == 0:
+        v[:] = 0.25                     # all equal
+    k = int(rng.integers(0, n))
+    if not np.array_equal(np.argpartition(v, k), aps(v, k)):
+        bad.append((n, k))
+
+mom5 = 0
+for n, k in ((200, 100), (1000, 37), (2500, 1250), (777, 700)):
+    v = adversary(n, k)
+    stats = {}
+    if not np.array_equal(np.argpartition(v, k), aps(v, k, stats=stats)):
+        bad.append(("adversary", n, k))
+    mom5 += stats.get("mom5", 0)
+print("BAD", bad, "MOM5", mom5)
+"""
+
+
+def test_introselect_restatement_matches_numpy_argpartition():
+    # pins oracle.argpartition_introselect on np.argpartition itself, with NumPy's
+    # SIMD select dispatch switched off (the portable introselect that aarch64 runs),
+    # on random weights, heavy ties, constant arrays and adversarial inputs that
+    # force the median-of-medians pivot
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _PIN_SCRIPT, root], capture_output=True, text=True,
+                       env=_numpy_without_simd_env(), timeout=600)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("BAD")][-1]
+    assert line.startswith("BAD [] "), line
+    assert int(line.split("MOM5")[1]) > 0
 
 
 def test_h2o_importance_sampling_matches_reference():
@@ -209,10 +307,13 @@ def test_dimer_trial_derivatives_match_finite_differences():
             np.testing.assert_allclose(d2[:, a, d], (pp - 2 * psi0 + pm) / (h * h) / psi0, rtol=1e-4, atol=1e-3)
 
 
-REF_PS = "/root/reference/pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f"
+# the reference checkout, when the environment names it (GBDMC_REFERENCE)
+REF_PS = os.path.join(os.environ.get("GBDMC_REFERENCE", ""),
+                      "pyvibdmc/sample_potentials/FortPots/Partridge_Schwenke_H2O/h2opes_v2.f")
 
 
-@pytest.mark.skipif(not os.path.exists(REF_PS), reason="the reference source is not present")
+@pytest.mark.skipif(not os.environ.get("GBDMC_REFERENCE") or not os.path.exists(REF_PS),
+                    reason="set GBDMC_REFERENCE to a reference checkout to pin the coefficients on its source")
 def test_ps_coefficients_match_the_fortran_source():
     """The committed Partridge-Schwenke tables against an independent read of the
     Fortran DATA statements and vibpot's first-call scaling (h2opes_v2.f:420-458)."""
