@@ -63,9 +63,15 @@ enum {
   GBDMC_PES_HO = 1,     /* p[0]=k : V = 1/2 k |x|^2                              */
   GBDMC_PES_H2O_LM = 2, /* O,H,H; p = De, a, re, ktheta, theta_e, krr            */
   GBDMC_PES_DIMER = 3,  /* O,H,H,O,H,H; p = De,a,re,ktheta,theta_e,krr,eps,sigma,qH,qO */
-  GBDMC_PES_H2O_PS = 4  /* Partridge-Schwenke water (J. Chem. Phys. 106, 4618 (1997)), the reference's
+  GBDMC_PES_H2O_PS = 4, /* Partridge-Schwenke water (J. Chem. Phys. 106, 4618 (1997)), the reference's
                            sample Fortran PES (h2opes_v2.f).  p[0] = 0: atoms O,H,H; p[0] = 1: H,H,O (the
                            order of the reference's calc_hoh_pot, calc_h2o_pot.f:1-30)            */
+  GBDMC_PES_EXTERNAL = 5 /* the caller's potential (any getpot, potential_manager.py:71-253): a step is
+                           gbdmc_sim_move, the caller's V written to dst->v, then gbdmc_sim_branch.
+                           p[0] = coordinates per walker nc (1..3*natoms; 0: 3*natoms), p[1] = dimensions
+                           per atom d (1, 2 or 3; 0: 3).  Walker arrays keep 3*natoms rows, of which the
+                           first nc are coordinate k = d*atom + dim and the rest padding; sigma[] is per
+                           atom of the caller's system (nc / d atoms, at most GBDMC_MAX_ATOMS).      */
 };
 
 typedef struct {
@@ -219,6 +225,23 @@ int gbdmc_sim_init(const gbdmc_sim_t* sim, const gbdmc_walkers_t* w, gbdmc_ctrl_
 int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
                    gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, const gbdmc_noise_t* noise,
                    void* stream);
+
+/* The two halves of a step around a potential the caller evaluates
+ * (sim->pes.kind == GBDMC_PES_EXTERNAL, plain DMC): gbdmc_sim_move is
+ * move_randomly (pyvibdmc.py:540-547) -- the logical walkers of src (through
+ * src->idx) moved into dst in order, dst->x, who and w written; the caller
+ * then writes V of the ctrl->n moved walkers to dst->v (the reference's
+ * potential call, :785-793) and gbdmc_sim_branch runs birth_or_death
+ * (:380-454), calc_vref (:651-661) and update_sim_arrays (:674-682) on them:
+ * discrete weighting writes dst->idx (the branched population is dst
+ * gathered through it), continuous weighting works in place.  The
+ * branching uniforms are the injected noise->u_branch or a Philox stream
+ * disjoint from the move's.  gbdmc_sim_init takes the start walkers' V from
+ * w->v for this kind.  Scratch as gbdmc_sim_step. */
+int gbdmc_sim_move(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                   gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, const gbdmc_noise_t* noise, void* stream);
+int gbdmc_sim_branch(const gbdmc_sim_t* sim, const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl_dev,
+                     void* scratch_dev, const gbdmc_noise_t* noise, void* stream);
 
 /* Batched ensemble of nrep <= GBDMC_MAX_REPLICAS independent replicas in
  * one launch per phase (persistent grid over all replicas' tiles).  sim->ld

@@ -18,7 +18,7 @@ import numpy as np
 __all__ = [
     "WAVENUMBERS", "ANGSTROMS", "AMU", "MASS_H", "MASS_O", "mass_au",
     "InjectedNoise", "splitmix64",
-    "pes_ho", "pes_h2o_lm", "pes_dimer", "grad_ho", "grad_h2o_lm", "grad_dimer",
+    "pes_ho", "pes_h2o_lm", "oh_stretch_harm", "reduced_mass_au", "pes_dimer", "grad_ho", "grad_h2o_lm", "grad_dimer",
     "h2o_internals", "TrialH2OGauss", "TrialHOGauss", "TrialDimerGauss", "finite_diff",
     "metropolis", "local_kin", "move_randomly", "birth_or_death_discrete",
     "continuous_update_and_branch", "argpartition_introselect", "introselect_adversary", "calc_vref", "calc_desc_wts",
@@ -122,6 +122,26 @@ def pes_ho(x, k):
 
 def grad_ho(x, k):
     return k * np.asarray(x, dtype=np.float64)
+
+
+def reduced_mass_au(a_amu, b_amu):
+    """Constants.reduced_mass (Constants.py:100-119): both masses to atomic
+    units first, then m1 m2 / (m1 + m2)."""
+    m1, m2 = mass_au(a_amu), mass_au(b_amu)
+    return m1 * m2 / (m1 + m2)
+
+
+def oh_stretch_harm(cds, kwargs=None):
+    """The reference's 1D sample potential (sample_potentials/PythonPots/
+    harmonicOscillator1D.py:13-17): 1/2 mu omega^2 x^2 with the O-H reduced
+    mass and omega = 3700 cm^-1, (N,1,1) -> (N,); with ``kwargs`` the
+    ``oh_stretch_harm_with_arg`` variant (:25-29), mass and frequency from
+    kwargs['mass'], kwargs['freq']."""
+    if kwargs is None:
+        mu, w = reduced_mass_au(MASS_O, MASS_H), 3700.0 * WAVENUMBERS
+    else:
+        mu, w = kwargs["mass"], kwargs["freq"]
+    return np.squeeze(0.5 * mu * w ** 2 * cds ** 2)
 
 
 def h2o_internals(x, o=0, h1=1, h2=2):

@@ -12,6 +12,7 @@ from .potentials import (Potential_GPU, PESFunction, harmonic_oscillator, h2o_lo
                          WATER_DIMER_EQ, to_soa, from_soa)
 from .imp_samp import ImpSampManager_GPU, TrialFunction, h2o_gaussian_trial, ho_gaussian_trial, \
     dimer_gaussian_trial
+from .potential_manager import Potential, Potential_NoMP, NN_Potential, Potential_Direct
 from .engine import DMC_Sim, HostWalkers, dmc_restart
 from .initial import HarmonicAnalysis, InitialConditioner
 from .batch import DMC_Batch, blocking_error
@@ -22,7 +23,7 @@ __all__ = ["HostWalkers", "HarmonicAnalysis", "InitialConditioner", "Constants",
            "harmonic_oscillator", "h2o_local_mode", "water_dimer", "partridge_schwenke", "ImpSampManager_GPU", "TrialFunction",
            "h2o_gaussian_trial", "ho_gaussian_trial", "dimer_gaussian_trial", "DMC_Sim", "dmc_restart", "DMC_Batch", "blocking_error",
            "MLPSurrogate", "NN_Potential_GPU", "NNDMC", "harvest_training_data", "WATER_DIMER_EQ",
-           "to_soa", "from_soa"]
+           "to_soa", "from_soa", "Potential", "Potential_NoMP", "NN_Potential", "Potential_Direct"]
 
 __version__ = "0.1.0"
 

@@ -13,7 +13,7 @@ MAX_ATOMS = 8
 
 OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY = 0, 1, 2, 3
 ST_NONFINITE_WEIGHT, ST_HUGE_WEIGHT, ST_POP_LOW, ST_POP_HIGH, ST_OVERFLOW, ST_TIMEOUT = 1, 2, 4, 8, 16, 32
-PES_HO, PES_H2O_LM, PES_DIMER, PES_H2O_PS = 1, 2, 3, 4
+PES_HO, PES_H2O_LM, PES_DIMER, PES_H2O_PS, PES_EXTERNAL = 1, 2, 3, 4, 5
 TRIAL_NONE, TRIAL_HO_GAUSS, TRIAL_H2O_GAUSS, TRIAL_DIMER_GAUSS = 0, 1, 2, 3
 NOISE_PHILOX32, NOISE_PHILOX64, NOISE_INJECTED = 0, 1, 2
 DISCRETE, CONTINUOUS = 0, 1
@@ -110,6 +110,9 @@ def load():
         "gbdmc_sim_init": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, P], C.c_int),
         "gbdmc_sim_step": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P,
                             C.POINTER(Noise), P], C.c_int),
+        "gbdmc_sim_move": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.POINTER(Noise), P],
+                           C.c_int),
+        "gbdmc_sim_branch": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, C.POINTER(Noise), P], C.c_int),
         "gbdmc_sim_step_host": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, P,
                                  C.POINTER(Noise), P], C.c_int),
         "gbdmc_desc_weights": ([P, P, P, C.c_int64, P, P], C.c_int),

@@ -10,14 +10,16 @@
 * The text log follows SimLogger's lines (simulation_utilities/sim_logger.py).
 """
 import glob
+import importlib
 import os
+import pickle
 
 import numpy as np
 
 from .constants import Constants
 
 __all__ = ["save_h5", "load_h5", "create_filesystem", "delete_older_checkpoints", "delete_future_checkpoints",
-           "checkpoint_step", "SimLogger"]
+           "checkpoint_step", "SimLogger", "load_checkpoint", "ReferenceCheckpoint"]
 
 try:  # optional dependency
     import h5py as _h5py
@@ -37,13 +39,57 @@ def save_h5(fname, keyz, valz):
 
 
 def load_h5(fname):
+    """Read a file written by save_h5: the HDF5 file when h5py is installed and
+    it exists, else the ``.npz`` written in its place."""
+    if _h5py is not None and os.path.exists(fname):
+        with _h5py.File(fname, "r") as hf:
+            return {k: hf[k][()] for k in hf.keys()}
     if os.path.exists(fname + ".npz"):
         with np.load(fname + ".npz") as z:
             return {k: z[k] for k in z.files}
-    if _h5py is None:
-        raise FileNotFoundError(fname)
-    with _h5py.File(fname, "r") as hf:
-        return {k: hf[k][()] for k in hf.keys()}
+    raise FileNotFoundError(fname)
+
+
+class ReferenceCheckpoint:
+    """The attributes of a checkpoint the reference wrote: SimArchivist.chkpt
+    pickles a copy of the DMC_Sim object, potential and trial removed
+    (sim_archive.py:25-32, pyvibdmc.py:934-947).  Unpickled without the
+    reference installed: the object's attribute dict lands here."""
+
+    def __setstate__(self, state):
+        self.__dict__.update(state)
+
+
+class _CheckpointUnpickler(pickle.Unpickler):
+    """Loads this engine's checkpoints (a dict) and the reference's (a pickled
+    DMC_Sim) with a fixed list of globals: the reference's DMC_Sim class
+    (mapped to ReferenceCheckpoint) and NumPy's array and scalar
+    reconstructors, whose module moved from numpy.core to numpy._core in
+    NumPy 2 (either spelling loads with either NumPy)."""
+
+    _NUMPY = {"_reconstruct", "scalar", "ndarray", "dtype", "_frombuffer"}
+
+    def find_class(self, module, name):
+        if (module, name) == ("pyvibdmc.pyvibdmc", "DMC_Sim"):
+            return ReferenceCheckpoint
+        if module in ("numpy", "numpy.core.multiarray", "numpy._core.multiarray", "numpy.core.numeric",
+                      "numpy._core.numeric") and name in self._NUMPY | {"ndarray", "dtype"}:
+            for m in (module, module.replace("numpy._core", "numpy.core"), module.replace("numpy.core", "numpy._core")):
+                try:
+                    return getattr(importlib.import_module(m), name)
+                except (ImportError, AttributeError):
+                    continue
+        if module == "numpy" and name in ("dtype", "ndarray"):
+            return getattr(np, name)
+        if module.startswith("numpy.dtypes") or (module == "builtins" and name in ("set", "frozenset", "slice")):
+            return super().find_class(module, name)
+        raise pickle.UnpicklingError(f"checkpoint refers to {module}.{name}, which a DMC checkpoint does not hold")
+
+
+def load_checkpoint(path):
+    """A checkpoint of this engine (dict) or of the reference (ReferenceCheckpoint)."""
+    with open(path, "rb") as fh:
+        return _CheckpointUnpickler(fh).load()
 
 
 def create_filesystem(output_folder):

@@ -56,6 +56,15 @@ struct Rng {
     ++used;
     return v;
   }
+  // the stream position after k 32-bit draws of a fresh generator
+  __device__ __forceinline__ void skip32(uint32_t k) {
+    slot += k / 4;
+    used = 4;
+    if (k % 4) {
+      buf = block();
+      used = (int)(k % 4);
+    }
+  }
   // uniform in [0,1) with 53 random bits
   // the 53 random bits m of uniform53() = m * 2^-53
   __device__ __forceinline__ uint64_t bits53() {

@@ -48,11 +48,19 @@ __global__ void __launch_bounds__(kMaxTPB) k_init(const __grid_constant__ gbdmc_
     const int64_t slot = T.off[r] + i;
     Partial p = partial_zero();
     if (i < n) {
-      double x[3 * A], g[3 * A];
+      double v;
+      if constexpr (PK == GBDMC_PES_EXTERNAL) {
+        v = W.v[slot];  // the caller's potential
+      } else {
+        double x[3 * A], g[3 * A];
 #pragma unroll
-      for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + slot];
-      double v = pes<PK, A, false>(x, S.pes, g);
-      if constexpr (TK != GBDMC_TRIAL_NONE) {
+        for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + slot];
+        v = pes<PK, A, false>(x, S.pes, g);
+      }
+      if constexpr (TK != GBDMC_TRIAL_NONE && PK != GBDMC_PES_EXTERNAL) {
+        double x[3 * A];
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) x[k] = W.x[k * ld + slot];
         double d1[3 * A], d2[3 * A];
         const double psi = trial<TK, A>(x, S.trial, d1, d2);
         const double ke = local_ke<A>(S, d2);
@@ -184,6 +192,54 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
         ctrl->ticket = 0;
       }
     }
+  }
+}
+
+// ------------------------------------- move for a caller-evaluated potential
+// move_randomly (pyvibdmc.py:540-547) alone: the logical walkers of `in`
+// (through in.idx) moved and written in order to `out`; nc coordinates per
+// walker, d per atom (the reference's (N, A, d) walkers, drawn as (N, d, A)
+// and transposed: coordinate k = d*atom + dim takes sigma[k / d]).  The
+// caller evaluates V on the moved walkers and gbdmc_sim_branch weighs them.
+template <int NM>
+__global__ void __launch_bounds__(kMaxTPB) k_move_ext(const __grid_constant__ gbdmc_sim_t S,
+                                                       const __grid_constant__ RepTable T, const gbdmc_walkers_t in,
+                                                       gbdmc_walkers_t out, const gbdmc_ctrl_t* ctrls, int nc, int d,
+                                                       const gbdmc_noise_t nz) {
+  const int64_t ld = S.ld;
+  const int ntile = T.tile_off[T.nrep];
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r = replica_of(T, tile);
+    const gbdmc_ctrl_t* ctrl = ctrls + r;
+    if (*(volatile const int*)&ctrl->status) continue;
+    const long long n = ctrl->n;
+    const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
+    if (i >= n) continue;
+    const int64_t base = T.off[r];
+    const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+    const int64_t dst = base + i;
+    Rng rng(S.seed, (uint64_t)ctrl->step, (uint64_t)i, T.stream[r]);
+    double z1 = 0.0;
+    for (int k = 0; k < nc; ++k) {
+      double z;
+      if constexpr (NM == GBDMC_NOISE_INJECTED) {
+        z = nz.normal[k * nz.ld_noise + dst];
+      } else if ((k & 1) == 0) {  // normals in pairs, in coordinate order
+        if constexpr (NM == GBDMC_NOISE_PHILOX32) {
+          float a, b;
+          rng.normal2_f32(a, b);
+          z = widen_f32(a);
+          z1 = widen_f32(b);
+        } else {
+          rng.normal2_f64(z, z1);
+        }
+      } else {
+        z = z1;
+      }
+      out.x[k * ld + dst] = __dadd_rn(in.x[k * ld + src], __dmul_rn(S.sigma[k / d], z));
+    }
+    if (out.who && in.who) out.who[dst] = in.who[src];
+    if (S.weighting == GBDMC_CONTINUOUS) out.w[dst] = in.w[src];
   }
 }
 
@@ -532,19 +588,21 @@ __device__ long long block_arg(const double* w, long long n, const unsigned char
   return res;
 }
 
+// A = 0: the atom count is sim->natoms (walkers of a caller-evaluated potential)
 template <int A, bool IS>
 __device__ void clone_walker(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t base, long long from, long long to) {
   const int64_t ld = S.ld;
   const int t = threadIdx.x;
+  const int nat = A > 0 ? A : S.natoms;
   const int64_t f = base + from, d = base + to;
-  if (t < 3 * A) {
+  if (t < 3 * nat) {
     W.x[t * ld + d] = W.x[t * ld + f];
     if constexpr (IS) W.f[t * ld + d] = W.f[t * ld + f];
-  } else if (t == 3 * A) {
+  } else if (t == 3 * nat) {
     W.v[d] = W.v[f];
-  } else if (t == 3 * A + 1) {
+  } else if (t == 3 * nat + 1) {
     if (W.who) W.who[d] = W.who[f];
-  } else if (t == 3 * A + 2) {
+  } else if (t == 3 * nat + 2) {
     if constexpr (IS) {
       W.psi[d] = W.psi[f];
       W.ke[d] = W.ke[f];
@@ -856,7 +914,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
     if (prof) cudaEventRecord(ev[1], s);
     if (S.weighting == GBDMC_DISCRETE) {
-      k_count<NM><<<G, T.tpb, 0, s>>>(S, T, dst.v, ctrl, L.part, L.counts, nz);
+      k_count<NM, true><<<G, T.tpb, 0, s>>>(S, T, dst.v, ctrl, L.part, L.counts, nz);
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {
@@ -1023,6 +1081,22 @@ static int step_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
   return dispatch_system(*S, what, f);
 }
 
+// Layout of a caller-evaluated potential's walkers (GBDMC_PES_EXTERNAL).
+static int ext_layout(const gbdmc_sim_t* S, const char* what, int& nc, int& d) {
+  nc = ext_coords(*S);
+  d = ext_dims(*S);
+  if (S->trial.kind != GBDMC_TRIAL_NONE) {
+    set_error("%s: a caller-evaluated potential runs plain DMC (trial kind must be GBDMC_TRIAL_NONE)", what);
+    return GBDMC_ERR_ARG;
+  }
+  if (d < 1 || d > 3 || nc < 1 || nc > 3 * S->natoms || nc % d || nc / d > GBDMC_MAX_ATOMS) {
+    set_error("%s: bad walker layout (nc=%d coordinates, d=%d per atom, %d storage atoms)", what, nc, d,
+              S->natoms);
+    return GBDMC_ERR_ARG;
+  }
+  return GBDMC_OK;
+}
+
 static int init_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nrep, const gbdmc_walkers_t* W,
                        gbdmc_ctrl_t* ctrl, void* scratch, void* stream, const char* what) {
   int rc = validate(S, W, ctrl, scratch, what);
@@ -1031,6 +1105,12 @@ static int init_common(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int nr
   rc = build_table(*S, reps, nrep, T, what);
   if (rc) return rc;
   const ScratchLayout L = scratch_layout(scratch, slot_extent(S->ld, reps, nrep), max_tiles_for(reps, nrep));
+  if (S->pes.kind == GBDMC_PES_EXTERNAL) {  // V of the start walkers is the caller's (W->v)
+    int nc, d;
+    rc = ext_layout(S, what, nc, d);
+    if (rc) return rc;
+    return run_init<GBDMC_PES_EXTERNAL, 1, GBDMC_TRIAL_NONE>(*S, T, *W, ctrl, L, (cudaStream_t)stream);
+  }
   InitF f{*S, T, *W, ctrl, L, (cudaStream_t)stream};
   return dispatch_system(*S, what, f);
 }
@@ -1086,6 +1166,108 @@ extern "C" int gbdmc_sim_step(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, 
   return step_common(S, &r, 1, src, dst, ctrl, scratch, noise, stream, "gbdmc_sim_step");
 }
 
+extern "C" int gbdmc_sim_move(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                              gbdmc_ctrl_t* ctrl, void* scratch, const gbdmc_noise_t* noise, void* stream) {
+  const char* what = "gbdmc_sim_move";
+  int rc = validate(S, src, ctrl, scratch, what);
+  if (rc) return rc;
+  rc = validate(S, dst, ctrl, scratch, what);
+  if (rc) return rc;
+  if (src->x == dst->x || src->v == dst->v || (src->who && src->who == dst->who)) {
+    set_error("%s: src and dst must use different arrays", what);
+    return GBDMC_ERR_ARG;
+  }
+  if (S->weighting == GBDMC_CONTINUOUS && (dst->idx || src->idx)) {
+    set_error("%s: continuous weighting works on compact walkers (idx must be NULL)", what);
+    return GBDMC_ERR_ARG;
+  }
+  int nc, d;
+  rc = ext_layout(S, what, nc, d);
+  if (rc) return rc;
+  gbdmc_noise_t nz{};
+  if (S->noise_mode == GBDMC_NOISE_INJECTED) {
+    if (!noise || !noise->normal || noise->ld_noise < 1) {
+      set_error("%s: injected noise buffers missing", what);
+      return GBDMC_ERR_ARG;
+    }
+    nz = *noise;
+  }
+  const gbdmc_replica_t r = single_replica(S);
+  RepTable T;
+  rc = build_table(*S, &r, 1, T, what);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (S->noise_mode) {
+    case GBDMC_NOISE_PHILOX32:
+      k_move_ext<GBDMC_NOISE_PHILOX32><<<grid_for(T), T.tpb, 0, s>>>(*S, T, *src, *dst, ctrl, nc, d, nz);
+      break;
+    case GBDMC_NOISE_PHILOX64:
+      k_move_ext<GBDMC_NOISE_PHILOX64><<<grid_for(T), T.tpb, 0, s>>>(*S, T, *src, *dst, ctrl, nc, d, nz);
+      break;
+    case GBDMC_NOISE_INJECTED:
+      k_move_ext<GBDMC_NOISE_INJECTED><<<grid_for(T), T.tpb, 0, s>>>(*S, T, *src, *dst, ctrl, nc, d, nz);
+      break;
+    default:
+      set_error("%s: unknown noise mode %d", what, S->noise_mode);
+      return GBDMC_ERR_ARG;
+  }
+  return check_launch(what);
+}
+
+extern "C" int gbdmc_sim_branch(const gbdmc_sim_t* S, const gbdmc_walkers_t* dst, gbdmc_ctrl_t* ctrl, void* scratch,
+                                const gbdmc_noise_t* noise, void* stream) {
+  const char* what = "gbdmc_sim_branch";
+  int rc = validate(S, dst, ctrl, scratch, what);
+  if (rc) return rc;
+  if (S->weighting == GBDMC_DISCRETE && !dst->idx) {
+    set_error("%s: discrete weighting writes the branch index: dst->idx is required", what);
+    return GBDMC_ERR_ARG;
+  }
+  if (S->weighting == GBDMC_CONTINUOUS && dst->idx) {
+    set_error("%s: continuous weighting works on compact walkers (idx must be NULL)", what);
+    return GBDMC_ERR_ARG;
+  }
+  int nc, d;
+  rc = ext_layout(S, what, nc, d);
+  if (rc) return rc;
+  gbdmc_noise_t nz{};
+  if (S->noise_mode == GBDMC_NOISE_INJECTED && S->weighting == GBDMC_DISCRETE) {
+    if (!noise || !noise->u_branch) {
+      set_error("%s: injected branching uniforms missing", what);
+      return GBDMC_ERR_ARG;
+    }
+    nz = *noise;
+  }
+  const gbdmc_replica_t r = single_replica(S);
+  RepTable T;
+  rc = build_table(*S, &r, 1, T, what);
+  if (rc) return rc;
+  const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(&r, 1));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (S->weighting == GBDMC_CONTINUOUS) {
+    k_cont_branch<0, false><<<1, kCTA, 0, s>>>(*S, T, *dst, ctrl, L.list, L.counts, L.flags);
+    return check_launch(what);
+  }
+  const int G = grid_for(T);
+  switch (S->noise_mode) {
+    case GBDMC_NOISE_PHILOX32:
+      k_count<GBDMC_NOISE_PHILOX32, false><<<G, T.tpb, 0, s>>>(*S, T, dst->v, ctrl, L.part, L.counts, nz);
+      break;
+    case GBDMC_NOISE_PHILOX64:
+      k_count<GBDMC_NOISE_PHILOX64, false><<<G, T.tpb, 0, s>>>(*S, T, dst->v, ctrl, L.part, L.counts, nz);
+      break;
+    case GBDMC_NOISE_INJECTED:
+      k_count<GBDMC_NOISE_INJECTED, false><<<G, T.tpb, 0, s>>>(*S, T, dst->v, ctrl, L.part, L.counts, nz);
+      break;
+    default:
+      set_error("%s: unknown noise mode %d", what, S->noise_mode);
+      return GBDMC_ERR_ARG;
+  }
+  k_count_finalize<<<1, kMaxTPB, 0, s>>>(*S, T, ctrl, L.part, L.prefix);
+  launch_branch(T, dst->idx, ctrl, L.prefix, L.counts, s);
+  return check_launch(what);
+}
+
 extern "C" int gbdmc_batch_init(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
                                 const gbdmc_walkers_t* W, gbdmc_ctrl_t* ctrl, void* scratch, void* stream) {
   if (!reps) {
@@ -1127,7 +1309,11 @@ extern "C" int gbdmc_walkers_compact(const gbdmc_sim_t* S, const gbdmc_replica_t
     case 1: return run_compact<1>(*S, T, *in, *out, ctrl, s);
     case 2: return run_compact<2>(*S, T, *in, *out, ctrl, s);
     case 3: return run_compact<3>(*S, T, *in, *out, ctrl, s);
+    case 4: return run_compact<4>(*S, T, *in, *out, ctrl, s);
+    case 5: return run_compact<5>(*S, T, *in, *out, ctrl, s);
     case 6: return run_compact<6>(*S, T, *in, *out, ctrl, s);
+    case 7: return run_compact<7>(*S, T, *in, *out, ctrl, s);
+    case 8: return run_compact<8>(*S, T, *in, *out, ctrl, s);
   }
   set_error("gbdmc_walkers_compact: unsupported natoms %d", S->natoms);
   return GBDMC_ERR_ARG;

@@ -259,9 +259,19 @@ __device__ __forceinline__ double local_ke(const gbdmc_sim_t& S, const double (&
   return -0.5 * s;
 }
 
+// Coordinates per walker and dimensions per atom of a simulation: the
+// caller's layout for GBDMC_PES_EXTERNAL (pes.p[0], pes.p[1]), else 3 per atom.
+__host__ __device__ __forceinline__ int ext_coords(const gbdmc_sim_t& S) {
+  return (S.pes.kind == GBDMC_PES_EXTERNAL && S.pes.p[0] > 0.0) ? (int)S.pes.p[0] : 3 * S.natoms;
+}
+__host__ __device__ __forceinline__ int ext_dims(const gbdmc_sim_t& S) {
+  return (S.pes.kind == GBDMC_PES_EXTERNAL && S.pes.p[1] > 0.0) ? (int)S.pes.p[1] : 3;
+}
+
 // Discrete weights and counts from stored fp64 energies with dt =
-// ctrl->dt_eff (the importance-sampled fp64 path).
-template <int NM>
+// ctrl->dt_eff (EFF: the importance-sampled fp64 path) or sim->dt (the
+// caller-evaluated potential).
+template <int NM, bool EFF>
 __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc_sim_t S,
                                                     const __grid_constant__ RepTable T, const double* __restrict__ V,
                                                     gbdmc_ctrl_t* ctrls, Partial* part, int* counts,
@@ -278,7 +288,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
     const long long n = ctrl->n;
     const long long step = ctrl->step;
     const double vref = ctrl->vref;
-    const double dt = ctrl->dt_eff;
+    const double dt = EFF ? ctrl->dt_eff : S.dt;
     const double n0 = (double)T.n0[r];
     const double w_hi = (n0 + n0 * 0.5) + 1.0;
     int flag = 0;
@@ -289,7 +299,13 @@ __global__ void __launch_bounds__(kMaxTPB) k_count(const __grid_constant__ gbdmc
         u = nz.u_branch[dst];
       } else {
         Rng rng(S.seed, (uint64_t)step, (uint64_t)i, T.stream[r]);
-        rng.slot = 64;  // stream disjoint from the move's draws
+        if (EFF) {
+          rng.slot = 64;  // stream disjoint from the importance-sampled move's draws
+        } else {
+          // the draw after the move's normals (ext_coords of them, in pairs),
+          // the branching uniform k_move takes for the same walker and step
+          rng.skip32((uint32_t)((ext_coords(S) + 1) / 2) * (NM == GBDMC_NOISE_PHILOX32 ? 2u : 4u));
+        }
         u = rng.uniform53();
       }
       const int c = branch_count(v, vref, dt, u, w_hi, flag, p.births, p.deaths);

@@ -54,15 +54,21 @@ class DMC_Sim:
             raise NotImplementedError(f"DMC_Sim options not provided by the GPU engine: {bad}")
         if branch_every != 1:
             raise NotImplementedError("the GPU engine branches every step (branch_every=1)")
-        if not isinstance(potential, Potential_GPU):
-            raise TypeError("potential must be a pyvibdmc_gb300.Potential_GPU (the PES is fused into the step "
-                            "kernel); wrap analytic surfaces with the factories in pyvibdmc_gb300.potentials")
+        # a built-in GPU surface is fused into the step kernel; any other object with
+        # the reference's getpot(cds) contract (potential_manager.py:71-253) is called on
+        # the moved walkers between the move and branching kernels
+        self._external = not isinstance(potential, Potential_GPU)
+        if self._external and not callable(getattr(potential, "getpot", None)):
+            raise TypeError("potential must have a getpot(cds, timeit=False) method returning (N,) hartree")
+        if self._external and imp_samp is not None:
+            raise NotImplementedError("importance sampling runs with the built-in GPU potentials "
+                                      "(pyvibdmc_gb300.potentials) and trial functions")
         self.atoms = atoms if isinstance(atoms, list) else [atoms]
         self.sim_name = sim_name
         self.output_folder = output_folder
         self.num_walkers = int(num_walkers)
         self.num_timesteps = int(num_timesteps)
-        self.potential_info = {k: v for k, v in vars(potential).items()}
+        self.potential_info = {k: v for k, v in vars(potential).items()} if hasattr(potential, "__dict__") else {}
         self.potential = potential
         self.weighting = weighting.lower()
         self.desc_wt_time_steps = desc_wt_steps
@@ -133,13 +139,22 @@ class DMC_Sim:
             raise Exception("Your number of atoms list does not match your number of masses you provided.")
         if coords.shape[1] != len(self.atoms):
             raise Exception("Your number of atoms list does not match the shape of your walkers.")
-        if coords.shape[2] != 3:
-            raise NotImplementedError("the GPU engine propagates 3D Cartesian walkers")
         self.natoms = coords.shape[1]
-        if self.natoms != self.potential.natoms:
-            raise ValueError(f"potential has {self.potential.natoms} atoms, walkers have {self.natoms}")
+        self.dims = coords.shape[2]
         if self.natoms > _capi.MAX_ATOMS:
             raise ValueError(f"at most {_capi.MAX_ATOMS} atoms")
+        if self._external:
+            if self.dims not in (1, 2, 3):
+                raise ValueError("walkers must have 1, 2 or 3 dimensions per atom")
+        else:
+            if self.dims != 3:
+                raise NotImplementedError("the built-in GPU potentials take 3D Cartesian walkers; pass a "
+                                          "getpot potential for 1D or 2D walkers")
+            if self.natoms != self.potential.natoms:
+                raise ValueError(f"potential has {self.potential.natoms} atoms, walkers have {self.natoms}")
+        # walker rows on the device: 3 per storage atom (the caller's nc = natoms*dims coordinates, padded)
+        self._ncoord = self.natoms * self.dims
+        self._store_atoms = (self._ncoord + 2) // 3
         self._sigmas = np.sqrt(self.delta_t / self.masses)
         self._alpha = 1.0 / (2.0 * self.delta_t) if self._deb_alpha is None else self._deb_alpha
         self._pop_thresh = [self.num_walkers - self.num_walkers * 0.5, self.num_walkers + self.num_walkers * 0.5]
@@ -184,11 +199,12 @@ class DMC_Sim:
         self._eff_ts = np.zeros(self.num_timesteps)
         self._desc_open = None
         self._graphs = {}
+        self._host_vstats = {}
         if self.write_files:
             archive.create_filesystem(self.output_folder)
 
     def _alloc(self, coords):
-        dev, ld, A = self.device, self.capacity, self.natoms
+        dev, ld, A = self.device, self.capacity, self._store_atoms
         f64 = dict(dtype=torch.float64, device=dev)
         IS = self.impsamp_manager is not None
         cont = self.weighting == "continuous"
@@ -206,7 +222,7 @@ class DMC_Sim:
         if cont:
             w0 = np.ones(len(coords)) if self.start_cont_wts is None else np.asarray(self.start_cont_wts, float)
             self._bufs[0]["w"][:len(coords)] = torch.as_tensor(w0, **f64)
-        self._bufs[0]["x"][:, :len(coords)] = to_soa(coords, dev)
+        self._bufs[0]["x"][:self._ncoord, :len(coords)] = to_soa(coords, dev)
         self._cur = 0
         self._lazy = False  # current buffer holds its walkers through a gather index
         self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
@@ -224,7 +240,7 @@ class DMC_Sim:
 
     def _make_sim(self):
         s = _capi.Sim()
-        s.natoms = self.natoms
+        s.natoms = self._store_atoms
         s.weighting = _capi.DISCRETE if self.weighting == "discrete" else _capi.CONTINUOUS
         s.noise_mode = self._noise_mode
         s.track_who = 1
@@ -240,12 +256,16 @@ class DMC_Sim:
         s.seed = self.seed & 0xFFFFFFFFFFFFFFFF
         s.block_threads = self.block_threads
         s.replica_id = self.replica_id
-        s.pes = self.potential.pes_struct()
+        if self._external:
+            s.pes.kind, s.pes.natoms = _capi.PES_EXTERNAL, self._store_atoms
+            s.pes.p[0], s.pes.p[1] = float(self._ncoord), float(self.dims)
+        else:
+            s.pes = self.potential.pes_struct()
         if self.impsamp_manager is not None:
             s.trial = self.impsamp_manager.trial_struct()
         else:
             s.trial.kind = _capi.TRIAL_NONE
-            s.trial.natoms = self.natoms
+            s.trial.natoms = self._store_atoms
         h = self._hist
         s.hist.vref, s.hist.pop = h["vref"].data_ptr(), h["pop"].data_ptr()
         s.hist.births, s.hist.deaths = h["births"].data_ptr(), h["deaths"].data_ptr()
@@ -285,6 +305,9 @@ class DMC_Sim:
         c.step = self.cur_timestep
         c.eff_ts = self._eff_ts[self.cur_timestep - 1] if self.cur_timestep > 0 else 0.0
         self._write_ctrl(c)
+        if self._external:  # step-0 potential (pyvibdmc.py:760-761) from the caller's getpot
+            b = self._bufs[self._cur]
+            b["v"][:c.n] = self._call_potential(b["x"], c.n)
         L = _capi.load()
         _capi.check(L.gbdmc_sim_init(C.byref(self._sim), C.byref(self._walker_struct(self._bufs[self._cur], False)),
                                      C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
@@ -329,11 +352,12 @@ class DMC_Sim:
             self._graphs[key] = g
         return g
 
-    def _injected_step(self, n):
-        """Host-supplied deviates in the reference's draw order (pyvibdmc.py:544, :556, :601, :392)."""
-        A = self.natoms
-        z = np.asarray(self.rng.standard_normal((n, 3, A)), dtype=np.float64)
-        zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(3 * A, n)), device=self.device)
+    def _injected_noise(self, n):
+        """Host-supplied deviates in the reference's draw order (pyvibdmc.py:544, :556, :601, :392):
+        normal (n, dims, natoms) transposed to (n, natoms, dims), then the uniforms."""
+        A, D = self.natoms, self.dims
+        z = np.asarray(self.rng.standard_normal((n, D, A)), dtype=np.float64)
+        zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(D * A, n)), device=self.device)
         ua = None
         if self.impsamp_manager is not None:
             ua = torch.as_tensor(np.asarray(self.rng.uniform(n), dtype=np.float64), device=self.device)
@@ -342,12 +366,71 @@ class DMC_Sim:
         nz = _capi.Noise()
         nz.normal, nz.u_branch = zs.data_ptr(), ub.data_ptr()
         nz.u_accept = ua.data_ptr() if ua is not None else None
-        nz.ld_noise = n
+        nz.ld_noise = max(n, 1)
         self._keep = (zs, ub, ua)
+        return nz
+
+    def _injected_step(self, n):
+        nz = self._injected_noise(n)
         self._cur, self._lazy = self._launch_step(self._cur, self._lazy, nz)
+
+    def _call_potential(self, x, n, timeit=False):
+        """V of the first n walkers of the SoA device array x from the caller's
+        potential: ``getpot_device`` on a CUDA tensor when the object has one,
+        else ``getpot`` on an (n, natoms, dims) NumPy array (the reference's call,
+        pyvibdmc.py:785-793).  Returns a float64 device tensor of length n."""
+        dev_fn = getattr(self.potential, "getpot_device", None)
+        xs = x[:self._ncoord, :n].t().reshape(n, self.natoms, self.dims)
+        t0 = time.perf_counter()
+        if dev_fn is not None:
+            v = dev_fn(xs.contiguous())
+            v = torch.as_tensor(v, dtype=torch.float64, device=self.device).reshape(-1)
+        else:
+            out = self.potential.getpot(np.ascontiguousarray(xs.cpu().numpy()))
+            v = torch.as_tensor(np.asarray(out, dtype=np.float64).reshape(-1), device=self.device)
+        self._pot_secs = time.perf_counter() - t0
+        if v.numel() != n:
+            raise ValueError(f"getpot returned {v.numel()} energies for {n} walkers")
+        return v
+
+    def _external_step(self, noise=None):
+        """One step around the caller's potential: gbdmc_sim_move, getpot on the
+        moved walkers, gbdmc_sim_branch (pyvibdmc.py:540-547, 785-793, 380-454,
+        651-682).  Returns False when a guard stopped the run."""
+        L = _capi.load()
+        n = self._n_now
+        src = self._walker_struct(self._bufs[self._cur], self._lazy)
+        b = self._bufs[1 - self._cur]
+        dst = self._walker_struct(b, True)
+        nz = C.byref(noise) if noise is not None else None
+        _capi.check(L.gbdmc_sim_move(C.byref(self._sim), C.byref(src), C.byref(dst), C.c_void_p(self._ctrl.data_ptr()),
+                                     C.c_void_p(self._scratch.data_ptr()), nz, self._stream()), "gbdmc_sim_move")
+        v = self._call_potential(b["x"], n)
+        b["v"][:n] = v
+        step = int(self._step_device)
+        vn = v.cpu().numpy() if n else np.zeros(1)
+        self._host_vstats[step] = (float(vn.min()), float(vn.max()), float(vn.mean()))
+        _capi.check(L.gbdmc_sim_branch(C.byref(self._sim), C.byref(dst), C.c_void_p(self._ctrl.data_ptr()),
+                                       C.c_void_p(self._scratch.data_ptr()), nz, self._stream()), "gbdmc_sim_branch")
+        self._cur, self._lazy = 1 - self._cur, self.weighting == "discrete"
+        c = self._read_ctrl()
+        self._n_now = int(c.n)
+        self._step_device = int(c.step)
+        return not c.status
 
     def _run_steps(self, nsteps):
         """Queue nsteps steps (no host sync in the Philox modes)."""
+        if self._external:
+            c = self._read_ctrl()
+            self._n_now, self._step_device = int(c.n), int(c.step)
+            for _ in range(nsteps):
+                if self._noise_mode == _capi.NOISE_INJECTED:
+                    nz = self._injected_noise(self._n_now)
+                else:
+                    nz = None
+                if not self._external_step(nz):
+                    return
+            return
         if self._noise_mode == _capi.NOISE_INJECTED:
             for _ in range(nsteps):
                 c = self._read_ctrl()
@@ -378,7 +461,8 @@ class DMC_Sim:
     def _coords_host(self, n=None):
         self._compact()
         n = self._n_device() if n is None else n
-        return from_soa(self._bufs[self._cur]["x"], n, self.natoms)
+        x = self._bufs[self._cur]["x"]
+        return x[:self._ncoord, :n].t().reshape(n, self.natoms, self.dims).cpu().numpy()
 
     def _begin_desc(self, t):
         """pyvibdmc.py:739-747."""
@@ -428,6 +512,11 @@ class DMC_Sim:
 
     def _sync_history(self, t0, t1):
         h = {k: v[t0:t1].cpu().numpy() for k, v in self._hist.items()}
+        if self._external:  # the potential's statistics come from the host-side energies
+            for t in range(t0, t1):
+                s = self._host_vstats.pop(t, None)
+                if s is not None:
+                    h["vmin"][t - t0], h["vmax"][t - t0], h["vmean"][t - t0] = s
         self._vref_vs_tau[t0:t1] = h["vref"]
         self._pop_vs_tau[t0:t1] = h["pop"]
         self._eff_ts[t0:t1] = h["eff_ts"]
@@ -595,6 +684,9 @@ class HostWalkers:
         self._graph = None
         if sim._noise_mode == _capi.NOISE_INJECTED:
             raise ValueError("HostWalkers steps with Philox deviates (rng='philox32' or 'philox64')")
+        if sim._external:
+            raise ValueError("HostWalkers steps the built-in GPU potentials; a getpot potential is stepped by "
+                             "DMC_Sim.run")
         sim._compact()
         torch.cuda.synchronize()
         self.sim = sim
@@ -691,8 +783,9 @@ def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsa
              if archive.checkpoint_step(p) is not None]
     if not files:
         raise FileNotFoundError(f"no checkpoint for {sim_name} in {chkpt_folder}/chkpts")
-    with open(max(files, key=archive.checkpoint_step), "rb") as fh:
-        st = pickle.load(fh)
+    st = archive.load_checkpoint(max(files, key=archive.checkpoint_step))
+    if isinstance(st, archive.ReferenceCheckpoint):
+        return _restart_from_reference(st, potential, chkpt_folder, sim_name, additional_timesteps, impsamp, **kw)
     nxt = int(st.get("_next_step", st["cur_timestep"]))
     archive.delete_future_checkpoints(chkpt_folder, sim_name, nxt)
     T = st["num_timesteps"] + additional_timesteps
@@ -710,4 +803,46 @@ def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsa
     sim._vref_vs_tau[:n] = st["_vref_vs_tau"]
     sim._pop_vs_tau[:n] = st["_pop_vs_tau"]
     sim._eff_ts[:n] = st["_eff_ts"]
+    return sim
+
+
+def _restart_from_reference(st, potential, chkpt_folder, sim_name, additional_timesteps, impsamp, **kw):
+    """dmc_restart from a checkpoint the reference wrote (its pickled DMC_Sim,
+    sim_archive.py:25-43).  As the reference's dmc_restart / _init_restart
+    (pyvibdmc.py:299-338, 949-965) does, the run continues with step
+    ``cur_timestep`` of the checkpoint, the schedules are extended by
+    ``additional_timesteps``, the step-0 potential and vref are taken afresh
+    from the saved walkers, and an open descendant-weighting window keeps its
+    parents, parent weights and ancestor indices."""
+    d = st.__dict__
+    nxt = int(d["cur_timestep"])
+    archive.delete_future_checkpoints(chkpt_folder, sim_name, nxt)
+    T = int(d["num_timesteps"]) + int(additional_timesteps)
+    masses = np.asarray(d["masses"], dtype=np.float64)
+    scalar_mass = list(d.get("_atm_nums", [])) == [-1] and masses.size == 1
+    coords = np.asarray(d["_walker_coords"], dtype=np.float64)
+    cont = d["weighting"] == "continuous"
+    kw.setdefault("seed", 0)
+    sim = DMC_Sim(sim_name=d["sim_name"], output_folder=d["output_folder"], weighting=d["weighting"],
+                  num_walkers=int(d["num_walkers"]), num_timesteps=T, equil_steps=int(d["equil_steps"]),
+                  chkpt_every=int(d["chkpt_every"]), wfn_every=int(d["wfn_every"]),
+                  desc_wt_steps=int(d["desc_wt_time_steps"]), atoms=list(d["atoms"]), delta_t=d["delta_t"],
+                  potential=potential, masses=float(masses[0]) if scalar_mass else list(masses),
+                  start_structures=coords, start_cont_wts=np.asarray(d["_cont_wts"]) if cont else None,
+                  branch_every=int(d.get("branch_every", 1)), log_every=int(d["log_every"]), cur_timestep=nxt,
+                  cont_wt_thresh=d.get("cont_wt_thresh"), imp_samp=impsamp, DEBUG_alpha=d.get("_deb_alpha"),
+                  DEBUG_save_training_every=d.get("_deb_training_every"), **kw)
+    n = min(len(d["_vref_vs_tau"]), T)
+    sim._vref_vs_tau[:n] = np.asarray(d["_vref_vs_tau"])[:n]
+    sim._pop_vs_tau[:n] = np.asarray(d["_pop_vs_tau"])[:n]
+    if impsamp is not None and d.get("eff_ts") is not None:
+        m = min(len(d["eff_ts"]), T)
+        sim._eff_ts[:m] = np.asarray(d["eff_ts"])[:m]
+    if d.get("_desc_wt"):  # inside a descendant-weighting window (pyvibdmc.py:739-747)
+        starts = [int(s) for s in np.asarray(d["_wfn_save_step"]) if s <= nxt]
+        sim._parent = np.asarray(d["_parent"], dtype=np.float64)
+        sim._parent_wts = np.asarray(d["_parent_wts"], dtype=np.float64) if cont else None
+        who = np.asarray(d["_who_from"], dtype=np.int32)
+        sim._bufs[sim._cur]["who"][:len(who)] = torch.as_tensor(who, device=sim.device)
+        sim._desc_open = max(starts) if starts else nxt
     return sim

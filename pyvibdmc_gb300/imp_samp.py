@@ -21,7 +21,7 @@ from .constants import Constants
 from .potentials import to_soa, from_soa, default_device, _ptr, _stream
 
 __all__ = ["ImpSampManager_GPU", "TrialFunction", "h2o_gaussian_trial", "ho_gaussian_trial",
-           "dimer_gaussian_trial"]
+           "dimer_gaussian_trial", "local_energy", "fit_trial"]
 
 
 class ImpSampManager_GPU:
@@ -140,3 +140,58 @@ def ho_gaussian_trial(masses, omega_wavenumbers, device=None):
     """Separable Gaussian with alpha_a = m_a omega per atom."""
     w = Constants.convert(omega_wavenumbers, "wavenumbers")
     return ImpSampManager_GPU("ho_gauss", [m * w for m in masses], natoms=len(masses), device=device)
+
+
+def local_energy(manager, potential, x, n, masses):
+    """E_L = V + local kinetic energy (imp_samp.py:49-53, pyvibdmc.py:807-809) of
+    the first n walkers of the SoA device array x (3A, ld): V from the GPU
+    potential, the kinetic part -1/2 sum_k (1/m) (d2 psi/dx_k^2)/psi from the
+    trial's adjoint kernel.  Returns a float64 device tensor."""
+    v = potential.eval_soa(x, n)
+    _, _, d2 = manager.eval_soa(x, n)
+    inv_m = torch.as_tensor(np.repeat(1.0 / np.asarray(masses, dtype=np.float64), 3), device=x.device)
+    return v - 0.5 * (inv_m[:, None] * d2[:, :n]).sum(0)
+
+
+def fit_trial(manager, potential, x, n, masses, maxiter=600, verbose=False):
+    """Variance minimisation of the local energy over a sample of walkers.
+
+    The trial's parameters are set to minimise Var(E_L) over the n walkers of
+    x (for example the walkers of a plain DMC run, which sample the ground
+    state): E_L is the same constant everywhere for the exact ground state, so
+    a smaller spread means a trial closer to it, a smaller time-step error of
+    the importance-sampled walk and a smaller variance of its energy.  The
+    symmetric parameters are fitted together: for 'h2o_gauss' the stretch
+    exponent and centre (shared by r1 and r2), the bend exponent and centre;
+    'dimer_gauss' adds the O-O exponent and centre.  Exponents are fitted on a
+    log scale (Nelder-Mead).  Returns a new ImpSampManager_GPU and the
+    standard deviations of E_L (hartree) before and after."""
+    from scipy.optimize import minimize
+    if manager.kind not in ("h2o_gauss", "dimer_gauss"):
+        raise ValueError("fit_trial fits the h2o_gauss and dimer_gauss trials")
+    dimer = manager.kind == "dimer_gauss"
+    a0, q0 = list(manager.alpha), list(manager.qe)
+    p0 = [np.log(a0[0]), np.log(a0[2]), q0[0], q0[2]] + ([np.log(a0[3]), q0[3]] if dimer else [])
+    v = potential.eval_soa(x, n)
+    inv_m = torch.as_tensor(np.repeat(1.0 / np.asarray(masses, dtype=np.float64), 3), device=x.device)
+
+    def make(p):
+        al = [np.exp(p[0]), np.exp(p[0]), np.exp(p[1])]
+        qe = [p[2], p[2], p[3]]
+        if dimer:
+            al.append(np.exp(p[4]))
+            qe.append(p[5])
+        return ImpSampManager_GPU(manager.kind, al, qe, natoms=manager.natoms, device=manager.device)
+
+    def spread(p):
+        _, _, d2 = make(p).eval_soa(x, n)
+        el = v - 0.5 * (inv_m[:, None] * d2[:, :n]).sum(0)
+        s = float(el.std())
+        return s if np.isfinite(s) else 1e30
+
+    s0 = spread(p0)
+    res = minimize(spread, p0, method="Nelder-Mead",
+                   options=dict(maxiter=maxiter, xatol=1e-4, fatol=s0 * 1e-6, adaptive=True))
+    if verbose:
+        print(f"fit_trial: sd(E_L) {s0:.6g} -> {res.fun:.6g} Eh in {res.nit} iterations")
+    return make(res.x), s0, float(res.fun)

@@ -191,7 +191,7 @@ def run_reference(pv, out_dir, name, x0, atoms, masses, dt, nsteps, pes, seed, w
     return out
 
 
-def main(ref_path, only=None):
+def main(ref_path, only=None):  # noqa: C901
     pv = _import_reference(ref_path)
     tmp = tempfile.mkdtemp(prefix="gbdmc_golden_")
     fixtures = {}
@@ -242,6 +242,87 @@ def main(ref_path, only=None):
         fixtures[name] = dict(x0=x0 if n <= 1000 else np.zeros(0), seed=seed, dt=10.0, nsteps=nsteps,
                               thresh=np.array(thr), equil=1, desc=nsteps - 2, numpy_version=np.__version__,
                               npy_disable_cpu_features=os.environ.get("NPY_DISABLE_CPU_FEATURES", ""), **r)
+
+    # --- the reference's own 1D sample potential (sample_potentials/PythonPots/
+    # harmonicOscillator1D.py), imported from the checkout, as its tests run it
+    # (tests/test_pyvibdmc.py:14-48: atoms ["O-H"], (1,1,1) start): discrete with a
+    # descendant window, continuous with both thresholds, and the pot_kwargs +
+    # pass_timestep variant through Potential_Direct.  Energies of probe geometries
+    # pin the oracle's restatement of the sample functions.
+    sys.path.insert(0, os.path.join(ref_path, "pyvibdmc", "sample_potentials", "PythonPots"))
+    import harmonicOscillator1D as ho1d  # noqa: E402
+    probe = 0.3 * oracle.InjectedNoise(808).standard_normal((64, 1, 1))
+    kw = {"mass": float(pv.Constants.reduced_mass("O-H")), "freq": float(pv.Constants.convert(3700.0, "wavenumbers"))}
+    n = 200
+    x0 = np.zeros((1, 1, 1))
+    runs = {}
+    for name, pot, weighting, thresh, seed in (
+            ("oh_1d", pv.Potential_Direct(ho1d.oh_stretch_harm), "discrete", None, 8),
+            ("oh_1d_cont", pv.Potential_Direct(ho1d.oh_stretch_harm), "continuous", [0.05, 2.5], 9),
+            ("oh_1d_kwargs", pv.Potential_Direct(ho1d.oh_stretch_harm_with_arg, pot_kwargs=dict(kw),
+                                                 pass_timestep=True), "discrete", None, 10)):
+        noise = oracle.InjectedNoise(seed)
+        kwd = dict(sim_name=name, output_folder=os.path.join(tmp, name), weighting=weighting, num_walkers=n,
+                   num_timesteps=60, equil_steps=20, chkpt_every=10 ** 6, wfn_every=10 ** 6, desc_wt_steps=15,
+                   atoms=["O-H"], delta_t=5.0, potential=pot, start_structures=x0.copy(), log_every=10 ** 6,
+                   cont_wt_thresh=thresh)
+        sim = pv.DMC_Sim(**kwd)
+        with _Patch(noise):
+            sim.run()
+        r = dict(vref=np.array(sim._vref_vs_tau), pop=np.array(sim._pop_vs_tau), x_final=np.array(sim._walker_coords),
+                 v_final=np.array(sim._walker_pots), seed=seed, n=n, dt=5.0, nsteps=60, equil=20, desc=15,
+                 thresh=np.array(thresh if thresh else []), masses=np.array(sim.masses))
+        if weighting == "continuous":
+            r["w_final"] = np.array(sim._cont_wts)
+        wf = [k for k in H5_STORE if "/wfns/" in k and k.startswith(kwd["output_folder"])]
+        for key, val in H5_STORE[sorted(wf)[0]].items():
+            r[f"wfn0_{key}"] = val
+        if name == "oh_1d":
+            r.update(probe=probe, probe_v=ho1d.oh_stretch_harm(probe.copy()),
+                     probe_v_kwargs=ho1d.oh_stretch_harm_with_arg(probe.copy(), dict(kw)),
+                     kw_mass=kw["mass"], kw_freq=kw["freq"])
+        runs[name] = r
+    fixtures.update(runs)
+
+    # --- checkpoints the reference writes (SimArchivist.chkpt: its pickled DMC_Sim) and
+    # the reference's own dmc_restart continuing from them: a 1D continuous-weight run
+    # checkpointed inside an open descendant-weighting window (like the reference's
+    # restart fixture chkpts/pytest_364.pickle), and a 3D discrete water run.  The
+    # checkpoint is the one a finished run leaves (written after its last step, with
+    # cur_timestep = that step; the reference's restart runs that step again).  The
+    # fixture keeps the checkpoint file's bytes and the restarted run's results.
+    p, masses = oracle.h2o_config()
+    eq = oracle.h2o_equilibrium(p)
+    for name, pot_fn, atoms, x0, weighting, thresh, steps, chk, add, s1, s2, dt in (
+            ("restart_oh_cont", ho1d.oh_stretch_harm, ["O-H"], np.zeros((1, 1, 1)), "continuous", [0.05, 2.5],
+             30, 29, 20, 11, 12, 5.0),
+            ("restart_h2o_disc", lambda c, p=p: oracle.pes_h2o_lm(c, p), ["O", "H", "H"],
+             eq[None] + 0.05 * oracle.InjectedNoise(909).standard_normal((256, 3, 3)), "discrete", None,
+             30, 29, 10, 13, 14, 10.0)):
+        folder = os.path.join(tmp, name)
+        n = 200 if len(x0) == 1 else len(x0)
+        kwd = dict(sim_name=name, output_folder=folder, weighting=weighting, num_walkers=n, num_timesteps=steps,
+                   equil_steps=5, chkpt_every=10 ** 6, wfn_every=1000, desc_wt_steps=30, atoms=atoms, delta_t=dt,
+                   potential=pv.Potential_Direct(pot_fn), start_structures=np.array(x0, copy=True),
+                   log_every=10 ** 6, cont_wt_thresh=thresh, masses=None if atoms == ["O-H"] else masses)
+        sim = pv.DMC_Sim(**kwd)
+        with _Patch(oracle.InjectedNoise(s1)):
+            sim.run()
+        ck = os.path.join(folder, "chkpts", f"{name}_{chk}.pickle")
+        blob = np.frombuffer(open(ck, "rb").read(), dtype=np.uint8).copy()
+        for k in [k for k in H5_STORE if k.startswith(folder)]:
+            del H5_STORE[k]
+        r2 = pv.dmc_restart(pv.Potential_Direct(pot_fn), folder, name, additional_timesteps=add)
+        with _Patch(oracle.InjectedNoise(s2)):
+            r2.run()
+        out = dict(pickle=blob, chkpt_step=chk, additional=add, seed2=s2, vref=np.array(r2._vref_vs_tau),
+                   pop=np.array(r2._pop_vs_tau), x_final=np.array(r2._walker_coords))
+        if weighting == "continuous":
+            out["w_final"] = np.array(r2._cont_wts)
+        wf = sorted(k for k in H5_STORE if "/wfns/" in k and k.startswith(folder))
+        for key, val in H5_STORE[wf[0]].items():
+            out[f"wfn0_{key}"] = val
+        fixtures[name] = out
 
     # --- config-3 family: importance sampling with the Gaussian internal trial
     alpha, qe = oracle.h2o_trial_config(p)

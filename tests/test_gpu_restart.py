@@ -92,3 +92,44 @@ def test_run_writes_the_reference_files(tmp_path, weighting):
             assert w["desc_wts"].sum() == s._pop_vs_tau[w["start"] + 4]
     assert sorted(os.listdir(f"{out}/chkpts")) == ["f_29.pickle"]
     assert "Simulation has finished." in open(f"{out}/f_log.txt").read()
+
+
+def _golden(name):
+    import os
+    with np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.mark.parametrize("name", ["restart_oh_cont", "restart_h2o_disc"])
+def test_restart_from_a_checkpoint_the_reference_wrote(name, tmp_path):
+    """dmc_restart reads the reference's own checkpoint (its pickled DMC_Sim, written
+    by the unmodified reference) and continues it as the reference's dmc_restart
+    does: the run restarted here matches the reference's restarted run on the same
+    deviates -- walkers bit for bit, weights, vref and descendant weights of the
+    window left open in the checkpoint within 1e-12."""
+    g = _golden(name)
+    folder = tmp_path / name
+    (folder / "chkpts").mkdir(parents=True)
+    (folder / "chkpts" / f"{name}_{int(g['chkpt_step'])}.pickle").write_bytes(g["pickle"].tobytes())
+    if name == "restart_oh_cont":
+        pot = pg.Potential_Direct(oracle.oh_stretch_harm)
+    else:
+        p, _ = oracle.h2o_config()
+        pot = pg.Potential_Direct(lambda c: oracle.pes_h2o_lm(c, p))
+    sim = pg.dmc_restart(pot, str(folder), name, additional_timesteps=int(g["additional"]),
+                         rng=oracle.InjectedNoise(int(g["seed2"])), write_files=False)
+    assert sim.cur_timestep == int(g["chkpt_step"])
+    sim.run()
+    if sim.weighting == "continuous":
+        x, w = sim.walkers
+        np.testing.assert_allclose(w, g["w_final"], rtol=1e-12)
+        np.testing.assert_allclose(sim._pop_vs_tau, g["pop"], rtol=1e-12)
+        np.testing.assert_allclose(sim.wfns[0]["parent_wts"], g["wfn0_parent_wts"], rtol=1e-12)
+        np.testing.assert_allclose(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"], rtol=1e-12)
+    else:
+        x = sim.walkers
+        np.testing.assert_array_equal(sim._pop_vs_tau, g["pop"])
+        assert np.array_equal(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"])
+    assert np.array_equal(x, g["x_final"])
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    assert np.array_equal(sim.wfns[0]["coords"], g["wfn0_coords"])

@@ -137,3 +137,42 @@ def test_dmc_sim_keeps_the_reference_constructor():
     for name in ("DMC_Sim", "dmc_restart", "Constants", "Potential_GPU", "ImpSampManager_GPU", "NN_Potential_GPU",
                  "HarmonicAnalysis", "InitialConditioner"):
         assert hasattr(pg, name), name
+
+
+def _golden(name):
+    with np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.mark.parametrize("name", ["restart_oh_cont", "restart_h2o_disc"])
+def test_reference_checkpoints_load_without_the_reference(name, tmp_path):
+    from pyvibdmc_gb300 import archive
+    g = _golden(name)
+    path = tmp_path / "c.pickle"
+    path.write_bytes(g["pickle"].tobytes())
+    st = archive.load_checkpoint(str(path))
+    assert isinstance(st, archive.ReferenceCheckpoint)
+    assert int(st.cur_timestep) == int(g["chkpt_step"]) and st.sim_name == name
+    assert st._walker_coords.ndim == 3 and st._desc_wt  # saved inside a descendant-weighting window
+    assert len(st._who_from) == len(st._walker_coords)
+
+
+def test_checkpoint_loader_refuses_foreign_globals(tmp_path):
+    import pickle
+    from pyvibdmc_gb300 import archive
+    path = tmp_path / "evil.pickle"
+    with open(path, "wb") as fh:
+        pickle.dump({"f": os.path.join}, fh, protocol=4)  # a function global: not checkpoint data
+    with pytest.raises(pickle.UnpicklingError):
+        archive.load_checkpoint(str(path))
+
+
+@pytest.mark.skipif(not os.environ.get("GBDMC_REFERENCE"), reason="set GBDMC_REFERENCE to a reference checkout")
+def test_the_reference_shipped_restart_fixture_loads():
+    # the reference's own restart fixture (sample_sim_data/chkpts/pytest_364.pickle,
+    # used by tests/test_pyvibdmc.py:152-169)
+    from pyvibdmc_gb300 import archive
+    st = archive.load_checkpoint(os.path.join(os.environ["GBDMC_REFERENCE"],
+                                              "pyvibdmc/sample_sim_data/chkpts/pytest_364.pickle"))
+    assert int(st.cur_timestep) == 364 and st.weighting == "continuous" and st._walker_coords.shape == (5000, 1, 1)
+    assert list(st._atm_nums) == [-1] and st.cont_wt_thresh == [0.002, 15]

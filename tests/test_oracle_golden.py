@@ -130,6 +130,37 @@ def check_cont_upper(name):
     assert not np.array_equal(low.x, sim.x)
 
 
+@pytest.mark.parametrize("name", ["oh_1d", "oh_1d_cont", "oh_1d_kwargs"])
+def test_reference_sample_potential_runs_match_reference(name):
+    # the reference's 1D sample potential (harmonicOscillator1D.py) run by the
+    # unmodified reference on (N, 1, 1) walkers: the oracle with its restatement
+    # of the sample function reproduces walkers, populations, vref and the
+    # descendant weights bit for bit
+    out = _in_numpy_without_simd(f"import test_oracle_golden as t; t.check_oh_1d({name!r}); print('OK')")
+    assert out.strip().endswith("OK")
+
+
+def check_oh_1d(name):
+    g = load(name)
+    g0 = load("oh_1d")
+    kw = {"mass": float(g0["kw_mass"]), "freq": float(g0["kw_freq"])}
+    pes = (lambda c: oracle.oh_stretch_harm(c, kw)) if name == "oh_1d_kwargs" else oracle.oh_stretch_harm
+    assert np.array_equal(oracle.oh_stretch_harm(g0["probe"]), g0["probe_v"])
+    assert np.array_equal(oracle.oh_stretch_harm(g0["probe"], kw), g0["probe_v_kwargs"])
+    n = int(g["n"])
+    cont = g["thresh"].size > 0
+    sim = oracle.OracleDMC(np.zeros((n, 1, 1)), g["masses"], float(g["dt"]), pes, oracle.InjectedNoise(int(g["seed"])),
+                           weighting="continuous" if cont else "discrete",
+                           cont_wt_thresh=list(g["thresh"]) if cont else None, equil_steps=int(g["equil"]),
+                           wfn_every=10 ** 6, desc_wt_steps=int(g["desc"])).run(int(g["nsteps"]))
+    assert np.array_equal(sim.x, g["x_final"])
+    assert np.array_equal(np.array(sim.vref_hist), g["vref"])
+    assert np.array_equal(np.array(sim.pop_hist), g["pop"])
+    assert np.array_equal(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"])
+    if cont:
+        assert np.array_equal(sim.w, g["w_final"])
+
+
 def test_continuous_replacement_rules_by_hand():
     # pyvibdmc.py:340-356, 432-454: below `lower` in slot order, then
     # np.argpartition(w, n_up)[:n_up], each replaced by a copy of the current
