@@ -8,14 +8,19 @@ branching + vref) over the current population.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  ``value``: device-resident walker-steps/s,
-each step timed with CUDA events on the launching stream, with a 256 MiB
-buffer written between steps so every step starts with the walkers in HBM
-(L2 flushed).  ``e2e``: the same metric through the C ABI with the walkers in
-pinned host memory: every step copies them host->device, runs
-``gbdmc_sim_step`` and copies the branched walkers and the control block
-back.  ``--impl reference`` times the CPU restatement of the reference's
-step loop (oracle/) on the host cores.
+Prints one JSON line (rank 0).  A bench step is one 50-step descendant-
+weighting window of the workload (gbdmc_desc_begin, 50 DMC steps in one
+gbdmc_sim_run launch with the walkers resident in shared memory,
+gbdmc_desc_weights).  ``value``: device-resident walker-steps/s, each window
+timed with CUDA events on the launching stream, a 256 MiB buffer written
+between windows so that every window starts with the walkers in HBM (L2
+flushed).  ``e2e``: the same metric through the C ABI with the walkers in
+page-locked host memory between calls: per window the walkers are copied
+host -> device, gbdmc_sim_run advances them, and the control block, the
+branched walkers and the window's history are copied back.  The per-step
+kernels (gbdmc_sim_step, L2 flushed every step) are reported under config.
+``--impl reference`` times the CPU restatement of the reference's step loop
+(oracle/) on the host cores.
 """
 import argparse
 import ctypes as C
@@ -242,41 +247,49 @@ def run_ours(args):
     sp = C.c_void_p(stream.cuda_stream)
     masses = [pg.Constants.mass("O"), pg.Constants.mass("H"), pg.Constants.mass("H")]
     K, W = args.steps, args.warmup
-    sim = pg.DMC_Sim(sim_name="bench", num_walkers=N_WALKERS, num_timesteps=W + 3 * K + 1100, equil_steps=10 ** 9,
+    T = (W + K + 4) * DESC_WINDOW + 2000
+    sim = pg.DMC_Sim(sim_name="bench", num_walkers=N_WALKERS, num_timesteps=T, equil_steps=10 ** 9,
                      atoms=["O", "H", "H"], masses=masses, delta_t=DT, potential=pg.h2o_local_mode(),
-                     start_structures=start_structures(N_WALKERS, 1 + rank), seed=1234 + rank, write_files=False)
+                     start_structures=start_structures(N_WALKERS, 1 + rank), seed=1234 + rank, write_files=False,
+                     fused_steps=DESC_WINDOW)
     sim._init_device()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     ctrl_ptr = C.c_void_p(sim._ctrl.data_ptr())
-
-    def who_ptr():
-        return C.c_void_p(sim._bufs[sim._cur]["who"].data_ptr())
-
+    run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(), dtype=torch.uint8, device=dev)
     desc = torch.zeros(int(sim.capacity), dtype=torch.float64, device=dev)
-    launches = [0]
+    evs = []
 
-    def one_step(i):
-        if i % DESC_WINDOW == 0:
-            launches[0] += 1 if sim._lazy else 0
-            sim._compact()
-            _capi.check(L.gbdmc_desc_begin(who_ptr(), ctrl_ptr, sp), "desc_begin")
-            launches[0] += 1
-        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
-        launches[0] += 2
-        if (i + 1) % DESC_WINDOW == 0:
-            sim._compact()
-            _capi.check(L.gbdmc_desc_weights(who_ptr(), None, ctrl_ptr, int(sim.capacity), C.c_void_p(desc.data_ptr()),
-                                             sp), "desc_weights")
-            launches[0] += 3
+    def window(step_end, ev=None):
+        """One descendant-weighting window of config 2: desc_begin, DESC_WINDOW
+        steps in one gbdmc_sim_run launch (walkers resident in shared memory),
+        desc_weights.  Three launches of this library."""
+        b = sim._bufs[sim._cur]
+        if ev is not None:
+            ev[0].record(stream)
+        _capi.check(L.gbdmc_desc_begin(C.c_void_p(b["who"].data_ptr()), ctrl_ptr, sp), "desc_begin")
+        if ev is not None:
+            ev[1].record(stream)
+        src = sim._walker_struct(b, False)
+        out = sim._bufs[1 - sim._cur]
+        dst = sim._walker_struct(out, False)
+        _capi.check(L.gbdmc_sim_run(C.byref(sim._sim), C.byref(src), C.byref(dst), ctrl_ptr,
+                                    C.c_void_p(run_scratch.data_ptr()), step_end, DESC_WINDOW, sp), "sim_run")
+        sim._cur = 1 - sim._cur
+        if ev is not None:
+            ev[2].record(stream)
+        _capi.check(L.gbdmc_desc_weights(C.c_void_p(out["who"].data_ptr()), None, ctrl_ptr, int(sim.capacity),
+                                         C.c_void_p(desc.data_ptr()), sp), "desc_weights")
+        if ev is not None:
+            ev[3].record(stream)
 
+    sim._compact()
+    s = int(sim._read_ctrl().step)
     for i in range(W):
-        one_step(i)
+        window(s + (i + 1) * DESC_WINDOW)
     torch.cuda.synchronize()
     step0 = int(sim._read_ctrl().step)
-    # ---- timed: per-step events, L2 flushed between steps
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    launches[0] = 0
+    # ---- timed: one event quadruple per window, L2 flushed between windows
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -284,60 +297,63 @@ def run_ours(args):
         wall0 = time.perf_counter()
         for i in range(K):
             flush.fill_(i & 0xFF)
-            ev0[i].record(stream)
-            one_step(W + i)
-            ev1[i].record(stream)
+            window(step0 + (i + 1) * DESC_WINDOW, evs[i])
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
-    gpu_launches = launches[0]
-    ms = float(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)))
+    gpu_launches = 3 * K
+    ms = float(sum(e[0].elapsed_time(e[3]) for e in evs))
+    run_ms = [e[1].elapsed_time(e[2]) for e in evs]
     c = sim._read_ctrl()
     if c.status:
         raise RuntimeError(f"device status {c.status} during the bench")
-    pop = sim._hist["pop"][step0 - 1:step0 - 1 + K].cpu().numpy()
-    walker_steps = float(pop.sum())  # population entering each timed step
+    step1 = int(c.step)
+    pops = sim._hist["pop"][step0 - 1:step1 - 1].cpu().numpy()
+    walker_steps = float(pops.sum())  # the population entering each timed step
     if dist is not None:
         ms, walker_steps = reduce_over_ranks(ms, walker_steps, dist, dev)
     value = walker_steps / (ms / 1e3)
     ms_per_step = ms / K
 
-    # ---- warm-L2 graph replay (information: back-to-back steps as DMC_Sim.run issues them)
-    gsteps = 32
-    sim.graph_steps = gsteps
-    if not sim._lazy:
-        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
-    g = sim._graph_for(sim._cur, sim._lazy)
-    g.replay()
-    torch.cuda.synchronize()
-    s_before = int(sim._read_ctrl().step)
-    reps = max(1, K // gsteps)
+    # ---- the same windows back to back without flushing (information)
     e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_before = int(sim._read_ctrl().step)
     e_a.record(stream)
-    for _ in range(reps):
-        g.replay()
+    for i in range(K):
+        window(s_before + (i + 1) * DESC_WINDOW)
     e_b.record(stream)
     torch.cuda.synchronize()
     s_after = int(sim._read_ctrl().step)
-    popg = sim._hist["pop"][s_before - 1:s_after - 1].cpu().numpy()
-    graph_rate = float(popg.sum()) / (e_a.elapsed_time(e_b) / 1e3)
+    popw = sim._hist["pop"][s_before - 1:s_after - 1].cpu().numpy()
+    warm_rate = float(popw.sum()) / (e_a.elapsed_time(e_b) / 1e3)
 
-    # ---- dominant kernel: event pairs around each move kernel launch (same protocol, L2 flushed)
-    _capi.check(L.gbdmc_prof_enable(1), "prof_enable")
-    kp = min(K, 4096)
+    # ---- the per-step kernels (gbdmc_sim_step: k_move + k_branch per step), L2 flushed per step
+    kp = min(max(K * DESC_WINDOW // 4, 100), 2000)
+    ps_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(kp)]
     s_before = int(sim._read_ctrl().step)
+    _capi.check(L.gbdmc_prof_enable(1), "prof_enable")
     for i in range(kp):
         flush.fill_(i & 0xFF)
+        ps_ev[i][0].record(stream)
         sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
+        ps_ev[i][1].record(stream)
     mv_ms, mv_n, sc_ms, sc_n = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
     _capi.check(L.gbdmc_prof_read(C.byref(mv_ms), C.byref(mv_n), C.byref(sc_ms), C.byref(sc_n)), "prof_read")
     _capi.check(L.gbdmc_prof_enable(0), "prof_enable")
     s_after = int(sim._read_ctrl().step)
     popp = sim._hist["pop"][s_before - 1:s_after - 1].cpu().numpy()
-    move_avg_s = mv_ms.value / 1e3 / max(mv_n.value, 1)
-    achieved = BYTES_MOVE_KERNEL * float(popp.mean()) / move_avg_s / 1e9
+    ps_ms = float(sum(a.elapsed_time(b) for a, b in ps_ev))
+    per_step = {"walker_steps_per_s": float(popp.sum()) / (ps_ms / 1e3), "steps": kp,
+                "us_per_step": ps_ms / kp * 1e3, "k_move_avg_us": mv_ms.value / max(mv_n.value, 1) * 1e3,
+                "l2": "flushed between steps"}
+    sim._compact()
+
+    # ---- roofline of the dominant kernel, k_run (the gbdmc_sim_run launch)
+    run_avg_s = float(np.mean(run_ms)) / 1e3
+    ws_per_launch = walker_steps / K if dist is None else float(pops.sum()) / K
+    achieved = BYTES_MOVE_KERNEL * ws_per_launch / run_avg_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "k_move_h2o_20k_traffic.json")
+    tr_path = os.path.join(ROOT, "profiles", "k_run_h2o_20k_traffic.json")
     if os.path.exists(tr_path):
         traffic = json.load(open(tr_path)).get("dram_bytes_per_launch")
 
@@ -350,40 +366,43 @@ def run_ours(args):
     e_b.record(stream)
     torch.cuda.synchronize()
     fp64_tflops = flops.value / (e_a.elapsed_time(e_b) / 1e3) / 1e12
-    # the bound that binds: FP64 FLOPs of k_move per walker (ncu DADD/DMUL/DFMA counts) over its event time
+    # the bound that binds: the FP64 FLOPs of a walker-step (ncu DADD/DMUL/DFMA counts) over the launch time
     fp64_roof = None
-    fp_path = os.path.join(ROOT, "profiles", "k_move_h2o_20k_fp64.json")
+    fp_path = os.path.join(ROOT, "profiles", "k_run_h2o_20k_fp64.json")
     if os.path.exists(fp_path):
-        fpw = json.load(open(fp_path))["fp64_flops_per_walker"]
-        ach = fpw * float(popp.mean()) / move_avg_s / 1e12
+        fpw = json.load(open(fp_path))["fp64_flops_per_walker_step"]
+        ach = fpw * ws_per_launch / run_avg_s / 1e12
         fp64_roof = {"bound": "fp64", "achieved": ach, "peak": fp64_tflops, "unit": "TFLOP/s",
                      "frac": ach / fp64_tflops, "peak_kind": "measured (gbdmc_fp64_fma_probe, this run)",
-                     "flops_per_walker": fpw}
+                     "flops_per_walker_step": fpw}
 
     # ---- e2e through the C ABI with host buffers
-    e2e_steps = max(50, min(K, 500))
-    e2e = run_e2e(sim, L, dev, e2e_steps)
-    st = run_e2e_staged(sim, L, dev, e2e_steps)
-    e2e["staged_copies"] = {"value": st["value"], "h2d_bytes_per_step": st["h2d_bytes_per_step"],
-                            "d2h_bytes_per_step": st["d2h_bytes_per_step"], "path": st["path"]}
+    e2e = run_e2e_windows(sim, L, dev, max(5, min(K, 100)), run_scratch)
+    e2e["per_step_host_resident"] = run_e2e(sim, L, dev, max(50, min(K * 10, 500)))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded start geometries, Philox4x32-10 deviates)",
             "config": {"workload": WORKLOAD, "walkers_per_gpu": N_WALKERS, "dt": DT, "atoms": "O,H,H",
                        "weighting": "discrete", "desc_window": DESC_WINDOW, "noise": "philox32",
-                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                       "graph_replay_l2_warm_walker_steps_per_s": graph_rate, "wall_s_timed": wall},
+                       "step": f"one {DESC_WINDOW}-step descendant-weighting window: gbdmc_desc_begin, "
+                               f"{DESC_WINDOW} DMC steps in one gbdmc_sim_run launch, gbdmc_desc_weights",
+                       "dmc_steps_timed": step1 - step0,
+                       "l2": "flushed between windows (256 MiB write); inside a window the walkers stay in "
+                             "shared memory", "parallelism": f"replicas x{world}",
+                       "windows_back_to_back_walker_steps_per_s": warm_rate,
+                       "per_step_kernels": per_step, "wall_s_timed": wall},
             "gpu_launches": gpu_launches,
-            "roofline": {"bound": "hbm", "kernel": "k_move (move+PES+weights+counts)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "bytes_per_walker": BYTES_MOVE_KERNEL,
-                         "kernel_avg_us": move_avg_s * 1e6, "scatter_avg_us": sc_ms.value / max(sc_n.value, 1) * 1e3,
-                         "fp64_fma_probe_tflops": fp64_tflops, "fp64": fp64_roof},
+            "roofline": {"bound": "hbm", "kernel": "k_run (gbdmc_sim_run: 50 steps of move+PES+weights+"
+                                                   "branching, walkers in shared memory)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": traffic, "bytes_per_walker_step": BYTES_MOVE_KERNEL,
+                         "kernel_avg_us": run_avg_s * 1e6, "fp64_fma_probe_tflops": fp64_tflops,
+                         "fp64": fp64_roof},
             "e2e": e2e}
     if not args.no_extras and world == 1:
         try:
-            line["extras"] = run_extras(max(64, min(K, 400)))
+            line["extras"] = run_extras(max(64, min(K * DESC_WINDOW, 400)))
         except Exception as exc:  # the headline line must still print
             line["extras"] = {"error": repr(exc)[:300]}
     if rank == 0 and world == 1:
@@ -396,6 +415,71 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_e2e_windows(sim, L, dev, windows, run_scratch):
+    """The headline e2e: the reference-facing C-ABI call with host buffers.
+    The walkers live in page-locked host memory between calls; per window
+    (one bench step) the N walkers' coordinates and ancestor ids are copied
+    host -> device, gbdmc_sim_run advances them DESC_WINDOW steps, and the
+    control block, then the N' walkers' coordinates, potentials and ancestor
+    ids and the window's vref / population history come back device -> host.
+    Host waits: one after the control block (for N'), one after the walkers."""
+    import torch
+    from pyvibdmc_gb300 import _capi
+    A3 = 3 * sim.natoms
+    cap = int(sim.capacity)
+    sim._compact()
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    cb = C.sizeof(_capi.Ctrl)
+    n = int(sim._read_ctrl().n)
+    b = sim._bufs[sim._cur]
+    hx = torch.empty((A3, cap), dtype=torch.float64).pin_memory()
+    hv = torch.empty(cap, dtype=torch.float64).pin_memory()
+    hw = torch.empty(cap, dtype=torch.int32).pin_memory()
+    hc = torch.empty(cb, dtype=torch.uint8).pin_memory()
+    hh = torch.empty((2, DESC_WINDOW), dtype=torch.float64).pin_memory()
+    hx[:, :n].copy_(b["x"][:, :n])
+    hw[:n].copy_(b["who"][:n])
+    ctrl_ptr = C.c_void_p(sim._ctrl.data_ptr())
+    step = int(sim._read_ctrl().step)
+    torch.cuda.synchronize()
+    h2d = d2h = 0
+    total = 0.0
+    t0 = time.perf_counter()
+    for _ in range(windows):
+        src, dst = sim._bufs[sim._cur], sim._bufs[1 - sim._cur]
+        src["x"][:, :n].copy_(hx[:, :n], non_blocking=True)
+        src["who"][:n].copy_(hw[:n], non_blocking=True)
+        h2d += (A3 * 8 + 4) * n
+        _capi.check(L.gbdmc_sim_run(C.byref(sim._sim), C.byref(sim._walker_struct(src, False)),
+                                    C.byref(sim._walker_struct(dst, False)), ctrl_ptr,
+                                    C.c_void_p(run_scratch.data_ptr()), step + DESC_WINDOW, DESC_WINDOW, sp),
+                    "sim_run")
+        sim._cur = 1 - sim._cur
+        hc.copy_(sim._ctrl, non_blocking=True)
+        stream.synchronize()
+        c = _capi.Ctrl.from_buffer_copy(hc.numpy().tobytes())
+        if c.status:
+            raise RuntimeError(f"device status {c.status} in the e2e leg")
+        k = int(c.step) - step
+        hx[:, :int(c.n)].copy_(dst["x"][:, :int(c.n)], non_blocking=True)
+        hv[:int(c.n)].copy_(dst["v"][:int(c.n)], non_blocking=True)
+        hw[:int(c.n)].copy_(dst["who"][:int(c.n)], non_blocking=True)
+        hh[0, :k].copy_(sim._hist["vref"][step:step + k], non_blocking=True)
+        hh[1, :k].copy_(sim._hist["pop"][step:step + k], non_blocking=True)
+        stream.synchronize()
+        total += n + float(hh[1, :k - 1].sum())  # the population entering each of the k steps
+        n, step = int(c.n), int(c.step)
+        d2h += cb + (A3 * 8 + 8 + 4) * n + 16 * k
+    secs = time.perf_counter() - t0
+    return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // windows,
+            "d2h_bytes_per_step": d2h // windows, "steps": windows,
+            "path": f"walkers in page-locked host memory between calls; per bench step (one {DESC_WINDOW}-step "
+                    "window) H2D of the N walkers' coordinates and ancestor ids, one gbdmc_sim_run call (C ABI), "
+                    "D2H of the control block, the N' walkers' coordinates, potentials and ancestor ids and the "
+                    "window's vref and population history; two host waits per window"}
 
 
 def _timed_graph_rate(run_steps, pop_of, steps):
@@ -665,52 +749,11 @@ def run_e2e(sim, L, dev, steps):
             "per_step_sync": sync}
 
 
-def run_e2e_staged(sim, L, dev, steps):
-    """Walkers in pinned host memory; per step: H2D walkers, gbdmc_sim_step,
-    gbdmc_walkers_compact, D2H branched walkers, potentials and the control
-    block (the reference-facing call with host buffers)."""
-    import torch
-    from pyvibdmc_gb300 import _capi
-    A3 = 3 * sim.natoms
-    cap = sim.capacity
-    sim._compact()
-    n = int(sim._read_ctrl().n)
-    host_x = torch.empty((A3, cap), dtype=torch.float64).pin_memory()
-    host_v = torch.empty(cap, dtype=torch.float64).pin_memory()
-    host_ctrl = torch.empty(C.sizeof(_capi.Ctrl), dtype=torch.uint8).pin_memory()
-    host_x[:, :n].copy_(sim._bufs[sim._cur]["x"][:, :n])
-    h2d = d2h = 0
-    total = 0.0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        b = sim._bufs[sim._cur]
-        b["x"].copy_(host_x, non_blocking=True)
-        h2d += A3 * cap * 8
-        total += n
-        sim._cur, sim._lazy = sim._launch_step(sim._cur, sim._lazy)
-        sim._compact()
-        nb = sim._bufs[sim._cur]
-        host_ctrl.copy_(sim._ctrl, non_blocking=True)
-        host_x.copy_(nb["x"], non_blocking=True)
-        host_v.copy_(nb["v"], non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        c = _capi.Ctrl.from_buffer_copy(host_ctrl.numpy().tobytes())
-        n = int(c.n)
-        d2h += (A3 + 1) * cap * 8 + C.sizeof(_capi.Ctrl)
-    torch.cuda.synchronize()
-    secs = time.perf_counter() - t0
-    return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // steps,
-            "d2h_bytes_per_step": d2h // steps, "steps": steps,
-            "path": "pinned host walker buffer -> H2D -> gbdmc_sim_step + gbdmc_walkers_compact (C ABI) -> "
-                    "D2H walkers, V, control block; host sync per step"}
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", dest="no_extras", action="store_true",
                     help="skip the IS / batched / surrogate workloads reported under 'extras'")

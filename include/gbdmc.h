@@ -226,6 +226,27 @@ int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbd
                    gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, const gbdmc_noise_t* noise,
                    void* stream);
 
+/* Up to max_steps steps of plain DMC in one launch, stopping before step
+ * step_end: the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two
+ * events, for discrete weighting, Philox deviates and a built-in potential.
+ * The walkers stay in shared memory across the steps (each block holds a
+ * contiguous run of the population, one grid barrier per step, bounded wait:
+ * GBDMC_ST_TIMEOUT on expiry); the deviates and branching uniforms are those of
+ * gbdmc_sim_step, so the trajectory is gbdmc_sim_step's (vref sums in another
+ * order, last bits).  src holds the ctrl->n compact walkers (idx NULL); dst
+ * receives the compact walkers after the last step run (x, v, who), or the
+ * moved unbranched walkers of a step whose guards tripped, or -- when no step
+ * runs (status set, step >= step_end) -- a copy of src, so a queue of calls
+ * alternating two buffers always leaves the walkers in the last call's dst.
+ * A launch may stop before max_steps when a block's share of the population
+ * outgrows its buffer; ctrl->step tells how far it got.  Scratch:
+ * gbdmc_sim_run_scratch_bytes(), zeroed before the first call (the kernel
+ * leaves it zeroed).  Returns GBDMC_ERR_CAPACITY, before any launch, when the
+ * per-block buffers of sim->n0 walkers do not fit shared memory. */
+size_t gbdmc_sim_run_scratch_bytes(void);
+int gbdmc_sim_run(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
+                  gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, int64_t step_end, int32_t max_steps, void* stream);
+
 /* The two halves of a step around a potential the caller evaluates
  * (sim->pes.kind == GBDMC_PES_EXTERNAL, plain DMC): gbdmc_sim_move is
  * move_randomly (pyvibdmc.py:540-547) -- the logical walkers of src (through

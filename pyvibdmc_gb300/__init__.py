@@ -11,7 +11,7 @@ from .potentials import (Potential_GPU, PESFunction, harmonic_oscillator, h2o_lo
                          partridge_schwenke,
                          WATER_DIMER_EQ, to_soa, from_soa)
 from .imp_samp import ImpSampManager_GPU, TrialFunction, h2o_gaussian_trial, ho_gaussian_trial, \
-    dimer_gaussian_trial
+    dimer_gaussian_trial, local_energy, fit_trial
 from .potential_manager import Potential, Potential_NoMP, NN_Potential, Potential_Direct
 from .engine import DMC_Sim, HostWalkers, dmc_restart
 from .initial import HarmonicAnalysis, InitialConditioner
@@ -21,7 +21,7 @@ from . import _capi
 
 __all__ = ["HostWalkers", "HarmonicAnalysis", "InitialConditioner", "Constants", "get_atomic_num", "get_atomic_string", "Potential_GPU", "PESFunction",
            "harmonic_oscillator", "h2o_local_mode", "water_dimer", "partridge_schwenke", "ImpSampManager_GPU", "TrialFunction",
-           "h2o_gaussian_trial", "ho_gaussian_trial", "dimer_gaussian_trial", "DMC_Sim", "dmc_restart", "DMC_Batch", "blocking_error",
+           "h2o_gaussian_trial", "ho_gaussian_trial", "dimer_gaussian_trial", "local_energy", "fit_trial", "DMC_Sim", "dmc_restart", "DMC_Batch", "blocking_error",
            "MLPSurrogate", "NN_Potential_GPU", "NNDMC", "harvest_training_data", "WATER_DIMER_EQ",
            "to_soa", "from_soa", "Potential", "Potential_NoMP", "NN_Potential", "Potential_Direct"]
 

@@ -110,6 +110,9 @@ def load():
         "gbdmc_sim_init": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, P], C.c_int),
         "gbdmc_sim_step": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P,
                             C.POINTER(Noise), P], C.c_int),
+        "gbdmc_sim_run_scratch_bytes": ([], C.c_size_t),
+        "gbdmc_sim_run": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.c_int64, C.c_int32, P],
+                          C.c_int),
         "gbdmc_sim_move": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.POINTER(Noise), P],
                            C.c_int),
         "gbdmc_sim_branch": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, C.POINTER(Noise), P], C.c_int),

@@ -14,8 +14,11 @@ that supplies the deviates on the host in the reference's call order),
 ``capacity`` (walker buffer size, default ``floor(1.5 N0) + 1`` rounded up to
 256), ``graph_steps`` (steps per captured CUDA graph), ``device``,
 ``write_files``, ``training_sink`` (callable receiving device walkers at the
-``DEBUG_save_training_every`` steps), ``replica_id`` (Philox stream) and
-``block_threads`` (tile width; 0 = chosen from the population).
+``DEBUG_save_training_every`` steps), ``replica_id`` (Philox stream),
+``block_threads`` (tile width; 0 = chosen from the population) and
+``fused_steps`` (plain discrete Philox runs: up to this many steps per launch
+of the multi-step kernel, walkers resident in shared memory; 0 = one launch
+pair per step, which ``block_threads`` also selects).
 """
 import ctypes as C
 import pickle
@@ -43,7 +46,7 @@ class DMC_Sim:
                  adiabatic_dmc=None, fixed_node=None, DEBUG_alpha=None, DEBUG_save_desc_wt_tracker=None,
                  DEBUG_save_training_every=None, DEBUG_save_before_bod=False, DEBUG_mass_change=None,
                  *, seed=0, rng="philox32", capacity=None, graph_steps=32, device=None, write_files=True,
-                 training_sink=None, replica_id=0, block_threads=0):
+                 training_sink=None, replica_id=0, block_threads=0, fused_steps=64):
         unsupported = {"imp_samp_oned": imp_samp_oned, "second_impsamp_displacement": second_impsamp_displacement,
                        "excited_state_imp_samp": excited_state_imp_samp, "adiabatic_dmc": adiabatic_dmc,
                        "fixed_node": fixed_node, "DEBUG_mass_change": DEBUG_mass_change,
@@ -57,9 +60,15 @@ class DMC_Sim:
         # a built-in GPU surface is fused into the step kernel; any other object with
         # the reference's getpot(cds) contract (potential_manager.py:71-253) is called on
         # the moved walkers between the move and branching kernels
-        self._external = not isinstance(potential, Potential_GPU)
+        from .surrogate import NN_Potential_GPU
+        self._nn_route = isinstance(potential, NN_Potential_GPU) and potential.fallback is not None
+        self._external = not isinstance(potential, Potential_GPU) and not self._nn_route
         if self._external and not callable(getattr(potential, "getpot", None)):
             raise TypeError("potential must have a getpot(cds, timeit=False) method returning (N,) hartree")
+        if self._nn_route and (weighting.lower() != "discrete" or not isinstance(rng, str) or int(cur_timestep) or
+                               (imp_samp is not None and getattr(imp_samp, "kind", None) != "dimer_gauss")):
+            raise NotImplementedError("the fused surrogate step runs fresh discrete-weighting runs with Philox "
+                                      "deviates (and the dimer trial for importance sampling)")
         if self._external and imp_samp is not None:
             raise NotImplementedError("importance sampling runs with the built-in GPU potentials "
                                       "(pyvibdmc_gb300.potentials) and trial functions")
@@ -92,6 +101,7 @@ class DMC_Sim:
         self.training_sink = training_sink
         self.replica_id = int(replica_id)
         self.block_threads = int(block_threads)
+        self.fused_steps = int(fused_steps)
         self.device = torch.device(device) if device is not None else default_device()
         self.masses = masses
         self._initialize(capacity)
@@ -134,7 +144,7 @@ class DMC_Sim:
             self._atm_nums = [-1]
         else:
             self.masses = np.array(self.masses, dtype=np.float64)
-            self._atm_nums = get_atomic_num(self.atoms)
+            self._atm_nums = get_atomic_num(self.atoms[0].split("-") if "-" in self.atoms[0] else self.atoms)
         if len(self.masses) != len(self.atoms):
             raise Exception("Your number of atoms list does not match your number of masses you provided.")
         if coords.shape[1] != len(self.atoms):
@@ -150,8 +160,9 @@ class DMC_Sim:
             if self.dims != 3:
                 raise NotImplementedError("the built-in GPU potentials take 3D Cartesian walkers; pass a "
                                           "getpot potential for 1D or 2D walkers")
-            if self.natoms != self.potential.natoms:
-                raise ValueError(f"potential has {self.potential.natoms} atoms, walkers have {self.natoms}")
+            pot_atoms = self.potential.fallback.natoms if self._nn_route else self.potential.natoms
+            if self.natoms != pot_atoms:
+                raise ValueError(f"potential has {pot_atoms} atoms, walkers have {self.natoms}")
         # walker rows on the device: 3 per storage atom (the caller's nc = natoms*dims coordinates, padded)
         self._ncoord = self.natoms * self.dims
         self._store_atoms = (self._ncoord + 2) // 3
@@ -176,7 +187,7 @@ class DMC_Sim:
                 raise ValueError("Invalid input for continuous weight threshold")
         elif self.weighting != "discrete":
             raise ValueError(f"weighting must be 'discrete' or 'continuous', got {self.weighting!r}")
-        if self.impsamp_manager is not None:
+        if self.impsamp_manager is not None and not self._nn_route:
             if getattr(self.impsamp_manager, "natoms", None) != self.natoms or \
                     not hasattr(self.impsamp_manager, "trial_struct"):
                 raise TypeError("imp_samp must be a pyvibdmc_gb300.ImpSampManager_GPU for these atoms")
@@ -193,6 +204,9 @@ class DMC_Sim:
         if cap < max(min_cap, n):
             raise ValueError(f"capacity must be >= {max(min_cap, n)}")
         self.capacity = (cap + 255) // 256 * 256
+        if self._nn_route:
+            self._nn_setup(coords)
+            return
         self._alloc(coords)
         self._vref_vs_tau = np.zeros(self.num_timesteps)
         self._pop_vs_tau = np.zeros(self.num_timesteps)
@@ -200,8 +214,80 @@ class DMC_Sim:
         self._desc_open = None
         self._graphs = {}
         self._host_vstats = {}
+        # the multi-step kernel: plain DMC, discrete weighting, Philox deviates, built-in surface
+        self._multi = (self.fused_steps > 0 and not self._external and self.weighting == "discrete" and
+                       self.impsamp_manager is None and self._noise_mode != _capi.NOISE_INJECTED and
+                       self.block_threads == 0)
+        self._multi_used = False
+        self._multi_launches = 0
         if self.write_files:
             archive.create_filesystem(self.output_folder)
+
+    def _nn_setup(self, coords):
+        """The fused surrogate step (NNDMC) in place of the FP64 buffers."""
+        from .surrogate import NNDMC
+        pot = self.potential
+        self._nnd = NNDMC(pot.model, pot.fallback, self.num_walkers, coords, self.masses, self.delta_t,
+                          max(self.num_timesteps, 1), seed=self.seed, audit_every=pot.audit_every, rng=self.rng,
+                          graph_steps=min(self.graph_steps, 16), replica_id=self.replica_id,
+                          bias_control=pot.bias_control, imp_samp=self.impsamp_manager)
+        self._vref_vs_tau = np.zeros(self.num_timesteps)
+        self._pop_vs_tau = np.zeros(self.num_timesteps)
+        self._eff_ts = np.zeros(self.num_timesteps)
+        self._desc_open = None
+        self._multi = self._multi_used = self._external = False
+        self._host_vstats = {}
+        if self.write_files:
+            archive.create_filesystem(self.output_folder)
+
+    def _propagate_nn(self):
+        """propagate (pyvibdmc.py:701-876) on the fused surrogate step: the steps
+        between events run as NNDMC batches (CUDA graphs); checkpoints,
+        descendant-weighting windows and histories as in the FP64 path."""
+        L = _capi.load()
+        nd = self._nnd
+        T = self.num_timesteps
+        nd.init()
+        t = 0
+        bounds = [b for b in self._boundaries() if b > 0] + [T]
+        ctrl_ptr = C.c_void_p(nd._ctrl.data_ptr())
+        while t < T:
+            self.cur_timestep = self._next_step = t
+            if t in self._chkpt_step and self.write_files:
+                archive.delete_older_checkpoints(self.output_folder, self.sim_name, t)
+                self._chkpt(t)
+            if t in self._wfn_save_step:
+                self._parent = nd.walkers(0).astype(np.float64)
+                self._parent_wts = None
+                _capi.check(L.gbdmc_desc_begin(C.c_void_p(nd._bufs[nd._cur]["who"].data_ptr()), ctrl_ptr,
+                                               self._stream()), "gbdmc_desc_begin")
+                self._desc_open = t
+            t_end = min(min(b for b in bounds if b > t), T)
+            try:
+                nd.run(t_end - t)
+            finally:
+                k = min(nd.step, T)
+                self._vref_vs_tau[t:k] = nd._hist["vref"][0, t:k].cpu().numpy()
+                self._pop_vs_tau[t:k] = nd._hist["pop"][0, t:k].cpu().numpy()
+            last = t_end - 1
+            if t_end in self._desc_wt_save_step and self._desc_open is not None:
+                nd.walkers(0)  # compact
+                npar = len(self._parent)
+                desc = torch.zeros(max(npar, 1), dtype=torch.float64, device=self.device)
+                _capi.check(L.gbdmc_desc_weights(C.c_void_p(nd._bufs[nd._cur]["who"].data_ptr()), None, ctrl_ptr,
+                                                 npar, C.c_void_p(desc.data_ptr()), self._stream()),
+                            "gbdmc_desc_weights")
+                self._desc_wts = desc[:npar].cpu().numpy()
+                rec = dict(start=last + 1 - self.desc_wt_time_steps, coords=self._parent, desc_wts=self._desc_wts,
+                           parent_wts=None)
+                self.wfns = getattr(self, "wfns", []) + [rec]
+                if self.write_files:
+                    archive.save_h5(f"{self.output_folder}/wfns/{self.sim_name}_wfn_{rec['start']}ts.hdf5",
+                                    ["coords", "desc_wts"], [self._parent, self._desc_wts])
+                self._desc_open = None
+            t = t_end
+        self.cur_timestep = T - 1
+        self._next_step = T
 
     def _alloc(self, coords):
         dev, ld, A = self.device, self.capacity, self._store_atoms
@@ -292,6 +378,8 @@ class DMC_Sim:
         return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def _read_ctrl(self):
+        if self._nn_route:
+            return self._nnd.ctrl(0)
         return _capi.Ctrl.from_buffer_copy(self._ctrl.cpu().numpy().tobytes())
 
     def _write_ctrl(self, ctrl):
@@ -412,14 +500,45 @@ class DMC_Sim:
         self._host_vstats[step] = (float(vn.min()), float(vn.max()), float(vn.mean()))
         _capi.check(L.gbdmc_sim_branch(C.byref(self._sim), C.byref(dst), C.c_void_p(self._ctrl.data_ptr()),
                                        C.c_void_p(self._scratch.data_ptr()), nz, self._stream()), "gbdmc_sim_branch")
-        self._cur, self._lazy = 1 - self._cur, self.weighting == "discrete"
         c = self._read_ctrl()
+        # a step whose guards tripped leaves its moved walkers in dst, unbranched
+        self._cur, self._lazy = 1 - self._cur, self.weighting == "discrete" and not c.status
         self._n_now = int(c.n)
         self._step_device = int(c.step)
         return not c.status
 
+    def _run_multi(self, nsteps):
+        """nsteps steps through gbdmc_sim_run: launches of up to fused_steps steps,
+        alternating the two walker buffers.  Returns False when the multi-step
+        kernel does not take this system (the per-block buffers do not fit)."""
+        L = _capi.load()
+        if not hasattr(self, "_run_scratch"):
+            self._run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(), dtype=torch.uint8, device=self.device)
+        self._compact()
+        c = self._read_ctrl()
+        end = int(c.step) + nsteps
+        K = self.fused_steps
+        while True:
+            for _ in range((end - int(c.step) + K - 1) // K):
+                src = self._walker_struct(self._bufs[self._cur], False)
+                dst = self._walker_struct(self._bufs[1 - self._cur], False)
+                rc = L.gbdmc_sim_run(C.byref(self._sim), C.byref(src), C.byref(dst), C.c_void_p(self._ctrl.data_ptr()),
+                                     C.c_void_p(self._run_scratch.data_ptr()), end, K, self._stream())
+                if rc == _capi.ERR_CAPACITY and not self._multi_used:
+                    self._multi = False
+                    return False
+                _capi.check(rc, "gbdmc_sim_run")
+                self._multi_used = True
+                self._multi_launches += 1
+                self._cur, self._lazy = 1 - self._cur, False
+            c = self._read_ctrl()
+            if c.status or int(c.step) >= end:
+                return True
+
     def _run_steps(self, nsteps):
         """Queue nsteps steps (no host sync in the Philox modes)."""
+        if self._multi and nsteps > 0 and self._run_multi(nsteps):
+            return
         if self._external:
             c = self._read_ctrl()
             self._n_now, self._step_device = int(c.n), int(c.step)
@@ -459,6 +578,8 @@ class DMC_Sim:
         return int(self._read_ctrl().n)
 
     def _coords_host(self, n=None):
+        if self._nn_route:
+            return self._nnd.walkers(0).astype(np.float64)
         self._compact()
         n = self._n_device() if n is None else n
         x = self._bufs[self._cur]["x"]
@@ -544,6 +665,8 @@ class DMC_Sim:
         t = self.cur_timestep
         if self.write_files:
             self._logger.beginning(self)
+        if self._nn_route:
+            return self._propagate_nn()
         self._init_device()
         bounds = [b for b in self._boundaries() if b > t] + [T]
         while t < T:
@@ -567,7 +690,9 @@ class DMC_Sim:
             if c.status:
                 done = int(c.err_step) - t
                 # the failing step moved its walkers into its dst buffer and did not branch
-                self._cur, self._lazy = cur0 ^ (done & 1) ^ 1, False
+                # (the multi-step launches pass them on to the last launch's output)
+                if not self._multi_used and not self._external:
+                    self._cur, self._lazy = cur0 ^ (done & 1) ^ 1, False
                 h = self._sync_history(t, int(c.err_step))
                 self.cur_timestep = self._next_step = int(c.err_step)
                 self._n_now = int(c.n)
@@ -629,7 +754,8 @@ class DMC_Sim:
             "potential", "impsamp_manager", "potential_info", "training_sink", "device", "rng")}
         st.update(_coords=self._coords_host(n), _vref_vs_tau=self._vref_vs_tau.copy(),
                   _pop_vs_tau=self._pop_vs_tau.copy(), _eff_ts=self._eff_ts.copy(),
-                  _cont_wts=None if "w" not in self._bufs[0] else self._bufs[self._cur]["w"][:n].cpu().numpy(),
+                  _cont_wts=None if self._nn_route or "w" not in self._bufs[0] else
+                  self._bufs[self._cur]["w"][:n].cpu().numpy(),
                   _masses=np.asarray(self.masses), _atm_nums=self._atm_nums,
                   _rng=self.rng if isinstance(self.rng, str) else "philox32",
                   _vref=float(self._read_ctrl().vref),

@@ -153,7 +153,7 @@ def local_energy(manager, potential, x, n, masses):
     return v - 0.5 * (inv_m[:, None] * d2[:, :n]).sum(0)
 
 
-def fit_trial(manager, potential, x, n, masses, maxiter=600, verbose=False):
+def fit_trial(manager, potential, x, n, masses, maxiter=600, fit_oo=False, verbose=False):
     """Variance minimisation of the local energy over a sample of walkers.
 
     The trial's parameters are set to minimise Var(E_L) over the n walkers of
@@ -163,7 +163,10 @@ def fit_trial(manager, potential, x, n, masses, maxiter=600, verbose=False):
     the importance-sampled walk and a smaller variance of its energy.  The
     symmetric parameters are fitted together: for 'h2o_gauss' the stretch
     exponent and centre (shared by r1 and r2), the bend exponent and centre;
-    'dimer_gauss' adds the O-O exponent and centre.  Exponents are fitted on a
+    for 'dimer_gauss' the monomers' four and, with ``fit_oo``, the O-O
+    exponent and centre (the O-O factor barely moves the time-step error of
+    the walk, and over a ground-state sample its fit can drift to an
+    unphysical centre, so by default it is kept).  Exponents are fitted on a
     log scale (Nelder-Mead).  Returns a new ImpSampManager_GPU and the
     standard deviations of E_L (hartree) before and after."""
     from scipy.optimize import minimize
@@ -171,7 +174,7 @@ def fit_trial(manager, potential, x, n, masses, maxiter=600, verbose=False):
         raise ValueError("fit_trial fits the h2o_gauss and dimer_gauss trials")
     dimer = manager.kind == "dimer_gauss"
     a0, q0 = list(manager.alpha), list(manager.qe)
-    p0 = [np.log(a0[0]), np.log(a0[2]), q0[0], q0[2]] + ([np.log(a0[3]), q0[3]] if dimer else [])
+    p0 = [np.log(a0[0]), np.log(a0[2]), q0[0], q0[2]] + ([np.log(a0[3]), q0[3]] if dimer and fit_oo else [])
     v = potential.eval_soa(x, n)
     inv_m = torch.as_tensor(np.repeat(1.0 / np.asarray(masses, dtype=np.float64), 3), device=x.device)
 
@@ -179,8 +182,8 @@ def fit_trial(manager, potential, x, n, masses, maxiter=600, verbose=False):
         al = [np.exp(p[0]), np.exp(p[0]), np.exp(p[1])]
         qe = [p[2], p[2], p[3]]
         if dimer:
-            al.append(np.exp(p[4]))
-            qe.append(p[5])
+            al.append(np.exp(p[4]) if fit_oo else a0[3])
+            qe.append(p[5] if fit_oo else q0[3])
         return ImpSampManager_GPU(manager.kind, al, qe, natoms=manager.natoms, device=manager.device)
 
     def spread(p):

@@ -247,11 +247,21 @@ class MLPSurrogate:
 
 class NN_Potential_GPU:
     """``getpot(cds, timeit=False)`` of a trained surrogate (the NN_Potential
-    contract of potential_manager.py:177-214, model held by the object)."""
+    contract of potential_manager.py:177-214, model held by the object).
 
-    def __init__(self, surrogate):
+    With ``fallback`` (the analytic water_dimer Potential_GPU) a
+    :class:`pyvibdmc_gb300.DMC_Sim` given this potential runs the fused
+    surrogate step (:class:`NNDMC`: tcgen05 network in the step kernel, the
+    fallback for walkers outside the training box and for a 1/``audit_every``
+    audit, online bias control ``bias_control``); without it DMC_Sim calls
+    ``getpot`` like any Python potential."""
+
+    def __init__(self, surrogate, fallback=None, audit_every=100, bias_control=0.02):
         self.model = surrogate
         self.natoms = 6
+        self.fallback = fallback
+        self.audit_every = int(audit_every)
+        self.bias_control = float(bias_control)
 
     def getpot(self, cds, timeit=False):
         t0 = time.time()

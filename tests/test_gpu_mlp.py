@@ -390,3 +390,30 @@ def test_surrogate_injected_step_matches_the_oracle(dimer_model, n0):
     np.testing.assert_array_equal(cnt[~amb], want[~amb])
     vref_want = (cnt * v).sum() / nn - (1.0 / (2.0 * dt)) * (nn - n0) / n0
     assert abs(c1.vref - vref_want) < 1e-9, (c1.vref, vref_want)
+
+
+def test_dmc_sim_with_a_surrogate_potential_runs_the_fused_step():
+    """DMC_Sim(potential=NN_Potential_GPU(model, fallback=water_dimer())) runs the
+    fused surrogate step: the same trajectory as NNDMC with the same seed, plus
+    the descendant-weighting windows and files of DMC_Sim; without a fallback the
+    surrogate is called through getpot like any Python potential."""
+    p, masses = oracle.dimer_config()
+    pot = pg.water_dimer()
+    x, v, g, _ = harvest_training_data(pot, 3000, 60, 10, pg.WATER_DIMER_EQ[None], masses, seed=3, equil=10)
+    m = MLPSurrogate(seed=0).fit(x, v, g, epochs=4, batch=2048, lr=3e-3)
+    sim = pg.DMC_Sim(num_walkers=3000, num_timesteps=80, equil_steps=20, wfn_every=1000, desc_wt_steps=30,
+                     atoms=["O", "H", "H"] * 2, masses=masses, delta_t=10.0,
+                     potential=pg.NN_Potential_GPU(m, fallback=pot), start_structures=pg.WATER_DIMER_EQ[None],
+                     seed=5, write_files=False)
+    sim.run()
+    nd = NNDMC(m, pot, 3000, pg.WATER_DIMER_EQ[None], masses, 10.0, 80, seed=5).init()
+    nd.run(80)
+    np.testing.assert_array_equal(sim._vref_vs_tau, nd.vref_history())
+    np.testing.assert_array_equal(sim._pop_vs_tau, nd.pop_history())
+    assert np.array_equal(sim.walkers, nd.walkers().astype(np.float64))
+    assert len(sim.wfns) == 1 and sim.wfns[0]["desc_wts"].sum() == sim._pop_vs_tau[49]
+    slow = pg.DMC_Sim(num_walkers=500, num_timesteps=5, equil_steps=100, atoms=["O", "H", "H"] * 2, masses=masses,
+                      delta_t=10.0, potential=pg.NN_Potential_GPU(m), start_structures=pg.WATER_DIMER_EQ[None],
+                      seed=5, write_files=False)
+    slow.run()
+    assert slow._external and np.all(np.isfinite(slow._vref_vs_tau))

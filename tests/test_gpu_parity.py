@@ -301,7 +301,7 @@ def test_philox_graph_batching_is_deterministic():
     for gs in (2, 32):
         sim = pg.DMC_Sim(num_walkers=4000, num_timesteps=100, equil_steps=1000, atoms=["O", "H", "H"], masses=m,
                          delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=123,
-                         graph_steps=gs, write_files=False)
+                         graph_steps=gs, write_files=False, fused_steps=0)
         sim.run()
         runs.append((sim._vref_vs_tau.copy(), sim.walkers))
     assert np.array_equal(runs[0][0], runs[1][0])
