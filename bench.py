@@ -247,7 +247,8 @@ def run_ours(args):
     sp = C.c_void_p(stream.cuda_stream)
     masses = [pg.Constants.mass("O"), pg.Constants.mass("H"), pg.Constants.mass("H")]
     K, W = args.steps, args.warmup
-    T = (W + K + 4) * DESC_WINDOW + 2000
+    # history length: warm-up, timed, back-to-back and e2e windows, the per-step leg and the host-resident leg
+    T = (W + 3 * K + 10) * DESC_WINDOW + 6000
     sim = pg.DMC_Sim(sim_name="bench", num_walkers=N_WALKERS, num_timesteps=T, equil_steps=10 ** 9,
                      atoms=["O", "H", "H"], masses=masses, delta_t=DT, potential=pg.h2o_local_mode(),
                      start_structures=start_structures(N_WALKERS, 1 + rank), seed=1234 + rank, write_files=False,
@@ -579,11 +580,11 @@ def run_extras(steps):
     dm = [pg.Constants.mass(a) for a in ("O", "H", "H", "O", "H", "H")]
     pot = pg.water_dimer()
     t_h = time.perf_counter()
-    x, v, g, _ = pg.harvest_training_data(pot, 200000, 210, 20, pg.WATER_DIMER_EQ[None], dm, seed=1, equil=20)
+    x, v, g, _ = pg.harvest_training_data(pot, 200000, 420, 20, pg.WATER_DIMER_EQ[None], dm, seed=1, equil=20)
     torch.cuda.synchronize()
     t_h = time.perf_counter() - t_h
     t_t = time.perf_counter()
-    m = pg.MLPSurrogate(seed=0).fit(x, v, g, epochs=30, batch=8192, lr=2e-3)
+    m = pg.MLPSurrogate(seed=0).fit(x, v, g, epochs=40, batch=8192, lr=2e-3)
     torch.cuda.synchronize()
     t_t = time.perf_counter() - t_t
     nd = pg.NNDMC(m, pot, 200000, pg.WATER_DIMER_EQ[None], dm, DT, steps + 64, seed=5, audit_every=100).init()
@@ -607,78 +608,135 @@ def run_extras(steps):
                                    "harvest_s": t_h, "train_s": t_t, "train_samples": int(x.shape[1]),
                                    "train_rmse_cm": m.history[-1]["rmse_e_cm"], "audit": nd.audit()}
     del nd, fp
-    out["is_nn_batched_dimer"] = run_combined_dimer(m, pot, dm)
+    # the dimer trial fitted to the harvested plain-run walkers (local-energy variance)
+    sel = torch.randperm(x.shape[1], device=x.device)[:300000]
+    xs = x[:, sel].contiguous()
+    trial, s0, s1 = pg.fit_trial(pg.dimer_gaussian_trial(), pot, xs, xs.shape[1], dm)
+    out["is_nn_batched_dimer"] = run_combined_dimer(m, pot, dm, trial)
+    out["is_nn_batched_dimer"]["trial"]["sd_local_energy_cm"] = [s0 / pg.Constants.atomic_units["wavenumbers"],
+                                                                 s1 / pg.Constants.atomic_units["wavenumbers"]]
     return out
 
 
-def run_combined_dimer(m, pot, dm, T=6000):
-    """The engine with all three accelerations on one system, the water dimer:
-    importance sampling (dimer trial), the tcgen05 surrogate PES and 64
-    batched replicas (N_r ~ U[1000, 65536]), against the plain FP64 dimer
-    path (200000 walkers, one replica, three seeds) at equal ZPE error bar
-    (efficiency = 1 / (error^2 x seconds)), and its ZPE against the FP64
-    importance-sampled dimer (same trial, dt).  The batch's error bar is the
-    scatter of its 64 independent replica ZPEs (N0-weighted); the single runs'
-    are blocking errors.  The replicas' own blocking errors, combined with
-    the same weights, give a second (less noisy, correlation-dependent)
-    estimate of the batch's error bar, reported beside it."""
+DIMER_TAU = 60000.0  # imaginary time of every run of the spec comparison (a.u.)
+DIMER_DTS = (10.0, 5.0)
+
+
+def zpe_estimate(vref_series_cm):
+    """The one error estimator of the spec comparison: the mean of the
+    production part (the last 3/4) of a vref series and its blocking error
+    (30 block means).  For a batch of replicas the series is the N0-weighted
+    mean of the replicas' vref at each step."""
+    import pyvibdmc_gb300 as pg
+    v = np.asarray(vref_series_cm, dtype=np.float64)
+    return pg.blocking_error(v[len(v) // 4:], 30)
+
+
+def extrapolate(res):
+    """Time-step extrapolation of a method measured at dt and dt/2 (linear in
+    dt, the leading error of the walk): E0 = 2 E(dt/2) - E(dt),
+    sigma0^2 = 4 sigma(dt/2)^2 + sigma(dt)^2, cost = the seconds of both runs;
+    efficiency at equal error = 1 / (sigma0^2 cost)."""
+    a, b = res[f"dt{DIMER_DTS[0]:g}"], res[f"dt{DIMER_DTS[1]:g}"]
+    e0 = 2 * b["zpe_cm"] - a["zpe_cm"]
+    s0 = float(np.sqrt(4 * b["err_cm"] ** 2 + a["err_cm"] ** 2))
+    cost = a["seconds"] + b["seconds"]
+    return {"zpe_cm": e0, "err_cm": s0, "seconds": cost, "efficiency": 1.0 / (s0 * s0 * cost) if cost > 0 else None}
+
+
+def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
+    """The spec comparison on the water dimer: the engine with its three
+    accelerations (importance sampling with the fitted dimer trial, the tcgen05
+    surrogate PES, 64 batched replicas with N_r ~ U[1000, 65536]) against the
+    plain FP64 GPU path (200000 walkers, one replica, several seeds), at equal
+    ZPE error including the time-step error: every method runs at dt = 10 and
+    5 for the same imaginary time, its ZPE is extrapolated to dt -> 0 and its
+    efficiency is 1 / (sigma0^2 x seconds) (zpe_estimate, extrapolate).  The
+    FP64 importance-sampled path with the same trial (100000 walkers) pins
+    the surrogate's accuracy at each dt; profiles/dimer_fp64_oracle.json holds
+    a long plain FP64 extrapolation of the same surface, the ZPE the three
+    accelerations must reproduce within 1 cm^-1."""
     import torch
     import pyvibdmc_gb300 as pg
-    trial = pg.dimer_gaussian_trial()
-    res = {}
+    conv = lambda v: pg.Constants.convert(v, "wavenumbers", to_AU=False)  # noqa: E731
+    res = {"estimator": "mean of the last 3/4 of the vref series (N0-weighted over replicas), blocking error of "
+                        "30 block means; dt -> 0 from dt = 10 and 5 (E0 = 2 E5 - E10)",
+           "trial": {"alpha": trial.alpha, "qe": trial.qe}}
 
-    def fp64(tag, imp, seeds):
-        zs, es, secs, ws = [], [], 0.0, 0.0
-        for seed in seeds:
-            sm = pg.DMC_Sim(num_walkers=200000, num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
-                            masses=dm, delta_t=DT, potential=pot, imp_samp=imp,
-                            start_structures=pg.WATER_DIMER_EQ[None], seed=seed, write_files=False, graph_steps=32)
-            sm._init_device()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            sm._run_steps(T)
-            torch.cuda.synchronize()
-            secs += time.perf_counter() - t0
-            vr = pg.Constants.convert(sm._hist["vref"].cpu().numpy()[T // 4:T], "wavenumbers", to_AU=False)
-            z, e = pg.blocking_error(vr, 30)
-            zs.append(z)
-            es.append(e)
-            ws += float(200000 + sm._hist["pop"].cpu().numpy()[:T - 1].sum())
-            del sm
-        z = float(np.mean(zs))
-        e = float(np.sqrt(np.sum(np.square(es))) / len(es))
-        res[tag] = {"walkers": 200000, "steps": T, "seeds": list(seeds), "seconds": secs,
-                    "walker_steps_per_s": ws / secs, "zpe_cm": z, "err_cm": e, "efficiency": 1.0 / (e * e * secs)}
+    def fp64(n, imp, seed, dt):
+        T = int(round(DIMER_TAU / dt))
+        sm = pg.DMC_Sim(num_walkers=n, num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2, masses=dm,
+                        delta_t=dt, potential=pot, imp_samp=imp, start_structures=pg.WATER_DIMER_EQ[None], seed=seed,
+                        write_files=False, graph_steps=32)
+        sm._init_device()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sm._run_steps(T)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        if sm._read_ctrl().status:
+            raise RuntimeError(f"fp64 dimer run stopped (status {sm._read_ctrl().status})")
+        vr = conv(sm._hist["vref"].cpu().numpy()[:T])
+        ws = float(n + sm._hist["pop"].cpu().numpy()[:T - 1].sum())
+        del sm
+        return vr, secs, ws
 
-    fp64("plain_fp64_200k", None, (13, 14, 15))
-    fp64("is_fp64_200k", trial, (13,))
+    for tag, n, imp, seeds in (("plain_fp64_200k", 200000, None, plain_seeds),
+                               ("is_fp64_100k", 100000, trial, (13,))):
+        res[tag] = {"walkers": n, "seeds": list(seeds)}
+        for dt in DIMER_DTS:
+            zs, es, secs, ws = [], [], 0.0, 0.0
+            for seed in seeds:
+                vr, sc, w = fp64(n, imp, seed, dt)
+                z, e = zpe_estimate(vr)
+                zs.append(z)
+                es.append(e)
+                secs += sc
+                ws += w
+            res[tag][f"dt{dt:g}"] = {"zpe_cm": float(np.mean(zs)),
+                                     "err_cm": float(np.sqrt(np.sum(np.square(es))) / len(es)),
+                                     "seconds": secs, "walker_steps_per_s": ws / secs, "steps": int(DIMER_TAU / dt)}
+        res[tag]["dt0"] = extrapolate(res[tag])
     ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
-    nd = pg.NNDMC(m, pot, ns, pg.WATER_DIMER_EQ[None], dm, DT, T + 16, seed=13, audit_every=100, imp_samp=trial,
-                  graph_steps=16).init()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    nd.run(T)
-    torch.cuda.synchronize()
-    secs = time.perf_counter() - t0
-    v = pg.Constants.convert(nd.vref_history()[:, T // 4:T], "wavenumbers", to_AU=False)
     w = np.asarray(ns, dtype=float)
-    zr = v.mean(1)
-    z = float((w * zr).sum() / w.sum())
-    e = float(np.sqrt((w * w * (zr - z) ** 2).sum() * len(w) / (len(w) - 1)) / w.sum())
-    # a second error estimate: each replica's own blocking error, combined with the same weights
-    eb = np.array([pg.blocking_error(v[r], 30)[1] for r in range(len(ns))])
-    e_rb = float(np.sqrt(np.sum((w * eb) ** 2)) / w.sum())
-    res["is_nn_64_replicas"] = {"replicas": len(ns), "walkers": int(sum(ns)), "steps": T, "seconds": secs,
-                                "walker_steps_per_s": nd.walker_steps(0, T) / secs, "zpe_cm": z, "err_cm": e,
-                                "err_blocking_cm": nd.zpe(start=T // 4)[1], "err_replica_blocking_cm": e_rb,
-                                "efficiency": 1.0 / (e * e * secs), "audit": nd.audit()}
-    base = res["plain_fp64_200k"]["efficiency"]
-    res["is_gain_fp64_at_equal_error"] = res["is_fp64_200k"]["efficiency"] / base
-    res["gain_vs_plain_fp64_at_equal_error"] = res["is_nn_64_replicas"]["efficiency"] / base
-    res["gain_vs_plain_fp64_at_equal_error_replica_blocking"] = 1.0 / (e_rb * e_rb * secs) / base
-    # the reference's CPU path on the same dimer (oracle port, plain discrete), a bounded
-    # sample: its error per walker-step is the plain FP64 run's (same algorithm), so the
-    # gain at equal error scales with the throughput ratio
+    tag = "is_nn_64_replicas"
+    res[tag] = {"replicas": len(ns), "walkers": int(sum(ns))}
+    for dt in DIMER_DTS:
+        T = int(round(DIMER_TAU / dt))
+        nd = pg.NNDMC(m, pot, ns, pg.WATER_DIMER_EQ[None], dm, dt, T + 16, seed=13, audit_every=100,
+                      imp_samp=trial, graph_steps=16).init()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nd.run(T)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        v = conv(nd.vref_history()[:, :T])
+        z, e = zpe_estimate((w[:, None] * v).sum(0) / w.sum())
+        res[tag][f"dt{dt:g}"] = {"zpe_cm": z, "err_cm": e, "seconds": secs, "steps": T,
+                                 "walker_steps_per_s": nd.walker_steps(0, T) / secs, "audit": nd.audit()}
+        del nd
+    res[tag]["dt0"] = extrapolate(res[tag])
+    base = res["plain_fp64_200k"]["dt0"]["efficiency"]
+    res["gain_vs_plain_fp64_at_equal_error"] = res[tag]["dt0"]["efficiency"] / base
+    res["is_fp64_gain_vs_plain_fp64_at_equal_error"] = res["is_fp64_100k"]["dt0"]["efficiency"] / base
+    for dt in DIMER_DTS:  # the same comparison at each fixed dt (statistical error only), for reference
+        k = f"dt{dt:g}"
+        e_of = lambda r: 1.0 / (r[k]["err_cm"] ** 2 * r[k]["seconds"])  # noqa: E731
+        res[f"gain_at_fixed_{k}"] = e_of(res[tag]) / e_of(res["plain_fp64_200k"])
+        d = res[tag][k]["zpe_cm"] - res["is_fp64_100k"][k]["zpe_cm"]
+        res[f"zpe_minus_fp64_is_{k}_cm"] = [d, float(np.hypot(res[tag][k]["err_cm"],
+                                                               res["is_fp64_100k"][k]["err_cm"]))]
+    a, b = res[tag]["dt0"], res["plain_fp64_200k"]["dt0"]
+    res["zpe_dt0_minus_plain_fp64_dt0_cm"] = [a["zpe_cm"] - b["zpe_cm"], float(np.hypot(a["err_cm"], b["err_cm"]))]
+    orc = os.path.join(ROOT, "profiles", "dimer_fp64_oracle.json")
+    if os.path.exists(orc):
+        o = json.load(open(orc))
+        res["fp64_oracle_dt0_cm"] = [o["zpe_dt0_cm"], o["err_dt0_cm"]]
+        res["zpe_dt0_minus_fp64_oracle_cm"] = [a["zpe_cm"] - o["zpe_dt0_cm"],
+                                               float(np.hypot(a["err_cm"], o["err_dt0_cm"]))]
+    # the reference's CPU path on the same dimer (oracle port, plain discrete), a bounded sample: its
+    # error per walker-step is the plain FP64 run's (same algorithm), so the gain at equal error scales
+    # with the throughput ratio
     cores = os.cpu_count() or 1
     cpu, ccores = cpu_reference_rate(20000, 20, 1, "dimer")[0], 1
     if cores > 1:
@@ -692,11 +750,45 @@ def run_combined_dimer(m, pot, dm, T=6000):
                                   "sample": "oracle restatement of DMC_Sim.propagate (plain, discrete), "
                                             "20000 dimer walkers, numpy; best of 1 process and a "
                                             f"{cores}-process PES pool"}
-    res["gain_vs_cpu_reference_at_equal_error"] = (res["gain_vs_plain_fp64_at_equal_error"] *
-                                                   res["plain_fp64_200k"]["walker_steps_per_s"] / cpu)
-    d = z - res["is_fp64_200k"]["zpe_cm"]
-    res["zpe_minus_fp64_is_cm"] = [d, float(np.hypot(e, res["is_fp64_200k"]["err_cm"]))]
+    plain_rate = res["plain_fp64_200k"]["dt10"]["walker_steps_per_s"]
+    res["gain_vs_cpu_reference_at_equal_error"] = res["gain_vs_plain_fp64_at_equal_error"] * plain_rate / cpu
     return res
+
+
+def dimer_oracle(plain_seeds=tuple(range(101, 165))):
+    """A long plain FP64 extrapolation of the water dimer's ZPE (200000 walkers,
+    64 seeds at dt = 10 and 5): the value profiles/dimer_fp64_oracle.json keeps
+    for the spec comparison."""
+    import torch
+    import pyvibdmc_gb300 as pg
+    dm = [pg.Constants.mass(a) for a in ("O", "H", "H", "O", "H", "H")]
+    pot = pg.water_dimer()
+    res = {}
+    t_all = time.perf_counter()
+    for dt in DIMER_DTS:
+        T = int(round(DIMER_TAU / dt))
+        zs, es = [], []
+        for seed in plain_seeds:
+            sm = pg.DMC_Sim(num_walkers=200000, num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"] * 2,
+                            masses=dm, delta_t=dt, potential=pot, start_structures=pg.WATER_DIMER_EQ[None], seed=seed,
+                            write_files=False, graph_steps=32)
+            sm._init_device()
+            sm._run_steps(T)
+            torch.cuda.synchronize()
+            if sm._read_ctrl().status:
+                continue  # a run that tripped a population guard is left out (and counted)
+            z, e = zpe_estimate(pg.Constants.convert(sm._hist["vref"].cpu().numpy()[:T], "wavenumbers", to_AU=False))
+            zs.append(z)
+            es.append(e)
+            del sm
+        res[f"dt{dt:g}"] = {"zpe_cm": float(np.mean(zs)), "err_cm": float(np.sqrt(np.sum(np.square(es))) / len(es)),
+                            "scatter_err_cm": float(np.std(zs, ddof=1) / np.sqrt(len(zs))), "runs": len(zs),
+                            "runs_left_out": len(plain_seeds) - len(zs)}
+    d0 = extrapolate({k: dict(v, seconds=0.0) for k, v in res.items()})
+    out = {"zpe_dt0_cm": d0["zpe_cm"], "err_dt0_cm": d0["err_cm"], "runs": res, "walkers": 200000,
+           "imaginary_time_au": DIMER_TAU, "seeds": [plain_seeds[0], plain_seeds[-1]],
+           "seconds": time.perf_counter() - t_all, "command": "python bench.py --dimer-oracle"}
+    print(json.dumps(out), flush=True)
 
 
 def run_e2e(sim, L, dev, steps):
@@ -757,10 +849,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", dest="no_extras", action="store_true",
                     help="skip the IS / batched / surrogate workloads reported under 'extras'")
+    ap.add_argument("--dimer-oracle", dest="dimer_oracle", action="store_true",
+                    help="print the long plain FP64 dt -> 0 ZPE of the water dimer (profiles/dimer_fp64_oracle.json)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.dimer_oracle:
+        dimer_oracle()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -11,7 +11,8 @@ silu'').
 """
 import numpy as np
 
-__all__ = ["mlp_forward", "mlp_loss_grads", "silu", "dsilu", "d2silu", "inv_dist_features"]
+__all__ = ["mlp_forward", "mlp_loss_grads", "silu", "dsilu", "d2silu", "inv_dist_features", "bf16", "f32",
+           "mlp_energy_tc"]
 
 
 def silu(z):
@@ -78,3 +79,46 @@ def inv_dist_features(x, v=None):
                 dv = v[:, i] - v[:, j]
                 t.append(-(d * dv).sum(-1) / r ** 3)
     return np.stack(f, 1), (np.stack(t, 1) if v is not None else None)
+
+
+def f32(a):
+    """Round to float32 (returned as float64)."""
+    return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def bf16(a):
+    """Round to bfloat16, nearest even (the conversion the kernels' bf16 packs use),
+    returned as float64."""
+    u = np.asarray(a, dtype=np.float64).astype(np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale):
+    """The tcgen05 inference kernel's arithmetic with its rounding points
+    (gbdmc_mlp_tc.cu): fp32 walkers; descriptors 1/r scaled to (1/r - mu)/sd in
+    fp32 and rounded to bf16 as the A operand; hidden layers with the weights
+    rounded to bf16 and halved (exact), the bias as a bf16 pair b_hi + b_lo of
+    b/2, products summed exactly (the tensor cores accumulate in fp32); the
+    accumulator is h = z/2 and silu(z) = h + h tanh(h) (exact tanh here: the
+    kernel's tanh.approx.f32 differs by at most 2^-10.99 relative); the
+    activations of layers 1 and 2 rounded to bf16, layer 3's kept in fp32;
+    the output h3 . w4 + b4 and V = e_mean + e_scale * output.  (N, 6, 3)
+    fp64 coordinates in, V (N,) out."""
+    x = f32(x)
+    f, _ = inv_dist_features(x)
+    scale = f32(inv_sd[:15])
+    shift = f32(-f32(mu[:15]) * scale)
+    D = np.zeros((len(x), 16))
+    D[:, :15] = bf16(f32(f32(f) * scale + shift))
+    h = D
+    for l in (1, 2, 3):
+        W = bf16(P[f"W{l}"]) * 0.5
+        hb = f32(0.5 * f32(P[f"b{l}"]))
+        b_hi = bf16(hb)
+        b_lo = bf16(f32(hb - b_hi))
+        z2 = h @ W + b_hi + b_lo
+        a = z2 + z2 * np.tanh(z2)
+        h = bf16(a) if l < 3 else f32(a)
+    e = h @ f32(P["w4"])
+    return float(e_mean) + float(e_scale) * (e + float(np.asarray(P["b4"]).ravel()[0]))

@@ -151,17 +151,18 @@ class MLPSurrogate:
         self.grads = {k: torch.zeros_like(v) for k, v in self.P.items()}
         self.g16 = torch.zeros(16, H, device=self.device)
 
-    def train_batch(self, xb, vb, gb, lr, w_e=1.0, w_f=0.5):
-        """One Adam step on a minibatch (x (18, B) fp64, V (B,), dV/dx (18, B)); returns (mse_E, mse_F)."""
+    def _forward_backward(self, xb, vb, gb, w_e, w_f):
+        """Loss gradients of one minibatch into self.grads (the kernels of a
+        training step before the Adam update).  The output bias b4 enters as a
+        shift of the targets, read on the device, so the launches take no value
+        that changes from step to step and can be captured in a CUDA graph."""
         L = _capi.load()
         B = xb.shape[1]
-        if getattr(self, "buf", None) is None or self.buf["feat"].shape[0] != B:
-            self._alloc(B)
         b, P, bf, G = self.buf, self.P, self.bf, self.grads
         vdir = torch.randn(18, B, dtype=torch.float64, device=self.device)
         vdir /= vdir.norm(dim=0, keepdim=True)
         self._features(xb, gb, vdir, b["feat"], b["tang"], b["et"])
-        b["e"].copy_(((vb - self.e_mean) / self.e_scale).float())
+        b["e"].copy_(((vb - self.e_mean) / self.e_scale).float() - P["b4"])
         s = _s()
         ck = _capi.check
         # forward: primal and tangent streams
@@ -176,7 +177,7 @@ class MLPSurrogate:
         for g in G.values():
             g.zero_()
         b["loss"].zero_()
-        ck(L.gbdmc_mlp_head(_p(b["H3"]), _p(b["Ht3"]), _p(P["w4"]), float(P["b4"].item()), _p(b["e"]), _p(b["et"]),
+        ck(L.gbdmc_mlp_head(_p(b["H3"]), _p(b["Ht3"]), _p(P["w4"]), 0.0, _p(b["e"]), _p(b["et"]),
                             B, w_e, w_f, _p(b["Hb3"]), _p(b["Htb3"]), _p(G["w4"]), _p(G["b4"]), _p(b["loss"]), s),
            "head")
         # backward
@@ -195,6 +196,42 @@ class MLPSurrogate:
                 ck(L.gbdmc_mlp_gemm(_p(b[f"Zb{l}"]), B, H, _p(wn), None, _p(b[f"Hb{l-1}"]), s), "gemm")
                 ck(L.gbdmc_mlp_gemm(_p(b[f"Ztb{l}"]), B, H, _p(wn), None, _p(b[f"Htb{l-1}"]), s), "gemm")
         G["W1"][15].zero_()
+
+    def train_batch(self, xb, vb, gb, lr, w_e=1.0, w_f=0.5, graph=False):
+        """One Adam step on a minibatch (x (18, B) fp64, V (B,), dV/dx (18, B)); returns (mse_E, mse_F).
+        With ``graph`` the forward and backward kernels of the step are captured
+        once into a CUDA graph (inputs copied into its fixed buffers) and
+        replayed; the Adam launches, which take the step's learning rate and
+        count, are issued directly."""
+        L = _capi.load()
+        B = xb.shape[1]
+        if getattr(self, "buf", None) is None or self.buf["feat"].shape[0] != B:
+            self._alloc(B)
+            self._tg = None
+        b, P, bf, G = self.buf, self.P, self.bf, self.grads
+        if not graph:
+            self._forward_backward(xb, vb, gb, w_e, w_f)
+        else:
+            key = (B, w_e, w_f, self.e_mean, self.e_scale)
+            if getattr(self, "_tg", None) is None or self._tg[0] != key:
+                sx, sv, sg = xb.clone(), vb.clone(), gb.clone()
+                side = torch.cuda.Stream(device=self.device)
+                side.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(side):
+                    self._forward_backward(sx, sv, sg, w_e, w_f)  # warm-up outside the capture
+                torch.cuda.current_stream().wait_stream(side)
+                gr = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(gr, stream=side):
+                    self._forward_backward(sx, sv, sg, w_e, w_f)
+                torch.cuda.current_stream().wait_stream(side)
+                self._tg = (key, gr, sx, sv, sg)
+            _, gr, sx, sv, sg = self._tg
+            sx.copy_(xb)
+            sv.copy_(vb)
+            sg.copy_(gb)
+            gr.replay()
+        s = _s()
+        ck = _capi.check
         self.t += 1
         for k, p in P.items():
             wt = bf.get(f"{k}t") if k in ("W1", "W2", "W3") else None
@@ -204,8 +241,10 @@ class MLPSurrogate:
                                 self.t, _p(wt), _p(wn), K, s), "adam")
         return b["loss"] / B
 
-    def fit(self, x, v, g, epochs=20, batch=4096, lr=2e-3, lr_final=5e-5, w_f=0.5, seed=0, verbose=False):
-        """Train on harvested data: x, g fp64 SoA (18, M) device tensors, v (M,) fp64."""
+    def fit(self, x, v, g, epochs=20, batch=4096, lr=2e-3, lr_final=5e-5, w_f=0.5, seed=0, verbose=False,
+            graph=True):
+        """Train on harvested data: x, g fp64 SoA (18, M) device tensors, v (M,) fp64.
+        ``graph``: replay each step's forward and backward kernels from a CUDA graph."""
         self.set_normalisation(x, v)
         M = x.shape[1]
         steps = epochs * (M // batch)
@@ -219,7 +258,8 @@ class MLPSurrogate:
             for i in range(nb):
                 idx = perm[i * batch:(i + 1) * batch]
                 lr_k = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps, 1)))
-                tot += self.train_batch(x[:, idx].contiguous(), v[idx], g[:, idx].contiguous(), lr_k, w_f=w_f)
+                tot += self.train_batch(x[:, idx].contiguous(), v[idx], g[:, idx].contiguous(), lr_k, w_f=w_f,
+                                        graph=graph)
                 k += 1
             rec = dict(epoch=ep, mse_e=float(tot[0] / nb), mse_f=float(tot[1] / nb),
                        rmse_e_cm=math.sqrt(float(tot[0] / nb)) * self.e_scale / Constants.atomic_units["wavenumbers"])

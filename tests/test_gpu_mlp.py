@@ -92,9 +92,9 @@ def test_training_gradients_match_oracle():
     b = m.buf
     D = b["feat"].cpu().double().numpy()
     U = b["tang"].cpu().double().numpy()
-    e = b["e"].cpu().double().numpy()
-    et = b["et"].cpu().double().numpy()
     P0["b4"] = P0["b4"][0]
+    e = b["e"].cpu().double().numpy() + P0["b4"]  # the kernels take the targets shifted by b4
+    et = b["et"].cpu().double().numpy()
     Go, loss = mo.mlp_loss_grads(P0, D, U, e, et, 1.0, 0.5)
     Go["W1"][15] = 0.0
     for k in Go:
@@ -106,20 +106,33 @@ def test_training_gradients_match_oracle():
 
 
 def test_inference_kernel_matches_oracle_forward():
+    """The tcgen05 inference kernel against the oracle of its arithmetic (bf16
+    operands and activations where the kernel rounds, exact tanh where the
+    kernel uses tanh.approx): the remaining differences are tanh.approx's and
+    rsqrtf's last bits, which move a fraction of the bf16 roundings by one
+    bf16 step.  Bars in units of the energy scale, and a planted mistake in the
+    oracle (two atoms swapped, which permutes descriptor columns) shows what
+    they catch."""
     m, x, xs, v, g = _small_model(2)
     for _ in range(30):
         m.train_batch(xs, v, g, lr=2e-3)
     P = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
-    P["b4"] = P["b4"][0]
-    f, _ = mo.inv_dist_features(x)
     mu, isd = m.mu.cpu().double().numpy(), m.inv_sd.cpu().double().numpy()
-    D = np.zeros((len(x), 16))
-    D[:, :15] = (f - mu[:15]) * isd[:15]
-    E, _, _ = mo.mlp_forward(P, D)
-    ref = m.e_mean + m.e_scale * E
+    ref = mo.mlp_energy_tc(P, x, mu, isd, m.e_mean, m.e_scale)
     got = m.energy(x)
     err = np.abs(got - ref) / m.e_scale
-    assert np.median(err) < 1e-2 and err.max() < 5e-2, (np.median(err), err.max())
+    assert np.median(err) < 1e-3 and err.max() < 1e-2, (np.median(err), err.max())
+    # the fp64 forward without the rounding (a looser oracle) for scale
+    f, _ = mo.inv_dist_features(x)
+    D = np.zeros((len(x), 16))
+    D[:, :15] = (f - mu[:15]) * isd[:15]
+    E, _, _ = mo.mlp_forward(dict(P, b4=P["b4"][0]), D)
+    loose = np.abs(got - (m.e_mean + m.e_scale * E)) / m.e_scale
+    assert np.median(err) < np.median(loose)
+    x_bad = x.copy()
+    x_bad[:, [4, 5]] = x_bad[:, [5, 4]]  # the hydrogens of water 2 swapped: descriptor columns permuted
+    bad = np.abs(got - mo.mlp_energy_tc(P, x_bad, mu, isd, m.e_mean, m.e_scale)) / m.e_scale
+    assert np.median(bad) > 10 * 1e-3
 
 
 def test_training_reduces_loss_and_surrogate_dmc_runs():
