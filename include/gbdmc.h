@@ -229,17 +229,17 @@ int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbd
 /* Up to max_steps steps of plain DMC in one launch, stopping before step
  * step_end: the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two
  * events, for discrete weighting, Philox deviates and a built-in potential.
- * The walkers stay in shared memory across the steps (each block holds a
- * contiguous run of the population, one grid barrier per step, bounded wait:
- * GBDMC_ST_TIMEOUT on expiry); the deviates and branching uniforms are those of
+ * Each block holds an even share of the population in shared memory during a
+ * step; the branched population goes through dst (compact, logical order)
+ * and is split evenly again, with two grid barriers per step (bounded waits:
+ * GBDMC_ST_TIMEOUT on expiry).  The deviates and branching uniforms are those of
  * gbdmc_sim_step, so the trajectory is gbdmc_sim_step's (vref sums in another
  * order, last bits).  src holds the ctrl->n compact walkers (idx NULL); dst
  * receives the compact walkers after the last step run (x, v, who), or the
  * moved unbranched walkers of a step whose guards tripped, or -- when no step
  * runs (status set, step >= step_end) -- a copy of src, so a queue of calls
  * alternating two buffers always leaves the walkers in the last call's dst.
- * A launch may stop before max_steps when a block's share of the population
- * outgrows its buffer; ctrl->step tells how far it got.  Scratch:
+ * ctrl->step tells how far a launch got.  Scratch:
  * gbdmc_sim_run_scratch_bytes(), zeroed before the first call (the kernel
  * leaves it zeroed).  Returns GBDMC_ERR_CAPACITY, before any launch, when the
  * per-block buffers of sim->n0 walkers do not fit shared memory. */
@@ -304,15 +304,18 @@ int gbdmc_sim_step_host(const gbdmc_sim_t* sim, const gbdmc_walkers_t* host, con
                         const gbdmc_noise_t* noise, void* stream);
 
 /* Allocation-free step (no counterpart in the reference).  For callers that
- * cannot allocate device memory -- e.g. code running while a CUDA graph is
- * being captured, or a plug-in that is handed only its input and output
- * buffers -- this is gbdmc_sim_step with its scratch taken from a static
+ * cannot allocate device memory -- a plug-in that is handed only its input
+ * and output buffers, or a host application whose own memory manager owns
+ * the device and forbids other allocations -- this is gbdmc_sim_step with
+ * its scratch taken from a static
  * device array of GBDMC_STATIC_SCRATCH_BYTES (1 MiB) inside the library, so
  * sim->ld is limited to gbdmc_sim_step_static_max_ld() walkers (larger ld
  * returns GBDMC_ERR_CAPACITY).  It calls no allocator.  The array is held
  * by every GPU that loads the library until the process exits.  The first
  * call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * (cudaGetSymbolAddress), so make that first call before any stream capture;
+ * the address is kept for the life of the process and is not valid after a
+ * cudaDeviceReset of that device.
  * All calls share the one array: calls that overlap on the GPU (other
  * streams, other threads) race and must be serialised by the caller.  The
  * scratch needs no zeroing between calls; every word a step reads is written

@@ -1,28 +1,29 @@
 // Many plain-DMC steps (discrete weighting, Philox deviates) in one launch:
 // the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two events.
 //
-// The walkers stay in shared memory across the steps.  CTA c of a
-// cooperative grid of G CTAs holds a contiguous run of the population in
-// its logical (np.repeat) order: it starts with walkers [c*N/G, (c+1)*N/G)
-// of the compact input, and after every branching its walkers' copies stay
-// with it, in order, so the population remains the concatenation of the
-// CTAs' runs.  One step:
+// The walkers of a step live in shared memory.  CTA c of a cooperative grid
+// of G CTAs holds the run [c*N/G, (c+1)*N/G) of the population in its logical
+// (np.repeat) order.  One step:
 //   1. every walker of the CTA moves (x + fl(sigma z) from Philox, keyed by
 //      its logical index base_c + i as in k_move), its potential, weight and
 //      count (pyvibdmc.py:540-547, :392-403); the CTA's partial (sum c,
 //      sum cV, births, deaths, guards; sum V / min / max when logging) goes
 //      to global memory;
-//   2. one grid barrier (bounded wait, GBDMC_ST_TIMEOUT on expiry);
+//   2. a grid barrier (bounded wait, GBDMC_ST_TIMEOUT on expiry);
 //   3. every CTA reduces the G partials in the same fixed order, so all
 //      of them hold the same N', vref' (calc_vref, :651-661) and guards, and
 //      its new base is the sum of the earlier CTAs' counts;
-//   4. the CTA branches its own walkers into its other shared buffer
-//      (np.repeat order within the CTA).
-// The last step of the launch (or a step after which some CTA's copies would
-// not fit its buffer) branches into the global output instead, compact in
-// logical order, and the launch ends; the next launch splits the population
-// evenly again.  A step whose guards trip writes its moved, unbranched
-// walkers to the output and stops, as the per-step kernels do.
+//   4. every CTA writes its walkers' copies (np.repeat order) to the output
+//      at their logical positions, so the output holds the branched
+//      population compact in logical order;
+//   5. a second grid barrier, and every CTA loads its even share of the new
+//      population back into shared memory (the shares differ by at most one
+//      walker, so no CTA's phase 1 runs longer than another's: without this
+//      rebalancing the runs of the CTAs that branch more grow step by step
+//      and the barrier waits for the largest).
+// After the last step of the launch the output is the result.  A step whose
+// guards trip writes its moved, unbranched walkers to the output and stops,
+// as the per-step kernels do.
 // The deviates and branching uniforms are those of the per-step kernels
 // (same Philox counters), so the trajectories agree; vref sums the CTA
 // partials in another order (last-bit differences).
@@ -104,10 +105,10 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
                                                  gbdmc_walkers_t out, gbdmc_ctrl_t* ctrl, const RunArgs R) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int capc = R.capc, G = gridDim.x, c = blockIdx.x;
-  double* xs[2] = {reinterpret_cast<double*>(smem), reinterpret_cast<double*>(smem) + 3 * A * capc};
-  double* vs = xs[1] + 3 * A * capc;
-  int* whos[2] = {reinterpret_cast<int*>(vs + capc), reinterpret_cast<int*>(vs + capc) + capc};
-  int* cnt = whos[1] + capc;
+  double* xs = reinterpret_cast<double*>(smem);  // [3A][capc]
+  double* vs = xs + 3 * A * capc;                // [capc]
+  int* whos = reinterpret_cast<int*>(vs + capc);  // [capc]
+  int* cnt = whos + capc;                         // [capc]
   __shared__ long long s_base, s_nc, s_nnew, s_N;
   __shared__ double s_vref;
   __shared__ int s_stop;  // 0 go on, 1 branch to the output and end, 2 guards tripped
@@ -146,14 +147,13 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       if (track) out.who[g] = in.who[g];
     }
   } else {
-    // the CTA's run of the compact input
+    // the CTA's even share of the compact input
     for (int i = threadIdx.x; i < s_nc; i += kRunTPB) {
       const int64_t g = s_base + i;
 #pragma unroll
-      for (int k = 0; k < 3 * A; ++k) xs[0][k * capc + i] = in.x[k * ld + g];
-      whos[0][i] = track ? in.who[g] : 0;
+      for (int k = 0; k < 3 * A; ++k) xs[k * capc + i] = in.x[k * ld + g];
+      whos[i] = track ? in.who[g] : 0;
     }
-    int cur = 0;
     for (unsigned t = 0;; ++t, ++step) {
       const long long base = s_base, nc = s_nc, N = s_N;
       const double vref = s_vref;
@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         gen_normals<NM, 3 * A>(rng, z);
 #pragma unroll
         for (int k = 0; k < 3 * A; ++k) {
-          x[k] = __dadd_rn(xs[cur][k * capc + i], __dmul_rn(S.sigma[k / 3], z[k]));
-          xs[cur][k * capc + i] = x[k];
+          x[k] = __dadd_rn(xs[k * capc + i], __dmul_rn(S.sigma[k / 3], z[k]));
+          xs[k * capc + i] = x[k];
         }
         const double v = pes<PK, A, false>(x, S.pes, g);
         vs[i] = v;
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         R.part[par * G + c] = p;
       }
       // 2. every CTA's partial
-      if (!run_barrier(R.sync, (unsigned)G * (t + 1))) {
+      if (!run_barrier(R.sync, (unsigned)G * (2 * t + 1))) {
         if (threadIdx.x == 0) {
           atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
           ctrl->err_step = (int)step;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       }
       // 3. the same reduction in every CTA: thread k takes CTAs k and k + kRunTPB
       Partial q = partial_zero();
-      long long below = 0, mx = 0, fl = 0;
+      long long below = 0, fl = 0;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int g = threadIdx.x + h * kRunTPB;
@@ -209,28 +209,18 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
           accumulate(q, r);
           q.aux = 0;
           if (g < c) below += r.c;
-          mx = max(mx, r.c);
           fl |= r.aux;
         }
       }
       q.aux = below;
       q = block_reduce_partial<STATS>(q);  // sums `below` too (aux)
-      mx = __reduce_max_sync(0xffffffffu, (unsigned)mx);
-      __shared__ long long s_mx[kRunTPB / 32];
       __shared__ int s_fl[kRunTPB / 32];
       fl = __reduce_or_sync(0xffffffffu, (unsigned)fl);
-      if ((threadIdx.x & 31) == 0) {
-        s_mx[threadIdx.x >> 5] = mx;
-        s_fl[threadIdx.x >> 5] = (int)fl;
-      }
+      if ((threadIdx.x & 31) == 0) s_fl[threadIdx.x >> 5] = (int)fl;
       __syncthreads();
       if (threadIdx.x == 0) {
-        long long m = 0;
         int f = 0;
-        for (int w = 0; w < kRunTPB / 32; ++w) {
-          m = max(m, s_mx[w]);
-          f |= s_fl[w];
-        }
+        for (int w = 0; w < kRunTPB / 32; ++w) f |= s_fl[w];
         const long long Nn = q.c;
         int st = f;
         if (!st) {
@@ -253,7 +243,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
             if (S.hist.deaths) S.hist.deaths[h] = (int)q.deaths;
           }
         }
-        s_stop = st ? 2 : ((m > capc || step + 1 >= R.step_end || (int)t + 1 >= R.kmax) ? 1 : 0);
+        s_stop = st ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || (Nn + G - 1) / G > capc) ? 1 : 0);
         if (c == 0) {
           if (st) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
             ctrl->n = N;
@@ -268,7 +258,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
             ctrl->step = step + 1;
           }
         }
-        s_nnew = q.aux;  // the new base: the earlier CTAs' copies
+        s_nnew = q.aux;  // the new logical base of this CTA's copies: the earlier CTAs' copies
         s_vref = vr;
         s_N = Nn;
       }
@@ -278,39 +268,48 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         for (int i = threadIdx.x; i < nc; i += kRunTPB) {
           const int64_t g = base + i;
 #pragma unroll
-          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = xs[cur][k * capc + i];
+          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = xs[k * capc + i];
           out.v[g] = vs[i];
-          if (track) out.who[g] = whos[cur][i];
+          if (track) out.who[g] = whos[i];
         }
         break;
       }
-      // 4. branch: the CTA's copies in np.repeat order
+      // 4. branch: the CTA's copies into the output at their logical positions
+      // (np.repeat order), the whole population compact in logical order
       const int tot = run_scan(cnt, (int)nc);
       const long long nb = s_nnew;
       for (int i = threadIdx.x; i < nc; i += kRunTPB) {
         const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
-        const int pos = cnt[i];
+        const int64_t g0 = nb + cnt[i];
         for (int r = 0; r < c0; ++r) {
-          if (stop) {
-            const int64_t g = nb + pos + r;
 #pragma unroll
-            for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = xs[cur][k * capc + i];
-            out.v[g] = vs[i];
-            if (track) out.who[g] = whos[cur][i];
-          } else {
-#pragma unroll
-            for (int k = 0; k < 3 * A; ++k) xs[cur ^ 1][k * capc + pos + r] = xs[cur][k * capc + i];
-            whos[cur ^ 1][pos + r] = whos[cur][i];
-          }
+          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g0 + r] = xs[k * capc + i];
+          out.v[g0 + r] = vs[i];
+          if (track) out.who[g0 + r] = whos[i];
         }
       }
       if (stop) break;
+      // 5. every CTA's copies written; each CTA takes its even share of the new
+      // population back into shared memory (read past L1: other SMs wrote it)
+      if (!run_barrier(R.sync, (unsigned)G * (2 * t + 2))) {
+        if (threadIdx.x == 0) {
+          atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+          ctrl->err_step = (int)step;
+        }
+        break;
+      }
+      const long long Nn = s_N, nbase = Nn * c / G, nnc = Nn * (c + 1) / G - nbase;
+      for (int i = threadIdx.x; i < nnc; i += kRunTPB) {
+        const int64_t g = nbase + i;
+#pragma unroll
+        for (int k = 0; k < 3 * A; ++k) xs[k * capc + i] = __ldcg(out.x + k * ld + g);
+        whos[i] = track ? __ldcg(out.who + g) : 0;
+      }
       __syncthreads();
       if (threadIdx.x == 0) {
-        s_base = nb;
-        s_nc = tot;
+        s_base = nbase;
+        s_nc = nnc;
       }
-      cur ^= 1;
       __syncthreads();
     }
   }
@@ -327,7 +326,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
 
 // ------------------------------------------------------------ host side
 static size_t run_smem_bytes(int A, int capc) {
-  return (size_t)capc * (2 * 3 * A * sizeof(double) + sizeof(double) + 2 * sizeof(int) + sizeof(int));
+  return (size_t)capc * (3 * A * sizeof(double) + sizeof(double) + 2 * sizeof(int));
 }
 
 struct RunShape {
@@ -387,15 +386,14 @@ static int run_dispatch(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const 
 }
 
 // Grid and per-CTA buffer of a launch: about 96 walkers per CTA, at most one
-// CTA per SM (and kRunMaxCTA); each CTA's buffer holds 2.25 times its share
-// of n0 (the population may grow to 1.5 n0, and a CTA's share by half again
-// before the launch stops and the population is split evenly again).
+// CTA per SM (and kRunMaxCTA); each CTA's buffer holds its even share of the
+// largest population the guard allows (1.5 n0) with a margin.
 static int run_shape(const gbdmc_sim_t& S, RunShape& sh) {
   const int A = S.natoms;
   int g = (int)((S.n0 + 95) / 96);
   const int lim = num_sms() < kRunMaxCTA ? num_sms() : kRunMaxCTA;
   g = g < 1 ? 1 : (g > lim ? lim : g);
-  const int64_t capc = ((S.n0 * 9 / 4 + g - 1) / g + 32 + 31) / 32 * 32;
+  const int64_t capc = ((S.n0 * 3 / 2 + 1 + g - 1) / g + 64 + 31) / 32 * 32;
   const size_t smem = run_smem_bytes(A, (int)capc);
   if (capc > INT32_MAX || smem > 200 * 1024) {
     set_error("gbdmc_sim_run: %lld walkers per block buffer do not fit shared memory (%zu bytes); use "

@@ -63,12 +63,12 @@ def test_multi_step_kernel_follows_the_per_step_trajectory(system):
     _same(a, b)
 
 
-def test_launches_that_stop_when_a_block_outgrows_its_buffer():
+def test_copies_that_pile_up_in_a_few_blocks_are_split_evenly():
     """The walkers of the first blocks sit at the bottom of a harmonic well and the
-    others high up its side, so the first blocks' shares grow by a fifth every step
-    while the population stays near N0: a block's copies outgrow its buffer, the
-    launch stops, the next launch splits the population evenly again, and the
-    trajectory is still the per-step kernels'."""
+    others high up its side, so the first blocks' walkers multiply by a fifth every
+    step while the population stays near N0: every step splits the branched
+    population evenly over the blocks again, one launch runs all 40 steps, and
+    the trajectory is the per-step kernels'."""
     ho = oracle.ho_config()
     n = 2000
     x0 = np.zeros((n, 1, 3))
@@ -76,7 +76,7 @@ def test_launches_that_stop_when_a_block_outgrows_its_buffer():
     a, b = _pair(num_walkers=n, num_timesteps=40, equil_steps=10 ** 6, atoms=["H"], masses=ho["masses"],
                  delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=29)
     _same(a, b)
-    assert a._multi_launches > 1  # 40 steps fit one launch of 64: the extra launches are the stops
+    assert a._multi_launches == 1
 
 
 def test_multi_step_guards_stop_with_the_moved_walkers():

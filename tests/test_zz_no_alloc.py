@@ -1,8 +1,8 @@
 """The allocation-free step entry point, gbdmc_sim_step_static.
 
-Some callers cannot allocate device memory: code running inside a CUDA graph
-being captured, under a framework's own caching allocator, or in a plug-in
-that only receives its input and output buffers.  gbdmc_sim_step_static runs
+Some callers cannot allocate device memory: code running under a framework
+whose caching allocator owns the device, or a plug-in that only receives its
+input and output buffers.  gbdmc_sim_step_static runs
 the same walker step as gbdmc_sim_step, but its scratch lives in a static
 device array inside libgbdmc.so instead of a caller-provided buffer.  This
 test drives both entry points through the C ABI on identical walkers for two
