@@ -112,17 +112,18 @@ def measured_peaks():
 
 # -------------------------------------------------------------- CPU sides
 class _NumpyNoise:
-    """NumPy Generator deviates for the CPU baseline (the reference draws from
-    NumPy's legacy global RandomState; the cost per deviate is similar)."""
+    """NumPy's legacy RandomState deviates for the CPU baseline, drawn as the
+    reference draws them (np.random.normal(0, sigmas, size) in move_randomly,
+    np.random.random(N) in birth_or_death, pyvibdmc.py:544, :392)."""
 
     def __init__(self, seed):
-        self.g = np.random.default_rng(seed)
+        self.g = np.random.RandomState(seed)
 
     def normal(self, loc=0.0, scale=1.0, size=None):
-        return loc + scale * self.g.standard_normal(size)
+        return self.g.normal(loc, scale, size)
 
     def random(self, size=None):
-        return self.g.random(size)
+        return self.g.random_sample(size)
 
 
 def _pool_pes(chunk):
@@ -540,10 +541,10 @@ def run_extras(steps):
     th = np.deg2rad(104.5)
     eq = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [1.81 * np.cos(th), 1.81 * np.sin(th), 0.0]])
     Tb = 4000
-    bi = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, Tb + 16, imp_samp=pg.h2o_gaussian_trial(),
+    bi = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, Tb + 400, imp_samp=pg.h2o_gaussian_trial(),
                       seed=5, start_noise=0.05, graph_steps=16)
     bi.init()
-    bi.autotune(steps_per_candidate=2)
+    bi.autotune(steps_per_candidate=20)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     bi.run(Tb)
@@ -559,23 +560,10 @@ def run_extras(steps):
            "walker_steps_per_s": ws / secs, "zpe_cm": z, "err_cm": e, "efficiency": 1.0 / (e * e * secs)}
     isb["gain_vs_plain_h2o_20k_at_equal_error"] = isb["efficiency"] / eff["plain"]["efficiency"]
     out["is_batched_64_replicas_h2o"] = isb
-    # batched ensemble: 64 replicas, N_r ~ U[1000, 65536] (seeded)
-    ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
-    th = np.deg2rad(104.5)
-    eq = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [1.81 * np.cos(th), 1.81 * np.sin(th), 0.0]])
-    b = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, steps + 64, seed=3, start_noise=0.05,
-                     graph_steps=16)
-    b.init()
-    tune = b.autotune(steps_per_candidate=3)
-    b.run(16)
-    torch.cuda.synchronize()
-    t0 = b.step
-    _, secs = _timed_graph_rate(lambda k: b.run(k, check=False), lambda: 0, steps)
-    b.check()
-    ws = b.walker_steps(t0, t0 + steps)
-    out["batched_64_replicas"] = {"walkers_total": int(sum(ns)), "walker_steps_per_s": ws / secs,
-                                  "us_per_step": secs / steps * 1e6,
-                                  "tile_width_per_bucket": {str(k): v[0] for k, v in tune.items()}}
+    # batched ensemble (config 5): 64 plain FP64 replicas, N_r ~ U[1000, 65536] (seeded), tile widths and
+    # graph length autotuned, 10000 steps; every replica's ZPE with its blocking error, and 16 of them
+    # against the individually run plain path (DMC_Sim, another seed)
+    out["batched_64_replicas"] = run_batched_replicas(masses)
     # surrogate dimer (200000 walkers) vs the analytic fp64 dimer
     dm = [pg.Constants.mass(a) for a in ("O", "H", "H", "O", "H", "H")]
     pot = pg.water_dimer()
@@ -642,6 +630,54 @@ def extrapolate(res):
     s0 = float(np.sqrt(4 * b["err_cm"] ** 2 + a["err_cm"] ** 2))
     cost = a["seconds"] + b["seconds"]
     return {"zpe_cm": e0, "err_cm": s0, "seconds": cost, "efficiency": 1.0 / (s0 * s0 * cost) if cost > 0 else None}
+
+
+def run_batched_replicas(masses, T=10000, nsingle=16):
+    """Config 5: 64 independent plain FP64 water replicas with N_r ~ U[1000,
+    65536] (seeded) stepped together (DMC_Batch: buckets by walker count, tile
+    width and graph length autotuned with 20 timed steps per candidate), for T
+    production steps.  Every replica's ZPE (the last 3/4 of its vref series,
+    blocking error of 30 blocks) and, for every fourth replica, the same
+    system run alone through the plain path (DMC_Sim, another Philox seed):
+    chi^2 of the differences over their combined errors."""
+    import torch
+    import pyvibdmc_gb300 as pg
+    ns = [int(v) for v in np.random.default_rng(0).integers(1000, 65537, size=64)]
+    th = np.deg2rad(104.5)
+    eq = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [1.81 * np.cos(th), 1.81 * np.sin(th), 0.0]])
+    b = pg.DMC_Batch(pg.h2o_local_mode(), ns, eq[None], masses, DT, T + 600, seed=3, start_noise=0.05,
+                     graph_steps=16)
+    b.init()
+    tune = b.autotune(steps_per_candidate=20)
+    b.run(16)
+    torch.cuda.synchronize()
+    s0 = b.step
+    _, secs = _timed_graph_rate(lambda k: b.run(k, check=False), lambda: 0, T)
+    b.check()
+    ws = b.walker_steps(s0, s0 + T)
+    conv = lambda v: pg.Constants.convert(v, "wavenumbers", to_AU=False)  # noqa: E731
+    vr = conv(b.vref_history()[:, s0:s0 + T])
+    table = [[ns[r]] + list(zpe_estimate(vr[r])) for r in range(len(ns))]
+    comp = []
+    for r in range(0, len(ns), len(ns) // nsingle):
+        sm = pg.DMC_Sim(num_walkers=ns[r], num_timesteps=T, equil_steps=10 ** 9, atoms=["O", "H", "H"], masses=masses,
+                        delta_t=DT, potential=pg.h2o_local_mode(), start_structures=start_structures(ns[r], 500 + r),
+                        seed=777, replica_id=r, write_files=False)
+        sm._init_device()
+        sm._run_steps(T)
+        torch.cuda.synchronize()
+        zs, es = zpe_estimate(conv(sm._hist["vref"].cpu().numpy()[:T]))
+        comp.append([r, ns[r], table[r][1], table[r][2], zs, es])
+        del sm
+    chi2 = float(sum(((zb - zs) / np.hypot(eb, es)) ** 2 for _, _, zb, eb, zs, es in comp))
+    return {"replicas": len(ns), "walkers_total": int(sum(ns)), "steps": T, "seconds": secs,
+            "walker_steps_per_s": ws / secs, "us_per_step": secs / T * 1e6,
+            "tile_width_per_bucket": {str(k): v[0] for k, v in tune.items() if k != "graph_steps"},
+            "graph_steps": tune["graph_steps"][0],
+            "zpe_per_replica_cm": {"columns": ["n0", "zpe_cm", "err_cm"], "rows": table},
+            "vs_single_runs": {"columns": ["replica", "n0", "batch_zpe_cm", "batch_err_cm", "single_zpe_cm",
+                                           "single_err_cm"], "rows": comp,
+                               "chi2": chi2, "dof": len(comp), "chi2_per_dof": chi2 / len(comp)}}
 
 
 def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):

@@ -12,7 +12,7 @@ silu'').
 import numpy as np
 
 __all__ = ["mlp_forward", "mlp_loss_grads", "silu", "dsilu", "d2silu", "inv_dist_features", "bf16", "f32",
-           "mlp_energy_tc"]
+           "mlp_energy_tc", "mlp_loss_grads_bf16"]
 
 
 def silu(z):
@@ -122,3 +122,47 @@ def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale):
         h = bf16(a) if l < 3 else f32(a)
     e = h @ f32(P["w4"])
     return float(e_mean) + float(e_scale) * (e + float(np.asarray(P["b4"]).ravel()[0]))
+
+
+def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5):
+    """The training kernels' arithmetic with their rounding points
+    (gbdmc_mlp.cu: k_gemm_xw, k_silu_fwd, k_head, k_silu_bwd, k_gemm_tn): every
+    GEMM operand rounded to bf16 (activations, tangents, back-propagated
+    signals and the weights), products summed exactly and the sum rounded to
+    fp32 (the tensor cores accumulate in fp32), the bias added in fp32; every
+    buffer the kernels store is fp32; the logistic function 1 / (1 + exp(-z))
+    in fp32.  The output bias enters as a shift of the targets (e here is
+    already shifted), so the head adds nothing.  D, U are the kernels' (M, 16)
+    descriptor and tangent rows, e, et their (M,) targets.  Returns the
+    gradients and the two loss sums."""
+    M = len(D)
+    Wb = {l: bf16(P[f"W{l}"]) for l in (1, 2, 3)}
+    w4 = f32(P["w4"])
+    h, ht = f32(D), f32(U)
+    cache = {}
+    for l in (1, 2, 3):
+        z = f32(f32(bf16(h) @ Wb[l]) + f32(P[f"b{l}"]))
+        zt = f32(bf16(ht) @ Wb[l])
+        s = f32(1.0 / f32(1.0 + f32(np.exp(-z))))
+        cache[l] = (h, ht, z, zt, s)
+        h = f32(z * s)
+        ht = f32(f32(s * f32(1.0 + f32(z * f32(1.0 - s)))) * zt)
+    E = f32(h @ w4)
+    Et = f32(ht @ w4)
+    dE = f32(2.0 * wE * f32(E - f32(e)) / M)
+    dEt = f32(2.0 * wF * f32(Et - f32(et)) / M)
+    G = {"w4": h.T @ dE + ht.T @ dEt, "b4": np.array([dE.sum()])}
+    hb = f32(np.outer(dE, w4))
+    htb = f32(np.outer(dEt, w4))
+    for l in (3, 2, 1):
+        hin, htin, z, zt, s = cache[l]
+        d1 = f32(s * f32(1.0 + f32(z * f32(1.0 - s))))
+        d2 = f32(f32(s * f32(1.0 - s)) * f32(2.0 + f32(z * f32(1.0 - f32(2.0 * s)))))
+        zb = bf16(f32(d1 * hb + f32(d2 * zt) * htb))
+        ztb = bf16(f32(d1 * htb))
+        G[f"W{l}"] = bf16(hin).T @ zb + bf16(htin).T @ ztb
+        G[f"b{l}"] = zb.sum(0)
+        hb = f32(zb @ Wb[l].T)
+        htb = f32(ztb @ Wb[l].T)
+    loss = (float(((E - f32(e)) ** 2).sum()), float(((Et - f32(et)) ** 2).sum()))
+    return G, loss

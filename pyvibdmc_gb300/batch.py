@@ -216,10 +216,15 @@ class DMC_Batch:
                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)), "gbdmc_batch_init")
         self.step = 0
 
-    def autotune(self, steps_per_candidate=4):
-        """Pick the tile width of each bucket by timing real steps of the run
-        (buckets stepped one after the other, CUDA events around each).
-        Returns {bucket index: (tpb, microseconds per step)}."""
+    def autotune(self, steps_per_candidate=20, graph_lengths=(8, 16, 32)):
+        """Pick the tile width of each bucket and the steps per CUDA graph by
+        timing real steps of the run: first every tile width on every bucket
+        (buckets stepped one after the other, CUDA events around each,
+        ``steps_per_candidate`` steps per width), then every graph length with
+        the chosen widths (replays covering at least ``steps_per_candidate``
+        steps, events around them).  Returns {bucket index: (tpb, microseconds
+        per step, all timings)} and records the graph length under
+        ``tuning['graph_steps']``."""
         if self.fixed_tpb:
             return {}
         if not self._lazy:
@@ -242,6 +247,25 @@ class DMC_Batch:
             bk["sim"] = self._make_sim(bk, tpb)
             self.tuning[b] = (tpb, timing[b][tpb], dict(timing[b]))
         self._graphs.clear()
+        gtime = {}
+        s = torch.cuda.current_stream()
+        for gl in graph_lengths:
+            self.graph_steps = max(2, int(gl) // 2 * 2)
+            self._graphs.clear()
+            self._graph(self._cur).replay()  # capture + one warm replay
+            self.step += self.graph_steps
+            reps = max(1, -(-steps_per_candidate // self.graph_steps))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                self._graph(self._cur).replay()
+            e1.record(s)
+            torch.cuda.synchronize()
+            self.step += reps * self.graph_steps
+            gtime[self.graph_steps] = e0.elapsed_time(e1) * 1e3 / (reps * self.graph_steps)
+        self.graph_steps = min(gtime, key=gtime.get)
+        self._graphs.clear()
+        self.tuning["graph_steps"] = (self.graph_steps, gtime[self.graph_steps], gtime)
         self.check()
         return dict(self.tuning)
 

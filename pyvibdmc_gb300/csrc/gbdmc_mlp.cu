@@ -150,12 +150,19 @@ __global__ void __launch_bounds__(256) k_gemm_tn(const float* __restrict__ X, co
 }
 
 // ------------------------------------------------------------ elementwise
+// The training kernels take the logistic function through CUDA's expf and an
+// IEEE division (a few fp32 ulps), so that the gradients can be checked
+// against an oracle that rounds where these kernels round; inference keeps
+// the tanh.approx form (sigmoidf_), whose error is below the bf16 rounding of
+// its activations.
+__device__ __forceinline__ float sigmoid_acc(float z) { return 1.f / (1.f + expf(-z)); }
+
 // H = silu(Z); Ht = silu'(Z) Zt  (tangent stream, may be NULL)
 __global__ void k_silu_fwd(const float* __restrict__ Z, const float* __restrict__ Zt, float* __restrict__ H,
                            float* __restrict__ Ht, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float z = Z[i];
-    const float s = sigmoidf_(z);
+    const float s = sigmoid_acc(z);
     H[i] = z * s;
     if (Ht) Ht[i] = s * (1.f + z * (1.f - s)) * Zt[i];
   }
@@ -167,7 +174,7 @@ __global__ void k_silu_bwd(const float* __restrict__ Z, const float* __restrict_
                            long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float z = Z[i];
-    const float s = sigmoidf_(z);
+    const float s = sigmoid_acc(z);
     const float d1 = s * (1.f + z * (1.f - s));
     const float d2 = s * (1.f - s) * (2.f + z * (1.f - 2.f * s));
     const float hb = Hb[i];

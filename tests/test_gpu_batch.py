@@ -51,6 +51,8 @@ def test_batch_autotune_and_zpe_consistency():
                      start_noise=0.05, buckets=(4096, 1 << 40))
     b.init()
     tune = b.autotune(steps_per_candidate=3)
+    gl, gus, gtable = tune.pop("graph_steps")
+    assert gl in gtable and set(gtable) == {8, 16, 32} and b.graph_steps == gl and gus > 0
     assert len(tune) == len(b.buckets)
     for tpb, us, table in tune.values():
         assert tpb in pg.DMC_Batch.CANDIDATES and us > 0
