@@ -466,6 +466,22 @@ int gbdmc_prof_read(double* move_ms, int64_t* move_launches, double* scatter_ms,
  * events around the call. */
 int gbdmc_fp64_fma_probe(double* sink_dev, int64_t iters, int32_t blocks, double* flops_out, void* stream);
 
+/* ---- compile-time bounds checking (no counterpart in the reference) ----
+ * libgbdmc_bc.so is the same library built with -DGBDMC_BOUNDS_CHECK: every
+ * data-dependent index of the step kernels (gather indices, copy positions,
+ * kill-list slots, the multi-step kernel's block buffers and output) is checked
+ * against its range; an index outside it sets the bit of its site (the
+ * gbdmc::BoundsSite numbering: 0 plain-move gather, 1 importance-sampled
+ * gather, 2 compaction gather, 3 gbdmc_sim_move gather, 4 discrete copy past
+ * the capacity, 5 continuous kill-list slot or argmax, 6 multi-step block
+ * buffer, 7 multi-step output, 8 surrogate copy past the capacity) and is
+ * replaced by the low end of the range, so the kernel never traps.
+ * gbdmc_bounds_check_enabled() is 1 in that build and 0 in libgbdmc.so;
+ * gbdmc_bounds_errors(clear) synchronises the device and returns the bits set
+ * since the last clear (always 0 in libgbdmc.so). */
+int gbdmc_bounds_check_enabled(void);
+uint32_t gbdmc_bounds_errors(int32_t clear);
+
 #ifdef __cplusplus
 }
 #endif

@@ -685,8 +685,9 @@ class OracleDMC:
 
     def __init__(self, x0, masses, dt, pes, noise, num_walkers=None, weighting="discrete",
                  trial=None, alpha=None, equil_steps=None, wfn_every=None, desc_wt_steps=None,
-                 cont_wt_thresh=None, start_cont_wts=None):
+                 cont_wt_thresh=None, start_cont_wts=None, branch_every=1):
         self.x = np.array(x0, dtype=np.float64, copy=True)
+        self.branch_every = int(branch_every)  # branching on steps t % branch_every == 0 (pyvibdmc.py:139)
         self.n0 = len(self.x) if num_walkers is None else num_walkers
         self.masses = np.asarray(masses, dtype=np.float64)
         self.dt = dt
@@ -765,11 +766,19 @@ class OracleDMC:
             self.v = self.pes(self.x)
             if self.trial is not None:
                 self.v = self.v + local_kin(self.inv_m3, self.sd)
+            branch = t % self.branch_every == 0
             dt = self.dt
-            if self.trial is not None:
+            if self.trial is not None and (branch or self.weighting == "continuous"):
+                # update_effetive_timestep (pyvibdmc.py:386-387, :832-834)
                 dt = self.dt * self.dt_factor
                 self.eff_ts.append(dt if t == 0 else self.eff_ts[-1] + dt)
-            if self.weighting == "discrete":
+            if not branch:
+                # off the branching schedule (pyvibdmc.py:828-837): discrete walkers
+                # are not weighted; continuous weights are updated, nothing replaced
+                if self.weighting == "continuous":
+                    self.w *= np.exp(-1.0 * (self.v - self.vref) * dt)
+                self.counters.append((0, 0, len(self.x), rej))
+            elif self.weighting == "discrete":
                 u = self.noise.random(size=len(self.x))
                 idx, counts, births, deaths = birth_or_death_discrete(self.v, self.vref, dt, u,
                                                                       self.pop_thresh[1])

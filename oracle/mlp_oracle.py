@@ -124,7 +124,7 @@ def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale):
     return float(e_mean) + float(e_scale) * (e + float(np.asarray(P["b4"]).ravel()[0]))
 
 
-def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5):
+def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5, magnitudes=False):
     """The training kernels' arithmetic with their rounding points
     (gbdmc_mlp.cu: k_gemm_xw, k_silu_fwd, k_head, k_silu_bwd, k_gemm_tn): every
     GEMM operand rounded to bf16 (activations, tangents, back-propagated
@@ -134,7 +134,9 @@ def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5):
     in fp32.  The output bias enters as a shift of the targets (e here is
     already shifted), so the head adds nothing.  D, U are the kernels' (M, 16)
     descriptor and tangent rows, e, et their (M,) targets.  Returns the
-    gradients and the two loss sums."""
+    gradients and the two loss sums; with ``magnitudes`` also the sums of the
+    magnitudes of the terms each gradient entry adds up (the scale of the
+    fp32 summation error, which cancellation leaves in place)."""
     M = len(D)
     Wb = {l: bf16(P[f"W{l}"]) for l in (1, 2, 3)}
     w4 = f32(P["w4"])
@@ -152,6 +154,7 @@ def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5):
     dE = f32(2.0 * wE * f32(E - f32(e)) / M)
     dEt = f32(2.0 * wF * f32(Et - f32(et)) / M)
     G = {"w4": h.T @ dE + ht.T @ dEt, "b4": np.array([dE.sum()])}
+    Gm = {"w4": np.abs(h).T @ np.abs(dE) + np.abs(ht).T @ np.abs(dEt), "b4": np.array([np.abs(dE).sum()])}
     hb = f32(np.outer(dE, w4))
     htb = f32(np.outer(dEt, w4))
     for l in (3, 2, 1):
@@ -162,7 +165,9 @@ def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5):
         ztb = bf16(f32(d1 * htb))
         G[f"W{l}"] = bf16(hin).T @ zb + bf16(htin).T @ ztb
         G[f"b{l}"] = zb.sum(0)
+        Gm[f"W{l}"] = np.abs(bf16(hin)).T @ np.abs(zb) + np.abs(bf16(htin)).T @ np.abs(ztb)
+        Gm[f"b{l}"] = np.abs(zb).sum(0)
         hb = f32(zb @ Wb[l].T)
         htb = f32(ztb @ Wb[l].T)
     loss = (float(((E - f32(e)) ** 2).sum()), float(((Et - f32(et)) ** 2).sum()))
-    return G, loss
+    return (G, loss, Gm) if magnitudes else (G, loss)

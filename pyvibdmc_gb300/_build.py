@@ -1,7 +1,10 @@
 """Build recipe for libgbdmc.so (sm_103a) -- nvcc, one object per .cu, in parallel.
 
-Usage: ``python -m pyvibdmc_gb300._build`` or ``pyvibdmc_gb300._build.build()``.
-The library lands in ``pyvibdmc_gb300/_lib/`` (in-tree, git-ignored).
+Usage: ``python -m pyvibdmc_gb300._build [-v] [-f]`` or ``pyvibdmc_gb300._build.build()``.
+The libraries land in ``pyvibdmc_gb300/_lib/`` (in-tree, git-ignored):
+libgbdmc.so and libgbdmc_bc.so, the same sources compiled with
+-DGBDMC_BOUNDS_CHECK (index checks that record an error bit instead of
+trapping; loaded when GBDMC_BOUNDS_CHECK=1).
 """
 import concurrent.futures as cf
 import glob
@@ -17,6 +20,8 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libgbdmc.so")
+LIB_BC = os.path.join(OUT_DIR, "libgbdmc_bc.so")
+VARIANTS = {"": (OBJ_DIR, LIB, []), "bc": (os.path.join(OUT_DIR, "obj_bc"), LIB_BC, ["-DGBDMC_BOUNDS_CHECK"])}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -44,20 +49,24 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False):
-    """Compile every CUDA source for sm_103a and link libgbdmc.so; returns its path."""
-    os.makedirs(OBJ_DIR, exist_ok=True)
+def build(verbose=False, force=False, variants=("", "bc")):
+    """Compile every CUDA source for sm_103a and link the libraries of
+    `variants` ("" libgbdmc.so, "bc" libgbdmc_bc.so), all objects in one
+    parallel pool; returns the path of libgbdmc.so."""
     nvcc = _nvcc()
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
     jobs = []
-    for src in _sources():
-        obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-        if force or _stale(obj, [src] + headers):
-            jobs.append((src, obj))
+    for v in variants:
+        obj_dir, _, extra = VARIANTS[v]
+        os.makedirs(obj_dir, exist_ok=True)
+        for src in _sources():
+            obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
+            if force or _stale(obj, [src] + headers):
+                jobs.append((src, obj, extra))
 
     def _compile(job):
-        src, obj = job
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+        src, obj, extra = job
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,17 +77,19 @@ def build(verbose=False, force=False):
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(_compile, jobs))
-    objs = [os.path.join(OBJ_DIR, os.path.basename(s)[:-3] + ".o") for s in _sources()]
-    if force or jobs or _stale(LIB, objs):
-        cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-        cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB + ".tmp"] + objs + \
-              ["-Xlinker", f"-rpath,{os.path.join(cuda, 'lib64')}"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(LIB + ".tmp", LIB)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    for v in variants:
+        obj_dir, lib, _ = VARIANTS[v]
+        objs = [os.path.join(obj_dir, os.path.basename(s)[:-3] + ".o") for s in _sources()]
+        if force or _stale(lib, objs):
+            cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", lib + ".tmp"] + objs + \
+                  ["-Xlinker", f"-rpath,{os.path.join(cuda, 'lib64')}"]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+            os.replace(lib + ".tmp", lib)
     return LIB
 
 

@@ -87,7 +87,9 @@ _lib = None
 
 
 def lib_path():
-    return _build.LIB
+    """libgbdmc.so, or its bounds-checked build libgbdmc_bc.so when the
+    environment sets GBDMC_BOUNDS_CHECK=1 (read at the first load)."""
+    return _build.LIB_BC if os.environ.get("GBDMC_BOUNDS_CHECK") == "1" else _build.LIB
 
 
 def load():
@@ -97,7 +99,7 @@ def load():
         return _lib
     path = lib_path()
     if not os.path.exists(path):
-        _build.build()
+        _build.build(variants=("bc",) if path == _build.LIB_BC else ("",))
     L = C.CDLL(path)
     P = C.c_void_p
     sig = {
@@ -154,6 +156,8 @@ def load():
         "gbdmc_prof_read": ([C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                              C.POINTER(C.c_int64)], C.c_int),
         "gbdmc_fp64_fma_probe": ([P, C.c_int64, C.c_int32, C.POINTER(C.c_double), P], C.c_int),
+        "gbdmc_bounds_check_enabled": ([], C.c_int),
+        "gbdmc_bounds_errors": ([C.c_int32], C.c_uint32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -82,6 +82,19 @@ extern "C" int gbdmc_abi_version(void) { return GBDMC_ABI_VERSION; }
 
 extern "C" const char* gbdmc_last_error(void) { return g_err; }
 
+extern "C" int gbdmc_bounds_check_enabled(void) {
+#ifdef GBDMC_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+extern "C" uint32_t gbdmc_bounds_errors(int32_t clear) {
+  if (cudaDeviceSynchronize() != cudaSuccess) return ~0u;
+  return bounds_read_step(clear) | bounds_read_run(clear) | bounds_read_mlp(clear) | bounds_read_mlp_tc(clear);
+}
+
 
 extern "C" int gbdmc_pes_eval(const gbdmc_pes_t* pes, const double* x, int64_t n, int64_t ld, double* v,
                               double* grad, void* stream) {

@@ -10,6 +10,54 @@ namespace gbdmc {
 constexpr int kMaxTPB = 256;  // largest tile (walkers per tile = threads per block)
 constexpr int kMinTPB = 32;
 
+// Compile-time bounds checking (-DGBDMC_BOUNDS_CHECK, the libgbdmc_bc.so
+// build).  Every data-dependent index of the step kernels passes through
+// GBDMC_BC(i, lo, hi, site): in the checked build an index outside [lo, hi)
+// sets bit `site` of this translation unit's error word and is replaced by lo,
+// so the access stays inside its buffer and the kernel carries on (it never
+// traps); gbdmc_bounds_errors() returns the OR of the words.  In the normal
+// build GBDMC_BC(i, ...) is i.
+enum BoundsSite {
+  kBcMoveGather = 0,     // gather index of the plain move outside the previous population
+  kBcIsGather = 1,       // the same in the importance-sampled move
+  kBcCompactGather = 2,  // the same in gbdmc_walkers_compact
+  kBcExtGather = 3,      // the same in the move of gbdmc_sim_move
+  kBcBranchWrite = 4,    // a copy past the replica's capacity (discrete branching)
+  kBcContSlot = 5,       // continuous branching: a kill-list slot or argmax outside the population
+  kBcRunShared = 6,      // multi-step kernel: a walker slot past the block's buffer
+  kBcRunOut = 7,         // multi-step kernel: an output position past the capacity
+  kBcSurrogateWrite = 8  // a copy past the capacity (surrogate single-pass branching)
+};
+#ifdef GBDMC_BOUNDS_CHECK
+static __device__ unsigned g_bounds_word;
+__device__ __forceinline__ long long bc_index(long long i, long long lo, long long hi, int site) {
+  if (i < lo || i >= hi) {
+    atomicOr(&g_bounds_word, 1u << site);
+    return lo;
+  }
+  return i;
+}
+#define GBDMC_BC(i, lo, hi, site) ::gbdmc::bc_index((long long)(i), (long long)(lo), (long long)(hi), (site))
+#define GBDMC_BOUNDS_READER(fn)                                                                   \
+  unsigned fn(int clear) {                                                                        \
+    unsigned v = 0;                                                                               \
+    if (cudaMemcpyFromSymbol(&v, ::gbdmc::g_bounds_word, sizeof v) != cudaSuccess) return ~0u;   \
+    if (clear) {                                                                                  \
+      const unsigned z = 0;                                                                       \
+      if (cudaMemcpyToSymbol(::gbdmc::g_bounds_word, &z, sizeof z) != cudaSuccess) return ~0u;    \
+    }                                                                                             \
+    return v;                                                                                     \
+  }
+#else
+#define GBDMC_BC(i, lo, hi, site) (i)
+#define GBDMC_BOUNDS_READER(fn) \
+  unsigned fn(int) { return 0u; }
+#endif
+unsigned bounds_read_step(int clear);
+unsigned bounds_read_run(int clear);
+unsigned bounds_read_mlp(int clear);
+unsigned bounds_read_mlp_tc(int clear);
+
 // Per-tile partial results of a walker kernel (64 bytes).
 struct Partial {
   long long c;       // sum of branch counts (or accepted moves)

@@ -766,6 +766,7 @@ static bool valid_net(const gbdmc_mlp_t* net) {
   return net && net->w1t && net->w2t && net->w3t && net->b1 && net->b2 && net->b3 && net->w4;
 }
 
+GBDMC_BOUNDS_READER(bounds_read_mlp)
 }  // namespace gbdmc
 
 using namespace gbdmc;

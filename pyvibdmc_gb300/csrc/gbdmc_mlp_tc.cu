@@ -512,4 +512,5 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
 }
 
+GBDMC_BOUNDS_READER(bounds_read_mlp_tc)
 }  // namespace gbdmc

@@ -2,26 +2,27 @@
 // the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two events.
 //
 // The walkers of a step live in shared memory.  CTA c of a cooperative grid
-// of G CTAs holds the run [c*N/G, (c+1)*N/G) of the population in its logical
-// (np.repeat) order.  One step:
+// of G CTAs holds a run [base_c, base_c + n_c) of the population in its
+// logical (np.repeat) order, the runs of the CTAs back to back.  One step:
 //   1. every walker of the CTA moves (x + fl(sigma z) from Philox, keyed by
 //      its logical index base_c + i as in k_move), its potential, weight and
-//      count (pyvibdmc.py:540-547, :392-403); the CTA's partial (sum c,
-//      sum cV, births, deaths, guards; sum V / min / max when logging) goes
+//      count (pyvibdmc.py:540-547, :392-403); the CTA's 16-byte partial (sum
+//      c, sum cV, deaths, guards; sum V / min / max when logging apart) goes
 //      to global memory;
 //   2. a grid barrier (bounded wait, GBDMC_ST_TIMEOUT on expiry);
-//   3. every CTA reduces the G partials in the same fixed order, so all
-//      of them hold the same N', vref' (calc_vref, :651-661) and guards, and
-//      its new base is the sum of the earlier CTAs' counts;
-//   4. every CTA writes its walkers' copies (np.repeat order) to the output
-//      at their logical positions, so the output holds the branched
-//      population compact in logical order;
-//   5. a second grid barrier, and every CTA loads its even share of the new
-//      population back into shared memory (the shares differ by at most one
-//      walker, so no CTA's phase 1 runs longer than another's: without this
-//      rebalancing the runs of the CTAs that branch more grow step by step
-//      and the barrier waits for the largest).
-// After the last step of the launch the output is the result.  A step whose
+//   3. warp 0 of every CTA reduces the G partials in the same fixed order, so
+//      all CTAs hold the same N', vref' (calc_vref, :651-661), guards and
+//      largest CTA count, and the CTA's new base is the earlier CTAs' counts;
+//   4. the CTA's copies (np.repeat order) become its next run.  Normally they
+//      stay in shared memory (the other half of a double buffer).  When the
+//      largest CTA's copies would take more warps than an even split of N'
+//      (or no double buffer fits), every CTA writes its copies to the output
+//      at their logical positions, a second grid barrier follows, and every
+//      CTA loads its even share of the new population back: the step's time
+//      is that of the CTA with the most walkers, so the runs are split evenly
+//      again before one of them grows by a warp.
+// After the last step of the launch the copies go to the output, which then
+// holds the branched population compact in logical order.  A step whose
 // guards trip writes its moved, unbranched walkers to the output and stops,
 // as the per-step kernels do.
 // The deviates and branching uniforms are those of the per-step kernels
@@ -36,8 +37,19 @@
 namespace gbdmc {
 
 constexpr int kRunTPB = 192;
-constexpr int kRunMaxCTA = 2 * kRunTPB;  // the partial reduction takes two CTAs per thread
+constexpr int kRunMaxCTA = 384;
 constexpr unsigned kRunSpinLimit = 1u << 22;
+
+// A CTA's sums of one step: one 16-byte load per CTA in the reduction.
+struct RunPart {
+  int c;         // sum of the branch counts (the CTA's copies)
+  unsigned df;   // deaths | guard bits << 24 (a CTA holds fewer than 2^24 walkers)
+  double s0;     // sum of c V
+};
+static_assert(sizeof(RunPart) == 16, "RunPart is 16 bytes");
+struct RunStats {  // only when the potential statistics are logged
+  double s1, vmin, vmax, pad;
+};
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -45,14 +57,19 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// Grid barrier over a monotonic arrival counter: returns false if the wait ran
-// out (the caller stops; the other CTAs' next waits run out as well).
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier over a monotonic arrival counter: the CTA's writes are released
+// by thread 0's arrival after the block barrier, the others' acquired by its
+// wait before the next one.  Returns false if the wait ran out (the caller
+// stops; the other CTAs' next waits run out as well).
 __device__ __forceinline__ bool run_barrier(unsigned* arrive, unsigned target) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(arrive, 1u);
+    red_release_add(arrive, 1u);
     int ok = 1;
     unsigned it = 0;
     while (ld_acquire(arrive) < target) {
@@ -60,9 +77,8 @@ __device__ __forceinline__ bool run_barrier(unsigned* arrive, unsigned target) {
         ok = 0;
         break;
       }
-      __nanosleep(64);
+      __nanosleep(32);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
@@ -96,22 +112,80 @@ struct RunArgs {
   int64_t step_end;  // stop before this step
   int kmax;          // and after at most this many steps
   int capc;          // walkers per CTA buffer
-  Partial* part;     // [2][G]
+  int dbuf;          // 1: two walker buffers per CTA (copies stay in shared memory)
+  RunPart* part;     // [2][G]
+  RunStats* stat;    // [2][G]
   unsigned* sync;    // [0] arrivals, [1] exits
 };
+
+// The CTA's sums of step 1, reduced over the block: valid in thread 0.
+template <bool STATS>
+__device__ __forceinline__ void run_block_sums(int& c, int& d, unsigned& f, double& s0, RunStats& st) {
+  __shared__ int4 sh_i[kRunTPB / 32];
+  __shared__ double sh_d[kRunTPB / 32][4];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  c = (int)__reduce_add_sync(full, (unsigned)c);
+  d = (int)__reduce_add_sync(full, (unsigned)d);
+  f = __reduce_or_sync(full, f);
+  if (STATS) {
+    warp_sum2(s0, st.s1);
+    st.vmin = dkey_inv(warp_min_key(dkey(st.vmin)));
+    st.vmax = dkey_inv(warp_max_key(dkey(st.vmax)));
+  } else {
+    s0 = warp_sum(s0);
+  }
+  if (lane == 0) {
+    sh_i[wid] = make_int4(c, d, (int)f, 0);
+    sh_d[wid][0] = s0;
+    if (STATS) {
+      sh_d[wid][1] = st.s1;
+      sh_d[wid][2] = st.vmin;
+      sh_d[wid][3] = st.vmax;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int4 a = sh_i[0];
+    s0 = sh_d[0][0];
+    if (STATS) {
+      st.s1 = sh_d[0][1];
+      st.vmin = sh_d[0][2];
+      st.vmax = sh_d[0][3];
+    }
+#pragma unroll
+    for (int w = 1; w < kRunTPB / 32; ++w) {
+      const int4 b = sh_i[w];
+      a.x += b.x;
+      a.y += b.y;
+      a.z |= b.z;
+      s0 += sh_d[w][0];
+      if (STATS) {
+        st.s1 += sh_d[w][1];
+        st.vmin = fmin(st.vmin, sh_d[w][2]);
+        st.vmax = fmax(st.vmax, sh_d[w][3]);
+      }
+    }
+    c = a.x;
+    d = a.y;
+    f = (unsigned)a.z;
+  }
+}
 
 template <int PK, int A, int NM, bool STATS>
 __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_sim_t S, const gbdmc_walkers_t in,
                                                  gbdmc_walkers_t out, gbdmc_ctrl_t* ctrl, const RunArgs R) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int capc = R.capc, G = gridDim.x, c = blockIdx.x;
-  double* xs = reinterpret_cast<double*>(smem);  // [3A][capc]
-  double* vs = xs + 3 * A * capc;                // [capc]
-  int* whos = reinterpret_cast<int*>(vs + capc);  // [capc]
-  int* cnt = whos + capc;                         // [capc]
+  const int capc = R.capc, G = gridDim.x, c = blockIdx.x, nbuf = R.dbuf ? 2 : 1;
+  const int lane = threadIdx.x & 31;
+  double* xsb = reinterpret_cast<double*>(smem);     // [nbuf][3A][capc]
+  double* vs = xsb + (size_t)nbuf * 3 * A * capc;     // [capc]
+  int* whob = reinterpret_cast<int*>(vs + capc);      // [nbuf][capc]
+  int* cnt = whob + (size_t)nbuf * capc;              // [capc]
   __shared__ long long s_base, s_nc, s_nnew, s_N;
   __shared__ double s_vref;
   __shared__ int s_stop;  // 0 go on, 1 branch to the output and end, 2 guards tripped
+  __shared__ int s_even;  // 1: every CTA takes its even share of the new population
   const int64_t ld = S.ld;
   const long long N0 = S.n0;
   const double n0 = (double)N0, w_hi = (n0 + n0 * 0.5) + 1.0;
@@ -147,19 +221,26 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       if (track) out.who[g] = in.who[g];
     }
   } else {
+    int cur = 0;
+    unsigned nbar = 0;  // grid barriers passed: every CTA takes the same ones (the same decisions)
     // the CTA's even share of the compact input
     for (int i = threadIdx.x; i < s_nc; i += kRunTPB) {
       const int64_t g = s_base + i;
+      const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
 #pragma unroll
-      for (int k = 0; k < 3 * A; ++k) xs[k * capc + i] = in.x[k * ld + g];
-      whos[i] = track ? in.who[g] : 0;
+      for (int k = 0; k < 3 * A; ++k) xsb[k * capc + j] = in.x[k * ld + g];
+      whob[j] = track ? in.who[g] : 0;
     }
     for (unsigned t = 0;; ++t, ++step) {
       const long long base = s_base, nc = s_nc, N = s_N;
       const double vref = s_vref;
+      double* xs = xsb + (size_t)cur * 3 * A * capc;
+      int* whos = whob + (size_t)cur * capc;
       // 1. move, potential, weight, count
-      Partial p = partial_zero();
-      int flag = 0;
+      int csum = 0, flag = 0;
+      long long births = 0, deaths = 0;
+      double s0 = 0.0;
+      RunStats st = {0.0, INFINITY, -INFINITY, 0.0};
       for (int i = threadIdx.x; i < nc; i += kRunTPB) {
         double x[3 * A], z[3 * A], g[3 * A];
         Rng rng(S.seed, (uint64_t)step, (uint64_t)(base + i), S.replica_id);
@@ -172,95 +253,130 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         const double v = pes<PK, A, false>(x, S.pes, g);
         vs[i] = v;
         if (STATS) {
-          p.s1 += v;
-          p.vmin = fmin(p.vmin, v);
-          p.vmax = fmax(p.vmax, v);
+          st.s1 += v;
+          st.vmin = fmin(st.vmin, v);
+          st.vmax = fmax(st.vmax, v);
         }
-        const int cn = branch_count(v, vref, S.dt, rng.uniform53(), w_hi, flag, p.births, p.deaths);
+        const int cn = branch_count(v, vref, S.dt, rng.uniform53(), w_hi, flag, births, deaths);
         cnt[i] = cn;
-        p.c += cn;
-        p.s0 += cn == 1 ? v : (double)cn * v;
+        csum += cn;
+        s0 += cn == 1 ? v : (double)cn * v;
       }
-      p.aux = __syncthreads_or(flag & GBDMC_ST_NONFINITE_WEIGHT) ? GBDMC_ST_NONFINITE_WEIGHT : 0;
-      p.aux |= __syncthreads_or(flag & GBDMC_ST_HUGE_WEIGHT) ? GBDMC_ST_HUGE_WEIGHT : 0;
-      const long long aux = p.aux;
-      p = block_reduce_partial<STATS>(p);
+      int dsum = (int)deaths;
+      unsigned fl = (unsigned)flag;
+      run_block_sums<STATS>(csum, dsum, fl, s0, st);
       const int par = t & 1;
       if (threadIdx.x == 0) {
-        p.aux = aux;
-        R.part[par * G + c] = p;
+        RunPart q;
+        q.c = csum;
+        q.df = (unsigned)dsum | (fl << 24);
+        q.s0 = s0;
+        R.part[par * G + c] = q;
+        if (STATS) R.stat[par * G + c] = st;
       }
       // 2. every CTA's partial
-      if (!run_barrier(R.sync, (unsigned)G * (2 * t + 1))) {
+      if (!run_barrier(R.sync, (unsigned)G * ++nbar)) {
         if (threadIdx.x == 0) {
           atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
           ctrl->err_step = (int)step;
         }
         break;
       }
-      // 3. the same reduction in every CTA: thread k takes CTAs k and k + kRunTPB
-      Partial q = partial_zero();
-      long long below = 0, fl = 0;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int g = threadIdx.x + h * kRunTPB;
-        if (g < G) {
-          const Partial r = load_partial(R.part + par * G + g);
-          accumulate(q, r);
-          q.aux = 0;
-          if (g < c) below += r.c;
-          fl |= r.aux;
-        }
-      }
-      q.aux = below;
-      q = block_reduce_partial<STATS>(q);  // sums `below` too (aux)
-      __shared__ int s_fl[kRunTPB / 32];
-      fl = __reduce_or_sync(0xffffffffu, (unsigned)fl);
-      if ((threadIdx.x & 31) == 0) s_fl[threadIdx.x >> 5] = (int)fl;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int f = 0;
-        for (int w = 0; w < kRunTPB / 32; ++w) f |= s_fl[w];
-        const long long Nn = q.c;
-        int st = f;
-        if (!st) {
-          if ((double)Nn < n0 - n0 * 0.5) st |= GBDMC_ST_POP_LOW;
-          if ((double)Nn > n0 + n0 * 0.5) st |= GBDMC_ST_POP_HIGH;
-          if (Nn > ld) st |= GBDMC_ST_OVERFLOW;
-        }
-        const double vr = q.s0 / (double)Nn - S.alpha * ((double)(Nn - N0) / n0);
-        if (c == 0 && step < S.hist.len) {
-          const int64_t h = step;
+      // 3. the same reduction in every CTA, in warp 0: lane l takes CTAs l, l + 32, ...
+      if (threadIdx.x < 32) {
+        const unsigned full = 0xffffffffu;
+        long long nn = 0, below = 0;  // 64-bit: a collapsing step's counts may pass 2^31
+        int nd = 0, cmax = 0;
+        unsigned f = 0;
+        double q0 = 0.0;
+        RunStats qs = {0.0, INFINITY, -INFINITY, 0.0};
+        for (int g = lane; g < G; g += 32) {
+          const int4 r = __ldcg(reinterpret_cast<const int4*>(R.part + par * G + g));
+          const int rc = r.x;
+          nn += rc;
+          nd += (int)((unsigned)r.y & 0xFFFFFFu);
+          f |= (unsigned)r.y >> 24;
+          q0 += __hiloint2double(r.w, r.z);
+          if (g < c) below += rc;
+          cmax = rc > cmax ? rc : cmax;
           if (STATS) {
-            if (S.hist.vmin) S.hist.vmin[h] = q.vmin;
-            if (S.hist.vmax) S.hist.vmax[h] = q.vmax;
-            if (S.hist.vmean) S.hist.vmean[h] = q.s1 / (double)N;
-          }
-          if (!st) {
-            if (S.hist.vref) S.hist.vref[h] = vr;
-            if (S.hist.pop) S.hist.pop[h] = (double)Nn;
-            if (S.hist.births) S.hist.births[h] = (int)q.births;
-            if (S.hist.deaths) S.hist.deaths[h] = (int)q.deaths;
+            const double2 a = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g));
+            const double2 b = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g) + 1);
+            qs.s1 += a.x;
+            qs.vmin = fmin(qs.vmin, a.y);
+            qs.vmax = fmax(qs.vmax, b.x);
           }
         }
-        s_stop = st ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || (Nn + G - 1) / G > capc) ? 1 : 0);
-        if (c == 0) {
-          if (st) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
-            ctrl->n = N;
-            ctrl->vref = vref;
-            ctrl->step = step;
-            ctrl->status = st;
-            ctrl->err_step = (int)step;
-          } else if (s_stop == 1) {
-            ctrl->n_prev = N;
-            ctrl->n = Nn;
-            ctrl->vref = vr;
-            ctrl->step = step + 1;
-          }
+        if (STATS) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) qs.s1 += __shfl_xor_sync(full, qs.s1, o);
+          qs.vmin = dkey_inv(warp_min_key(dkey(qs.vmin)));
+          qs.vmax = dkey_inv(warp_max_key(dkey(qs.vmax)));
         }
-        s_nnew = q.aux;  // the new logical base of this CTA's copies: the earlier CTAs' copies
-        s_vref = vr;
-        s_N = Nn;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          nn += __shfl_xor_sync(full, nn, o);
+          below += __shfl_xor_sync(full, below, o);
+        }
+        nd = (int)__reduce_add_sync(full, (unsigned)nd);
+        cmax = (int)__reduce_max_sync(full, (unsigned)cmax);
+        f = __reduce_or_sync(full, f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) q0 += __shfl_xor_sync(full, q0, o);
+        const long long Nn = nn;
+        // the step's divisions, one SIMT division: <V> of the branched population
+        // (lane 0), the population term (lane 1), the mean potential (lane 2)
+        const double num = lane == 0 ? q0 : (lane == 1 ? (double)(Nn - N0) : qs.s1);
+        const double den = lane == 0 ? (double)Nn : (lane == 1 ? n0 : (double)N);
+        const double qq = num / den;
+        const double vbar = __shfl_sync(full, qq, 0), corr = __shfl_sync(full, qq, 1);
+        const double vmean = __shfl_sync(full, qq, 2);
+        if (lane == 0) {
+          int st2 = (int)f;
+          if (!st2) {
+            if ((double)Nn < n0 - n0 * 0.5) st2 |= GBDMC_ST_POP_LOW;
+            if ((double)Nn > n0 + n0 * 0.5) st2 |= GBDMC_ST_POP_HIGH;
+            if (Nn > ld) st2 |= GBDMC_ST_OVERFLOW;
+          }
+          const double vr = vbar - S.alpha * corr;
+          if (c == 0 && step < S.hist.len) {
+            const int64_t h = step;
+            if (STATS) {
+              if (S.hist.vmin) S.hist.vmin[h] = qs.vmin;
+              if (S.hist.vmax) S.hist.vmax[h] = qs.vmax;
+              if (S.hist.vmean) S.hist.vmean[h] = vmean;
+            }
+            if (!st2) {
+              if (S.hist.vref) S.hist.vref[h] = vr;
+              if (S.hist.pop) S.hist.pop[h] = (double)Nn;
+              if (S.hist.births) S.hist.births[h] = (int)(Nn - (N - nd));  // sum of max(c - 1, 0)
+              if (S.hist.deaths) S.hist.deaths[h] = nd;
+            }
+          }
+          const long long even = (Nn + G - 1) / G;
+          const int stop = st2 ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || even > capc) ? 1 : 0);
+          s_stop = stop;
+          // the largest CTA's copies against the warps of an even split
+          const long long lim = ((even + 31) / 32) * 32;
+          s_even = !R.dbuf || (long long)cmax > (lim < capc ? lim : (long long)capc);
+          if (c == 0) {
+            if (st2) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
+              ctrl->n = N;
+              ctrl->vref = vref;
+              ctrl->step = step;
+              ctrl->status = st2;
+              ctrl->err_step = (int)step;
+            } else if (stop == 1) {
+              ctrl->n_prev = N;
+              ctrl->n = Nn;
+              ctrl->vref = vr;
+              ctrl->step = step + 1;
+            }
+          }
+          s_nnew = below;  // the new logical base of this CTA's copies: the earlier CTAs' copies
+          s_vref = vr;
+          s_N = Nn;
+        }
       }
       __syncthreads();
       const int stop = s_stop;
@@ -274,41 +390,63 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         }
         break;
       }
-      // 4. branch: the CTA's copies into the output at their logical positions
-      // (np.repeat order), the whole population compact in logical order
+      // 4. branch: the CTA's copies in np.repeat order
       const int tot = run_scan(cnt, (int)nc);
       const long long nb = s_nnew;
-      for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-        const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
-        const int64_t g0 = nb + cnt[i];
-        for (int r = 0; r < c0; ++r) {
+      if (stop || s_even) {
+        // into the output at their logical positions: the whole population compact in logical order
+        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
+          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
+          const int64_t g0 = nb + cnt[i];
+          for (int r = 0; r < c0; ++r) {
+            const int64_t go = GBDMC_BC(g0 + r, 0, ld, kBcRunOut);
 #pragma unroll
-          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g0 + r] = xs[k * capc + i];
-          out.v[g0 + r] = vs[i];
-          if (track) out.who[g0 + r] = whos[i];
+            for (int k = 0; k < 3 * A; ++k) out.x[k * ld + go] = xs[k * capc + i];
+            out.v[go] = vs[i];
+            if (track) out.who[go] = whos[i];
+          }
         }
-      }
-      if (stop) break;
-      // 5. every CTA's copies written; each CTA takes its even share of the new
-      // population back into shared memory (read past L1: other SMs wrote it)
-      if (!run_barrier(R.sync, (unsigned)G * (2 * t + 2))) {
+        if (stop) break;
+        // every CTA's copies written; each CTA takes its even share of the new
+        // population back into shared memory (read past L1: other SMs wrote it)
+        if (!run_barrier(R.sync, (unsigned)G * ++nbar)) {
+          if (threadIdx.x == 0) {
+            atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+            ctrl->err_step = (int)step;
+          }
+          break;
+        }
+        const long long Nn = s_N, nbase = Nn * c / G, nnc = Nn * (c + 1) / G - nbase;
+        for (int i = threadIdx.x; i < nnc; i += kRunTPB) {
+          const int64_t g = nbase + i;
+          const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
+#pragma unroll
+          for (int k = 0; k < 3 * A; ++k) xs[k * capc + j] = __ldcg(out.x + k * ld + g);
+          whos[j] = track ? __ldcg(out.who + g) : 0;
+        }
         if (threadIdx.x == 0) {
-          atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
-          ctrl->err_step = (int)step;
+          s_base = nbase;
+          s_nc = nnc;
         }
-        break;
-      }
-      const long long Nn = s_N, nbase = Nn * c / G, nnc = Nn * (c + 1) / G - nbase;
-      for (int i = threadIdx.x; i < nnc; i += kRunTPB) {
-        const int64_t g = nbase + i;
+      } else {
+        // into the other buffer: the CTA's next run is its copies, at logical base nb
+        double* xn = xsb + (size_t)(cur ^ 1) * 3 * A * capc;
+        int* wn = whob + (size_t)(cur ^ 1) * capc;
+        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
+          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
+          const int j0 = cnt[i];
+          for (int r = 0; r < c0; ++r) {
+            const int j = (int)GBDMC_BC(j0 + r, 0, capc, kBcRunShared);
 #pragma unroll
-        for (int k = 0; k < 3 * A; ++k) xs[k * capc + i] = __ldcg(out.x + k * ld + g);
-        whos[i] = track ? __ldcg(out.who + g) : 0;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        s_base = nbase;
-        s_nc = nnc;
+            for (int k = 0; k < 3 * A; ++k) xn[k * capc + j] = xs[k * capc + i];
+            wn[j] = whos[i];
+          }
+        }
+        cur ^= 1;
+        if (threadIdx.x == 0) {
+          s_base = nb;
+          s_nc = tot;
+        }
       }
       __syncthreads();
     }
@@ -325,12 +463,12 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
 }
 
 // ------------------------------------------------------------ host side
-static size_t run_smem_bytes(int A, int capc) {
-  return (size_t)capc * (3 * A * sizeof(double) + sizeof(double) + 2 * sizeof(int));
+static size_t run_smem_bytes(int A, int capc, int nbuf) {
+  return (size_t)capc * (nbuf * (3 * A * sizeof(double) + sizeof(int)) + sizeof(double) + sizeof(int));
 }
 
 struct RunShape {
-  int grid, capc;
+  int grid, capc, dbuf;
   size_t smem;
 };
 
@@ -385,33 +523,39 @@ static int run_dispatch(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const 
                : run_launch<PK, A, GBDMC_NOISE_PHILOX64, false>(S, src, dst, ctrl, R, sh, s);
 }
 
-// Grid and per-CTA buffer of a launch: about 96 walkers per CTA, at most one
+// Grid and per-CTA buffers of a launch: about 96 walkers per CTA, at most one
 // CTA per SM (and kRunMaxCTA); each CTA's buffer holds its even share of the
-// largest population the guard allows (1.5 n0) with a margin.
+// largest population the guard allows (1.5 n0) with a margin.  Two buffers
+// per CTA (the copies of a step stay in shared memory) when they fit, else one
+// (every step splits the population evenly through the output).
 static int run_shape(const gbdmc_sim_t& S, RunShape& sh) {
   const int A = S.natoms;
   int g = (int)((S.n0 + 95) / 96);
   const int lim = num_sms() < kRunMaxCTA ? num_sms() : kRunMaxCTA;
   g = g < 1 ? 1 : (g > lim ? lim : g);
   const int64_t capc = ((S.n0 * 3 / 2 + 1 + g - 1) / g + 64 + 31) / 32 * 32;
-  const size_t smem = run_smem_bytes(A, (int)capc);
-  if (capc > INT32_MAX || smem > 200 * 1024) {
+  const size_t smax = 200 * 1024;
+  if (capc > (1 << 20) || run_smem_bytes(A, (int)capc, 1) > smax) {
     set_error("gbdmc_sim_run: %lld walkers per block buffer do not fit shared memory (%zu bytes); use "
-              "gbdmc_sim_step", (long long)capc, smem);
+              "gbdmc_sim_step", (long long)capc, run_smem_bytes(A, (int)(capc > (1 << 20) ? 1 << 20 : capc), 1));
     return GBDMC_ERR_CAPACITY;
   }
   sh.grid = g;
   sh.capc = (int)capc;
-  sh.smem = smem;
+  sh.dbuf = run_smem_bytes(A, (int)capc, 2) <= smax ? 1 : 0;
+  sh.smem = run_smem_bytes(A, (int)capc, sh.dbuf ? 2 : 1);
   return GBDMC_OK;
 }
+
+GBDMC_BOUNDS_READER(bounds_read_run)
 
 }  // namespace gbdmc
 
 using namespace gbdmc;
 
 extern "C" size_t gbdmc_sim_run_scratch_bytes(void) {
-  return align256(sizeof(Partial) * 2 * kRunMaxCTA) + align256(2 * sizeof(unsigned));
+  return align256(sizeof(RunPart) * 2 * kRunMaxCTA) + align256(sizeof(RunStats) * 2 * kRunMaxCTA) +
+         align256(2 * sizeof(unsigned));
 }
 
 extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
@@ -444,10 +588,14 @@ extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, c
   char* b = (char*)scratch;
   RunArgs R;
   R.step_end = step_end;
-  R.kmax = max_steps;
+  // at most two grid barriers per step on a 32-bit arrival counter
+  const int kcap = (int)((1u << 31) / (2u * (unsigned)sh.grid));
+  R.kmax = max_steps < kcap ? max_steps : kcap;
   R.capc = sh.capc;
-  R.part = (Partial*)b;
-  R.sync = (unsigned*)(b + align256(sizeof(Partial) * 2 * kRunMaxCTA));
+  R.dbuf = sh.dbuf;
+  R.part = (RunPart*)b;
+  R.stat = (RunStats*)(b + align256(sizeof(RunPart) * 2 * kRunMaxCTA));
+  R.sync = (unsigned*)(b + align256(sizeof(RunPart) * 2 * kRunMaxCTA) + align256(sizeof(RunStats) * 2 * kRunMaxCTA));
   cudaStream_t s = (cudaStream_t)stream;
   const int PK = S->pes.kind, A = S->natoms;
   if (PK == GBDMC_PES_HO && A == 1) return run_dispatch<GBDMC_PES_HO, 1>(*S, *src, *dst, ctrl, R, sh, s);

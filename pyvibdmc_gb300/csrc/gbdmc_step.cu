@@ -131,6 +131,9 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
     }
     if (*(volatile int*)&ctrl->status) continue;  // replica stopped by a previous kernel
     const long long n = ctrl->n;
+#ifdef GBDMC_BOUNDS_CHECK
+    if (in.idx && i < n) (void)GBDMC_BC(in.idx[base + i], 0, ctrl->n_prev, kBcMoveGather);
+#endif
     if (!in.idx && i < n) {
 #pragma unroll
       for (int k = 0; k < 3 * A; ++k) x[k] = in.x[k * ld + src];
@@ -216,7 +219,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_move_ext(const __grid_constant__ gb
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     if (i >= n) continue;
     const int64_t base = T.off[r];
-    const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+    const int64_t src = base + (in.idx ? (int64_t)GBDMC_BC(in.idx[base + i], 0, ctrl->n_prev, kBcExtGather) : i);
     const int64_t dst = base + i;
     Rng rng(S.seed, (uint64_t)ctrl->step, (uint64_t)i, T.stream[r]);
     double z1 = 0.0;
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_is_move(const __grid_constant__ gbd
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     Partial p = partial_zero();
     if (i < n) {
-      const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+      const int64_t src = base + (in.idx ? (int64_t)GBDMC_BC(in.idx[base + i], 0, ctrl->n_prev, kBcIsGather) : i);
       const int64_t dst = base + i;
       double x[3 * A], y[3 * A], fx[3 * A], fy[3 * A], sdy[3 * A], g[3 * A];
 #pragma unroll
@@ -417,7 +420,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_branch(const __grid_constant__ RepT
       const int64_t base = T.off[r[u]];
       const long long cap = T.cap[r[u]];
       for (int q = 0; q < c[u]; ++q)
-        if (dest + q < cap) idx[base + dest + q] = (int32_t)i[u];
+        if (GBDMC_BC(dest + q, 0, cap + 1, kBcBranchWrite) < cap) idx[base + dest + q] = (int32_t)i[u];
     }
     __syncthreads();
   }
@@ -512,7 +515,8 @@ __global__ void __launch_bounds__(kMaxTPB) k_compact(const __grid_constant__ gbd
     const int64_t i = (int64_t)(tile - T.tile_off[r]) * blockDim.x + threadIdx.x;
     if (i >= n) continue;
     const int64_t base = T.off[r];
-    const int64_t src = base + (in.idx ? (int64_t)in.idx[base + i] : i);
+    const int64_t src =
+        base + (in.idx ? (int64_t)GBDMC_BC(in.idx[base + i], 0, ctrls[r].n_prev, kBcCompactGather) : i);
     const int64_t dst = base + i;
 #pragma unroll
     for (int k = 0; k < 3 * A; ++k) out.x[k * ld + dst] = in.x[k * ld + src];
@@ -667,8 +671,8 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   const long long nk = block_compact_flags(flags, n, list);
   long long nb = nk;
   for (long long j = 0; j < nk; ++j) {
-    const long long to = list[j];
-    const long long m = block_arg<true>(w, n, nullptr);
+    const long long to = GBDMC_BC(list[j], 0, n, kBcContSlot);
+    const long long m = GBDMC_BC(block_arg<true>(w, n, nullptr), 0, n, kBcContSlot);
     clone_walker<A, IS>(S, W, base, m, to);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -703,8 +707,8 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
     }
     const long long nk2 = nup;
     for (long long j = 0; j < nk2; ++j) {
-      const long long to = list[j];
-      const long long m = block_arg<true>(w, n, nullptr);
+      const long long to = GBDMC_BC(list[j], 0, n, kBcContSlot);
+      const long long m = GBDMC_BC(block_arg<true>(w, n, nullptr), 0, n, kBcContSlot);
       clone_walker<A, IS>(S, W, base, m, to);
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -1452,6 +1456,7 @@ static int static_scratch_ptr(void** out) {
   *out = g_static_scratch_ptr[dev];
   return GBDMC_OK;
 }
+GBDMC_BOUNDS_READER(bounds_read_step)
 }  // namespace gbdmc
 
 extern "C" size_t gbdmc_sim_step_static_max_ld(void) {

@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kMaxTPB) k_count_branch_f32(const __grid_const
 #pragma unroll
       for (int k = 0; k < WPT; ++k) {
         for (int q = 0; q < c[k]; ++q)
-          if (dest + q < cap) idx[base + dest + q] = (int32_t)(ib + k);
+          if (GBDMC_BC(dest + q, 0, cap + 1, kBcSurrogateWrite) < cap) idx[base + dest + q] = (int32_t)(ib + k);
         dest += c[k];
       }
       // the replica's last tile finalises it (block-uniform)

@@ -20,6 +20,7 @@ that supplies the deviates on the host in the reference's call order),
 of the multi-step kernel, walkers resident in shared memory; 0 = one launch
 pair per step, which ``block_threads`` also selects).
 """
+import contextlib
 import ctypes as C
 import pickle
 import time
@@ -31,6 +32,25 @@ from . import _capi
 from . import archive
 from .constants import Constants, get_atomic_num
 from .potentials import Potential_GPU, default_device, to_soa, from_soa
+
+try:  # NVTX ranges around the host's phases (step batches, events), seen by nsys / ncu --nvtx
+    from torch.cuda import nvtx as _nvtx
+    _nvtx.range_push("gbdmc")
+    _nvtx.range_pop()
+except Exception:  # a torch without NVTX: the ranges are skipped
+    _nvtx = None
+
+
+@contextlib.contextmanager
+def nvtx_range(name):
+    if _nvtx is None:
+        yield
+        return
+    _nvtx.range_push(name)
+    try:
+        yield
+    finally:
+        _nvtx.range_pop()
 
 __all__ = ["DMC_Sim", "HostWalkers", "dmc_restart"]
 
@@ -55,8 +75,10 @@ class DMC_Sim:
         bad = [k for k, v in unsupported.items() if v not in (None, False)]
         if bad:
             raise NotImplementedError(f"DMC_Sim options not provided by the GPU engine: {bad}")
-        if branch_every != 1:
-            raise NotImplementedError("the GPU engine branches every step (branch_every=1)")
+        if int(branch_every) < 1:
+            raise ValueError("branch_every must be >= 1")
+        if int(branch_every) != 1 and imp_samp is not None and weighting.lower() == "discrete":
+            raise NotImplementedError("branch_every > 1 with importance-sampled discrete weighting")
         # a built-in GPU surface is fused into the step kernel; any other object with
         # the reference's getpot(cds) contract (potential_manager.py:71-253) is called on
         # the moved walkers between the move and branching kernels
@@ -66,6 +88,7 @@ class DMC_Sim:
         if self._external and not callable(getattr(potential, "getpot", None)):
             raise TypeError("potential must have a getpot(cds, timeit=False) method returning (N,) hartree")
         if self._nn_route and (weighting.lower() != "discrete" or not isinstance(rng, str) or int(cur_timestep) or
+                               int(branch_every) != 1 or
                                (imp_samp is not None and getattr(imp_samp, "kind", None) != "dimer_gauss")):
             raise NotImplementedError("the fused surrogate step runs fresh discrete-weighting runs with Philox "
                                       "deviates (and the dimer trial for importance sampling)")
@@ -81,7 +104,7 @@ class DMC_Sim:
         self.potential = potential
         self.weighting = weighting.lower()
         self.desc_wt_time_steps = desc_wt_steps
-        self.branch_every = branch_every
+        self.branch_every = int(branch_every)
         self.delta_t = delta_t
         self.start_structures = start_structures
         self.start_cont_wts = start_cont_wts
@@ -217,7 +240,7 @@ class DMC_Sim:
         # the multi-step kernel: plain DMC, discrete weighting, Philox deviates, built-in surface
         self._multi = (self.fused_steps > 0 and not self._external and self.weighting == "discrete" and
                        self.impsamp_manager is None and self._noise_mode != _capi.NOISE_INJECTED and
-                       self.block_threads == 0)
+                       self.block_threads == 0 and self.branch_every == 1)
         self._multi_used = False
         self._multi_launches = 0
         if self.write_files:
@@ -401,13 +424,28 @@ class DMC_Sim:
                                      C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
                                      self._stream()), "gbdmc_sim_init")
 
-    def _launch_step(self, cur, lazy, noise=None):
+    def _step_sim(self, step):
+        """The system description for step `step`.  Off the branching schedule
+        (steps t % branch_every != 0, pyvibdmc.py:139, :828-837) discrete walkers
+        are not weighted -- the branching dt is 0, so every weight is 1, every
+        count 1 and vref the plain mean (calc_vref, :651-661) -- and continuous
+        weights are updated without replacements (both thresholds off)."""
+        if self.branch_every == 1 or step % self.branch_every == 0:
+            return self._sim
+        s = _capi.Sim.from_buffer_copy(self._sim)
+        if self.weighting == "discrete":
+            s.dt = 0.0
+        else:
+            s.thresh_lower, s.thresh_upper = -1.0, 0.0
+        return s
+
+    def _launch_step(self, cur, lazy, noise=None, sim=None):
         """Queue one step reading buffer `cur` (through its gather index when
         `lazy`) and writing the other buffer; returns the new (cur, lazy)."""
         L = _capi.load()
         src = self._walker_struct(self._bufs[cur], lazy)
         dst = self._walker_struct(self._bufs[1 - cur], True)
-        rc = L.gbdmc_sim_step(C.byref(self._sim), C.byref(src), C.byref(dst),
+        rc = L.gbdmc_sim_step(C.byref(self._sim if sim is None else sim), C.byref(src), C.byref(dst),
                               C.c_void_p(self._ctrl.data_ptr()), C.c_void_p(self._scratch.data_ptr()),
                               C.byref(noise) if noise is not None else None, self._stream())
         _capi.check(rc, "gbdmc_sim_step")
@@ -440,9 +478,10 @@ class DMC_Sim:
             self._graphs[key] = g
         return g
 
-    def _injected_noise(self, n):
+    def _injected_noise(self, n, branch=True):
         """Host-supplied deviates in the reference's draw order (pyvibdmc.py:544, :556, :601, :392):
-        normal (n, dims, natoms) transposed to (n, natoms, dims), then the uniforms."""
+        normal (n, dims, natoms) transposed to (n, natoms, dims), then the uniforms (the
+        branching ones only on a branching step)."""
         A, D = self.natoms, self.dims
         z = np.asarray(self.rng.standard_normal((n, D, A)), dtype=np.float64)
         zs = torch.as_tensor(np.ascontiguousarray(z.transpose(2, 1, 0).reshape(D * A, n)), device=self.device)
@@ -450,7 +489,8 @@ class DMC_Sim:
         if self.impsamp_manager is not None:
             ua = torch.as_tensor(np.asarray(self.rng.uniform(n), dtype=np.float64), device=self.device)
         ub = torch.as_tensor(np.asarray(self.rng.uniform(n), dtype=np.float64), device=self.device) \
-            if self.weighting == "discrete" else torch.zeros(max(n, 1), dtype=torch.float64, device=self.device)
+            if self.weighting == "discrete" and branch else \
+            torch.zeros(max(n, 1), dtype=torch.float64, device=self.device)
         nz = _capi.Noise()
         nz.normal, nz.u_branch = zs.data_ptr(), ub.data_ptr()
         nz.u_accept = ua.data_ptr() if ua is not None else None
@@ -481,7 +521,7 @@ class DMC_Sim:
             raise ValueError(f"getpot returned {v.numel()} energies for {n} walkers")
         return v
 
-    def _external_step(self, noise=None):
+    def _external_step(self, noise=None, sim=None):
         """One step around the caller's potential: gbdmc_sim_move, getpot on the
         moved walkers, gbdmc_sim_branch (pyvibdmc.py:540-547, 785-793, 380-454,
         651-682).  Returns False when a guard stopped the run."""
@@ -498,7 +538,8 @@ class DMC_Sim:
         step = int(self._step_device)
         vn = v.cpu().numpy() if n else np.zeros(1)
         self._host_vstats[step] = (float(vn.min()), float(vn.max()), float(vn.mean()))
-        _capi.check(L.gbdmc_sim_branch(C.byref(self._sim), C.byref(dst), C.c_void_p(self._ctrl.data_ptr()),
+        _capi.check(L.gbdmc_sim_branch(C.byref(self._sim if sim is None else sim), C.byref(dst),
+                                       C.c_void_p(self._ctrl.data_ptr()),
                                        C.c_void_p(self._scratch.data_ptr()), nz, self._stream()), "gbdmc_sim_branch")
         c = self._read_ctrl()
         # a step whose guards tripped leaves its moved walkers in dst, unbranched
@@ -535,8 +576,31 @@ class DMC_Sim:
             if c.status or int(c.step) >= end:
                 return True
 
+    def _run_steps_schedule(self, nsteps):
+        """nsteps steps with branching every branch_every steps: one launch per
+        step with that step's system description (_step_sim)."""
+        c = self._read_ctrl()
+        step, self._n_now, self._step_device = int(c.step), int(c.n), int(c.step)
+        sync = self._external or self._noise_mode == _capi.NOISE_INJECTED
+        for k in range(nsteps):
+            if sync:
+                c = self._read_ctrl()
+                if c.status:
+                    return
+                self._n_now = int(c.n)
+            sim = self._step_sim(step + k)
+            br = (step + k) % self.branch_every == 0
+            nz = self._injected_noise(self._n_now, br) if self._noise_mode == _capi.NOISE_INJECTED else None
+            if self._external:
+                if not self._external_step(nz, sim):
+                    return
+            else:
+                self._cur, self._lazy = self._launch_step(self._cur, self._lazy, nz, sim)
+
     def _run_steps(self, nsteps):
         """Queue nsteps steps (no host sync in the Philox modes)."""
+        if self.branch_every != 1:
+            return self._run_steps_schedule(nsteps)
         if self._multi and nsteps > 0 and self._run_multi(nsteps):
             return
         if self._external:
@@ -673,10 +737,12 @@ class DMC_Sim:
             # as pyvibdmc.py:710-711: a checkpoint at step t holds the walkers before step t
             self.cur_timestep = self._next_step = t
             if t in self._chkpt_step and self.write_files:
-                archive.delete_older_checkpoints(self.output_folder, self.sim_name, t)
-                self._chkpt(t)
+                with nvtx_range("gbdmc.checkpoint"):
+                    archive.delete_older_checkpoints(self.output_folder, self.sim_name, t)
+                    self._chkpt(t)
             if t in self._wfn_save_step:
-                self._begin_desc(t)
+                with nvtx_range("gbdmc.desc_begin"):
+                    self._begin_desc(t)
             t_end = min(b for b in bounds if b > t)
             t_end = min(t_end, T)
             self._pop_before = self._n_device() if self.impsamp_manager is not None else 0
@@ -684,8 +750,9 @@ class DMC_Sim:
             if self.weighting == "discrete" and not self._lazy and self._noise_mode != _capi.NOISE_INJECTED:
                 cur0 = self._cur  # the first step of the batch is a direct launch from this buffer
             t_start = time.perf_counter()
-            self._run_steps(t_end - t)
-            c = self._read_ctrl()
+            with nvtx_range(f"gbdmc.steps {t}-{t_end}"):
+                self._run_steps(t_end - t)
+                c = self._read_ctrl()
             secs = time.perf_counter() - t_start
             if c.status:
                 done = int(c.err_step) - t
@@ -703,7 +770,8 @@ class DMC_Sim:
             self.cur_timestep = t_end - 1
             last = t_end - 1
             if t_end in self._desc_wt_save_step and self._desc_open is not None:
-                self._end_desc(last)
+                with nvtx_range("gbdmc.desc_end"):
+                    self._end_desc(last)
             if last in self._train_step:
                 self._harvest(last)
             t = t_end
@@ -813,6 +881,8 @@ class HostWalkers:
         if sim._external:
             raise ValueError("HostWalkers steps the built-in GPU potentials; a getpot potential is stepped by "
                              "DMC_Sim.run")
+        if sim.branch_every != 1:
+            raise ValueError("HostWalkers branches every step; a branch_every schedule is stepped by DMC_Sim.run")
         sim._compact()
         torch.cuda.synchronize()
         self.sim = sim
@@ -915,8 +985,8 @@ def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsa
     nxt = int(st.get("_next_step", st["cur_timestep"]))
     archive.delete_future_checkpoints(chkpt_folder, sim_name, nxt)
     T = st["num_timesteps"] + additional_timesteps
-    for k in ("replica_id", "block_threads"):  # the Philox stream and the reduction order of the saved run
-        if k in st:
+    for k in ("replica_id", "block_threads", "branch_every"):  # the Philox stream, the reduction order
+        if k in st:                                             # and the branching schedule of the saved run
             kw.setdefault(k, st[k])
     sim = DMC_Sim(sim_name=st["sim_name"], output_folder=st["output_folder"], weighting=st["weighting"],
                   num_walkers=st["num_walkers"], num_timesteps=T, equil_steps=st["equil_steps"],

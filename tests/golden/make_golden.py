@@ -164,14 +164,14 @@ def derivs(cds):
 
 
 def run_reference(pv, out_dir, name, x0, atoms, masses, dt, nsteps, pes, seed, weighting="discrete",
-                  imp=None, equil=None, wfn_every=None, desc=None, thresh=None):
+                  imp=None, equil=None, wfn_every=None, desc=None, thresh=None, branch_every=1):
     noise = oracle.InjectedNoise(seed)
     kw = dict(sim_name=name, output_folder=os.path.join(out_dir, name), weighting=weighting,
               num_walkers=len(x0), num_timesteps=nsteps, equil_steps=equil if equil is not None else nsteps + 10,
               chkpt_every=10 ** 6, wfn_every=wfn_every or 10 ** 6, desc_wt_steps=desc or 1,
               atoms=atoms, masses=masses, delta_t=dt, potential=pv.Potential_Direct(pes),
               start_structures=np.array(x0, copy=True), log_every=10 ** 6, cont_wt_thresh=thresh,
-              imp_samp=imp)
+              imp_samp=imp, branch_every=branch_every)
     sim = pv.DMC_Sim(**kw)
     with _Patch(noise):
         sim.run()
@@ -220,6 +220,20 @@ def main(ref_path, only=None):  # noqa: C901
     r = run_reference(pv, tmp, "h2o_cont", x0, ["O", "H", "H"], masses, 10.0, 40, pes, seed=3,
                       weighting="continuous", thresh=0.2)
     fixtures["h2o_continuous"] = dict(x0=x0, seed=3, dt=10.0, nsteps=40, thresh=0.2, **r)
+
+    # --- branching every third (discrete, with a descendant window) and every fourth
+    # (continuous) step only (pyvibdmc.py:139, :828-837): off the schedule discrete
+    # walkers are not weighted and continuous weights are updated without replacements
+    n = 256
+    x0 = eq[None] + 0.05 * oracle.InjectedNoise(404).standard_normal((n, 3, 3))
+    r = run_reference(pv, tmp, "h2o_be", x0, ["O", "H", "H"], masses, 10.0, 30, pes, seed=21, equil=8,
+                      wfn_every=1000, desc=12, branch_every=3)
+    fixtures["h2o_branch_every"] = dict(x0=x0, seed=21, dt=10.0, nsteps=30, equil=8, desc=12, branch_every=3, **r)
+    n = 192
+    x0 = eq[None] + 0.05 * oracle.InjectedNoise(405).standard_normal((n, 3, 3))
+    r = run_reference(pv, tmp, "h2o_cbe", x0, ["O", "H", "H"], masses, 10.0, 24, pes, seed=22,
+                      weighting="continuous", thresh=0.2, branch_every=4)
+    fixtures["h2o_cont_branch_every"] = dict(x0=x0, seed=22, dt=10.0, nsteps=24, thresh=0.2, branch_every=4, **r)
 
     # --- continuous weights with both thresholds.  The reference replaces the walkers
     # above the upper threshold in np.argpartition order (portable introselect, see the

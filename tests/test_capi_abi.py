@@ -32,6 +32,17 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(raw, name), f"{name} declared in include/ but not exported"
 
 
+def test_bounds_checked_build_exports_the_same_symbols():
+    from pyvibdmc_gb300 import _build, _capi
+    if not os.path.exists(_build.LIB_BC):
+        _build.build(variants=("bc",))
+    bc = ctypes.CDLL(_build.LIB_BC)
+    for name in declared_symbols():
+        assert hasattr(bc, name), f"{name} not exported by the bounds-checked build"
+    assert bc.gbdmc_bounds_check_enabled() == 1
+    assert _capi.load().gbdmc_bounds_check_enabled() == 0
+
+
 def test_struct_layout_matches():
     from pyvibdmc_gb300 import _capi
     _capi.load()

@@ -251,6 +251,35 @@ def test_engine_importance_sampling_vs_reference():
     np.testing.assert_allclose(sim.walkers, g["x_final"], rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("surface", ["fused", "python"])
+def test_engine_branch_every_vs_reference(surface):
+    """Branching on every third step (discrete, with a descendant window) and
+    every fourth (continuous) only, as the unmodified reference runs them with
+    branch_every (pyvibdmc.py:139, :828-837): the built-in surface fused into
+    the step kernel and the same surface as a Python getpot."""
+    p, m = oracle.h2o_config()
+
+    def pot():
+        return pg.h2o_local_mode() if surface == "fused" else pg.Potential_Direct(lambda c: oracle.pes_h2o_lm(c, p))
+
+    g = load("h2o_branch_every")
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pot(), int(g["seed"]), int(g["nsteps"]), equil=int(g["equil"]),
+               wfn_every=1000, desc=int(g["desc"]), branch_every=int(g["branch_every"]))
+    sim.run()
+    np.testing.assert_array_equal(sim._pop_vs_tau, g["pop"])
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+    assert np.array_equal(sim.walkers, g["x_final"])
+    assert np.array_equal(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"])
+    g = load("h2o_cont_branch_every")
+    sim = _sim(g["x0"], m, ["O", "H", "H"], pot(), int(g["seed"]), int(g["nsteps"]), weighting="continuous",
+               cont_wt_thresh=float(g["thresh"]), branch_every=int(g["branch_every"]))
+    sim.run()
+    x, w = sim.walkers
+    assert np.array_equal(x, g["x_final"])
+    np.testing.assert_allclose(w, g["w_final"], rtol=1e-12)
+    np.testing.assert_allclose(sim._vref_vs_tau, g["vref"], rtol=0, atol=1e-12)
+
+
 def test_engine_dimer_importance_sampling_vs_oracle():
     """Importance-sampled dimer DMC (dimer trial) against the oracle step loop on the same
     injected deviates; tolerances as for the water IS case."""

@@ -80,12 +80,20 @@ def test_sim_logger_writes_the_reference_lines(tmp_path):
                                  dict(excited_state_imp_samp=True), dict(adiabatic_dmc={"steps": 1}),
                                  dict(fixed_node={"g": 1}), dict(DEBUG_mass_change={"factor": 2}),
                                  dict(DEBUG_save_desc_wt_tracker=True), dict(DEBUG_save_before_bod=True),
-                                 dict(branch_every=2)])
+                                 dict(branch_every=2, imp_samp="trial")])
 def test_unsupported_reference_options_raise(opt):
     x0 = np.zeros((1, 3, 3))
+    if opt.get("imp_samp") == "trial":  # branch_every > 1 is refused only with importance-sampled discrete weights
+        opt = dict(opt, imp_samp=pg.h2o_gaussian_trial(device="cpu"))
     with pytest.raises(NotImplementedError):
         pg.DMC_Sim(num_walkers=10, atoms=["O", "H", "H"], potential=pg.h2o_local_mode(), start_structures=x0,
                    write_files=False, **opt)
+
+
+def test_branch_every_must_be_positive():
+    with pytest.raises(ValueError, match="branch_every"):
+        pg.DMC_Sim(num_walkers=10, atoms=["O", "H", "H"], potential=pg.h2o_local_mode(),
+                   start_structures=np.zeros((1, 3, 3)), write_files=False, branch_every=0)
 
 
 def test_potential_must_be_a_gpu_potential():

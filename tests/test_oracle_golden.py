@@ -62,6 +62,29 @@ def test_h2o_continuous_matches_reference():
     assert sum(c[0] for c in sim.counters) > 0  # branching happened
 
 
+def test_branch_every_matches_reference():
+    """Branching on every third (discrete) and fourth (continuous) step only."""
+    p, m = oracle.h2o_config()
+    g = load("h2o_branch_every")
+    sim = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), equil_steps=int(g["equil"]), wfn_every=1000,
+                           desc_wt_steps=int(g["desc"]), branch_every=int(g["branch_every"])).run(int(g["nsteps"]))
+    # vref within a few ulps: NumPy's SIMD sums peel for the array's address alignment
+    np.testing.assert_allclose(np.array(sim.vref_hist), g["vref"], rtol=0, atol=5e-17)
+    assert np.array_equal(np.array(sim.pop_hist), g["pop"])
+    assert np.array_equal(sim.x, g["x_final"])
+    assert np.array_equal(sim.wfns[0]["desc_wts"], g["wfn0_desc_wts"])
+    pops = np.array(sim.pop_hist)
+    assert (pops[1::3] == pops[0::3][:len(pops[1::3])]).all() and (pops[2::3] == pops[1::3][:len(pops[2::3])]).all()
+    g = load("h2o_cont_branch_every")
+    sim = oracle.OracleDMC(g["x0"], m, float(g["dt"]), lambda c: oracle.pes_h2o_lm(c, p),
+                           oracle.InjectedNoise(int(g["seed"])), weighting="continuous",
+                           cont_wt_thresh=float(g["thresh"]), branch_every=int(g["branch_every"])).run(int(g["nsteps"]))
+    np.testing.assert_allclose(np.array(sim.vref_hist), g["vref"], rtol=0, atol=5e-17)
+    assert np.array_equal(sim.x, g["x_final"])
+    np.testing.assert_allclose(sim.w, g["w_final"], rtol=1e-13)  # the vref ulps, compounded over 24 steps
+
+
 def _cont_upper_fixture(name):
     g = load(name)
     p, m = oracle.h2o_config()
