@@ -229,17 +229,22 @@ int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbd
 /* Up to max_steps steps of plain DMC in one launch, stopping before step
  * step_end: the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two
  * events, for discrete weighting, Philox deviates and a built-in potential.
- * Each block holds an even share of the population in shared memory during a
- * step; the branched population goes through dst (compact, logical order)
- * and is split evenly again, with two grid barriers per step (bounded waits:
- * GBDMC_ST_TIMEOUT on expiry).  The deviates and branching uniforms are those of
+ * Each block holds a run of the population (in logical order) in shared
+ * memory; one grid barrier per step exchanges the blocks' sums (vref, N' and
+ * every block's count).  A block's copies stay in its shared memory, except
+ * when the largest block's copies would take more warps than an even split
+ * (or two buffers per block do not fit): then the branched population goes
+ * through dst (compact, logical order) and a second grid barrier lets every
+ * block load its even share.  Waits are bounded (GBDMC_ST_TIMEOUT on expiry).
+ * The deviates and branching uniforms are those of
  * gbdmc_sim_step, so the trajectory is gbdmc_sim_step's (vref sums in another
  * order, last bits).  src holds the ctrl->n compact walkers (idx NULL); dst
  * receives the compact walkers after the last step run (x, v, who), or the
  * moved unbranched walkers of a step whose guards tripped, or -- when no step
  * runs (status set, step >= step_end) -- a copy of src, so a queue of calls
  * alternating two buffers always leaves the walkers in the last call's dst.
- * ctrl->step tells how far a launch got.  Scratch:
+ * ctrl->step tells how far a launch got (a launch runs at most 2^30 / blocks
+ * steps: the barrier counter is 32 bits).  Scratch:
  * gbdmc_sim_run_scratch_bytes(), zeroed before the first call (the kernel
  * leaves it zeroed).  Returns GBDMC_ERR_CAPACITY, before any launch, when the
  * per-block buffers of sim->n0 walkers do not fit shared memory. */

@@ -87,11 +87,13 @@ def test_training_gradients_match_oracle():
     kernels' arithmetic (bf16 GEMM operands, fp32 buffers and accumulation).
     What remains is the fp32 summation order of the tensor cores and the
     atomics (and expf's last bits, which move a few bf16 roundings by one
-    step): measured about 1e-5 of the gradient norm, where the sums cancel,
-    and far less of the summed terms' magnitudes, the scale of an fp32
-    summation error.  The fp64 gradients without the rounding are only a
-    bf16-sized match, and a planted mistake in the oracle (descriptor columns
-    3 and 4 swapped) is far outside the bars."""
+    step): about 1e-5 of the gradient norm, where the sums cancel, and less
+    of the summed terms' magnitudes, the scale of an fp32 summation error.
+    Measured on a GB300: at most 4.2e-5 of the norm (layer 1, whose gradients
+    collect the flips of all later layers) and 9.5e-6 of the magnitudes.  The
+    fp64 gradients without the rounding are only a bf16-sized match, and a
+    planted mistake in the oracle (descriptor columns 3 and 4 swapped) is far
+    outside the bars."""
     m, x, xs, v, g = _small_model(1)
     P0 = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
     torch.manual_seed(0)
@@ -116,8 +118,8 @@ def test_training_gradients_match_oracle():
     Gt, _, Gm = mo.mlp_loss_grads_bf16(P0, D, U, e, et, 1.0, 0.5, magnitudes=True)
     rel, mag = errors(dict(Gt)), errors(dict(Gt), Gm)
     print("relative to the gradient norm:", rel, "\nrelative to the summed magnitudes:", mag)
-    assert max(rel.values()) < 5e-5, rel
-    assert max(mag.values()) < 1e-5, mag
+    assert max(rel.values()) < 1e-4, rel
+    assert max(mag.values()) < 2e-5, mag
     loose = errors(mo.mlp_loss_grads(dict(P0, b4=0.0), D, U, e, et, 1.0, 0.5)[0])
     assert max(loose.values()) < 5e-2, loose
     Dp = D.copy()
