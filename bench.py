@@ -607,7 +607,10 @@ def run_extras(steps):
 
 
 DIMER_TAU = 60000.0  # imaginary time of every run of the spec comparison (a.u.)
-DIMER_DTS = (10.0, 5.0)
+# dt and dt/2 of the extrapolation.  Both walks' time-step errors bend between
+# dt = 10 and 5 (plain and importance-sampled, measured at 10, 5 and 2.5), so
+# the straight line runs through 5 and 2.5, where they are close to linear.
+DIMER_DTS = (5.0, 2.5)
 
 
 def zpe_estimate(vref_series_cm):
@@ -685,8 +688,8 @@ def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
     accelerations (importance sampling with the fitted dimer trial, the tcgen05
     surrogate PES, 64 batched replicas with N_r ~ U[1000, 65536]) against the
     plain FP64 GPU path (200000 walkers, one replica, several seeds), at equal
-    ZPE error including the time-step error: every method runs at dt = 10 and
-    5 for the same imaginary time, its ZPE is extrapolated to dt -> 0 and its
+    ZPE error including the time-step error: every method runs at dt = 5 and
+    2.5 for the same imaginary time, its ZPE is extrapolated to dt -> 0 and its
     efficiency is 1 / (sigma0^2 x seconds) (zpe_estimate, extrapolate).  The
     FP64 importance-sampled path with the same trial (100000 walkers) pins
     the surrogate's accuracy at each dt; profiles/dimer_fp64_oracle.json holds
@@ -696,7 +699,7 @@ def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
     import pyvibdmc_gb300 as pg
     conv = lambda v: pg.Constants.convert(v, "wavenumbers", to_AU=False)  # noqa: E731
     res = {"estimator": "mean of the last 3/4 of the vref series (N0-weighted over replicas), blocking error of "
-                        "30 block means; dt -> 0 from dt = 10 and 5 (E0 = 2 E5 - E10)",
+                        "30 block means; dt -> 0 from dt = 5 and 2.5 (E0 = 2 E2.5 - E5)",
            "trial": {"alpha": trial.alpha, "qe": trial.qe}}
 
     def fp64(n, imp, seed, dt):
@@ -786,14 +789,14 @@ def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
                                   "sample": "oracle restatement of DMC_Sim.propagate (plain, discrete), "
                                             "20000 dimer walkers, numpy; best of 1 process and a "
                                             f"{cores}-process PES pool"}
-    plain_rate = res["plain_fp64_200k"]["dt10"]["walker_steps_per_s"]
+    plain_rate = res["plain_fp64_200k"][f"dt{DIMER_DTS[0]:g}"]["walker_steps_per_s"]
     res["gain_vs_cpu_reference_at_equal_error"] = res["gain_vs_plain_fp64_at_equal_error"] * plain_rate / cpu
     return res
 
 
 def dimer_oracle(plain_seeds=tuple(range(101, 165))):
     """A long plain FP64 extrapolation of the water dimer's ZPE (200000 walkers,
-    64 seeds at dt = 10 and 5): the value profiles/dimer_fp64_oracle.json keeps
+    64 seeds at dt = 5 and 2.5): the value profiles/dimer_fp64_oracle.json keeps
     for the spec comparison."""
     import torch
     import pyvibdmc_gb300 as pg

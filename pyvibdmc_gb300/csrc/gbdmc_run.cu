@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
   double* vs = xsb + (size_t)nbuf * 3 * A * capc;     // [capc]
   int* whob = reinterpret_cast<int*>(vs + capc);      // [nbuf][capc]
   int* cnt = whob + (size_t)nbuf * capc;              // [capc]
+  int* src = cnt + capc;                              // [capc] the run's walker i is slot src[i] of its buffer
   __shared__ long long s_base, s_nc, s_nnew, s_N;
   __shared__ double s_vref;
   __shared__ int s_stop;  // 0 go on, 1 branch to the output and end, 2 guards tripped
@@ -221,8 +222,9 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       if (track) out.who[g] = in.who[g];
     }
   } else {
-    int cur = 0;
-    unsigned nbar = 0;  // grid barriers passed: every CTA takes the same ones (the same decisions)
+    int rd = 0;          // the buffer holding the CTA's run
+    bool gather = false;  // its walker i is slot src[i] (the copies of the last step) or slot i
+    unsigned nbar = 0;    // grid barriers passed: every CTA takes the same ones (the same decisions)
     // the CTA's even share of the compact input
     for (int i = threadIdx.x; i < s_nc; i += kRunTPB) {
       const int64_t g = s_base + i;
@@ -234,8 +236,13 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
     for (unsigned t = 0;; ++t, ++step) {
       const long long base = s_base, nc = s_nc, N = s_N;
       const double vref = s_vref;
-      double* xs = xsb + (size_t)cur * 3 * A * capc;
-      int* whos = whob + (size_t)cur * capc;
+      // the moved walkers go to the other buffer (in place with one buffer, where
+      // every step starts from an even share, gather false)
+      const int wr = R.dbuf ? rd ^ 1 : rd;
+      const double* xr = xsb + (size_t)rd * 3 * A * capc;
+      double* xs = xsb + (size_t)wr * 3 * A * capc;
+      const int* whor = whob + (size_t)rd * capc;
+      int* whos = whob + (size_t)wr * capc;
       // 1. move, potential, weight, count
       int csum = 0, flag = 0;
       long long births = 0, deaths = 0;
@@ -243,13 +250,15 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       RunStats st = {0.0, INFINITY, -INFINITY, 0.0};
       for (int i = threadIdx.x; i < nc; i += kRunTPB) {
         double x[3 * A], z[3 * A], g[3 * A];
+        const int j = gather ? (int)GBDMC_BC(src[i], 0, capc, kBcRunShared) : i;
         Rng rng(S.seed, (uint64_t)step, (uint64_t)(base + i), S.replica_id);
         gen_normals<NM, 3 * A>(rng, z);
 #pragma unroll
         for (int k = 0; k < 3 * A; ++k) {
-          x[k] = __dadd_rn(xs[k * capc + i], __dmul_rn(S.sigma[k / 3], z[k]));
+          x[k] = __dadd_rn(xr[k * capc + j], __dmul_rn(S.sigma[k / 3], z[k]));
           xs[k * capc + i] = x[k];
         }
+        if (track) whos[i] = whor[j];
         const double v = pes<PK, A, false>(x, S.pes, g);
         vs[i] = v;
         if (STATS) {
@@ -290,16 +299,25 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         unsigned f = 0;
         double q0 = 0.0;
         RunStats qs = {0.0, INFINITY, -INFINITY, 0.0};
-        for (int g = lane; g < G; g += 32) {
-          const int4 r = __ldcg(reinterpret_cast<const int4*>(R.part + par * G + g));
+        // all of the lane's partials are loaded before any is used: one L2 round trip
+        int4 rp[kRunMaxCTA / 32];
+#pragma unroll
+        for (int k = 0; k < kRunMaxCTA / 32; ++k) {
+          const int g = lane + 32 * k;
+          rp[k] = g < G ? __ldcg(reinterpret_cast<const int4*>(R.part + par * G + g)) : make_int4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int k = 0; k < kRunMaxCTA / 32; ++k) {
+          const int g = lane + 32 * k;
+          const int4 r = rp[k];  // zeros past G: they add nothing
           const int rc = r.x;
           nn += rc;
           nd += (int)((unsigned)r.y & 0xFFFFFFu);
           f |= (unsigned)r.y >> 24;
-          q0 += __hiloint2double(r.w, r.z);
+          if (g < G) q0 += __hiloint2double(r.w, r.z);  // the same additions in every CTA
           if (g < c) below += rc;
           cmax = rc > cmax ? rc : cmax;
-          if (STATS) {
+          if (STATS && g < G) {
             const double2 a = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g));
             const double2 b = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g) + 1);
             qs.s1 += a.x;
@@ -356,8 +374,10 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
           const long long even = (Nn + G - 1) / G;
           const int stop = st2 ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || even > capc) ? 1 : 0);
           s_stop = stop;
-          // the largest CTA's copies against the warps of an even split
-          const long long lim = ((even + 31) / 32) * 32;
+          // the largest CTA's copies against the warps of an even split plus one: a
+          // warp more costs the largest block ~4% of its move (the FP64 work is per
+          // walker), an even split through the output ~15% of a step
+          const long long lim = ((even + 31) / 32) * 32 + 32;
           s_even = !R.dbuf || (long long)cmax > (lim < capc ? lim : (long long)capc);
           if (c == 0) {
             if (st2) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
@@ -417,32 +437,32 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
           break;
         }
         const long long Nn = s_N, nbase = Nn * c / G, nnc = Nn * (c + 1) / G - nbase;
+        const int ld_buf = R.dbuf ? wr ^ 1 : wr;  // the moved walkers are in the output now
+        double* xl = xsb + (size_t)ld_buf * 3 * A * capc;
+        int* wl = whob + (size_t)ld_buf * capc;
         for (int i = threadIdx.x; i < nnc; i += kRunTPB) {
           const int64_t g = nbase + i;
           const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
 #pragma unroll
-          for (int k = 0; k < 3 * A; ++k) xs[k * capc + j] = __ldcg(out.x + k * ld + g);
-          whos[j] = track ? __ldcg(out.who + g) : 0;
+          for (int k = 0; k < 3 * A; ++k) xl[k * capc + j] = __ldcg(out.x + k * ld + g);
+          wl[j] = track ? __ldcg(out.who + g) : 0;
         }
+        rd = ld_buf;
+        gather = false;
         if (threadIdx.x == 0) {
           s_base = nbase;
           s_nc = nnc;
         }
       } else {
-        // into the other buffer: the CTA's next run is its copies, at logical base nb
-        double* xn = xsb + (size_t)(cur ^ 1) * 3 * A * capc;
-        int* wn = whob + (size_t)(cur ^ 1) * capc;
+        // the CTA's next run is its copies, at logical base nb: copy r of walker i
+        // is the next step's walker cnt[i] + r, read from slot i of this step's buffer
         for (int i = threadIdx.x; i < nc; i += kRunTPB) {
           const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
           const int j0 = cnt[i];
-          for (int r = 0; r < c0; ++r) {
-            const int j = (int)GBDMC_BC(j0 + r, 0, capc, kBcRunShared);
-#pragma unroll
-            for (int k = 0; k < 3 * A; ++k) xn[k * capc + j] = xs[k * capc + i];
-            wn[j] = whos[i];
-          }
+          for (int r = 0; r < c0; ++r) src[GBDMC_BC(j0 + r, 0, capc, kBcRunShared)] = i;
         }
-        cur ^= 1;
+        rd = wr;
+        gather = true;
         if (threadIdx.x == 0) {
           s_base = nb;
           s_nc = tot;
@@ -464,7 +484,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
 
 // ------------------------------------------------------------ host side
 static size_t run_smem_bytes(int A, int capc, int nbuf) {
-  return (size_t)capc * (nbuf * (3 * A * sizeof(double) + sizeof(int)) + sizeof(double) + sizeof(int));
+  return (size_t)capc * (nbuf * (3 * A * sizeof(double) + sizeof(int)) + sizeof(double) + 2 * sizeof(int));
 }
 
 struct RunShape {
