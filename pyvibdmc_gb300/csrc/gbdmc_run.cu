@@ -85,6 +85,30 @@ __device__ __forceinline__ bool run_barrier(unsigned* arrive, unsigned target) {
   return s_ok != 0;
 }
 
+// The two halves of the per-step barrier, apart so that a block's own work
+// (the scan of its counts) runs while the other blocks arrive.  Thread 0
+// arrives after writing the block's partial: the release orders that write
+// before the arrival.  run_wait: bounded, false when the wait ran out.
+__device__ __forceinline__ void run_arrive(unsigned* arrive) { red_release_add(arrive, 1u); }
+
+__device__ __forceinline__ bool run_wait(const unsigned* arrive, unsigned target) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned it = 0;
+    while (ld_acquire(arrive) < target) {
+      if (++it > kRunSpinLimit) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Exclusive scan of cnt[0..n) in place (chunks of the block), returns the total.
 __device__ __forceinline__ int run_scan(int* cnt, int n) {
   __shared__ int ws[kRunTPB / 32];
@@ -282,9 +306,22 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         q.s0 = s0;
         R.part[par * G + c] = q;
         if (STATS) R.stat[par * G + c] = st;
+        run_arrive(R.sync);
+      }
+      // while the others arrive: the exclusive scan of the block's counts and the
+      // gather index of its copies (copy r of walker i is the block's next walker
+      // cnt[i] + r, read from slot i of this step's buffer), used if the step keeps
+      // its copies in the block
+      const int tot = run_scan(cnt, (int)nc);
+      if (R.dbuf) {
+        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
+          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
+          const int j0 = cnt[i];
+          for (int r = 0; r < c0; ++r) src[GBDMC_BC(j0 + r, 0, capc, kBcRunShared)] = i;
+        }
       }
       // 2. every CTA's partial
-      if (!run_barrier(R.sync, (unsigned)G * ++nbar)) {
+      if (!run_wait(R.sync, (unsigned)G * ++nbar)) {
         if (threadIdx.x == 0) {
           atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
           ctrl->err_step = (int)step;
@@ -294,17 +331,20 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
       // 3. the same reduction in every CTA, in warp 0: lane l takes CTAs l, l + 32, ...
       if (threadIdx.x < 32) {
         const unsigned full = 0xffffffffu;
-        long long nn = 0, below = 0;  // 64-bit: a collapsing step's counts may pass 2^31
+        unsigned nn = 0, below = 0;
         int nd = 0, cmax = 0;
         unsigned f = 0;
         double q0 = 0.0;
         RunStats qs = {0.0, INFINITY, -INFINITY, 0.0};
-        // all of the lane's partials are loaded before any is used: one L2 round trip
+        // all of the lane's partials are loaded before any is used: one L2 round
+        // trip (predicated: every block reads every partial once, so that no L2
+        // line is hit by more requests than there are blocks)
         int4 rp[kRunMaxCTA / 32];
+        const int4* pp = reinterpret_cast<const int4*>(R.part + par * G);
 #pragma unroll
         for (int k = 0; k < kRunMaxCTA / 32; ++k) {
           const int g = lane + 32 * k;
-          rp[k] = g < G ? __ldcg(reinterpret_cast<const int4*>(R.part + par * G + g)) : make_int4(0, 0, 0, 0);
+          rp[k] = g < G ? __ldcg(pp + g) : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int k = 0; k < kRunMaxCTA / 32; ++k) {
@@ -331,17 +371,17 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
           qs.vmin = dkey_inv(warp_min_key(dkey(qs.vmin)));
           qs.vmax = dkey_inv(warp_max_key(dkey(qs.vmax)));
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          nn += __shfl_xor_sync(full, nn, o);
-          below += __shfl_xor_sync(full, below, o);
-        }
+        nn = __reduce_add_sync(full, nn);
+        below = __reduce_add_sync(full, below);
         nd = (int)__reduce_add_sync(full, (unsigned)nd);
         cmax = (int)__reduce_max_sync(full, (unsigned)cmax);
         f = __reduce_or_sync(full, f);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) q0 += __shfl_xor_sync(full, q0, o);
-        const long long Nn = nn;
+        // 32-bit sums: exact while every block holds fewer than 2^31 / kRunMaxCTA
+        // copies; a larger block count is a population past any guard (N' > 1.5 N0)
+        const bool huge = cmax >= (int)(0x7fffffff / kRunMaxCTA);
+        const long long Nn = huge ? (long long)INT32_MAX * 4 : (long long)nn;
         // the step's divisions, one SIMT division: <V> of the branched population
         // (lane 0), the population term (lane 1), the mean potential (lane 2)
         const double num = lane == 0 ? q0 : (lane == 1 ? (double)(Nn - N0) : qs.s1);
@@ -371,7 +411,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
               if (S.hist.deaths) S.hist.deaths[h] = nd;
             }
           }
-          const long long even = (Nn + G - 1) / G;
+          const long long even = huge ? (long long)INT32_MAX : (long long)((nn + (unsigned)G - 1u) / (unsigned)G);
           const int stop = st2 ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || even > capc) ? 1 : 0);
           s_stop = stop;
           // the largest CTA's copies against the warps of an even split plus one: a
@@ -411,7 +451,6 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
         break;
       }
       // 4. branch: the CTA's copies in np.repeat order
-      const int tot = run_scan(cnt, (int)nc);
       const long long nb = s_nnew;
       if (stop || s_even) {
         // into the output at their logical positions: the whole population compact in logical order
@@ -454,13 +493,7 @@ __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_s
           s_nc = nnc;
         }
       } else {
-        // the CTA's next run is its copies, at logical base nb: copy r of walker i
-        // is the next step's walker cnt[i] + r, read from slot i of this step's buffer
-        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
-          const int j0 = cnt[i];
-          for (int r = 0; r < c0; ++r) src[GBDMC_BC(j0 + r, 0, capc, kBcRunShared)] = i;
-        }
+        // the CTA's next run is its copies (their gather index is written), at logical base nb
         rd = wr;
         gather = true;
         if (threadIdx.x == 0) {
