@@ -257,7 +257,7 @@ def run_ours(args):
     sim._init_device()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     ctrl_ptr = C.c_void_p(sim._ctrl.data_ptr())
-    run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(), dtype=torch.uint8, device=dev)
+    run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(sim.capacity), dtype=torch.uint8, device=dev)
     desc = torch.zeros(int(sim.capacity), dtype=torch.float64, device=dev)
     evs = []
 

@@ -117,6 +117,9 @@ typedef struct {
   double* ke;   /* [ld] local kinetic energy (importance sampling)          */
   double* w;    /* [ld] continuous weights, or NULL                         */
   int32_t* idx; /* [ld] gather index of the logical walkers, or NULL        */
+  uint64_t* key; /* [ld] lineage keys of gbdmc_sim_run's Philox streams, or
+                    NULL (then a launch takes the logical indices); read at a
+                    launch's start and written with its output            */
 } gbdmc_walkers_t;
 
 /* device-resident control block (caller allocates sizeof(gbdmc_ctrl_t)) */
@@ -230,25 +233,38 @@ int gbdmc_sim_step(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbd
  * step_end: the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two
  * events, for discrete weighting, Philox deviates and a built-in potential.
  * Each block holds a run of the population (in logical order) in shared
- * memory; one grid barrier per step exchanges the blocks' sums (vref, N' and
- * every block's count).  A block's copies stay in its shared memory, except
- * when the largest block's copies would take more warps than an even split
- * (or two buffers per block do not fit): then the branched population goes
- * through dst (compact, logical order) and a second grid barrier lets every
- * block load its even share.  Waits are bounded (GBDMC_ST_TIMEOUT on expiry).
- * The deviates and branching uniforms are those of
- * gbdmc_sim_step, so the trajectory is gbdmc_sim_step's (vref sums in another
- * order, last bits).  src holds the ctrl->n compact walkers (idx NULL); dst
- * receives the compact walkers after the last step run (x, v, who), or the
- * moved unbranched walkers of a step whose guards tripped, or -- when no step
- * runs (status set, step >= step_end) -- a copy of src, so a queue of calls
- * alternating two buffers always leaves the walkers in the last call's dst.
- * ctrl->step tells how far a launch got (a launch runs at most 2^30 / blocks
- * steps: the barrier counter is 32 bits).  Scratch:
- * gbdmc_sim_run_scratch_bytes(), zeroed before the first call (the kernel
- * leaves it zeroed).  Returns GBDMC_ERR_CAPACITY, before any launch, when the
- * per-block buffers of sim->n0 walkers do not fit shared memory. */
-size_t gbdmc_sim_run_scratch_bytes(void);
+ * memory and keeps its walkers' copies there; a reducer warp per block
+ * exchanges the blocks' sums of a step (vref, N', every block's count)
+ * through one grid barrier while the block's other warps move the next step.
+ * When the largest block's run would take more warps than an even split plus
+ * one, or a block's copies do not fit its buffer, the walkers are split
+ * evenly again through dst and a second grid barrier.  Waits are bounded
+ * (GBDMC_ST_TIMEOUT on expiry).
+ * The algorithm is gbdmc_sim_step's; the noise differs: a walker draws its
+ * deviates and branching uniform from the Philox stream of its lineage key
+ * (src->key, or its logical index when src->key is NULL; copy 0 keeps its
+ * parent's key, copy r >= 1 of a walker with key k branching at step s takes
+ * the SplitMix64 finaliser of k + r * 0x9E3779B97F4A7C15 + s *
+ * 0xD1B54A32D192ED03), not of its logical index at every step; dst->key
+ * (when not NULL) receives the keys with the walkers, so a walk split over
+ * several launches is the walk of one.  src holds the ctrl->n compact walkers (idx NULL);
+ * dst receives the compact walkers after the last step run (x, v, who), or
+ * the moved unbranched walkers of a step whose guards tripped, or -- when no
+ * step runs (status set, step >= step_end) -- a copy of src, so a queue of
+ * calls alternating two buffers always leaves the walkers in the last call's
+ * dst.  ctrl->step tells how far a launch got (a launch runs at most 2^30 /
+ * blocks steps).  Scratch: gbdmc_sim_run_scratch_bytes(sim->ld), zeroed before
+ * the first call (the kernel leaves its barrier words zeroed).  Returns
+ * GBDMC_ERR_CAPACITY, before any launch, when the per-block buffers of
+ * sim->n0 walkers do not fit shared memory. */
+size_t gbdmc_sim_run_scratch_bytes(int64_t ld);
+/* The multi-step kernel's noise of n walkers with lineage keys keys_dev at
+ * step `step` (sim's seed, replica_id and noise mode, which must be a Philox
+ * mode; 1, 3 or 6 atoms): normal_dev [3A][ld_noise] and u_dev [n], in the
+ * layout of gbdmc_noise_t, so that gbdmc_sim_step on this injected noise
+ * follows gbdmc_sim_run's walk step by step. */
+int gbdmc_lineage_noise(const gbdmc_sim_t* sim, const uint64_t* keys_dev, int64_t n, int64_t step,
+                        double* normal_dev, int64_t ld_noise, double* u_dev, void* stream);
 int gbdmc_sim_run(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
                   gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, int64_t step_end, int32_t max_steps, void* stream);
 

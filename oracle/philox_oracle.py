@@ -25,7 +25,7 @@ use a relative tolerance of a few fp32 ulps; the Philox words are exact.
 """
 import numpy as np
 
-__all__ = ["philox4x32_10", "PhiloxStream", "philox_normals", "philox_branch_uniform"]
+__all__ = ["philox4x32_10", "PhiloxStream", "philox_normals", "philox_branch_uniform", "lineage_key"]
 
 _M32 = np.uint64(0xFFFFFFFF)
 
@@ -49,24 +49,32 @@ def philox4x32_10(c0, c1, c2, c3, k0, k1):
 
 
 class PhiloxStream:
-    """The 32-bit draws of walkers ``walkers`` at step ``step`` (vectorised)."""
+    """The 32-bit draws of walkers ``walkers`` at step ``step`` (vectorised).
+    With ``lineage`` the walkers are 64-bit lineage keys (the multi-step
+    kernel's streams): counter = (key low word, key high word, step low word,
+    slot | replica << 8 | 1 << 31)."""
 
-    def __init__(self, seed, step, walkers, replica=0):
+    def __init__(self, seed, step, walkers, replica=0, lineage=False):
         self.k0 = int(seed) & 0xFFFFFFFF
         self.k1 = (int(seed) >> 32) & 0xFFFFFFFF
         self.i = np.asarray(walkers, dtype=np.uint64)
         self.s_lo = int(step) & 0xFFFFFFFF
         self.s_hi = (int(step) >> 32) & 0xFFFFFFFF
         self.rep = int(replica)
+        self.lineage = bool(lineage)
         self.slot = 0
         self.buf = None
         self.used = 4
 
     def _block(self):
         n = self.i.shape
-        c = philox4x32_10(self.i, np.full(n, self.s_lo, np.uint64),
-                          np.full(n, self.slot | (self.rep << 8), np.uint64),
-                          np.full(n, self.s_hi, np.uint64) ^ (self.i >> np.uint64(31)), self.k0, self.k1)
+        if self.lineage:
+            c = philox4x32_10(self.i & _M32, self.i >> np.uint64(32), np.full(n, self.s_lo, np.uint64),
+                              np.full(n, self.slot | (self.rep << 8) | 0x80000000, np.uint64), self.k0, self.k1)
+        else:
+            c = philox4x32_10(self.i, np.full(n, self.s_lo, np.uint64),
+                              np.full(n, self.slot | (self.rep << 8), np.uint64),
+                              np.full(n, self.s_hi, np.uint64) ^ (self.i >> np.uint64(31)), self.k0, self.k1)
         self.slot += 1
         return c
 
@@ -100,10 +108,10 @@ class PhiloxStream:
         return rad * np.cos(ang), rad * np.sin(ang)
 
 
-def philox_normals(seed, step, walkers, ncoord, mode="philox32", replica=0):
+def philox_normals(seed, step, walkers, ncoord, mode="philox32", replica=0, lineage=False):
     """(ncoord, len(walkers)) normals as the move kernel draws them, plus the stream
     positioned for the branch uniform."""
-    st = PhiloxStream(seed, step, walkers, replica)
+    st = PhiloxStream(seed, step, walkers, replica, lineage)
     out = np.empty((ncoord, len(st.i)), dtype=np.float64)
     for k in range(0, ncoord, 2):
         a, b = st.normal2_f32() if mode == "philox32" else st.normal2_f64()
@@ -117,3 +125,20 @@ def philox_branch_uniform(seed, step, walkers, ncoord, mode="philox32", replica=
     """The branching uniform of each walker: the draw after its ncoord normals."""
     _, st = philox_normals(seed, step, walkers, ncoord, mode, replica)
     return st.uniform53()
+
+
+def lineage_key(k, r, step):
+    """Lineage keys of the multi-step kernel's walkers: copy r of a walker with
+    key k, branching at step ``step``, keeps k for r = 0 and takes the
+    SplitMix64 finaliser (Steele, Lea, Flood 2014; Vigna's constants) of
+    k + r * 0x9E3779B97F4A7C15 + step * 0xD1B54A32D192ED03 for r >= 1 (uint64
+    arrays, wrapping arithmetic)."""
+    k = np.asarray(k, dtype=np.uint64)
+    r = np.asarray(r, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = k + r * np.uint64(0x9E3779B97F4A7C15) + np.uint64(int(step) & 0xFFFFFFFFFFFFFFFF) * \
+            np.uint64(0xD1B54A32D192ED03)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return np.where(r == 0, k, z)

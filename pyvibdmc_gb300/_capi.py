@@ -29,7 +29,8 @@ class Trial(C.Structure):
 
 class Walkers(C.Structure):
     _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("f", C.c_void_p),
-                ("psi", C.c_void_p), ("ke", C.c_void_p), ("w", C.c_void_p), ("idx", C.c_void_p)]
+                ("psi", C.c_void_p), ("ke", C.c_void_p), ("w", C.c_void_p), ("idx", C.c_void_p),
+                ("key", C.c_void_p)]
 
 
 class Ctrl(C.Structure):
@@ -112,7 +113,8 @@ def load():
         "gbdmc_sim_init": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, P], C.c_int),
         "gbdmc_sim_step": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P,
                             C.POINTER(Noise), P], C.c_int),
-        "gbdmc_sim_run_scratch_bytes": ([], C.c_size_t),
+        "gbdmc_sim_run_scratch_bytes": ([C.c_int64], C.c_size_t),
+        "gbdmc_lineage_noise": ([C.POINTER(Sim), P, C.c_int64, C.c_int64, P, C.c_int64, P, P], C.c_int),
         "gbdmc_sim_run": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.c_int64, C.c_int32, P],
                           C.c_int),
         "gbdmc_sim_move": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.POINTER(Noise), P],

@@ -33,17 +33,27 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
-// Counter layout: (walker index, step low word, stream slot | replica << 8, step high word).
-struct Rng {
-  uint32_t k0, k1, i, s_lo, s_hi, rep;
+// Counter layouts.  Index streams (LIN false): (walker index, step low word,
+// stream slot | replica << 8, step high word).  Lineage streams (LIN true, the
+// multi-step kernel, whose walkers are named by a 64-bit lineage key instead
+// of their position): (key low word, key high word, step low word, stream slot
+// | replica << 8 | 1 << 31); the top bit keeps the two kinds of counters apart
+// (replica ids stay below 2^23).
+template <bool LIN>
+struct RngT {
+  uint32_t k0, k1, i, s_lo, s_hi, rep;  // LIN: i, s_hi = the lineage key's low and high words
   uint32_t slot;
   U4 buf;
   int used;
-  __device__ Rng(uint64_t seed, uint64_t step, uint64_t walker, uint32_t replica = 0)
-      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), i((uint32_t)walker),
-        s_lo((uint32_t)step), s_hi((uint32_t)(step >> 32)), rep(replica), slot(0), used(4) {}
+  __device__ RngT(uint64_t seed, uint64_t step, uint64_t walker, uint32_t replica = 0)
+      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), i((uint32_t)walker), s_lo((uint32_t)step),
+        s_hi(LIN ? (uint32_t)(walker >> 32) : (uint32_t)(step >> 32)), rep(replica), slot(0), used(4) {}
   __device__ __forceinline__ U4 block() {
-    U4 c{i, s_lo, slot | (rep << 8), s_hi ^ (uint32_t)(i >> 31)};
+    U4 c;
+    if constexpr (LIN)
+      c = U4{i, s_hi, s_lo, slot | (rep << 8) | 0x80000000u};
+    else
+      c = U4{i, s_lo, slot | (rep << 8), s_hi ^ (uint32_t)(i >> 31)};
     ++slot;
     return philox4x32_10(c, k0, k1);
   }
@@ -112,6 +122,22 @@ struct Rng {
     z1 = rad * s;
   }
 };
+using Rng = RngT<false>;
+using RngL = RngT<true>;
+
+// The lineage key of copy r of a walker with key k, made at step `step`:
+// copy 0 keeps k, copy r >= 1 takes the SplitMix64 finaliser (Steele, Lea,
+// Flood 2014; Vigna's constants) of k + r * 0x9E3779B97F4A7C15 + step *
+// 0xD1B54A32D192ED03.  The step keeps a walker that branches at two steps
+// from giving two children the same key; every walker's key stays distinct
+// (up to 64-bit collisions).
+__host__ __device__ __forceinline__ uint64_t lineage_key(uint64_t k, int r, uint64_t step) {
+  if (r == 0) return k;
+  uint64_t z = k + (uint64_t)r * 0x9E3779B97F4A7C15ull + step * 0xD1B54A32D192ED03ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
 
 // fp64 -> fp32 with round-to-nearest-even on the integer pipes only (the
 // fp64 pipe runs a conversion at about the cost of two FMAs per warp).  Equal
@@ -178,8 +204,8 @@ __device__ __forceinline__ double widen_f32(float f) {
 }
 
 // Fill z[0..n) with standard normals for the chosen noise mode.
-template <int NM, int N>
-__device__ __forceinline__ void gen_normals(Rng& g, double (&z)[N]) {
+template <int NM, int N, class G>
+__device__ __forceinline__ void gen_normals(G& g, double (&z)[N]) {
   if constexpr (NM == GBDMC_NOISE_PHILOX32) {
 #pragma unroll
     for (int k = 0; k < N; k += 2) {

@@ -1,33 +1,39 @@
 // Many plain-DMC steps (discrete weighting, Philox deviates) in one launch:
 // the loop of DMC_Sim.propagate (pyvibdmc.py:710-876) between two events.
 //
-// The walkers of a step live in shared memory.  CTA c of a cooperative grid
-// of G CTAs holds a run [base_c, base_c + n_c) of the population in its
-// logical (np.repeat) order, the runs of the CTAs back to back.  One step:
-//   1. every walker of the CTA moves (x + fl(sigma z) from Philox, keyed by
-//      its logical index base_c + i as in k_move), its potential, weight and
-//      count (pyvibdmc.py:540-547, :392-403); the CTA's 16-byte partial (sum
-//      c, sum cV, deaths, guards; sum V / min / max when logging apart) goes
-//      to global memory;
-//   2. a grid barrier (bounded wait, GBDMC_ST_TIMEOUT on expiry);
-//   3. warp 0 of every CTA reduces the G partials in the same fixed order, so
-//      all CTAs hold the same N', vref' (calc_vref, :651-661), guards and
-//      largest CTA count, and the CTA's new base is the earlier CTAs' counts;
-//   4. the CTA's copies (np.repeat order) become its next run.  Normally they
-//      stay in shared memory (the other half of a double buffer).  When the
-//      largest CTA's copies would take more warps than an even split of N'
-//      (or no double buffer fits), every CTA writes its copies to the output
-//      at their logical positions, a second grid barrier follows, and every
-//      CTA loads its even share of the new population back: the step's time
-//      is that of the CTA with the most walkers, so the runs are split evenly
-//      again before one of them grows by a warp.
-// After the last step of the launch the copies go to the output, which then
-// holds the branched population compact in logical order.  A step whose
-// guards trip writes its moved, unbranched walkers to the output and stops,
-// as the per-step kernels do.
-// The deviates and branching uniforms are those of the per-step kernels
-// (same Philox counters), so the trajectories agree; vref sums the CTA
-// partials in another order (last-bit differences).
+// The walkers live in shared memory.  CTA c of a cooperative grid of G CTAs
+// holds a run [base_c, base_c + n_c) of the population in its logical
+// (np.repeat) order.  A CTA is six mover warps and one reducer warp:
+//   movers, step t:  move every walker of the run and evaluate V (the walker
+//     draws from the Philox stream of its 64-bit lineage key, so nothing in
+//     the move depends on other CTAs); barrier A with the reducer, which has
+//     by then published step t-1's global results (vref_t, N_t, this CTA's
+//     logical base, what to do next); weights and counts with vref_t; barrier
+//     B (the CTA's per-thread sums handed to the reducer); scan of the counts
+//     and the copies' gather index and lineage keys (copy r of walker i is the
+//     next run's walker cnt[i] + r with key lineage_key(key_i, r, step)).
+//   reducer, after barrier B of step t (while the movers move step t+1):
+//     the CTA's sums into a 16-byte partial, grid arrival, wait for all G
+//     arrivals (bounded), all partials reduced in the same fixed order in
+//     every CTA (N', vref, guards, the largest CTA count, this CTA's base),
+//     the history and control block (CTA 0), the next action; barrier A.
+// So the grid-wide reduction of a step runs behind the next step's move.
+// The action after step t, the same in every CTA:
+//   go on with the copies where they are;
+//   exchange: the largest CTA's run would take more warps than an even split
+//     plus one, so the moved walkers of step t+1 are split evenly through
+//     global memory (second grid barrier) before their weights;
+//   overflow: a CTA's copies did not fit its buffer: step t's copies are split
+//     evenly through global memory and step t+1 is moved again (the lineage
+//     keys make the walk independent of where a walker is moved);
+//   stop: the launch's last step, or a population whose even split does not
+//     fit the buffers: step t's copies go to the output in logical order;
+//   guard: a guard tripped at step t: its moved, unbranched walkers go to the
+//     output, as the per-step kernels leave them.
+// The walk is the per-step kernels' algorithm with another noise stream: a
+// walker's deviates and branching uniform come from its lineage key (its
+// logical index at the launch's start) instead of its logical index at every
+// step.
 #include <cmath>
 #include <mutex>
 #include "gbdmc_device.cuh"
@@ -36,19 +42,32 @@
 
 namespace gbdmc {
 
-constexpr int kRunTPB = 192;
+constexpr int kRunMovers = 192;               // six mover warps
+constexpr int kRunTPB = kRunMovers + 32;      // and the reducer warp
 constexpr int kRunMaxCTA = 384;
 constexpr unsigned kRunSpinLimit = 1u << 22;
+constexpr unsigned kRunOverflowBit = 0x40u;   // a CTA's copies exceed its buffer (partial flag)
+
+enum RunAction { kRunGoOn = 0, kRunExchange = 1, kRunOverflow = 2, kRunStop = 3, kRunGuard = 4 };
 
 // A CTA's sums of one step: one 16-byte load per CTA in the reduction.
 struct RunPart {
   int c;         // sum of the branch counts (the CTA's copies)
-  unsigned df;   // deaths | guard bits << 24 (a CTA holds fewer than 2^24 walkers)
+  unsigned df;   // deaths | flags << 24 (a CTA holds fewer than 2^24 walkers)
   double s0;     // sum of c V
 };
 static_assert(sizeof(RunPart) == 16, "RunPart is 16 bytes");
 struct RunStats {  // only when the potential statistics are logged
   double s1, vmin, vmax, pad;
+};
+
+// A step's global results as the movers use them (published by the reducer).
+struct RunRes {
+  long long n;      // the population after the step (N')
+  long long below;  // this CTA's logical base of its copies: the earlier CTAs' counts
+  double vref;      // vref after the step
+  int action;       // RunAction
+  int pad;
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -61,73 +80,52 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
 
-// Grid barrier over a monotonic arrival counter: the CTA's writes are released
-// by thread 0's arrival after the block barrier, the others' acquired by its
-// wait before the next one.  Returns false if the wait ran out (the caller
-// stops; the other CTAs' next waits run out as well).
-__device__ __forceinline__ bool run_barrier(unsigned* arrive, unsigned target) {
+// Bounded wait of one thread for a monotonic arrival counter to reach target.
+__device__ __forceinline__ bool run_poll(const unsigned* arrive, unsigned target) {
+  unsigned it = 0;
+  while (ld_acquire(arrive) < target) {
+    if (++it > kRunSpinLimit) return false;
+    __nanosleep(32);
+  }
+  return true;
+}
+
+// Named barriers: all 224 threads (movers and reducer), the 192 movers.
+__device__ __forceinline__ void bar_all() { asm volatile("bar.sync 1, 224;" ::: "memory"); }
+__device__ __forceinline__ void bar_mov() { asm volatile("bar.sync 2, 192;" ::: "memory"); }
+
+// Grid barrier of the movers (the exchanges): their writes released by thread
+// 0's arrival after the movers' barrier, the others' acquired by its wait.
+__device__ __forceinline__ bool mov_grid_barrier(unsigned* arrive, unsigned target) {
   __shared__ int s_ok;
-  __syncthreads();
+  bar_mov();
   if (threadIdx.x == 0) {
     red_release_add(arrive, 1u);
-    int ok = 1;
-    unsigned it = 0;
-    while (ld_acquire(arrive) < target) {
-      if (++it > kRunSpinLimit) {
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
-    }
-    s_ok = ok;
+    s_ok = run_poll(arrive, target) ? 1 : 0;
   }
-  __syncthreads();
+  bar_mov();
   return s_ok != 0;
 }
 
-// The two halves of the per-step barrier, apart so that a block's own work
-// (the scan of its counts) runs while the other blocks arrive.  Thread 0
-// arrives after writing the block's partial: the release orders that write
-// before the arrival.  run_wait: bounded, false when the wait ran out.
-__device__ __forceinline__ void run_arrive(unsigned* arrive) { red_release_add(arrive, 1u); }
-
-__device__ __forceinline__ bool run_wait(const unsigned* arrive, unsigned target) {
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    unsigned it = 0;
-    while (ld_acquire(arrive) < target) {
-      if (++it > kRunSpinLimit) {
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
-// Exclusive scan of cnt[0..n) in place (chunks of the block), returns the total.
-__device__ __forceinline__ int run_scan(int* cnt, int n) {
-  __shared__ int ws[kRunTPB / 32];
+// Exclusive scan of cnt[0..n) in place by the movers, returns the total.
+__device__ __forceinline__ int mov_scan(int* cnt, int n) {
+  __shared__ int ws[kRunMovers / 32];
   __shared__ int s_run;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_run = 0;
-  __syncthreads();
-  for (int b = 0; b < n; b += kRunTPB) {
+  bar_mov();
+  for (int b = 0; b < n; b += kRunMovers) {
     const int i = b + threadIdx.x;
     const int c = i < n ? cnt[i] : 0;
     const int inc = warp_incl_scan(c);
     if (lane == 31) ws[wid] = inc;
-    __syncthreads();
+    bar_mov();
     int off = s_run;
     for (int w = 0; w < wid; ++w) off += ws[w];
     if (i < n) cnt[i] = off + inc - c;
-    __syncthreads();
-    if (threadIdx.x == kRunTPB - 1) s_run = off + inc;
-    __syncthreads();
+    bar_mov();
+    if (threadIdx.x == kRunMovers - 1) s_run = off + inc;
+    bar_mov();
   }
   return s_run;
 }
@@ -136,392 +134,514 @@ struct RunArgs {
   int64_t step_end;  // stop before this step
   int kmax;          // and after at most this many steps
   int capc;          // walkers per CTA buffer
-  int dbuf;          // 1: two walker buffers per CTA (copies stay in shared memory)
   RunPart* part;     // [2][G]
   RunStats* stat;    // [2][G]
-  unsigned* sync;    // [0] arrivals, [1] exits
+  uint64_t* gkey;    // [ld] lineage keys of the exchanges
+  uint64_t* gu;      // [ld] branching-uniform bits of the exchanges
+  unsigned* sync;    // [0] partial arrivals, [1] exits, [2] exchange arrivals
 };
 
-// The CTA's sums of step 1, reduced over the block: valid in thread 0.
-template <bool STATS>
-__device__ __forceinline__ void run_block_sums(int& c, int& d, unsigned& f, double& s0, RunStats& st) {
-  __shared__ int4 sh_i[kRunTPB / 32];
-  __shared__ double sh_d[kRunTPB / 32][4];
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  c = (int)__reduce_add_sync(full, (unsigned)c);
-  d = (int)__reduce_add_sync(full, (unsigned)d);
-  f = __reduce_or_sync(full, f);
-  if (STATS) {
-    warp_sum2(s0, st.s1);
-    st.vmin = dkey_inv(warp_min_key(dkey(st.vmin)));
-    st.vmax = dkey_inv(warp_max_key(dkey(st.vmax)));
-  } else {
-    s0 = warp_sum(s0);
-  }
-  if (lane == 0) {
-    sh_i[wid] = make_int4(c, d, (int)f, 0);
-    sh_d[wid][0] = s0;
-    if (STATS) {
-      sh_d[wid][1] = st.s1;
-      sh_d[wid][2] = st.vmin;
-      sh_d[wid][3] = st.vmax;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int4 a = sh_i[0];
-    s0 = sh_d[0][0];
-    if (STATS) {
-      st.s1 = sh_d[0][1];
-      st.vmin = sh_d[0][2];
-      st.vmax = sh_d[0][3];
-    }
-#pragma unroll
-    for (int w = 1; w < kRunTPB / 32; ++w) {
-      const int4 b = sh_i[w];
-      a.x += b.x;
-      a.y += b.y;
-      a.z |= b.z;
-      s0 += sh_d[w][0];
-      if (STATS) {
-        st.s1 += sh_d[w][1];
-        st.vmin = fmin(st.vmin, sh_d[w][2]);
-        st.vmax = fmax(st.vmax, sh_d[w][3]);
-      }
-    }
-    c = a.x;
-    d = a.y;
-    f = (unsigned)a.z;
-  }
-}
+// The CTA's shared walker state: buffer b of each double-buffered array is at
+// base + b * stride (arithmetic, so that no array of pointers sits in local memory).
+template <int A>
+struct RunSm {
+  double* x0;      // [2][3A][capc] coordinates (source / moved)
+  double* v0;      // [2][capc] V of the walkers moved into buffer b
+  uint64_t* key0;  // [2][capc] lineage keys: the run's, the next run's
+  uint64_t* u;     // [capc] the moved walkers' branching-uniform bits
+  int* who0;       // [2][capc] ancestor ids
+  int* cnt;        // [capc] counts, then their exclusive scan
+  int* src;        // [capc] the next run's walker i is the copy of slot src[i]
+  int capc;
+  __device__ __forceinline__ double* x(int b) const { return x0 + (size_t)b * 3 * A * capc; }
+  __device__ __forceinline__ double* v(int b) const { return v0 + (size_t)b * capc; }
+  __device__ __forceinline__ uint64_t* key(int b) const { return key0 + (size_t)b * capc; }
+  __device__ __forceinline__ int* who(int b) const { return who0 + (size_t)b * capc; }
+};
 
 template <int PK, int A, int NM, bool STATS>
 __global__ void __launch_bounds__(kRunTPB) k_run(const __grid_constant__ gbdmc_sim_t S, const gbdmc_walkers_t in,
                                                  gbdmc_walkers_t out, gbdmc_ctrl_t* ctrl, const RunArgs R) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int capc = R.capc, G = gridDim.x, c = blockIdx.x, nbuf = R.dbuf ? 2 : 1;
-  const int lane = threadIdx.x & 31;
-  double* xsb = reinterpret_cast<double*>(smem);     // [nbuf][3A][capc]
-  double* vs = xsb + (size_t)nbuf * 3 * A * capc;     // [capc]
-  int* whob = reinterpret_cast<int*>(vs + capc);      // [nbuf][capc]
-  int* cnt = whob + (size_t)nbuf * capc;              // [capc]
-  int* src = cnt + capc;                              // [capc] the run's walker i is slot src[i] of its buffer
-  __shared__ long long s_base, s_nc, s_nnew, s_N;
-  __shared__ double s_vref;
-  __shared__ int s_stop;  // 0 go on, 1 branch to the output and end, 2 guards tripped
-  __shared__ int s_even;  // 1: every CTA takes its even share of the new population
+  const int capc = R.capc, G = gridDim.x, c = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool mover = tid < kRunMovers;
+  RunSm<A> W;
+  {
+    double* d = reinterpret_cast<double*>(smem);
+    W.capc = capc;
+    W.x0 = d;
+    W.v0 = d + (size_t)2 * 3 * A * capc;
+    uint64_t* q = reinterpret_cast<uint64_t*>(W.v0 + 2 * capc);
+    W.key0 = q;
+    W.u = q + 2 * capc;
+    int* ip = reinterpret_cast<int*>(q + 3 * capc);
+    W.who0 = ip;
+    W.cnt = ip + 2 * capc;
+    W.src = ip + 3 * capc;
+  }
+  __shared__ int pc[kRunMovers], pd[kRunMovers];
+  __shared__ unsigned pf[kRunMovers];
+  __shared__ double ps[kRunMovers];
+  __shared__ RunStats pst[STATS ? kRunMovers : 1];
+  __shared__ RunRes res[2];
+  __shared__ int s_abort;
   const int64_t ld = S.ld;
   const long long N0 = S.n0;
   const double n0 = (double)N0, w_hi = (n0 + n0 * 0.5) + 1.0;
   const bool track = in.who && out.who;
-  long long step = ctrl->step;
-  int status = *(volatile int*)&ctrl->status;
+  const long long step0 = ctrl->step;
+  const int status0 = *(volatile int*)&ctrl->status;
   const long long N_in = ctrl->n;
-  if (!status && step < R.step_end && (N_in < 0 || N_in > ld || (N_in + G - 1) / G > capc)) {
+  const double vref_in = ctrl->vref;
+  bool run = !status0 && step0 < R.step_end;
+  if (run && (N_in < 0 || N_in > ld || (N_in + G - 1) / G > capc)) {
     // a start population whose even split does not fit the blocks' buffers (more
     // than the 1.5 n0 the population guard allows): refused, nothing is moved
-    status = GBDMC_ST_OVERFLOW;
-    if (c == 0 && threadIdx.x == 0) {
+    run = false;
+    if (c == 0 && tid == 0) {
       ctrl->status = GBDMC_ST_OVERFLOW;
-      ctrl->err_step = (int)step;
+      ctrl->err_step = (int)step0;
     }
   }
-  if (threadIdx.x == 0) {
-    const long long N = N_in < 0 ? 0 : (N_in > ld ? ld : N_in);
-    s_N = N;
-    s_base = N * c / G;
-    s_nc = N * (c + 1) / G - s_base;
-    s_vref = ctrl->vref;
-  }
+  const long long Nst = N_in < 0 ? 0 : (N_in > ld ? ld : N_in);
+  if (tid == 0) s_abort = 0;
   __syncthreads();
-  if (status || step >= R.step_end) {
+  if (!run) {
     // no step to run: the walkers pass through, so a queue of launches always
     // leaves the current walkers in the last launch's output
-    const int64_t N = s_N;
-    for (int64_t g = (int64_t)c * kRunTPB + threadIdx.x; g < N; g += (int64_t)G * kRunTPB) {
+    for (int64_t g = (int64_t)c * kRunTPB + tid; g < Nst; g += (int64_t)G * kRunTPB) {
 #pragma unroll
       for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = in.x[k * ld + g];
       out.v[g] = in.v[g];
       if (track) out.who[g] = in.who[g];
+      if (out.key) out.key[g] = in.key ? in.key[g] : (uint64_t)g;
     }
-  } else {
-    int rd = 0;          // the buffer holding the CTA's run
-    bool gather = false;  // its walker i is slot src[i] (the copies of the last step) or slot i
-    unsigned nbar = 0;    // grid barriers passed: every CTA takes the same ones (the same decisions)
-    // the CTA's even share of the compact input
-    for (int i = threadIdx.x; i < s_nc; i += kRunTPB) {
-      const int64_t g = s_base + i;
+  } else if (mover) {
+    // ------------------------------------------------------------ movers
+    // the CTA's even share of the compact input, with its lineage keys (the
+    // logical indices when the input has none)
+    long long base = Nst * c / G;
+    int n = (int)(Nst * (c + 1) / G - base);
+    for (int i = tid; i < n; i += kRunMovers) {
+      const int64_t g = base + i;
       const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
 #pragma unroll
-      for (int k = 0; k < 3 * A; ++k) xsb[k * capc + j] = in.x[k * ld + g];
-      whob[j] = track ? in.who[g] : 0;
+      for (int k = 0; k < 3 * A; ++k) W.x(0)[k * capc + j] = in.x[k * ld + g];
+      W.who(0)[j] = track ? in.who[g] : 0;
+      W.key(0)[j] = in.key ? in.key[g] : (uint64_t)g;
     }
+    int sb = 0, kq = 0;         // source buffer of the run, its keys
+    bool gather = false;        // the run's walker i is slot src[i] of buffer sb (else slot i)
+    int mb = 0, n_prev = 0;     // the previous step: its moved buffer, run size and copies
+    int tot_prev = 0;
+    long long base_prev = 0, step = step0;
+    unsigned nx = 0;            // exchange barriers passed
+    bool moved = true;          // the run of this step has been moved
     for (unsigned t = 0;; ++t, ++step) {
-      const long long base = s_base, nc = s_nc, N = s_N;
-      const double vref = s_vref;
-      // the moved walkers go to the other buffer (in place with one buffer, where
-      // every step starts from an even share, gather false)
-      const int wr = R.dbuf ? rd ^ 1 : rd;
-      const double* xr = xsb + (size_t)rd * 3 * A * capc;
-      double* xs = xsb + (size_t)wr * 3 * A * capc;
-      const int* whor = whob + (size_t)rd * capc;
-      int* whos = whob + (size_t)wr * capc;
-      // 1. move, potential, weight, count
+      if ((long long)t > (long long)R.kmax + 1) break;  // never reached: the stop action ends the launch (the reducer checks the same)
+      const bool prev_last = t > 0 && ((int)t >= R.kmax || step >= R.step_end);
+      const int db = sb ^ 1;
+      // 1. move and potential (no step to move after the launch's last step)
+      if (!prev_last) {
+        for (int i = tid; i < n; i += kRunMovers) {
+          double x[3 * A], z[3 * A], gr[3 * A];
+          const int j = gather ? (int)GBDMC_BC(W.src[i], 0, capc, kBcRunShared) : i;
+          RngL rng(S.seed, (uint64_t)step, W.key(kq)[i], S.replica_id);
+          gen_normals<NM, 3 * A>(rng, z);
+          const double* xr = W.x(sb);
+          double* xw = W.x(db);
+#pragma unroll
+          for (int k = 0; k < 3 * A; ++k) {
+            x[k] = __dadd_rn(xr[k * capc + j], __dmul_rn(S.sigma[k / 3], z[k]));
+            xw[k * capc + i] = x[k];
+          }
+          W.v(db)[i] = pes<PK, A, false>(x, S.pes, gr);
+          W.u[i] = rng.bits53();
+          if (track) W.who(db)[i] = W.who(sb)[j];
+        }
+      }
+      int cur = db;  // the buffer with this step's moved walkers
+      // 2. barrier A: the previous step's global results
+      bar_all();
+      const RunRes rp = t == 0 ? RunRes{Nst, base, vref_in, kRunGoOn, 0} : res[(t - 1) & 1];
+      if (rp.action == kRunGuard) {
+        // step t-1's moved, unbranched walkers (buffer mb), compact in logical order
+        for (int i = tid; i < n_prev; i += kRunMovers) {
+          const int64_t g = GBDMC_BC(base_prev + i, 0, ld, kBcRunOut);
+#pragma unroll
+          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = W.x(mb)[k * capc + i];
+          out.v[g] = W.v(mb)[i];
+          if (track) out.who[g] = W.who(mb)[i];
+          if (out.key) out.key[g] = W.key(kq ^ 1)[i];
+        }
+        break;
+      }
+      if (rp.action == kRunStop || rp.action == kRunOverflow) {
+        // step t-1's copies at their logical positions: the output, or the
+        // exchange area from which every CTA loads an even share
+        const bool stop = rp.action == kRunStop;
+        for (int i = tid; i < n_prev; i += kRunMovers) {
+          const int c0 = (i + 1 < n_prev ? W.cnt[i + 1] : tot_prev) - W.cnt[i];
+          const int64_t g0 = rp.below + W.cnt[i];
+          for (int r = 0; r < c0; ++r) {
+            const int64_t go = GBDMC_BC(g0 + r, 0, ld, kBcRunOut);
+#pragma unroll
+            for (int k = 0; k < 3 * A; ++k) out.x[k * ld + go] = W.x(mb)[k * capc + i];
+            out.v[go] = W.v(mb)[i];
+            if (track) out.who[go] = W.who(mb)[i];
+            const uint64_t kr = lineage_key(W.key(kq ^ 1)[i], r, (uint64_t)(step - 1));  // step t-1's copies
+            if (!stop) R.gkey[go] = kr;
+            else if (out.key) out.key[go] = kr;
+          }
+        }
+        if (stop) break;
+        if (!mov_grid_barrier(R.sync + 2, (unsigned)G * ++nx)) {
+          if (tid == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+          s_abort = 1;
+          moved = false;
+        } else {
+          // the even share of step t-1's copies is this step's run; move it again
+          base = rp.n * c / G;
+          n = (int)(rp.n * (c + 1) / G - base);
+          const int lb = db;  // neither step t-1's moved walkers (mb) nor needed any more
+          for (int i = tid; i < n; i += kRunMovers) {
+            const int64_t g = base + i;
+            const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
+#pragma unroll
+            for (int k = 0; k < 3 * A; ++k) W.x(lb)[k * capc + j] = __ldcg(out.x + k * ld + g);
+            W.who(lb)[j] = track ? __ldcg(out.who + g) : 0;
+            W.key(kq)[j] = __ldcg(R.gkey + g);
+          }
+          bar_mov();
+          sb = lb;
+          gather = false;
+          const int db2 = sb ^ 1;
+          for (int i = tid; i < n; i += kRunMovers) {
+            double x[3 * A], z[3 * A], gr[3 * A];
+            RngL rng(S.seed, (uint64_t)step, W.key(kq)[i], S.replica_id);
+            gen_normals<NM, 3 * A>(rng, z);
+#pragma unroll
+            for (int k = 0; k < 3 * A; ++k) {
+              x[k] = __dadd_rn(W.x(sb)[k * capc + i], __dmul_rn(S.sigma[k / 3], z[k]));
+              W.x(db2)[k * capc + i] = x[k];
+            }
+            W.v(db2)[i] = pes<PK, A, false>(x, S.pes, gr);
+            W.u[i] = rng.bits53();
+            if (track) W.who(db2)[i] = W.who(sb)[i];
+          }
+          cur = db2;
+        }
+      } else {
+        base = rp.below;
+        if (rp.action == kRunExchange) {
+          // this step's moved walkers split evenly: through the exchange area
+          for (int i = tid; i < n; i += kRunMovers) {
+            const int64_t g = GBDMC_BC(base + i, 0, ld, kBcRunOut);
+#pragma unroll
+            for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = W.x(cur)[k * capc + i];
+            out.v[g] = W.v(cur)[i];
+            if (track) out.who[g] = W.who(cur)[i];
+            R.gkey[g] = W.key(kq)[i];
+            R.gu[g] = W.u[i];
+          }
+          if (!mov_grid_barrier(R.sync + 2, (unsigned)G * ++nx)) {
+            if (tid == 0) atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+            s_abort = 1;
+            moved = false;
+          } else {
+            base = rp.n * c / G;
+            n = (int)(rp.n * (c + 1) / G - base);
+            const int lb = cur ^ 1;
+            for (int i = tid; i < n; i += kRunMovers) {
+              const int64_t g = base + i;
+              const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
+#pragma unroll
+              for (int k = 0; k < 3 * A; ++k) W.x(lb)[k * capc + j] = __ldcg(out.x + k * ld + g);
+              W.v(lb)[j] = __ldcg(out.v + g);
+              W.who(lb)[j] = track ? __ldcg(out.who + g) : 0;
+              W.key(kq)[j] = __ldcg(R.gkey + g);
+              W.u[j] = __ldcg(R.gu + g);
+            }
+            cur = lb;
+          }
+        }
+      }
+      // 3. weights and counts with this step's vref
+      const double vref = rp.vref;
       int csum = 0, flag = 0;
       long long births = 0, deaths = 0;
       double s0 = 0.0;
       RunStats st = {0.0, INFINITY, -INFINITY, 0.0};
-      for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-        double x[3 * A], z[3 * A], g[3 * A];
-        const int j = gather ? (int)GBDMC_BC(src[i], 0, capc, kBcRunShared) : i;
-        Rng rng(S.seed, (uint64_t)step, (uint64_t)(base + i), S.replica_id);
-        gen_normals<NM, 3 * A>(rng, z);
+      if (moved) {
+        bar_mov();
+        for (int i = tid; i < n; i += kRunMovers) {
+          const double v = W.v(cur)[i];
+          if (STATS) {
+            st.s1 += v;
+            st.vmin = fmin(st.vmin, v);
+            st.vmax = fmax(st.vmax, v);
+          }
+          const int cn = branch_count(v, vref, S.dt, (double)W.u[i] * 0x1.0p-53, w_hi, flag, births, deaths);
+          W.cnt[i] = cn;
+          csum += cn;
+          s0 += cn == 1 ? v : (double)cn * v;
+        }
+      }
+      pc[tid] = csum;
+      pd[tid] = (int)deaths;
+      pf[tid] = (unsigned)flag;
+      ps[tid] = s0;
+      if (STATS) pst[tid] = st;
+      // 4. barrier B: the sums to the reducer
+      bar_all();
+      if (s_abort) {
+        moved = true;
+        continue;  // the reducer publishes the abort at the next barrier A
+      }
+      // 5. the copies' gather index and lineage keys (the next run)
+      const int tot = mov_scan(W.cnt, n);
+      for (int i = tid; i < n; i += kRunMovers) {
+        const int c0 = (i + 1 < n ? W.cnt[i + 1] : tot) - W.cnt[i];
+        const int j0 = W.cnt[i];
+        for (int r = 0; r < c0; ++r) {
+          const int j = j0 + r;
+          if (j < capc) {  // a CTA's copies past its buffer: the overflow action follows
+            W.src[j] = i;
+            W.key(kq ^ 1)[j] = lineage_key(W.key(kq)[i], r, (uint64_t)step);
+          }
+        }
+      }
+      bar_mov();
+      mb = cur;
+      n_prev = n;
+      tot_prev = tot;
+      base_prev = base;
+      sb = cur;
+      kq ^= 1;
+      gather = true;
+      n = tot < capc ? tot : capc;
+    }
+  } else {
+    // ----------------------------------------------------------- reducer
+    long long N = Nst;  // the population moved at step t
+    double vref = vref_in;
+    long long step = step0;
+    unsigned narr = 0;
+    for (unsigned t = 0;; ++t, ++step) {
+      if ((long long)t > (long long)R.kmax + 1) break;  // as the movers
+      // barrier A of step t: the movers have read nothing of step t yet
+      bar_all();
+      if (t > 0) {
+        const int act = res[(t - 1) & 1].action;
+        if (act == kRunGuard || act == kRunStop) break;
+      }
+      // barrier B of step t: the movers' per-thread sums
+      bar_all();
+      const unsigned full = 0xffffffffu;
+      int cc = 0, dd = 0;
+      unsigned ff = 0;
+      double q = 0.0;
+      RunStats qs = {0.0, INFINITY, -INFINITY, 0.0};
 #pragma unroll
-        for (int k = 0; k < 3 * A; ++k) {
-          x[k] = __dadd_rn(xr[k * capc + j], __dmul_rn(S.sigma[k / 3], z[k]));
-          xs[k * capc + i] = x[k];
-        }
-        if (track) whos[i] = whor[j];
-        const double v = pes<PK, A, false>(x, S.pes, g);
-        vs[i] = v;
+      for (int w = 0; w < kRunMovers / 32; ++w) {
+        const int k = lane + 32 * w;
+        cc += pc[k];
+        dd += pd[k];
+        ff |= pf[k];
+        q += ps[k];
         if (STATS) {
-          st.s1 += v;
-          st.vmin = fmin(st.vmin, v);
-          st.vmax = fmax(st.vmax, v);
+          qs.s1 += pst[k].s1;
+          qs.vmin = fmin(qs.vmin, pst[k].vmin);
+          qs.vmax = fmax(qs.vmax, pst[k].vmax);
         }
-        const int cn = branch_count(v, vref, S.dt, rng.uniform53(), w_hi, flag, births, deaths);
-        cnt[i] = cn;
-        csum += cn;
-        s0 += cn == 1 ? v : (double)cn * v;
       }
-      int dsum = (int)deaths;
-      unsigned fl = (unsigned)flag;
-      run_block_sums<STATS>(csum, dsum, fl, s0, st);
+      cc = (int)__reduce_add_sync(full, (unsigned)cc);
+      dd = (int)__reduce_add_sync(full, (unsigned)dd);
+      ff = __reduce_or_sync(full, ff);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(full, q, o);
+      if (STATS) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) qs.s1 += __shfl_xor_sync(full, qs.s1, o);
+        qs.vmin = dkey_inv(warp_min_key(dkey(qs.vmin)));
+        qs.vmax = dkey_inv(warp_max_key(dkey(qs.vmax)));
+      }
       const int par = t & 1;
-      if (threadIdx.x == 0) {
-        RunPart q;
-        q.c = csum;
-        q.df = (unsigned)dsum | (fl << 24);
-        q.s0 = s0;
-        R.part[par * G + c] = q;
-        if (STATS) R.stat[par * G + c] = st;
-        run_arrive(R.sync);
+      bool ok = s_abort == 0;  // the movers gave up on an exchange barrier: no arrival
+      if (lane == 0 && ok) {
+        if (cc > capc) ff |= kRunOverflowBit;
+        RunPart pp;
+        pp.c = cc;
+        pp.df = (unsigned)dd | (ff << 24);
+        pp.s0 = q;
+        R.part[par * G + c] = pp;
+        if (STATS) R.stat[par * G + c] = qs;
+        red_release_add(R.sync, 1u);
+        ok = run_poll(R.sync, (unsigned)G * ++narr);
+      } else if (ok) {
+        ++narr;
       }
-      // while the others arrive: the exclusive scan of the block's counts and the
-      // gather index of its copies (copy r of walker i is the block's next walker
-      // cnt[i] + r, read from slot i of this step's buffer), used if the step keeps
-      // its copies in the block
-      const int tot = run_scan(cnt, (int)nc);
-      if (R.dbuf) {
-        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
-          const int j0 = cnt[i];
-          for (int r = 0; r < c0; ++r) src[GBDMC_BC(j0 + r, 0, capc, kBcRunShared)] = i;
-        }
-      }
-      // 2. every CTA's partial
-      if (!run_wait(R.sync, (unsigned)G * ++nbar)) {
-        if (threadIdx.x == 0) {
-          atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
-          ctrl->err_step = (int)step;
-        }
-        break;
-      }
-      // 3. the same reduction in every CTA, in warp 0: lane l takes CTAs l, l + 32, ...
-      if (threadIdx.x < 32) {
-        const unsigned full = 0xffffffffu;
-        unsigned nn = 0, below = 0;
-        int nd = 0, cmax = 0;
-        unsigned f = 0;
-        double q0 = 0.0;
-        RunStats qs = {0.0, INFINITY, -INFINITY, 0.0};
-        // all of the lane's partials are loaded before any is used: one L2 round
-        // trip (predicated: every block reads every partial once, so that no L2
-        // line is hit by more requests than there are blocks)
-        int4 rp[kRunMaxCTA / 32];
+      ok = __shfl_sync(full, ok ? 1 : 0, 0) != 0;
+      __syncwarp();  // lane 0's acquire of the arrivals orders the warp's loads of the partials
+      // every CTA's partial: the same reduction in every CTA (all loads first)
+      unsigned nn = 0, below = 0;
+      int nd = 0, cmax = 0;
+      unsigned f = 0;
+      double q0 = 0.0;
+      RunStats rs = {0.0, INFINITY, -INFINITY, 0.0};
+      if (ok) {
+        int4 rpv[kRunMaxCTA / 32];
         const int4* pp = reinterpret_cast<const int4*>(R.part + par * G);
 #pragma unroll
         for (int k = 0; k < kRunMaxCTA / 32; ++k) {
           const int g = lane + 32 * k;
-          rp[k] = g < G ? __ldcg(pp + g) : make_int4(0, 0, 0, 0);
+          rpv[k] = g < G ? __ldcg(pp + g) : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int k = 0; k < kRunMaxCTA / 32; ++k) {
           const int g = lane + 32 * k;
-          const int4 r = rp[k];  // zeros past G: they add nothing
+          const int4 r = rpv[k];
           const int rc = r.x;
-          nn += rc;
+          nn += (unsigned)rc;
           nd += (int)((unsigned)r.y & 0xFFFFFFu);
           f |= (unsigned)r.y >> 24;
-          if (g < G) q0 += __hiloint2double(r.w, r.z);  // the same additions in every CTA
-          if (g < c) below += rc;
+          if (g < G) q0 += __hiloint2double(r.w, r.z);
+          if (g < c) below += (unsigned)rc;
           cmax = rc > cmax ? rc : cmax;
           if (STATS && g < G) {
             const double2 a = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g));
             const double2 b = __ldcg(reinterpret_cast<const double2*>(R.stat + par * G + g) + 1);
-            qs.s1 += a.x;
-            qs.vmin = fmin(qs.vmin, a.y);
-            qs.vmax = fmax(qs.vmax, b.x);
+            rs.s1 += a.x;
+            rs.vmin = fmin(rs.vmin, a.y);
+            rs.vmax = fmax(rs.vmax, b.x);
           }
         }
-        if (STATS) {
+      }
+      if (STATS) {
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) qs.s1 += __shfl_xor_sync(full, qs.s1, o);
-          qs.vmin = dkey_inv(warp_min_key(dkey(qs.vmin)));
-          qs.vmax = dkey_inv(warp_max_key(dkey(qs.vmax)));
-        }
-        nn = __reduce_add_sync(full, nn);
-        below = __reduce_add_sync(full, below);
-        nd = (int)__reduce_add_sync(full, (unsigned)nd);
-        cmax = (int)__reduce_max_sync(full, (unsigned)cmax);
-        f = __reduce_or_sync(full, f);
+        for (int o = 16; o > 0; o >>= 1) rs.s1 += __shfl_xor_sync(full, rs.s1, o);
+        rs.vmin = dkey_inv(warp_min_key(dkey(rs.vmin)));
+        rs.vmax = dkey_inv(warp_max_key(dkey(rs.vmax)));
+      }
+      nn = __reduce_add_sync(full, nn);
+      below = __reduce_add_sync(full, below);
+      nd = (int)__reduce_add_sync(full, (unsigned)nd);
+      cmax = (int)__reduce_max_sync(full, (unsigned)cmax);
+      f = __reduce_or_sync(full, f);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) q0 += __shfl_xor_sync(full, q0, o);
-        // 32-bit sums: exact while every block holds fewer than 2^31 / kRunMaxCTA
-        // copies; a larger block count is a population past any guard (N' > 1.5 N0)
-        const bool huge = cmax >= (int)(0x7fffffff / kRunMaxCTA);
-        const long long Nn = huge ? (long long)INT32_MAX * 4 : (long long)nn;
-        // the step's divisions, one SIMT division: <V> of the branched population
-        // (lane 0), the population term (lane 1), the mean potential (lane 2)
-        const double num = lane == 0 ? q0 : (lane == 1 ? (double)(Nn - N0) : qs.s1);
-        const double den = lane == 0 ? (double)Nn : (lane == 1 ? n0 : (double)N);
-        const double qq = num / den;
-        const double vbar = __shfl_sync(full, qq, 0), corr = __shfl_sync(full, qq, 1);
-        const double vmean = __shfl_sync(full, qq, 2);
-        if (lane == 0) {
-          int st2 = (int)f;
+      for (int o = 16; o > 0; o >>= 1) q0 += __shfl_xor_sync(full, q0, o);
+      // 32-bit sums: exact while every block holds fewer than 2^31 / kRunMaxCTA
+      // copies; a larger block count is a population past any guard (N' > 1.5 N0)
+      const bool huge = cmax >= (int)(0x7fffffff / kRunMaxCTA);
+      const long long Nn = huge ? (long long)INT32_MAX * 4 : (long long)nn;
+      // the step's divisions, one SIMT division: <V> of the branched population
+      // (lane 0), the population term (lane 1), the mean potential (lane 2)
+      const double num = lane == 0 ? q0 : (lane == 1 ? (double)(Nn - N0) : rs.s1);
+      const double den = lane == 0 ? (double)Nn : (lane == 1 ? n0 : (double)N);
+      const double qq = num / den;
+      const double vbar = __shfl_sync(full, qq, 0), corr = __shfl_sync(full, qq, 1);
+      const double vmean = __shfl_sync(full, qq, 2);
+      const double vr = vbar - S.alpha * corr;
+      int st2 = ok ? (int)(f & 0x3Fu) : GBDMC_ST_TIMEOUT;
+      if (!st2) {
+        if ((double)Nn < n0 - n0 * 0.5) st2 |= GBDMC_ST_POP_LOW;
+        if ((double)Nn > n0 + n0 * 0.5) st2 |= GBDMC_ST_POP_HIGH;
+        if (Nn > ld) st2 |= GBDMC_ST_OVERFLOW;
+      }
+      const long long even = huge ? (long long)INT32_MAX : (long long)((nn + (unsigned)G - 1u) / (unsigned)G);
+      const bool last = (int)t + 1 >= R.kmax || step + 1 >= R.step_end;
+      // the largest CTA's copies against the warps of an even split plus one
+      const long long lim = ((even + 31) / 32) * 32 + 32;
+      int act = kRunGoOn;
+      if (st2) act = kRunGuard;
+      else if (last || even > capc) act = kRunStop;
+      else if (f & kRunOverflowBit) act = kRunOverflow;
+      else if ((long long)cmax > (lim < capc ? lim : (long long)capc)) act = kRunExchange;
+      if (lane == 0) {
+        if (c == 0 && step < S.hist.len && ok) {
+          const int64_t h = step;
+          if (STATS) {
+            if (S.hist.vmin) S.hist.vmin[h] = rs.vmin;
+            if (S.hist.vmax) S.hist.vmax[h] = rs.vmax;
+            if (S.hist.vmean) S.hist.vmean[h] = vmean;
+          }
           if (!st2) {
-            if ((double)Nn < n0 - n0 * 0.5) st2 |= GBDMC_ST_POP_LOW;
-            if ((double)Nn > n0 + n0 * 0.5) st2 |= GBDMC_ST_POP_HIGH;
-            if (Nn > ld) st2 |= GBDMC_ST_OVERFLOW;
-          }
-          const double vr = vbar - S.alpha * corr;
-          if (c == 0 && step < S.hist.len) {
-            const int64_t h = step;
-            if (STATS) {
-              if (S.hist.vmin) S.hist.vmin[h] = qs.vmin;
-              if (S.hist.vmax) S.hist.vmax[h] = qs.vmax;
-              if (S.hist.vmean) S.hist.vmean[h] = vmean;
-            }
-            if (!st2) {
-              if (S.hist.vref) S.hist.vref[h] = vr;
-              if (S.hist.pop) S.hist.pop[h] = (double)Nn;
-              if (S.hist.births) S.hist.births[h] = (int)(Nn - (N - nd));  // sum of max(c - 1, 0)
-              if (S.hist.deaths) S.hist.deaths[h] = nd;
-            }
-          }
-          const long long even = huge ? (long long)INT32_MAX : (long long)((nn + (unsigned)G - 1u) / (unsigned)G);
-          const int stop = st2 ? 2 : ((step + 1 >= R.step_end || (int)t + 1 >= R.kmax || even > capc) ? 1 : 0);
-          s_stop = stop;
-          // the largest CTA's copies against the warps of an even split plus one: a
-          // warp more costs the largest block ~4% of its move (the FP64 work is per
-          // walker), an even split through the output ~15% of a step
-          const long long lim = ((even + 31) / 32) * 32 + 32;
-          s_even = !R.dbuf || (long long)cmax > (lim < capc ? lim : (long long)capc);
-          if (c == 0) {
-            if (st2) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
-              ctrl->n = N;
-              ctrl->vref = vref;
-              ctrl->step = step;
-              ctrl->status = st2;
-              ctrl->err_step = (int)step;
-            } else if (stop == 1) {
-              ctrl->n_prev = N;
-              ctrl->n = Nn;
-              ctrl->vref = vr;
-              ctrl->step = step + 1;
-            }
-          }
-          s_nnew = below;  // the new logical base of this CTA's copies: the earlier CTAs' copies
-          s_vref = vr;
-          s_N = Nn;
-        }
-      }
-      __syncthreads();
-      const int stop = s_stop;
-      if (stop == 2) {  // the moved, unbranched walkers, compact in logical order
-        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-          const int64_t g = base + i;
-#pragma unroll
-          for (int k = 0; k < 3 * A; ++k) out.x[k * ld + g] = xs[k * capc + i];
-          out.v[g] = vs[i];
-          if (track) out.who[g] = whos[i];
-        }
-        break;
-      }
-      // 4. branch: the CTA's copies in np.repeat order
-      const long long nb = s_nnew;
-      if (stop || s_even) {
-        // into the output at their logical positions: the whole population compact in logical order
-        for (int i = threadIdx.x; i < nc; i += kRunTPB) {
-          const int c0 = (i + 1 < nc ? cnt[i + 1] : tot) - cnt[i];
-          const int64_t g0 = nb + cnt[i];
-          for (int r = 0; r < c0; ++r) {
-            const int64_t go = GBDMC_BC(g0 + r, 0, ld, kBcRunOut);
-#pragma unroll
-            for (int k = 0; k < 3 * A; ++k) out.x[k * ld + go] = xs[k * capc + i];
-            out.v[go] = vs[i];
-            if (track) out.who[go] = whos[i];
+            if (S.hist.vref) S.hist.vref[h] = vr;
+            if (S.hist.pop) S.hist.pop[h] = (double)Nn;
+            if (S.hist.births) S.hist.births[h] = (int)(Nn - (N - nd));  // sum of max(c - 1, 0)
+            if (S.hist.deaths) S.hist.deaths[h] = nd;
           }
         }
-        if (stop) break;
-        // every CTA's copies written; each CTA takes its even share of the new
-        // population back into shared memory (read past L1: other SMs wrote it)
-        if (!run_barrier(R.sync, (unsigned)G * ++nbar)) {
-          if (threadIdx.x == 0) {
-            atomicOr(&ctrl->status, GBDMC_ST_TIMEOUT);
+        if (c == 0) {
+          if (st2) {  // as a failed per-step call leaves it: moved walkers, N, vref and step of the step
+            ctrl->n = N;
+            ctrl->vref = vref;
+            ctrl->step = step;
+            atomicOr(&ctrl->status, st2);
             ctrl->err_step = (int)step;
+          } else if (act == kRunStop) {
+            ctrl->n_prev = N;
+            ctrl->n = Nn;
+            ctrl->vref = vr;
+            ctrl->step = step + 1;
           }
-          break;
         }
-        const long long Nn = s_N, nbase = Nn * c / G, nnc = Nn * (c + 1) / G - nbase;
-        const int ld_buf = R.dbuf ? wr ^ 1 : wr;  // the moved walkers are in the output now
-        double* xl = xsb + (size_t)ld_buf * 3 * A * capc;
-        int* wl = whob + (size_t)ld_buf * capc;
-        for (int i = threadIdx.x; i < nnc; i += kRunTPB) {
-          const int64_t g = nbase + i;
-          const int j = (int)GBDMC_BC(i, 0, capc, kBcRunShared);
-#pragma unroll
-          for (int k = 0; k < 3 * A; ++k) xl[k * capc + j] = __ldcg(out.x + k * ld + g);
-          wl[j] = track ? __ldcg(out.who + g) : 0;
-        }
-        rd = ld_buf;
-        gather = false;
-        if (threadIdx.x == 0) {
-          s_base = nbase;
-          s_nc = nnc;
-        }
-      } else {
-        // the CTA's next run is its copies (their gather index is written), at logical base nb
-        rd = wr;
-        gather = true;
-        if (threadIdx.x == 0) {
-          s_base = nb;
-          s_nc = tot;
-        }
+        res[par] = RunRes{Nn, (long long)below, vr, act, 0};
       }
-      __syncthreads();
+      N = Nn;
+      vref = vr;
     }
   }
   // the last CTA out resets the barrier words for the next launch
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     __threadfence();
     if (atomicAdd(&R.sync[1], 1u) == (unsigned)G - 1) {
       R.sync[0] = 0;
       R.sync[1] = 0;
+      R.sync[2] = 0;
     }
   }
 }
 
+// The deviates and branching uniforms of walkers with the given lineage keys
+// at one step, as the multi-step kernel draws them (for checking its
+// trajectory with the per-step kernels on injected noise).
+template <int NM, int A>
+__global__ void k_lineage_noise(uint64_t seed, uint32_t replica, int64_t step, const uint64_t* __restrict__ keys,
+                                int64_t n, double* __restrict__ normal, int64_t ldn, double* __restrict__ u) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    RngL rng(seed, (uint64_t)step, keys[i], replica);
+    double z[3 * A];
+    gen_normals<NM, 3 * A>(rng, z);
+#pragma unroll
+    for (int k = 0; k < 3 * A; ++k) normal[k * ldn + i] = z[k];
+    u[i] = rng.uniform53();
+  }
+}
+
+template <int NM>
+static void lineage_noise_launch(const gbdmc_sim_t& S, const uint64_t* keys, int64_t n, int64_t step, double* normal,
+                                 int64_t ldn, double* u, cudaStream_t s) {
+  const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  if (S.natoms == 1)
+    k_lineage_noise<NM, 1><<<grid, 256, 0, s>>>(S.seed, S.replica_id, step, keys, n, normal, ldn, u);
+  else if (S.natoms == 3)
+    k_lineage_noise<NM, 3><<<grid, 256, 0, s>>>(S.seed, S.replica_id, step, keys, n, normal, ldn, u);
+  else
+    k_lineage_noise<NM, 6><<<grid, 256, 0, s>>>(S.seed, S.replica_id, step, keys, n, normal, ldn, u);
+}
+
 // ------------------------------------------------------------ host side
-static size_t run_smem_bytes(int A, int capc, int nbuf) {
-  return (size_t)capc * (nbuf * (3 * A * sizeof(double) + sizeof(int)) + sizeof(double) + 2 * sizeof(int));
+// Per walker slot: two coordinate buffers, two V, two lineage keys, the
+// branching-uniform bits, two ancestor ids, the count and the gather index.
+static size_t run_smem_bytes(int A, int capc) {
+  return (size_t)capc * (2 * 3 * A * sizeof(double) + 2 * sizeof(double) + 3 * sizeof(uint64_t) + 4 * sizeof(int));
 }
 
 struct RunShape {
-  int grid, capc, dbuf;
+  int grid, capc;
   size_t smem;
 };
 
@@ -577,10 +697,8 @@ static int run_dispatch(const gbdmc_sim_t& S, const gbdmc_walkers_t& src, const 
 }
 
 // Grid and per-CTA buffers of a launch: about 96 walkers per CTA, at most one
-// CTA per SM (and kRunMaxCTA); each CTA's buffer holds its even share of the
-// largest population the guard allows (1.5 n0) with a margin.  Two buffers
-// per CTA (the copies of a step stay in shared memory) when they fit, else one
-// (every step splits the population evenly through the output).
+// CTA per SM (and kRunMaxCTA); each CTA's buffers hold its even share of the
+// largest population the guard allows (1.5 n0) with a margin.
 static int run_shape(const gbdmc_sim_t& S, RunShape& sh) {
   const int A = S.natoms;
   int g = (int)((S.n0 + 95) / 96);
@@ -588,16 +706,20 @@ static int run_shape(const gbdmc_sim_t& S, RunShape& sh) {
   g = g < 1 ? 1 : (g > lim ? lim : g);
   const int64_t capc = ((S.n0 * 3 / 2 + 1 + g - 1) / g + 64 + 31) / 32 * 32;
   const size_t smax = 200 * 1024;
-  if (capc > (1 << 20) || run_smem_bytes(A, (int)capc, 1) > smax) {
+  if (capc > (1 << 20) || run_smem_bytes(A, (int)capc) > smax) {
     set_error("gbdmc_sim_run: %lld walkers per block buffer do not fit shared memory (%zu bytes); use "
-              "gbdmc_sim_step", (long long)capc, run_smem_bytes(A, (int)(capc > (1 << 20) ? 1 << 20 : capc), 1));
+              "gbdmc_sim_step", (long long)capc, run_smem_bytes(A, (int)(capc > (1 << 20) ? 1 << 20 : capc)));
     return GBDMC_ERR_CAPACITY;
   }
   sh.grid = g;
   sh.capc = (int)capc;
-  sh.dbuf = run_smem_bytes(A, (int)capc, 2) <= smax ? 1 : 0;
-  sh.smem = run_smem_bytes(A, (int)capc, sh.dbuf ? 2 : 1);
+  sh.smem = run_smem_bytes(A, (int)capc);
   return GBDMC_OK;
+}
+
+static size_t run_scratch_head() {
+  return align256(sizeof(RunPart) * 2 * kRunMaxCTA) + align256(sizeof(RunStats) * 2 * kRunMaxCTA) +
+         align256(4 * sizeof(unsigned));
 }
 
 GBDMC_BOUNDS_READER(bounds_read_run)
@@ -606,9 +728,8 @@ GBDMC_BOUNDS_READER(bounds_read_run)
 
 using namespace gbdmc;
 
-extern "C" size_t gbdmc_sim_run_scratch_bytes(void) {
-  return align256(sizeof(RunPart) * 2 * kRunMaxCTA) + align256(sizeof(RunStats) * 2 * kRunMaxCTA) +
-         align256(2 * sizeof(unsigned));
+extern "C" size_t gbdmc_sim_run_scratch_bytes(int64_t ld) {
+  return run_scratch_head() + 2 * align256((size_t)(ld > 0 ? ld : 0) * sizeof(uint64_t));
 }
 
 extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
@@ -645,10 +766,11 @@ extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, c
   const int kcap = (int)((1u << 31) / (2u * (unsigned)sh.grid));
   R.kmax = max_steps < kcap ? max_steps : kcap;
   R.capc = sh.capc;
-  R.dbuf = sh.dbuf;
   R.part = (RunPart*)b;
   R.stat = (RunStats*)(b + align256(sizeof(RunPart) * 2 * kRunMaxCTA));
   R.sync = (unsigned*)(b + align256(sizeof(RunPart) * 2 * kRunMaxCTA) + align256(sizeof(RunStats) * 2 * kRunMaxCTA));
+  R.gkey = (uint64_t*)(b + run_scratch_head());
+  R.gu = (uint64_t*)(b + run_scratch_head() + align256((size_t)S->ld * sizeof(uint64_t)));
   cudaStream_t s = (cudaStream_t)stream;
   const int PK = S->pes.kind, A = S->natoms;
   if (PK == GBDMC_PES_HO && A == 1) return run_dispatch<GBDMC_PES_HO, 1>(*S, *src, *dst, ctrl, R, sh, s);
@@ -658,4 +780,23 @@ extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, c
   if (PK == GBDMC_PES_DIMER && A == 6) return run_dispatch<GBDMC_PES_DIMER, 6>(*S, *src, *dst, ctrl, R, sh, s);
   set_error("%s: unsupported system (pes %d, atoms %d)", what, PK, A);
   return GBDMC_ERR_ARG;
+}
+
+extern "C" int gbdmc_lineage_noise(const gbdmc_sim_t* sim, const uint64_t* keys_dev, int64_t n, int64_t step,
+                                   double* normal_dev, int64_t ld_noise, double* u_dev, void* stream) {
+  if (!sim || n < 0 || ld_noise < n || (n > 0 && (!keys_dev || !normal_dev || !u_dev))) {
+    set_error("gbdmc_lineage_noise: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  if (sim->natoms != 1 && sim->natoms != 3 && sim->natoms != 6) {
+    set_error("gbdmc_lineage_noise: %d atoms (1, 3 or 6)", sim->natoms);
+    return GBDMC_ERR_ARG;
+  }
+  if (n == 0) return GBDMC_OK;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (sim->noise_mode == GBDMC_NOISE_PHILOX64)
+    lineage_noise_launch<GBDMC_NOISE_PHILOX64>(*sim, keys_dev, n, step, normal_dev, ld_noise, u_dev, s);
+  else
+    lineage_noise_launch<GBDMC_NOISE_PHILOX32>(*sim, keys_dev, n, step, normal_dev, ld_noise, u_dev, s);
+  return check_launch("gbdmc_lineage_noise");
 }

@@ -17,8 +17,10 @@ that supplies the deviates on the host in the reference's call order),
 ``DEBUG_save_training_every`` steps), ``replica_id`` (Philox stream),
 ``block_threads`` (tile width; 0 = chosen from the population) and
 ``fused_steps`` (plain discrete Philox runs: up to this many steps per launch
-of the multi-step kernel, walkers resident in shared memory; 0 = one launch
-pair per step, which ``block_threads`` also selects).
+of the multi-step kernel, walkers resident in shared memory; its walkers draw
+from the Philox streams of their lineage keys, which travel with them from
+launch to launch and into checkpoints; 0 = one launch pair per step with the
+index-keyed streams, which ``block_threads`` also selects).
 """
 import contextlib
 import ctypes as C
@@ -320,7 +322,8 @@ class DMC_Sim:
         self._bufs = []
         for _ in range(2):
             b = dict(x=torch.zeros(3 * A, ld, **f64), v=torch.zeros(ld, **f64),
-                     who=torch.zeros(ld, dtype=torch.int32, device=dev))
+                     who=torch.zeros(ld, dtype=torch.int32, device=dev),
+                     key=torch.zeros(ld, dtype=torch.int64, device=dev))  # the multi-step kernel's lineage keys
             if IS:
                 b.update(f=torch.zeros(3 * A, ld, **f64), psi=torch.zeros(ld, **f64), ke=torch.zeros(ld, **f64))
             if cont:
@@ -332,6 +335,7 @@ class DMC_Sim:
             w0 = np.ones(len(coords)) if self.start_cont_wts is None else np.asarray(self.start_cont_wts, float)
             self._bufs[0]["w"][:len(coords)] = torch.as_tensor(w0, **f64)
         self._bufs[0]["x"][:self._ncoord, :len(coords)] = to_soa(coords, dev)
+        self._bufs[0]["key"][:len(coords)] = torch.arange(len(coords), dtype=torch.int64, device=dev)
         self._cur = 0
         self._lazy = False  # current buffer holds its walkers through a gather index
         self._ctrl = torch.zeros(C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
@@ -393,6 +397,8 @@ class DMC_Sim:
             w.w = b["w"].data_ptr()
         if with_idx and "idx" in b:
             w.idx = b["idx"].data_ptr()
+        if "key" in b:
+            w.key = b["key"].data_ptr()
         return w
 
     # ------------------------------------------------------- device calls
@@ -554,7 +560,7 @@ class DMC_Sim:
         kernel does not take this system (the per-block buffers do not fit)."""
         L = _capi.load()
         if not hasattr(self, "_run_scratch"):
-            self._run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(), dtype=torch.uint8, device=self.device)
+            self._run_scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(self.capacity), dtype=torch.uint8, device=self.device)
         self._compact()
         c = self._read_ctrl()
         end = int(c.step) + nsteps
@@ -821,6 +827,7 @@ class DMC_Sim:
         st = {k: v for k, v in self.__dict__.items() if not k.startswith("_") and k not in (
             "potential", "impsamp_manager", "potential_info", "training_sink", "device", "rng")}
         st.update(_coords=self._coords_host(n), _vref_vs_tau=self._vref_vs_tau.copy(),
+                  _keys=None if self._nn_route else self._bufs[self._cur]["key"][:n].cpu().numpy().copy(),
                   _pop_vs_tau=self._pop_vs_tau.copy(), _eff_ts=self._eff_ts.copy(),
                   _cont_wts=None if self._nn_route or "w" not in self._bufs[0] else
                   self._bufs[self._cur]["w"][:n].cpu().numpy(),
@@ -999,6 +1006,9 @@ def dmc_restart(potential, chkpt_folder, sim_name, additional_timesteps=0, impsa
     sim._vref_vs_tau[:n] = st["_vref_vs_tau"]
     sim._pop_vs_tau[:n] = st["_pop_vs_tau"]
     sim._eff_ts[:n] = st["_eff_ts"]
+    if st.get("_keys") is not None and not sim._nn_route:  # the multi-step kernel's walk goes on unchanged
+        k = torch.as_tensor(np.asarray(st["_keys"]), dtype=torch.int64, device=sim.device)
+        sim._bufs[sim._cur]["key"][:len(k)] = k
     return sim
 
 

@@ -5,7 +5,7 @@ checked against its range, and none of these runs may set an error bit.
 The cases run in a child process that loads the checked library
 (GBDMC_BOUNDS_CHECK=1): the plain step on injected deviates against the oracle
 at N = 1, 31, 33 and 1025 (bit-exact, or the same population-guard stop), the
-multi-step kernel against the per-step kernels, continuous weighting with
+multi-step kernel against its replayed walk, continuous weighting with
 both thresholds and importance sampling against the reference fixtures, a
 Python getpot through gbdmc_sim_move / gbdmc_sim_branch, and the surrogate
 step.  One more case feeds gbdmc_walkers_compact a gather index that lies
@@ -66,13 +66,17 @@ for n in (1, 31, 33, 1025):
         ok = err is not None
     out[f"plain_{n}"] = [bool(ok), int(L.gbdmc_bounds_errors(1))]
 
-# the multi-step kernel against the per-step kernels (Philox deviates)
+# the multi-step kernel against its walk replayed by the per-step kernels
+from lineage_harness import replay
 for n in (31, 33, 1025):
     x0 = eq[None] + 0.05 * oracle.InjectedNoise(60 + n).standard_normal((n, 3, 3))
     a = sim(x0, pg.h2o_local_mode(), num_timesteps=100, seed=11, fused_steps=64)
-    b = sim(x0, pg.h2o_local_mode(), num_timesteps=100, seed=11, fused_steps=0)
-    a.run(); b.run()
-    ok = a._multi_used and np.array_equal(a._pop_vs_tau, b._pop_vs_tau) and np.array_equal(a.walkers, b.walkers)
+    a.run()
+    kw = dict(num_walkers=n, num_timesteps=100, equil_steps=10 ** 6, atoms=["O", "H", "H"], masses=m,
+              delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=11)
+    b, _ = replay(100, **kw)
+    ok = a._multi_used and np.array_equal(a._hist["pop"].cpu().numpy()[:100],
+                                          b._hist["pop"].cpu().numpy()[:100]) and np.array_equal(a.walkers, b.walkers)
     out[f"multi_{n}"] = [bool(ok), int(L.gbdmc_bounds_errors(1))]
 
 # continuous weighting with both thresholds (the reference fixture)

@@ -98,7 +98,7 @@ def test_python_surface_reproduces_the_fused_step(weighting):
               weighting=weighting)
     if weighting == "continuous":
         kw["cont_wt_thresh"] = [0.05, 3.0]
-    fused = pg.DMC_Sim(potential=pg.h2o_local_mode(), **kw)
+    fused = pg.DMC_Sim(potential=pg.h2o_local_mode(), fused_steps=0, **kw)  # the per-step kernels' noise
     fused.run()
     ext = pg.DMC_Sim(potential=pg.Potential_Direct(lambda c: oracle.pes_h2o_lm(c, p)), **kw)
     ext.run()
@@ -134,7 +134,7 @@ def test_device_tensor_potential_reproduces_the_fused_step():
     x0 = 0.1 * oracle.InjectedNoise(33).standard_normal((2000, 1, 3))
     kw = dict(num_walkers=2000, num_timesteps=30, equil_steps=10 ** 6, atoms=["H"], masses=ho["masses"],
               delta_t=10.0, start_structures=x0, seed=9, write_files=False)
-    fused = pg.DMC_Sim(potential=pg.harmonic_oscillator(), **kw)
+    fused = pg.DMC_Sim(potential=pg.harmonic_oscillator(), fused_steps=0, **kw)
     fused.run()
     pot = TorchHO(ho["k"])
     ext = pg.DMC_Sim(potential=pot, **kw)

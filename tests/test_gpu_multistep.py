@@ -1,9 +1,9 @@
 """The multi-step kernel (gbdmc_sim_run: many plain DMC steps per launch, the
-walkers resident in shared memory, one grid barrier per step) against the
-per-step kernels (gbdmc_sim_step).  Both draw the same Philox deviates and
-branching uniforms, so the trajectories agree: populations, walkers,
-ancestor indices and descendant weights bit for bit, vref within 1e-12 Eh
-(the multi-step kernel sums the per-block partials in another order)."""
+walkers resident in shared memory, the grid-wide reduction of a step behind
+the next step's move) against its walk replayed by the per-step kernels
+(gbdmc_sim_step on the same lineage-keyed Philox noise, tests/lineage_harness.py):
+populations, walkers and ancestor ids bit for bit, vref within 1e-12 Eh (the
+multi-step kernel adds the per-block sums in another order)."""
 import ctypes as C
 
 import numpy as np
@@ -12,40 +12,52 @@ import torch
 
 import oracle
 import pyvibdmc_gb300 as pg
+from lineage_harness import replay
 
 pytestmark = pytest.mark.gpu
+K = 64  # steps per launch (fused_steps)
 
 
-def _pair(**kw):
-    runs = []
-    for fused in (64, 0):
-        sim = pg.DMC_Sim(write_files=False, fused_steps=fused, **kw)
-        sim.run()
-        runs.append(sim)
-    return runs
+def _fused(**kw):
+    sim = pg.DMC_Sim(write_files=False, fused_steps=K, **kw)
+    sim.run()
+    return sim
 
 
-def _same(a, b):
-    np.testing.assert_array_equal(a._pop_vs_tau, b._pop_vs_tau)
-    np.testing.assert_allclose(a._vref_vs_tau, b._vref_vs_tau, rtol=0, atol=1e-12)
+def _who(sim):
+    sim._compact()
+    n = int(sim._read_ctrl().n)
+    return sim._bufs[sim._cur]["who"][:n].cpu().numpy()
+
+
+def _same(a, b, steps, who=True):
+    """a: the multi-step kernel's run, b: the replay."""
+    assert a._multi_used
+    pa = a._hist["pop"].cpu().numpy()[:steps]
+    pb = b._hist["pop"].cpu().numpy()[:steps]
+    np.testing.assert_array_equal(pa, pb)
+    np.testing.assert_allclose(a._hist["vref"].cpu().numpy()[:steps], b._hist["vref"].cpu().numpy()[:steps],
+                               rtol=0, atol=1e-12)
     assert np.array_equal(a.walkers, b.walkers)
+    if who:
+        assert np.array_equal(_who(a), _who(b))
 
 
 @pytest.mark.parametrize("n", [31, 33, 1025, 20000])
-def test_multi_step_kernel_follows_the_per_step_trajectory_h2o(n):
+def test_multi_step_kernel_follows_its_replayed_walk_h2o(n):
     p, m = oracle.h2o_config()
     x0 = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(5).standard_normal((n, 3, 3))
     steps = 200 if n > 1000 else 100
-    a, b = _pair(num_walkers=n, num_timesteps=steps, equil_steps=30, wfn_every=1000, desc_wt_steps=50,
-                 atoms=["O", "H", "H"], masses=m, delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0,
-                 seed=17)
-    assert a._multi_used and not b._multi_used
-    _same(a, b)
-    assert np.array_equal(a.wfns[0]["desc_wts"], b.wfns[0]["desc_wts"])
+    kw = dict(num_walkers=n, num_timesteps=steps, equil_steps=10 ** 6, atoms=["O", "H", "H"], masses=m,
+              delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=17)
+    a = _fused(**kw)
+    b, stopped = replay(steps, **kw)
+    assert not stopped
+    _same(a, b, steps)
 
 
 @pytest.mark.parametrize("system", ["ho", "dimer", "ps"])
-def test_multi_step_kernel_follows_the_per_step_trajectory(system):
+def test_multi_step_kernel_follows_its_replayed_walk(system):
     if system == "ho":
         ho = oracle.ho_config()
         kw = dict(atoms=["H"], masses=ho["masses"], potential=pg.harmonic_oscillator(),
@@ -59,23 +71,48 @@ def test_multi_step_kernel_follows_the_per_step_trajectory(system):
         x0 = np.array([[0.0, 0.0, 0.0], [1.81, 0.0, 0.0], [-0.45, 1.75, 0.0]])
         kw = dict(atoms=["O", "H", "H"], masses=m, potential=pg.partridge_schwenke(), num_walkers=4000,
                   start_structures=x0[None] + 0.03 * oracle.InjectedNoise(7).standard_normal((4000, 3, 3)))
-    a, b = _pair(num_timesteps=150, equil_steps=10 ** 6, delta_t=10.0, seed=23, **kw)
-    _same(a, b)
+    kw.update(num_timesteps=150, equil_steps=10 ** 6, delta_t=10.0, seed=23)
+    a = _fused(**kw)
+    b, stopped = replay(150, **kw)
+    assert not stopped
+    _same(a, b, 150)
+
+
+def test_descendant_windows_split_the_launches_not_the_walk():
+    """Events end launches: a descendant-weighting window from step 30 to 80
+    gives launches [0, 30), [30, 80), [80, 144), [144, 200); the lineage keys
+    travel with the walkers, so the walk is the replayed one, and the window's
+    descendant weights come from the ancestor ids the kernel carries."""
+    p, m = oracle.h2o_config()
+    n = 3000
+    x0 = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(15).standard_normal((n, 3, 3))
+    kw = dict(num_walkers=n, num_timesteps=200, equil_steps=30, wfn_every=1000, desc_wt_steps=50,
+              atoms=["O", "H", "H"], masses=m, delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0,
+              seed=19)
+    a = _fused(**kw)
+    assert a._multi_launches == 4
+    b, _ = replay(200, **dict(kw, equil_steps=10 ** 6))
+    _same(a, b, 200, who=False)  # the window restarts the ancestor ids at step 30
+    assert len(a.wfns) == 1
+    d = a.wfns[0]["desc_wts"]
+    assert d.sum() == int(a._hist["pop"].cpu().numpy()[79]) and len(d) == len(a.wfns[0]["coords"])
 
 
 def test_copies_that_pile_up_in_a_few_blocks_are_split_evenly():
-    """The walkers of the first blocks sit at the bottom of a harmonic well and the
-    others high up its side, so the first blocks' walkers multiply by a fifth every
-    step while the population stays near N0: every step splits the branched
-    population evenly over the blocks again, one launch runs all 40 steps, and
-    the trajectory is the per-step kernels'."""
+    """The walkers of the first blocks sit at the bottom of a harmonic well and
+    the others high up its side, so the first blocks' walkers multiply by a
+    fifth every step while the population stays near N0: the runs are split
+    evenly again whenever the largest would take another warp, one launch runs
+    all 40 steps, and the walk is the replayed one."""
     ho = oracle.ho_config()
     n = 2000
     x0 = np.zeros((n, 1, 3))
     x0[200:, 0, 0] = np.sqrt(2 * 0.02 / ho["k"])  # V = 0.02 Eh
-    a, b = _pair(num_walkers=n, num_timesteps=40, equil_steps=10 ** 6, atoms=["H"], masses=ho["masses"],
-                 delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=29)
-    _same(a, b)
+    kw = dict(num_walkers=n, num_timesteps=40, equil_steps=10 ** 6, atoms=["H"], masses=ho["masses"],
+              delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=29)
+    a = _fused(**kw)
+    b, _ = replay(40, **kw)
+    _same(a, b, 40)
     assert a._multi_launches == 1
 
 
@@ -86,17 +123,18 @@ def test_multi_step_guards_stop_with_the_moved_walkers():
     x0 = np.zeros((100, 1, 3))
     x0[:, 0, 0] = np.sqrt(2 * 2.0 / ho["k"])
     x0[37, 0, 0] = 0.0  # a huge weight for walker 37 on the first step
-    out = []
-    for fused in (64, 0):
-        sim = pg.DMC_Sim(num_walkers=100, num_timesteps=20, equil_steps=1000, atoms=["H"], masses=ho["masses"],
-                         delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=3,
-                         write_files=False, fused_steps=fused)
-        with pytest.raises(ValueError, match="Massive walker"):
-            sim.run()
-        c = sim._read_ctrl()
-        out.append((int(c.n), int(c.err_step), sim._coords_host()))
-    assert out[0][0] == out[1][0] == 100 and out[0][1] == out[1][1] == 0
-    assert np.array_equal(out[0][2], out[1][2])
+    kw = dict(num_walkers=100, num_timesteps=20, equil_steps=1000, atoms=["H"], masses=ho["masses"],
+              delta_t=10.0, potential=pg.harmonic_oscillator(), start_structures=x0, seed=3)
+    sim = pg.DMC_Sim(write_files=False, fused_steps=K, **kw)
+    with pytest.raises(ValueError, match="Massive walker"):
+        sim.run()
+    c = sim._read_ctrl()
+    b, stopped = replay(20, **kw)
+    assert stopped
+    cb = b._read_ctrl()
+    assert int(c.n) == int(cb.n) == 100 and int(c.err_step) == int(cb.err_step) == 0
+    assert int(c.status) == int(cb.status)
+    assert np.array_equal(sim._coords_host(), b._coords_host())
 
 
 def test_sim_run_entry_point_checks_its_arguments():
@@ -108,3 +146,27 @@ def test_sim_run_entry_point_checks_its_arguments():
                          C.c_void_p(16), 10, 4, None)
     assert rc == pg._capi.ERR_ARG and b"discrete" in L.gbdmc_last_error()
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("mode", ["philox32", "philox64"])
+def test_lineage_noise_matches_the_oracle_stream(mode):
+    """gbdmc_lineage_noise (the multi-step kernel's noise) against the oracle's
+    restatement of the lineage-keyed Philox stream: every deviate (8 fp32 ulps
+    in philox32, whose log/sin/cos differ from NumPy's in the last bits; 1e-12
+    in philox64) and every branching uniform exactly."""
+    from oracle.philox_oracle import philox_normals, lineage_key
+    L = pg._capi.load()
+    n, seed, step = 4096, 0x0123456789ABCDEF, 77
+    keys = lineage_key(np.arange(n, dtype=np.uint64) * np.uint64(7919), np.arange(n) % 3, 12)
+    s = pg._capi.Sim(natoms=3, seed=seed, replica_id=5)
+    s.noise_mode = pg._capi.NOISE_PHILOX32 if mode == "philox32" else pg._capi.NOISE_PHILOX64
+    kd = torch.as_tensor(keys.view(np.int64), device="cuda")
+    z = torch.empty((9, n), dtype=torch.float64, device="cuda")
+    u = torch.empty(n, dtype=torch.float64, device="cuda")
+    pg._capi.check(L.gbdmc_lineage_noise(C.byref(s), C.c_void_p(kd.data_ptr()), n, step, C.c_void_p(z.data_ptr()), n,
+                                         C.c_void_p(u.data_ptr()), None))
+    torch.cuda.synchronize()
+    zr, st = philox_normals(seed, step, keys, 9, mode, replica=5, lineage=True)
+    tol = dict(rtol=1e-6, atol=1e-6) if mode == "philox32" else dict(rtol=0, atol=1e-12)
+    np.testing.assert_allclose(z.cpu().numpy(), zr, **tol)
+    np.testing.assert_array_equal(u.cpu().numpy(), st.uniform53())

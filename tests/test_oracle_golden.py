@@ -395,3 +395,22 @@ def test_ps_oracle_is_near_zero_at_its_expansion_centre():
     v = pes_ps(ohh)
     assert abs(v[0]) < 1.0 * oracle.WAVENUMBERS
     np.testing.assert_allclose(pes_ps(ohh[:, [1, 2, 0]], order="HHO"), v, rtol=0, atol=1e-15)
+
+
+def test_lineage_keys_stay_distinct_through_branching():
+    """The multi-step kernel's walkers are named by lineage keys (copy 0 keeps
+    its parent's key, copy r >= 1 derives one from the parent's key, r and the
+    step): through 300 steps of random births and deaths every key in the
+    population stays distinct, including for walkers that branch at several
+    steps, so no two walkers ever share a Philox stream."""
+    from oracle.philox_oracle import lineage_key
+    g = np.random.default_rng(3)
+    keys = np.arange(2000, dtype=np.uint64)
+    for step in range(300):
+        c = g.choice([0, 0, 1, 1, 1, 1, 2, 3], size=len(keys), p=None)  # mean 9/8
+        if c.sum() > 3000:  # population control, as vref does
+            c[np.flatnonzero(c > 1)[: c.sum() - 2000]] = 1
+        a = np.repeat(np.arange(len(keys)), c)
+        first = np.searchsorted(a, a, side="left")
+        keys = lineage_key(keys[a], np.arange(len(a)) - first, step)
+        assert len(np.unique(keys)) == len(keys), step
