@@ -374,9 +374,12 @@ size_t gbdmc_struct_size(int32_t which);
 
 /* ---- MLP surrogate of the water-dimer PES (BF16 tensor cores, FP32 accumulation) ----
  * Replaces the user model behind NN_Potential.getpot
- * (simulation_utilities/potential_manager.py:177-214) and the distance
- * descriptor of DistIt (tensorflow_descriptors/distance_descriptors.py:102-113,
- * method 'distance' inverted): 15 inverse O/H distances -> 3 x 128 SiLU -> 1.
+ * (simulation_utilities/potential_manager.py:177-214) and the descriptor of
+ * DistIt (tensorflow_descriptors/distance_descriptors.py:102-113, 154-165, 177-213):
+ * the upper triangle of the Coulomb matrix z_i z_j / r_ij, normalised per
+ * pair (which absorbs the charges, so the network sees (1/r - mu) / sd),
+ * optionally in DistIt's sorted atom order (sort_atoms):
+ * 15 descriptors -> 3 x 128 SiLU -> 1.
  * Weight matrices are bf16 and stored transposed (n-major): wNt[n*K + k]. */
 #define GBDMC_MLP_HIDDEN 128
 #define GBDMC_MLP_INPUT 16 /* 15 features, padded */
@@ -401,7 +404,11 @@ typedef struct {
   int32_t engine;      /* 0: mma.sync BF16 kernels; 1: tcgen05 (TMEM accumulators, one thread per walker) */
   float bias_beta;     /* online bias control: c <- (1-b) c + b <V_nn - V_analytic>_audit each step, and the
                           next step's surrogate energies are V_nn - c (0 = off) */
-  int32_t pad;
+  int32_t sort_atoms;  /* 1: descriptors in the canonical atom order of DistIt(method='coulomb',
+                          sorted_atoms=[[0],[1,2],[3],[4,5]], sorted_groups=[[0,1,2],[3,4,5]])
+                          (distance_descriptors.py:115-152): the hydrogens of each water by the column
+                          norms of the Coulomb matrix, then the waters by their columns' summed norms;
+                          0: the given order */
 } gbdmc_mlp_t;
 
 /* fp32-coordinate walkers of the surrogate path (SoA [18][ld]).  With a trial
@@ -438,19 +445,23 @@ int gbdmc_mlp_head(const float* h3_dev, const float* ht3_dev, const float* w4_de
 int gbdmc_mlp_adam(float* p_dev, const float* g_dev, float* m_dev, float* v_dev, int64_t n, float lr, float beta1,
                    float beta2, float eps, int32_t t, uint16_t* wt_dev, uint16_t* wn_dev, int32_t k, void* stream);
 /* Normalised descriptors of n dimers (fp64 SoA [18][ld]); with vdir (SoA, may be NULL) also the normalised
- * directional derivative of the descriptors and et = (dV/dx . v) / e_scale from grad (SoA). */
+ * directional derivative of the descriptors and et = (dV/dx . v) / e_scale from grad (SoA).  sort_atoms as in
+ * gbdmc_mlp_t (the descriptors and their derivatives in the canonical atom order). */
 int gbdmc_dimer_features(const double* x_dev, int64_t ld, int64_t n, const float* mu_dev, const float* inv_sd_dev,
                          const double* vdir_dev, const double* grad_dev, float e_scale, float* feat_dev,
-                         float* tang_dev, float* et_dev, void* stream);
+                         float* tang_dev, float* et_dev, int32_t sort_atoms, void* stream);
 /* Surrogate energies of n walkers (fp32 SoA [18][ld]); outside_dev[i] = 1 for walkers outside the training box
  * (may be NULL; not cleared).  With net->engine == 1 (tcgen05) status_dev (device int, required) is set to 1 if a
  * bounded wait for the tensor cores gave up.  n = 0 reads and writes nothing. */
 int gbdmc_mlp_energy(const gbdmc_mlp_t* net, const float* x_dev, int64_t ld, int64_t n, double* v_dev,
                      int32_t* outside_dev, int32_t* status_dev, void* stream);
 /* Surrogate DMC (discrete weighting, fp32 coordinates, sim->pes = the analytic dimer PES used for the audit
- * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[8] (zeroed by the caller before
+ * subset and the out-of-box fallback).  Step 0 energies are analytic.  audit_dev[9] (zeroed by the caller before
  * the first step): [0] audited walkers, [1] sum (V_nn - V_analytic), [2] sum (V_nn - V_analytic)^2,
- * [3] fallbacks, [4] current bias correction c (hartree), [5..7] bookkeeping of the bias control.
+ * [3] fallbacks, [4] the mixed-average bias correction c_mix (hartree: the moving average of the audited
+ * errors), [5..7] bookkeeping of the bias control, [8] an offset the caller may set between steps (the
+ * difference of the pure and mixed averages of the error, gbdmc_mlp_fw_*); the surrogate energies of a step
+ * are V_nn - (c_mix + offset).
  * With sim->trial.kind = GBDMC_TRIAL_DIMER_GAUSS (tcgen05 engine only) the step is importance sampled
  * (pyvibdmc.py:549-612 in fp32: drift-diffusion proposal, trial at the proposal, Metropolis test, local
  * energy V_nn + KE, weights with dt_eff = dt * accepted / N).  The batch_ forms run nrep replicas laid out
@@ -463,6 +474,21 @@ int gbdmc_mlp_sim_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbd
                        const gbdmc_noise_t* noise, void* stream);
 int gbdmc_mlp_compact(const gbdmc_sim_t* sim, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
                       const gbdmc_ctrl_t* ctrl_dev, void* stream);
+/* Forward walking of the surrogate's error delta = V_nn - V_analytic (the descendant weights of
+ * pyvibdmc.py:663-672 applied to delta): the pure-distribution average sum_s D_s delta_s / sum_s D_s over
+ * a window, D_s the descendants of walker s at the window's end, against the mixed average over the same
+ * walkers.  The walkers must be compact (gbdmc_mlp_batch_compact).  fw_begin: vnn_dev and outside_dev are
+ * gbdmc_mlp_energy of the ld slots (outside_dev zeroed before); every live slot s gets who[s] = s and
+ * delta_dev[s] = V_nn - V_analytic(fp32) (0 outside the training box).  fw_end: over the live walkers,
+ * delta_dev[who].  Both write part_dev[2 * GBDMC_FW_BLOCKS]: per block (sum, count), to be summed in block
+ * order.  reps/nrep as for gbdmc_mlp_batch_step. */
+#define GBDMC_FW_BLOCKS 512
+int gbdmc_mlp_fw_begin(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                       const gbdmc_walkers_f32_t* w, const gbdmc_ctrl_t* ctrl_dev, const double* vnn_dev,
+                       const int32_t* outside_dev, double* delta_dev, double* part_dev, void* stream);
+int gbdmc_mlp_fw_end(const gbdmc_sim_t* sim, const gbdmc_replica_t* reps, int32_t nrep,
+                     const gbdmc_walkers_f32_t* w, const gbdmc_ctrl_t* ctrl_dev, const double* delta_dev,
+                     double* part_dev, void* stream);
 int gbdmc_mlp_batch_init(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps, int32_t nrep,
                          const gbdmc_walkers_f32_t* w, gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, void* stream);
 int gbdmc_mlp_batch_step(const gbdmc_sim_t* sim, const gbdmc_mlp_t* net, const gbdmc_replica_t* reps, int32_t nrep,

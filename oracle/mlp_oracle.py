@@ -12,7 +12,9 @@ silu'').
 import numpy as np
 
 __all__ = ["mlp_forward", "mlp_loss_grads", "silu", "dsilu", "d2silu", "inv_dist_features", "bf16", "f32",
-           "mlp_energy_tc", "mlp_loss_grads_bf16"]
+           "mlp_energy_tc", "mlp_loss_grads_bf16", "dimer_sort_perm", "DIMER_Z"]
+
+DIMER_Z = np.array([8.0, 1.0, 1.0, 8.0, 1.0, 1.0])  # O, H, H, O, H, H
 
 
 def silu(z):
@@ -67,8 +69,50 @@ def mlp_loss_grads(P, D, U, e, et, wE=1.0, wF=0.5):
     return G, loss
 
 
-def inv_dist_features(x, v=None):
-    """1/r_ij (15 pairs, i<j) and their directional derivative along v, (N,6,3) inputs."""
+def dimer_sort_perm(x):
+    """Canonical atom order of water dimers, (N,6,3) -> (N,6) permutations
+    (position p holds atom perm[:, p]) and the relative margins of the three
+    decisions (N,3), restating DistIt with method 'coulomb',
+    sorted_atoms=[[0],[1,2],[3],[4,5]] and sorted_groups=[[0,1,2],[3,4,5]]
+    (tensorflow_descriptors/distance_descriptors.py:115-152, 177-213):
+      - Coulomb matrix M_ij = z_i z_j / r_ij, M_ii = z_i^2.4 / 2 (:154-165);
+      - sort_atoms (:115-131): within each group of like atoms, descending
+        column norm of M (NumPy's argsort of -norm over six entries is an
+        insertion sort, so ties keep the given order);
+      - sort_groups (:133-152), on the atom-sorted matrix: the groups by
+        descending sum of their columns' norms (the same sums, since atom
+        sorting permutes columns within a group)."""
+    x = np.asarray(x, dtype=np.float64)
+    z = DIMER_Z
+    d = x[:, :, None, :] - x[:, None, :, :]
+    r = np.sqrt((d ** 2).sum(-1))
+    n = len(x)
+    M = np.empty((n, 6, 6))
+    off = ~np.eye(6, dtype=bool)
+    M[:, off] = (np.outer(z, z)[off])[None] / r[:, off]
+    M[:, np.arange(6), np.arange(6)] = 0.5 * z ** 2.4
+    cn = np.linalg.norm(M, axis=1)
+    perm = np.tile(np.arange(6), (n, 1))
+    sa = cn[:, 2] > cn[:, 1]
+    sb = cn[:, 5] > cn[:, 4]
+    perm[sa, 1], perm[sa, 2] = 2, 1
+    perm[sb, 4], perm[sb, 5] = 5, 4
+    ta, tb = cn[:, :3].sum(1), cn[:, 3:].sum(1)
+    sg = tb > ta
+    perm[sg] = perm[sg][:, [3, 4, 5, 0, 1, 2]]
+    marg = np.stack([np.abs(cn[:, 2] - cn[:, 1]) / cn[:, 1], np.abs(cn[:, 5] - cn[:, 4]) / cn[:, 4],
+                     np.abs(tb - ta) / ta], 1)
+    return perm, marg
+
+
+def inv_dist_features(x, v=None, sort=False):
+    """1/r_ij (15 pairs, i<j) and their directional derivative along v, (N,6,3)
+    inputs; with sort, of the atoms in the canonical order of dimer_sort_perm."""
+    if sort:
+        perm, _ = dimer_sort_perm(x)
+        rows = np.arange(len(x))[:, None]
+        x = np.asarray(x)[rows, perm]
+        v = None if v is None else np.asarray(v)[rows, perm]
     f, t = [], []
     for i in range(6):
         for j in range(i + 1, 6):
@@ -94,7 +138,7 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale):
+def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale, sort=False):
     """The tcgen05 inference kernel's arithmetic with its rounding points
     (gbdmc_mlp_tc.cu): fp32 walkers; descriptors 1/r scaled to (1/r - mu)/sd in
     fp32 and rounded to bf16 as the A operand; hidden layers with the weights
@@ -104,9 +148,9 @@ def mlp_energy_tc(P, x, mu, inv_sd, e_mean, e_scale):
     kernel's tanh.approx.f32 differs by at most 2^-10.99 relative); the
     activations of layers 1 and 2 rounded to bf16, layer 3's kept in fp32;
     the output h3 . w4 + b4 and V = e_mean + e_scale * output.  (N, 6, 3)
-    fp64 coordinates in, V (N,) out."""
+    fp64 coordinates in, V (N,) out; sort as in inv_dist_features."""
     x = f32(x)
-    f, _ = inv_dist_features(x)
+    f, _ = inv_dist_features(x, sort=sort)
     scale = f32(inv_sd[:15])
     shift = f32(-f32(mu[:15]) * scale)
     D = np.zeros((len(x), 16))

@@ -56,6 +56,7 @@ class Sim(C.Structure):
 
 
 MAX_REPLICAS = 64
+FW_BLOCKS = 512  # GBDMC_FW_BLOCKS
 
 
 class Replica(C.Structure):
@@ -74,7 +75,7 @@ class MLP(C.Structure):
                 ("e_mean", C.c_float), ("e_scale", C.c_float), ("hull_margin", C.c_float),
                 ("feat_mu", C.c_float * 16), ("feat_inv_sd", C.c_float * 16), ("feat_lo", C.c_float * 16),
                 ("feat_hi", C.c_float * 16), ("audit_every", C.c_int32), ("engine", C.c_int32),
-                ("bias_beta", C.c_float), ("pad", C.c_int32)]
+                ("bias_beta", C.c_float), ("sort_atoms", C.c_int32)]
 
 
 class WalkersF32(C.Structure):
@@ -139,7 +140,7 @@ def load():
         "gbdmc_mlp_head": ([P, P, P, C.c_float, P, P, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P], C.c_int),
         "gbdmc_mlp_adam": ([P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P, P,
                             C.c_int32, P], C.c_int),
-        "gbdmc_dimer_features": ([P, C.c_int64, C.c_int64, P, P, P, P, C.c_float, P, P, P, P], C.c_int),
+        "gbdmc_dimer_features": ([P, C.c_int64, C.c_int64, P, P, P, P, C.c_float, P, P, P, C.c_int32, P], C.c_int),
         "gbdmc_mlp_energy": ([C.POINTER(MLP), P, C.c_int64, C.c_int64, P, P, P, P], C.c_int),
         "gbdmc_mlp_sim_init": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), P, P, P], C.c_int),
         "gbdmc_mlp_sim_step": ([C.POINTER(Sim), C.POINTER(MLP), C.POINTER(WalkersF32), C.POINTER(WalkersF32), P, P,
@@ -151,6 +152,8 @@ def load():
                                   C.POINTER(WalkersF32), P, P, P, C.POINTER(Noise), P], C.c_int),
         "gbdmc_mlp_batch_compact": ([C.POINTER(Sim), P, C.c_int32, C.POINTER(WalkersF32), C.POINTER(WalkersF32),
                                      P, P], C.c_int),
+        "gbdmc_mlp_fw_begin": ([C.POINTER(Sim), P, C.c_int32, C.POINTER(WalkersF32), P, P, P, P, P, P], C.c_int),
+        "gbdmc_mlp_fw_end": ([C.POINTER(Sim), P, C.c_int32, C.POINTER(WalkersF32), P, P, P, P], C.c_int),
         "gbdmc_sim_step_static": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, C.POINTER(Noise), P],
                                   C.c_int),
         "gbdmc_sim_step_static_max_ld": ([], C.c_size_t),

@@ -267,13 +267,16 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, floa
 
 // ------------------------------------------------------------- features
 // Inverse distances of the 15 atom pairs (i<j, combinations order of the
-// reference's descriptor, tensorflow_descriptors/distance_descriptors.py:66-68)
-// normalised (d - mu) * inv_sd; with a direction v, also the normalised
-// directional derivative u = (dd/dx) v, and et = (dV/dx . v) / e_scale.
+// reference's descriptor, tensorflow_descriptors/distance_descriptors.py:66-68),
+// with sorted in the canonical atom order of dimer_sort_pairs, normalised
+// (d - mu) * inv_sd; with a direction v, also the normalised directional
+// derivative u = (dd/dx) v (permuted with the descriptors), and et = (dV/dx .
+// v) / e_scale (a permutation of equivalent atoms leaves V unchanged).
 template <typename T>
 __global__ void k_features(const T* __restrict__ x, long long ldx, long long n, const float* __restrict__ mu,
                            const float* __restrict__ inv_sd, const T* __restrict__ vdir, const double* __restrict__ grad,
-                           float e_scale, float* __restrict__ feat, float* __restrict__ tang, float* __restrict__ et) {
+                           float e_scale, float* __restrict__ feat, float* __restrict__ tang, float* __restrict__ et,
+                           int sorted) {
   for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (long long)gridDim.x * blockDim.x) {
     float xs[18], vs[18];
 #pragma unroll
@@ -281,20 +284,25 @@ __global__ void k_features(const T* __restrict__ x, long long ldx, long long n, 
       xs[k] = (float)x[k * ldx + s];
       vs[k] = vdir ? (float)vdir[k * ldx + s] : 0.f;
     }
+    float ir[15], tg[15];
     int q = 0;
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
 #pragma unroll
       for (int j = i + 1; j < 6; ++j) {
         const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
-        const float ir = rsqrtf(dx * dx + dy * dy + dz * dz);
-        feat[s * kIn + q] = (ir - mu[q]) * inv_sd[q];
-        if (tang) {
-          const float dvx = vs[3 * i] - vs[3 * j], dvy = vs[3 * i + 1] - vs[3 * j + 1], dvz = vs[3 * i + 2] - vs[3 * j + 2];
-          tang[s * kIn + q] = -(dx * dvx + dy * dvy + dz * dvz) * ir * ir * ir * inv_sd[q];
-        }
+        const float r = rsqrtf(dx * dx + dy * dy + dz * dz);
+        const float dvx = vs[3 * i] - vs[3 * j], dvy = vs[3 * i + 1] - vs[3 * j + 1], dvz = vs[3 * i + 2] - vs[3 * j + 2];
+        ir[q] = r;
+        tg[q] = -(dx * dvx + dy * dvy + dz * dvz) * r * r * r;
         ++q;
       }
+    }
+    if (sorted) dimer_sort_pairs<true>(ir, tg);
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      feat[s * kIn + k] = (ir[k] - mu[k]) * inv_sd[k];
+      if (tang) tang[s * kIn + k] = tg[k] * inv_sd[k];
     }
     feat[s * kIn + 15] = 0.f;
     if (tang) tang[s * kIn + 15] = 0.f;
@@ -447,7 +455,7 @@ __global__ void __launch_bounds__(256) k_mlp_move_energy(const __grid_constant__
                                                           const __grid_constant__ FeatBox B) {
   extern __shared__ __align__(16) unsigned char smraw[];
   MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smraw);
-  const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
+  const double corr = audit ? audit[4] + audit[8] : 0.0;  // online bias correction (hartree)
   load_net(sm, net);
   __syncthreads();
   const int64_t ld = S.ld;
@@ -531,7 +539,8 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntile2; t += gridDim.x * blockDim.x) tstat[t] = 0ull;
   if (blockIdx.x == 0 && threadIdx.x < 2) sync[threadIdx.x] = 0u;
   const int64_t ld = S.ld;
-  const double c_used = *(volatile const double*)(audit + 4);  // correction applied to this step's V_nn
+  const double c_mix = *(volatile const double*)(audit + 4);  // mixed-average part of the correction
+  const double c_used = c_mix + audit[8];                        // correction applied to this step's V_nn
   const int nrep = T.nrep;
   const int wpb = blockDim.x >> 5;
   if (threadIdx.x < 32) {
@@ -606,7 +615,9 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
       if (t != 0.0) atomicAdd(audit + threadIdx.x, t);
     }
   }
-  // last block: c <- (1 - beta) c + beta * (mean audited error of this step)
+  // last block: c_mix <- (1 - beta) c_mix + beta * (mean audited error of this
+  // step); the next step applies c_mix + audit[8] (the pure-weighting offset
+  // the host sets from forward-walking windows, 0 without them)
   __shared__ bool am_last;
   __threadfence();
   __syncthreads();
@@ -619,7 +630,7 @@ __global__ void __launch_bounds__(128) k_mlp_audit(const __grid_constant__ gbdmc
     __threadfence();
     const double cnt = *(volatile double*)(audit + 0) - audit[5];
     const double sum = *(volatile double*)(audit + 1) - audit[6];
-    if (beta > 0.f && cnt > 0.0) audit[4] = (1.0 - (double)beta) * c_used + (double)beta * (sum / cnt);
+    if (beta > 0.f && cnt > 0.0) audit[4] = (1.0 - (double)beta) * c_mix + (double)beta * (sum / cnt);
     audit[5] = audit[0];
     audit[6] = audit[1];
     *reinterpret_cast<unsigned long long*>(audit + 7) = 0ull;
@@ -762,8 +773,68 @@ static int set_mlp_smem(const void* fn) {
   return GBDMC_OK;
 }
 
+// ---------------------------------------------------- forward walking
+// The descendant-weighted (pure-distribution) average of the surrogate's
+// error delta = V_nn - V_analytic, the forward-walking estimator of the
+// descendant weights of pyvibdmc.py:663-672 applied to delta.  At a window's
+// start every live walker s of the compact population gets who[s] = s and
+// delta[s]; the step kernels carry who to the copies; at the window's end
+// summing delta[who] over the live population gives sum_s D_s delta_s, D_s
+// the number of descendants of s.  Each block writes its partial (sum,
+// count), replicas and walkers visited in a fixed order, so the host's sum
+// in block order is reproducible.
+constexpr int kFwThreads = 256;
+
+template <bool BEGIN>
+__global__ void __launch_bounds__(kFwThreads) k_fw(const __grid_constant__ RepTable T,
+                                                   const gbdmc_ctrl_t* __restrict__ ctrls, const float* __restrict__ x,
+                                                   int64_t ld, int32_t* __restrict__ who,
+                                                   const double* __restrict__ vnn, const int32_t* __restrict__ outside,
+                                                   const __grid_constant__ StepF32 P, double* __restrict__ delta,
+                                                   double* __restrict__ part) {
+  double s_d = 0.0, s_n = 0.0;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < T.nrep; ++r) {
+    const int64_t cap = T.cap[r], off = T.off[r];
+    int64_t n = ctrls[r].n;
+    n = n < 0 ? 0 : (n > cap ? cap : n);
+    for (int64_t i = tid; i < n; i += nth) {
+      const int64_t s = off + i;
+      double d;
+      if constexpr (BEGIN) {
+        float xs[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) xs[k] = x[k * ld + s];
+        d = outside[s] ? 0.0 : vnn[s] - (double)dimer_energy_f32(xs, P.pes);
+        delta[s] = d;
+        who[s] = (int32_t)s;
+      } else {
+        const int32_t a = who[s];
+        if (a < 0 || (int64_t)a >= ld) continue;  // not in an open window: not counted
+        d = delta[a];
+      }
+      s_d += d;
+      s_n += 1.0;
+    }
+  }
+  __shared__ double red[kFwThreads / 32][2];
+  s_d = warp_sum(s_d);
+  s_n = warp_sum(s_n);
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5][0] = s_d;
+    red[threadIdx.x >> 5][1] = s_n;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double t = 0.0;
+    for (int w = 0; w < kFwThreads / 32; ++w) t += red[w][threadIdx.x];
+    part[2 * blockIdx.x + threadIdx.x] = t;
+  }
+}
+
 static bool valid_net(const gbdmc_mlp_t* net) {
-  return net && net->w1t && net->w2t && net->w3t && net->b1 && net->b2 && net->b3 && net->w4;
+  return net && net->w1t && net->w2t && net->w3t && net->b1 && net->b2 && net->b3 && net->w4 &&
+         (net->sort_atoms == 0 || net->sort_atoms == 1);
 }
 
 GBDMC_BOUNDS_READER(bounds_read_mlp)
@@ -851,14 +922,15 @@ extern "C" int gbdmc_mlp_adam(float* p, const float* g, float* m, float* v, int6
 
 extern "C" int gbdmc_dimer_features(const double* x, int64_t ld, int64_t n, const float* mu, const float* inv_sd,
                                     const double* vdir, const double* grad, float e_scale, float* feat, float* tang,
-                                    float* et, void* stream) {
-  if (!x || !mu || !inv_sd || !feat || n < 0 || ld < n || (vdir && !tang) || (et && (!vdir || !grad))) {
+                                    float* et, int32_t sort_atoms, void* stream) {
+  if (!x || !mu || !inv_sd || !feat || n < 0 || ld < n || (vdir && !tang) || (et && (!vdir || !grad)) ||
+      sort_atoms < 0 || sort_atoms > 1) {
     set_error("gbdmc_dimer_features: invalid arguments");
     return GBDMC_ERR_ARG;
   }
   if (n == 0) return GBDMC_OK;
   k_features<double><<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(x, ld, n, mu, inv_sd, vdir, grad, e_scale, feat,
-                                                                     vdir ? tang : nullptr, et);
+                                                                     vdir ? tang : nullptr, et, sort_atoms);
   return check_launch("gbdmc_dimer_features");
 }
 
@@ -1072,4 +1144,35 @@ extern "C" int gbdmc_mlp_batch_compact(const gbdmc_sim_t* S, const gbdmc_replica
 extern "C" int gbdmc_mlp_compact(const gbdmc_sim_t* S, const gbdmc_walkers_f32_t* in, const gbdmc_walkers_f32_t* out,
                                  const gbdmc_ctrl_t* ctrl, void* stream) {
   return gbdmc_mlp_batch_compact(S, nullptr, 0, in, out, ctrl, stream);
+}
+
+extern "C" int gbdmc_mlp_fw_begin(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                  const gbdmc_walkers_f32_t* w, const gbdmc_ctrl_t* ctrl, const double* vnn,
+                                  const int32_t* outside, double* delta, double* part, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, reps, nrep, T, "gbdmc_mlp_fw_begin");
+  if (rc) return rc;
+  if (!w || !w->x || !w->who || !ctrl || !vnn || !outside || !delta || !part) {
+    set_error("gbdmc_mlp_fw_begin: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  k_fw<true><<<GBDMC_FW_BLOCKS, kFwThreads, 0, (cudaStream_t)stream>>>(T, ctrl, w->x, S->ld, w->who, vnn, outside,
+                                                                        step_f32(*S), delta, part);
+  return check_launch("gbdmc_mlp_fw_begin");
+}
+
+extern "C" int gbdmc_mlp_fw_end(const gbdmc_sim_t* S, const gbdmc_replica_t* reps, int32_t nrep,
+                                const gbdmc_walkers_f32_t* w, const gbdmc_ctrl_t* ctrl, const double* delta,
+                                double* part, void* stream) {
+  RepTable T;
+  int rc = mlp_table(S, reps, nrep, T, "gbdmc_mlp_fw_end");
+  if (rc) return rc;
+  if (!w || !w->who || !ctrl || !delta || !part) {
+    set_error("gbdmc_mlp_fw_end: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  k_fw<false><<<GBDMC_FW_BLOCKS, kFwThreads, 0, (cudaStream_t)stream>>>(T, ctrl, nullptr, S->ld, w->who, nullptr,
+                                                                         nullptr, step_f32(*S), const_cast<double*>(delta),
+                                                                         part);
+  return check_launch("gbdmc_mlp_fw_end");
 }

@@ -234,9 +234,11 @@ __device__ __forceinline__ float dimer_energy_f32(const float (&x)[18], const fl
 
 // The descriptor normalisation and training box of a network, prepared on
 // the host: f_q = r_q scale_q + shift_q (scale = 1/sd, shift = -mu/sd) and
-// the box [lo_q - margin, hi_q + margin].
+// the box [lo_q - margin, hi_q + margin]; sorted: the atoms are put in the
+// canonical order of dimer_sort_pairs before the descriptors are formed.
 struct FeatBox {
   float scale[15], shift[15], lo[15], hi[15];
+  int sorted;
 };
 
 inline FeatBox feat_box(const gbdmc_mlp_t& net) {
@@ -247,25 +249,96 @@ inline FeatBox feat_box(const gbdmc_mlp_t& net) {
     B.lo[q] = net.feat_lo[q] - net.hull_margin;
     B.hi[q] = net.feat_hi[q] + net.hull_margin;
   }
+  B.sorted = net.sort_atoms != 0;
   return B;
 }
 
-// Descriptors of one walker into the warp's feature row (15 normalised inverse
-// pair distances, then a zero pad); returns true when the walker lies outside
-// the training box.
-__device__ __forceinline__ bool walker_features(const float (&xs)[18], const FeatBox& B, float* row) {
+// Exchange a[i] and a[j] when c (selects, no divergence).
+template <typename A>
+__device__ __forceinline__ void cswap(bool c, A&& a, int i, int j) {
+  const float u = a[i], w = a[j];
+  a[i] = c ? w : u;
+  a[j] = c ? u : w;
+}
+
+// Pair index of atoms (i, j), i < j, in itertools.combinations order:
+// (0,1) 0, (0,2) 1, (0,3) 2, (0,4) 3, (0,5) 4, (1,2) 5, (1,3) 6, (1,4) 7,
+// (1,5) 8, (2,3) 9, (2,4) 10, (2,5) 11, (3,4) 12, (3,5) 13, (4,5) 14.
+//
+// The water dimer (O,H,H,O,H,H) in the canonical atom order of DistIt with
+// method 'coulomb', sorted_atoms [[0],[1,2],[3],[4,5]] and sorted_groups
+// [[0,1,2],[3,4,5]] (tensorflow_descriptors/distance_descriptors.py:115-152,
+// 154-165, 177-213).  On the Coulomb matrix M (M_ij = z_i z_j / r_ij, M_ii = z_i^2.4
+// / 2, z = 8, 1, 1, 8, 1, 1):
+//   1. in each water the hydrogen with the larger column norm of M first;
+//   2. the water whose columns' norms sum higher first.
+// Decided on ir (the 15 inverse pair distances, original order); applies the
+// atom permutation to the pair values ir and, when t is given, t (the
+// directional derivatives of the same descriptors).  A permutation of
+// equivalent atoms leaves the descriptor values of a walker unchanged as a
+// set, so every copy of a geometry under the dimer's eight-element
+// permutation group gets the same descriptors.  Ties keep the given order.
+template <bool TANG, typename A, typename Tg>
+__device__ __forceinline__ void dimer_sort_pairs(A&& ir, Tg&& t) {
+  // Column c of M has norm sqrt(M_cc^2 + z_c^2 s_c), s_c = sum_{i != c} z_i^2 / r_ic^2.
+  // Two hydrogens of a water share z and M_cc, so their norms order as their s.
+  float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  {
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+      for (int j = i + 1; j < 6; ++j) {
+        const float w = ir[q] * ir[q];
+        s[i] = fmaf((j % 3 == 0) ? 64.f : 1.f, w, s[i]);
+        s[j] = fmaf((i % 3 == 0) ? 64.f : 1.f, w, s[j]);
+        ++q;
+      }
+    }
+  }
+  const bool sA = s[2] > s[1], sB = s[5] > s[4];
+  constexpr float dO2 = 5404.7044f;  // (8^2.4 / 2)^2 = 5404.70440...
+  constexpr float dH2 = 0.25f;       // (1^2.4 / 2)^2
+  const float nA = sqrtf(fmaf(64.f, s[0], dO2)) + sqrtf(dH2 + s[1]) + sqrtf(dH2 + s[2]);
+  const float nB = sqrtf(fmaf(64.f, s[3], dO2)) + sqrtf(dH2 + s[4]) + sqrtf(dH2 + s[5]);
+  const bool sG = nB > nA;
+  // 1. hydrogens 1 <-> 2, then 4 <-> 5
+  cswap(sA, ir, 0, 1), cswap(sA, ir, 6, 9), cswap(sA, ir, 7, 10), cswap(sA, ir, 8, 11);
+  cswap(sB, ir, 3, 4), cswap(sB, ir, 7, 8), cswap(sB, ir, 10, 11), cswap(sB, ir, 12, 13);
+  // 2. waters (0,1,2) <-> (3,4,5)
+  cswap(sG, ir, 0, 12), cswap(sG, ir, 1, 13), cswap(sG, ir, 3, 6), cswap(sG, ir, 4, 9), cswap(sG, ir, 5, 14),
+      cswap(sG, ir, 8, 10);
+  if constexpr (TANG) {
+    cswap(sA, t, 0, 1), cswap(sA, t, 6, 9), cswap(sA, t, 7, 10), cswap(sA, t, 8, 11);
+    cswap(sB, t, 3, 4), cswap(sB, t, 7, 8), cswap(sB, t, 10, 11), cswap(sB, t, 12, 13);
+    cswap(sG, t, 0, 12), cswap(sG, t, 1, 13), cswap(sG, t, 3, 6), cswap(sG, t, 4, 9), cswap(sG, t, 5, 14),
+        cswap(sG, t, 8, 10);
+  }
+}
+
+// Descriptors of one walker into its feature row (15 normalised inverse pair
+// distances, in the canonical atom order when B.sorted, then a zero pad):
+// a register array float[16] or a row of shared memory (float*); returns
+// true when the walker lies outside the training box.  The pair values are
+// formed in the row itself and normalised there.
+template <typename Row>
+__device__ __forceinline__ bool walker_features(const float (&xs)[18], const FeatBox& B, Row&& row) {
   int q = 0;
-  bool out = false;
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = i + 1; j < 6; ++j) {
       const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
-      const float f = fmaf(rsqrtf(dx * dx + dy * dy + dz * dz), B.scale[q], B.shift[q]);
-      out |= (f < B.lo[q]) || (f > B.hi[q]);
-      row[q] = f;
-      ++q;
+      row[q++] = rsqrtf(dx * dx + dy * dy + dz * dz);
     }
+  }
+  if (B.sorted) dimer_sort_pairs<false>(row, row);
+  bool out = false;
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {
+    const float f = fmaf(row[k], B.scale[k], B.shift[k]);
+    out |= (f < B.lo[k]) || (f > B.hi[k]);
+    row[k] = f;
   }
   row[15] = 0.f;
   return out;

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
   // then wait for the previous step's kernels (programmatic launch)
   const uint32_t tmem = setup(sm, net);
   pdl_wait();
-  const double corr = audit ? audit[4] : 0.0;  // online bias correction (hartree)
+  const double corr = audit ? audit[4] + audit[8] : 0.0;  // online bias correction (hartree)
   // V = (e_mean - corr) + e_scale (e + b4) (+ KE): the fp64 constants once per thread
   const double v_off = (double)net.e_mean - corr, v_scale = (double)net.e_scale;
   const int g = threadIdx.x >> 7;

@@ -49,10 +49,17 @@ def _bf16_bits(t):
 
 
 class MLPSurrogate:
-    def __init__(self, device=None, seed=0, engine=1):
-        """engine: 1 = tcgen05 inference kernels (default), 0 = mma.sync kernels."""
+    def __init__(self, device=None, seed=0, engine=1, sort_atoms=True):
+        """engine: 1 = tcgen05 inference kernels (default), 0 = mma.sync kernels.
+        sort_atoms: descriptors in the canonical atom order of pyvibdmc's
+        DistIt(method='coulomb', sorted_atoms=[[0],[1,2],[3],[4,5]],
+        sorted_groups=[[0,1,2],[3,4,5]]) (distance_descriptors.py:115-152), so
+        that the eight copies of a geometry under exchange of the hydrogens of a
+        water and of the two waters get the same energy; False keeps the given
+        atom order (the unsorted DistIt)."""
         self.device = torch.device(device) if device is not None else default_device()
         self.engine = int(engine)
+        self.sort_atoms = bool(sort_atoms)
         g = torch.Generator().manual_seed(seed)
         f32 = dict(dtype=torch.float32)
 
@@ -97,6 +104,7 @@ class MLPSurrogate:
         n.audit_every = int(audit_every)
         n.engine = int(self.engine if engine is None else engine)
         n.bias_beta = float(bias_beta)
+        n.sort_atoms = int(self.sort_atoms)
         return n
 
     def energy_soa(self, x32, n, ld=None, engine=None):
@@ -125,7 +133,7 @@ class MLPSurrogate:
         feat = torch.empty(m, 16, dtype=torch.float32, device=self.device)
         zeros, ones = torch.zeros(16, device=self.device), torch.ones(16, device=self.device)
         _capi.check(L.gbdmc_dimer_features(_p(x), m, m, _p(zeros), _p(ones), None, None, 1.0, _p(feat), None, None,
-                                           _s()), "gbdmc_dimer_features")
+                                           int(self.sort_atoms), _s()), "gbdmc_dimer_features")
         mu = feat.mean(0)
         sd = feat.std(0).clamp_min(1e-6)
         mu[15], sd[15] = 0.0, 1.0
@@ -139,7 +147,8 @@ class MLPSurrogate:
         L = _capi.load()
         n = xb.shape[1]
         _capi.check(L.gbdmc_dimer_features(_p(xb), n, n, _p(self.mu), _p(self.inv_sd), _p(vdir), _p(gb),
-                                           float(self.e_scale), _p(feat), _p(tang), _p(et), _s()),
+                                           float(self.e_scale), _p(feat), _p(tang), _p(et), int(self.sort_atoms),
+                                           _s()),
                     "gbdmc_dimer_features")
 
     def _alloc(self, B):
@@ -273,7 +282,7 @@ class MLPSurrogate:
     def state_dict(self):
         return dict(P={k: v.detach().cpu() for k, v in self.P.items()}, mu=self.mu.cpu(), inv_sd=self.inv_sd.cpu(),
                     lo=self.lo.cpu(), hi=self.hi.cpu(), e_mean=self.e_mean, e_scale=self.e_scale,
-                    hull_margin=self.hull_margin)
+                    hull_margin=self.hull_margin, sort_atoms=self.sort_atoms)
 
     def load_state_dict(self, st):
         for k, v in st["P"].items():
@@ -281,6 +290,7 @@ class MLPSurrogate:
         self.mu, self.inv_sd = st["mu"].to(self.device), st["inv_sd"].to(self.device)
         self.lo, self.hi = st["lo"], st["hi"]
         self.e_mean, self.e_scale, self.hull_margin = st["e_mean"], st["e_scale"], st["hull_margin"]
+        self.sort_atoms = bool(st.get("sort_atoms", False))
         self._refresh_bf16()
         return self
 
@@ -343,10 +353,25 @@ class NNDMC:
     importance sampled on the tensor-core engine: drift-diffusion proposal,
     trial psi at the proposal and Metropolis test in fp32, local energy
     V_nn + KE, weights with dt_eff = dt * accepted / N (pyvibdmc.py:549-612).
+
+    Bias control (``bias_control`` = b > 0): every step the surrogate energies
+    are V_nn - c, c = c_mix + c_pure.  c_mix is the moving average (weight b
+    per step) of the audited errors V_nn - V over the walkers, which sample
+    the mixed distribution (psi_T phi, or phi without a trial).  The DMC
+    energy moves with the error averaged over phi^2 (first-order
+    perturbation), so with ``bias_weighting="pure"`` c_pure is the
+    forward-walking difference of the two averages: in back-to-back windows
+    of ``fw_time`` (a.u. of imaginary time) the errors of all walkers at a
+    window's start are weighted by their descendants at its end (the
+    descendant weights of pyvibdmc.py:663-672) and set against their plain
+    mean; c_pure is the running mean of the windows' differences (later
+    windows weighted 1/4, so the first, near the start geometry, are
+    forgotten).  ``"mixed"`` keeps c_pure = 0.
     """
 
     def __init__(self, surrogate, potential, num_walkers, start_structures, masses, delta_t, num_timesteps, seed=0,
-                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0, bias_control=0.02, imp_samp=None):
+                 audit_every=100, rng="philox32", graph_steps=16, replica_id=0, bias_control=0.02, imp_samp=None,
+                 bias_weighting="pure", fw_time=2000.0):
         if not isinstance(potential, Potential_GPU) or potential.kind != "water_dimer":
             raise TypeError("the audit/fallback potential must be the analytic water_dimer Potential_GPU")
         self.model, self.potential = surrogate, potential
@@ -403,7 +428,7 @@ class NNDMC:
             nbytes = L.gbdmc_scratch_bytes(cap)
         self._ctrl = torch.zeros(self.R * C.sizeof(_capi.Ctrl), dtype=torch.uint8, device=dev)
         self._scratch = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
-        self._audit = torch.zeros(8, dtype=torch.float64, device=dev)
+        self._audit = torch.zeros(10, dtype=torch.float64, device=dev)
         self._hist = dict(vref=torch.zeros(self.R, self.T, dtype=torch.float64, device=dev),
                           pop=torch.zeros(self.R, self.T, dtype=torch.float64, device=dev))
         s = _capi.Sim()
@@ -425,6 +450,12 @@ class NNDMC:
         self._net = surrogate.net_struct(audit_every, bias_beta=bias_control)
         self._graphs = {}
         self.step = 0
+        if bias_weighting not in ("pure", "mixed"):
+            raise ValueError("bias_weighting is 'pure' or 'mixed'")
+        # forward-walking windows of whole graphs of steps
+        self._fw_on = bias_control > 0 and bias_weighting == "pure"
+        self._fw_len = max(self.graph_steps, int(round(fw_time / self.dt / self.graph_steps)) * self.graph_steps)
+        self._fw_next, self._fw_open, self._fw_hist, self._fw_offset = self._fw_len, False, [], 0.0
 
     def _w(self, b, with_idx):
         w = _capi.WalkersF32()
@@ -486,7 +517,7 @@ class NNDMC:
             self._graphs[cur] = g
         return g
 
-    def run(self, nsteps, check=True):
+    def _advance(self, nsteps):
         if not isinstance(self.rng, str):
             for _ in range(nsteps):
                 n = int(self.ctrl().n)
@@ -501,7 +532,7 @@ class NNDMC:
                 self._cur, self._lazy = self._launch(self._cur, self._lazy, nz)
                 torch.cuda.synchronize()
             self.step += nsteps
-            return self._check() if check else self
+            return
         done = 0
         if nsteps and not self._lazy:
             self._cur, self._lazy = self._launch(self._cur, self._lazy)
@@ -513,7 +544,80 @@ class NNDMC:
             self._cur, self._lazy = self._launch(self._cur, True)
             done += 1
         self.step += nsteps
+
+    def run(self, nsteps, check=True):
+        """Advance nsteps steps (graph replays of graph_steps launches with
+        Philox deviates), closing and opening the forward-walking windows of
+        the bias control on the way."""
+        done = 0
+        while done < nsteps:
+            k = nsteps - done
+            if self._fw_on:
+                k = min(k, self._fw_next - self.step)
+            self._advance(k)
+            done += k
+            if self._fw_on and self.step == self._fw_next:
+                self._fw_boundary()
+                self._fw_next += self._fw_len
         return self._check() if check else self
+
+    def _compact(self):
+        if self._lazy:
+            L = _capi.load()
+            reps, nrep = self._rep_args()
+            _capi.check(L.gbdmc_mlp_batch_compact(C.byref(self._sim), reps, nrep,
+                                                  C.byref(self._w(self._bufs[self._cur], True)),
+                                                  C.byref(self._w(self._bufs[1 - self._cur], False)),
+                                                  _p(self._ctrl), _s()), "gbdmc_mlp_batch_compact")
+            self._cur, self._lazy = 1 - self._cur, False
+
+    def _fw_parts(self):
+        p = self._fw_part.cpu().numpy().reshape(-1, 2)
+        return float(p[:, 0].sum()), float(p[:, 1].sum())
+
+    def _fw_boundary(self):
+        """Close the open forward-walking window (pure average of its start
+        walkers' errors over their descendants now alive; update c_pure) and
+        open the next one on the current walkers."""
+        L = _capi.load()
+        reps, nrep = self._rep_args()
+        self._compact()
+        w = self._w(self._bufs[self._cur], False)
+        if not hasattr(self, "_fw_delta"):
+            dev = self.device
+            self._fw_delta = torch.zeros(self.ld, dtype=torch.float64, device=dev)
+            self._fw_vnn = torch.zeros(self.ld, dtype=torch.float64, device=dev)
+            self._fw_out = torch.zeros(self.ld, dtype=torch.int32, device=dev)
+            self._fw_st = torch.zeros(1, dtype=torch.int32, device=dev)
+            self._fw_part = torch.zeros(2 * _capi.FW_BLOCKS, dtype=torch.float64, device=dev)
+        if self._fw_open:
+            _capi.check(L.gbdmc_mlp_fw_end(C.byref(self._sim), reps, nrep, C.byref(w), _p(self._ctrl),
+                                           _p(self._fw_delta), _p(self._fw_part), _s()), "gbdmc_mlp_fw_end")
+            s, n = self._fw_parts()
+            if n > 0:
+                pure = s / n
+                self._fw_hist.append((self.step, self._fw_mixed, pure))
+                a = max(1.0 / len(self._fw_hist), 0.25)
+                self._fw_offset += a * ((pure - self._fw_mixed) - self._fw_offset)
+                self._audit[8] = self._fw_offset
+        self._fw_out.zero_()
+        _capi.check(L.gbdmc_mlp_energy(C.byref(self._net), _p(self._bufs[self._cur]["x"]), self.ld, self.ld,
+                                       _p(self._fw_vnn), _p(self._fw_out), _p(self._fw_st), _s()), "gbdmc_mlp_energy")
+        _capi.check(L.gbdmc_mlp_fw_begin(C.byref(self._sim), reps, nrep, C.byref(w), _p(self._ctrl),
+                                         _p(self._fw_vnn), _p(self._fw_out), _p(self._fw_delta), _p(self._fw_part),
+                                         _s()), "gbdmc_mlp_fw_begin")
+        s, n = self._fw_parts()
+        if int(self._fw_st.item()):
+            raise RuntimeError("gbdmc_mlp_energy: a bounded tensor-core wait timed out")
+        self._fw_mixed, self._fw_open = (s / n if n > 0 else 0.0), True
+
+    def fw_history(self):
+        """The closed forward-walking windows: (end step, mixed and pure
+        averages of the start walkers' errors V_nn - V in cm^-1), (K, 3)."""
+        w = Constants.atomic_units["wavenumbers"]
+        h = np.array(self._fw_hist, dtype=np.float64).reshape(-1, 3)
+        h[:, 1:] /= w
+        return h
 
     def _check(self):
         for r, c in enumerate(self.ctrls()):
@@ -548,22 +652,17 @@ class NNDMC:
         return float(prev[:, t0:t1].sum())
 
     def audit(self):
-        """(audited walkers, mean and RMS of V_nn - V_analytic in cm^-1, fallbacks)."""
+        """Audited walkers, mean and RMS of V_nn - V_analytic (cm^-1), fallbacks,
+        the bias correction applied now (c_mix + c_pure), c_pure and the
+        number of closed forward-walking windows."""
         a = self._audit.cpu().numpy()
         n = max(a[0], 1.0)
         w = Constants.atomic_units["wavenumbers"]
         return dict(audited=int(a[0]), mean_cm=a[1] / n / w, rms_cm=math.sqrt(a[2] / n) / w, fallbacks=int(a[3]),
-                    bias_correction_cm=a[4] / w)
+                    bias_correction_cm=(a[4] + a[8]) / w, pure_offset_cm=a[8] / w, fw_windows=len(self._fw_hist))
 
     def walkers(self, r=0):
-        if self._lazy:
-            L = _capi.load()
-            reps, nrep = self._rep_args()
-            _capi.check(L.gbdmc_mlp_batch_compact(C.byref(self._sim), reps, nrep,
-                                                  C.byref(self._w(self._bufs[self._cur], True)),
-                                                  C.byref(self._w(self._bufs[1 - self._cur], False)),
-                                                  _p(self._ctrl), _s()), "gbdmc_mlp_batch_compact")
-            self._cur, self._lazy = 1 - self._cur, False
+        self._compact()
         n = int(self.ctrl(r).n)
         off = int(self.offs[r])
         return from_soa(self._bufs[self._cur]["x"][:, off:off + n], n, 6)

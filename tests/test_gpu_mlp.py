@@ -50,12 +50,34 @@ def test_gemm_tn_matches_torch(K, M):
     torch.testing.assert_close(G, ref, rtol=1e-4, atol=1e-3)
 
 
-def test_features_match_oracle():
+def _group_copies(x):
+    """Each geometry under one of the eight permutations of like atoms (the
+    hydrogens of either water, the two waters), cycling through them."""
+    perms = []
+    for g in (False, True):
+        for a in (False, True):
+            for b in (False, True):
+                w1, w2 = ([0, 2, 1] if a else [0, 1, 2]), ([3, 5, 4] if b else [3, 4, 5])
+                perms.append((w2 + w1) if g else (w1 + w2))
+    perms = np.array(perms)
+    return x[np.arange(len(x))[:, None], perms[np.arange(len(x)) % 8]]
+
+
+@pytest.mark.parametrize("sort", [False, True])
+def test_features_match_oracle(sort):
+    """Descriptors and their directional derivatives against the oracle (with
+    sort: DistIt's sorted atom order, which the oracle restates and the
+    reference's own DistIt pins).  The kernel decides the order in fp32: the
+    walkers whose decisions are within 1e-4 of a tie (relative, by the
+    oracle's fp64 norms) are left out, and at least 90 % remain."""
     x = oracle.dimer_equilibrium()[None] + 0.1 * oracle.InjectedNoise(3).standard_normal((300, 6, 3))
+    x = _group_copies(x)
     v = oracle.InjectedNoise(4).standard_normal((300, 6, 3))
     p, _ = oracle.dimer_config()
     grad = oracle.grad_dimer(x, p)
-    f_ref, t_ref = mo.inv_dist_features(x, v)
+    f_ref, t_ref = mo.inv_dist_features(x, v, sort=sort)
+    keep = mo.dimer_sort_perm(x)[1].min(1) > 1e-4 if sort else np.ones(300, bool)
+    assert keep.mean() > 0.9
     mu = torch.linspace(0.1, 0.3, 16, device="cuda")
     isd = torch.linspace(1.0, 2.0, 16, device="cuda")
     L = _capi.load()
@@ -64,10 +86,10 @@ def test_features_match_oracle():
     tang = torch.empty(300, 16, device="cuda")
     et = torch.empty(300, device="cuda")
     _capi.check(L.gbdmc_dimer_features(_p(xs), 300, 300, _p(mu), _p(isd), _p(vs), _p(gs), 0.01, _p(feat), _p(tang),
-                                       _p(et), _s()))
+                                       _p(et), int(sort), _s()))
     mu_, isd_ = mu.cpu().numpy()[:15], isd.cpu().numpy()[:15]
-    np.testing.assert_allclose(feat.cpu().numpy()[:, :15], (f_ref - mu_) * isd_, rtol=1e-5, atol=1e-5)
-    np.testing.assert_allclose(tang.cpu().numpy()[:, :15], t_ref * isd_, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(feat.cpu().numpy()[keep, :15], ((f_ref - mu_) * isd_)[keep], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(tang.cpu().numpy()[keep, :15], (t_ref * isd_)[keep], rtol=1e-4, atol=1e-5)
     np.testing.assert_allclose(et.cpu().numpy(), (grad * v).sum((1, 2)) / 0.01, rtol=1e-4, atol=1e-4)
 
 
@@ -143,21 +165,34 @@ def test_inference_kernel_matches_oracle_forward():
         m.train_batch(xs, v, g, lr=2e-3)
     P = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
     mu, isd = m.mu.cpu().double().numpy(), m.inv_sd.cpu().double().numpy()
-    ref = mo.mlp_energy_tc(P, x, mu, isd, m.e_mean, m.e_scale)
+    assert m.sort_atoms
+    keep = mo.dimer_sort_perm(x)[1].min(1) > 1e-4  # fp32 order decisions away from a tie
+    assert keep.mean() > 0.9
+    ref = mo.mlp_energy_tc(P, x, mu, isd, m.e_mean, m.e_scale, sort=True)
     got = m.energy(x)
-    err = np.abs(got - ref) / m.e_scale
+    err = (np.abs(got - ref) / m.e_scale)[keep]
     assert np.median(err) < 1e-3 and err.max() < 1e-2, (np.median(err), err.max())
     # the fp64 forward without the rounding (a looser oracle) for scale
-    f, _ = mo.inv_dist_features(x)
+    f, _ = mo.inv_dist_features(x, sort=True)
     D = np.zeros((len(x), 16))
     D[:, :15] = (f - mu[:15]) * isd[:15]
     E, _, _ = mo.mlp_forward(dict(P, b4=P["b4"][0]), D)
-    loose = np.abs(got - (m.e_mean + m.e_scale * E)) / m.e_scale
+    loose = (np.abs(got - (m.e_mean + m.e_scale * E)) / m.e_scale)[keep]
     assert np.median(err) < np.median(loose)
     x_bad = x.copy()
-    x_bad[:, [4, 5]] = x_bad[:, [5, 4]]  # the hydrogens of water 2 swapped: descriptor columns permuted
-    bad = np.abs(got - mo.mlp_energy_tc(P, x_bad, mu, isd, m.e_mean, m.e_scale)) / m.e_scale
+    x_bad[:, [3, 4]] = x_bad[:, [4, 3]]  # an oxygen and a hydrogen exchanged: other descriptors
+    bad = np.abs(got - mo.mlp_energy_tc(P, x_bad, mu, isd, m.e_mean, m.e_scale, sort=True)) / m.e_scale
     assert np.median(bad) > 10 * 1e-3
+    # every copy of a geometry under the permutations of like atoms gets the same energy, bit for bit
+    # (the same pair values in the same canonical places), away from the order's ties
+    got8 = m.energy(_group_copies(np.repeat(x[:64], 8, axis=0)))
+    k64 = keep[:64]
+    same = got8.reshape(64, 8)
+    assert np.array_equal(same[k64], np.repeat(same[k64, :1], 8, axis=1))
+    # and the unsorted descriptor does not have that property
+    m.sort_atoms = False
+    un8 = m.energy(_group_copies(np.repeat(x[:64], 8, axis=0))).reshape(64, 8)
+    assert np.median(np.abs(un8 - un8[:, :1]).max(1)) / m.e_scale > 1e-3
 
 
 def test_training_reduces_loss_and_surrogate_dmc_runs():

@@ -61,3 +61,49 @@ def test_bf16_emulation_is_within_bf16_error_of_the_exact_gradients():
     for k in exact:
         rel = np.linalg.norm(np.ravel(emul[k]) - np.ravel(exact[k])) / np.linalg.norm(np.ravel(exact[k]))
         assert 1e-5 < rel < 3e-2, (k, rel)  # bf16-sized: neither exact nor off
+
+
+def _golden_distit():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "distit_dimer.npz"))
+
+
+def _pair_charges():
+    z = mo.DIMER_Z
+    return np.array([z[i] * z[j] for i in range(6) for j in range(i + 1, 6)])
+
+
+def test_sorted_dimer_descriptor_matches_the_reference_distit():
+    """The oracle's canonical atom order against the reference's own DistIt
+    (method 'coulomb', sorted_atoms=[[0],[1,2],[3],[4,5]],
+    sorted_groups=[[0,1,2],[3,4,5]]) on 512 displaced dimers, each under one of
+    the eight permutations of like atoms (tests/golden/make_distit_golden.py):
+    the sorted and the unsorted Coulomb descriptors agree to rounding, and the
+    sorting changes the descriptor of most of them."""
+    d = _golden_distit()
+    zz = _pair_charges()
+    f, _ = mo.inv_dist_features(d["x"], sort=True)
+    np.testing.assert_allclose(f * zz, d["sorted"], rtol=1e-13, atol=0)
+    f0, _ = mo.inv_dist_features(d["x"])
+    np.testing.assert_allclose(f0 * zz, d["unsorted"], rtol=1e-13, atol=0)
+    assert np.mean(np.any(d["sorted"] != d["unsorted"], axis=1)) > 0.5
+
+
+def test_sorted_descriptor_is_invariant_under_the_dimer_permutations():
+    """All eight copies of a geometry under exchange of the hydrogens of either
+    water and of the two waters get the same sorted descriptor and derivative;
+    a planted mistake (an oxygen exchanged with a hydrogen) does not."""
+    d = _golden_distit()
+    x = d["x"][:32]
+    v = np.random.default_rng(5).standard_normal(x.shape)
+    f0, t0 = mo.inv_dist_features(x, v, sort=True)
+    for g in (False, True):
+        for a in (False, True):
+            for b in (False, True):
+                w1, w2 = ([0, 2, 1] if a else [0, 1, 2]), ([3, 5, 4] if b else [3, 4, 5])
+                p = (w2 + w1) if g else (w1 + w2)
+                f, t = mo.inv_dist_features(x[:, p], v[:, p], sort=True)
+                np.testing.assert_allclose(f, f0, rtol=1e-15, atol=0)
+                np.testing.assert_allclose(t, t0, rtol=1e-12, atol=1e-15)
+    fb, _ = mo.inv_dist_features(x[:, [0, 1, 2, 4, 3, 5]], sort=True)
+    assert np.all(np.abs(fb - f0).max(1) > 1e-3)
