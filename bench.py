@@ -607,10 +607,12 @@ def run_extras(steps):
 
 
 DIMER_TAU = 60000.0  # imaginary time of every run of the spec comparison (a.u.)
-# dt and dt/2 of the extrapolation.  Both walks' time-step errors bend between
-# dt = 10 and 5 (plain and importance-sampled, measured at 10, 5 and 2.5), so
-# the straight line runs through 5 and 2.5, where they are close to linear.
-DIMER_DTS = (5.0, 2.5)
+# dt and dt/2 of the extrapolation.  The walks' time-step errors are curved
+# (plain FP64 dimer, 64 seeds each: E(2.5) - E(5) = 1.72 and E(1.25) - E(2.5)
+# = 0.59 cm^-1), and a straight line keeps a bias of -12.5 b for the steps 5
+# and 2.5 (b the dt^2 coefficient) but a quarter of it for 2.5 and 1.25:
+# +0.72 and +0.18 cm^-1 for the plain walk.
+DIMER_DTS = (2.5, 1.25)
 
 
 def zpe_estimate(vref_series_cm):
@@ -688,18 +690,21 @@ def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
     accelerations (importance sampling with the fitted dimer trial, the tcgen05
     surrogate PES, 64 batched replicas with N_r ~ U[1000, 65536]) against the
     plain FP64 GPU path (200000 walkers, one replica, several seeds), at equal
-    ZPE error including the time-step error: every method runs at dt = 5 and
-    2.5 for the same imaginary time, its ZPE is extrapolated to dt -> 0 and its
+    ZPE error including the time-step error: every method runs at dt = 2.5 and
+    1.25 for the same imaginary time, its ZPE is extrapolated to dt -> 0 and its
     efficiency is 1 / (sigma0^2 x seconds) (zpe_estimate, extrapolate).  The
     FP64 importance-sampled path with the same trial (100000 walkers) pins
     the surrogate's accuracy at each dt; profiles/dimer_fp64_oracle.json holds
-    a long plain FP64 extrapolation of the same surface, the ZPE the three
-    accelerations must reproduce within 1 cm^-1."""
+    a long plain FP64 extrapolation of the same surface (dt = 5, 2.5, 1.25,
+    the parabola through the three), the ZPE the three accelerations must
+    reproduce within 1 cm^-1."""
     import torch
     import pyvibdmc_gb300 as pg
     conv = lambda v: pg.Constants.convert(v, "wavenumbers", to_AU=False)  # noqa: E731
     res = {"estimator": "mean of the last 3/4 of the vref series (N0-weighted over replicas), blocking error of "
-                        "30 block means; dt -> 0 from dt = 5 and 2.5 (E0 = 2 E2.5 - E5)",
+                        "30 block means; dt -> 0 from dt = 2.5 and 1.25 (E0 = 2 E1.25 - E2.5)",
+           "surrogate": "sorted-atom Coulomb descriptor (DistIt order); bias control on the audited errors, "
+                        "weighted by descendants in forward-walking windows of 2000 a.u.",
            "trial": {"alpha": trial.alpha, "qe": trial.qe}}
 
     def fp64(n, imp, seed, dt):
@@ -794,17 +799,48 @@ def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18)):
     return res
 
 
-def dimer_oracle(plain_seeds=tuple(range(101, 165))):
-    """A long plain FP64 extrapolation of the water dimer's ZPE (200000 walkers,
-    64 seeds at dt = 5 and 2.5): the value profiles/dimer_fp64_oracle.json keeps
-    for the spec comparison."""
+def oracle_extrapolation(runs):
+    """dt -> 0 of the plain FP64 dimer ZPEs in ``runs`` ({"dt<dt>": {zpe_cm,
+    err_cm}}): the straight line through each pair of neighbouring steps
+    (E0 = 2 E(h/2) - E(h)) and, with dt = 5, 2.5 and 1.25, the parabola
+    through the three (Richardson: E0 = (E(5) - 6 E(2.5) + 8 E(1.25)) / 3,
+    which removes the dt^2 term the straight lines keep).  The oracle value
+    is the parabola when all three steps are present."""
+    out = {}
+    dts = sorted((float(k[2:]) for k in runs), reverse=True)
+    for h, h2 in zip(dts, dts[1:]):
+        if abs(h2 * 2 - h) < 1e-12:
+            a, b = runs[f"dt{h:g}"], runs[f"dt{h2:g}"]
+            out[f"linear_{h:g}_{h2:g}"] = [2 * b["zpe_cm"] - a["zpe_cm"],
+                                           float(np.sqrt(4 * b["err_cm"] ** 2 + a["err_cm"] ** 2))]
+    if all(f"dt{d:g}" in runs for d in (5.0, 2.5, 1.25)):
+        e = [runs[f"dt{d:g}"] for d in (5.0, 2.5, 1.25)]
+        out["quadratic_5_2.5_1.25"] = [(e[0]["zpe_cm"] - 6 * e[1]["zpe_cm"] + 8 * e[2]["zpe_cm"]) / 3,
+                                        float(np.sqrt(e[0]["err_cm"] ** 2 + 36 * e[1]["err_cm"] ** 2 +
+                                                      64 * e[2]["err_cm"] ** 2) / 3)]
+        out["zpe_dt0_cm"], out["err_dt0_cm"] = out["quadratic_5_2.5_1.25"]
+    else:
+        k = next(iter(out))
+        out["zpe_dt0_cm"], out["err_dt0_cm"] = out[k]
+    return out
+
+
+def dimer_oracle(dts, merge=None, plain_seeds=tuple(range(101, 165))):
+    """A long plain FP64 extrapolation of the water dimer's ZPE (200000
+    walkers, 64 seeds at each dt, 60000 a.u. of imaginary time per run): the
+    value profiles/dimer_fp64_oracle.json keeps for the north-star
+    comparison.  ``merge``: a JSON file of this function whose runs at other
+    steps are kept."""
     import torch
     import pyvibdmc_gb300 as pg
     dm = [pg.Constants.mass(a) for a in ("O", "H", "H", "O", "H", "H")]
     pot = pg.water_dimer()
-    res = {}
+    res, secs = {}, 0.0
+    if merge:
+        old = json.load(open(merge))
+        res, secs = dict(old["runs"]), float(old.get("seconds", 0.0))
     t_all = time.perf_counter()
-    for dt in DIMER_DTS:
+    for dt in dts:
         T = int(round(DIMER_TAU / dt))
         zs, es = [], []
         for seed in plain_seeds:
@@ -823,10 +859,10 @@ def dimer_oracle(plain_seeds=tuple(range(101, 165))):
         res[f"dt{dt:g}"] = {"zpe_cm": float(np.mean(zs)), "err_cm": float(np.sqrt(np.sum(np.square(es))) / len(es)),
                             "scatter_err_cm": float(np.std(zs, ddof=1) / np.sqrt(len(zs))), "runs": len(zs),
                             "runs_left_out": len(plain_seeds) - len(zs)}
-    d0 = extrapolate({k: dict(v, seconds=0.0) for k, v in res.items()})
-    out = {"zpe_dt0_cm": d0["zpe_cm"], "err_dt0_cm": d0["err_cm"], "runs": res, "walkers": 200000,
-           "imaginary_time_au": DIMER_TAU, "seeds": [plain_seeds[0], plain_seeds[-1]],
-           "seconds": time.perf_counter() - t_all, "command": "python bench.py --dimer-oracle"}
+    out = dict(oracle_extrapolation(res), runs=res, walkers=200000, imaginary_time_au=DIMER_TAU,
+               seeds=[plain_seeds[0], plain_seeds[-1]], seconds=secs + time.perf_counter() - t_all,
+               command="python bench.py --dimer-oracle " + ",".join(f"{d:g}" for d in sorted(
+                   (float(k[2:]) for k in res), reverse=True)))
     print(json.dumps(out), flush=True)
 
 
@@ -888,13 +924,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", dest="no_extras", action="store_true",
                     help="skip the IS / batched / surrogate workloads reported under 'extras'")
-    ap.add_argument("--dimer-oracle", dest="dimer_oracle", action="store_true",
-                    help="print the long plain FP64 dt -> 0 ZPE of the water dimer (profiles/dimer_fp64_oracle.json)")
+    ap.add_argument("--dimer-oracle", dest="dimer_oracle", default=None, metavar="DT,...",
+                    help="print the long plain FP64 dt -> 0 ZPE of the water dimer from runs at these time steps "
+                         "(profiles/dimer_fp64_oracle.json: 5,2.5,1.25)")
+    ap.add_argument("--merge", default=None, help="with --dimer-oracle: keep the runs of this oracle JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.dimer_oracle:
-        dimer_oracle()
+        dimer_oracle([float(v) for v in args.dimer_oracle.split(",")], args.merge)
     elif args.impl == "reference":
         run_reference(args)
     else:
