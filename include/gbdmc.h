@@ -369,7 +369,7 @@ int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);
 /* sizeof() of the ABI structs, for binding self-checks:
  * 0 gbdmc_sim_t, 1 gbdmc_walkers_t, 2 gbdmc_ctrl_t, 3 gbdmc_noise_t,
  * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t, 7 gbdmc_replica_t, 8 gbdmc_mlp_t,
- * 9 gbdmc_walkers_f32_t; 0 for unknown ids. */
+ * 9 gbdmc_walkers_f32_t, 10 gbdmc_adam_param_t; 0 for unknown ids. */
 size_t gbdmc_struct_size(int32_t which);
 
 /* ---- MLP surrogate of the water-dimer PES (BF16 tensor cores, FP32 accumulation) ----
@@ -432,14 +432,45 @@ int gbdmc_mlp_gemm(const float* x_dev, int64_t m, int32_t k, const uint16_t* wt_
 int gbdmc_mlp_gemm_tn(const float* x_dev, const float* d_dev, int64_t m, int32_t k, float* g_dev, void* stream);
 /* H = silu(Z), Ht = silu'(Z) Zt (Zt/Ht may be NULL). */
 int gbdmc_mlp_silu_fwd(const float* z_dev, const float* zt_dev, float* h_dev, float* ht_dev, int64_t n, void* stream);
-/* Zb = silu'(Z) Hb + silu''(Z) Zt Htb, Ztb = silu'(Z) Htb (Zt/Htb/Ztb may be NULL). */
+/* Zb = silu'(Z) Hb + silu''(Z) Zt Htb, Ztb = silu'(Z) Htb (Zt/Htb/Ztb may be NULL) on rows of 128 columns
+ * (n a multiple of 128); with gbias_dev (may be NULL) also gbias[c] += sum over rows of Zb[., c], the
+ * layer's bias gradient (fp32 atomics). */
 int gbdmc_mlp_silu_bwd(const float* z_dev, const float* zt_dev, const float* hb_dev, const float* htb_dev,
-                       float* zb_dev, float* ztb_dev, int64_t n, void* stream);
+                       float* zb_dev, float* ztb_dev, int64_t n, float* gbias_dev, void* stream);
 /* Output layer + loss wE<(E-e)^2> + wF<(Et-et)^2>; writes dL/dH3, dL/dHt3 and accumulates dL/dw4, dL/db4,
- * loss[0] = sum (E-e)^2, loss[1] = sum (Et-et)^2. */
-int gbdmc_mlp_head(const float* h3_dev, const float* ht3_dev, const float* w4_dev, float b4, const float* e_dev,
-                   const float* et_dev, int64_t m, float w_e, float w_f, float* h3b_dev, float* ht3b_dev,
-                   float* gw4_dev, float* gb4_dev, double* loss_dev, void* stream);
+ * loss[0] += sum (E-e)^2, loss[1] += sum (Et-et)^2.  b4 is read from b4_dev when that is not NULL. */
+int gbdmc_mlp_head(const float* h3_dev, const float* ht3_dev, const float* w4_dev, float b4, const float* b4_dev,
+                   const float* e_dev, const float* et_dev, int64_t m, float w_e, float w_f, float* h3b_dev,
+                   float* ht3b_dev, float* gw4_dev, float* gb4_dev, double* loss_dev, void* stream);
+/* The inputs of a training batch, so that a batch can be one CUDA graph: samples [off, off + b) of the data
+ * set (fp64 SoA x_dev, grad_dev [18][ld], v_dev [ld]) with off = ctl_dev[1]; feat (descriptors, as
+ * gbdmc_dimer_features), and along a random unit direction u of the 18 coordinates (Philox normals of
+ * (seed, ctl_dev[0], sample), normalised) tang (their derivative) and et = (dV/dx . u) / e_scale; the
+ * energy target e = (V - e_mean) / e_scale - *b4_dev.  ctl_dev: [0] Adam steps taken, [1] batch offset. */
+int gbdmc_mlp_train_inputs(const double* x_dev, const double* v_dev, const double* grad_dev, int64_t ld, int64_t b,
+                           const int64_t* ctl_dev, uint64_t seed, const float* mu_dev, const float* inv_sd_dev,
+                           float e_mean, float e_scale, const float* b4_dev, int32_t sort_atoms, float* feat_dev,
+                           float* tang_dev, float* et_dev, float* e_dev, void* stream);
+/* One parameter of gbdmc_mlp_adam_all: fp32 values, gradient, Adam moments (n each); for a K x 128 weight
+ * matrix (n = 128 K) the bf16 copies wt (transposed) and wn (row-major) to refresh, either may be NULL. */
+typedef struct {
+  float* p;
+  float* g;
+  float* m;
+  float* v;
+  uint16_t* wt;
+  uint16_t* wn;
+  int64_t n;
+  int32_t k;
+  int32_t pad;
+} gbdmc_adam_param_t;
+/* One Adam step on nq <= 8 parameters in one launch: t = ctl_dev[0] + 1, learning rate
+ * lr_min + (lr0 - lr_min) (1 + cos(pi (t - 1 - t0) / steps)) / 2; every gradient is cleared after use; the
+ * launch then sets ctl_dev[0] = t and advances ctl_dev[1] by batch.  ticket_dev: a device uint, zero before
+ * the first call (the kernel leaves it zero). */
+int gbdmc_mlp_adam_all(const gbdmc_adam_param_t* params, int32_t nq, float lr0, float lr_min, float beta1,
+                       float beta2, float eps, int64_t t0, int64_t steps, int64_t batch, int64_t* ctl_dev,
+                       uint32_t* ticket_dev, void* stream);
 /* Adam step (t >= 1) on fp32 parameters; for a K x 128 weight matrix also refreshes its bf16 copies:
  * wt transposed (n-major, forward GEMM) and wn row-major (backward GEMM); either may be NULL. */
 int gbdmc_mlp_adam(float* p_dev, const float* g_dev, float* m_dev, float* v_dev, int64_t n, float lr, float beta1,

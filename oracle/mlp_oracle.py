@@ -175,8 +175,10 @@ def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5, magnitudes=False):
     signals and the weights), products summed exactly and the sum rounded to
     fp32 (the tensor cores accumulate in fp32), the bias added in fp32; every
     buffer the kernels store is fp32; the logistic function 1 / (1 + exp(-z))
-    in fp32.  The output bias enters as a shift of the targets (e here is
-    already shifted), so the head adds nothing.  D, U are the kernels' (M, 16)
+    in fp32; a layer's bias gradient is the column sum of the SiLU
+    backward's fp32 output (before its bf16 rounding as a GEMM operand).  The
+    output bias enters as a shift of the targets (e here is already shifted),
+    so the head adds nothing.  D, U are the kernels' (M, 16)
     descriptor and tangent rows, e, et their (M,) targets.  Returns the
     gradients and the two loss sums; with ``magnitudes`` also the sums of the
     magnitudes of the terms each gradient entry adds up (the scale of the
@@ -205,12 +207,13 @@ def mlp_loss_grads_bf16(P, D, U, e, et, wE=1.0, wF=0.5, magnitudes=False):
         hin, htin, z, zt, s = cache[l]
         d1 = f32(s * f32(1.0 + f32(z * f32(1.0 - s))))
         d2 = f32(f32(s * f32(1.0 - s)) * f32(2.0 + f32(z * f32(1.0 - f32(2.0 * s)))))
-        zb = bf16(f32(d1 * hb + f32(d2 * zt) * htb))
+        zb32 = f32(d1 * hb + f32(d2 * zt) * htb)  # the SiLU backward's fp32 output
+        zb = bf16(zb32)  # as a GEMM operand
         ztb = bf16(f32(d1 * htb))
         G[f"W{l}"] = bf16(hin).T @ zb + bf16(htin).T @ ztb
-        G[f"b{l}"] = zb.sum(0)
+        G[f"b{l}"] = zb32.sum(0)  # summed by the SiLU backward itself, in fp32
         Gm[f"W{l}"] = np.abs(bf16(hin)).T @ np.abs(zb) + np.abs(bf16(htin)).T @ np.abs(ztb)
-        Gm[f"b{l}"] = np.abs(zb).sum(0)
+        Gm[f"b{l}"] = np.abs(zb32).sum(0)
         hb = f32(zb @ Wb[l].T)
         htb = f32(ztb @ Wb[l].T)
     loss = (float(((E - f32(e)) ** 2).sum()), float(((Et - f32(et)) ** 2).sum()))

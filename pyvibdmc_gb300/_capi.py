@@ -83,7 +83,12 @@ class WalkersF32(C.Structure):
                 ("f", C.c_void_p), ("lnpsi", C.c_void_p), ("ke", C.c_void_p)]
 
 
-_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32]
+class AdamParam(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("g", C.c_void_p), ("m", C.c_void_p), ("v", C.c_void_p), ("wt", C.c_void_p),
+                ("wn", C.c_void_p), ("n", C.c_int64), ("k", C.c_int32), ("pad", C.c_int32)]
+
+
+_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32, AdamParam]
 
 _lib = None
 
@@ -136,8 +141,13 @@ def load():
         "gbdmc_mlp_gemm": ([P, C.c_int64, C.c_int32, P, P, P, P], C.c_int),
         "gbdmc_mlp_gemm_tn": ([P, P, C.c_int64, C.c_int32, P, P], C.c_int),
         "gbdmc_mlp_silu_fwd": ([P, P, P, P, C.c_int64, P], C.c_int),
-        "gbdmc_mlp_silu_bwd": ([P, P, P, P, P, P, C.c_int64, P], C.c_int),
-        "gbdmc_mlp_head": ([P, P, P, C.c_float, P, P, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P], C.c_int),
+        "gbdmc_mlp_silu_bwd": ([P, P, P, P, P, P, C.c_int64, P, P], C.c_int),
+        "gbdmc_mlp_head": ([P, P, P, C.c_float, P, P, P, C.c_int64, C.c_float, C.c_float, P, P, P, P, P, P],
+                           C.c_int),
+        "gbdmc_mlp_train_inputs": ([P, P, P, C.c_int64, C.c_int64, P, C.c_uint64, P, P, C.c_float, C.c_float, P,
+                                    C.c_int32, P, P, P, P, P], C.c_int),
+        "gbdmc_mlp_adam_all": ([P, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int64,
+                                C.c_int64, C.c_int64, P, P, P], C.c_int),
         "gbdmc_mlp_adam": ([P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P, P,
                             C.c_int32, P], C.c_int),
         "gbdmc_dimer_features": ([P, C.c_int64, C.c_int64, P, P, P, P, C.c_float, P, P, P, C.c_int32, P], C.c_int),

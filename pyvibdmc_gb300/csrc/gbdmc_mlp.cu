@@ -168,36 +168,58 @@ __global__ void k_silu_fwd(const float* __restrict__ Z, const float* __restrict_
   }
 }
 
-// Zb = silu'(Z) Hb + silu''(Z) Zt Htb ;  Ztb = silu'(Z) Htb
-__global__ void k_silu_bwd(const float* __restrict__ Z, const float* __restrict__ Zt, const float* __restrict__ Hb,
-                           const float* __restrict__ Htb, float* __restrict__ Zb, float* __restrict__ Ztb,
-                           long long n) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+// Zb = silu'(Z) Hb + silu''(Z) Zt Htb ;  Ztb = silu'(Z) Htb, on rows of 128
+// columns; with gbias also the bias gradient gbias[c] += sum over rows of
+// Zb[., c] (each thread keeps one column, a block adds its two row halves
+// and issues one atomic per column).
+__global__ void __launch_bounds__(256) k_silu_bwd(const float* __restrict__ Z, const float* __restrict__ Zt,
+                                                  const float* __restrict__ Hb, const float* __restrict__ Htb,
+                                                  float* __restrict__ Zb, float* __restrict__ Ztb, long long rows,
+                                                  float* __restrict__ gbias) {
+  const int c = threadIdx.x & (kH - 1);
+  float acc = 0.f;
+  for (long long r = 2LL * blockIdx.x + (threadIdx.x >> 7); r < rows; r += 2LL * gridDim.x) {
+    const long long i = r * kH + c;
     const float z = Z[i];
     const float s = sigmoid_acc(z);
     const float d1 = s * (1.f + z * (1.f - s));
     const float d2 = s * (1.f - s) * (2.f + z * (1.f - 2.f * s));
     const float hb = Hb[i];
+    float zb;
     if (Zt) {
       const float htb = Htb[i];
-      Zb[i] = d1 * hb + d2 * Zt[i] * htb;
+      zb = d1 * hb + d2 * Zt[i] * htb;
       Ztb[i] = d1 * htb;
     } else {
-      Zb[i] = d1 * hb;
+      zb = d1 * hb;
     }
+    Zb[i] = zb;
+    acc += zb;
+  }
+  if (gbias) {
+    __shared__ float half[kH];
+    if (threadIdx.x >= kH) half[c] = acc;
+    __syncthreads();
+    if (threadIdx.x < kH) atomicAdd(gbias + c, acc + half[c]);
   }
 }
 
 // Output layer and loss, one warp per sample:
 //   E = H3 w4 + b4, Et = Ht3 w4;  L = wE (E - e)^2 + wF (Et - et)^2 (mean over samples)
-//   writes dL/dH3, dL/dHt3, accumulates dL/dw4, dL/db4 and the loss terms.
-__global__ void k_head(const float* __restrict__ H3, const float* __restrict__ Ht3, const float* __restrict__ w4,
-                       float b4, const float* __restrict__ e_true, const float* __restrict__ et_true, long long M,
-                       float wE, float wF, float* __restrict__ H3b, float* __restrict__ Ht3b, float* __restrict__ gw4,
-                       float* __restrict__ gb4, double* __restrict__ loss) {
-  const int lane = threadIdx.x & 31;
+//   writes dL/dH3, dL/dHt3, accumulates dL/dw4, dL/db4 and the loss terms
+//   (per block in shared memory, then one atomic per quantity and block).
+//   b4 is read on the device when b4_dev is given.
+__global__ void __launch_bounds__(256) k_head(const float* __restrict__ H3, const float* __restrict__ Ht3,
+                                              const float* __restrict__ w4, float b4_val,
+                                              const float* __restrict__ b4_dev, const float* __restrict__ e_true,
+                                              const float* __restrict__ et_true, long long M, float wE, float wF,
+                                              float* __restrict__ H3b, float* __restrict__ Ht3b,
+                                              float* __restrict__ gw4, float* __restrict__ gb4,
+                                              double* __restrict__ loss) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const float b4 = b4_dev ? *b4_dev : b4_val;
   float gw[4] = {0.f, 0.f, 0.f, 0.f}, gb = 0.f;
   double lE = 0.0, lF = 0.0;
   for (long long s = warp; s < M; s += nw) {
@@ -233,12 +255,33 @@ __global__ void k_head(const float* __restrict__ H3, const float* __restrict__ H
     }
     gb += de;
   }
+  __shared__ float sgw[8][kH];
+  __shared__ float sgb[8];
+  __shared__ double sl[8][2];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) atomicAdd(gw4 + lane + 32 * q, gw[q]);
+  for (int q = 0; q < 4; ++q) sgw[wid][lane + 32 * q] = gw[q];
   if (lane == 0) {
-    atomicAdd(gb4, gb);
-    atomicAdd(loss, lE);
-    atomicAdd(loss + 1, lF);
+    sgb[wid] = gb;
+    sl[wid][0] = lE;
+    sl[wid][1] = lF;
+  }
+  __syncthreads();
+  const int nwb = blockDim.x >> 5;
+  if (threadIdx.x < kH) {
+    float t = 0.f;
+    for (int w = 0; w < nwb; ++w) t += sgw[w][threadIdx.x];
+    atomicAdd(gw4 + threadIdx.x, t);
+  } else if (threadIdx.x == kH) {
+    float t = 0.f;
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < nwb; ++w) {
+      t += sgb[w];
+      a += sl[w][0];
+      b += sl[w][1];
+    }
+    atomicAdd(gb4, t);
+    atomicAdd(loss, a);
+    atomicAdd(loss + 1, b);
   }
 }
 
@@ -269,9 +312,42 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, floa
 // Inverse distances of the 15 atom pairs (i<j, combinations order of the
 // reference's descriptor, tensorflow_descriptors/distance_descriptors.py:66-68),
 // with sorted in the canonical atom order of dimer_sort_pairs, normalised
-// (d - mu) * inv_sd; with a direction v, also the normalised directional
-// derivative u = (dd/dx) v (permuted with the descriptors), and et = (dV/dx .
-// v) / e_scale (a permutation of equivalent atoms leaves V unchanged).
+// (d - mu) * inv_sd into frow[0..15]; with TANG also the normalised
+// directional derivative along vs (permuted with the descriptors) into
+// trow[0..15].
+template <bool TANG>
+__device__ __forceinline__ void pair_features(const float (&xs)[18], const float (&vs)[18], int sorted,
+                                              const float* __restrict__ mu, const float* __restrict__ inv_sd,
+                                              float* __restrict__ frow, float* __restrict__ trow) {
+  float ir[15], tg[15];
+  int q = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = i + 1; j < 6; ++j) {
+      const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
+      const float r = rsqrtf(dx * dx + dy * dy + dz * dz);
+      ir[q] = r;
+      if constexpr (TANG) {
+        const float dvx = vs[3 * i] - vs[3 * j], dvy = vs[3 * i + 1] - vs[3 * j + 1], dvz = vs[3 * i + 2] - vs[3 * j + 2];
+        tg[q] = -(dx * dvx + dy * dvy + dz * dvz) * r * r * r;
+      }
+      ++q;
+    }
+  }
+  if (sorted) dimer_sort_pairs<TANG>(ir, tg);
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {
+    frow[k] = (ir[k] - mu[k]) * inv_sd[k];
+    if constexpr (TANG) trow[k] = tg[k] * inv_sd[k];
+  }
+  frow[15] = 0.f;
+  if constexpr (TANG) trow[15] = 0.f;
+}
+
+// Descriptors (and with a direction v their derivative along v, and et =
+// (dV/dx . v) / e_scale; a permutation of equivalent atoms leaves V
+// unchanged) of n walkers.
 template <typename T>
 __global__ void k_features(const T* __restrict__ x, long long ldx, long long n, const float* __restrict__ mu,
                            const float* __restrict__ inv_sd, const T* __restrict__ vdir, const double* __restrict__ grad,
@@ -284,34 +360,119 @@ __global__ void k_features(const T* __restrict__ x, long long ldx, long long n, 
       xs[k] = (float)x[k * ldx + s];
       vs[k] = vdir ? (float)vdir[k * ldx + s] : 0.f;
     }
-    float ir[15], tg[15];
-    int q = 0;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-#pragma unroll
-      for (int j = i + 1; j < 6; ++j) {
-        const float dx = xs[3 * i] - xs[3 * j], dy = xs[3 * i + 1] - xs[3 * j + 1], dz = xs[3 * i + 2] - xs[3 * j + 2];
-        const float r = rsqrtf(dx * dx + dy * dy + dz * dz);
-        const float dvx = vs[3 * i] - vs[3 * j], dvy = vs[3 * i + 1] - vs[3 * j + 1], dvz = vs[3 * i + 2] - vs[3 * j + 2];
-        ir[q] = r;
-        tg[q] = -(dx * dvx + dy * dvy + dz * dvz) * r * r * r;
-        ++q;
-      }
-    }
-    if (sorted) dimer_sort_pairs<true>(ir, tg);
-#pragma unroll
-    for (int k = 0; k < 15; ++k) {
-      feat[s * kIn + k] = (ir[k] - mu[k]) * inv_sd[k];
-      if (tang) tang[s * kIn + k] = tg[k] * inv_sd[k];
-    }
-    feat[s * kIn + 15] = 0.f;
-    if (tang) tang[s * kIn + 15] = 0.f;
+    if (tang)
+      pair_features<true>(xs, vs, sorted, mu, inv_sd, feat + s * kIn, tang + s * kIn);
+    else
+      pair_features<false>(xs, vs, sorted, mu, inv_sd, feat + s * kIn, nullptr);
     if (et) {
       double d = 0.0;
 #pragma unroll
       for (int k = 0; k < 18; ++k) d += grad[k * ldx + s] * (double)vs[k];
       et[s] = (float)(d / (double)e_scale);
     }
+  }
+}
+
+// ------------------------------------------------------- training batches
+// A training batch runs as one CUDA graph: its samples are read at the
+// device-side offset ctl[1], the tangent directions are drawn on the device
+// from the device step count ctl[0], and one Adam kernel updates every
+// parameter, clears the gradients and advances ctl.
+//
+// Inputs of samples [off, off + B) of the data set (fp64 SoA [18][ld] x and
+// grad, v[ld]), off = ctl[1]: descriptors and, along a random unit direction u
+// of the 18 coordinates (18 Philox normals of (seed, step ctl[0], sample),
+// normalised), their derivative, et = (dV/dx . u) / e_scale and the energy
+// target e = (V - e_mean) / e_scale - b4.
+__global__ void k_train_inputs(const double* __restrict__ x, const double* __restrict__ v,
+                               const double* __restrict__ grad, long long ld, long long B,
+                               const long long* __restrict__ ctl, unsigned long long seed,
+                               const float* __restrict__ mu, const float* __restrict__ inv_sd, float e_mean,
+                               float e_scale, const float* __restrict__ b4, int sorted, float* __restrict__ feat,
+                               float* __restrict__ tang, float* __restrict__ et, float* __restrict__ e) {
+  const long long step = ctl[0], off = ctl[1];
+  const float b4v = *b4;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < B; s += (long long)gridDim.x * blockDim.x) {
+    const long long j = off + s;
+    float xs[18], u[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) xs[k] = (float)x[k * ld + j];
+    Rng rng(seed, (uint64_t)step, (uint64_t)s);
+    float nn = 0.f;
+#pragma unroll
+    for (int k = 0; k < 18; k += 2) {
+      rng.normal2_f32(u[k], u[k + 1]);
+      nn = fmaf(u[k], u[k], fmaf(u[k + 1], u[k + 1], nn));
+    }
+    const float inv = rsqrtf(nn);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) u[k] *= inv;
+    pair_features<true>(xs, u, sorted, mu, inv_sd, feat + s * kIn, tang + s * kIn);
+    double d = 0.0;
+#pragma unroll
+    for (int k = 0; k < 18; ++k) d += grad[k * ld + j] * (double)u[k];
+    et[s] = (float)(d / (double)e_scale);
+    e[s] = (float)((v[j] - (double)e_mean) / (double)e_scale) - b4v;
+  }
+}
+
+// One Adam step on every parameter of the network (pyvibdmc's Keras
+// training has no counterpart; Adam as Kingma & Ba 2015): the step t =
+// ctl[0] + 1, the learning rate of the cosine schedule lr_min + (lr0 -
+// lr_min) (1 + cos(pi k / steps)) / 2 at k = t - 1 - t0, the gradients
+// cleared after use, the bf16 copies of the weight matrices refreshed; the
+// last block to finish (ticket) advances ctl[0] and the batch offset ctl[1].
+struct AdamAll {
+  float* p[8];
+  float* g[8];
+  float* m[8];
+  float* v[8];
+  uint16_t* wt[8];
+  uint16_t* wn[8];
+  int k[8];
+  long long start[9];
+  int nq;
+  float lr0, lr_min, b1, b2, eps;
+  long long t0, steps, batch;
+};
+
+__global__ void __launch_bounds__(256) k_adam_all(const __grid_constant__ AdamAll A, long long* ctl,
+                                                  unsigned int* ticket) {
+  const long long t = ctl[0] + 1;
+  const long long kk = t - 1 - A.t0;
+  const float lr = A.lr_min + 0.5f * (A.lr0 - A.lr_min) *
+                                  (1.f + cosf(3.14159265358979f * (float)kk / (float)(A.steps > 0 ? A.steps : 1)));
+  const float c1 = 1.0f / (1.0f - powf(A.b1, (float)t)), c2 = 1.0f / (1.0f - powf(A.b2, (float)t));
+  const long long total = A.start[A.nq];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int q = 0;
+    while (q + 1 < A.nq && i >= A.start[q + 1]) ++q;
+    const long long e = i - A.start[q];
+    const float gr = A.g[q][e];
+    const float mi = A.b1 * A.m[q][e] + (1.f - A.b1) * gr;
+    const float vi = A.b2 * A.v[q][e] + (1.f - A.b2) * gr * gr;
+    A.m[q][e] = mi;
+    A.v[q][e] = vi;
+    const float pi = A.p[q][e] - lr * (mi * c1) / (sqrtf(vi * c2) + A.eps);
+    A.p[q][e] = pi;
+    A.g[q][e] = 0.f;
+    if (A.wt[q] || A.wn[q]) {
+      const long long k = e / kH, nn = e % kH;
+      const __nv_bfloat16 b = __float2bfloat16_rn(pi);
+      if (A.wt[q]) A.wt[q][nn * A.k[q] + k] = *reinterpret_cast<const uint16_t*>(&b);
+      if (A.wn[q]) A.wn[q][e] = *reinterpret_cast<const uint16_t*>(&b);
+    }
+  }
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    ctl[0] = t;
+    ctl[1] += A.batch;
+    *ticket = 0u;
   }
 }
 
@@ -886,27 +1047,73 @@ extern "C" int gbdmc_mlp_silu_fwd(const float* z, const float* zt, float* h, flo
 }
 
 extern "C" int gbdmc_mlp_silu_bwd(const float* z, const float* zt, const float* hb, const float* htb, float* zb,
-                                  float* ztb, int64_t n, void* stream) {
-  if (!z || !hb || !zb || n < 0 || (zt && (!htb || !ztb))) {
-    set_error("gbdmc_mlp_silu_bwd: invalid arguments");
+                                  float* ztb, int64_t n, float* gbias, void* stream) {
+  if (!z || !hb || !zb || n < 0 || n % kH || (zt && (!htb || !ztb))) {
+    set_error("gbdmc_mlp_silu_bwd: invalid arguments (n a multiple of 128)");
     return GBDMC_ERR_ARG;
   }
   if (n == 0) return GBDMC_OK;
-  k_silu_bwd<<<ew_grid(n), 256, 0, (cudaStream_t)stream>>>(z, zt, hb, htb, zb, ztb, n);
+  const long long rows = n / kH;
+  long long grid = (rows + 1) / 2;
+  if (grid > 2LL * num_sms()) grid = 2LL * num_sms();
+  k_silu_bwd<<<(int)grid, 256, 0, (cudaStream_t)stream>>>(z, zt, hb, htb, zb, ztb, rows, gbias);
   return check_launch("gbdmc_mlp_silu_bwd");
 }
 
-extern "C" int gbdmc_mlp_head(const float* h3, const float* ht3, const float* w4, float b4, const float* e,
-                              const float* et, int64_t m, float w_e, float w_f, float* h3b, float* ht3b, float* gw4,
-                              float* gb4, double* loss, void* stream) {
+extern "C" int gbdmc_mlp_head(const float* h3, const float* ht3, const float* w4, float b4, const float* b4_dev,
+                              const float* e, const float* et, int64_t m, float w_e, float w_f, float* h3b, float* ht3b,
+                              float* gw4, float* gb4, double* loss, void* stream) {
   if (!h3 || !w4 || !e || !h3b || !gw4 || !gb4 || !loss || m < 1 || (ht3 && (!et || !ht3b))) {
     set_error("gbdmc_mlp_head: invalid arguments");
     return GBDMC_ERR_ARG;
   }
-  long long warps = m < 8LL * 256 * num_sms() / 32 ? m : 8LL * 256 * num_sms() / 32;
-  const int grid = (int)((warps * 32 + 255) / 256);
-  k_head<<<grid, 256, 0, (cudaStream_t)stream>>>(h3, ht3, w4, b4, e, et, m, w_e, w_f, h3b, ht3b, gw4, gb4, loss);
+  long long grid = (m + 7) / 8;
+  if (grid > num_sms()) grid = num_sms();
+  k_head<<<(int)grid, 256, 0, (cudaStream_t)stream>>>(h3, ht3, w4, b4, b4_dev, e, et, m, w_e, w_f, h3b, ht3b, gw4,
+                                                       gb4, loss);
   return check_launch("gbdmc_mlp_head");
+}
+
+extern "C" int gbdmc_mlp_train_inputs(const double* x, const double* v, const double* grad, int64_t ld, int64_t b,
+                                      const int64_t* ctl, uint64_t seed, const float* mu, const float* inv_sd,
+                                      float e_mean, float e_scale, const float* b4_dev, int32_t sort_atoms,
+                                      float* feat, float* tang, float* et, float* e, void* stream) {
+  if (!x || !v || !grad || !ctl || !mu || !inv_sd || !b4_dev || !feat || !tang || !et || !e || b < 1 || ld < b ||
+      sort_atoms < 0 || sort_atoms > 1) {
+    set_error("gbdmc_mlp_train_inputs: invalid arguments");
+    return GBDMC_ERR_ARG;
+  }
+  k_train_inputs<<<ew_grid(b), 256, 0, (cudaStream_t)stream>>>(x, v, grad, ld, b, (const long long*)ctl, seed, mu,
+                                                                 inv_sd, e_mean, e_scale, b4_dev, sort_atoms, feat,
+                                                                 tang, et, e);
+  return check_launch("gbdmc_mlp_train_inputs");
+}
+
+extern "C" int gbdmc_mlp_adam_all(const gbdmc_adam_param_t* params, int32_t nq, float lr0, float lr_min, float b1,
+                                  float b2, float eps, int64_t t0, int64_t steps, int64_t batch, int64_t* ctl,
+                                  uint32_t* ticket, void* stream) {
+  if (!params || nq < 1 || nq > 8 || !ctl || !ticket || steps < 1 || t0 < 0) {
+    set_error("gbdmc_mlp_adam_all: invalid arguments (1 to 8 parameters)");
+    return GBDMC_ERR_ARG;
+  }
+  AdamAll A{};
+  A.nq = nq;
+  A.start[0] = 0;
+  for (int q = 0; q < nq; ++q) {
+    const gbdmc_adam_param_t& P = params[q];
+    if (!P.p || !P.g || !P.m || !P.v || P.n < 1 || ((P.wt || P.wn) && P.n != (int64_t)P.k * kH)) {
+      set_error("gbdmc_mlp_adam_all: invalid parameter %d", q);
+      return GBDMC_ERR_ARG;
+    }
+    A.p[q] = P.p, A.g[q] = P.g, A.m[q] = P.m, A.v[q] = P.v, A.wt[q] = P.wt, A.wn[q] = P.wn, A.k[q] = P.k;
+    A.start[q + 1] = A.start[q] + P.n;
+  }
+  A.lr0 = lr0, A.lr_min = lr_min, A.b1 = b1, A.b2 = b2, A.eps = eps;
+  A.t0 = t0, A.steps = steps, A.batch = batch;
+  long long grid = (A.start[nq] + 255) / 256;
+  if (grid > 2LL * num_sms()) grid = 2LL * num_sms();
+  k_adam_all<<<(int)grid, 256, 0, (cudaStream_t)stream>>>(A, (long long*)ctl, ticket);
+  return check_launch("gbdmc_mlp_adam_all");
 }
 
 extern "C" int gbdmc_mlp_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,

@@ -148,33 +148,42 @@ class MLPSurrogate:
         n = xb.shape[1]
         _capi.check(L.gbdmc_dimer_features(_p(xb), n, n, _p(self.mu), _p(self.inv_sd), _p(vdir), _p(gb),
                                            float(self.e_scale), _p(feat), _p(tang), _p(et), int(self.sort_atoms),
-                                           _s()),
-                    "gbdmc_dimer_features")
+                                           _s()), "gbdmc_dimer_features")
 
     def _alloc(self, B):
         f = lambda *s: torch.empty(*s, dtype=torch.float32, device=self.device)  # noqa: E731
-        self.buf = dict(feat=f(B, 16), tang=f(B, 16), et=f(B), e=f(B), ones=torch.ones(B, 16, device=self.device),
+        self.buf = dict(feat=f(B, 16), tang=f(B, 16), et=f(B), e=f(B),
                         **{f"{k}{l}": f(B, H) for k in ("Z", "Zt", "H", "Ht", "Zb", "Ztb", "Hb", "Htb")
                            for l in (1, 2, 3)},
                         loss=torch.zeros(2, dtype=torch.float64, device=self.device))
-        self.grads = {k: torch.zeros_like(v) for k, v in self.P.items()}
-        self.g16 = torch.zeros(16, H, device=self.device)
+        # the gradients are views of one buffer, cleared by the Adam launch after use
+        n = sum(v.numel() for v in self.P.values())
+        self._gflat = torch.zeros(n, dtype=torch.float32, device=self.device)
+        self.grads, o = {}, 0
+        for k, v in self.P.items():
+            self.grads[k] = self._gflat[o:o + v.numel()].view_as(v)
+            o += v.numel()
+        if getattr(self, "_ctl", None) is None:
+            self._ctl = torch.tensor([self.t, 0], dtype=torch.int64, device=self.device)
+            self._ticket = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._B = B
 
-    def _forward_backward(self, xb, vb, gb, w_e, w_f):
-        """Loss gradients of one minibatch into self.grads (the kernels of a
-        training step before the Adam update).  The output bias b4 enters as a
-        shift of the targets, read on the device, so the launches take no value
-        that changes from step to step and can be captured in a CUDA graph."""
+    def _batch_kernels(self, X, V, G, ld, w_e, w_f, seed):
+        """The kernels of one training batch before the Adam update: inputs of
+        samples [ctl[1], ctl[1] + B) of (X, V, G) (fp64 SoA with leading
+        dimension ld), forward (primal and tangent streams), head and loss,
+        backward with the bias gradients fused into the SiLU backward.  Every
+        value that changes from batch to batch lives on the device, so the
+        launches can be captured in a CUDA graph."""
         L = _capi.load()
-        B = xb.shape[1]
-        b, P, bf, G = self.buf, self.P, self.bf, self.grads
-        vdir = torch.randn(18, B, dtype=torch.float64, device=self.device)
-        vdir /= vdir.norm(dim=0, keepdim=True)
-        self._features(xb, gb, vdir, b["feat"], b["tang"], b["et"])
-        b["e"].copy_(((vb - self.e_mean) / self.e_scale).float() - P["b4"])
+        B = self._B
+        b, P, bf, Gr = self.buf, self.P, self.bf, self.grads
         s = _s()
         ck = _capi.check
-        # forward: primal and tangent streams
+        ck(L.gbdmc_mlp_train_inputs(_p(X), _p(V), _p(G), ld, B, _p(self._ctl), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                    _p(self.mu), _p(self.inv_sd), float(self.e_mean), float(self.e_scale), _p(P["b4"]),
+                                    int(self.sort_atoms), _p(b["feat"]), _p(b["tang"]), _p(b["et"]), _p(b["e"]), s),
+           "train_inputs")
         ck(L.gbdmc_mlp_gemm(_p(b["feat"]), B, 16, _p(bf["W1t"]), _p(P["b1"]), _p(b["Z1"]), s), "gemm")
         ck(L.gbdmc_mlp_gemm(_p(b["tang"]), B, 16, _p(bf["W1t"]), None, _p(b["Zt1"]), s), "gemm")
         ck(L.gbdmc_mlp_silu_fwd(_p(b["Z1"]), _p(b["Zt1"]), _p(b["H1"]), _p(b["Ht1"]), B * H, s), "silu")
@@ -183,100 +192,110 @@ class MLPSurrogate:
             ck(L.gbdmc_mlp_gemm(_p(b[f"Ht{l-1}"]), B, H, _p(bf[wt]), None, _p(b[f"Zt{l}"]), s), "gemm")
             ck(L.gbdmc_mlp_silu_fwd(_p(b[f"Z{l}"]), _p(b[f"Zt{l}"]), _p(b[f"H{l}"]), _p(b[f"Ht{l}"]), B * H, s),
                "silu")
-        for g in G.values():
-            g.zero_()
-        b["loss"].zero_()
-        ck(L.gbdmc_mlp_head(_p(b["H3"]), _p(b["Ht3"]), _p(P["w4"]), 0.0, _p(b["e"]), _p(b["et"]),
-                            B, w_e, w_f, _p(b["Hb3"]), _p(b["Htb3"]), _p(G["w4"]), _p(G["b4"]), _p(b["loss"]), s),
+        # the targets e already carry -b4, so the head adds no b4 (b4's gradient is still accumulated)
+        ck(L.gbdmc_mlp_head(_p(b["H3"]), _p(b["Ht3"]), _p(P["w4"]), 0.0, None, _p(b["e"]), _p(b["et"]),
+                            B, w_e, w_f, _p(b["Hb3"]), _p(b["Htb3"]), _p(Gr["w4"]), _p(Gr["b4"]), _p(b["loss"]), s),
            "head")
-        # backward
         for l in (3, 2, 1):
             ck(L.gbdmc_mlp_silu_bwd(_p(b[f"Z{l}"]), _p(b[f"Zt{l}"]), _p(b[f"Hb{l}"]), _p(b[f"Htb{l}"]),
-                                    _p(b[f"Zb{l}"]), _p(b[f"Ztb{l}"]), B * H, s), "silu_bwd")
+                                    _p(b[f"Zb{l}"]), _p(b[f"Ztb{l}"]), B * H, _p(Gr[f"b{l}"]), s), "silu_bwd")
             K = H if l > 1 else 16
             xin, xtin = (b[f"H{l-1}"], b[f"Ht{l-1}"]) if l > 1 else (b["feat"], b["tang"])
-            ck(L.gbdmc_mlp_gemm_tn(_p(xin), _p(b[f"Zb{l}"]), B, K, _p(G[f"W{l}"]), s), "gemm_tn")
-            ck(L.gbdmc_mlp_gemm_tn(_p(xtin), _p(b[f"Ztb{l}"]), B, K, _p(G[f"W{l}"]), s), "gemm_tn")
-            self.g16.zero_()
-            ck(L.gbdmc_mlp_gemm_tn(_p(b["ones"]), _p(b[f"Zb{l}"]), B, 16, _p(self.g16), s), "gemm_tn")
-            G[f"b{l}"].copy_(self.g16[0])
+            ck(L.gbdmc_mlp_gemm_tn(_p(xin), _p(b[f"Zb{l}"]), B, K, _p(Gr[f"W{l}"]), s), "gemm_tn")
+            ck(L.gbdmc_mlp_gemm_tn(_p(xtin), _p(b[f"Ztb{l}"]), B, K, _p(Gr[f"W{l}"]), s), "gemm_tn")
             if l > 1:
                 wn = bf[f"W{l}n"]
                 ck(L.gbdmc_mlp_gemm(_p(b[f"Zb{l}"]), B, H, _p(wn), None, _p(b[f"Hb{l-1}"]), s), "gemm")
                 ck(L.gbdmc_mlp_gemm(_p(b[f"Ztb{l}"]), B, H, _p(wn), None, _p(b[f"Htb{l-1}"]), s), "gemm")
-        G["W1"][15].zero_()
 
-    def train_batch(self, xb, vb, gb, lr, w_e=1.0, w_f=0.5, graph=False):
-        """One Adam step on a minibatch (x (18, B) fp64, V (B,), dV/dx (18, B)); returns (mse_E, mse_F).
-        With ``graph`` the forward and backward kernels of the step are captured
-        once into a CUDA graph (inputs copied into its fixed buffers) and
-        replayed; the Adam launches, which take the step's learning rate and
-        count, are issued directly."""
+    def _adam(self, lr0, lr_min, t0, steps):
+        """One Adam launch over all parameters (gradients cleared, ctl advanced)."""
         L = _capi.load()
+        tab = (_capi.AdamParam * len(self.P))()
+        for q, (k, p) in enumerate(self.P.items()):
+            a = tab[q]
+            a.p, a.g, a.m, a.v = p.data_ptr(), self.grads[k].data_ptr(), self.M[k].data_ptr(), self.V[k].data_ptr()
+            a.n = p.numel()
+            if k in ("W1", "W2", "W3"):
+                a.wt = self.bf[f"{k}t"].data_ptr()
+                a.wn = self.bf[f"{k}n"].data_ptr() if k != "W1" else None
+                a.k = 16 if k == "W1" else H
+        _capi.check(L.gbdmc_mlp_adam_all(tab, len(self.P), float(lr0), float(lr_min), 0.9, 0.999, 1e-8, int(t0),
+                                         int(steps), int(self._B), _p(self._ctl), _p(self._ticket), _s()),
+                    "gbdmc_mlp_adam_all")
+
+    def loss_gradients(self, xb, vb, gb, w_e=1.0, w_f=0.5, seed=0):
+        """The loss gradients of one minibatch (x, dV/dx (18, B) fp64, V (B,)) in
+        self.grads, and the batch's inputs in self.buf; no update."""
         B = xb.shape[1]
-        if getattr(self, "buf", None) is None or self.buf["feat"].shape[0] != B:
+        if getattr(self, "buf", None) is None or self._B != B:
             self._alloc(B)
             self._tg = None
-        b, P, bf, G = self.buf, self.P, self.bf, self.grads
-        if not graph:
-            self._forward_backward(xb, vb, gb, w_e, w_f)
-        else:
-            key = (B, w_e, w_f, self.e_mean, self.e_scale)
-            if getattr(self, "_tg", None) is None or self._tg[0] != key:
-                sx, sv, sg = xb.clone(), vb.clone(), gb.clone()
-                side = torch.cuda.Stream(device=self.device)
-                side.wait_stream(torch.cuda.current_stream())
-                with torch.cuda.stream(side):
-                    self._forward_backward(sx, sv, sg, w_e, w_f)  # warm-up outside the capture
-                torch.cuda.current_stream().wait_stream(side)
-                gr = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(gr, stream=side):
-                    self._forward_backward(sx, sv, sg, w_e, w_f)
-                torch.cuda.current_stream().wait_stream(side)
-                self._tg = (key, gr, sx, sv, sg)
-            _, gr, sx, sv, sg = self._tg
-            sx.copy_(xb)
-            sv.copy_(vb)
-            sg.copy_(gb)
-            gr.replay()
-        s = _s()
-        ck = _capi.check
+        self._gflat.zero_()
+        self.buf["loss"].zero_()
+        self._ctl[1] = 0
+        self._batch_kernels(xb, vb, gb, B, w_e, w_f, seed)
+        return self.buf["loss"] / B
+
+    def train_batch(self, xb, vb, gb, lr, w_e=1.0, w_f=0.5, seed=0):
+        """One Adam step on a minibatch (x (18, B) fp64, V (B,), dV/dx (18, B));
+        returns (mse_E, mse_F)."""
+        loss = self.loss_gradients(xb, vb, gb, w_e, w_f, seed).clone()
+        self._adam(lr, lr, int(self._ctl[0].item()), 1)
         self.t += 1
-        for k, p in P.items():
-            wt = bf.get(f"{k}t") if k in ("W1", "W2", "W3") else None
-            wn = bf.get(f"{k}n") if k in ("W2", "W3") else None
-            K = 16 if k == "W1" else H
-            ck(L.gbdmc_mlp_adam(_p(p), _p(G[k]), _p(self.M[k]), _p(self.V[k]), p.numel(), lr, 0.9, 0.999, 1e-8,
-                                self.t, _p(wt), _p(wn), K, s), "adam")
-        return b["loss"] / B
+        return loss
 
     def fit(self, x, v, g, epochs=20, batch=4096, lr=2e-3, lr_final=5e-5, w_f=0.5, seed=0, verbose=False,
             graph=True):
         """Train on harvested data: x, g fp64 SoA (18, M) device tensors, v (M,) fp64.
-        ``graph``: replay each step's forward and backward kernels from a CUDA graph."""
+        Each epoch the data set is shuffled into one buffer (three gathers);
+        a batch is then the kernels of ``_batch_kernels`` and one Adam launch,
+        captured once into a CUDA graph (``graph``) whose launches read the
+        batch offset, the step count and the learning rate schedule on the
+        device, so an epoch is nb replays and one read of the loss."""
         self.set_normalisation(x, v)
         M = x.shape[1]
-        steps = epochs * (M // batch)
+        nb = M // batch
+        steps = epochs * nb
+        if getattr(self, "buf", None) is None or self._B != batch:
+            self._alloc(batch)
         gen = torch.Generator(device=self.device).manual_seed(seed)
-        k = 0
-        t0 = time.perf_counter()
+        xe, ve, ge = torch.empty_like(x), torch.empty_like(v), torch.empty_like(g)
+        self._gflat.zero_()
+        self._ctl[0] = self.t
+        t0 = self.t
+        body = lambda: (self._batch_kernels(xe, ve, ge, M, 1.0, w_f, seed),  # noqa: E731
+                        self._adam(lr, lr_final, t0, steps))
+        gr = None
+        tstart = time.perf_counter()
         for ep in range(epochs):
             perm = torch.randperm(M, device=self.device, generator=gen)
-            tot = torch.zeros(2, dtype=torch.float64, device=self.device)
-            nb = M // batch
+            torch.index_select(x, 1, perm, out=xe)
+            torch.index_select(v, 0, perm, out=ve)
+            torch.index_select(g, 1, perm, out=ge)
+            self._ctl[1] = 0
+            self.buf["loss"].zero_()
             for i in range(nb):
-                idx = perm[i * batch:(i + 1) * batch]
-                lr_k = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps, 1)))
-                tot += self.train_batch(x[:, idx].contiguous(), v[idx], g[:, idx].contiguous(), lr_k, w_f=w_f,
-                                        graph=graph)
-                k += 1
-            rec = dict(epoch=ep, mse_e=float(tot[0] / nb), mse_f=float(tot[1] / nb),
-                       rmse_e_cm=math.sqrt(float(tot[0] / nb)) * self.e_scale / Constants.atomic_units["wavenumbers"])
+                if not graph:
+                    body()
+                    continue
+                if gr is None:
+                    side = torch.cuda.Stream(device=self.device)
+                    side.wait_stream(torch.cuda.current_stream())
+                    gr = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(gr, stream=side):
+                        body()
+                    torch.cuda.current_stream().wait_stream(side)
+                gr.replay()
+            tot = self.buf["loss"].cpu().numpy() / (nb * batch)
+            rec = dict(epoch=ep, mse_e=float(tot[0]), mse_f=float(tot[1]),
+                       rmse_e_cm=math.sqrt(float(tot[0])) * self.e_scale / Constants.atomic_units["wavenumbers"])
             self.history.append(rec)
             if verbose:
                 print(rec, flush=True)
         torch.cuda.synchronize()
-        self.train_seconds = time.perf_counter() - t0
+        self.t += steps
+        self.train_seconds = time.perf_counter() - tstart
         return self
 
     def state_dict(self):

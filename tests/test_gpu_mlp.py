@@ -118,9 +118,7 @@ def test_training_gradients_match_oracle():
     outside the bars."""
     m, x, xs, v, g = _small_model(1)
     P0 = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
-    torch.manual_seed(0)
-    torch.cuda.manual_seed(0)
-    m.train_batch(xs, v, g, lr=0.0)  # lr 0: gradients only (Adam with lr 0 leaves the parameters)
+    m.loss_gradients(xs, v, g)
     Gg = {k: t.detach().cpu().double().numpy() for k, t in m.grads.items()}
     b = m.buf
     D = b["feat"].cpu().double().numpy()
@@ -148,8 +146,10 @@ def test_training_gradients_match_oracle():
     Dp[:, [3, 4]] = Dp[:, [4, 3]]
     planted = errors(mo.mlp_loss_grads_bf16(P0, Dp, U, e, et, 1.0, 0.5)[0])
     assert min(planted.values()) > 1e-3, planted
+    m.train_batch(xs, v, g, lr=0.0)  # Adam with lr 0 leaves the parameters and clears the gradients
     for k, t in m.P.items():
         np.testing.assert_array_equal(t.detach().cpu().double().numpy().ravel(), np.ravel(P0[k]))
+    assert not any(bool(t.any()) for t in m.grads.values())
 
 
 def test_inference_kernel_matches_oracle_forward():
