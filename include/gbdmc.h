@@ -425,11 +425,21 @@ typedef struct {
   float* ke;
 } gbdmc_walkers_f32_t;
 
-/* Training kernels.  Y[M x 128] = X[M x K] W + b (K = 16 or 128; X fp32 rounded to bf16). */
+/* Training kernels (bf16 operands, fp32 accumulation).  mma.sync m16n8k16:
+ * Y[M x 128] = X[M x K] W + b (K = 16 or 128; X fp32 rounded to bf16). */
 int gbdmc_mlp_gemm(const float* x_dev, int64_t m, int32_t k, const uint16_t* wt_dev, const float* bias_dev,
                    float* y_dev, void* stream);
 /* G[K x 128] += X^T D over the m rows (fp32 atomics). */
 int gbdmc_mlp_gemm_tn(const float* x_dev, const float* d_dev, int64_t m, int32_t k, float* g_dev, void* stream);
+/* The same two GEMMs on the tcgen05 tensor cores (M = N = 128 MMAs, the accumulator in tensor memory,
+ * operands staged in the canonical K-major layout; gemm_tn stages X^T and D^T and adds each CTA's partial
+ * with one fp32 atomic per element). */
+int gbdmc_mlp_gemm_tc(const float* x_dev, int64_t m, int32_t k, const uint16_t* wt_dev, const float* bias_dev,
+                      float* y_dev, void* stream);
+int gbdmc_mlp_gemm_tn_tc(const float* x_dev, const float* d_dev, int64_t m, int32_t k, float* g_dev, void* stream);
+/* 1 if a bounded tensor-core wait of the tcgen05 training GEMMs gave up since the last clear (synchronises),
+ * 0 if not, -1 on a CUDA error; clear != 0 resets it. */
+int gbdmc_mlp_gemm_status(int32_t clear);
 /* H = silu(Z), Ht = silu'(Z) Zt (Zt/Ht may be NULL). */
 int gbdmc_mlp_silu_fwd(const float* z_dev, const float* zt_dev, float* h_dev, float* ht_dev, int64_t n, void* stream);
 /* Zb = silu'(Z) Hb + silu''(Z) Zt Htb, Ztb = silu'(Z) Htb (Zt/Htb/Ztb may be NULL) on rows of 128 columns

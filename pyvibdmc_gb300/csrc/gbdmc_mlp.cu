@@ -1,16 +1,20 @@
-// MLP surrogate of the water-dimer PES on BF16 tensor cores (mma.sync
-// m16n8k16, FP32 accumulation).
+// MLP surrogate of the water-dimer PES: the mma.sync (m16n8k16, BF16, FP32
+// accumulation) inference path, the training pipeline and the surrogate DMC
+// step's audit and counting kernels.
 //
 // Network: 15 inverse O/H distances (normalised, padded to 16) -> 128 -> 128
-// -> 128 (SiLU) -> 1.  Inference keeps a warp's 16 walkers' activations in
-// registers from layer to layer: the m16n8 accumulator fragments of one layer
-// are repacked as the m16k16 A fragments of the next, and the weights stay in
-// shared memory for the whole persistent CTA.
+// -> 128 (SiLU) -> 1.  The mma.sync inference keeps a warp's 16 walkers'
+// activations in registers from layer to layer: the m16n8 accumulator
+// fragments of one layer are repacked as the m16k16 A fragments of the next,
+// and the weights stay in shared memory for the whole persistent CTA.
 //
-// Training (force matching) uses the same fragments in three generic kernels:
-// Y = X W (+b), G += X^T D, and fused SiLU forward/backward with a tangent
-// (directional-derivative) stream, so that d(E . u)/dW -- the gradient of the
-// force residual -- is one more pass of the same GEMMs.
+// Training (force matching): the GEMMs Y = X W (+b) and G += X^T D run on the
+// tcgen05 tensor cores (gbdmc_mlp_tc.cu); here are the fused SiLU
+// forward/backward with a tangent (directional-derivative) stream, so that
+// d(E . u)/dW -- the gradient of the force residual -- is one more pass of
+// the same GEMMs, the head, the batch inputs and the fused Adam step.
+#include <mutex>
+
 #include "gbdmc_mlp_common.cuh"
 
 namespace gbdmc {
@@ -1003,6 +1007,19 @@ GBDMC_BOUNDS_READER(bounds_read_mlp)
 
 using namespace gbdmc;
 
+// Set by the tcgen05 training GEMMs when a bounded tensor-core wait gave up.
+__device__ int g_tc_gemm_err;
+
+static int* tc_gemm_err_ptr() {
+  static std::mutex mu;
+  static int* ptr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptr[dev] && cudaGetSymbolAddress((void**)&ptr[dev], g_tc_gemm_err) != cudaSuccess) ptr[dev] = nullptr;
+  return ptr[dev];
+}
+
 extern "C" int gbdmc_mlp_gemm(const float* x, int64_t m, int32_t k, const uint16_t* wt, const float* bias, float* y,
                               void* stream) {
   if (!x || !wt || !y || m < 0 || (k != 16 && k != 128)) {
@@ -1034,6 +1051,47 @@ extern "C" int gbdmc_mlp_gemm_tn(const float* x, const float* d, int64_t m, int3
   else
     k_gemm_tn<128><<<(int)grid, 256, 0, s>>>(x, d, m, g);
   return check_launch("gbdmc_mlp_gemm_tn");
+}
+
+extern "C" int gbdmc_mlp_gemm_tc(const float* x, int64_t m, int32_t k, const uint16_t* wt, const float* bias, float* y,
+                              void* stream) {
+  if (!x || !wt || !y || m < 0 || (k != 16 && k != 128)) {
+    set_error("gbdmc_mlp_gemm_tc: invalid arguments (k must be 16 or 128)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  int* err = tc_gemm_err_ptr();
+  if (!err) {
+    set_error("gbdmc_mlp_gemm_tc: no device status word");
+    return GBDMC_ERR_CUDA;
+  }
+  return launch_tc_gemm_xw(x, m, k, wt, bias, y, err, (cudaStream_t)stream);
+}
+
+extern "C" int gbdmc_mlp_gemm_tn_tc(const float* x, const float* d, int64_t m, int32_t k, float* g, void* stream) {
+  if (!x || !d || !g || m < 0 || (k != 16 && k != 128)) {
+    set_error("gbdmc_mlp_gemm_tn_tc: invalid arguments (k must be 16 or 128)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  int* err = tc_gemm_err_ptr();
+  if (!err) {
+    set_error("gbdmc_mlp_gemm_tn_tc: no device status word");
+    return GBDMC_ERR_CUDA;
+  }
+  return launch_tc_gemm_tn(x, d, m, k, g, err, (cudaStream_t)stream);
+}
+
+extern "C" int gbdmc_mlp_gemm_status(int32_t clear) {
+  int* err = tc_gemm_err_ptr();
+  if (!err) return -1;
+  int v = 0;
+  if (cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (clear && v) {
+    const int z = 0;
+    if (cudaMemcpy(err, &z, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+  }
+  return v;
 }
 
 extern "C" int gbdmc_mlp_silu_fwd(const float* z, const float* zt, float* h, float* ht, int64_t n, void* stream) {

@@ -475,6 +475,206 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
   teardown<kGroups>(tmem);
 }
 
+// ------------------------------------------------------------ training GEMMs
+// The GEMMs of a training step on the same tensor-core path: 128-thread CTAs,
+// M = 128 x N = 128 MMAs with K = 16 per instruction, operands in shared
+// memory in the canonical K-major layout, the fp32 accumulator in 128 TMEM
+// columns, bounded mbarrier waits (a timeout sets *err and the CTA returns).
+
+// Y[M x 128] = X[M x K] W[K x 128] (+ bias): tiles of 128 rows, one row per
+// thread.  B = Wt (n-major [128][K], bf16) staged once per CTA; A = the tile's
+// rows of X rounded to bf16; the bias is added in the fp32 epilogue.
+template <int K>
+struct XwSmem {
+  alignas(128) unsigned char w[kN * K * 2];
+  alignas(128) unsigned char a[kRows * K * 2];
+  alignas(8) unsigned long long mbar;
+  uint32_t tmem_base;
+};
+
+__device__ __forceinline__ uint32_t tc_alloc_setup(uint32_t* base_slot, unsigned long long* mbar) {
+  if (threadIdx.x == 0) mbar_init(saddr(mbar));
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(base_slot)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  return *base_slot;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict__ X, long long M,
+                                                         const uint16_t* __restrict__ Wt,
+                                                         const float* __restrict__ bias, float* __restrict__ Y,
+                                                         int* __restrict__ err) {
+  constexpr int KG = K / 8;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  XwSmem<K>& sm = *reinterpret_cast<XwSmem<K>*>(smraw);
+  const int t = threadIdx.x;
+  for (int c = t; c < kN * KG; c += blockDim.x) {
+    const int n = c / KG, kg = c % KG;
+    *reinterpret_cast<uint4*>(sm.w + canon_off(n, 8 * kg, KG)) =
+        __ldg(reinterpret_cast<const uint4*>(Wt + (size_t)n * K + 8 * kg));
+  }
+  const uint32_t tmem = tc_alloc_setup(&sm.tmem_base, &sm.mbar);
+  const uint32_t trow = tmem + ((uint32_t)(32 * (t >> 5)) << 16);
+  uint32_t phase = 0;
+  for (long long base = (long long)blockIdx.x * kRows; base < M; base += (long long)gridDim.x * kRows) {
+    const long long r = base + t;
+#pragma unroll
+    for (int kg = 0; kg < KG; ++kg) {
+      float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+      if (r < M) {
+        lo = *reinterpret_cast<const float4*>(X + r * K + 8 * kg);
+        hi = *reinterpret_cast<const float4*>(X + r * K + 8 * kg + 4);
+      }
+      *reinterpret_cast<uint4*>(sm.a + canon_off(t, 8 * kg, KG)) =
+          make_uint4(pack_bf16(lo.x, lo.y), pack_bf16(lo.z, lo.w), pack_bf16(hi.x, hi.y), pack_bf16(hi.z, hi.w));
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc_fence_after();
+      const uint32_t a0 = saddr(sm.a), b0 = saddr(sm.w);
+#pragma unroll
+      for (int s = 0; s < K / 16; ++s)
+        umma(tmem, smem_desc(a0 + 256u * s, kCore, KG * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
+             s > 0 ? 1u : 0u);
+      umma_commit(saddr(&sm.mbar));
+    }
+    const bool ok = mbar_wait(saddr(&sm.mbar), phase);
+    phase ^= 1u;
+    tc_fence_after();
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      break;
+    }
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float rr[32];
+      tmem_ld32(trow + 32 * c, rr);
+      if (r < M) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          const int col = 32 * c + j;
+          float4 o = make_float4(rr[j], rr[j + 1], rr[j + 2], rr[j + 3]);
+          if (bias) {
+            o.x += bias[col];
+            o.y += bias[col + 1];
+            o.z += bias[col + 2];
+            o.w += bias[col + 3];
+          }
+          *reinterpret_cast<float4*>(Y + r * kN + col) = o;
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();  // TMEM rows read and A free before the next tile's MMAs
+  }
+  teardown<1>(tmem);
+}
+
+// G[K x 128] += X[M x K]^T D[M x 128]: the sum over the M rows runs along the
+// MMA's K.  A = X^T (rows = the K features; for K = 16 rows 16..127 stay
+// zero), B = D^T (rows = the 128 outputs), both staged transposed in the
+// canonical K-major layout 128 rows of X and D at a time: lane l of warp w
+// loads column 32 w + l of 8 consecutive rows (each load a coalesced 128-byte
+// row segment across the warp) and stores them as one 16-byte core-matrix
+// row.  A CTA accumulates its chunks in TMEM and adds its K x 128 partial to
+// G with fp32 vector atomics (four elements each).
+struct TnSmem {
+  alignas(128) unsigned char a[kRows * kRows * 2];
+  alignas(128) unsigned char b[kN * kRows * 2];
+  alignas(8) unsigned long long mbar;
+  uint32_t tmem_base;
+};
+
+// 8 rows r0 .. r0 + 7 of column c of a row-major [rows][ld] fp32 matrix as
+// 8 bf16 in one 16-byte value (rows at or past r_end read as 0).
+__device__ __forceinline__ uint4 column8_bf16(const float* __restrict__ P, long long ld, long long r0,
+                                              long long r_end, int c) {
+  float v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = (r0 + i < r_end) ? P[(r0 + i) * ld + c] : 0.f;
+  return make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_tc_gemm_tn(const float* __restrict__ X, const float* __restrict__ D,
+                                                         long long M, long long rows_per_cta, float* __restrict__ G,
+                                                         int* __restrict__ err) {
+  constexpr int KG = kRows / 8;  // 16 core columns: 128 rows of X and D per chunk
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  TnSmem& sm = *reinterpret_cast<TnSmem*>(smraw);
+  const int t = threadIdx.x, w = t >> 5, l = t & 31;
+  if (K < kRows)
+    for (int c = t; c < kRows * kRows * 2 / 16; c += blockDim.x)
+      reinterpret_cast<uint4*>(sm.a)[c] = make_uint4(0u, 0u, 0u, 0u);
+  const uint32_t tmem = tc_alloc_setup(&sm.tmem_base, &sm.mbar);
+  const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);
+  const long long r_begin = (long long)blockIdx.x * rows_per_cta;
+  const long long r_end = r_begin + rows_per_cta < M ? r_begin + rows_per_cta : M;
+  uint32_t phase = 0;
+  bool any = false, ok = true;
+  for (long long c0 = r_begin; c0 < r_end; c0 += kRows) {
+    // B = D^T: output column n = 32 w + l, the 16 blocks of 8 rows
+#pragma unroll 8
+    for (int sb = 0; sb < KG; ++sb)
+      *reinterpret_cast<uint4*>(sm.b + canon_off(32 * w + l, 8 * sb, KG)) =
+          column8_bf16(D, kN, c0 + 8 * sb, r_end, 32 * w + l);
+    if (K == kRows) {
+#pragma unroll 8
+      for (int sb = 0; sb < KG; ++sb)
+        *reinterpret_cast<uint4*>(sm.a + canon_off(32 * w + l, 8 * sb, KG)) =
+            column8_bf16(X, K, c0 + 8 * sb, r_end, 32 * w + l);
+    } else {  // K = 16: feature t % 16, blocks t / 16 and t / 16 + 8
+      const int f = t % K;
+      for (int sb = t / K; sb < KG; sb += kThreads / K)
+        *reinterpret_cast<uint4*>(sm.a + canon_off(f, 8 * sb, KG)) = column8_bf16(X, K, c0 + 8 * sb, r_end, f);
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc_fence_after();
+      const uint32_t a0 = saddr(sm.a), b0 = saddr(sm.b);
+#pragma unroll
+      for (int s = 0; s < KG / 2; ++s)
+        umma(tmem, smem_desc(a0 + 256u * s, kCore, KG * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
+             (any || s > 0) ? 1u : 0u);
+      umma_commit(saddr(&sm.mbar));
+    }
+    ok = mbar_wait(saddr(&sm.mbar), phase);
+    phase ^= 1u;
+    tc_fence_after();
+    any = true;
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      break;
+    }
+  }
+  if (any && ok) {
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float rr[32];
+      tmem_ld32(trow + 32 * c, rr);
+      if (t < K) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4)  // vector atomics: a quarter of the transactions
+          atomicAdd(reinterpret_cast<float4*>(G + t * kN + 32 * c + j),
+                    make_float4(rr[j], rr[j + 1], rr[j + 2], rr[j + 3]));
+      }
+    }
+  }
+  teardown<1>(tmem);
+}
+
 }  // namespace tc
 
 int tc_smem_bytes() { return (int)sizeof(tc::TcSmem) + 1024; }
@@ -510,6 +710,50 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
   launch_pdl_smem(tc::k_mlp_tc_move_energy, g, tc::kThreads * tc::kGroups, (size_t)tc_group_smem_bytes(), s, S, T,
                   net, in, out, ctrl, list, flags, audit, nz, step_f32(S), feat_box(net));
   return check_launch("gbdmc_mlp_sim_step (tcgen05)");
+}
+
+// The training GEMMs on tcgen05 (err: a device int set to 1 if a bounded
+// tensor-core wait gave up; the caller's buffer).
+int launch_tc_gemm_xw(const float* x, long long m, int k, const uint16_t* wt, const float* bias, float* y, int* err,
+                      cudaStream_t s) {
+  // at least 70 KB of shared memory, so that at most three CTAs share an SM and
+  // their 3 x 128 TMEM columns always fit (an allocation never waits)
+  int smem = (int)(k == 16 ? sizeof(tc::XwSmem<16>) : sizeof(tc::XwSmem<128>)) + 1024;
+  if (smem < 70 * 1024) smem = 70 * 1024;
+  const void* f = k == 16 ? (const void*)tc::k_tc_gemm_xw<16> : (const void*)tc::k_tc_gemm_xw<128>;
+  const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) {
+    set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  long long g = (m + tc::kRows - 1) / tc::kRows;
+  if (g > 3LL * num_sms()) g = 3LL * num_sms();
+  if (k == 16)
+    tc::k_tc_gemm_xw<16><<<(int)g, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+  else
+    tc::k_tc_gemm_xw<128><<<(int)g, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+  return check_launch("gbdmc_mlp_gemm (tcgen05)");
+}
+
+int launch_tc_gemm_tn(const float* x, const float* d, long long m, int k, float* g, int* err, cudaStream_t s) {
+  int smem = (int)sizeof(tc::TnSmem) + 1024;
+  if (smem < 70 * 1024) smem = 70 * 1024;  // at most three CTAs (3 x 128 TMEM columns) per SM
+  const void* f = k == 16 ? (const void*)tc::k_tc_gemm_tn<16> : (const void*)tc::k_tc_gemm_tn<128>;
+  const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) {
+    set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  // one 128-row chunk per CTA while the chunks fit three CTAs per SM
+  const long long chunks = (m + tc::kRows - 1) / tc::kRows;
+  long long per = 1;
+  if ((chunks + per - 1) / per > 3LL * num_sms()) per = (chunks + 3LL * num_sms() - 1) / (3LL * num_sms());
+  const long long grid = (chunks + per - 1) / per;
+  if (k == 16)
+    tc::k_tc_gemm_tn<16><<<(int)grid, tc::kThreads, smem, s>>>(x, d, m, per * tc::kRows, g, err);
+  else
+    tc::k_tc_gemm_tn<128><<<(int)grid, tc::kThreads, smem, s>>>(x, d, m, per * tc::kRows, g, err);
+  return check_launch("gbdmc_mlp_gemm_tn (tcgen05)");
 }
 
 GBDMC_BOUNDS_READER(bounds_read_mlp_tc)

@@ -22,32 +22,38 @@ def bf(t):
     return t.to(torch.bfloat16).float()
 
 
+@pytest.mark.parametrize("engine", ["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("K", [16, 128])
 @pytest.mark.parametrize("M", [1, 37, 1000, 4096])
-def test_gemm_xw_matches_torch(K, M):
+def test_gemm_xw_matches_torch(K, M, engine):
     L = _capi.load()
+    gemm = L.gbdmc_mlp_gemm if engine == "mma_sync" else L.gbdmc_mlp_gemm_tc
     g = torch.Generator(device="cuda").manual_seed(K + M)
     X = torch.randn(M, K, device="cuda", generator=g)
     W = torch.randn(K, 128, device="cuda", generator=g) / np.sqrt(K)
     b = torch.randn(128, device="cuda", generator=g)
     Wt = W.t().contiguous().to(torch.bfloat16).view(torch.int16)
     Y = torch.empty(M, 128, device="cuda")
-    _capi.check(L.gbdmc_mlp_gemm(_p(X), M, K, _p(Wt), _p(b), _p(Y), _s()))
+    _capi.check(gemm(_p(X), M, K, _p(Wt), _p(b), _p(Y), _s()))
     ref = bf(X) @ bf(W) + b
     torch.testing.assert_close(Y, ref, rtol=1e-4, atol=1e-4)
+    assert L.gbdmc_mlp_gemm_status(1) == 0
 
 
+@pytest.mark.parametrize("engine", ["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("K", [16, 128])
 @pytest.mark.parametrize("M", [5, 64, 3001])
-def test_gemm_tn_matches_torch(K, M):
+def test_gemm_tn_matches_torch(K, M, engine):
     L = _capi.load()
+    gemm_tn = L.gbdmc_mlp_gemm_tn if engine == "mma_sync" else L.gbdmc_mlp_gemm_tn_tc
     g = torch.Generator(device="cuda").manual_seed(7 * K + M)
     X = torch.randn(M, K, device="cuda", generator=g)
     D = torch.randn(M, 128, device="cuda", generator=g)
     G = torch.ones(K, 128, device="cuda")
-    _capi.check(L.gbdmc_mlp_gemm_tn(_p(X), _p(D), M, K, _p(G), _s()))
+    _capi.check(gemm_tn(_p(X), _p(D), M, K, _p(G), _s()))
     ref = 1.0 + bf(X).t() @ bf(D)
     torch.testing.assert_close(G, ref, rtol=1e-4, atol=1e-3)
+    assert L.gbdmc_mlp_gemm_status(1) == 0
 
 
 def _group_copies(x):
@@ -104,7 +110,8 @@ def _small_model(seed=0):
     return m, x, xs, v, g
 
 
-def test_training_gradients_match_oracle():
+@pytest.mark.parametrize("train_engine", ["auto", "mma_sync", "tcgen05"])
+def test_training_gradients_match_oracle(train_engine):
     """One training step's gradients against the oracle of the training
     kernels' arithmetic (bf16 GEMM operands, fp32 buffers and accumulation).
     What remains is the fp32 summation order of the tensor cores and the
@@ -117,6 +124,7 @@ def test_training_gradients_match_oracle():
     planted mistake in the oracle (descriptor columns 3 and 4 swapped) is far
     outside the bars."""
     m, x, xs, v, g = _small_model(1)
+    m.train_engine = train_engine  # the training GEMMs' engines
     P0 = {k: t.detach().cpu().double().numpy() for k, t in m.P.items()}
     m.loss_gradients(xs, v, g)
     Gg = {k: t.detach().cpu().double().numpy() for k, t in m.grads.items()}
