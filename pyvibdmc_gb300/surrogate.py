@@ -265,6 +265,8 @@ class MLPSurrogate:
         self.set_normalisation(x, v)
         M = x.shape[1]
         nb = M // batch
+        if nb < 1:
+            raise ValueError(f"the data set ({M} samples) is smaller than one batch ({batch})")
         steps = epochs * nb
         if getattr(self, "buf", None) is None or self._B != batch:
             self._alloc(batch)

@@ -72,3 +72,27 @@ def test_static_scratch_rejects_oversized_capacity():
                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == _capi.ERR_CAPACITY
     assert b"static scratch" in L.gbdmc_last_error()
+
+
+def _sim_cont(seed, n=3000):
+    _, m = oracle.h2o_config()
+    x0 = oracle.h2o_equilibrium()[None] + 0.05 * oracle.InjectedNoise(22).standard_normal((n, 3, 3))
+    sim = pg.DMC_Sim(num_walkers=n, num_timesteps=8, equil_steps=10 ** 6, atoms=["O", "H", "H"], masses=m,
+                     delta_t=10.0, potential=pg.h2o_local_mode(), start_structures=x0, seed=seed,
+                     weighting="continuous", write_files=False)
+    sim._init_device()
+    return sim
+
+
+def test_static_scratch_after_another_shape_and_continuous_weighting():
+    """The static array left dirty by steps of another shape (500 walkers,
+    continuous weighting) changes nothing: discrete and continuous steps
+    through the static scratch then match the caller-scratch steps."""
+    _two_steps(_sim_cont(5, n=500), static=True)
+    n_a, vref_a, _, x_a = _two_steps(_sim(17), static=False)
+    n_b, vref_b, _, x_b = _two_steps(_sim(17), static=True)
+    assert n_a == n_b and abs(vref_a - vref_b) <= 1e-12 and np.array_equal(x_a, x_b)
+    n_a, vref_a, _, (x_a, w_a) = _two_steps(_sim_cont(9), static=False)
+    n_b, vref_b, _, (x_b, w_b) = _two_steps(_sim_cont(9), static=True)
+    assert n_a == n_b and abs(vref_a - vref_b) <= 1e-12
+    assert np.array_equal(x_a, x_b) and np.array_equal(w_a, w_b)
