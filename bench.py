@@ -420,68 +420,62 @@ def run_ours(args):
 
 
 def run_e2e_windows(sim, L, dev, windows, run_scratch):
-    """The headline e2e: the reference-facing C-ABI call with host buffers.
-    The walkers live in page-locked host memory between calls; per window
-    (one bench step) the N walkers' coordinates and ancestor ids are copied
-    host -> device, gbdmc_sim_run advances them DESC_WINDOW steps, and the
-    control block, then the N' walkers' coordinates, potentials and ancestor
-    ids and the window's vref / population history come back device -> host.
-    Host waits: one after the control block (for N'), one after the walkers."""
+    """The headline e2e: the reference-facing C-ABI call with host buffers,
+    gbdmc_sim_run_host.  The walkers (coordinates, potentials, ancestor ids,
+    lineage keys) live in page-locked host memory between calls, as the
+    reference's NumPy walker arrays do; per window (one bench step) one call
+    copies the N walkers host -> device, runs DESC_WINDOW steps in one
+    gbdmc_sim_run launch, and copies the control block, every slot of the
+    output buffers and the window's vref / population history device -> host,
+    with one stream wait."""
     import torch
     from pyvibdmc_gb300 import _capi
     A3 = 3 * sim.natoms
-    cap = int(sim.capacity)
     sim._compact()
+    ld = int(sim._sim.ld)
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
     cb = C.sizeof(_capi.Ctrl)
-    n = int(sim._read_ctrl().n)
-    b = sim._bufs[sim._cur]
-    hx = torch.empty((A3, cap), dtype=torch.float64).pin_memory()
-    hv = torch.empty(cap, dtype=torch.float64).pin_memory()
-    hw = torch.empty(cap, dtype=torch.int32).pin_memory()
+    b0, b1 = sim._bufs[sim._cur], sim._bufs[1 - sim._cur]
+    hx = torch.empty((A3, ld), dtype=torch.float64).pin_memory()
+    hv = torch.empty(ld, dtype=torch.float64).pin_memory()
+    hw = torch.empty(ld, dtype=torch.int32).pin_memory()
+    hk = torch.empty(ld, dtype=torch.int64).pin_memory()
     hc = torch.empty(cb, dtype=torch.uint8).pin_memory()
     hh = torch.empty((2, DESC_WINDOW), dtype=torch.float64).pin_memory()
-    hx[:, :n].copy_(b["x"][:, :n])
-    hw[:n].copy_(b["who"][:n])
-    ctrl_ptr = C.c_void_p(sim._ctrl.data_ptr())
-    step = int(sim._read_ctrl().step)
+    n = int(sim._read_ctrl().n)
+    hx[:, :n].copy_(b0["x"][:, :n])
+    hw[:n].copy_(b0["who"][:n])
+    hk[:n].copy_(b0["key"][:n])
+    hc.copy_(sim._ctrl)
     torch.cuda.synchronize()
+    ctrl_host = _capi.Ctrl.from_address(hc.data_ptr())
+    host = _capi.HostWalkersC(x=hx.data_ptr(), v=hv.data_ptr(), who=hw.data_ptr(), key=hk.data_ptr(), ld=ld)
+    w_src, w_dst = sim._walker_struct(b0, False), sim._walker_struct(b1, False)
+    ctrl_ptr, scr, hist = C.c_void_p(sim._ctrl.data_ptr()), C.c_void_p(run_scratch.data_ptr()), C.c_void_p(hh.data_ptr())
     h2d = d2h = 0
     total = 0.0
     t0 = time.perf_counter()
     for _ in range(windows):
-        src, dst = sim._bufs[sim._cur], sim._bufs[1 - sim._cur]
-        src["x"][:, :n].copy_(hx[:, :n], non_blocking=True)
-        src["who"][:n].copy_(hw[:n], non_blocking=True)
-        h2d += (A3 * 8 + 4) * n
-        _capi.check(L.gbdmc_sim_run(C.byref(sim._sim), C.byref(sim._walker_struct(src, False)),
-                                    C.byref(sim._walker_struct(dst, False)), ctrl_ptr,
-                                    C.c_void_p(run_scratch.data_ptr()), step + DESC_WINDOW, DESC_WINDOW, sp),
-                    "sim_run")
-        sim._cur = 1 - sim._cur
-        hc.copy_(sim._ctrl, non_blocking=True)
-        stream.synchronize()
-        c = _capi.Ctrl.from_buffer_copy(hc.numpy().tobytes())
-        if c.status:
-            raise RuntimeError(f"device status {c.status} in the e2e leg")
-        k = int(c.step) - step
-        hx[:, :int(c.n)].copy_(dst["x"][:, :int(c.n)], non_blocking=True)
-        hv[:int(c.n)].copy_(dst["v"][:int(c.n)], non_blocking=True)
-        hw[:int(c.n)].copy_(dst["who"][:int(c.n)], non_blocking=True)
-        hh[0, :k].copy_(sim._hist["vref"][step:step + k], non_blocking=True)
-        hh[1, :k].copy_(sim._hist["pop"][step:step + k], non_blocking=True)
-        stream.synchronize()
+        n, step = int(ctrl_host.n), int(ctrl_host.step)
+        _capi.check(L.gbdmc_sim_run_host(C.byref(sim._sim), C.byref(host), C.byref(w_src), C.byref(w_dst), ctrl_ptr,
+                                         C.byref(ctrl_host), scr, step + DESC_WINDOW, DESC_WINDOW, hist, sp),
+                    "gbdmc_sim_run_host")
+        if ctrl_host.status:
+            raise RuntimeError(f"device status {ctrl_host.status} in the e2e leg")
+        k = int(ctrl_host.step) - step
         total += n + float(hh[1, :k - 1].sum())  # the population entering each of the k steps
-        n, step = int(c.n), int(c.step)
-        d2h += cb + (A3 * 8 + 8 + 4) * n + 16 * k
+        h2d += (A3 * 8 + 4 + 8) * n
+        d2h += cb + (A3 * 8 + 8 + 4 + 8) * ld + 16 * k
     secs = time.perf_counter() - t0
+    sim._cur, sim._lazy = 1 - sim._cur, False  # the walkers are in the output buffer (and on the host)
     return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // windows,
             "d2h_bytes_per_step": d2h // windows, "steps": windows,
             "path": f"walkers in page-locked host memory between calls; per bench step (one {DESC_WINDOW}-step "
-                    "window) H2D of the N walkers' coordinates and ancestor ids, one gbdmc_sim_run call (C ABI), "
-                    "D2H of the control block, the N' walkers' coordinates, potentials and ancestor ids and the "
-                    "window's vref and population history; two host waits per window"}
+                    "window) one gbdmc_sim_run_host call (C ABI): H2D of the N walkers' coordinates, ancestor ids "
+                    "and lineage keys, one gbdmc_sim_run launch, D2H of the control block, every slot of the output "
+                    "walkers (coordinates, potentials, ancestor ids, keys) and the window's vref and population "
+                    "history; one stream wait per window"}
 
 
 def _timed_graph_rate(run_steps, pop_of, steps):

@@ -268,6 +268,34 @@ int gbdmc_lineage_noise(const gbdmc_sim_t* sim, const uint64_t* keys_dev, int64_
 int gbdmc_sim_run(const gbdmc_sim_t* sim, const gbdmc_walkers_t* src, const gbdmc_walkers_t* dst,
                   gbdmc_ctrl_t* ctrl_dev, void* scratch_dev, int64_t step_end, int32_t max_steps, void* stream);
 
+/* Walkers in (page-locked) host memory for gbdmc_sim_run_host, in the SoA
+ * layout of gbdmc_walkers_t with leading dimension ld >= sim->ld. */
+typedef struct {
+  double* x;     /* [3A][ld] coordinates (bohr)                        */
+  double* v;     /* [ld] potentials (written), or NULL                 */
+  int32_t* who;  /* [ld] ancestor ids, or NULL (needed when tracked)  */
+  uint64_t* key; /* [ld] lineage keys, or NULL (logical indices)      */
+  int64_t ld;
+} gbdmc_host_walkers_t;
+
+/* gbdmc_sim_run on walkers that live in host memory between calls, as the
+ * reference's NumPy walker arrays do (propagate, pyvibdmc.py:701-876).
+ * ctrl_host holds the control block as the previous call (or, after
+ * gbdmc_sim_init, a copy of ctrl_dev) left it.  One call:
+ *   1. copies the ctrl_host->n walkers of host (x, who, key) into dev_src;
+ *   2. runs gbdmc_sim_run(sim, dev_src, dev_dst, ...);
+ *   3. copies back the control block to ctrl_host, every slot of dev_dst
+ *      (x, v, who, key: the first ctrl_host->n are the walkers) to host, and,
+ *      with hist_host, the vref and population history of up to max_steps
+ *      steps from the call's first step to hist_host[0..max_steps) and
+ *      hist_host[max_steps..2 max_steps);
+ *   4. waits for the stream once.
+ * dev_src and dev_dst are device walker buffers of sim->ld slots; their key
+ * arrays are used when host->key is set. */
+int gbdmc_sim_run_host(const gbdmc_sim_t* sim, gbdmc_host_walkers_t* host, const gbdmc_walkers_t* dev_src,
+                       const gbdmc_walkers_t* dev_dst, gbdmc_ctrl_t* ctrl_dev, gbdmc_ctrl_t* ctrl_host,
+                       void* scratch_dev, int64_t step_end, int32_t max_steps, double* hist_host, void* stream);
+
 /* The two halves of a step around a potential the caller evaluates
  * (sim->pes.kind == GBDMC_PES_EXTERNAL, plain DMC): gbdmc_sim_move is
  * move_randomly (pyvibdmc.py:540-547) -- the logical walkers of src (through
@@ -369,7 +397,7 @@ int gbdmc_desc_begin(int32_t* who_dev, const int64_t* n_dev, void* stream);
 /* sizeof() of the ABI structs, for binding self-checks:
  * 0 gbdmc_sim_t, 1 gbdmc_walkers_t, 2 gbdmc_ctrl_t, 3 gbdmc_noise_t,
  * 4 gbdmc_pes_t, 5 gbdmc_trial_t, 6 gbdmc_history_t, 7 gbdmc_replica_t, 8 gbdmc_mlp_t,
- * 9 gbdmc_walkers_f32_t, 10 gbdmc_adam_param_t; 0 for unknown ids. */
+ * 9 gbdmc_walkers_f32_t, 10 gbdmc_adam_param_t, 11 gbdmc_host_walkers_t; 0 for unknown ids. */
 size_t gbdmc_struct_size(int32_t which);
 
 /* ---- MLP surrogate of the water-dimer PES (BF16 tensor cores, FP32 accumulation) ----

@@ -88,7 +88,11 @@ class AdamParam(C.Structure):
                 ("wn", C.c_void_p), ("n", C.c_int64), ("k", C.c_int32), ("pad", C.c_int32)]
 
 
-_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32, AdamParam]
+class HostWalkersC(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("who", C.c_void_p), ("key", C.c_void_p), ("ld", C.c_int64)]
+
+
+_STRUCTS = [Sim, Walkers, Ctrl, Noise, PES, Trial, History, Replica, MLP, WalkersF32, AdamParam, HostWalkersC]
 
 _lib = None
 
@@ -123,6 +127,8 @@ def load():
         "gbdmc_lineage_noise": ([C.POINTER(Sim), P, C.c_int64, C.c_int64, P, C.c_int64, P, P], C.c_int),
         "gbdmc_sim_run": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.c_int64, C.c_int32, P],
                           C.c_int),
+        "gbdmc_sim_run_host": ([C.POINTER(Sim), C.POINTER(HostWalkersC), C.POINTER(Walkers), C.POINTER(Walkers), P,
+                                C.POINTER(Ctrl), P, C.c_int64, C.c_int32, P, P], C.c_int),
         "gbdmc_sim_move": ([C.POINTER(Sim), C.POINTER(Walkers), C.POINTER(Walkers), P, P, C.POINTER(Noise), P],
                            C.c_int),
         "gbdmc_sim_branch": ([C.POINTER(Sim), C.POINTER(Walkers), P, P, C.POINTER(Noise), P], C.c_int),

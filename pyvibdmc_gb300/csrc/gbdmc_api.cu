@@ -194,6 +194,7 @@ extern "C" size_t gbdmc_struct_size(int32_t which) {
     case 8: return sizeof(gbdmc_mlp_t);
     case 9: return sizeof(gbdmc_walkers_f32_t);
     case 10: return sizeof(gbdmc_adam_param_t);
+    case 11: return sizeof(gbdmc_host_walkers_t);
   }
   return 0;
 }

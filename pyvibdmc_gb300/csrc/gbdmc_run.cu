@@ -782,6 +782,65 @@ extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, c
   return GBDMC_ERR_ARG;
 }
 
+extern "C" int gbdmc_sim_run_host(const gbdmc_sim_t* S, gbdmc_host_walkers_t* host, const gbdmc_walkers_t* dev_src,
+                                  const gbdmc_walkers_t* dev_dst, gbdmc_ctrl_t* ctrl, gbdmc_ctrl_t* ctrl_host,
+                                  void* scratch, int64_t step_end, int32_t max_steps, double* hist_host,
+                                  void* stream) {
+  const char* what = "gbdmc_sim_run_host";
+  if (!S || !host || !host->x || !dev_src || !dev_dst || !ctrl || !ctrl_host || !dev_src->x || !dev_dst->x ||
+      !dev_dst->v || host->ld < S->ld || max_steps < 1) {
+    set_error("%s: null argument, host->ld below sim->ld, or max_steps < 1", what);
+    return GBDMC_ERR_ARG;
+  }
+  const int64_t n = ctrl_host->n;
+  if (n < 0 || n > S->ld || (host->who && (!dev_src->who || !dev_dst->who)) ||
+      (host->key && (!dev_src->key || !dev_dst->key)) || (S->track_who && !host->who)) {
+    set_error("%s: bad population (%lld) or missing device arrays for the host's who / key", what, (long long)n);
+    return GBDMC_ERR_ARG;
+  }
+  gbdmc_walkers_t src = *dev_src, dst = *dev_dst;
+  if (!host->key) src.key = dst.key = nullptr;  // the launch takes the logical indices
+  const cudaStream_t s = (cudaStream_t)stream;
+  const int A3 = 3 * S->natoms;
+  const size_t dp = (size_t)S->ld * sizeof(double), hp = (size_t)host->ld * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  if (n > 0) {
+    e = cudaMemcpy2DAsync(src.x, dp, host->x, hp, (size_t)n * sizeof(double), A3, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && host->who)
+      e = cudaMemcpyAsync(src.who, host->who, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && host->key)
+      e = cudaMemcpyAsync(src.key, host->key, (size_t)n * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      set_error("%s: host -> device copy: %s", what, cudaGetErrorString(e));
+      return GBDMC_ERR_CUDA;
+    }
+  }
+  const int64_t step0 = ctrl_host->step;
+  int rc = gbdmc_sim_run(S, &src, &dst, ctrl, scratch, step_end, max_steps, stream);
+  if (rc) return rc;
+  const size_t L = (size_t)S->ld;
+  e = cudaMemcpyAsync(ctrl_host, ctrl, sizeof(gbdmc_ctrl_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpy2DAsync(host->x, hp, dst.x, dp, L * sizeof(double), A3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && host->v) e = cudaMemcpyAsync(host->v, dst.v, L * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && host->who)
+    e = cudaMemcpyAsync(host->who, dst.who, L * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && host->key)
+    e = cudaMemcpyAsync(host->key, dst.key, L * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && hist_host && S->hist.vref && S->hist.pop && step0 >= 0 && step0 < S->hist.len) {
+    const int64_t k = S->hist.len - step0 < max_steps ? S->hist.len - step0 : max_steps;
+    e = cudaMemcpyAsync(hist_host, S->hist.vref + step0, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hist_host + max_steps, S->hist.pop + step0, (size_t)k * sizeof(double),
+                          cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_error("%s: device -> host copy: %s", what, cudaGetErrorString(e));
+    return GBDMC_ERR_CUDA;
+  }
+  return GBDMC_OK;
+}
+
 extern "C" int gbdmc_lineage_noise(const gbdmc_sim_t* sim, const uint64_t* keys_dev, int64_t n, int64_t step,
                                    double* normal_dev, int64_t ld_noise, double* u_dev, void* stream) {
   if (!sim || n < 0 || ld_noise < n || (n > 0 && (!keys_dev || !normal_dev || !u_dev))) {

@@ -170,3 +170,56 @@ def test_lineage_noise_matches_the_oracle_stream(mode):
     tol = dict(rtol=1e-6, atol=1e-6) if mode == "philox32" else dict(rtol=0, atol=1e-12)
     np.testing.assert_allclose(z.cpu().numpy(), zr, **tol)
     np.testing.assert_array_equal(u.cpu().numpy(), st.uniform53())
+
+
+def test_host_walker_entry_point_follows_the_device_resident_walk():
+    """gbdmc_sim_run_host -- the walkers in page-locked host memory between
+    calls, one call per 50-step window -- against DMC_Sim's device-resident
+    launches of the same walk: vref history, populations and walkers bit for
+    bit (the lineage keys travel through the host arrays)."""
+    p, m = oracle.h2o_config()
+    n = 3000
+    x0 = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(41).standard_normal((n, 3, 3))
+    kw = dict(num_walkers=n, num_timesteps=200, equil_steps=10 ** 6, atoms=["O", "H", "H"], masses=m, delta_t=10.0,
+              potential=pg.h2o_local_mode(), start_structures=x0, seed=31)
+    a = pg.DMC_Sim(write_files=False, fused_steps=50, **kw)  # the same launch boundaries: the same vref sums
+    a.run()
+    assert a._multi_used
+    b = pg.DMC_Sim(write_files=False, fused_steps=50, **kw)
+    b._init_device()
+    L = pg._capi.load()
+    ld = int(b._sim.ld)
+    scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(b.capacity), dtype=torch.uint8, device="cuda")
+    hx = torch.zeros((9, ld), dtype=torch.float64).pin_memory()
+    hv = torch.zeros(ld, dtype=torch.float64).pin_memory()
+    hw = torch.zeros(ld, dtype=torch.int32).pin_memory()
+    hk = torch.zeros(ld, dtype=torch.int64).pin_memory()
+    hc = torch.zeros(C.sizeof(pg._capi.Ctrl), dtype=torch.uint8).pin_memory()
+    hh = torch.zeros((2, 50), dtype=torch.float64).pin_memory()
+    b0, b1 = b._bufs[b._cur], b._bufs[1 - b._cur]
+    n0 = int(b._read_ctrl().n)
+    hx[:, :n0].copy_(b0["x"][:, :n0])
+    hw[:n0].copy_(b0["who"][:n0])
+    hk[:n0].copy_(b0["key"][:n0])
+    hc.copy_(b._ctrl)
+    torch.cuda.synchronize()
+    ctrl = pg._capi.Ctrl.from_address(hc.data_ptr())
+    host = pg._capi.HostWalkersC(x=hx.data_ptr(), v=hv.data_ptr(), who=hw.data_ptr(), key=hk.data_ptr(), ld=ld)
+    ws, wd = b._walker_struct(b0, False), b._walker_struct(b1, False)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    vref, pop = [], []
+    for _ in range(4):
+        step = int(ctrl.step)
+        pg._capi.check(L.gbdmc_sim_run_host(C.byref(b._sim), C.byref(host), C.byref(ws), C.byref(wd),
+                                            C.c_void_p(b._ctrl.data_ptr()), C.byref(ctrl),
+                                            C.c_void_p(scratch.data_ptr()), step + 50, 50, C.c_void_p(hh.data_ptr()),
+                                            stream))
+        assert ctrl.status == 0 and ctrl.step == step + 50
+        vref.append(hh[0].numpy().copy())
+        pop.append(hh[1].numpy().copy())
+    assert np.array_equal(np.concatenate(vref), a._hist["vref"].cpu().numpy()[:200])
+    assert np.array_equal(np.concatenate(pop), a._hist["pop"].cpu().numpy()[:200])
+    nn = int(ctrl.n)
+    xb = np.ascontiguousarray(hx[:, :nn].numpy().T).reshape(nn, 3, 3)
+    assert np.array_equal(xb, a.walkers)
+    assert np.array_equal(hw[:nn].numpy(), _who(a))
