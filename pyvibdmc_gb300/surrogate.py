@@ -1,7 +1,9 @@
 """MLP surrogate of the water-dimer PES: training, inference and DMC.
 
-* :class:`MLPSurrogate` -- 15 inverse O/H distances -> 3 x 128 SiLU -> 1,
-  BF16 tensor-core kernels with FP32 accumulation (libgbdmc ``gbdmc_mlp_*``).
+* :class:`MLPSurrogate` -- 15 inverse O/H distances (the Coulomb descriptor
+  of the reference's DistIt, normalised per pair, by default with DistIt's
+  sorted atom order) -> 3 x 128 SiLU -> 1, BF16 tensor-core kernels with
+  FP32 accumulation (libgbdmc ``gbdmc_mlp_*``).
   Trained on geometries, energies and adjoint forces (``gbdmc_pes_eval``
   gradients) harvested from a plain FP64 run.  Force matching uses a random
   direction v per sample: the network's directional derivative
@@ -15,9 +17,11 @@
   every walker outside the training box get the analytic FP64 energy, and the
   audited differences are accumulated as the surrogate's error estimate.  With
   ``bias_control`` = b > 0 the mean audited error of each step updates an
-  exponential moving average c <- (1-b) c + b <V_nn - V>, and the surrogate
-  energies of the next step are V_nn - c: the analytic PES, which audits the
-  surrogate, also removes its mean error on the current walker distribution.
+  exponential moving average c_mix <- (1-b) c_mix + b <V_nn - V>, and the
+  surrogate energies of the next step are V_nn - (c_mix + c_pure), where
+  c_pure (forward walking, ``bias_weighting="pure"``) turns the walkers'
+  mixed-distribution average of the error into the pure-distribution one
+  the DMC energy responds to.
 """
 import ctypes as C
 import math
