@@ -482,21 +482,29 @@ __global__ void __launch_bounds__(kThreads * kGroups) k_mlp_tc_move_energy(
 // columns, bounded mbarrier waits (a timeout sets *err and the CTA returns).
 
 // Y[M x 128] = X[M x K] W[K x 128] (+ bias): tiles of 128 rows, one row per
-// thread.  B = Wt (n-major [128][K], bf16) staged once per CTA; A = the tile's
-// rows of X rounded to bf16; the bias is added in the fp32 epilogue.
+// thread; CTA (x, y) takes output columns 64 y .. 64 y + 63 of tiles x, x +
+// gridDim.x, ... (two CTAs per tile: twice the CTAs of a batch, half the
+// epilogue each).  B = those 64 rows of Wt (n-major [128][K], bf16) staged
+// once per CTA; A = the tile's rows of X rounded to bf16; the accumulator is
+// 64 TMEM columns; the bias is added in the fp32 epilogue.
+constexpr int kXwN = 64;
+constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kXwN >> 3) << 17) |
+                               ((uint32_t)(kRows >> 4) << 24);
+
 template <int K>
 struct XwSmem {
-  alignas(128) unsigned char w[kN * K * 2];
+  alignas(128) unsigned char w[kXwN * K * 2];
   alignas(128) unsigned char a[kRows * K * 2];
   alignas(8) unsigned long long mbar;
   uint32_t tmem_base;
 };
 
-__device__ __forceinline__ uint32_t tc_alloc_setup(uint32_t* base_slot, unsigned long long* mbar) {
+__device__ __forceinline__ uint32_t tc_alloc_setup(uint32_t* base_slot, unsigned long long* mbar,
+                                                   uint32_t cols = kCols) {
   if (threadIdx.x == 0) mbar_init(saddr(mbar));
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(base_slot)),
-                 "r"(kCols)
+                 "r"(cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -505,6 +513,14 @@ __device__ __forceinline__ uint32_t tc_alloc_setup(uint32_t* base_slot, unsigned
   __syncthreads();
   tc_fence_after();
   return *base_slot;
+}
+
+__device__ __forceinline__ void umma_n64(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdescN64), "r"(accumulate)
+      : "memory");
 }
 
 template <int K>
@@ -516,12 +532,13 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict
   extern __shared__ __align__(1024) unsigned char smraw[];
   XwSmem<K>& sm = *reinterpret_cast<XwSmem<K>*>(smraw);
   const int t = threadIdx.x;
-  for (int c = t; c < kN * KG; c += blockDim.x) {
+  const int n0 = kXwN * (int)blockIdx.y;  // this CTA's first output column
+  for (int c = t; c < kXwN * KG; c += blockDim.x) {
     const int n = c / KG, kg = c % KG;
     *reinterpret_cast<uint4*>(sm.w + canon_off(n, 8 * kg, KG)) =
-        __ldg(reinterpret_cast<const uint4*>(Wt + (size_t)n * K + 8 * kg));
+        __ldg(reinterpret_cast<const uint4*>(Wt + (size_t)(n0 + n) * K + 8 * kg));
   }
-  const uint32_t tmem = tc_alloc_setup(&sm.tmem_base, &sm.mbar);
+  const uint32_t tmem = tc_alloc_setup(&sm.tmem_base, &sm.mbar, kXwN);
   const uint32_t trow = tmem + ((uint32_t)(32 * (t >> 5)) << 16);
   uint32_t phase = 0;
   for (long long base = (long long)blockIdx.x * kRows; base < M; base += (long long)gridDim.x * kRows) {
@@ -544,8 +561,8 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict
       const uint32_t a0 = saddr(sm.a), b0 = saddr(sm.w);
 #pragma unroll
       for (int s = 0; s < K / 16; ++s)
-        umma(tmem, smem_desc(a0 + 256u * s, kCore, KG * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
-             s > 0 ? 1u : 0u);
+        umma_n64(tmem, smem_desc(a0 + 256u * s, kCore, KG * kCore), smem_desc(b0 + 256u * s, kCore, KG * kCore),
+                 s > 0 ? 1u : 0u);
       umma_commit(saddr(&sm.mbar));
     }
     const bool ok = mbar_wait(saddr(&sm.mbar), phase);
@@ -556,13 +573,13 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict
       break;
     }
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < kXwN / 32; ++c) {
       float rr[32];
       tmem_ld32(trow + 32 * c, rr);
       if (r < M) {
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
-          const int col = 32 * c + j;
+          const int col = n0 + 32 * c + j;
           float4 o = make_float4(rr[j], rr[j + 1], rr[j + 2], rr[j + 3]);
           if (bias) {
             o.x += bias[col];
@@ -577,7 +594,11 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict
     tc_fence_before();
     __syncthreads();  // TMEM rows read and A free before the next tile's MMAs
   }
-  teardown<1>(tmem);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kXwN)
+                           : "memory");
 }
 
 // G[K x 128] += X[M x K]^T D[M x 128]: the sum over the M rows runs along the
@@ -727,11 +748,12 @@ int launch_tc_gemm_xw(const float* x, long long m, int k, const uint16_t* wt, co
     return GBDMC_ERR_CUDA;
   }
   long long g = (m + tc::kRows - 1) / tc::kRows;
-  if (g > 3LL * num_sms()) g = 3LL * num_sms();
+  if (g > 3LL * num_sms() / 2) g = 3LL * num_sms() / 2;
+  const dim3 grid((unsigned)g, tc::kN / tc::kXwN);  // two CTAs per 128-row tile, 64 output columns each
   if (k == 16)
-    tc::k_tc_gemm_xw<16><<<(int)g, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+    tc::k_tc_gemm_xw<16><<<grid, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
   else
-    tc::k_tc_gemm_xw<128><<<(int)g, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+    tc::k_tc_gemm_xw<128><<<grid, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
   return check_launch("gbdmc_mlp_gemm (tcgen05)");
 }
 

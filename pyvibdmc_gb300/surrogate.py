@@ -57,8 +57,8 @@ class MLPSurrogate:
         """engine: 1 = tcgen05 inference kernels (default), 0 = mma.sync kernels.
         train_engine: the training GEMMs on "mma_sync", on "tcgen05", or
         "auto": each GEMM on the engine measured faster for 8192-sample
-        batches on a GB300 (Y = XW on mma.sync, 8.3 against 12.4 us for K =
-        128; G += X^T D on tcgen05, 10.3 against 14.4 us).
+        batches on a GB300 (Y = XW on mma.sync, 8.3 against 10.2 us for K =
+        128; G += X^T D on tcgen05, 10.4 against 14.4 us).
         sort_atoms: descriptors in the canonical atom order of pyvibdmc's
         DistIt(method='coulomb', sorted_atoms=[[0],[1,2],[3],[4,5]],
         sorted_groups=[[0,1,2],[3,4,5]]) (distance_descriptors.py:115-152), so
