@@ -424,10 +424,10 @@ def run_e2e_windows(sim, L, dev, windows, run_scratch):
     gbdmc_sim_run_host.  The walkers (coordinates, potentials, ancestor ids,
     lineage keys) live in page-locked host memory between calls, as the
     reference's NumPy walker arrays do; per window (one bench step) one call
-    copies the N walkers host -> device, runs DESC_WINDOW steps in one
-    gbdmc_sim_run launch, and copies the control block, every slot of the
-    output buffers and the window's vref / population history device -> host,
-    with one stream wait."""
+    runs DESC_WINDOW steps in one gbdmc_sim_run launch that reads the N
+    walkers from the host arrays over the host link, then a kernel writes the
+    control block, the N' walkers and the window's vref / population history
+    into host memory; one stream wait."""
     import torch
     from pyvibdmc_gb300 import _capi
     A3 = 3 * sim.natoms
@@ -466,16 +466,16 @@ def run_e2e_windows(sim, L, dev, windows, run_scratch):
         k = int(ctrl_host.step) - step
         total += n + float(hh[1, :k - 1].sum())  # the population entering each of the k steps
         h2d += (A3 * 8 + 4 + 8) * n
-        d2h += cb + (A3 * 8 + 8 + 4 + 8) * ld + 16 * k
+        d2h += cb + (A3 * 8 + 8 + 4 + 8) * int(ctrl_host.n) + 16 * k
     secs = time.perf_counter() - t0
     sim._cur, sim._lazy = 1 - sim._cur, False  # the walkers are in the output buffer (and on the host)
     return {"value": total / secs, "unit": UNIT, "h2d_bytes_per_step": h2d // windows,
             "d2h_bytes_per_step": d2h // windows, "steps": windows,
             "path": f"walkers in page-locked host memory between calls; per bench step (one {DESC_WINDOW}-step "
-                    "window) one gbdmc_sim_run_host call (C ABI): H2D of the N walkers' coordinates, ancestor ids "
-                    "and lineage keys, one gbdmc_sim_run launch, D2H of the control block, every slot of the output "
-                    "walkers (coordinates, potentials, ancestor ids, keys) and the window's vref and population "
-                    "history; one stream wait per window"}
+                    "window) one gbdmc_sim_run_host call (C ABI): one gbdmc_sim_run launch reading the N walkers' "
+                    "coordinates, ancestor ids and lineage keys from host memory, one kernel writing the control "
+                    "block, the N' walkers (coordinates, potentials, ancestor ids, keys) and the window's vref and "
+                    "population history to host memory; one stream wait per window"}
 
 
 def _timed_graph_rate(run_steps, pop_of, steps):

@@ -280,16 +280,18 @@ typedef struct {
 
 /* gbdmc_sim_run on walkers that live in host memory between calls, as the
  * reference's NumPy walker arrays do (propagate, pyvibdmc.py:701-876).
- * ctrl_host holds the control block as the previous call (or, after
- * gbdmc_sim_init, a copy of ctrl_dev) left it.  One call:
- *   1. copies the ctrl_host->n walkers of host (x, who, key) into dev_src;
- *   2. runs gbdmc_sim_run(sim, dev_src, dev_dst, ...);
- *   3. copies back the control block to ctrl_host, every slot of dev_dst
- *      (x, v, who, key: the first ctrl_host->n are the walkers) to host, and,
- *      with hist_host, the vref and population history of up to max_steps
- *      steps from the call's first step to hist_host[0..max_steps) and
- *      hist_host[max_steps..2 max_steps);
- *   4. waits for the stream once.
+ * The host arrays must be page-locked (cudaHostAlloc / cudaHostRegister:
+ * the device reads and writes them over the host link).  ctrl_host holds the
+ * control block as the previous call (or, after gbdmc_sim_init, a copy of
+ * ctrl_dev) left it; it must be page-locked too.  One call:
+ *   1. the ctrl_host->n walkers of host (x, who, key) are the launch's input:
+ *      read in place when host->ld == sim->ld, else copied into dev_src;
+ *   2. gbdmc_sim_run(sim, input, dev_dst, ...) runs;
+ *   3. a kernel writes the control block to ctrl_host, the ctrl->n walkers of
+ *      dev_dst (x, v, who, key) into host, and, with hist_host, the vref and
+ *      population history of the steps run (at most max_steps) to
+ *      hist_host[0..) and hist_host[max_steps..);
+ *   4. the call waits for the stream once.
  * dev_src and dev_dst are device walker buffers of sim->ld slots; their key
  * arrays are used when host->key is set. */
 int gbdmc_sim_run_host(const gbdmc_sim_t* sim, gbdmc_host_walkers_t* host, const gbdmc_walkers_t* dev_src,

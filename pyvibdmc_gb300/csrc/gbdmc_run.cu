@@ -782,6 +782,33 @@ extern "C" int gbdmc_sim_run(const gbdmc_sim_t* S, const gbdmc_walkers_t* src, c
   return GBDMC_ERR_ARG;
 }
 
+// The output of a gbdmc_sim_run_host call written straight into the host's
+// page-locked arrays over the host link: the control block, the ctrl->n
+// walkers of dst (x, v, who, key) and the history of the steps run.
+__global__ void k_export_host(const gbdmc_ctrl_t* __restrict__ ctrl, gbdmc_walkers_t dst, int64_t ld, int A3,
+                              gbdmc_host_walkers_t host, gbdmc_ctrl_t* ctrl_host, gbdmc_history_t hist, int64_t step0,
+                              int32_t max_steps, double* hist_host) {
+  const int64_t n = ctrl->n;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  if (tid == 0) *ctrl_host = *ctrl;
+  const int64_t m = n < ld ? (n < 0 ? 0 : n) : ld;
+  for (int64_t i = tid; i < m; i += nth) {
+    for (int k = 0; k < A3; ++k) host.x[k * host.ld + i] = dst.x[k * ld + i];
+    if (host.v) host.v[i] = dst.v[i];
+    if (host.who) host.who[i] = dst.who[i];
+    if (host.key) host.key[i] = dst.key[i];
+  }
+  if (hist_host && hist.vref && hist.pop && step0 >= 0 && step0 < hist.len) {
+    int64_t k = ctrl->step - step0;
+    if (k > max_steps) k = max_steps;
+    if (k > hist.len - step0) k = hist.len - step0;
+    for (int64_t j = tid; j < k; j += nth) {
+      hist_host[j] = hist.vref[step0 + j];
+      hist_host[max_steps + j] = hist.pop[step0 + j];
+    }
+  }
+}
+
 extern "C" int gbdmc_sim_run_host(const gbdmc_sim_t* S, gbdmc_host_walkers_t* host, const gbdmc_walkers_t* dev_src,
                                   const gbdmc_walkers_t* dev_dst, gbdmc_ctrl_t* ctrl, gbdmc_ctrl_t* ctrl_host,
                                   void* scratch, int64_t step_end, int32_t max_steps, double* hist_host,
@@ -802,9 +829,15 @@ extern "C" int gbdmc_sim_run_host(const gbdmc_sim_t* S, gbdmc_host_walkers_t* ho
   if (!host->key) src.key = dst.key = nullptr;  // the launch takes the logical indices
   const cudaStream_t s = (cudaStream_t)stream;
   const int A3 = 3 * S->natoms;
-  const size_t dp = (size_t)S->ld * sizeof(double), hp = (size_t)host->ld * sizeof(double);
   cudaError_t e = cudaSuccess;
-  if (n > 0) {
+  if (host->ld == S->ld) {
+    // the launch reads its input straight from the host arrays (page-locked
+    // memory is addressable from the device under unified addressing)
+    src.x = host->x;
+    src.who = host->who ? host->who : src.who;
+    src.key = host->key;
+  } else if (n > 0) {
+    const size_t dp = (size_t)S->ld * sizeof(double), hp = (size_t)host->ld * sizeof(double);
     e = cudaMemcpy2DAsync(src.x, dp, host->x, hp, (size_t)n * sizeof(double), A3, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && host->who)
       e = cudaMemcpyAsync(src.who, host->who, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s);
@@ -818,24 +851,12 @@ extern "C" int gbdmc_sim_run_host(const gbdmc_sim_t* S, gbdmc_host_walkers_t* ho
   const int64_t step0 = ctrl_host->step;
   int rc = gbdmc_sim_run(S, &src, &dst, ctrl, scratch, step_end, max_steps, stream);
   if (rc) return rc;
-  const size_t L = (size_t)S->ld;
-  e = cudaMemcpyAsync(ctrl_host, ctrl, sizeof(gbdmc_ctrl_t), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaMemcpy2DAsync(host->x, hp, dst.x, dp, L * sizeof(double), A3, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && host->v) e = cudaMemcpyAsync(host->v, dst.v, L * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && host->who)
-    e = cudaMemcpyAsync(host->who, dst.who, L * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && host->key)
-    e = cudaMemcpyAsync(host->key, dst.key, L * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && hist_host && S->hist.vref && S->hist.pop && step0 >= 0 && step0 < S->hist.len) {
-    const int64_t k = S->hist.len - step0 < max_steps ? S->hist.len - step0 : max_steps;
-    e = cudaMemcpyAsync(hist_host, S->hist.vref + step0, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(hist_host + max_steps, S->hist.pop + step0, (size_t)k * sizeof(double),
-                          cudaMemcpyDeviceToHost, s);
-  }
+  k_export_host<<<2 * num_sms(), 256, 0, s>>>(ctrl, dst, S->ld, A3, *host, ctrl_host, S->hist, step0, max_steps,
+                                              hist_host);
+  e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
-    set_error("%s: device -> host copy: %s", what, cudaGetErrorString(e));
+    set_error("%s: %s", what, cudaGetErrorString(e));
     return GBDMC_ERR_CUDA;
   }
   return GBDMC_OK;

@@ -172,11 +172,14 @@ def test_lineage_noise_matches_the_oracle_stream(mode):
     np.testing.assert_array_equal(u.cpu().numpy(), st.uniform53())
 
 
-def test_host_walker_entry_point_follows_the_device_resident_walk():
+@pytest.mark.parametrize("pad", [0, 64])
+def test_host_walker_entry_point_follows_the_device_resident_walk(pad):
     """gbdmc_sim_run_host -- the walkers in page-locked host memory between
     calls, one call per 50-step window -- against DMC_Sim's device-resident
     launches of the same walk: vref history, populations and walkers bit for
-    bit (the lineage keys travel through the host arrays)."""
+    bit (the lineage keys travel through the host arrays).  pad 0: host arrays
+    with the device's leading dimension, read by the launch in place; pad 64:
+    another leading dimension, copied in first."""
     p, m = oracle.h2o_config()
     n = 3000
     x0 = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(41).standard_normal((n, 3, 3))
@@ -189,11 +192,12 @@ def test_host_walker_entry_point_follows_the_device_resident_walk():
     b._init_device()
     L = pg._capi.load()
     ld = int(b._sim.ld)
+    hld = ld + pad
     scratch = torch.zeros(L.gbdmc_sim_run_scratch_bytes(b.capacity), dtype=torch.uint8, device="cuda")
-    hx = torch.zeros((9, ld), dtype=torch.float64).pin_memory()
-    hv = torch.zeros(ld, dtype=torch.float64).pin_memory()
-    hw = torch.zeros(ld, dtype=torch.int32).pin_memory()
-    hk = torch.zeros(ld, dtype=torch.int64).pin_memory()
+    hx = torch.zeros((9, hld), dtype=torch.float64).pin_memory()
+    hv = torch.zeros(hld, dtype=torch.float64).pin_memory()
+    hw = torch.zeros(hld, dtype=torch.int32).pin_memory()
+    hk = torch.zeros(hld, dtype=torch.int64).pin_memory()
     hc = torch.zeros(C.sizeof(pg._capi.Ctrl), dtype=torch.uint8).pin_memory()
     hh = torch.zeros((2, 50), dtype=torch.float64).pin_memory()
     b0, b1 = b._bufs[b._cur], b._bufs[1 - b._cur]
@@ -204,7 +208,7 @@ def test_host_walker_entry_point_follows_the_device_resident_walk():
     hc.copy_(b._ctrl)
     torch.cuda.synchronize()
     ctrl = pg._capi.Ctrl.from_address(hc.data_ptr())
-    host = pg._capi.HostWalkersC(x=hx.data_ptr(), v=hv.data_ptr(), who=hw.data_ptr(), key=hk.data_ptr(), ld=ld)
+    host = pg._capi.HostWalkersC(x=hx.data_ptr(), v=hv.data_ptr(), who=hw.data_ptr(), key=hk.data_ptr(), ld=hld)
     ws, wd = b._walker_struct(b0, False), b._walker_struct(b1, False)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     vref, pop = [], []
