@@ -554,6 +554,19 @@ def run_extras(steps):
            "walker_steps_per_s": ws / secs, "zpe_cm": z, "err_cm": e, "efficiency": 1.0 / (e * e * secs)}
     isb["gain_vs_plain_h2o_20k_at_equal_error"] = isb["efficiency"] / eff["plain"]["efficiency"]
     out["is_batched_64_replicas_h2o"] = isb
+    # continuous weighting (pyvibdmc.py:432-454), H2O, 20000 walkers: the per-step kernels with the
+    # sequential argmax cloning of every walker below 1/N0
+    sc = pg.DMC_Sim(num_walkers=20000, num_timesteps=1264, equil_steps=10 ** 9, atoms=["O", "H", "H"],
+                    masses=masses, delta_t=DT, potential=pg.h2o_local_mode(), start_structures=start_structures(20000, 13),
+                    seed=17, weighting="continuous", write_files=False, graph_steps=16)
+    sc._init_device()
+    sc._run_steps(64)
+    torch.cuda.synchronize()
+    _, secs = _timed_graph_rate(sc._run_steps, lambda: 0, 1000)
+    kills = sc._hist["births"][64:1064].cpu().numpy()
+    out["continuous_h2o_20k"] = {"walker_steps_per_s": 20000 * 1000 / secs, "us_per_step": secs / 1000 * 1e6,
+                                 "clones_per_step": float(kills.mean())}
+    del sc
     # batched ensemble (config 5): 64 plain FP64 replicas, N_r ~ U[1000, 65536] (seeded), tile widths and
     # graph length autotuned, 10000 steps; every replica's ZPE with its blocking error, and 16 of them
     # against the individually run plain path (DMC_Sim, another seed)

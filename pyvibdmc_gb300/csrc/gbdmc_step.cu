@@ -636,11 +636,189 @@ __device__ long long block_compact_flags(const unsigned char* flag, long long n,
   return total;
 }
 
+// The kills below the lower threshold (pyvibdmc.py:340-356, :432-439): for
+// each kill-list slot to_j in order, the walker m_j of the largest weight
+// (the first on ties, np.argmax) is cloned into to_j and both keep half its
+// weight.  The argmax runs in one warp over per-chunk maxima kept in shared
+// memory; after a kill only the chunks of m_j and to_j are scanned again, so
+// a kill costs a few hundred cycles instead of a block-wide pass over all n
+// weights.  The copies are deferred: aux[to_j] = m_j records where each
+// killed slot takes its walker from, and afterwards every copy follows the
+// chain aux[.] through slots killed earlier (flags 2) to an original walker,
+// all kills in parallel.  The argmax can be a slot that is still waiting to
+// be killed only when every other weight has fallen below the threshold; if
+// that happens the copies run one kill at a time in kill order instead, the
+// reference's order.  w: the weights (global); flags: 1 for kill slots
+// (set to 2 as they are killed); the CTA's 1024 threads call it.
+constexpr int kChunkMin = 64;
+constexpr int kMaxChunks = 2048;
+
+template <int A, bool IS>
+__device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t base, double* wg, long long n,
+                           const int* list, long long nk, int* aux, unsigned char* flags, double* ws, int ws_cap) {
+  __shared__ double s_cv[kMaxChunks];
+  __shared__ int s_ci[kMaxChunks];
+  __shared__ int s_patho;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  // the weights in shared memory while the kills run, when they fit
+  const bool in_smem = n <= ws_cap;
+  double* w = in_smem ? ws : wg;
+  if (in_smem) {
+    for (long long i = threadIdx.x; i < n; i += kCTA) ws[i] = wg[i];
+    __syncthreads();
+  }
+  const long long K = (long long)kChunkMin * ((n + (long long)kChunkMin * kMaxChunks - 1) / ((long long)kChunkMin * kMaxChunks));
+  const int nch = (int)((n + K - 1) / K);
+  // per-chunk maxima (value, first index) of the current weights
+  auto chunk_max = [&](int c, double& bv, int& bi) {
+    bv = -CUDART_INF;
+    bi = -1;
+    const long long e = (c + 1) * K < n ? (c + 1) * K : n;
+    for (long long i = c * K + lane; i < e; i += 32) {
+      const double x = w[i];
+      if (bi < 0 || x > bv) {
+        bv = x;
+        bi = (int)i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(full, bv, o);
+      const int oi = __shfl_xor_sync(full, bi, o);
+      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+  };
+  if (threadIdx.x == 0) s_patho = 0;
+  for (int c = wid; c < nch; c += kCTA / 32) {
+    double bv;
+    int bi;
+    chunk_max(c, bv, bi);
+    if (lane == 0) {
+      s_cv[c] = bv;
+      s_ci[c] = bi;
+    }
+  }
+  __syncthreads();
+  if (wid == 0) {
+    int patho = 0;
+    for (long long j0 = 0; j0 < nk; j0 += 32) {
+      // lane q holds kill j0 + q: its slot, then the slot it is cloned from
+      const int myto = j0 + lane < nk ? list[j0 + lane] : -1;
+      const int cnt = nk - j0 < 32 ? (int)(nk - j0) : 32;
+      int mym = 0;
+      for (int q = 0; q < cnt; ++q) {
+        const long long to = GBDMC_BC(__shfl_sync(full, myto, q), 0, n, kBcContSlot);
+        double bv = -CUDART_INF;
+        int bi = -1;
+        for (int c = lane; c < nch; c += 32) {
+          const double x = s_cv[c];
+          const int xi = s_ci[c];
+          if (bi < 0 || x > bv || (x == bv && xi < bi)) {
+            bv = x;
+            bi = xi;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const double ov = __shfl_xor_sync(full, bv, o);
+          const int oi = __shfl_xor_sync(full, bi, o);
+          if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+            bv = ov;
+            bi = oi;
+          }
+        }
+        const long long m = GBDMC_BC(bi, 0, n, kBcContSlot);
+        // a slot still waiting to be killed can be the largest only when every
+        // weight is below the threshold: then the copies keep the kill order
+        if (bv < S.thresh_lower) patho = 1;
+        const double h = bv / 2.0;  // bv == w[m]
+        if (lane == q) mym = (int)m;
+        if (lane == 0) {
+          w[m] = h;
+          w[to] = h;
+        }
+        __syncwarp();
+        const int cm = (int)(m / K), ct = (int)(to / K);
+        double v1;
+        int i1;
+        chunk_max(cm, v1, i1);  // m's chunk lost its largest weight: scanned again
+        if (lane == 0) {
+          s_cv[cm] = v1;
+          s_ci[cm] = i1;
+        }
+        if (ct != cm) {
+          // to's chunk: only w[to] changed, so its largest is the old one or h
+          // at to -- unless the old largest was to itself, whose weight may
+          // have fallen (h can be below it when every weight is small): then
+          // the chunk is scanned again
+          const double cv = s_cv[ct];
+          const int ci = s_ci[ct];
+          if (ci == (int)to) {
+            chunk_max(ct, v1, i1);
+            if (lane == 0) {
+              s_cv[ct] = v1;
+              s_ci[ct] = i1;
+            }
+          } else if (lane == 0 && (h > cv || (h == cv && (int)to < ci))) {
+            s_cv[ct] = h;
+            s_ci[ct] = (int)to;
+          }
+        }
+        __syncwarp();
+      }
+      if (lane < cnt) {  // the batch's sources and killed marks, once per 32 kills
+        aux[myto] = mym;
+        flags[myto] = 2;
+      }
+    }
+    if (lane == 0) s_patho = patho;
+  }
+  __syncthreads();
+  if (in_smem) {
+    for (long long i = threadIdx.x; i < n; i += kCTA) wg[i] = ws[i];
+    __syncthreads();
+  }
+  const int nat = A > 0 ? A : S.natoms;
+  const int64_t ld = S.ld;
+  if (!s_patho) {
+    // every killed slot from the original walker at the end of its chain
+    for (long long j = threadIdx.x; j < nk; j += kCTA) {
+      const long long to = list[j];
+      long long src = aux[to];
+      while (flags[src] == 2) src = aux[src];
+      const int64_t f = base + src, d = base + to;
+      for (int k = 0; k < 3 * nat; ++k) {
+        W.x[k * ld + d] = W.x[k * ld + f];
+        if constexpr (IS) W.f[k * ld + d] = W.f[k * ld + f];
+      }
+      W.v[d] = W.v[f];
+      if (W.who) W.who[d] = W.who[f];
+      if constexpr (IS) {
+        W.psi[d] = W.psi[f];
+        W.ke[d] = W.ke[f];
+      }
+    }
+  } else {
+    // the reference's order, one kill at a time (a source may be killed later)
+    for (long long j = 0; j < nk; ++j) {
+      const long long to = list[j];
+      clone_walker<A, IS>(S, W, base, aux[to], to);
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+}
+
 template <int A, bool IS>
 __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gbdmc_sim_t S,
                                                        const __grid_constant__ RepTable T, gbdmc_walkers_t W,
                                                        gbdmc_ctrl_t* ctrls, int* list_all, int* aux_all,
-                                                       unsigned char* flags_all) {
+                                                       unsigned char* flags_all, int ws_cap) {
+  extern __shared__ double ws_dyn[];  // ws_cap doubles: the weights during the kills
   const int r = blockIdx.x;
   gbdmc_ctrl_t* ctrl = ctrls + r;
   if (*(volatile int*)&ctrl->status) return;
@@ -670,6 +848,9 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   }
   const long long nk = block_compact_flags(flags, n, list);
   long long nb = nk;
+  if (nk > 0 && nk < n) {
+    fast_kills<A, IS>(S, W, base, w, n, list, nk, aux_all + base, flags, ws_dyn, ws_cap);
+  } else {
   for (long long j = 0; j < nk; ++j) {
     const long long to = GBDMC_BC(list[j], 0, n, kBcContSlot);
     const long long m = GBDMC_BC(block_arg<true>(w, n, nullptr), 0, n, kBcContSlot);
@@ -681,6 +862,7 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
       w[to] = h;
     }
     __syncthreads();
+  }
   }
   if (S.thresh_upper > 0.0) {
     if (threadIdx.x == 0) s_nb = 0;
@@ -762,6 +944,20 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
       ctrl->reserved[1] = __double_as_longlong(wmn);
     }
   }
+}
+
+// One CTA per replica; the weights of replicas of up to kWsMax walkers sit in
+// shared memory while their kills run.
+constexpr int kWsMax = 24000;
+template <int A, bool IS>
+static void launch_cont_branch(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& dst,
+                               gbdmc_ctrl_t* ctrl, int* list, int* aux, unsigned char* flags, cudaStream_t s) {
+  long long cap = 0;
+  for (int r = 0; r < T.nrep; ++r) cap = T.cap[r] > cap ? T.cap[r] : cap;
+  const int ws_cap = (int)(cap < kWsMax ? cap : kWsMax);
+  const size_t smem = (size_t)ws_cap * sizeof(double);
+  cudaFuncSetAttribute((const void*)k_cont_branch<A, IS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_cont_branch<A, IS><<<T.nrep, kCTA, smem, s>>>(S, T, dst, ctrl, list, aux, flags, ws_cap);
 }
 
 // np.argpartition of one weight array by one CTA (gbdmc_argpartition).
@@ -912,7 +1108,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     } else {
       k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      k_cont_branch<A, false><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.counts, L.flags);
+      launch_cont_branch<A, false>(S, T, dst, ctrl, L.list, L.counts, L.flags, s);
     }
   } else {
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
@@ -922,7 +1118,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {
-      k_cont_branch<A, true><<<T.nrep, kCTA, 0, s>>>(S, T, dst, ctrl, L.list, L.counts, L.flags);
+      launch_cont_branch<A, true>(S, T, dst, ctrl, L.list, L.counts, L.flags, s);
     }
   }
   if (prof) {
@@ -1249,7 +1445,7 @@ extern "C" int gbdmc_sim_branch(const gbdmc_sim_t* S, const gbdmc_walkers_t* dst
   const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(&r, 1));
   cudaStream_t s = (cudaStream_t)stream;
   if (S->weighting == GBDMC_CONTINUOUS) {
-    k_cont_branch<0, false><<<1, kCTA, 0, s>>>(*S, T, *dst, ctrl, L.list, L.counts, L.flags);
+    launch_cont_branch<0, false>(*S, T, *dst, ctrl, L.list, L.counts, L.flags, s);
     return check_launch(what);
   }
   const int G = grid_for(T);

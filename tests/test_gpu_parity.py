@@ -579,3 +579,26 @@ def test_argpartition_kernel_matches_numpy_introselect():
         assert np.array_equal(got[:k], ref[:k]), label
         if k >= 3:
             assert np.array_equal(got, ref), label
+
+
+@pytest.mark.parametrize("thresh", [0.3, 0.9])
+def test_continuous_kills_many_and_tied_vs_oracle(thresh):
+    """Continuous weighting where many walkers die each step against the
+    oracle's sequential argmax cloning (pyvibdmc.py:340-356) on the same
+    injected deviates.  The walkers start on a few shared geometries, so many
+    weights tie (the first index wins, np.argmax). With the threshold at 0.9
+    nearly every weight falls below it, and the largest weight can be a walker
+    still waiting to die, the case where the kernel copies in kill order.
+    Walkers bit-exact, weights to 1e-12 (CUDA's exp vs NumPy's)."""
+    p, m = oracle.h2o_config()
+    base = oracle.h2o_equilibrium(p)[None] + 0.05 * oracle.InjectedNoise(71).standard_normal((8, 3, 3))
+    x0 = np.repeat(base, 64, axis=0)  # 512 walkers on 8 geometries: tied weights at the first step
+    nsteps = 6
+    ref = oracle.OracleDMC(x0, m, 10.0, lambda c: oracle.pes_h2o_lm(c, p), oracle.InjectedNoise(31),
+                           weighting="continuous", cont_wt_thresh=thresh).run(nsteps)
+    sim = _sim(x0, m, ["O", "H", "H"], pg.h2o_local_mode(), 31, nsteps, weighting="continuous",
+               cont_wt_thresh=thresh)
+    sim.run()
+    x, w = sim.walkers
+    assert np.array_equal(x, ref.x)
+    np.testing.assert_allclose(w, ref.w, rtol=1e-12)
