@@ -668,18 +668,22 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
     for (long long i = threadIdx.x; i < n; i += kCTA) ws[i] = wg[i];
     __syncthreads();
   }
-  const long long K = (long long)kChunkMin * ((n + (long long)kChunkMin * kMaxChunks - 1) / ((long long)kChunkMin * kMaxChunks));
-  const int nch = (int)((n + K - 1) / K);
+  // chunks of 2^lk weights (at least kChunkMin, at most kMaxChunks chunks): the
+  // chunk of a slot is a shift, and the indices are 32-bit (n < 2^31)
+  int lk = 6;  // kChunkMin = 64
+  while ((n + (1LL << lk) - 1) >> lk > kMaxChunks) ++lk;
+  const int ni = (int)n;
+  const int nch = (ni + (1 << lk) - 1) >> lk;
   // per-chunk maxima (value, first index) of the current weights
   auto chunk_max = [&](int c, double& bv, int& bi) {
     bv = -CUDART_INF;
     bi = -1;
-    const long long e = (c + 1) * K < n ? (c + 1) * K : n;
-    for (long long i = c * K + lane; i < e; i += 32) {
+    const int e = ((c + 1) << lk) < ni ? ((c + 1) << lk) : ni;
+    for (int i = (c << lk) + lane; i < e; i += 32) {
       const double x = w[i];
       if (bi < 0 || x > bv) {
         bv = x;
-        bi = (int)i;
+        bi = i;
       }
     }
 #pragma unroll
@@ -735,14 +739,14 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
         // a slot still waiting to be killed can be the largest only when every
         // weight is below the threshold: then the copies keep the kill order
         if (bv < S.thresh_lower) patho = 1;
-        const double h = bv / 2.0;  // bv == w[m]
+        const double h = bv * 0.5;  // bv == w[m]; halving is exact
         if (lane == q) mym = (int)m;
         if (lane == 0) {
           w[m] = h;
           w[to] = h;
         }
         __syncwarp();
-        const int cm = (int)(m / K), ct = (int)(to / K);
+        const int cm = (int)m >> lk, ct = (int)to >> lk;
         double v1;
         int i1;
         chunk_max(cm, v1, i1);  // m's chunk lost its largest weight: scanned again
