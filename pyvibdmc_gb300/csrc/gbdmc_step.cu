@@ -650,13 +650,17 @@ __device__ long long block_compact_flags(const unsigned char* flag, long long n,
 // that happens the copies run one kill at a time in kill order instead, the
 // reference's order.  w: the weights (global); flags: 1 for kill slots
 // (set to 2 as they are killed); the CTA's 1024 threads call it.
-constexpr int kChunkMin = 64;
+constexpr int kChunkLogMin = 6;  // chunks of at least 64 weights
 constexpr int kMaxChunks = 2048;
 
 template <int A, bool IS>
 __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t base, double* wg, long long n,
                            const int* list, long long nk, int* aux, unsigned char* flags, double* ws, int ws_cap) {
-  __shared__ double s_cv[kMaxChunks];
+  // The weights are non-negative and finite here, so their bit patterns as
+  // signed 64-bit integers order like their values: the comparisons run on
+  // the integer pipes (a warp-wide FP64 instruction costs tens of cycles on
+  // this part's narrow FP64 pipe).
+  __shared__ long long s_cv[kMaxChunks];  // chunk maxima: the weight's bits
   __shared__ int s_ci[kMaxChunks];
   __shared__ int s_patho;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -668,46 +672,51 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
     for (long long i = threadIdx.x; i < n; i += kCTA) ws[i] = wg[i];
     __syncthreads();
   }
-  // chunks of 2^lk weights (at least kChunkMin, at most kMaxChunks chunks): the
+  // chunks of 2^lk weights (lk >= kChunkLogMin, at most kMaxChunks chunks): the
   // chunk of a slot is a shift, and the indices are 32-bit (n < 2^31)
-  int lk = 6;  // kChunkMin = 64
+  int lk = kChunkLogMin;
   while ((n + (1LL << lk) - 1) >> lk > kMaxChunks) ++lk;
   const int ni = (int)n;
   const int nch = (ni + (1 << lk) - 1) >> lk;
-  // per-chunk maxima (value, first index) of the current weights
-  auto chunk_max = [&](int c, double& bv, int& bi) {
-    bv = -CUDART_INF;
-    bi = -1;
-    const int e = ((c + 1) << lk) < ni ? ((c + 1) << lk) : ni;
-    for (int i = (c << lk) + lane; i < e; i += 32) {
-      const double x = w[i];
-      if (bi < 0 || x > bv) {
-        bv = x;
-        bi = i;
-      }
-    }
+  // (key, index) of the largest weight, the first index on ties, over a warp
+  auto warp_best = [&](long long& bk, int& bi) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double ov = __shfl_xor_sync(full, bv, o);
+      const long long ok = __shfl_xor_sync(full, bk, o);
       const int oi = __shfl_xor_sync(full, bi, o);
-      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
-        bv = ov;
+      if (oi >= 0 && (bi < 0 || ok > bk || (ok == bk && oi < bi))) {
+        bk = ok;
         bi = oi;
       }
     }
   };
+  // per-chunk maxima of the current weights
+  auto chunk_max = [&](int c, long long& bk, int& bi) {
+    bk = -1;
+    bi = -1;
+    const int e = ((c + 1) << lk) < ni ? ((c + 1) << lk) : ni;
+    for (int i = (c << lk) + lane; i < e; i += 32) {
+      const long long x = __double_as_longlong(w[i]);
+      if (bi < 0 || x > bk) {
+        bk = x;
+        bi = i;
+      }
+    }
+    warp_best(bk, bi);
+  };
   if (threadIdx.x == 0) s_patho = 0;
   for (int c = wid; c < nch; c += kCTA / 32) {
-    double bv;
+    long long bk;
     int bi;
-    chunk_max(c, bv, bi);
+    chunk_max(c, bk, bi);
     if (lane == 0) {
-      s_cv[c] = bv;
+      s_cv[c] = bk;
       s_ci[c] = bi;
     }
   }
   __syncthreads();
   if (wid == 0) {
+    const long long thr_key = __double_as_longlong(S.thresh_lower);  // > 0: ordered like the weights
     int patho = 0;
     for (long long j0 = 0; j0 < nk; j0 += 32) {
       // lane q holds kill j0 + q: its slot, then the slot it is cloned from
@@ -716,30 +725,23 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
       int mym = 0;
       for (int q = 0; q < cnt; ++q) {
         const long long to = GBDMC_BC(__shfl_sync(full, myto, q), 0, n, kBcContSlot);
-        double bv = -CUDART_INF;
+        long long bk = -1;
         int bi = -1;
         for (int c = lane; c < nch; c += 32) {
-          const double x = s_cv[c];
+          const long long x = s_cv[c];
           const int xi = s_ci[c];
-          if (bi < 0 || x > bv || (x == bv && xi < bi)) {
-            bv = x;
+          if (bi < 0 || x > bk || (x == bk && xi < bi)) {
+            bk = x;
             bi = xi;
           }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const double ov = __shfl_xor_sync(full, bv, o);
-          const int oi = __shfl_xor_sync(full, bi, o);
-          if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
-            bv = ov;
-            bi = oi;
-          }
-        }
+        warp_best(bk, bi);
         const long long m = GBDMC_BC(bi, 0, n, kBcContSlot);
         // a slot still waiting to be killed can be the largest only when every
         // weight is below the threshold: then the copies keep the kill order
-        if (bv < S.thresh_lower) patho = 1;
-        const double h = bv * 0.5;  // bv == w[m]; halving is exact
+        if (bk < thr_key) patho = 1;
+        const double h = __longlong_as_double(bk) * 0.5;  // w[m] halved (exact)
+        const long long hk = __double_as_longlong(h);
         if (lane == q) mym = (int)m;
         if (lane == 0) {
           w[m] = h;
@@ -747,11 +749,11 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
         }
         __syncwarp();
         const int cm = (int)m >> lk, ct = (int)to >> lk;
-        double v1;
+        long long k1;
         int i1;
-        chunk_max(cm, v1, i1);  // m's chunk lost its largest weight: scanned again
+        chunk_max(cm, k1, i1);  // m's chunk lost its largest weight: scanned again
         if (lane == 0) {
-          s_cv[cm] = v1;
+          s_cv[cm] = k1;
           s_ci[cm] = i1;
         }
         if (ct != cm) {
@@ -759,16 +761,16 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
           // at to -- unless the old largest was to itself, whose weight may
           // have fallen (h can be below it when every weight is small): then
           // the chunk is scanned again
-          const double cv = s_cv[ct];
+          const long long ck = s_cv[ct];
           const int ci = s_ci[ct];
           if (ci == (int)to) {
-            chunk_max(ct, v1, i1);
+            chunk_max(ct, k1, i1);
             if (lane == 0) {
-              s_cv[ct] = v1;
+              s_cv[ct] = k1;
               s_ci[ct] = i1;
             }
-          } else if (lane == 0 && (h > cv || (h == cv && (int)to < ci))) {
-            s_cv[ct] = h;
+          } else if (lane == 0 && (hk > ck || (hk == ck && (int)to < ci))) {
+            s_cv[ct] = hk;
             s_ci[ct] = (int)to;
           }
         }
@@ -836,13 +838,15 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   int* list = list_all + base;
   unsigned char* flags = flags_all + base;
   __shared__ long long s_nb;
-  int bad = 0;
+  int bad = 0, neg = 0;
   for (long long i = threadIdx.x; i < n; i += kCTA) {
     const double wi = w[i] * exp(__dmul_rn(-__dsub_rn(v[i], vref), dt));
     w[i] = wi;
     if (!isfinite(wi)) bad = 1;
+    if (signbit(wi)) neg = 1;
     flags[i] = (wi < S.thresh_lower) ? 1 : 0;
   }
+  const bool any_neg = __syncthreads_or(neg);
   if (__syncthreads_or(bad)) {
     if (threadIdx.x == 0) {
       ctrl->status |= GBDMC_ST_NONFINITE_WEIGHT;
@@ -852,7 +856,7 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   }
   const long long nk = block_compact_flags(flags, n, list);
   long long nb = nk;
-  if (nk > 0 && nk < n) {
+  if (nk > 0 && nk < n && !any_neg && S.thresh_lower > 0.0) {
     fast_kills<A, IS>(S, W, base, w, n, list, nk, aux_all + base, flags, ws_dyn, ws_cap);
   } else {
   for (long long j = 0; j < nk; ++j) {
