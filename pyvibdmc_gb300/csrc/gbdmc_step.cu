@@ -673,31 +673,39 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
     __syncthreads();
   }
   // chunks of 2^lk weights (lk >= kChunkLogMin, at most kMaxChunks chunks): the
-  // chunk of a slot is a shift, and the indices are 32-bit (n < 2^31)
+  // chunk of a slot is a shift, and the indices are 32-bit (n < 2^31).  A kill
+  // reads about 2 ceil(chunks / 32) chunk maxima and ceil(2^lk / 32) weights
+  // per lane; lk minimises their sum (the result does not depend on lk).
   int lk = kChunkLogMin;
   while ((n + (1LL << lk) - 1) >> lk > kMaxChunks) ++lk;
+  {
+    auto cost = [&](int l) {
+      const long long ch = (n + (1LL << l) - 1) >> l;
+      return 2 * ((ch + 31) >> 5) + (((1LL << l) + 31) >> 5);
+    };
+    for (int l = lk + 1; l < 20 && cost(l) < cost(lk); ++l) lk = l;
+  }
   const int ni = (int)n;
   const int nch = (ni + (1 << lk) - 1) >> lk;
-  // (key, index) of the largest weight, the first index on ties, over a warp
+  // (key, index) of the largest weight, the first index on ties, over a warp:
+  // the keys are non-negative, so the high words, then the low words of the
+  // lanes that hold the largest high word, order them as unsigned integers
+  constexpr int kNone = 0x7fffffff;  // a lane without a weight: key 0, last index
   auto warp_best = [&](long long& bk, int& bi) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const long long ok = __shfl_xor_sync(full, bk, o);
-      const int oi = __shfl_xor_sync(full, bi, o);
-      if (oi >= 0 && (bi < 0 || ok > bk || (ok == bk && oi < bi))) {
-        bk = ok;
-        bi = oi;
-      }
-    }
+    const unsigned hi = (unsigned)((unsigned long long)bk >> 32), lo = (unsigned)bk;
+    const unsigned mh = __reduce_max_sync(full, hi);
+    const unsigned ml = __reduce_max_sync(full, hi == mh ? lo : 0u);
+    bi = (int)__reduce_min_sync(full, (hi == mh && lo == ml) ? (unsigned)bi : (unsigned)kNone);
+    bk = (long long)(((unsigned long long)mh << 32) | ml);
   };
   // per-chunk maxima of the current weights
   auto chunk_max = [&](int c, long long& bk, int& bi) {
-    bk = -1;
-    bi = -1;
+    bk = 0;
+    bi = kNone;
     const int e = ((c + 1) << lk) < ni ? ((c + 1) << lk) : ni;
     for (int i = (c << lk) + lane; i < e; i += 32) {
       const long long x = __double_as_longlong(w[i]);
-      if (bi < 0 || x > bk) {
+      if (bi == kNone || x > bk) {
         bk = x;
         bi = i;
       }
@@ -725,12 +733,13 @@ __device__ void fast_kills(const gbdmc_sim_t& S, gbdmc_walkers_t& W, int64_t bas
       int mym = 0;
       for (int q = 0; q < cnt; ++q) {
         const long long to = GBDMC_BC(__shfl_sync(full, myto, q), 0, n, kBcContSlot);
-        long long bk = -1;
-        int bi = -1;
+        long long bk = 0;
+        int bi = kNone;
+#pragma unroll 4
         for (int c = lane; c < nch; c += 32) {
           const long long x = s_cv[c];
           const int xi = s_ci[c];
-          if (bi < 0 || x > bk || (x == bk && xi < bi)) {
+          if (x > bk || (x == bk && xi < bi)) {
             bk = x;
             bi = xi;
           }
