@@ -467,6 +467,14 @@ int gbdmc_mlp_gemm_tn(const float* x_dev, const float* d_dev, int64_t m, int32_t
 int gbdmc_mlp_gemm_tc(const float* x_dev, int64_t m, int32_t k, const uint16_t* wt_dev, const float* bias_dev,
                       float* y_dev, void* stream);
 int gbdmc_mlp_gemm_tn_tc(const float* x_dev, const float* d_dev, int64_t m, int32_t k, float* g_dev, void* stream);
+/* Two GEMMs of one weight matrix in one launch (engine 0: mma.sync, 1: tcgen05): Y0 = X0 W + b0 and
+ * Y1 = X1 W + b1 (either bias may be NULL), e.g. a layer's primal and tangent streams; and
+ * G += X0^T D0 + X1^T D1.  Each equals the two single calls. */
+int gbdmc_mlp_gemm_pair(const float* x0_dev, const float* x1_dev, int64_t m, int32_t k, const uint16_t* wt_dev,
+                        const float* bias0_dev, const float* bias1_dev, float* y0_dev, float* y1_dev, int32_t engine,
+                        void* stream);
+int gbdmc_mlp_gemm_tn_pair(const float* x0_dev, const float* d0_dev, const float* x1_dev, const float* d1_dev,
+                           int64_t m, int32_t k, float* g_dev, int32_t engine, void* stream);
 /* 1 if a bounded tensor-core wait of the tcgen05 training GEMMs gave up since the last clear (synchronises),
  * 0 if not, -1 on a CUDA error; clear != 0 resets it. */
 int gbdmc_mlp_gemm_status(int32_t clear);

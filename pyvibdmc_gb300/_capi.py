@@ -153,6 +153,8 @@ def load():
         "gbdmc_mlp_gemm_status": ([C.c_int32], C.c_int),
         "gbdmc_mlp_gemm_tc": ([P, C.c_int64, C.c_int32, P, P, P, P], C.c_int),
         "gbdmc_mlp_gemm_tn_tc": ([P, P, C.c_int64, C.c_int32, P, P], C.c_int),
+        "gbdmc_mlp_gemm_pair": ([P, P, C.c_int64, C.c_int32, P, P, P, P, P, C.c_int32, P], C.c_int),
+        "gbdmc_mlp_gemm_tn_pair": ([P, P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
         "gbdmc_mlp_train_inputs": ([P, P, P, C.c_int64, C.c_int64, P, C.c_uint64, P, P, C.c_float, C.c_float, P,
                                     C.c_int32, P, P, P, P, P], C.c_int),
         "gbdmc_mlp_adam_all": ([P, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int64,

@@ -192,8 +192,10 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
                               const gbdmc_walkers_f32_t& in, const gbdmc_walkers_f32_t& out, gbdmc_ctrl_t* ctrl,
                               int* list, unsigned char* flags, const double* audit, const gbdmc_noise_t& nz,
                               cudaStream_t s);
-int launch_tc_gemm_xw(const float* x, long long m, int k, const uint16_t* wt, const float* bias, float* y, int* err,
-                      cudaStream_t s);
-int launch_tc_gemm_tn(const float* x, const float* d, long long m, int k, float* g, int* err, cudaStream_t s);
+// the tcgen05 training GEMMs over npair (1 or 2) operand sets: set 1 is (x1, b1, y1) / (x1, d1)
+int launch_tc_gemm_xw(const float* x0, const float* x1, long long m, int k, const uint16_t* wt, const float* b0,
+                      const float* b1, float* y0, float* y1, int npair, int* err, cudaStream_t s);
+int launch_tc_gemm_tn(const float* x0, const float* d0, const float* x1, const float* d1, long long m, int k,
+                      float* g, int npair, int* err, cudaStream_t s);
 
 }  // namespace gbdmc

@@ -56,10 +56,16 @@ __device__ __forceinline__ void mma_row16(float (&acc)[16][4], const uint32_t (&
 
 // --------------------------------------------------------- training GEMMs
 // Y[M x 128] = X[M x K] W[K x 128] (+ bias); X fp32 row-major, Wt bf16 [128][K].
+// blockIdx.y selects one of two operand sets that share W (a pair of GEMMs,
+// e.g. the primal and tangent streams of a layer, in one launch).
 template <int K>
-__global__ void __launch_bounds__(256) k_gemm_xw(const float* __restrict__ X, long long M,
-                                                  const uint16_t* __restrict__ Wt, const float* __restrict__ bias,
-                                                  float* __restrict__ Y) {
+__global__ void __launch_bounds__(256) k_gemm_xw(const float* __restrict__ X0, const float* __restrict__ X1,
+                                                  long long M, const uint16_t* __restrict__ Wt,
+                                                  const float* __restrict__ bias0, const float* __restrict__ bias1,
+                                                  float* __restrict__ Y0, float* __restrict__ Y1) {
+  const float* __restrict__ X = blockIdx.y ? X1 : X0;
+  const float* __restrict__ bias = blockIdx.y ? bias1 : bias0;
+  float* __restrict__ Y = blockIdx.y ? Y1 : Y0;
   constexpr int P = K == kH ? kPadH : kPadI;
   __shared__ __align__(16) uint16_t Ws[kH * P];
   load_wt(Ws, Wt, K, P);
@@ -98,9 +104,13 @@ __global__ void __launch_bounds__(256) k_gemm_xw(const float* __restrict__ X, lo
 
 // G[K x 128] += X[M x K]^T D[M x 128]: chunks of 64 rows staged transposed in
 // smem (bf16), reduced over M in registers, then one fp32 atomicAdd per element.
+// blockIdx.y selects one of two (X, D) pairs accumulated into the same G.
 template <int K>
-__global__ void __launch_bounds__(256) k_gemm_tn(const float* __restrict__ X, const float* __restrict__ D,
+__global__ void __launch_bounds__(256) k_gemm_tn(const float* __restrict__ X0, const float* __restrict__ D0,
+                                                  const float* __restrict__ X1, const float* __restrict__ D1,
                                                   long long M, float* __restrict__ G) {
+  const float* __restrict__ X = blockIdx.y ? X1 : X0;
+  const float* __restrict__ D = blockIdx.y ? D1 : D0;
   constexpr int CH = 64, PC = CH + 8;
   __shared__ __align__(16) uint16_t Xt[K * PC];
   __shared__ __align__(16) uint16_t Dt[kH * PC];
@@ -1020,6 +1030,33 @@ static int* tc_gemm_err_ptr() {
   return ptr[dev];
 }
 
+namespace {
+// The mma.sync training GEMMs over npair (1 or 2) operand sets.
+int launch_gemm_xw(const float* x0, const float* x1, long long m, int k, const uint16_t* wt, const float* b0,
+                   const float* b1, float* y0, float* y1, int npair, cudaStream_t s) {
+  long long g = (m + 127) / 128;
+  if (g > 4LL * num_sms()) g = 4LL * num_sms();
+  const dim3 grid((unsigned)g, (unsigned)npair);
+  if (k == 16)
+    k_gemm_xw<16><<<grid, 256, 0, s>>>(x0, x1, m, wt, b0, b1, y0, y1);
+  else
+    k_gemm_xw<128><<<grid, 256, 0, s>>>(x0, x1, m, wt, b0, b1, y0, y1);
+  return check_launch("gbdmc_mlp_gemm");
+}
+
+int launch_gemm_tn(const float* x0, const float* d0, const float* x1, const float* d1, long long m, int k, float* g,
+                   int npair, cudaStream_t s) {
+  long long grid = (m + 63) / 64;
+  if (grid > 2LL * num_sms()) grid = 2LL * num_sms();
+  const dim3 gr((unsigned)grid, (unsigned)npair);
+  if (k == 16)
+    k_gemm_tn<16><<<gr, 256, 0, s>>>(x0, d0, x1, d1, m, g);
+  else
+    k_gemm_tn<128><<<gr, 256, 0, s>>>(x0, d0, x1, d1, m, g);
+  return check_launch("gbdmc_mlp_gemm_tn");
+}
+}  // namespace
+
 extern "C" int gbdmc_mlp_gemm(const float* x, int64_t m, int32_t k, const uint16_t* wt, const float* bias, float* y,
                               void* stream) {
   if (!x || !wt || !y || m < 0 || (k != 16 && k != 128)) {
@@ -1027,14 +1064,7 @@ extern "C" int gbdmc_mlp_gemm(const float* x, int64_t m, int32_t k, const uint16
     return GBDMC_ERR_ARG;
   }
   if (m == 0) return GBDMC_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  long long g = (m + 127) / 128;
-  if (g > 4LL * num_sms()) g = 4LL * num_sms();
-  if (k == 16)
-    k_gemm_xw<16><<<(int)g, 256, 0, s>>>(x, m, wt, bias, y);
-  else
-    k_gemm_xw<128><<<(int)g, 256, 0, s>>>(x, m, wt, bias, y);
-  return check_launch("gbdmc_mlp_gemm");
+  return launch_gemm_xw(x, x, m, k, wt, bias, bias, y, y, 1, (cudaStream_t)stream);
 }
 
 extern "C" int gbdmc_mlp_gemm_tn(const float* x, const float* d, int64_t m, int32_t k, float* g, void* stream) {
@@ -1043,14 +1073,7 @@ extern "C" int gbdmc_mlp_gemm_tn(const float* x, const float* d, int64_t m, int3
     return GBDMC_ERR_ARG;
   }
   if (m == 0) return GBDMC_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  long long grid = (m + 63) / 64;
-  if (grid > 2LL * num_sms()) grid = 2LL * num_sms();
-  if (k == 16)
-    k_gemm_tn<16><<<(int)grid, 256, 0, s>>>(x, d, m, g);
-  else
-    k_gemm_tn<128><<<(int)grid, 256, 0, s>>>(x, d, m, g);
-  return check_launch("gbdmc_mlp_gemm_tn");
+  return launch_gemm_tn(x, d, x, d, m, k, g, 1, (cudaStream_t)stream);
 }
 
 extern "C" int gbdmc_mlp_gemm_tc(const float* x, int64_t m, int32_t k, const uint16_t* wt, const float* bias, float* y,
@@ -1065,7 +1088,7 @@ extern "C" int gbdmc_mlp_gemm_tc(const float* x, int64_t m, int32_t k, const uin
     set_error("gbdmc_mlp_gemm_tc: no device status word");
     return GBDMC_ERR_CUDA;
   }
-  return launch_tc_gemm_xw(x, m, k, wt, bias, y, err, (cudaStream_t)stream);
+  return launch_tc_gemm_xw(x, x, m, k, wt, bias, bias, y, y, 1, err, (cudaStream_t)stream);
 }
 
 extern "C" int gbdmc_mlp_gemm_tn_tc(const float* x, const float* d, int64_t m, int32_t k, float* g, void* stream) {
@@ -1079,7 +1102,40 @@ extern "C" int gbdmc_mlp_gemm_tn_tc(const float* x, const float* d, int64_t m, i
     set_error("gbdmc_mlp_gemm_tn_tc: no device status word");
     return GBDMC_ERR_CUDA;
   }
-  return launch_tc_gemm_tn(x, d, m, k, g, err, (cudaStream_t)stream);
+  return launch_tc_gemm_tn(x, d, x, d, m, k, g, 1, err, (cudaStream_t)stream);
+}
+
+extern "C" int gbdmc_mlp_gemm_pair(const float* x0, const float* x1, int64_t m, int32_t k, const uint16_t* wt,
+                                   const float* bias0, const float* bias1, float* y0, float* y1, int32_t engine,
+                                   void* stream) {
+  if (!x0 || !x1 || !wt || !y0 || !y1 || m < 0 || (k != 16 && k != 128) || (engine != 0 && engine != 1)) {
+    set_error("gbdmc_mlp_gemm_pair: invalid arguments (k must be 16 or 128, engine 0 or 1)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  if (engine == 0) return launch_gemm_xw(x0, x1, m, k, wt, bias0, bias1, y0, y1, 2, (cudaStream_t)stream);
+  int* err = tc_gemm_err_ptr();
+  if (!err) {
+    set_error("gbdmc_mlp_gemm_pair: no device status word");
+    return GBDMC_ERR_CUDA;
+  }
+  return launch_tc_gemm_xw(x0, x1, m, k, wt, bias0, bias1, y0, y1, 2, err, (cudaStream_t)stream);
+}
+
+extern "C" int gbdmc_mlp_gemm_tn_pair(const float* x0, const float* d0, const float* x1, const float* d1, int64_t m,
+                                      int32_t k, float* g, int32_t engine, void* stream) {
+  if (!x0 || !d0 || !x1 || !d1 || !g || m < 0 || (k != 16 && k != 128) || (engine != 0 && engine != 1)) {
+    set_error("gbdmc_mlp_gemm_tn_pair: invalid arguments (k must be 16 or 128, engine 0 or 1)");
+    return GBDMC_ERR_ARG;
+  }
+  if (m == 0) return GBDMC_OK;
+  if (engine == 0) return launch_gemm_tn(x0, d0, x1, d1, m, k, g, 2, (cudaStream_t)stream);
+  int* err = tc_gemm_err_ptr();
+  if (!err) {
+    set_error("gbdmc_mlp_gemm_tn_pair: no device status word");
+    return GBDMC_ERR_CUDA;
+  }
+  return launch_tc_gemm_tn(x0, d0, x1, d1, m, k, g, 2, err, (cudaStream_t)stream);
 }
 
 extern "C" int gbdmc_mlp_gemm_status(int32_t clear) {

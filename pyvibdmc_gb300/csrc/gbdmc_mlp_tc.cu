@@ -523,11 +523,16 @@ __device__ __forceinline__ void umma_n64(uint32_t d_tmem, uint64_t adesc, uint64
       : "memory");
 }
 
+// blockIdx.z selects one of two operand sets that share W.
 template <int K>
-__global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict__ X, long long M,
-                                                         const uint16_t* __restrict__ Wt,
-                                                         const float* __restrict__ bias, float* __restrict__ Y,
-                                                         int* __restrict__ err) {
+__global__ void __launch_bounds__(kThreads) k_tc_gemm_xw(const float* __restrict__ X0, const float* __restrict__ X1,
+                                                         long long M, const uint16_t* __restrict__ Wt,
+                                                         const float* __restrict__ bias0,
+                                                         const float* __restrict__ bias1, float* __restrict__ Y0,
+                                                         float* __restrict__ Y1, int* __restrict__ err) {
+  const float* __restrict__ X = blockIdx.z ? X1 : X0;
+  const float* __restrict__ bias = blockIdx.z ? bias1 : bias0;
+  float* __restrict__ Y = blockIdx.z ? Y1 : Y0;
   constexpr int KG = K / 8;
   extern __shared__ __align__(1024) unsigned char smraw[];
   XwSmem<K>& sm = *reinterpret_cast<XwSmem<K>*>(smraw);
@@ -626,10 +631,14 @@ __device__ __forceinline__ uint4 column8_bf16(const float* __restrict__ P, long 
   return make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
 }
 
+// blockIdx.y selects one of two (X, D) pairs accumulated into the same G.
 template <int K>
-__global__ void __launch_bounds__(kThreads) k_tc_gemm_tn(const float* __restrict__ X, const float* __restrict__ D,
+__global__ void __launch_bounds__(kThreads) k_tc_gemm_tn(const float* __restrict__ X0, const float* __restrict__ D0,
+                                                         const float* __restrict__ X1, const float* __restrict__ D1,
                                                          long long M, long long rows_per_cta, float* __restrict__ G,
                                                          int* __restrict__ err) {
+  const float* __restrict__ X = blockIdx.y ? X1 : X0;
+  const float* __restrict__ D = blockIdx.y ? D1 : D0;
   constexpr int KG = kRows / 8;  // 16 core columns: 128 rows of X and D per chunk
   extern __shared__ __align__(1024) unsigned char smraw[];
   TnSmem& sm = *reinterpret_cast<TnSmem*>(smraw);
@@ -735,8 +744,8 @@ int launch_mlp_tc_move_energy(const gbdmc_sim_t& S, const RepTable& T, const gbd
 
 // The training GEMMs on tcgen05 (err: a device int set to 1 if a bounded
 // tensor-core wait gave up; the caller's buffer).
-int launch_tc_gemm_xw(const float* x, long long m, int k, const uint16_t* wt, const float* bias, float* y, int* err,
-                      cudaStream_t s) {
+int launch_tc_gemm_xw(const float* x0, const float* x1, long long m, int k, const uint16_t* wt, const float* b0,
+                      const float* b1, float* y0, float* y1, int npair, int* err, cudaStream_t s) {
   // at least 70 KB of shared memory, so that at most three CTAs share an SM and
   // their 3 x 128 TMEM columns always fit (an allocation never waits)
   int smem = (int)(k == 16 ? sizeof(tc::XwSmem<16>) : sizeof(tc::XwSmem<128>)) + 1024;
@@ -749,15 +758,17 @@ int launch_tc_gemm_xw(const float* x, long long m, int k, const uint16_t* wt, co
   }
   long long g = (m + tc::kRows - 1) / tc::kRows;
   if (g > 3LL * num_sms() / 2) g = 3LL * num_sms() / 2;
-  const dim3 grid((unsigned)g, tc::kN / tc::kXwN);  // two CTAs per 128-row tile, 64 output columns each
+  // two CTAs per 128-row tile, 64 output columns each, per operand set
+  const dim3 grid((unsigned)g, tc::kN / tc::kXwN, (unsigned)npair);
   if (k == 16)
-    tc::k_tc_gemm_xw<16><<<grid, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+    tc::k_tc_gemm_xw<16><<<grid, tc::kThreads, smem, s>>>(x0, x1, m, wt, b0, b1, y0, y1, err);
   else
-    tc::k_tc_gemm_xw<128><<<grid, tc::kThreads, smem, s>>>(x, m, wt, bias, y, err);
+    tc::k_tc_gemm_xw<128><<<grid, tc::kThreads, smem, s>>>(x0, x1, m, wt, b0, b1, y0, y1, err);
   return check_launch("gbdmc_mlp_gemm (tcgen05)");
 }
 
-int launch_tc_gemm_tn(const float* x, const float* d, long long m, int k, float* g, int* err, cudaStream_t s) {
+int launch_tc_gemm_tn(const float* x0, const float* d0, const float* x1, const float* d1, long long m, int k,
+                      float* g, int npair, int* err, cudaStream_t s) {
   int smem = (int)sizeof(tc::TnSmem) + 1024;
   if (smem < 70 * 1024) smem = 70 * 1024;  // at most three CTAs (3 x 128 TMEM columns) per SM
   const void* f = k == 16 ? (const void*)tc::k_tc_gemm_tn<16> : (const void*)tc::k_tc_gemm_tn<128>;
@@ -766,15 +777,17 @@ int launch_tc_gemm_tn(const float* x, const float* d, long long m, int k, float*
     set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
     return GBDMC_ERR_CUDA;
   }
-  // one 128-row chunk per CTA while the chunks fit three CTAs per SM
+  // one 128-row chunk per CTA while the chunks of all operand sets fit three CTAs per SM
   const long long chunks = (m + tc::kRows - 1) / tc::kRows;
+  const long long slots = 3LL * num_sms() / npair;
   long long per = 1;
-  if ((chunks + per - 1) / per > 3LL * num_sms()) per = (chunks + 3LL * num_sms() - 1) / (3LL * num_sms());
+  if (chunks > slots) per = (chunks + slots - 1) / slots;
   const long long grid = (chunks + per - 1) / per;
+  const dim3 gr((unsigned)grid, (unsigned)npair);
   if (k == 16)
-    tc::k_tc_gemm_tn<16><<<(int)grid, tc::kThreads, smem, s>>>(x, d, m, per * tc::kRows, g, err);
+    tc::k_tc_gemm_tn<16><<<gr, tc::kThreads, smem, s>>>(x0, d0, x1, d1, m, per * tc::kRows, g, err);
   else
-    tc::k_tc_gemm_tn<128><<<(int)grid, tc::kThreads, smem, s>>>(x, d, m, per * tc::kRows, g, err);
+    tc::k_tc_gemm_tn<128><<<gr, tc::kThreads, smem, s>>>(x0, d0, x1, d1, m, per * tc::kRows, g, err);
   return check_launch("gbdmc_mlp_gemm_tn (tcgen05)");
 }
 

@@ -191,18 +191,24 @@ class MLPSurrogate:
         b, P, bf, Gr = self.buf, self.P, self.bf, self.grads
         s = _s()
         ck = _capi.check
-        gemm = L.gbdmc_mlp_gemm_tc if self.train_engine == "tcgen05" else L.gbdmc_mlp_gemm
-        gemm_tn = L.gbdmc_mlp_gemm_tn if self.train_engine == "mma_sync" else L.gbdmc_mlp_gemm_tn_tc
+        # engines (0 mma.sync, 1 tcgen05) of Y = XW and G += X^T D; each launch
+        # runs the primal and tangent streams of a layer together
+        exw = 1 if self.train_engine == "tcgen05" else 0
+        etn = 0 if self.train_engine == "mma_sync" else 1
+
+        def gemm2(x0, x1, m, k, wt, b0, y0, y1):
+            ck(L.gbdmc_mlp_gemm_pair(_p(x0), _p(x1), m, k, _p(wt), b0, None, _p(y0), _p(y1), exw, s), "gemm_pair")
+
+        def gemm_tn2(x0, d0, x1, d1, m, k, g):
+            ck(L.gbdmc_mlp_gemm_tn_pair(_p(x0), _p(d0), _p(x1), _p(d1), m, k, _p(g), etn, s), "gemm_tn_pair")
         ck(L.gbdmc_mlp_train_inputs(_p(X), _p(V), _p(G), ld, B, _p(self._ctl), int(seed) & 0xFFFFFFFFFFFFFFFF,
                                     _p(self.mu), _p(self.inv_sd), float(self.e_mean), float(self.e_scale), _p(P["b4"]),
                                     int(self.sort_atoms), _p(b["feat"]), _p(b["tang"]), _p(b["et"]), _p(b["e"]), s),
            "train_inputs")
-        ck(gemm(_p(b["feat"]), B, 16, _p(bf["W1t"]), _p(P["b1"]), _p(b["Z1"]), s), "gemm")
-        ck(gemm(_p(b["tang"]), B, 16, _p(bf["W1t"]), None, _p(b["Zt1"]), s), "gemm")
+        gemm2(b["feat"], b["tang"], B, 16, bf["W1t"], _p(P["b1"]), b["Z1"], b["Zt1"])
         ck(L.gbdmc_mlp_silu_fwd(_p(b["Z1"]), _p(b["Zt1"]), _p(b["H1"]), _p(b["Ht1"]), B * H, s), "silu")
         for l, (wt, bias) in ((2, ("W2t", "b2")), (3, ("W3t", "b3"))):
-            ck(gemm(_p(b[f"H{l-1}"]), B, H, _p(bf[wt]), _p(P[bias]), _p(b[f"Z{l}"]), s), "gemm")
-            ck(gemm(_p(b[f"Ht{l-1}"]), B, H, _p(bf[wt]), None, _p(b[f"Zt{l}"]), s), "gemm")
+            gemm2(b[f"H{l-1}"], b[f"Ht{l-1}"], B, H, bf[wt], _p(P[bias]), b[f"Z{l}"], b[f"Zt{l}"])
             ck(L.gbdmc_mlp_silu_fwd(_p(b[f"Z{l}"]), _p(b[f"Zt{l}"]), _p(b[f"H{l}"]), _p(b[f"Ht{l}"]), B * H, s),
                "silu")
         # the targets e already carry -b4, so the head adds no b4 (b4's gradient is still accumulated)
@@ -214,12 +220,9 @@ class MLPSurrogate:
                                     _p(b[f"Zb{l}"]), _p(b[f"Ztb{l}"]), B * H, _p(Gr[f"b{l}"]), s), "silu_bwd")
             K = H if l > 1 else 16
             xin, xtin = (b[f"H{l-1}"], b[f"Ht{l-1}"]) if l > 1 else (b["feat"], b["tang"])
-            ck(gemm_tn(_p(xin), _p(b[f"Zb{l}"]), B, K, _p(Gr[f"W{l}"]), s), "gemm_tn")
-            ck(gemm_tn(_p(xtin), _p(b[f"Ztb{l}"]), B, K, _p(Gr[f"W{l}"]), s), "gemm_tn")
+            gemm_tn2(xin, b[f"Zb{l}"], xtin, b[f"Ztb{l}"], B, K, Gr[f"W{l}"])
             if l > 1:
-                wn = bf[f"W{l}n"]
-                ck(gemm(_p(b[f"Zb{l}"]), B, H, _p(wn), None, _p(b[f"Hb{l-1}"]), s), "gemm")
-                ck(gemm(_p(b[f"Ztb{l}"]), B, H, _p(wn), None, _p(b[f"Htb{l-1}"]), s), "gemm")
+                gemm2(b[f"Zb{l}"], b[f"Ztb{l}"], B, H, bf[f"W{l}n"], None, b[f"Hb{l-1}"], b[f"Htb{l-1}"])
 
     def _adam(self, lr0, lr_min, t0, steps):
         """One Adam launch over all parameters (gradients cleared, ctl advanced)."""

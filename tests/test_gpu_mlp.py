@@ -56,6 +56,33 @@ def test_gemm_tn_matches_torch(K, M, engine):
     assert L.gbdmc_mlp_gemm_status(1) == 0
 
 
+@pytest.mark.parametrize("engine", [0, 1])
+@pytest.mark.parametrize("K", [16, 128])
+@pytest.mark.parametrize("M", [37, 8192])
+def test_gemm_pairs_match_single_calls(K, M, engine):
+    """gbdmc_mlp_gemm_pair gives each operand set's single-call result bit for
+    bit (one bias or none); gbdmc_mlp_gemm_tn_pair accumulates both sets."""
+    L = _capi.load()
+    gemm = L.gbdmc_mlp_gemm if engine == 0 else L.gbdmc_mlp_gemm_tc
+    g = torch.Generator(device="cuda").manual_seed(3 * K + M + engine)
+    X0, X1 = (torch.randn(M, K, device="cuda", generator=g) for _ in range(2))
+    D0, D1 = (torch.randn(M, 128, device="cuda", generator=g) for _ in range(2))
+    W = torch.randn(K, 128, device="cuda", generator=g) / np.sqrt(K)
+    b = torch.randn(128, device="cuda", generator=g)
+    Wt = W.t().contiguous().to(torch.bfloat16).view(torch.int16)
+    Y0, Y1, R0, R1 = (torch.empty(M, 128, device="cuda") for _ in range(4))
+    _capi.check(L.gbdmc_mlp_gemm_pair(_p(X0), _p(X1), M, K, _p(Wt), _p(b), None, _p(Y0), _p(Y1), engine, _s()))
+    _capi.check(gemm(_p(X0), M, K, _p(Wt), _p(b), _p(R0), _s()))
+    _capi.check(gemm(_p(X1), M, K, _p(Wt), None, _p(R1), _s()))
+    assert torch.equal(Y0, R0) and torch.equal(Y1, R1)
+    G = torch.ones(K, 128, device="cuda")
+    _capi.check(L.gbdmc_mlp_gemm_tn_pair(_p(X0), _p(D0), _p(X1), _p(D1), M, K, _p(G), engine, _s()))
+    ref = 1.0 + bf(X0).t() @ bf(D0) + bf(X1).t() @ bf(D1)
+    torch.testing.assert_close(G, ref, rtol=1e-4, atol=2e-3)
+    assert L.gbdmc_mlp_gemm_status(1) == 0
+    assert L.gbdmc_mlp_gemm_pair(_p(X0), _p(X1), M, K, _p(Wt), None, None, _p(Y0), _p(Y1), 2, _s()) == _capi.ERR_ARG
+
+
 def _group_copies(x):
     """Each geometry under one of the eight permutations of like atoms (the
     hydrogens of either water, the two waters), cycling through them."""
