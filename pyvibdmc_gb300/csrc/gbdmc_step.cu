@@ -179,7 +179,11 @@ __global__ void __launch_bounds__(kMaxTPB) k_move(const __grid_constant__ gbdmc_
         p.c = c;
         p.s0 = c == 1 ? v : (double)c * v;
       } else if (S.weighting == GBDMC_CONTINUOUS) {
-        out.w[dst] = in.w[src];
+        // this step's weight update (pyvibdmc.py:433, :837) on every SM, with the
+        // vref that k_cont_branch reads (it writes the next one): the exp of
+        // each walker is FP64 work that the one-CTA branching kernel would
+        // otherwise do on a single SM
+        out.w[dst] = in.w[src] * exp(__dmul_rn(-__dsub_rn(v, vref), S.dt));
       }
     }
     if (COUNT) flag_weights(ctrl, flag);
@@ -832,7 +836,7 @@ template <int A, bool IS>
 __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gbdmc_sim_t S,
                                                        const __grid_constant__ RepTable T, gbdmc_walkers_t W,
                                                        gbdmc_ctrl_t* ctrls, int* list_all, int* aux_all,
-                                                       unsigned char* flags_all, int ws_cap) {
+                                                       unsigned char* flags_all, int ws_cap, int weighted) {
   extern __shared__ double ws_dyn[];  // ws_cap doubles: the weights during the kills
   const int r = blockIdx.x;
   gbdmc_ctrl_t* ctrl = ctrls + r;
@@ -849,8 +853,12 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   __shared__ long long s_nb;
   int bad = 0, neg = 0;
   for (long long i = threadIdx.x; i < n; i += kCTA) {
-    const double wi = w[i] * exp(__dmul_rn(-__dsub_rn(v[i], vref), dt));
-    w[i] = wi;
+    // weighted: the move kernel has applied this step's factor already
+    double wi = w[i];
+    if (!weighted) {
+      wi *= exp(__dmul_rn(-__dsub_rn(v[i], vref), dt));
+      w[i] = wi;
+    }
     if (!isfinite(wi)) bad = 1;
     if (signbit(wi)) neg = 1;
     flags[i] = (wi < S.thresh_lower) ? 1 : 0;
@@ -966,15 +974,17 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
 // One CTA per replica; the weights of replicas of up to kWsMax walkers sit in
 // shared memory while their kills run.
 constexpr int kWsMax = 24000;
+// weighted: the move kernel has multiplied this step's factor into the weights.
 template <int A, bool IS>
 static void launch_cont_branch(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_walkers_t& dst,
-                               gbdmc_ctrl_t* ctrl, int* list, int* aux, unsigned char* flags, cudaStream_t s) {
+                               gbdmc_ctrl_t* ctrl, int* list, int* aux, unsigned char* flags, bool weighted,
+                               cudaStream_t s) {
   long long cap = 0;
   for (int r = 0; r < T.nrep; ++r) cap = T.cap[r] > cap ? T.cap[r] : cap;
   const int ws_cap = (int)(cap < kWsMax ? cap : kWsMax);
   const size_t smem = (size_t)ws_cap * sizeof(double);
   cudaFuncSetAttribute((const void*)k_cont_branch<A, IS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_cont_branch<A, IS><<<T.nrep, kCTA, smem, s>>>(S, T, dst, ctrl, list, aux, flags, ws_cap);
+  k_cont_branch<A, IS><<<T.nrep, kCTA, smem, s>>>(S, T, dst, ctrl, list, aux, flags, ws_cap, weighted ? 1 : 0);
 }
 
 // np.argpartition of one weight array by one CTA (gbdmc_argpartition).
@@ -1125,7 +1135,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
     } else {
       k_move<PK, A, NM, false, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, L.prefix, L.counts, nz);
       if (prof) cudaEventRecord(ev[1], s);
-      launch_cont_branch<A, false>(S, T, dst, ctrl, L.list, L.counts, L.flags, s);
+      launch_cont_branch<A, false>(S, T, dst, ctrl, L.list, L.counts, L.flags, true, s);
     }
   } else {
     k_is_move<PK, A, TK, NM, STATS><<<G, T.tpb, 0, s>>>(S, T, src, dst, ctrl, L.part, nz);
@@ -1135,7 +1145,7 @@ static void launch_step(const gbdmc_sim_t& S, const RepTable& T, const gbdmc_wal
       k_count_finalize<<<T.nrep, kMaxTPB, 0, s>>>(S, T, ctrl, L.part, L.prefix);
       launch_branch_to<A, true>(T, S, dst, ctrl, L, bt, s);
     } else {
-      launch_cont_branch<A, true>(S, T, dst, ctrl, L.list, L.counts, L.flags, s);
+      launch_cont_branch<A, true>(S, T, dst, ctrl, L.list, L.counts, L.flags, false, s);
     }
   }
   if (prof) {
@@ -1462,7 +1472,7 @@ extern "C" int gbdmc_sim_branch(const gbdmc_sim_t* S, const gbdmc_walkers_t* dst
   const ScratchLayout L = scratch_layout(scratch, S->ld, max_tiles_for(&r, 1));
   cudaStream_t s = (cudaStream_t)stream;
   if (S->weighting == GBDMC_CONTINUOUS) {
-    launch_cont_branch<0, false>(*S, T, *dst, ctrl, L.list, L.counts, L.flags, s);
+    launch_cont_branch<0, false>(*S, T, *dst, ctrl, L.list, L.counts, L.flags, false, s);
     return check_launch(what);
   }
   const int G = grid_for(T);
