@@ -852,6 +852,12 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
   unsigned char* flags = flags_all + base;
   __shared__ long long s_nb;
   int bad = 0, neg = 0;
+  // the tests on the weight's bits (integer pipes): with a positive threshold,
+  // wi < thresh_lower holds exactly when the signed 64-bit patterns compare so
+  // for every finite wi (a negative wi has a negative pattern)
+  const long long thr_key = __double_as_longlong(S.thresh_lower);
+  const bool key_cmp = S.thresh_lower > 0.0;
+  constexpr long long kExpMask = 0x7FF0000000000000LL;
   for (long long i = threadIdx.x; i < n; i += kCTA) {
     // weighted: the move kernel has applied this step's factor already
     double wi = w[i];
@@ -859,9 +865,10 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
       wi *= exp(__dmul_rn(-__dsub_rn(v[i], vref), dt));
       w[i] = wi;
     }
-    if (!isfinite(wi)) bad = 1;
-    if (signbit(wi)) neg = 1;
-    flags[i] = (wi < S.thresh_lower) ? 1 : 0;
+    const long long k = __double_as_longlong(wi);
+    if ((k & kExpMask) == kExpMask) bad = 1;  // inf or NaN
+    if (k < 0) neg = 1;                         // the sign bit
+    flags[i] = (key_cmp ? k < thr_key : wi < S.thresh_lower) ? 1 : 0;
   }
   const bool any_neg = __syncthreads_or(neg);
   if (__syncthreads_or(bad)) {
@@ -928,12 +935,28 @@ __global__ void __launch_bounds__(kCTA) k_cont_branch(const __grid_constant__ gb
     nb += nk2;
   }
   double swv = 0.0, sw = 0.0, wmx = -CUDART_INF, wmn = CUDART_INF;
-  for (long long i = threadIdx.x; i < n; i += kCTA) {
-    const double wi = w[i];
-    swv += v[i] * wi;
-    sw += wi;
-    wmx = fmax(wmx, wi);
-    wmn = fmin(wmn, wi);
+  if (!any_neg) {
+    // non-negative weights order like their bit patterns: the extremes on the
+    // integer pipes (the patterns of -inf and +inf start them)
+    long long kmx = __double_as_longlong(-CUDART_INF), kmn = __double_as_longlong(CUDART_INF);
+    for (long long i = threadIdx.x; i < n; i += kCTA) {
+      const double wi = w[i];
+      swv += v[i] * wi;
+      sw += wi;
+      const long long k = __double_as_longlong(wi);
+      kmx = k > kmx ? k : kmx;
+      kmn = k < kmn ? k : kmn;
+    }
+    wmx = __longlong_as_double(kmx);
+    wmn = __longlong_as_double(kmn);
+  } else {
+    for (long long i = threadIdx.x; i < n; i += kCTA) {
+      const double wi = w[i];
+      swv += v[i] * wi;
+      sw += wi;
+      wmx = fmax(wmx, wi);
+      wmn = fmin(wmn, wi);
+    }
   }
   __shared__ double r4[4][kCTA / 32];
   swv = warp_sum(swv);
