@@ -15,9 +15,12 @@ gbdmc_desc_weights).  ``value``: device-resident walker-steps/s, each window
 timed with CUDA events on the launching stream, a 256 MiB buffer written
 between windows so that every window starts with the walkers in HBM (L2
 flushed).  ``e2e``: the same metric through the C ABI with the walkers in
-page-locked host memory between calls: per window the walkers are copied
-host -> device, gbdmc_sim_run advances them, and the control block, the
-branched walkers and the window's history are copied back.  The per-step
+page-locked host memory between calls: per window one gbdmc_sim_run_host
+call, whose gbdmc_sim_run launch reads the walkers from the host arrays and
+whose second kernel writes the control block, the branched walkers and the
+window's history back into host memory, then one stream wait (three untimed
+warm-up windows first; the timed region is the host's wall clock around the
+calls).  The per-step
 kernels (gbdmc_sim_step, L2 flushed every step) are reported under config.
 ``--impl reference`` times the CPU restatement of the reference's step loop
 (oracle/) on the host cores.
