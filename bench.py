@@ -631,7 +631,7 @@ def run_extras(steps):
     return out
 
 
-DIMER_TAU = 60000.0  # imaginary time of every run of the spec comparison (a.u.)
+DIMER_TAU = 60000.0  # imaginary time of every run of the dimer efficiency comparison (a.u.)
 # dt and dt/2 of the extrapolation.  The walks' time-step errors are curved
 # (plain FP64 dimer, 64 seeds each: E(2.5) - E(5) = 1.72 and E(1.25) - E(2.5)
 # = 0.59 cm^-1), and a straight line keeps a bias of -12.5 b for the steps 5
@@ -641,7 +641,7 @@ DIMER_DTS = (2.5, 1.25)
 
 
 def zpe_estimate(vref_series_cm):
-    """The one error estimator of the spec comparison: the mean of the
+    """The one error estimator of the dimer efficiency comparison: the mean of the
     production part (the last 3/4) of a vref series and its blocking error
     (30 block means).  For a batch of replicas the series is the N0-weighted
     mean of the replicas' vref at each step."""
@@ -711,7 +711,7 @@ def run_batched_replicas(masses, T=10000, nsingle=16):
 
 
 def run_combined_dimer(m, pot, dm, trial, plain_seeds=(13, 14, 15, 16, 17, 18), prep_s=None):
-    """The spec comparison on the water dimer: the engine with its three
+    """The efficiency comparison on the water dimer: the engine with its three
     accelerations (importance sampling with the fitted dimer trial, the tcgen05
     surrogate PES, 64 batched replicas with N_r ~ U[1000, 65536]) against the
     plain FP64 GPU path (200000 walkers, one replica, several seeds), at equal
@@ -858,7 +858,7 @@ def oracle_extrapolation(runs):
 def dimer_oracle(dts, merge=None, plain_seeds=tuple(range(101, 165))):
     """A long plain FP64 extrapolation of the water dimer's ZPE (200000
     walkers, 64 seeds at each dt, 60000 a.u. of imaginary time per run): the
-    value profiles/dimer_fp64_oracle.json keeps for the north-star
+    value profiles/dimer_fp64_oracle.json keeps for the dimer efficiency
     comparison.  ``merge``: a JSON file of this function whose runs at other
     steps are kept."""
     import torch
