@@ -69,6 +69,24 @@ def test_error_reporting_without_gpu():
     assert L.gbdmc_pes_eval(ctypes.byref(pes), None, 2, 1, None, None, None) == _capi.ERR_ARG  # ld < n
 
 
+def test_gemm_pairs_refuse_bad_arguments_without_gpu():
+    """The pair GEMMs check their arguments before any CUDA call: a null
+    operand, K other than 16 or 128, an engine other than 0 or 1 and m < 0 are
+    refused, and m = 0 returns at once (the pointer is never dereferenced)."""
+    from pyvibdmc_gb300 import _capi
+    L = _capi.load()
+    p = ctypes.c_void_p(256)
+    xw = lambda x0, m, k, e: L.gbdmc_mlp_gemm_pair(x0, p, m, k, p, None, None, p, p, e, None)  # noqa: E731
+    tn = lambda x0, m, k, e: L.gbdmc_mlp_gemm_tn_pair(x0, p, p, p, m, k, p, e, None)  # noqa: E731
+    for f in (xw, tn):
+        assert f(None, 8, 16, 0) == _capi.ERR_ARG
+        assert f(p, 8, 5, 0) == _capi.ERR_ARG
+        assert f(p, 8, 16, 2) == _capi.ERR_ARG
+        assert f(p, -1, 128, 1) == _capi.ERR_ARG
+        assert f(p, 0, 128, 1) == _capi.OK
+    assert b"engine 0 or 1" in L.gbdmc_last_error()  # the last refusal's message
+
+
 def test_replica_table_is_checked_before_any_launch():
     """Bad replica tables are refused on the host (no pointer is touched)."""
     from pyvibdmc_gb300 import _capi
